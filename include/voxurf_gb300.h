@@ -145,6 +145,184 @@ int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, f
                          int channel_last, int tv_enabled, float tv_weight, int tv_dense_mode, double lr,
                          double beta1, double beta2, double eps, int64_t step, int zero_grad, void* stream);
 
+/* ---- Gaussian smoothing (Voxurf._gaussian_3dconv, lib/voxurf_fine.py:246-258,
+ *      used at voxurf_fine.py:638 / voxurf_coarse.py:531) ------------------- */
+
+/* out = G * in on an [X,Y,Z] grid with replicate padding; taps_host: the
+ * normalised 1-D kernel (ksize odd, <= 9; the 3-D kernel is its cube).
+ * tmp1/tmp2: two [X,Y,Z] scratch grids. */
+int vx_smooth3d(const float* in, float* out, float* tmp1, float* tmp2, int64_t X, int64_t Y, int64_t Z,
+                const float* taps_host, int ksize, void* stream);
+/* grad_in (+)= G^T grad_out (exact adjoint of the clamped convolution). */
+int vx_smooth3d_adjoint(const float* grad_out, float* grad_in, float* tmp1, float* tmp2, int64_t X, int64_t Y,
+                        int64_t Z, const float* taps_host, int ksize, int accumulate, void* stream);
+
+/* ---- fused fine-model rendering (Voxurf.forward, lib/voxurf_fine.py:620-802) */
+
+typedef struct {
+  int64_t X, Y, Z;     /* grid size (world_size)                   */
+  float xyz_min[3];    /* model xyz_min (host copy of the buffer)  */
+  float xyz_max[3];
+} vx_grid_geom;
+
+/* DenseGrid.forward (lib/grid.py:47-58): trilinear lookup with
+ * F.grid_sample(align_corners=True, padding zeros) semantics.  grid: C
+ * channels, channel-first ([C,X,Y,Z]) or channel-last ([X,Y,Z,C]);
+ * xyz [n,3] world coordinates; out [n,C]. */
+int vx_grid_sample(const float* grid, int64_t C, int channel_last, const vx_grid_geom* geom, const float* xyz,
+                   int64_t n_pts, float* out, void* stream);
+/* Adjoint: grad_grid += scatter of grad_out [n,C] (atomic adds). */
+int vx_grid_sample_backward(const float* grad_out, int64_t C, int channel_last, const vx_grid_geom* geom,
+                            const float* xyz, int64_t n_pts, float* grad_grid, void* stream);
+
+/* Ray march: sample_ray (voxurf_fine.py:593-617) + mask (:631-636) +
+ * grid_sampler with FD gradient (:640, 502-534) + neus alpha (:643, 463-500)
+ * + alpha/weight compaction (:647-676) + Alphas2Weights (:667, 981-988). */
+typedef struct {
+  const float* rays_o;      /* [N,3] */
+  const float* rays_d;      /* [N,3] */
+  const float* viewdirs;    /* [N,3] */
+  int64_t n_rays;
+  float near;
+  float stepdist;           /* stepsize * voxel_size                           */
+  vx_grid_geom grid;
+  const float* sdf_smooth;  /* [X,Y,Z] smoothed SDF                            */
+  float voxel_size;
+  const uint8_t* mask;      /* optional MaskGrid bool grid (NULL: none)        */
+  int64_t mask_X, mask_Y, mask_Z;
+  float mask_scale[3], mask_shift[3];
+  float inv_s;              /* 1 / s_val                                       */
+  float dist;               /* stepsize * voxel_size                           */
+  float fast_color_thres;
+  int64_t max_steps;        /* slot capacity per ray (>= every ray's N_steps)  */
+  void* rec;                /* out [N*max_steps] 16-byte records               */
+  float* dw_slot;           /* out [N*max_steps] (zeroed at written slots)     */
+  int32_t* n1;              /* out [N] kept samples (alpha > thres, to stop)   */
+  int32_t* n2;              /* out [N] shaded samples (weight > thres)         */
+  float* alphainv_last;     /* out [N]                                         */
+} vx_fine_march_args;
+int vx_fine_march(const vx_fine_march_args* args, void* stream);
+
+/* Dense rows of the shaded samples, ray-major (s2_off = exclusive scan of n2,
+ * [N+1], e.g. from vx_exclusive_scan_i32). */
+typedef struct {
+  const float* rays_o;
+  const float* rays_d;
+  int64_t n_rays;
+  float near, stepdist;
+  float xyz_min[3], xyz_max[3];
+  int64_t max_steps;
+  const void* rec;
+  const int32_t* n1;
+  const int64_t* s2_off;
+  int32_t* ray2;    /* out [S2] */
+  int32_t* step2;   /* out [S2] */
+  int32_t* slot2;   /* out [S2] */
+  float* w2;        /* out [S2] */
+  float* alpha2;    /* out [S2] */
+  float* pts2;      /* out [S2,3] */
+} vx_fine_compact_args;
+int vx_fine_compact(const vx_fine_compact_args* args, void* stream);
+
+/* Feature layout of the two color MLPs (voxurf_fine.py:694-739). */
+typedef struct {
+  int64_t K;              /* number of displacements in sorted(set(grad_feat+k_grad_feat)) */
+  float disp[4];          /* the displacements; 1.0 must be present           */
+  int64_t posbase_pe, viewbase_pe, k_posbase_pe, k_viewbase_pe;
+  int32_t center_sdf, use_rgbnet_k0, k_center_sdf;
+  int32_t k0_channels;    /* 12 */
+} vx_fine_feature_cfg;
+
+typedef struct {
+  int64_t n_rows;
+  const int32_t* ray2;
+  const float* pts2;
+  const float* viewdirs;
+  vx_grid_geom grid;
+  const float* sdf_smooth;
+  float voxel_size;
+  const float* k0_f32;      /* [X,Y,Z,12] FP32, or NULL                        */
+  const void* k0_bf16;      /* [X,Y,Z,12] BF16, or NULL                        */
+  vx_fine_feature_cfg cfg;
+  int64_t ld1, ld2;         /* row strides (elements) of X1 and X2             */
+  void* X1;                 /* out rgbnet input [S2, ld1]                      */
+  void* X2;                 /* out k_rgbnet input [S2, ld2] (last 3 = logits, filled by the caller) */
+  int32_t out_bf16;         /* X1/X2 element type: 0 FP32, 1 BF16              */
+  float* normal_out;        /* optional [S2,3] FD gradient (render_grad)       */
+} vx_fine_features_args;
+int vx_fine_features(const vx_fine_features_args* args, void* stream);
+
+/* segment_coo compositing (voxurf_fine.py:753-777). */
+typedef struct {
+  int64_t n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;       /* [S2,3] rgbnet logits                            */
+  const float* klogit;      /* [S2,3] k-branch logits, or NULL                 */
+  const float* alphainv_last;
+  float bg;
+  float* rgb0;              /* out [N,3] rgb_marched0                          */
+  float* rgbk;              /* out [N,3] rgb_marched (clamped), if klogit      */
+  float* rgbk_raw;          /* out [N,3] before the clamp, if klogit           */
+  const float* normal2;     /* optional [S2,3]                                 */
+  const int32_t* step2;     /* optional, for depth                             */
+  float dist;
+  float* normal_out;        /* optional [N,3]                                  */
+  float* depth_out;         /* optional [N]                                    */
+  float* wsum_out;          /* optional [N]                                    */
+} vx_fine_composite_args;
+int vx_fine_composite(const vx_fine_composite_args* args, void* stream);
+
+typedef struct {
+  int64_t n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;
+  const float* klogit;
+  const float* rgbk_raw;
+  const float* g_rgb0;      /* [N,3] or NULL */
+  const float* g_rgbk;      /* [N,3] or NULL */
+  float bg;
+  const float* g_last_in;   /* [N] extra gradient of alphainv_last, or NULL    */
+  float* d_logit;           /* out [S2,3] */
+  float* d_klogit;          /* out [S2,3] */
+  float* d_w2;              /* out [S2]   */
+  float* d_last;            /* out [N]    */
+} vx_fine_composite_bwd_args;
+int vx_fine_composite_backward(const vx_fine_composite_bwd_args* args, void* stream);
+
+/* Backward of the march + features: gradients of the smoothed SDF grid
+ * (accumulated into d_sdf_smooth) and of k0 (accumulated, channel-last). */
+typedef struct {
+  int64_t n_rays;
+  int64_t n_rows;
+  const float* rays_o;
+  const float* rays_d;
+  const float* viewdirs;
+  float near, stepdist;
+  vx_grid_geom grid;
+  const float* sdf_smooth;
+  float voxel_size;
+  float inv_s, dist;
+  int64_t max_steps;
+  const void* rec;
+  float* dw_slot;
+  const int32_t* n1;
+  const float* alphainv_last;
+  const float* d_last;      /* [N] gradient of alphainv_last                    */
+  const float* pts2;
+  const int32_t* slot2;
+  const float* dw2;         /* [S2] gradient of the shaded weights              */
+  vx_fine_feature_cfg cfg;
+  int64_t ld1, ld2;
+  const void* dX1;
+  const void* dX2;
+  int32_t in_bf16;
+  float* d_sdf_smooth;      /* [X,Y,Z] accumulated                              */
+  float* d_k0;              /* [X,Y,Z,12] accumulated                           */
+} vx_fine_backward_args;
+int vx_fine_backward(const vx_fine_backward_args* args, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,282 @@
+"""ORACLE — test infrastructure only (never imported by the product).
+
+CPU restatement, in torch, of the reference Voxurf training/rendering step
+(lib/voxurf_fine.py:440-802 and lib/voxurf_coarse.py:323-619, the loss of
+run.py:600-659, the TV add-grad of grid.py:67-78 and lib/utils.py:Adam),
+runnable in float64 (the correctness oracle) or float32 (the timed CPU
+baseline).  The reference's CUDA ops come from oracle/ops.py.  Ray sampling
+and the mask lookup always run in float32 with the kernels' operation order
+so that sample sets are bit-identical to the GPU's.
+
+The module takes its parameters from a voxurf_gb300 model's state (converted
+to channel-first layout and the oracle dtype), so both sides start from the
+same weights.  tests/golden/ pins this restatement against the reference's
+own Python model code.
+"""
+from __future__ import annotations
+
+import copy
+import math
+
+import numpy as np
+import torch
+import torch.nn as nn
+import torch.nn.functional as F
+
+from .ops import Alphas2WeightsOracle, RenderUtilsOracle, tv_add_grad_torch, TotalVariationOracle
+
+
+def gaussian_kernel3d(ksize: int, sigma: float) -> np.ndarray:
+    """Voxurf._gaussian_3dconv weights (voxurf_fine.py:246-258), rounded to
+    float32 as the reference stores them."""
+    x = np.arange(-(ksize // 2), ksize // 2 + 1, 1)
+    xx, yy, zz = np.meshgrid(x, x, x)
+    k = np.exp(-(xx ** 2 + yy ** 2 + zz ** 2) / (2 * sigma ** 2))
+    return (k / k.sum()).astype(np.float32)
+
+
+def smooth3d(grid: torch.Tensor, kernel: torch.Tensor) -> torch.Tensor:
+    """nn.Conv3d(1,1,k,padding=k//2,padding_mode='replicate') with no bias."""
+    p = kernel.shape[-1] // 2
+    return F.conv3d(F.pad(grid, (p, p, p, p, p, p), mode="replicate"), kernel[None, None])
+
+
+def grid_sample_pts(grid, xyz, xyz_min, xyz_max):
+    """DenseGrid.forward / grid_sampler (grid.py:47-58, voxurf_fine.py:507-520)."""
+    C = grid.shape[1]
+    ind_norm = ((xyz - xyz_min) / (xyz_max - xyz_min)).flip((-1,)) * 2 - 1
+    out = F.grid_sample(grid, ind_norm.reshape(1, 1, 1, -1, 3), mode="bilinear", align_corners=True)
+    return out.reshape(C, -1).T
+
+
+def sample_sdfs(xyz, grid, displace_list, xyz_min, xyz_max, voxel_size, use_grad_norm):
+    """voxurf_fine.py:537-577."""
+    n = xyz.shape[0]
+    xyz = xyz.reshape(1, 1, 1, -1, 3)
+    ind_norm = ((xyz - xyz_min) / (xyz_max - xyz_min)).flip((-1,)) * 2 - 1
+    gs = grid.size()[-3:]
+    size_zyx = torch.tensor([gs[2], gs[1], gs[0]])
+    ind = ((ind_norm + 1) / 2) * (size_zyx - 1)
+    offset = torch.tensor([[-1, 0, 0], [1, 0, 0], [0, -1, 0], [0, 1, 0], [0, 0, -1], [0, 0, 1]])
+    displace = torch.tensor(displace_list)
+    offset = offset[:, None, :] * displace[None, :, None]
+    all_ind = ind.unsqueeze(-2) + offset.view(-1, 3)
+    all_ind = all_ind.view(1, 1, 1, -1, 3)
+    for a in range(3):
+        all_ind[..., a] = all_ind[..., a].clamp(min=0, max=int(size_zyx[a]) - 1)
+    all_ind_norm = (all_ind / (size_zyx - 1)) * 2 - 1
+    feat = F.grid_sample(grid, all_ind_norm, mode="bilinear", align_corners=True)
+    K = len(displace_list)
+    all_ind = all_ind.view(1, 1, 1, -1, 6, K, 3)
+    diff = all_ind[:, :, :, :, 1::2, :, :] - all_ind[:, :, :, :, 0::2, :, :]
+    diff, _ = diff.max(dim=-1)
+    feat_ = feat.view(1, 1, 1, -1, 6, K)
+    feat_diff = feat_[:, :, :, :, 1::2, :] - feat_[:, :, :, :, 0::2, :]
+    grad = feat_diff / diff / voxel_size
+    feat = feat.view(n, 6, K)
+    grad = grad.view(n, 3, K)
+    if use_grad_norm:
+        grad = grad / (grad.norm(dim=1, keepdim=True) + 1e-5)
+    return feat.view(n, 6 * K), grad.view(n, 3 * K)
+
+
+def neus_alpha(viewdirs, ray_id, dist, sdf, gradients, inv_s):
+    """voxurf_fine.py:475-499 (use_mid, cos_anneal_ratio = 1)."""
+    dirs = viewdirs[ray_id]
+    true_cos = (dirs * gradients).sum(-1, keepdim=True)
+    iter_cos = -(F.relu(-true_cos * 0.5 + 0.5) * 0.0 + F.relu(-true_cos) * 1.0)
+    sdf = sdf.unsqueeze(-1)
+    est_next = sdf + iter_cos * dist * 0.5
+    est_prev = sdf - iter_cos * dist * 0.5
+    prev_cdf = torch.sigmoid(est_prev * inv_s)
+    next_cdf = torch.sigmoid(est_next * inv_s)
+    p = prev_cdf - next_cdf
+    c = prev_cdf
+    return ((p + 1e-5) / (c + 1e-5)).clip(0.0, 1.0).squeeze(-1)
+
+
+def pe(x, freq):
+    emb = (x.unsqueeze(-1) * freq).flatten(-2)
+    return torch.cat([x, emb.sin(), emb.cos()], -1)
+
+
+def f32(v) -> float:
+    return float(np.float32(v))
+
+
+class OracleFine(nn.Module):
+    """Reference fine-stage step (voxurf_fine.py:620-802) with parameters
+    copied from a voxurf_gb300 fine model."""
+
+    def __init__(self, model, dtype=torch.float64):
+        super().__init__()
+        self.dtype = dtype
+        sd = {k: v.detach().cpu() for k, v in model.state_dict().items()}
+        self.sdf_grid = nn.Parameter(sd["sdf.grid"].contiguous().to(dtype))
+        self.k0_grid = nn.Parameter(sd["k0.grid"].contiguous().to(dtype))
+        self.rgbnet = copy.deepcopy(model.rgbnet).cpu().to(dtype)
+        self.k_rgbnet = copy.deepcopy(model.k_rgbnet).cpu().to(dtype)
+        self.xyz_min = sd["xyz_min"].to(dtype)
+        self.xyz_max = sd["xyz_max"].to(dtype)
+        self.xyz_min32 = sd["xyz_min"].float()
+        self.xyz_max32 = sd["xyz_max"].float()
+        self.voxel_size = f32(model.voxel_size)
+        self.fast_color_thres = model.fast_color_thres
+        self.smooth_sdf = model.smooth_sdf
+        if self.smooth_sdf:
+            self.kernel = torch.from_numpy(gaussian_kernel3d(model.smooth_ksize, model.smooth_sigma)).to(dtype)
+        self.posfreq = sd["posfreq"].to(dtype)
+        self.viewfreq = sd["viewfreq"].to(dtype)
+        self.k_posfreq = sd["k_posfreq"].to(dtype)
+        self.k_viewfreq = sd["k_viewfreq"].to(dtype)
+        for k in ("s_ratio", "s_start", "s_learn", "step_start", "center_sdf", "use_rgbnet_k0", "k_center_sdf",
+                  "k_res", "k_detach_1", "k_detach_2", "use_rgb_k", "use_grad_norm", "grad_feat", "k_grad_feat",
+                  "sdf_feat", "k_sdf_feat"):
+            setattr(self, k, getattr(model, k))
+        self.s_val = model.s_val.clone().float().cpu()
+        self.mask = None
+        if model.mask_cache is not None:
+            mc = model.mask_cache
+            self.mask = (mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
+
+    def smoothed(self):
+        return smooth3d(self.sdf_grid, self.kernel) if self.smooth_sdf else self.sdf_grid
+
+    def forward(self, rays_o, rays_d, viewdirs, global_step=None, **rk):
+        dt = self.dtype
+        N = len(rays_o)
+        stepdist = f32(rk["stepsize"] * np.float32(self.voxel_size))
+        ru = RenderUtilsOracle
+        ray_pts, mask_outbbox, ray_id, step_id, _, _, _ = ru.sample_pts_on_rays(
+            rays_o.float().cpu(), rays_d.float().cpu(), self.xyz_min32, self.xyz_max32, rk["near"], 1e9, stepdist)
+        inb = ~mask_outbbox
+        ray_pts32, ray_id, step_id = ray_pts[inb], ray_id[inb], step_id[inb]
+        if self.mask is not None:
+            m = ru.maskcache_lookup(self.mask[0], ray_pts32, self.mask[1], self.mask[2])
+            ray_pts32, ray_id, step_id = ray_pts32[m], ray_id[m], step_id[m]
+        ray_pts = ray_pts32.to(dt)
+        viewdirs = viewdirs.cpu().to(dt)
+        sdf_grid = self.smoothed()
+        sdf = grid_sample_pts(sdf_grid, ray_pts, self.xyz_min, self.xyz_max)[:, 0]
+        _, g = sample_sdfs(ray_pts, sdf_grid, [1.0], self.xyz_min, self.xyz_max, self.voxel_size, False)
+        gradient = torch.cat([g[:, [2]], g[:, [1]], g[:, [0]]], dim=-1)
+        dist = f32(rk["stepsize"] * np.float32(self.voxel_size))
+        if global_step is not None:
+            if not self.s_learn:
+                s_val = 1.0 / (global_step + self.s_ratio / self.s_start - self.step_start) * self.s_ratio
+                self.s_val = torch.ones(1) * s_val
+            else:
+                s_val = float(self.s_val.item())
+        else:
+            s_val = 0
+        inv_s = float((torch.ones(1) / self.s_val.float()).item())
+        alpha = neus_alpha(viewdirs, ray_id, dist, sdf, gradient, inv_s)
+        thr = self.fast_color_thres
+        if thr > 0:
+            m = alpha > thr
+            alpha, ray_id, ray_pts, step_id, gradient, sdf = alpha[m], ray_id[m], ray_pts[m], step_id[m], \
+                gradient[m], sdf[m]
+        weights, alphainv_last = Alphas2WeightsOracle.apply(alpha, ray_id, N)
+        if thr > 0:
+            m = weights > thr
+            weights, alpha, ray_pts, ray_id, step_id, gradient, sdf = weights[m], alpha[m], ray_pts[m], ray_id[m], \
+                step_id[m], gradient[m], sdf[m]
+        k0 = grid_sample_pts(self.k0_grid, ray_pts, self.xyz_min, self.xyz_max)
+        disps = sorted(set(tuple(self.grad_feat) + tuple(self.k_grad_feat)))
+        all_feat, all_grad = sample_sdfs(ray_pts, sdf_grid, disps, self.xyz_min, self.xyz_max, self.voxel_size,
+                                         self.use_grad_norm)
+        rays_xyz = (ray_pts - self.xyz_min) / (self.xyz_max - self.xyz_min)
+        xyz_emb = pe(rays_xyz, self.posfreq)
+        view_emb = pe(viewdirs, self.viewfreq)
+        parts = ([k0] if self.use_rgbnet_k0 else []) + [xyz_emb, view_emb[ray_id]]
+        if self.center_sdf:
+            parts.append(sdf[:, None])
+        parts += [all_feat, all_grad]
+        rgb_feat = torch.cat(parts, -1)
+        rgb_logit = self.rgbnet(rgb_feat)
+        rgb = torch.sigmoid(rgb_logit)
+        out = {"alphainv_cum": alphainv_last, "weights": weights, "raw_rgb": rgb, "raw_alpha": alpha,
+               "gradient": gradient, "ray_id": ray_id, "step_id": step_id, "s_val": s_val, "rgb_feat": rgb_feat}
+        bg = rk["bg"]
+        if self.use_rgb_k:
+            k_feat = torch.cat([k0, pe(rays_xyz, self.k_posfreq), pe(viewdirs, self.k_viewfreq)[ray_id], gradient]
+                               + ([sdf[:, None]] if self.k_center_sdf else []), -1)
+            if self.k_res:
+                k_feat = torch.cat([k_feat, rgb_logit.detach() if self.k_detach_1 else rgb_logit], -1)
+            base = rgb_logit.detach() if self.k_detach_2 else rgb_logit
+            k_rgb = torch.sigmoid(base + self.k_rgbnet(k_feat))
+            k_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * k_rgb) \
+                + alphainv_last[..., None] * bg
+            out["rgb_marched"] = k_marched.clamp(0, 1)
+            out["k_rgb_feat"] = k_feat
+        rgb_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * rgb) \
+            + alphainv_last[..., None] * bg
+        if self.use_rgb_k:
+            out["rgb_marched0"] = rgb_marched
+        else:
+            out["rgb_marched"] = rgb_marched
+        if rk.get("render_depth", False):
+            with torch.no_grad():
+                out["depth"] = torch.zeros([N], dtype=dt).index_add(0, ray_id, weights * step_id * dist)
+        if rk.get("render_grad", False):
+            normal = gradient / (gradient.norm(2, -1, keepdim=True) + 1e-6)
+            out["normal_marched"] = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * normal)
+        return out
+
+
+def train_loss(ret, target, weight_main=1.0, weight_entropy_last=0.001, weight_rgb0=0.5):
+    """run.py:604-636 (the loss terms of the fine dtu_e2e stage)."""
+    target = target.to(ret["rgb_marched"].dtype)
+    loss = weight_main * F.mse_loss(ret["rgb_marched"], target)
+    if weight_entropy_last > 0:
+        # run.py:608 indexes [..., -1] of a 1-D tensor: the LAST RAY only
+        pout = ret["alphainv_cum"][..., -1].clamp(1e-6, 1 - 1e-6)
+        loss = loss + weight_entropy_last * (-(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean())
+    if weight_rgb0 > 0 and "rgb_marched0" in ret:
+        loss = loss + F.mse_loss(ret["rgb_marched0"], target) * weight_rgb0
+    return loss
+
+
+class UtilsAdam:
+    """lib/utils.py:54-199 (Adam with per-voxel lr) in plain torch."""
+
+    def __init__(self, groups, betas=(0.9, 0.99), eps=1e-8):
+        self.groups = groups  # list of (params, lr)
+        self.betas, self.eps = betas, eps
+        self.state = {}
+        self.per_lr = None
+
+    @torch.no_grad()
+    def step(self):
+        b1, b2 = self.betas
+        for params, lr in self.groups:
+            for p in params:
+                if p.grad is None:
+                    continue
+                st = self.state.setdefault(id(p), {"step": 0, "m": torch.zeros_like(p), "v": torch.zeros_like(p)})
+                st["step"] += 1
+                t = st["step"]
+                bc1, bc2 = 1 - b1 ** t, 1 - b2 ** t
+                st["m"].mul_(b1).add_(p.grad, alpha=1 - b1)
+                st["v"].mul_(b2).addcmul_(p.grad, p.grad, value=1 - b2)
+                denom = (st["v"].sqrt() / math.sqrt(bc2)).add_(self.eps)
+                per_lr = self.per_lr if (self.per_lr is not None and p.shape == self.per_lr.shape) else None
+                if per_lr is not None:
+                    p.addcdiv_(st["m"] * per_lr, denom, value=-lr / bc1)
+                else:
+                    p.addcdiv_(st["m"], denom, value=-lr / bc1)
+
+
+def tv_add_grad(grid_param, weight, world_size_max, dense_mode, mask=None):
+    """Voxurf.*_total_variation_add_grad (voxurf_fine.py:403-409) -> grid.py:67-78."""
+    w = weight * world_size_max / 128
+    if grid_param.grad is None:
+        grid_param.grad = torch.zeros_like(grid_param)
+    if grid_param.dtype == torch.float32:
+        if mask is None:
+            TotalVariationOracle.total_variation_add_grad(grid_param.data, grid_param.grad, w, w, w, dense_mode)
+        else:
+            TotalVariationOracle.total_variation_add_grad_new(grid_param.data, grid_param.grad, mask, w, w, w,
+                                                              dense_mode)
+    else:
+        tv_add_grad_torch(grid_param.data, grid_param.grad, w, w, w, dense_mode, mask)

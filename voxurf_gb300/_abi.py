@@ -1,0 +1,130 @@
+"""ctypes mirrors of the parameter structs in include/voxurf_gb300.h (fused
+renderer, smoothing) and thin callers.  Field order and types must match
+the header exactly."""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _native
+
+P = C.c_void_p
+F = C.c_float
+I64 = C.c_int64
+I32 = C.c_int32
+
+
+class GridGeom(C.Structure):
+    _fields_ = [("X", I64), ("Y", I64), ("Z", I64), ("xyz_min", F * 3), ("xyz_max", F * 3)]
+
+
+class FineMarchArgs(C.Structure):
+    _fields_ = [
+        ("rays_o", P), ("rays_d", P), ("viewdirs", P), ("n_rays", I64), ("near", F), ("stepdist", F),
+        ("grid", GridGeom), ("sdf_smooth", P), ("voxel_size", F),
+        ("mask", P), ("mask_X", I64), ("mask_Y", I64), ("mask_Z", I64), ("mask_scale", F * 3), ("mask_shift", F * 3),
+        ("inv_s", F), ("dist", F), ("fast_color_thres", F), ("max_steps", I64),
+        ("rec", P), ("dw_slot", P), ("n1", P), ("n2", P), ("alphainv_last", P),
+    ]
+
+
+class FineCompactArgs(C.Structure):
+    _fields_ = [
+        ("rays_o", P), ("rays_d", P), ("n_rays", I64), ("near", F), ("stepdist", F), ("xyz_min", F * 3),
+        ("xyz_max", F * 3), ("max_steps", I64), ("rec", P), ("n1", P), ("s2_off", P),
+        ("ray2", P), ("step2", P), ("slot2", P), ("w2", P), ("alpha2", P), ("pts2", P),
+    ]
+
+
+class FineFeatureCfg(C.Structure):
+    _fields_ = [
+        ("K", I64), ("disp", F * 4), ("posbase_pe", I64), ("viewbase_pe", I64), ("k_posbase_pe", I64),
+        ("k_viewbase_pe", I64), ("center_sdf", I32), ("use_rgbnet_k0", I32), ("k_center_sdf", I32),
+        ("k0_channels", I32),
+    ]
+
+
+class FineFeaturesArgs(C.Structure):
+    _fields_ = [
+        ("n_rows", I64), ("ray2", P), ("pts2", P), ("viewdirs", P), ("grid", GridGeom), ("sdf_smooth", P),
+        ("voxel_size", F), ("k0_f32", P), ("k0_bf16", P), ("cfg", FineFeatureCfg), ("ld1", I64), ("ld2", I64),
+        ("X1", P), ("X2", P), ("out_bf16", I32), ("normal_out", P),
+    ]
+
+
+class FineCompositeArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("s2_off", P), ("w2", P), ("logit", P), ("klogit", P), ("alphainv_last", P), ("bg", F),
+        ("rgb0", P), ("rgbk", P), ("rgbk_raw", P), ("normal2", P), ("step2", P), ("dist", F),
+        ("normal_out", P), ("depth_out", P), ("wsum_out", P),
+    ]
+
+
+class FineCompositeBwdArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("s2_off", P), ("w2", P), ("logit", P), ("klogit", P), ("rgbk_raw", P), ("g_rgb0", P),
+        ("g_rgbk", P), ("bg", F), ("g_last_in", P), ("d_logit", P), ("d_klogit", P), ("d_w2", P), ("d_last", P),
+    ]
+
+
+class FineBackwardArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("n_rows", I64), ("rays_o", P), ("rays_d", P), ("viewdirs", P), ("near", F),
+        ("stepdist", F), ("grid", GridGeom), ("sdf_smooth", P), ("voxel_size", F), ("inv_s", F), ("dist", F),
+        ("max_steps", I64), ("rec", P), ("dw_slot", P), ("n1", P), ("alphainv_last", P), ("d_last", P),
+        ("pts2", P), ("slot2", P), ("dw2", P), ("cfg", FineFeatureCfg), ("ld1", I64), ("ld2", I64), ("dX1", P),
+        ("dX2", P), ("in_bf16", I32), ("d_sdf_smooth", P), ("d_k0", P),
+    ]
+
+
+_STRUCT_FNS = {
+    "vx_fine_march": FineMarchArgs,
+    "vx_fine_compact": FineCompactArgs,
+    "vx_fine_features": FineFeaturesArgs,
+    "vx_fine_composite": FineCompositeArgs,
+    "vx_fine_composite_backward": FineCompositeBwdArgs,
+    "vx_fine_backward": FineBackwardArgs,
+}
+
+_declared = False
+
+
+def _declare():
+    global _declared
+    if _declared:
+        return
+    lib = _native.load()
+    for name, st in _STRUCT_FNS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = [C.POINTER(st), C.c_void_p]
+        fn.restype = C.c_int
+    lib.vx_smooth3d.argtypes = [P, P, P, P, I64, I64, I64, P, C.c_int, P]
+    lib.vx_smooth3d.restype = C.c_int
+    lib.vx_smooth3d_adjoint.argtypes = [P, P, P, P, I64, I64, I64, P, C.c_int, C.c_int, P]
+    lib.vx_smooth3d_adjoint.restype = C.c_int
+    for name in ("vx_grid_sample", "vx_grid_sample_backward"):
+        fn = getattr(lib, name)
+        fn.argtypes = [P, I64, C.c_int, C.POINTER(GridGeom), P, I64, P, P]
+        fn.restype = C.c_int
+    _declared = True
+
+
+def grid_sample(name: str, grid_ptr, C_: int, channel_last: bool, geom: GridGeom, xyz_ptr, n: int, out_ptr,
+                stream: int) -> None:
+    _declare()
+    fn = getattr(_native.load(), name)
+    _native.check(fn(grid_ptr, C_, int(channel_last), C.byref(geom), xyz_ptr, n, out_ptr, stream), name)
+
+
+def call_struct(name: str, args: C.Structure, stream: int) -> None:
+    _declare()
+    fn = getattr(_native.load(), name)
+    _native.check(fn(C.byref(args), stream), name)
+
+
+def call(name: str, *args) -> None:
+    _declare()
+    _native.call(name, *args)
+
+
+def struct_names() -> list[str]:
+    return list(_STRUCT_FNS) + ["vx_smooth3d", "vx_smooth3d_adjoint", "vx_grid_sample", "vx_grid_sample_backward"]

@@ -1,0 +1,68 @@
+"""Workload definitions: model kwargs and synthetic scenes of the five
+benchmark configurations (coarse 96^3, fine 256^3, gradient check 32^3,
+render server 4 x 256^3, long rays 384^3).
+
+Model hyper-parameters follow the reference's DTU configs
+(configs/dtu_e2e/coarse.py:60-76 and configs/dtu_e2e/fine.py:136-165 on top
+of configs/default_fine_s.py:107-138) except where the workload says
+otherwise (grid size, smoothing, MLP width).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import synthetic
+
+BBOX = ([-1.0, -1.0, -1.0], [1.0, 1.0, 1.0])
+
+
+def fine_model_kwargs(R: int = 256, precision: str = "fp32", width: int = 192, smooth: bool = True) -> dict:
+    """Fine stage (lib/voxurf_fine.py) with the dtu_e2e/fine.py settings:
+    rgbnet 70 -> 192 x3 -> 3, k_rgbnet 60 -> 192 x3 -> 3, hierarchical
+    displacements (0.5, 1, 1.5), center_sdf, k_res, grad norm, s_ratio 50,
+    s_start 0.05; Gaussian smoothing 5^3 sigma 0.8 of the SDF each step."""
+    return dict(
+        xyz_min=BBOX[0], xyz_max=BBOX[1], num_voxels=R ** 3, num_voxels_base=R ** 3, alpha_init=1e-2,
+        fast_color_thres=1e-4, rgbnet_dim=12, rgbnet_depth=4, rgbnet_width=width, posbase_pe=5, viewbase_pe=1,
+        k_posbase_pe=5, k_viewbase_pe=1, k_res=True, k_rgbnet_depth=4, center_sdf=True,
+        grad_feat=(0.5, 1.0, 1.5), sdf_feat=(0.5, 1.0, 1.5), k_grad_feat=(1.0,), use_grad_norm=True,
+        s_ratio=50, s_start=0.05, smooth_ksize=5 if smooth else 0, smooth_sigma=0.8, precision=precision,
+    )
+
+
+FINE_RENDER_KWARGS = dict(near=0.1, far=6.0, bg=0, stepsize=0.5, inverse_y=True, flip_x=False, flip_y=False)
+
+
+def build_fine_model(R: int = 256, precision: str = "fp32", device="cuda", seed: int = 0, scene: str = "sphere_torus",
+                     mask_voxels: float | None = None, width: int = 192, smooth: bool = True):
+    """Fine Voxurf model with the synthetic scene loaded.  mask_voxels: if
+    given, a MaskGrid of |SDF| < mask_voxels*voxel_size (the |SDF| < 0.05
+    mask of the 256^3 workload is mask_voxels = 6.4)."""
+    from .grid import MaskGrid
+    from .voxurf_fine import Voxurf
+
+    torch.manual_seed(seed)
+    sdf = torch.from_numpy(synthetic.make_sdf(scene, R, seed=seed))
+    mask = None
+    if mask_voxels is not None:
+        thr = mask_voxels * 2.0 / R
+        mask = MaskGrid(mask=(sdf.abs() < thr), xyz_min=BBOX[0], xyz_max=BBOX[1])
+    model = Voxurf(**fine_model_kwargs(R, precision, width, smooth), mask_grid=None)
+    with torch.no_grad():
+        model.sdf.grid.data = sdf[None, None].clone()
+        k0 = synthetic.make_k0(R, 12, seed=seed + 1)
+        model.k0.grid.data = k0.permute(3, 0, 1, 2)[None].contiguous(memory_format=torch.channels_last_3d)
+    model = model.to(device)
+    if mask is not None:
+        # as Voxurf.__init__ with a mask cache: record the non-empty mask and
+        # set the SDF to 1 outside it (voxurf_fine.py:192-196, 353-367)
+        model.mask_cache = mask.to(device)
+        model._set_nonempty_mask()
+    if precision == "bf16":
+        model.refresh_k0_shadow()
+    return model
+
+
+def train_targets(n: int, seed: int = 0) -> np.ndarray:
+    return np.random.default_rng(seed + 7).uniform(0, 1, size=(n, 3)).astype(np.float32)

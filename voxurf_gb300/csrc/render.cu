@@ -1,0 +1,1079 @@
+// Fused per-ray volume rendering of the Voxurf fine model
+// (lib/voxurf_fine.py:620-802) and its hand-written backward.
+//
+// Forward, one warp per ray, 32 samples per iteration:
+//   march    : bbox clip + sample positions (render_utils_kernel.cu:12-194,
+//              bit-identical to sample_pts_on_rays), mask lookup
+//              (render_utils_kernel.cu:374-392), SDF + 6 finite-difference
+//              probes on the smoothed grid (voxurf_fine.py:502-577 with
+//              displace 1.0), NeuS alpha (voxurf_fine.py:463-500), the
+//              alpha > thres compaction (:647-654), the transmittance scan
+//              with the T < 1e-3 stop (render_utils_kernel.cu:577-605, FP64
+//              carry) and the weight > thres flag (:668-676).  Survivors go to
+//              per-ray slots; nothing is written for culled samples.
+//   compact  : per-ray survivors of the weight test -> dense rows (ray-major,
+//              near-to-far, the order of the reference's masked tensors).
+//   features : per shaded row, centre SDF, hierarchical probes (6K values,
+//              normalised gradients), k0 trilinear (channel-last, FP32 or
+//              BF16 storage), positional encodings -> the two MLP inputs.
+//   composite: per ray, sum w*sigmoid(logit) + alphainv_last*bg, k-branch
+//              clamped (voxurf_fine.py:753-763).
+// Backward recomputes every interpolated value (no per-sample activations
+// are stored besides alpha, T, w) and scatters into dense FP32 gradient grids
+// with red.global.add (vectorised .v4 for k0).
+#include <math.h>
+#include "common.cuh"
+#include "trilinear.cuh"
+
+namespace vx {
+
+constexpr int MAX_K = 4;  // hierarchical displacements (configs use <= 4)
+
+struct MarchParams {
+  const float* rays_o;
+  const float* rays_d;
+  const float* viewdirs;
+  int n_rays;
+  float near, stepdist;
+  float bmin[3], bmax[3];  // model xyz_min/xyz_max
+  GridGeom g;              // SDF grid geometry (same bbox)
+  const float* sdf;        // smoothed SDF grid [X,Y,Z]
+  float voxel_size;
+  const uint8_t* mask;     // optional bool grid for maskcache_lookup semantics
+  int mX, mY, mZ;
+  float mscale[3], mshift[3];
+  float inv_s, dist, thres;
+  int max_steps;
+  // outputs
+  float4* rec;        // [n_rays*max_steps] {step|s2flag<<31, alpha, T, w}
+  float* dw_slot;     // zeroed at every written slot
+  int* n1;            // survivors of alpha > thres up to the stop, per ray
+  int* n2;            // of which weight > thres
+  float* alphainv_last;
+  int* err;
+};
+
+// ---- exact sample positions (shared with sampling.cu semantics) ------------
+struct RayFrame {
+  float st[3], dr[3];
+  int64_t n_steps;
+};
+
+__device__ __forceinline__ RayFrame ray_frame(const float* o, const float* d, const float* mn, const float* mx,
+                                              float near, float stepdist) {
+  const float far = 1e9f;  // voxurf_fine.py:605
+  const float vx = (d[0] == 0.f) ? 1e-6f : d[0];
+  const float vy = (d[1] == 0.f) ? 1e-6f : d[1];
+  const float vz = (d[2] == 0.f) ? 1e-6f : d[2];
+  const float ax = fdiv(fsub(mx[0], o[0]), vx), ay = fdiv(fsub(mx[1], o[1]), vy), az = fdiv(fsub(mx[2], o[2]), vz);
+  const float bx = fdiv(fsub(mn[0], o[0]), vx), by = fdiv(fsub(mn[1], o[1]), vy), bz = fdiv(fsub(mn[2], o[2]), vz);
+  const float t_min = fmaxf(fminf(fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz)), far), near);
+  const float t_max = fmaxf(fminf(fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)), far), near);
+  const float rn = __fsqrt_rn(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
+  RayFrame f;
+  const float c = ceilf(fdiv(fmul(fsub(t_max, t_min), rn), stepdist));
+  f.n_steps = (int64_t)fmax((double)c, 1.0);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    f.st[a] = fadd(o[a], fmul(d[a], t_min));
+    f.dr[a] = fdiv(d[a], rn);
+  }
+  return f;
+}
+
+__device__ __forceinline__ void sample_point(const RayFrame& f, float stepdist, int k, float p[3]) {
+  const float dist = fmul(stepdist, (float)k);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) p[a] = fadd(f.st[a], fmul(f.dr[a], dist));
+}
+
+// ---- SDF value + finite-difference gradient (sample_sdfs, one displacement) -
+struct Probe {
+  float fm, fp;     // values at index -d and +d (clamped)
+  float inv_diff;   // 1 / (clamped index difference)
+  Corners cm, cp;
+};
+
+__device__ __forceinline__ void probe_axis(const float* __restrict__ sdf, const GridGeom& g, const float ind[3],
+                                           int axis, float d, Probe& pr, bool keep_corners) {
+  float im[3] = {ind[0], ind[1], ind[2]};
+  float ip[3] = {ind[0], ind[1], ind[2]};
+  const float hi = (float)(gsize(g, axis) - 1);
+  im[axis] = fminf(fmaxf(ind[axis] - d, 0.f), hi);
+  ip[axis] = fminf(fmaxf(ind[axis] + d, 0.f), hi);
+  Corners cm = corners_of(g, im[0], im[1], im[2]);
+  Corners cp = corners_of(g, ip[0], ip[1], ip[2]);
+  pr.fm = gather1(sdf, cm);
+  pr.fp = gather1(sdf, cp);
+  pr.inv_diff = 1.f / (ip[axis] - im[axis]);
+  if (keep_corners) {
+    pr.cm = cm;
+    pr.cp = cp;
+  }
+}
+
+__device__ __forceinline__ void to_index(const GridGeom& g, const float p[3], float ind[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) ind[a] = world_to_index(g, a, p[a]);
+}
+
+// SDF and gradient (xyz order) at one point: centre + 6 probes at +-1 voxel.
+__device__ __forceinline__ void sdf_and_grad(const float* __restrict__ sdf, const GridGeom& g, float voxel_size,
+                                             const float ind[3], float* s, float gr[3]) {
+  *s = sample1(sdf, g, ind[0], ind[1], ind[2]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    Probe pr;
+    probe_axis(sdf, g, ind, a, 1.f, pr, false);
+    gr[a] = ((pr.fp - pr.fm) * pr.inv_diff) / voxel_size;
+  }
+}
+
+__device__ __forceinline__ float sigmoidf_(float x) { return 1.f / (1.f + expf(-x)); }
+
+// NeuS s-density alpha (voxurf_fine.py:475-499, cos_anneal_ratio = 1).
+struct AlphaState {
+  float alpha, raw, P, Q, cosv;
+};
+
+__device__ __forceinline__ AlphaState neus_alpha(float s, const float gr[3], const float v[3], float inv_s,
+                                                 float dist) {
+  AlphaState a;
+  a.cosv = v[0] * gr[0] + v[1] * gr[1] + v[2] * gr[2];
+  const float ic = fminf(a.cosv, 0.f);  // -relu(-cos)
+  const float h = ic * dist * 0.5f;
+  const float next = s + h, prev = s - h;
+  a.P = sigmoidf_(prev * inv_s);
+  a.Q = sigmoidf_(next * inv_s);
+  a.raw = (a.P - a.Q + 1e-5f) / (a.P + 1e-5f);
+  a.alpha = fminf(fmaxf(a.raw, 0.f), 1.f);
+  return a;
+}
+
+__device__ __forceinline__ bool outside_bbox(const float p[3], const float* mn, const float* mx) {
+  return (mn[0] > p[0]) | (mn[1] > p[1]) | (mn[2] > p[2]) | (mx[0] < p[0]) | (mx[1] < p[1]) | (mx[2] < p[2]);
+}
+
+__device__ __forceinline__ bool mask_hit(const MarchParams& P, const float p[3]) {
+  int ijk[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) ijk[a] = (int)roundf(fadd(fmul(p[a], P.mscale[a]), P.mshift[a]));
+  if (ijk[0] < 0 || ijk[0] >= P.mX || ijk[1] < 0 || ijk[1] >= P.mY || ijk[2] < 0 || ijk[2] >= P.mZ) return false;
+  return P.mask[((int64_t)ijk[0] * P.mY + ijk[1]) * P.mZ + ijk[2]] != 0;
+}
+
+__global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  int64_t n_steps = f.n_steps;
+  if (n_steps > P.max_steps) {
+    if (lane == 0) set_device_error(P.err, VX_ERR_CAPACITY);
+    n_steps = P.max_steps;
+  }
+  const int64_t slot0 = (int64_t)r * P.max_steps;
+  double carry = 1.0;
+  int cnt1 = 0, cnt2 = 0;
+  bool stopped = false;
+  double last = 1.0;
+  for (int base = 0; base < n_steps && !stopped; base += 32) {
+    const int k = base + lane;
+    bool keep = false;
+    float alpha = 0.f;
+    if (k < n_steps) {
+      float p[3];
+      sample_point(f, P.stepdist, k, p);
+      bool inb = !outside_bbox(p, P.bmin, P.bmax);
+      if (inb && P.mask) inb = mask_hit(P, p);
+      if (inb) {
+        float ind[3], s, gr[3];
+        to_index(P.g, p, ind);
+        sdf_and_grad(P.sdf, P.g, P.voxel_size, ind, &s, gr);
+        alpha = neus_alpha(s, gr, v, P.inv_s, P.dist).alpha;
+        keep = alpha > P.thres;
+      }
+    }
+    const unsigned keep_mask = __ballot_sync(0xffffffffu, keep);
+    if (keep_mask == 0u) continue;
+    const double fct = keep ? 1.0 - (double)alpha : 1.0;
+    const double incl = warp_inclusive_prod(fct) * carry;
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = carry;
+    const unsigned stop_mask = __ballot_sync(0xffffffffu, keep && incl < 1e-3);
+    unsigned live = keep_mask;
+    if (stop_mask) {
+      const int ks = __ffs(stop_mask) - 1;
+      live &= (ks == 31) ? 0xffffffffu : ((2u << ks) - 1u);
+      last = __shfl_sync(0xffffffffu, incl, ks);
+      stopped = true;
+    }
+    const bool mine = (live >> lane) & 1u;
+    const float T = (float)excl;
+    const float w = T * alpha;
+    const bool s2 = mine && (w > P.thres);
+    if (mine) {
+      const int64_t slot = slot0 + cnt1 + __popc(live & lt_mask);
+      const unsigned tag = (unsigned)k | (s2 ? 0x80000000u : 0u);
+      P.rec[slot] = make_float4(__uint_as_float(tag), alpha, T, w);
+      P.dw_slot[slot] = 0.f;
+    }
+    cnt1 += __popc(live);
+    cnt2 += __popc(__ballot_sync(0xffffffffu, s2));
+    if (!stopped) carry = __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) {
+    P.n1[r] = cnt1;
+    P.n2[r] = cnt2;
+    P.alphainv_last[r] = (float)(stopped ? last : carry);
+  }
+}
+
+// ---- compaction of the shaded samples -------------------------------------
+struct CompactParams {
+  const float* rays_o;
+  const float* rays_d;
+  int n_rays;
+  float near, stepdist;
+  float bmin[3], bmax[3];
+  int max_steps;
+  const float4* rec;
+  const int* n1;
+  const int64_t* s2_off;  // exclusive scan of n2, [n_rays+1]
+  // outputs, one row per shaded sample
+  int* ray2;
+  int* step2;
+  int* slot2;
+  float* w2;
+  float* alpha2;
+  float* pts2;  // [S2, 3]
+};
+
+__global__ void __launch_bounds__(256) compact_fine_kernel(CompactParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const int n = P.n1[r];
+  int64_t row = P.s2_off[r];
+  if (P.s2_off[r + 1] == row) return;
+  float o[3], d[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  const int64_t slot0 = (int64_t)r * P.max_steps;
+  for (int base = 0; base < n; base += 32) {
+    const int j = base + lane;
+    float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool s2 = false;
+    if (j < n) {
+      rc = P.rec[slot0 + j];
+      s2 = (__float_as_uint(rc.x) & 0x80000000u) != 0u;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, s2);
+    if (s2) {
+      const int64_t o2 = row + __popc(m & ((1u << lane) - 1u));
+      const int k = (int)(__float_as_uint(rc.x) & 0x7fffffffu);
+      float p[3];
+      sample_point(f, P.stepdist, k, p);
+      P.ray2[o2] = r;
+      P.step2[o2] = k;
+      P.slot2[o2] = (int)(slot0 + j);
+      P.w2[o2] = rc.w;
+      P.alpha2[o2] = rc.y;
+      P.pts2[3 * o2 + 0] = p[0];
+      P.pts2[3 * o2 + 1] = p[1];
+      P.pts2[3 * o2 + 2] = p[2];
+    }
+    row += __popc(m);
+  }
+}
+
+// ---- features of the shaded samples ----------------------------------------
+struct FeatParams {
+  int64_t n_rows;
+  const int* ray2;
+  const float* pts2;
+  const float* viewdirs;
+  GridGeom g;
+  const float* sdf;  // smoothed
+  float voxel_size;
+  const float* k0f;            // [X,Y,Z,12] FP32 (or null)
+  const __nv_bfloat16* k0h;    // [X,Y,Z,12] BF16 (or null)
+  int K;
+  float disp[MAX_K];
+  int k_unit;                  // index of displacement 1.0 in disp
+  int pos_pe, view_pe, kpos_pe, kview_pe;
+  int center_sdf, use_rgbnet_k0, k_center_sdf;
+  int ld1, ld2;                // row strides of X1, X2
+  void* X1;
+  void* X2;
+  int out_bf16;
+  // optional per-row outputs for the render path
+  float* normal_out;   // [S2,3] gradient (xyz, unnormalised) or null
+};
+
+template <typename T>
+__device__ __forceinline__ void put(T* row, int c, float v);
+template <>
+__device__ __forceinline__ void put<float>(float* row, int c, float v) { row[c] = v; }
+template <>
+__device__ __forceinline__ void put<__nv_bfloat16>(__nv_bfloat16* row, int c, float v) {
+  row[c] = __float2bfloat16_rn(v);
+}
+
+template <typename T>
+__device__ __forceinline__ int put_pe(T* row, int c, const float x[3], int n_freq) {
+  // [x, sin(x*2^f) (axis-major), cos(...)] as torch.cat([x, emb.sin(), emb.cos()])
+  // with emb = (x.unsqueeze(-1) * freq).flatten(-2)  (voxurf_fine.py:694-698).
+#pragma unroll
+  for (int a = 0; a < 3; ++a) put(row, c + a, x[a]);
+  c += 3;
+  for (int a = 0; a < 3; ++a)
+    for (int q = 0; q < n_freq; ++q) put(row, c + a * n_freq + q, sinf(x[a] * (float)(1 << q)));
+  c += 3 * n_freq;
+  for (int a = 0; a < 3; ++a)
+    for (int q = 0; q < n_freq; ++q) put(row, c + a * n_freq + q, cosf(x[a] * (float)(1 << q)));
+  return c + 3 * n_freq;
+}
+
+// Hierarchical features of one point: feat[6K] (dir-major: z-,z+,y-,y+,x-,x+
+// each over K) and grad[3K] (pair-major z,y,x, normalised per K when
+// use_grad_norm), and the unnormalised d=1 gradient in xyz order.
+__device__ __forceinline__ void hier_features(const float* __restrict__ sdf, const GridGeom& g, float vs,
+                                              const float ind[3], int K, const float* disp, float feat[6 * MAX_K],
+                                              float graw[3 * MAX_K]) {
+  for (int kk = 0; kk < K; ++kk) {
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) {
+      const int axis = 2 - pair;  // zyx
+      Probe pr;
+      probe_axis(sdf, g, ind, axis, disp[kk], pr, false);
+      feat[(2 * pair + 0) * K + kk] = pr.fm;
+      feat[(2 * pair + 1) * K + kk] = pr.fp;
+      graw[pair * K + kk] = ((pr.fp - pr.fm) * pr.inv_diff) / vs;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= P.n_rows) return;
+  const int r = P.ray2[row];
+  const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
+  const float v[3] = {__ldg(P.viewdirs + 3 * r), __ldg(P.viewdirs + 3 * r + 1), __ldg(P.viewdirs + 3 * r + 2)};
+  float ind[3];
+  to_index(P.g, p, ind);
+  const float s = sample1(P.sdf, P.g, ind[0], ind[1], ind[2]);
+  float feat[6 * MAX_K], graw[3 * MAX_K];
+  hier_features(P.sdf, P.g, P.voxel_size, ind, P.K, P.disp, feat, graw);
+  // gradient for k_rgbnet: unnormalised, displacement 1.0, xyz order
+  const float gx = graw[2 * P.K + P.k_unit], gy = graw[1 * P.K + P.k_unit], gz = graw[0 * P.K + P.k_unit];
+  float k0v[12];
+  const Corners c = corners_of(P.g, ind[0], ind[1], ind[2]);
+  if (P.k0h)
+    gatherC<12>(P.k0h, c, k0v);
+  else
+    gatherC<12>(P.k0f, c, k0v);
+  float xyzn[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) xyzn[a] = (p[a] - P.g.mn[a]) / (P.g.mx[a] - P.g.mn[a]);
+
+  T* x1 = reinterpret_cast<T*>(P.X1) + row * P.ld1;
+  int col = 0;
+  if (P.use_rgbnet_k0)
+    for (int ch = 0; ch < 12; ++ch) put(x1, col++, k0v[ch]);
+  col = put_pe(x1, col, xyzn, P.pos_pe);
+  col = put_pe(x1, col, v, P.view_pe);
+  if (P.center_sdf) put(x1, col++, s);
+  for (int q = 0; q < 6 * P.K; ++q) put(x1, col++, feat[q]);
+  for (int kk = 0; kk < P.K; ++kk) {
+    const float a = graw[0 * P.K + kk], b = graw[1 * P.K + kk], cc = graw[2 * P.K + kk];
+    const float nrm = sqrtf(a * a + b * b + cc * cc) + 1e-5f;
+    put(x1, col + 0 * P.K + kk, a / nrm);
+    put(x1, col + 1 * P.K + kk, b / nrm);
+    put(x1, col + 2 * P.K + kk, cc / nrm);
+  }
+  T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
+  col = 0;
+  for (int ch = 0; ch < 12; ++ch) put(x2, col++, k0v[ch]);
+  col = put_pe(x2, col, xyzn, P.kpos_pe);
+  col = put_pe(x2, col, v, P.kview_pe);
+  put(x2, col++, gx);
+  put(x2, col++, gy);
+  put(x2, col++, gz);
+  if (P.k_center_sdf) put(x2, col++, s);
+  if (P.normal_out) {
+    P.normal_out[3 * row + 0] = gx;
+    P.normal_out[3 * row + 1] = gy;
+    P.normal_out[3 * row + 2] = gz;
+  }
+}
+
+// ---- compositing ------------------------------------------------------------
+struct CompositeParams {
+  int n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;    // [S2,3] rgbnet output
+  const float* klogit;   // [S2,3] rgb_logit + k_rgbnet output (or null)
+  const float* alphainv_last;
+  float bg;
+  float* rgb0;     // [N,3] sum w*sigmoid(logit) + alphainv*bg
+  float* rgbk;     // [N,3] clamp(sum w*sigmoid(klogit) + alphainv*bg, 0, 1) (if klogit)
+  float* rgbk_raw; // [N,3] before the clamp
+  // optional render extras
+  const float* normal2;  // [S2,3] or null
+  const int* step2;
+  float dist;
+  float* normal_out;     // [N,3]
+  float* depth_out;      // [N]
+  float* wsum_out;       // [N]
+};
+
+__global__ void __launch_bounds__(256) composite_fine_kernel(CompositeParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const int64_t b = P.s2_off[r], e = P.s2_off[r + 1];
+  float a0[3] = {0.f, 0.f, 0.f}, ak[3] = {0.f, 0.f, 0.f}, an[3] = {0.f, 0.f, 0.f};
+  float dep = 0.f, ws = 0.f;
+  for (int64_t i = b + lane; i < e; i += 32) {
+    const float w = P.w2[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      a0[c] += w * sigmoidf_(P.logit[3 * i + c]);
+      if (P.klogit) ak[c] += w * sigmoidf_(P.klogit[3 * i + c]);
+    }
+    ws += w;
+    if (P.normal2) {
+      const float nx = P.normal2[3 * i], ny = P.normal2[3 * i + 1], nz = P.normal2[3 * i + 2];
+      const float inv = 1.f / (sqrtf(nx * nx + ny * ny + nz * nz) + 1e-6f);
+      an[0] += w * nx * inv;
+      an[1] += w * ny * inv;
+      an[2] += w * nz * inv;
+    }
+    if (P.depth_out) dep += w * ((float)P.step2[i] * P.dist);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    a0[c] = warp_sum(a0[c]);
+    ak[c] = warp_sum(ak[c]);
+    an[c] = warp_sum(an[c]);
+  }
+  dep = warp_sum(dep);
+  ws = warp_sum(ws);
+  if (lane == 0) {
+    const float bgt = P.alphainv_last[r] * P.bg;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      P.rgb0[3 * r + c] = a0[c] + bgt;
+      if (P.klogit) {
+        const float raw = ak[c] + bgt;
+        P.rgbk_raw[3 * r + c] = raw;
+        P.rgbk[3 * r + c] = fminf(fmaxf(raw, 0.f), 1.f);
+      }
+      if (P.normal_out) P.normal_out[3 * r + c] = an[c];
+    }
+    if (P.depth_out) P.depth_out[r] = dep;
+    if (P.wsum_out) P.wsum_out[r] = ws;
+  }
+}
+
+struct CompositeBwdParams {
+  int n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;
+  const float* klogit;
+  const float* rgbk_raw;
+  const float* g_rgb0;  // [N,3] or null
+  const float* g_rgbk;  // [N,3] or null
+  float bg;
+  const float* g_last_in;  // [N] extra grad of alphainv_last (e.g. entropy) or null
+  float* d_logit;   // [S2,3]
+  float* d_klogit;  // [S2,3] or null
+  float* d_w2;      // [S2]
+  float* d_last;    // [N]
+};
+
+__global__ void __launch_bounds__(256) composite_fine_bwd_kernel(CompositeBwdParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  float g0[3] = {0.f, 0.f, 0.f}, gk[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (P.g_rgb0) g0[c] = P.g_rgb0[3 * r + c];
+    if (P.g_rgbk && P.klogit) {
+      const float raw = P.rgbk_raw[3 * r + c];
+      gk[c] = (raw >= 0.f && raw <= 1.f) ? P.g_rgbk[3 * r + c] : 0.f;  // clamp backward
+    }
+  }
+  const int64_t b = P.s2_off[r], e = P.s2_off[r + 1];
+  for (int64_t i = b + lane; i < e; i += 32) {
+    const float w = P.w2[i];
+    float dw = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float y0 = sigmoidf_(P.logit[3 * i + c]);
+      P.d_logit[3 * i + c] = (w * g0[c]) * (1.f - y0) * y0;
+      dw += g0[c] * y0;
+      if (P.klogit) {
+        const float yk = sigmoidf_(P.klogit[3 * i + c]);
+        P.d_klogit[3 * i + c] = (w * gk[c]) * (1.f - yk) * yk;
+        dw += gk[c] * yk;
+      }
+    }
+    P.d_w2[i] = dw;
+  }
+  if (lane == 0) {
+    float dl = P.bg * (g0[0] + g0[1] + g0[2] + gk[0] + gk[1] + gk[2]);
+    if (P.g_last_in) dl += P.g_last_in[r];
+    P.d_last[r] = dl;
+  }
+}
+
+// ---- backward: features of shaded rows -> dense gradient grids ---------------
+struct FeatBwdParams {
+  int64_t n_rows;
+  const float* pts2;
+  GridGeom g;
+  const float* sdf;  // smoothed (recompute)
+  float voxel_size;
+  int K;
+  float disp[MAX_K];
+  int k_unit;
+  int pos_pe, view_pe, kpos_pe, kview_pe;
+  int center_sdf, use_rgbnet_k0, k_center_sdf;
+  int ld1, ld2;
+  const void* dX1;
+  const void* dX2;
+  int in_bf16;
+  const float* dw2;      // [S2] weight grads (scattered to slots)
+  const int* slot2;
+  float* dw_slot;
+  float* d_sdf;          // [X,Y,Z] grad of the smoothed grid
+  float* d_k0;           // [X,Y,Z,12] channel-last
+};
+
+template <typename T>
+__device__ __forceinline__ float get(const T* row, int c);
+template <>
+__device__ __forceinline__ float get<float>(const float* row, int c) { return row[c]; }
+template <>
+__device__ __forceinline__ float get<__nv_bfloat16>(const __nv_bfloat16* row, int c) {
+  return __bfloat162float(row[c]);
+}
+
+__device__ __forceinline__ void scatter_probe_axis(float* __restrict__ dgrid, const GridGeom& g, const float ind[3],
+                                                   int axis, float d, float dfm, float dfp) {
+  float im[3] = {ind[0], ind[1], ind[2]};
+  float ip[3] = {ind[0], ind[1], ind[2]};
+  const float hi = (float)(gsize(g, axis) - 1);
+  im[axis] = fminf(fmaxf(ind[axis] - d, 0.f), hi);
+  ip[axis] = fminf(fmaxf(ind[axis] + d, 0.f), hi);
+  if (dfm != 0.f) scatter1(dgrid, corners_of(g, im[0], im[1], im[2]), dfm);
+  if (dfp != 0.f) scatter1(dgrid, corners_of(g, ip[0], ip[1], ip[2]), dfp);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) features_fine_bwd_kernel(FeatBwdParams P) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= P.n_rows) return;
+  P.dw_slot[P.slot2[row]] = P.dw2[row];
+  const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
+  float ind[3];
+  to_index(P.g, p, ind);
+  const T* dx1 = reinterpret_cast<const T*>(P.dX1) + row * P.ld1;
+  const T* dx2 = reinterpret_cast<const T*>(P.dX2) + row * P.ld2;
+  // column layout (must mirror features_fine_kernel)
+  int c1 = (P.use_rgbnet_k0 ? 12 : 0) + (3 + 6 * P.pos_pe) + (3 + 6 * P.view_pe);
+  float d_center = 0.f;
+  if (P.center_sdf) d_center += get(dx1, c1++);
+  const int feat_col = c1;
+  const int grad_col = c1 + 6 * P.K;
+  int c2 = 12 + (3 + 6 * P.kpos_pe) + (3 + 6 * P.kview_pe);
+  const float dgx = get(dx2, c2), dgy = get(dx2, c2 + 1), dgz = get(dx2, c2 + 2);
+  c2 += 3;
+  if (P.k_center_sdf) d_center += get(dx2, c2++);
+  // centre value and k0 share the same corners
+  const Corners cc = corners_of(P.g, ind[0], ind[1], ind[2]);
+  if (d_center != 0.f) scatter1(P.d_sdf, cc, d_center);
+  float dk0[12];
+#pragma unroll
+  for (int ch = 0; ch < 12; ++ch) dk0[ch] = get(dx2, ch);
+  if (P.use_rgbnet_k0)
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) dk0[ch] += get(dx1, ch);
+  scatterC<12>(P.d_k0, cc, dk0);
+  // hierarchical probes
+  for (int kk = 0; kk < P.K; ++kk) {
+    float fm[3], fp[3], invd[3], gr[3];
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) {
+      Probe pr;
+      probe_axis(P.sdf, P.g, ind, 2 - pair, P.disp[kk], pr, false);
+      fm[pair] = pr.fm;
+      fp[pair] = pr.fp;
+      invd[pair] = pr.inv_diff;
+      gr[pair] = ((pr.fp - pr.fm) * pr.inv_diff) / P.voxel_size;
+    }
+    // d of the normalised gradient: n = g / (|g| + eps)
+    const float sn = sqrtf(gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
+    const float den = sn + 1e-5f;
+    float dn[3], dg[3];
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) dn[pair] = get(dx1, grad_col + pair * P.K + kk);
+    const float gdn = gr[0] * dn[0] + gr[1] * dn[1] + gr[2] * dn[2];
+    const float corr = sn > 0.f ? gdn / (sn * den * den) : 0.f;
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) dg[pair] = dn[pair] / den - gr[pair] * corr;
+    if (kk == P.k_unit) {
+      dg[0] += dgz;  // pairs are z, y, x
+      dg[1] += dgy;
+      dg[2] += dgx;
+    }
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) {
+      const float dfd = dg[pair] * invd[pair] / P.voxel_size;  // d(fp - fm)
+      const float dfm = get(dx1, feat_col + (2 * pair + 0) * P.K + kk) - dfd;
+      const float dfp = get(dx1, feat_col + (2 * pair + 1) * P.K + kk) + dfd;
+      scatter_probe_axis(P.d_sdf, P.g, ind, 2 - pair, P.disp[kk], dfm, dfp);
+    }
+  }
+}
+
+// ---- backward: transmittance scan + NeuS alpha, per ray ----------------------
+struct GeomBwdParams {
+  const float* rays_o;
+  const float* rays_d;
+  const float* viewdirs;
+  int n_rays;
+  float near, stepdist;
+  float bmin[3], bmax[3];
+  GridGeom g;
+  const float* sdf;
+  float voxel_size;
+  float inv_s, dist;
+  int max_steps;
+  const float4* rec;
+  const float* dw_slot;
+  const int* n1;
+  const float* alphainv_last;
+  const float* d_last;
+  float* d_sdf;
+};
+
+__global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const int n = P.n1[r];
+  if (n == 0) return;
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  const int64_t slot0 = (int64_t)r * P.max_steps;
+  double carry = (double)(P.d_last[r] * P.alphainv_last[r]);
+  for (int top = n; top > 0; top -= 32) {
+    const int j = top - 32 + lane;
+    const bool valid = j >= 0;
+    float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float gw = 0.f;
+    if (valid) {
+      rc = P.rec[slot0 + j];
+      gw = P.dw_slot[slot0 + j];
+    }
+    const float alpha = rc.y, T = rc.z, w = rc.w;
+    const double term = valid ? (double)(gw * w) : 0.0;
+    const double suffix = warp_inclusive_suffix_sum(term);
+    double after = __shfl_down_sync(0xffffffffu, suffix, 1);
+    if (lane == 31) after = 0.0;
+    const double back = carry + after;
+    carry += __shfl_sync(0xffffffffu, suffix, 0);
+    if (!valid) continue;
+    const float d_alpha = (float)((double)(gw * T) - back / ((double)(1.f - alpha) + 1e-10));
+    if (d_alpha == 0.f) continue;
+    const int k = (int)(__float_as_uint(rc.x) & 0x7fffffffu);
+    float p[3], ind[3], s, gr[3];
+    sample_point(f, P.stepdist, k, p);
+    to_index(P.g, p, ind);
+    sdf_and_grad(P.sdf, P.g, P.voxel_size, ind, &s, gr);
+    const AlphaState a = neus_alpha(s, gr, v, P.inv_s, P.dist);
+    if (!(a.raw >= 0.f && a.raw <= 1.f)) continue;  // clip backward
+    const float den = a.P + 1e-5f;
+    const float dP = d_alpha * a.Q / (den * den);
+    const float dQ = -d_alpha / den;
+    const float d_prev = dP * a.P * (1.f - a.P) * P.inv_s;
+    const float d_next = dQ * a.Q * (1.f - a.Q) * P.inv_s;
+    const float d_s = d_prev + d_next;
+    const float d_ic = (d_next - d_prev) * P.dist * 0.5f;
+    const float d_cos = a.cosv < 0.f ? d_ic : 0.f;
+    scatter1(P.d_sdf, corners_of(P.g, ind[0], ind[1], ind[2]), d_s);
+#pragma unroll
+    for (int axis = 0; axis < 3; ++axis) {
+      const float dg = d_cos * v[axis];
+      if (dg == 0.f) continue;
+      float im[3] = {ind[0], ind[1], ind[2]}, ip[3] = {ind[0], ind[1], ind[2]};
+      const float hi = (float)(gsize(P.g, axis) - 1);
+      im[axis] = fminf(fmaxf(ind[axis] - 1.f, 0.f), hi);
+      ip[axis] = fminf(fmaxf(ind[axis] + 1.f, 0.f), hi);
+      const float dfd = dg / (ip[axis] - im[axis]) / P.voxel_size;
+      scatter1(P.d_sdf, corners_of(P.g, ip[0], ip[1], ip[2]), dfd);
+      scatter1(P.d_sdf, corners_of(P.g, im[0], im[1], im[2]), -dfd);
+    }
+  }
+}
+
+inline unsigned warp_blocks(int64_t n_items, int warps_per_block = 8) {
+  return (unsigned)((n_items + warps_per_block - 1) / warps_per_block);
+}
+
+// ---- generic DenseGrid.forward (lib/grid.py:47-58) and its adjoint ------------
+__global__ void grid_sample_kernel(const float* __restrict__ grid, int C, int channel_last, GridGeom g,
+                                   const float* __restrict__ xyz, int64_t n, float* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  float ind[3];
+  to_index(g, p, ind);
+  const Corners c = corners_of(g, ind[0], ind[1], ind[2]);
+  const int64_t vox = (int64_t)g.X * g.Y * g.Z;
+  for (int ch = 0; ch < C; ++ch) {
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (c.off[q] < 0) continue;
+      const int64_t o = channel_last ? (int64_t)c.off[q] * C + ch : (int64_t)ch * vox + c.off[q];
+      acc += c.w[q] * __ldg(grid + o);
+    }
+    out[i * C + ch] = acc;
+  }
+}
+
+__global__ void grid_sample_bwd_kernel(const float* __restrict__ grad_out, int C, int channel_last, GridGeom g,
+                                       const float* __restrict__ xyz, int64_t n, float* __restrict__ grad_grid) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  float ind[3];
+  to_index(g, p, ind);
+  const Corners c = corners_of(g, ind[0], ind[1], ind[2]);
+  const int64_t vox = (int64_t)g.X * g.Y * g.Z;
+  for (int ch = 0; ch < C; ++ch) {
+    const float d = grad_out[i * C + ch];
+    if (d == 0.f) continue;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (c.off[q] < 0 || c.w[q] == 0.f) continue;
+      const int64_t o = channel_last ? (int64_t)c.off[q] * C + ch : (int64_t)ch * vox + c.off[q];
+      atomicAdd(grad_grid + o, c.w[q] * d);
+    }
+  }
+}
+
+}  // namespace vx
+
+using namespace vx;
+
+// The C ABI below takes the parameter structs declared in voxurf_gb300.h;
+// they mirror the device structs field by field.
+extern "C" {
+
+static GridGeom geom_from(const vx_grid_geom* gg) {
+  GridGeom g;
+  g.X = (int)gg->X;
+  g.Y = (int)gg->Y;
+  g.Z = (int)gg->Z;
+  for (int a = 0; a < 3; ++a) {
+    g.mn[a] = gg->xyz_min[a];
+    g.mx[a] = gg->xyz_max[a];
+  }
+  return g;
+}
+
+int vx_grid_sample(const float* grid, int64_t C, int channel_last, const vx_grid_geom* geom, const float* xyz,
+                   int64_t n_pts, float* out, void* stream) {
+  if (!geom || C <= 0 || n_pts < 0) return VX_ERR_ARG;
+  if (n_pts == 0) return VX_OK;
+  if (!grid || !xyz || !out) return VX_ERR_ARG;
+  if (geom->X * geom->Y * geom->Z > INT32_MAX) return VX_ERR_ARG;
+  grid_sample_kernel<<<grid_for(n_pts, 128), 128, 0, as_stream(stream)>>>(grid, (int)C, channel_last,
+                                                                         geom_from(geom), xyz, n_pts, out);
+  return launch_status();
+}
+
+int vx_grid_sample_backward(const float* grad_out, int64_t C, int channel_last, const vx_grid_geom* geom,
+                            const float* xyz, int64_t n_pts, float* grad_grid, void* stream) {
+  if (!geom || C <= 0 || n_pts < 0) return VX_ERR_ARG;
+  if (n_pts == 0) return VX_OK;
+  if (!grad_out || !xyz || !grad_grid) return VX_ERR_ARG;
+  if (geom->X * geom->Y * geom->Z > INT32_MAX) return VX_ERR_ARG;
+  grid_sample_bwd_kernel<<<grid_for(n_pts, 128), 128, 0, as_stream(stream)>>>(grad_out, (int)C, channel_last,
+                                                                             geom_from(geom), xyz, n_pts, grad_grid);
+  return launch_status();
+}
+
+int vx_fine_march(const vx_fine_march_args* A, void* stream) {
+  if (!A || A->n_rays < 0 || A->max_steps <= 0) return VX_ERR_ARG;
+  if (A->n_rays == 0) return VX_OK;
+  if (!A->rays_o || !A->rays_d || !A->viewdirs || !A->sdf_smooth || !A->rec || !A->dw_slot || !A->n1 || !A->n2 ||
+      !A->alphainv_last)
+    return VX_ERR_ARG;
+  if ((int64_t)A->n_rays * A->max_steps > INT32_MAX) return VX_ERR_ARG;
+  MarchParams P;
+  P.rays_o = A->rays_o;
+  P.rays_d = A->rays_d;
+  P.viewdirs = A->viewdirs;
+  P.n_rays = (int)A->n_rays;
+  P.near = A->near;
+  P.stepdist = A->stepdist;
+  for (int a = 0; a < 3; ++a) {
+    P.bmin[a] = A->grid.xyz_min[a];
+    P.bmax[a] = A->grid.xyz_max[a];
+  }
+  P.g = geom_from(&A->grid);
+  P.sdf = A->sdf_smooth;
+  P.voxel_size = A->voxel_size;
+  P.mask = A->mask;
+  P.mX = (int)A->mask_X;
+  P.mY = (int)A->mask_Y;
+  P.mZ = (int)A->mask_Z;
+  for (int a = 0; a < 3; ++a) {
+    P.mscale[a] = A->mask_scale[a];
+    P.mshift[a] = A->mask_shift[a];
+  }
+  P.inv_s = A->inv_s;
+  P.dist = A->dist;
+  P.thres = A->fast_color_thres;
+  P.max_steps = (int)A->max_steps;
+  P.rec = reinterpret_cast<float4*>(A->rec);
+  P.dw_slot = A->dw_slot;
+  P.n1 = A->n1;
+  P.n2 = A->n2;
+  P.alphainv_last = A->alphainv_last;
+  P.err = device_error_ptr();
+  march_fine_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_fine_compact(const vx_fine_compact_args* A, void* stream) {
+  if (!A || A->n_rays < 0) return VX_ERR_ARG;
+  if (A->n_rays == 0) return VX_OK;
+  CompactParams P;
+  P.rays_o = A->rays_o;
+  P.rays_d = A->rays_d;
+  P.n_rays = (int)A->n_rays;
+  P.near = A->near;
+  P.stepdist = A->stepdist;
+  for (int a = 0; a < 3; ++a) {
+    P.bmin[a] = A->xyz_min[a];
+    P.bmax[a] = A->xyz_max[a];
+  }
+  P.max_steps = (int)A->max_steps;
+  P.rec = reinterpret_cast<const float4*>(A->rec);
+  P.n1 = A->n1;
+  P.s2_off = A->s2_off;
+  P.ray2 = A->ray2;
+  P.step2 = A->step2;
+  P.slot2 = A->slot2;
+  P.w2 = A->w2;
+  P.alpha2 = A->alpha2;
+  P.pts2 = A->pts2;
+  compact_fine_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+static int fill_feat_common(const vx_fine_feature_cfg* c, int& K, float* disp, int& k_unit) {
+  K = (int)c->K;
+  if (K < 1 || K > MAX_K) return VX_ERR_ARG;
+  k_unit = -1;
+  for (int i = 0; i < K; ++i) {
+    disp[i] = c->disp[i];
+    if (c->disp[i] == 1.0f) k_unit = i;
+  }
+  if (k_unit < 0) return VX_ERR_ARG;  // k_grad_feat = (1.0,) must be among the displacements
+  if (c->k0_channels != 12) return VX_ERR_UNSUPPORTED;
+  if (c->posbase_pe < 0 || c->posbase_pe > 16 || c->viewbase_pe < 0 || c->viewbase_pe > 16 ||
+      c->k_posbase_pe < 0 || c->k_posbase_pe > 16 || c->k_viewbase_pe < 0 || c->k_viewbase_pe > 16)
+    return VX_ERR_ARG;
+  return VX_OK;
+}
+
+// Column counts the feature kernels write (must equal the row strides).
+static int64_t x1_cols(const vx_fine_feature_cfg* c) {
+  return (c->use_rgbnet_k0 ? 12 : 0) + (3 + 6 * c->posbase_pe) + (3 + 6 * c->viewbase_pe) + (c->center_sdf ? 1 : 0) +
+         9 * c->K;
+}
+static int64_t x2_cols(const vx_fine_feature_cfg* c) {
+  return 12 + (3 + 6 * c->k_posbase_pe) + (3 + 6 * c->k_viewbase_pe) + 3 + (c->k_center_sdf ? 1 : 0);
+}
+
+int vx_fine_features(const vx_fine_features_args* A, void* stream) {
+  if (!A || A->n_rows < 0) return VX_ERR_ARG;
+  if (A->n_rows == 0) return VX_OK;
+  FeatParams P;
+  int s = fill_feat_common(&A->cfg, P.K, P.disp, P.k_unit);
+  if (s) return s;
+  if ((!A->k0_f32 && !A->k0_bf16) || !A->sdf_smooth || !A->X1 || !A->X2) return VX_ERR_ARG;
+  if (A->ld1 != x1_cols(&A->cfg) || A->ld2 != x2_cols(&A->cfg)) return VX_ERR_ARG;
+  P.n_rows = A->n_rows;
+  P.ray2 = A->ray2;
+  P.pts2 = A->pts2;
+  P.viewdirs = A->viewdirs;
+  P.g = geom_from(&A->grid);
+  P.sdf = A->sdf_smooth;
+  P.voxel_size = A->voxel_size;
+  P.k0f = A->k0_f32;
+  P.k0h = reinterpret_cast<const __nv_bfloat16*>(A->k0_bf16);
+  P.pos_pe = (int)A->cfg.posbase_pe;
+  P.view_pe = (int)A->cfg.viewbase_pe;
+  P.kpos_pe = (int)A->cfg.k_posbase_pe;
+  P.kview_pe = (int)A->cfg.k_viewbase_pe;
+  P.center_sdf = A->cfg.center_sdf;
+  P.use_rgbnet_k0 = A->cfg.use_rgbnet_k0;
+  P.k_center_sdf = A->cfg.k_center_sdf;
+  P.ld1 = (int)A->ld1;
+  P.ld2 = (int)A->ld2;
+  P.X1 = A->X1;
+  P.X2 = A->X2;
+  P.out_bf16 = A->out_bf16;
+  P.normal_out = A->normal_out;
+  const unsigned b = (unsigned)((A->n_rows + 127) / 128);
+  if (A->out_bf16)
+    features_fine_kernel<__nv_bfloat16><<<b, 128, 0, as_stream(stream)>>>(P);
+  else
+    features_fine_kernel<float><<<b, 128, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_fine_composite(const vx_fine_composite_args* A, void* stream) {
+  if (!A || A->n_rays < 0) return VX_ERR_ARG;
+  if (A->n_rays == 0) return VX_OK;
+  CompositeParams P;
+  P.n_rays = (int)A->n_rays;
+  P.s2_off = A->s2_off;
+  P.w2 = A->w2;
+  P.logit = A->logit;
+  P.klogit = A->klogit;
+  P.alphainv_last = A->alphainv_last;
+  P.bg = A->bg;
+  P.rgb0 = A->rgb0;
+  P.rgbk = A->rgbk;
+  P.rgbk_raw = A->rgbk_raw;
+  P.normal2 = A->normal2;
+  P.step2 = A->step2;
+  P.dist = A->dist;
+  P.normal_out = A->normal_out;
+  P.depth_out = A->depth_out;
+  P.wsum_out = A->wsum_out;
+  composite_fine_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_fine_composite_backward(const vx_fine_composite_bwd_args* A, void* stream) {
+  if (!A || A->n_rays < 0) return VX_ERR_ARG;
+  if (A->n_rays == 0) return VX_OK;
+  CompositeBwdParams P;
+  P.n_rays = (int)A->n_rays;
+  P.s2_off = A->s2_off;
+  P.w2 = A->w2;
+  P.logit = A->logit;
+  P.klogit = A->klogit;
+  P.rgbk_raw = A->rgbk_raw;
+  P.g_rgb0 = A->g_rgb0;
+  P.g_rgbk = A->g_rgbk;
+  P.bg = A->bg;
+  P.g_last_in = A->g_last_in;
+  P.d_logit = A->d_logit;
+  P.d_klogit = A->d_klogit;
+  P.d_w2 = A->d_w2;
+  P.d_last = A->d_last;
+  composite_fine_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_fine_backward(const vx_fine_backward_args* A, void* stream) {
+  if (!A || A->n_rays < 0 || A->n_rows < 0) return VX_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  if (A->n_rows > 0) {
+    FeatBwdParams F;
+    int s = fill_feat_common(&A->cfg, F.K, F.disp, F.k_unit);
+    if (s) return s;
+    if (A->ld1 != x1_cols(&A->cfg) || A->ld2 != x2_cols(&A->cfg)) return VX_ERR_ARG;
+    F.n_rows = A->n_rows;
+    F.pts2 = A->pts2;
+    F.g = geom_from(&A->grid);
+    F.sdf = A->sdf_smooth;
+    F.voxel_size = A->voxel_size;
+    F.pos_pe = (int)A->cfg.posbase_pe;
+    F.view_pe = (int)A->cfg.viewbase_pe;
+    F.kpos_pe = (int)A->cfg.k_posbase_pe;
+    F.kview_pe = (int)A->cfg.k_viewbase_pe;
+    F.center_sdf = A->cfg.center_sdf;
+    F.use_rgbnet_k0 = A->cfg.use_rgbnet_k0;
+    F.k_center_sdf = A->cfg.k_center_sdf;
+    F.ld1 = (int)A->ld1;
+    F.ld2 = (int)A->ld2;
+    F.dX1 = A->dX1;
+    F.dX2 = A->dX2;
+    F.in_bf16 = A->in_bf16;
+    F.dw2 = A->dw2;
+    F.slot2 = A->slot2;
+    F.dw_slot = A->dw_slot;
+    F.d_sdf = A->d_sdf_smooth;
+    F.d_k0 = A->d_k0;
+    const unsigned b = (unsigned)((A->n_rows + 127) / 128);
+    if (A->in_bf16)
+      features_fine_bwd_kernel<__nv_bfloat16><<<b, 128, 0, st>>>(F);
+    else
+      features_fine_bwd_kernel<float><<<b, 128, 0, st>>>(F);
+    s = launch_status();
+    if (s) return s;
+  }
+  if (A->n_rays == 0) return VX_OK;
+  GeomBwdParams G;
+  G.rays_o = A->rays_o;
+  G.rays_d = A->rays_d;
+  G.viewdirs = A->viewdirs;
+  G.n_rays = (int)A->n_rays;
+  G.near = A->near;
+  G.stepdist = A->stepdist;
+  for (int a = 0; a < 3; ++a) {
+    G.bmin[a] = A->grid.xyz_min[a];
+    G.bmax[a] = A->grid.xyz_max[a];
+  }
+  G.g = geom_from(&A->grid);
+  G.sdf = A->sdf_smooth;
+  G.voxel_size = A->voxel_size;
+  G.inv_s = A->inv_s;
+  G.dist = A->dist;
+  G.max_steps = (int)A->max_steps;
+  G.rec = reinterpret_cast<const float4*>(A->rec);
+  G.dw_slot = A->dw_slot;
+  G.n1 = A->n1;
+  G.alphainv_last = A->alphainv_last;
+  G.d_last = A->d_last;
+  G.d_sdf = A->d_sdf_smooth;
+  geometry_fine_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, st>>>(G);
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,172 @@
+"""Host-side mirror of lib/grid.py: DenseGrid and MaskGrid.
+
+Same constructor arguments, attribute names (``grid``, ``xyz_min``,
+``xyz_max``, ``mask``, ``xyz2ijk_scale``, ``xyz2ijk_shift``), methods and
+state_dict keys/shapes as the reference, so checkpoints move between the two.
+Differences by design:
+  * multi-channel grids are kept in ``torch.channels_last_3d`` memory format:
+    the logical shape stays [1, C, X, Y, Z] but the storage is [X, Y, Z, C],
+    so one trilinear corner is one contiguous C-vector;
+  * ``forward`` runs the sm_103a trilinear kernel (F.grid_sample semantics,
+    align_corners=True, zero padding) with a hand-written backward;
+  * ``total_variation_add_grad`` runs the TV kernel directly on either layout.
+"""
+from __future__ import annotations
+
+import torch
+import torch.nn as nn
+import torch.nn.functional as F
+
+from . import _abi, render_utils_cuda
+from ._torch import call, ptr, stream_ptr
+
+
+def create_grid(type, **kwargs):
+    if type == "DenseGrid":
+        return DenseGrid(**kwargs)
+    raise NotImplementedError(f"{type} is not part of this build (the Voxurf models only create DenseGrid)")
+
+
+def grid_geom(world_size, xyz_min, xyz_max) -> _abi.GridGeom:
+    g = _abi.GridGeom()
+    g.X, g.Y, g.Z = (int(s) for s in world_size)
+    for a in range(3):
+        g.xyz_min[a] = float(xyz_min[a])
+        g.xyz_max[a] = float(xyz_max[a])
+    return g
+
+
+class _GridSample(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, grid, xyz, geom, channel_last):
+        C = grid.size(1)
+        n = xyz.size(0)
+        out = torch.empty((n, C), dtype=torch.float32, device=xyz.device)
+        _abi.grid_sample("vx_grid_sample", ptr(grid), C, channel_last, geom, ptr(xyz), n, ptr(out), stream_ptr())
+        ctx.save_for_backward(xyz)
+        ctx.geom, ctx.channel_last, ctx.grid_like = geom, channel_last, grid
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (xyz,) = ctx.saved_tensors
+        grid = ctx.grid_like
+        g = torch.zeros_like(grid)  # preserves the channels_last_3d layout
+        grad_out = grad_out.contiguous()
+        _abi.grid_sample("vx_grid_sample_backward", ptr(grad_out), grid.size(1), ctx.channel_last, ctx.geom, ptr(xyz),
+                         xyz.size(0), ptr(g), stream_ptr())
+        return g, None, None, None
+
+
+def _is_channel_last(t: torch.Tensor) -> bool:
+    return t.size(1) > 1 and t.is_contiguous(memory_format=torch.channels_last_3d) and not t.is_contiguous()
+
+
+class DenseGrid(nn.Module):
+    """lib/grid.py:38-89."""
+
+    def __init__(self, channels, world_size, xyz_min, xyz_max, channel_last: bool = True, **kwargs):
+        super().__init__()
+        self.channels = channels
+        self.world_size = world_size
+        self.channel_last = bool(channel_last) and channels > 1
+        self.register_buffer("xyz_min", torch.as_tensor(xyz_min, dtype=torch.float32).clone())
+        self.register_buffer("xyz_max", torch.as_tensor(xyz_max, dtype=torch.float32).clone())
+        self.grid = nn.Parameter(self._layout(torch.zeros([1, channels, *[int(s) for s in world_size]])))
+
+    def _layout(self, t: torch.Tensor) -> torch.Tensor:
+        if self.channel_last:
+            return t.contiguous(memory_format=torch.channels_last_3d)
+        return t.contiguous()
+
+    def _load_from_state_dict(self, state_dict, prefix, *args, **kwargs):
+        # checkpoints store [1,C,X,Y,Z] in either layout; keep ours
+        key = prefix + "grid"
+        if key in state_dict:
+            state_dict[key] = self._layout(state_dict[key])
+        super()._load_from_state_dict(state_dict, prefix, *args, **kwargs)
+
+    def geom(self) -> _abi.GridGeom:
+        return grid_geom(self.grid.shape[2:], self.xyz_min.tolist(), self.xyz_max.tolist())
+
+    def forward(self, xyz):
+        shape = xyz.shape[:-1]
+        pts = xyz.reshape(-1, 3).contiguous().float()
+        out = _GridSample.apply(self.grid, pts, self.geom(), _is_channel_last(self.grid))
+        out = out.reshape(*shape, self.channels)
+        if self.channels == 1:
+            out = out.squeeze(-1)
+        return out
+
+    def scale_volume_grid(self, new_world_size):
+        if self.channels == 0:
+            self.grid = nn.Parameter(torch.zeros([1, self.channels, *new_world_size]))
+        else:
+            self.grid = nn.Parameter(self._layout(
+                F.interpolate(self.grid.data.contiguous(), size=tuple(int(s) for s in new_world_size),
+                              mode="trilinear", align_corners=True)))
+
+    def total_variation_add_grad(self, wx, wy, wz, dense_mode, mask=None):
+        """In place on grid.grad (lib/grid.py:67-78)."""
+        g = self.grid
+        if g.grad is None:
+            g.grad = torch.zeros_like(g)
+        cl = _is_channel_last(g)
+        C, X, Y, Z = g.size(1), g.size(2), g.size(3), g.size(4)
+        if mask is None:
+            call("vx_total_variation_add_grad", ptr(g), ptr(g.grad), float(wx), float(wy), float(wz),
+                 int(bool(dense_mode)), C, X, Y, Z, int(cl), stream_ptr())
+        else:
+            mask = mask.detach()
+            if C > 1 and mask.size() != g.size():
+                mask = mask.repeat(1, C, 1, 1, 1)
+            assert mask.size() == g.size()
+            mask = mask.float().contiguous(memory_format=torch.channels_last_3d if cl else torch.contiguous_format)
+            call("vx_total_variation_add_grad_new", ptr(g), ptr(g.grad), ptr(mask), float(wx), float(wy), float(wz),
+                 int(bool(dense_mode)), C, X, Y, Z, int(cl), stream_ptr())
+
+    def get_dense_grid(self):
+        return self.grid
+
+    @torch.no_grad()
+    def __isub__(self, val):
+        self.grid.data -= val
+        return self
+
+    def extra_repr(self):
+        ws = self.world_size.tolist() if hasattr(self.world_size, "tolist") else list(self.world_size)
+        return f"channels={self.channels}, world_size={ws}"
+
+
+class MaskGrid(nn.Module):
+    """lib/grid.py:212-245: nearest-voxel lookup of known free space."""
+
+    def __init__(self, path=None, mask_cache_thres=None, mask=None, xyz_min=None, xyz_max=None):
+        super().__init__()
+        if path is not None:
+            st = torch.load(path, map_location="cpu")
+            self.mask_cache_thres = mask_cache_thres
+            density = F.max_pool3d(st["model_state_dict"]["density.grid"], kernel_size=3, padding=1, stride=1)
+            alpha = 1 - torch.exp(-F.softplus(density + st["model_state_dict"]["act_shift"]) *
+                                  st["model_kwargs"]["voxel_size_ratio"])
+            mask = (alpha >= self.mask_cache_thres).squeeze(0).squeeze(0)
+            xyz_min = torch.Tensor(st["model_kwargs"]["xyz_min"])
+            xyz_max = torch.Tensor(st["model_kwargs"]["xyz_max"])
+        else:
+            mask = mask.bool()
+            xyz_min = torch.as_tensor(xyz_min, dtype=torch.float32)
+            xyz_max = torch.as_tensor(xyz_max, dtype=torch.float32)
+        self.register_buffer("mask", mask.contiguous())
+        xyz_len = xyz_max - xyz_min
+        self.register_buffer("xyz2ijk_scale", (torch.Tensor(list(mask.shape)) - 1) / xyz_len)
+        self.register_buffer("xyz2ijk_shift", -xyz_min * self.xyz2ijk_scale)
+
+    @torch.no_grad()
+    def forward(self, xyz):
+        shape = xyz.shape[:-1]
+        xyz = xyz.reshape(-1, 3).contiguous()
+        mask = render_utils_cuda.maskcache_lookup(self.mask, xyz, self.xyz2ijk_scale, self.xyz2ijk_shift)
+        return mask.reshape(shape)
+
+    def extra_repr(self):
+        return f"mask.shape={list(self.mask.shape)}"
