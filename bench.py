@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the Voxurf fine-stage training step on GB300.
+
+Workload (the 256^3 fine configuration): SDF grid 256^3 FP32 (sphere r=0.45
+union torus R=0.6 r=0.15, noise 0.005, seeded), k0 256^3 x 12 ~ N(0,0.1),
+mask |SDF| < 0.05, rgbnet 70->192x3->3 and k_rgbnet 60->192x3->3, Gaussian
+smoothing 5^3 sigma 0.8, stepsize 0.5 voxel, 8192 rays per step drawn from
+49 cameras (1600x1200, f = 1.2 W) on the radius-3 sphere, targets U(0,1).
+One step = forward + loss + hand-written backward + TV (weight 1e-4 on sdf
+and k0) + Adam (lr 1e-3) on both grids and both MLPs.
+
+`value` is train rays/s of the plain FP32 path with ray batches resident in
+HBM; `e2e` is the same step through the public API with each batch copied
+from pinned host memory and the loss read back inside the timed region;
+`fused_bf16` repeats the step with k0 sampled from BF16 and both MLPs in
+BF16 (FP32 accumulation).  The working set (~10 GB of grids and Adam state
+swept every step) is far larger than L2, so no flush is needed.
+
+--impl reference times the reference algorithm on the host CPU (the oracle's
+torch restatement of the reference step, FP32, all host threads) on the
+same workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "train rays/s (fine stage fwd+bwd+TV+Adam, 256^3, 8192 rays/step)"
+UNIT = "rays/s"
+R = 256
+N_RAYS = 8192
+MASK_VOXELS = 6.4  # |SDF| < 0.05 at voxel size 2/256
+
+# Dominant kernel: the fused TV + Adam sweep over the k0 grid.  Algorithmic
+# bytes per element: read p_old, grad, exp_avg, exp_avg_sq (16 B) + write
+# p_new, exp_avg, exp_avg_sq (12 B) = 28 B (TV neighbour reads hit L1/L2).
+K0_ELEMS = R ** 3 * 12
+SWEEP_BYTES_PER_ELEM = 28
+# DRAM traffic of one k0 sweep launch from an ncu capture of this workload's
+# kernel (profiles/grid_tv_adam_k0.md); None until captured.
+SWEEP_NCU_TRAFFIC = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-bf16", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if (torch.cuda.is_available() and args.impl == "ours") else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available() and args.impl == "ours":
+        torch.cuda.set_device(local)
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def make_batches(n_batches, seed=0):
+    import numpy as np
+
+    from voxurf_gb300 import configs, synthetic
+
+    o, d, v = synthetic.random_rays(N_RAYS * n_batches, seed=seed)
+    t = configs.train_targets(N_RAYS * n_batches, seed)
+    return [np.ascontiguousarray(a.reshape(n_batches, N_RAYS, 3)) for a in (o, d, v, t)]
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from voxurf_gb300 import _native, configs
+    from voxurf_gb300.train import FineTrainer
+
+    dev = torch.device("cuda", local)
+    rk = dict(configs.FINE_RENDER_KWARGS)
+    n_b = args.warmup + args.steps
+    host = make_batches(n_b, seed=rank)
+    dev_batches = [torch.from_numpy(a).to(dev) for a in host]
+
+    def build(precision):
+        model = configs.build_fine_model(R, precision, device=dev, seed=0, mask_voxels=MASK_VOXELS)
+        return model, FineTrainer(model, n_rays=N_RAYS)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world > 1:
+            t = torch.tensor([x], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    # ---- plain FP32, device-resident batches ---------------------------------
+    model, tr = build("fp32")
+    sweep_ms = []
+    orig_grid_step = tr.optimizer._grid_step
+
+    def timed_grid_step(p, *a, **k):
+        if p is model.k0.grid and timing["on"]:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            orig_grid_step(p, *a, **k)
+            e1.record()
+            timing["events"].append((e0, e1))
+        else:
+            orig_grid_step(p, *a, **k)
+
+    timing = {"on": False, "events": []}
+    tr.optimizer._grid_step = timed_grid_step
+    for i in range(args.warmup):
+        tr.step(dev_batches[0][i], dev_batches[1][i], dev_batches[2][i], dev_batches[3][i], rk)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    timing["on"] = True
+    l0 = _native.launch_count()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record()
+    for i in range(args.warmup, n_b):
+        tr.step(dev_batches[0][i], dev_batches[1][i], dev_batches[2][i], dev_batches[3][i], rk)
+    e_end.record()
+    barrier()
+    launches = _native.launch_count() - l0
+    timing["on"] = False
+    ms = e_start.elapsed_time(e_end)
+    clk = clocks.stop()
+    sweep_ms = [a.elapsed_time(b) for a, b in timing["events"]]
+    t_total = max_over_ranks(ms / 1000.0)
+    value = world * N_RAYS * args.steps / t_total
+    shaded = int(model._last_frame.S2)
+
+    # ---- e2e: same step, batches from pinned host memory, loss read back -------
+    pinned = [torch.from_numpy(a).pin_memory() for a in host]
+    barrier()
+    w0 = time.perf_counter()
+    e2e_losses = []
+    for i in range(args.warmup, n_b):
+        xs = [p[i].to(dev, non_blocking=True) for p in pinned]
+        loss, _ = tr.step(xs[0], xs[1], xs[2], xs[3], rk)
+        e2e_losses.append(float(loss.item()))
+    barrier()
+    t_e2e = max_over_ranks(time.perf_counter() - w0)
+    e2e = world * N_RAYS * args.steps / t_e2e
+    h2d = sum(p[0].numel() * p[0].element_size() for p in pinned)
+    del tr, model
+    torch.cuda.empty_cache()
+
+    # ---- fused BF16 variant --------------------------------------------------
+    bf16 = None
+    if not args.no_bf16:
+        model, tr = build("bf16")
+        for i in range(args.warmup):
+            tr.step(dev_batches[0][i], dev_batches[1][i], dev_batches[2][i], dev_batches[3][i], rk)
+        barrier()
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record()
+        for i in range(args.warmup, n_b):
+            tr.step(dev_batches[0][i], dev_batches[1][i], dev_batches[2][i], dev_batches[3][i], rk)
+        b1.record()
+        barrier()
+        tb = max_over_ranks(b0.elapsed_time(b1) / 1000.0)
+        bf16 = {"value": world * N_RAYS * args.steps / tb, "unit": UNIT, "ms_per_step": 1000 * tb / args.steps,
+                "speedup_vs_fp32": (world * N_RAYS * args.steps / tb) / value}
+        del tr, model
+        torch.cuda.empty_cache()
+
+    peak, peak_src = measured_peaks()
+    sweep_avg = sum(sweep_ms) / max(len(sweep_ms), 1)
+    alg_bytes = K0_ELEMS * SWEEP_BYTES_PER_ELEM
+    achieved = alg_bytes / (sweep_avg / 1000.0) / 1e9 if sweep_avg > 0 else None
+    roofline = {"kernel": "grid_tv_adam_kernel (k0 TV+Adam sweep)", "bound": "hbm", "achieved": achieved,
+                "peak": peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                else "fallback 6800 GB/s", "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                "bytes_per_launch": alg_bytes, "launch_ms": sweep_avg,
+                "traffic": SWEEP_NCU_TRAFFIC}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_total * 1000 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "voxurf fine stage train step: SDF 256^3 f32 + k0 256^3x12 f32, 8192 rays/step, "
+                                   "stepsize 0.5, mask |SDF|<0.05, MLP 192x4 (x2), TV 1e-4, Adam 1e-3",
+                       "rays_per_step": N_RAYS, "grid": R, "shaded_samples_last_step": shaded,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "no flush: ~10 GB of grids + Adam state swept per step (> 129 MB L2)"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4},
+            "fused_bf16": bf16,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line))
+
+
+def cpu_baseline(seconds_hint=20.0):
+    """The reference step on the host CPU (oracle restatement, FP32, all
+    threads): full steps at 1024 and 4096 rays on the 256^3 grids, fitted
+    t(n) = a + b n and evaluated at 8192 rays (the dense TV/Adam/smoothing
+    work is the constant a)."""
+    import torch
+
+    from oracle.bench_cpu import time_reference_step
+
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    res = time_reference_step(R, [1024, 4096], N_RAYS)
+    return {"value": res["rays_per_s"], "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": res["sample"]}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import torch
+
+    from oracle.bench_cpu import time_reference_step
+
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    res = time_reference_step(R, [1024, 4096], N_RAYS, repeats=max(1, min(args.steps, 2)))
+    v = res["rays_per_s"]
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * N_RAYS / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "voxurf fine stage train step: SDF 256^3 f32 + k0 256^3x12 f32, 8192 rays/step, "
+                               "stepsize 0.5, mask |SDF|<0.05, MLP 192x4 (x2), TV 1e-4, Adam 1e-3",
+                   "rays_per_step": N_RAYS, "grid": R},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": res["sample"]},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

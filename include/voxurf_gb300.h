@@ -43,6 +43,8 @@ int vx_version(void);
 const char* vx_status_string(int status);
 int vx_last_cuda_error(void);
 const char* vx_cuda_error_string(int code);
+/* Number of kernels this library has launched in the process so far. */
+unsigned long long vx_launch_count(void);
 /* Reads and clears the device error word (synchronises `stream`). */
 int vx_device_error(void* stream, int* out_code);
 
@@ -270,6 +272,7 @@ typedef struct {
   float* normal_out;        /* optional [N,3]                                  */
   float* depth_out;         /* optional [N]                                    */
   float* wsum_out;          /* optional [N]                                    */
+  int32_t has_k;            /* 1: the k-branch is used (klogit/rgbk/rgbk_raw)  */
 } vx_fine_composite_args;
 int vx_fine_composite(const vx_fine_composite_args* args, void* stream);
 
@@ -288,6 +291,7 @@ typedef struct {
   float* d_klogit;          /* out [S2,3] */
   float* d_w2;              /* out [S2]   */
   float* d_last;            /* out [N]    */
+  int32_t has_k;            /* 1: the k-branch is used                         */
 } vx_fine_composite_bwd_args;
 int vx_fine_composite_backward(const vx_fine_composite_bwd_args* args, void* stream);
 

@@ -27,12 +27,13 @@ from .ops import Alphas2WeightsOracle, RenderUtilsOracle, tv_add_grad_torch, Tot
 
 
 def gaussian_kernel3d(ksize: int, sigma: float) -> np.ndarray:
-    """Voxurf._gaussian_3dconv weights (voxurf_fine.py:246-258), rounded to
-    float32 as the reference stores them."""
+    """Voxurf._gaussian_3dconv weights (voxurf_fine.py:246-258): the
+    exponentials are cast to the (float32) grid dtype first and normalised
+    by their float32 sum, as the reference does."""
     x = np.arange(-(ksize // 2), ksize // 2 + 1, 1)
     xx, yy, zz = np.meshgrid(x, x, x)
-    k = np.exp(-(xx ** 2 + yy ** 2 + zz ** 2) / (2 * sigma ** 2))
-    return (k / k.sum()).astype(np.float32)
+    k = torch.from_numpy(np.exp(-(xx ** 2 + yy ** 2 + zz ** 2) / (2 * sigma ** 2))).float()
+    return (k / k.sum()).numpy()
 
 
 def smooth3d(grid: torch.Tensor, kernel: torch.Tensor) -> torch.Tensor:

@@ -1,0 +1,211 @@
+"""Generates the golden vectors of tests/golden/ by running the REFERENCE
+Voxurf Python code (lib/voxurf_fine.py, lib/voxurf_coarse.py, lib/grid.py,
+lib/utils.py) on the CPU in float64.
+
+Run in a container that has the reference sources (default path below, or
+$VOXURF_REFERENCE); the GPU machine never runs this.  The reference imports
+several packages that are absent here and JIT-builds CUDA extensions; this
+script stubs them:
+  * cv2, mcubes, matplotlib, plyfile, imageio, skimage, trimesh, lpips ->
+    empty modules (imported, never used on this path);
+  * torch_scatter.segment_coo(src, index, out, reduce='sum') ->
+    out.index_add(0, index, src) (same sum);
+  * torch.utils.cpp_extension.load -> the oracle's restatement of the CUDA
+    ops (oracle/ops.py), since no GPU exists here;
+  * Tensor.cuda / Module.cuda -> no-ops.
+PYTHONDONTWRITEBYTECODE keeps the read-only reference tree clean.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import importlib.abc
+import importlib.machinery
+import os
+import sys
+import types
+
+os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
+sys.dont_write_bytecode = True
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("VOXURF_REFERENCE", "/root/reference")
+sys.path.insert(0, REPO)
+
+from oracle.ops import RenderUtilsOracle, TotalVariationOracle  # noqa: E402
+
+STUBS = ("cv2", "mcubes", "matplotlib", "matplotlib.pyplot", "matplotlib.cm", "plyfile", "imageio", "skimage",
+         "skimage.measure", "trimesh", "lpips", "mmcv")
+
+
+class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
+    def find_spec(self, name, path, target=None):
+        if name in STUBS:
+            return importlib.machinery.ModuleSpec(name, self, is_package=True)
+        return None
+
+    def create_module(self, spec):
+        m = types.ModuleType(spec.name)
+        m.__path__ = []
+
+        def _attr(attr):
+            if attr.startswith("__"):
+                raise AttributeError(attr)
+            return type(attr, (), {})
+
+        m.__getattr__ = _attr
+        return m
+
+    def exec_module(self, module):
+        pass
+
+
+def install_stubs():
+    sys.meta_path.insert(0, _StubFinder())
+    ts = types.ModuleType("torch_scatter")
+
+    def segment_coo(src, index, out=None, reduce="sum"):
+        assert reduce == "sum"
+        return out.to(src.dtype).index_add(0, index, src)
+
+    ts.segment_coo = segment_coo
+    sys.modules["torch_scatter"] = ts
+    import torch.utils.cpp_extension as cpp
+
+    def fake_load(name, sources=None, verbose=False, **kw):
+        if name == "render_utils_cuda":
+            return RenderUtilsOracle
+        if name == "total_variation_cuda":
+            return TotalVariationOracle
+        return types.SimpleNamespace()
+
+    cpp.load = fake_load
+    # like a real .cuda(), a Parameter comes back as a plain tensor (so the
+    # reference's `self.s_val = nn.Parameter(...).cuda()` stays unregistered
+    # and float32 under model.double(), voxurf_fine.py:61)
+    torch.Tensor.cuda = lambda self, *a, **k: self.data if isinstance(self, torch.nn.Parameter) else self
+    torch.nn.Module.cuda = lambda self, *a, **k: self
+    sys.path.insert(0, REF)
+
+
+def _state_from_ours(model):
+    sd = {k: v.detach().cpu().contiguous() for k, v in model.state_dict().items()}
+    return sd
+
+
+def fine_step_fixture(path, R=16, n_rays=128, width=64, mask_voxels=3.0, bg=1, seed=3):
+    """One fine-stage training step of the reference model in float64."""
+    import lib.grid as rgrid
+    import lib.voxurf_fine as rf
+    from voxurf_gb300 import configs, synthetic
+    from voxurf_gb300.grid import MaskGrid
+
+    ours = configs.build_fine_model(R, "fp32", device="cpu", seed=seed, width=width, mask_voxels=None)
+    kw = configs.fine_model_kwargs(R, "fp32", width)
+    kw.pop("precision")
+    ref = rf.Voxurf(**kw)
+    sd = _state_from_ours(ours)
+    missing, unexpected = ref.load_state_dict(sd, strict=False)
+    assert not unexpected, unexpected
+    # mask |SDF| < mask_voxels voxels through the reference's MaskGrid, then the
+    # reference's own non-empty-mask initialisation (voxurf_fine.py:353-367)
+    mask_bool = ref.sdf.grid.detach()[0, 0].abs() < mask_voxels * 2.0 / R
+    ref.mask_cache = rgrid.MaskGrid(mask=mask_bool, xyz_min=kw["xyz_min"], xyz_max=kw["xyz_max"])
+    ref._set_nonempty_mask()
+    sd = {k: v for k, v in ref.state_dict().items()}
+    sd["mask_cache.mask"] = mask_bool
+    ref = ref.double()
+    ro, rd, vd = synthetic.random_rays(n_rays, seed=seed + 11)
+    tgt = configs.train_targets(n_rays, seed)
+    rk = dict(configs.FINE_RENDER_KWARGS, bg=bg)
+    T = lambda a: torch.from_numpy(a).double()
+    ret = ref(T(ro), T(rd), T(vd), global_step=1, **rk)
+    # run.py:604-636 with the fine dtu_e2e weights (main 1, entropy_last 1e-3, rgb0 0.5)
+    target = T(tgt)
+    loss = 1.0 * torch.nn.functional.mse_loss(ret["rgb_marched"], target)
+    pout = ret["alphainv_cum"][..., -1].clamp(1e-6, 1 - 1e-6)
+    loss = loss + 0.001 * (-(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean())
+    loss = loss + torch.nn.functional.mse_loss(ret["rgb_marched0"], target) * 0.5
+    loss.backward()
+    out = {
+        "R": R, "n_rays": n_rays, "width": width, "mask_voxels": mask_voxels, "bg": bg, "seed": seed,
+        "rays_o": ro, "rays_d": rd, "viewdirs": vd, "target": tgt,
+        "rgb_marched": ret["rgb_marched"].detach().numpy(), "rgb_marched0": ret["rgb_marched0"].detach().numpy(),
+        "alphainv_cum": ret["alphainv_cum"].detach().numpy(), "weights": ret["weights"].detach().numpy(),
+        "loss": np.array(loss.item()),
+        "grad_sdf": ref.sdf.grid.grad.numpy(), "grad_k0": ref.k0.grid.grad.numpy(),
+    }
+    for name, p in list(ref.rgbnet.named_parameters()) + [("k." + n, p) for n, p in ref.k_rgbnet.named_parameters()]:
+        out["grad_mlp." + name] = p.grad.numpy()
+    for k, v in sd.items():
+        if v.dtype.is_floating_point:
+            out["state." + k] = v.float().numpy()
+        elif v.dtype == torch.bool:
+            out["state." + k] = v.numpy()
+    np.savez_compressed(path, **out)
+    print("wrote", path, "shaded samples", ret["weights"].numel())
+
+
+def ops_fixture(path, seed=5):
+    """Reference torch code for individual pieces of the path."""
+    import lib.grid as rgrid
+    import lib.utils as rutils
+    import lib.voxurf_fine as rf
+
+    g = torch.Generator().manual_seed(seed)
+    out = {}
+    # (1) cumprod_exclusive / get_ray_marching_ray (voxurf_fine.py:947-954):
+    # weights of rays that never reach T < 1e-3
+    alpha = torch.rand((64, 100), generator=g, dtype=torch.float64) * 0.02
+    w, alphainv_cum = rf.get_ray_marching_ray(alpha)
+    out.update({"march_alpha": alpha.numpy(), "march_weights": w.numpy(), "march_alphainv": alphainv_cum.numpy()})
+    # (2) utils.Adam (utils.py:54-199) incl. per-voxel lr on the first param
+    p0 = torch.randn((4, 5, 6), generator=g)
+    p1 = torch.randn((33,), generator=g)
+    params = [torch.nn.Parameter(p0.clone()), torch.nn.Parameter(p1.clone())]
+    opt = rutils.Adam([{"params": [params[0]], "lr": 1e-2}, {"params": [params[1]], "lr": 3e-3}], betas=(0.9, 0.99))
+    count = torch.randint(1, 9, (4, 5, 6), generator=g)
+    opt.set_pervoxel_lr(count)
+    grads = []
+    for it in range(3):
+        gs = [torch.randn(p.shape, generator=g) * 1e-2 for p in params]
+        grads.append(gs)
+        for p, gg in zip(params, gs):
+            p.grad = gg.clone()
+        opt.step()
+    out.update({"adam_p0": p0.numpy(), "adam_p1": p1.numpy(), "adam_count": count.numpy(),
+                "adam_grads0": np.stack([gs[0].numpy() for gs in grads]),
+                "adam_grads1": np.stack([gs[1].numpy() for gs in grads]),
+                "adam_out0": params[0].detach().numpy(), "adam_out1": params[1].detach().numpy()})
+    # (3) DenseGrid.forward (grid.py:47-58)
+    dg = rgrid.DenseGrid(channels=5, world_size=torch.tensor([7, 9, 11]), xyz_min=[-1.0, -0.5, -2.0],
+                         xyz_max=[1.0, 1.5, 0.5])
+    dg.grid.data = torch.randn((1, 5, 7, 9, 11), generator=g)
+    xyz = torch.rand((500, 3), generator=g) * torch.tensor([2.4, 2.4, 2.9]) + torch.tensor([-1.2, -0.7, -2.2])
+    out.update({"dg_grid": dg.grid.data.numpy(), "dg_xyz": xyz.numpy(), "dg_out": dg(xyz).detach().numpy()})
+    # (4) Gaussian smoothing (voxurf_fine.py:246-258) and the central-difference
+    #     gradient grid (voxurf_fine.py:440-450)
+    sdf = torch.randn((1, 1, 12, 10, 14), generator=g)
+    holder = types.SimpleNamespace(sdf=types.SimpleNamespace(grid=sdf), voxel_size=torch.tensor(0.0625))
+    conv = rf.Voxurf._gaussian_3dconv(holder, ksize=5, sigma=0.8)
+    out.update({"smooth_in": sdf.numpy(), "smooth_out": conv(sdf).detach().numpy()})
+    holder.grad_mode = "interpolate"
+    gradient = rf.Voxurf.neus_sdf_gradient(holder, mode="interpolate", sdf=sdf)
+    out.update({"sdfgrad_out": gradient.numpy(), "sdfgrad_voxel": np.array(0.0625)})
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
+def main():
+    install_stubs()
+    torch.set_default_dtype(torch.float32)
+    ops_fixture(os.path.join(HERE, "ops_golden.npz"))
+    fine_step_fixture(os.path.join(HERE, "fine_step_golden.npz"))
+
+
+if __name__ == "__main__":
+    main()

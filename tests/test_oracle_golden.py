@@ -1,0 +1,98 @@
+"""Pins the oracle against golden vectors produced by the reference's own
+Python code (tests/golden/make_golden.py runs lib/voxurf_fine.py, lib/grid.py
+and lib/utils.py in float64 on the CPU).  CPU only."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cref
+from oracle.voxurf_oracle import OracleFine, UtilsAdam, gaussian_kernel3d, grid_sample_pts, smooth3d, train_loss
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+OPS = np.load(os.path.join(HERE, "ops_golden.npz"))
+FINE = np.load(os.path.join(HERE, "fine_step_golden.npz"))
+
+
+def test_alpha2weight_matches_reference_cumprod():
+    """get_ray_marching_ray (voxurf_fine.py:951-954) == alpha2weight on rays
+    that never reach T < 1e-3."""
+    alpha = OPS["march_alpha"]
+    n_rays, n = alpha.shape
+    ray_id = np.repeat(np.arange(n_rays), n)
+    w, T, last, i_s, i_e = cref.alpha2weight(alpha.reshape(-1), ray_id, n_rays)
+    np.testing.assert_allclose(w.reshape(n_rays, n), OPS["march_weights"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(last, OPS["march_alphainv"][:, -1], rtol=1e-13, atol=0)
+    # float32 (reference-kernel arithmetic) agrees to float32 precision
+    w32, *_ = cref.alpha2weight(alpha.reshape(-1).astype(np.float32), ray_id, n_rays)
+    np.testing.assert_allclose(w32.reshape(n_rays, n), OPS["march_weights"], rtol=2e-6, atol=0)
+
+
+def test_utils_adam_restatement():
+    p0, p1 = torch.from_numpy(OPS["adam_p0"]).clone(), torch.from_numpy(OPS["adam_p1"]).clone()
+    params = [torch.nn.Parameter(p0), torch.nn.Parameter(p1)]
+    opt = UtilsAdam([([params[0]], 1e-2), ([params[1]], 3e-3)], betas=(0.9, 0.99))
+    count = torch.from_numpy(OPS["adam_count"])
+    opt.per_lr = count.float() / count.max()
+    for it in range(3):
+        params[0].grad = torch.from_numpy(OPS["adam_grads0"][it]).clone()
+        params[1].grad = torch.from_numpy(OPS["adam_grads1"][it]).clone()
+        opt.step()
+    np.testing.assert_array_equal(params[0].detach().numpy(), OPS["adam_out0"])
+    np.testing.assert_array_equal(params[1].detach().numpy(), OPS["adam_out1"])
+
+
+def test_dense_grid_restatement():
+    grid = torch.from_numpy(OPS["dg_grid"])
+    xyz = torch.from_numpy(OPS["dg_xyz"])
+    out = grid_sample_pts(grid, xyz, torch.tensor([-1.0, -0.5, -2.0]), torch.tensor([1.0, 1.5, 0.5]))
+    np.testing.assert_array_equal(out.numpy(), OPS["dg_out"])
+
+
+def test_smoothing_restatement():
+    k = torch.from_numpy(gaussian_kernel3d(5, 0.8))
+    out = smooth3d(torch.from_numpy(OPS["smooth_in"]), k)
+    np.testing.assert_allclose(out.numpy(), OPS["smooth_out"], rtol=1e-6, atol=1e-7)
+
+
+def _model_from_fixture(device="cpu", precision="fp32"):
+    from voxurf_gb300 import configs
+    from voxurf_gb300.grid import MaskGrid
+
+    R, width = int(FINE["R"]), int(FINE["width"])
+    model = configs.build_fine_model(R, precision, device="cpu", seed=int(FINE["seed"]), width=width)
+    sd = {k[len("state."):]: torch.from_numpy(FINE[k]) for k in FINE.files if k.startswith("state.")}
+    model.load_state_dict(sd, strict=False)
+    model = model.to(device)
+    mask = sd["mask_cache.mask"]
+    model.mask_cache = MaskGrid(mask=mask, xyz_min=[-1, -1, -1], xyz_max=[1, 1, 1]).to(device)
+    model.nonempty_mask = mask[None, None].to(device)
+    if precision == "bf16":
+        model.refresh_k0_shadow()
+    return model
+
+
+def fine_fixture_inputs():
+    rk = dict(near=0.1, far=6.0, bg=float(FINE["bg"]), stepsize=0.5)
+    return FINE["rays_o"], FINE["rays_d"], FINE["viewdirs"], FINE["target"], rk
+
+
+def test_fine_step_oracle_matches_reference():
+    model = _model_from_fixture()
+    oracle = OracleFine(model, dtype=torch.float64)
+    ro, rd, vd, tgt, rk = fine_fixture_inputs()
+    ret = oracle(torch.from_numpy(ro), torch.from_numpy(rd), torch.from_numpy(vd), global_step=1, **rk)
+    loss = train_loss(ret, torch.from_numpy(tgt).double())
+    loss.backward()
+    assert ret["weights"].numel() == FINE["weights"].size
+    np.testing.assert_allclose(ret["weights"].detach().numpy(), FINE["weights"], rtol=1e-12, atol=1e-15)
+    for k in ("rgb_marched", "rgb_marched0", "alphainv_cum"):
+        np.testing.assert_allclose(ret[k].detach().numpy(), FINE[k], rtol=1e-12, atol=1e-15)
+    assert abs(loss.item() - float(FINE["loss"])) < 1e-13
+    np.testing.assert_allclose(oracle.sdf_grid.grad.numpy(), FINE["grad_sdf"], rtol=1e-9, atol=1e-15)
+    np.testing.assert_allclose(oracle.k0_grid.grad.numpy(), FINE["grad_k0"], rtol=1e-9, atol=1e-15)
+    for n, p in oracle.rgbnet.named_parameters():
+        np.testing.assert_allclose(p.grad.numpy(), FINE["grad_mlp." + n], rtol=1e-9, atol=1e-15)
+    for n, p in oracle.k_rgbnet.named_parameters():
+        np.testing.assert_allclose(p.grad.numpy(), FINE["grad_mlp.k." + n], rtol=1e-9, atol=1e-15)

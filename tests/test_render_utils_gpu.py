@@ -130,9 +130,17 @@ def test_alpha2weight_fwd_bwd(cuda, n_rays, max_len, alpha_hi):
     assert np.array_equal(gis[keep], i_s[keep])
     assert np.array_equal(gie[keep], i_e[keep])
     samp_keep = keep[ray_id]
-    np.testing.assert_allclose(gw[samp_keep], w[samp_keep], rtol=2e-6, atol=1e-9)
-    np.testing.assert_allclose(gT[samp_keep], T[samp_keep], rtol=2e-6, atol=1e-9)
-    np.testing.assert_allclose(glast[keep], last[keep], rtol=2e-6, atol=1e-9)
+    # against the FP64 scan (the GPU carries T in FP64 and rounds once)
+    w64, T64, last64, _, _ = cref.alpha2weight(alpha.astype(np.float64), ray_id, n_rays)
+    np.testing.assert_allclose(gw[samp_keep], w64[samp_keep], rtol=3e-7, atol=1e-12)
+    np.testing.assert_allclose(gT[samp_keep], T64[samp_keep], rtol=3e-7, atol=1e-12)
+    np.testing.assert_allclose(glast[keep], last64[keep], rtol=3e-7, atol=1e-12)
+    # against the reference's serial float loop: its own rounding grows with
+    # the ray length (about sqrt(n) ulps)
+    rt = 2e-6 if max_len <= 700 else 2e-5
+    np.testing.assert_allclose(gw[samp_keep], w[samp_keep], rtol=rt, atol=1e-9)
+    np.testing.assert_allclose(gT[samp_keep], T[samp_keep], rtol=rt, atol=1e-9)
+    np.testing.assert_allclose(glast[keep], last[keep], rtol=rt, atol=1e-9)
 
     rng = np.random.default_rng(3)
     grad_w = rng.normal(size=alpha.size).astype(np.float32)

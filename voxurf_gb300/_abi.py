@@ -55,7 +55,7 @@ class FineCompositeArgs(C.Structure):
     _fields_ = [
         ("n_rays", I64), ("s2_off", P), ("w2", P), ("logit", P), ("klogit", P), ("alphainv_last", P), ("bg", F),
         ("rgb0", P), ("rgbk", P), ("rgbk_raw", P), ("normal2", P), ("step2", P), ("dist", F),
-        ("normal_out", P), ("depth_out", P), ("wsum_out", P),
+        ("normal_out", P), ("depth_out", P), ("wsum_out", P), ("has_k", I32),
     ]
 
 
@@ -63,6 +63,7 @@ class FineCompositeBwdArgs(C.Structure):
     _fields_ = [
         ("n_rays", I64), ("s2_off", P), ("w2", P), ("logit", P), ("klogit", P), ("rgbk_raw", P), ("g_rgb0", P),
         ("g_rgbk", P), ("bg", F), ("g_last_in", P), ("d_logit", P), ("d_klogit", P), ("d_w2", P), ("d_last", P),
+        ("has_k", I32),
     ]
 
 

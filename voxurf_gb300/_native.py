@@ -29,6 +29,7 @@ _SIGNATURES = {
     "vx_version": [],
     "vx_status_string": [c_int],
     "vx_last_cuda_error": [],
+    "vx_launch_count": [],
     "vx_cuda_error_string": [c_int],
     "vx_device_error": [c_ptr, c_ptr],
     "vx_scan_scratch_bytes": [c_i64],
@@ -62,6 +63,7 @@ _RESTYPES = {
     "vx_status_string": C.c_char_p,
     "vx_cuda_error_string": C.c_char_p,
     "vx_scan_scratch_bytes": c_size,
+    "vx_launch_count": C.c_ulonglong,
 }
 
 
@@ -114,6 +116,11 @@ def call(name: str, *args) -> None:
     """Calls entry point `name` and raises on a non-zero status."""
     fn = getattr(load(), name)
     check(fn(*args), name)
+
+
+def launch_count() -> int:
+    """Kernels launched by libvoxurf_gb300 in this process so far."""
+    return int(load().vx_launch_count())
 
 
 def device_error(stream_ptr: int) -> int:

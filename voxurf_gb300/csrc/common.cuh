@@ -19,8 +19,12 @@ namespace vx {
 
 // Last CUDA error seen by any entry point of this library (host-side copy).
 extern int g_last_cuda_error;
+// Number of kernel launches issued by this library (every launch is
+// followed by exactly one launch_status() call).
+extern unsigned long long g_launch_count;
 
 inline int launch_status() {
+  __atomic_add_fetch(&g_launch_count, 1ull, __ATOMIC_RELAXED);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_last_cuda_error = (int)e;

@@ -131,9 +131,18 @@ __device__ __forceinline__ void sdf_and_grad(const float* __restrict__ sdf, cons
 
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.f / (1.f + expf(-x)); }
 
-// NeuS s-density alpha (voxurf_fine.py:475-499, cos_anneal_ratio = 1).
+// NeuS s-density alpha (voxurf_fine.py:475-499, cos_anneal_ratio = 1):
+//   P = sigmoid(prev*inv_s), Q = sigmoid(next*inv_s),
+//   alpha = clip((P - Q + 1e-5) / (P + 1e-5), 0, 1).
+// Away from the surface P and Q both approach 1 and the literal P - Q loses
+// all FP32 precision (about 1e-3 relative error at alpha ~ 1e-4, which flips
+// the fast_color_thres decisions against an FP64 evaluation).  The same
+// quantity is formed without cancellation:
+//   P - Q = sigmoid(a) * sigmoid(-b) * (-expm1(b - a)),  a = prev*inv_s,
+// b = next*inv_s (b <= a), and 1 - P, 1 - Q are taken as sigmoid(-a),
+// sigmoid(-b) in the backward.
 struct AlphaState {
-  float alpha, raw, P, Q, cosv;
+  float alpha, raw, P, Q, nP, nQ, cosv;
 };
 
 __device__ __forceinline__ AlphaState neus_alpha(float s, const float gr[3], const float v[3], float inv_s,
@@ -143,9 +152,13 @@ __device__ __forceinline__ AlphaState neus_alpha(float s, const float gr[3], con
   const float ic = fminf(a.cosv, 0.f);  // -relu(-cos)
   const float h = ic * dist * 0.5f;
   const float next = s + h, prev = s - h;
-  a.P = sigmoidf_(prev * inv_s);
-  a.Q = sigmoidf_(next * inv_s);
-  a.raw = (a.P - a.Q + 1e-5f) / (a.P + 1e-5f);
+  const float xa = prev * inv_s, xb = next * inv_s;
+  a.P = sigmoidf_(xa);
+  a.Q = sigmoidf_(xb);
+  a.nP = sigmoidf_(-xa);
+  a.nQ = sigmoidf_(-xb);
+  const float pmq = -(a.P * a.nQ) * expm1f(xb - xa);
+  a.raw = (pmq + 1e-5f) / (a.P + 1e-5f);
   a.alpha = fminf(fmaxf(a.raw, 0.f), 1.f);
   return a;
 }
@@ -440,6 +453,7 @@ struct CompositeParams {
   float* normal_out;     // [N,3]
   float* depth_out;      // [N]
   float* wsum_out;       // [N]
+  int has_k;             // k-branch present (an empty klogit has a null pointer)
 };
 
 __global__ void __launch_bounds__(256) composite_fine_kernel(CompositeParams P) {
@@ -454,7 +468,7 @@ __global__ void __launch_bounds__(256) composite_fine_kernel(CompositeParams P) 
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       a0[c] += w * sigmoidf_(P.logit[3 * i + c]);
-      if (P.klogit) ak[c] += w * sigmoidf_(P.klogit[3 * i + c]);
+      if (P.has_k) ak[c] += w * sigmoidf_(P.klogit[3 * i + c]);
     }
     ws += w;
     if (P.normal2) {
@@ -479,7 +493,7 @@ __global__ void __launch_bounds__(256) composite_fine_kernel(CompositeParams P) 
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       P.rgb0[3 * r + c] = a0[c] + bgt;
-      if (P.klogit) {
+      if (P.has_k) {
         const float raw = ak[c] + bgt;
         P.rgbk_raw[3 * r + c] = raw;
         P.rgbk[3 * r + c] = fminf(fmaxf(raw, 0.f), 1.f);
@@ -506,6 +520,7 @@ struct CompositeBwdParams {
   float* d_klogit;  // [S2,3] or null
   float* d_w2;      // [S2]
   float* d_last;    // [N]
+  int has_k;
 };
 
 __global__ void __launch_bounds__(256) composite_fine_bwd_kernel(CompositeBwdParams P) {
@@ -516,7 +531,7 @@ __global__ void __launch_bounds__(256) composite_fine_bwd_kernel(CompositeBwdPar
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     if (P.g_rgb0) g0[c] = P.g_rgb0[3 * r + c];
-    if (P.g_rgbk && P.klogit) {
+    if (P.g_rgbk && P.has_k) {
       const float raw = P.rgbk_raw[3 * r + c];
       gk[c] = (raw >= 0.f && raw <= 1.f) ? P.g_rgbk[3 * r + c] : 0.f;  // clamp backward
     }
@@ -530,7 +545,7 @@ __global__ void __launch_bounds__(256) composite_fine_bwd_kernel(CompositeBwdPar
       const float y0 = sigmoidf_(P.logit[3 * i + c]);
       P.d_logit[3 * i + c] = (w * g0[c]) * (1.f - y0) * y0;
       dw += g0[c] * y0;
-      if (P.klogit) {
+      if (P.has_k) {
         const float yk = sigmoidf_(P.klogit[3 * i + c]);
         P.d_klogit[3 * i + c] = (w * gk[c]) * (1.f - yk) * yk;
         dw += gk[c] * yk;
@@ -721,8 +736,8 @@ __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P)
     const float den = a.P + 1e-5f;
     const float dP = d_alpha * a.Q / (den * den);
     const float dQ = -d_alpha / den;
-    const float d_prev = dP * a.P * (1.f - a.P) * P.inv_s;
-    const float d_next = dQ * a.Q * (1.f - a.Q) * P.inv_s;
+    const float d_prev = dP * a.P * a.nP * P.inv_s;
+    const float d_next = dQ * a.Q * a.nQ * P.inv_s;
     const float d_s = d_prev + d_next;
     const float d_ic = (d_next - d_prev) * P.dist * 0.5f;
     const float d_cos = a.cosv < 0.f ? d_ic : 0.f;
@@ -984,6 +999,7 @@ int vx_fine_composite(const vx_fine_composite_args* A, void* stream) {
   P.normal_out = A->normal_out;
   P.depth_out = A->depth_out;
   P.wsum_out = A->wsum_out;
+  P.has_k = A->has_k;
   composite_fine_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
   return launch_status();
 }
@@ -1006,6 +1022,7 @@ int vx_fine_composite_backward(const vx_fine_composite_bwd_args* A, void* stream
   P.d_klogit = A->d_klogit;
   P.d_w2 = A->d_w2;
   P.d_last = A->d_last;
+  P.has_k = A->has_k;
   composite_fine_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
   return launch_status();
 }

@@ -5,6 +5,7 @@
 namespace vx {
 
 int g_last_cuda_error = 0;
+unsigned long long g_launch_count = 0;
 static __device__ int g_device_error = 0;
 
 int* device_error_ptr() {
@@ -51,6 +52,8 @@ const char* vx_status_string(int status) {
 }
 
 int vx_last_cuda_error(void) { return vx::g_last_cuda_error; }
+
+unsigned long long vx_launch_count(void) { return __atomic_load_n(&vx::g_launch_count, __ATOMIC_RELAXED); }
 
 const char* vx_cuda_error_string(int code) { return cudaGetErrorString((cudaError_t)code); }
 

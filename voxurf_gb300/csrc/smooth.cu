@@ -90,7 +90,11 @@ int vx_smooth3d(const float* in, float* out, float* tmp1, float* tmp2, int64_t X
   cudaStream_t st = as_stream(stream);
   const unsigned b = pass_blocks(X * Y * Z);
   smooth_axis_kernel<false, false><<<b, 256, 0, st>>>(in, tmp1, (int)X, (int)Y, (int)Z, 0, t);
+  int s = launch_status();
+  if (s) return s;
   smooth_axis_kernel<false, false><<<b, 256, 0, st>>>(tmp1, tmp2, (int)X, (int)Y, (int)Z, 1, t);
+  s = launch_status();
+  if (s) return s;
   smooth_axis_kernel<false, false><<<b, 256, 0, st>>>(tmp2, out, (int)X, (int)Y, (int)Z, 2, t);
   return launch_status();
 }
@@ -106,7 +110,11 @@ int vx_smooth3d_adjoint(const float* grad_out, float* grad_in, float* tmp1, floa
   cudaStream_t st = as_stream(stream);
   const unsigned b = pass_blocks(X * Y * Z);
   smooth_axis_kernel<true, false><<<b, 256, 0, st>>>(grad_out, tmp1, (int)X, (int)Y, (int)Z, 2, t);
+  int s = launch_status();
+  if (s) return s;
   smooth_axis_kernel<true, false><<<b, 256, 0, st>>>(tmp1, tmp2, (int)X, (int)Y, (int)Z, 1, t);
+  s = launch_status();
+  if (s) return s;
   if (accumulate)
     smooth_axis_kernel<true, true><<<b, 256, 0, st>>>(tmp2, grad_in, (int)X, (int)Y, (int)Z, 0, t);
   else

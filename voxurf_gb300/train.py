@@ -1,0 +1,69 @@
+"""The fused training step of the Voxurf fine stage (run.py:599-659).
+
+One step = model forward on a ray batch, the run.py loss (photometric on the
+k-branch, 0.5 x photometric on rgbnet, entropy of the last ray's
+transmittance), the hand-written backward, then one sweep per grid that
+applies the total-variation gradient (run.py:641-658 ->
+Voxurf.*_total_variation_add_grad, weight / N_rays) together with the Adam
+update, and one Adam launch per MLP tensor.
+"""
+from __future__ import annotations
+
+import torch
+import torch.nn.functional as F
+
+from .utils import Adam
+
+
+def fine_loss(ret, target, weight_main=1.0, weight_entropy_last=0.001, weight_rgb0=0.5):
+    """run.py:604-636 with the fine dtu_e2e weights (configs/dtu_e2e/fine.py:104-105
+    and the surf_train default weight_entropy_last, default_fine_s.py:63)."""
+    loss = weight_main * F.mse_loss(ret["rgb_marched"], target)
+    if weight_entropy_last > 0:
+        # run.py:608: [..., -1] of the 1-D alphainv_cum selects the last ray
+        pout = ret["alphainv_cum"][..., -1].clamp(1e-6, 1 - 1e-6)
+        loss = loss + weight_entropy_last * (-(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean())
+    if weight_rgb0 > 0 and "rgb_marched0" in ret:
+        loss = loss + F.mse_loss(ret["rgb_marched0"], target) * weight_rgb0
+    return loss
+
+
+class FineTrainer:
+    """Owns the optimizer of a fine Voxurf model and runs fused steps.
+
+    lr_* are the per-group learning rates (utils.create_optimizer_or_freeze_model
+    groups sdf / k0 / rgbnet / k_rgbnet); tv_sdf / tv_k0 are the weights
+    given to *_total_variation_add_grad before the division by the batch
+    size (run.py:647-655); tv_dense mirrors `global_step < tv_dense_before`.
+    """
+
+    def __init__(self, model, lr_sdf=1e-3, lr_k0=1e-3, lr_rgbnet=1e-3, lr_k_rgbnet=1e-3, tv_sdf=1e-4, tv_k0=1e-4,
+                 tv_dense=True, n_rays=8192, loss_weights=(1.0, 0.001, 0.5)):
+        self.model = model
+        self.n_rays = n_rays
+        scale = float(model.world_size.max()) / 128  # voxurf_fine.py:404, 408
+        shadow = None
+        if model.precision == "bf16":
+            shadow = model._k0_shadow if model._k0_shadow is not None else model.refresh_k0_shadow()
+        groups = [
+            {"params": [model.sdf.grid], "lr": lr_sdf, "name": "sdf", "tv_weight": tv_sdf / n_rays * scale,
+             "tv_dense": tv_dense},
+            {"params": [model.k0.grid], "lr": lr_k0, "name": "k0", "tv_weight": tv_k0 / n_rays * scale,
+             "tv_dense": tv_dense, "shadow": shadow},
+            {"params": list(model.rgbnet.parameters()), "lr": lr_rgbnet, "name": "rgbnet"},
+            {"params": list(model.k_rgbnet.parameters()), "lr": lr_k_rgbnet, "name": "k_rgbnet"},
+        ]
+        self.optimizer = Adam(groups, betas=(0.9, 0.99))
+        self.loss_weights = loss_weights
+        self.global_step = 0
+        self.render_kwargs = None
+
+    def step(self, rays_o, rays_d, viewdirs, target, render_kwargs, global_step=None):
+        if global_step is None:
+            self.global_step += 1
+            global_step = self.global_step
+        ret = self.model(rays_o, rays_d, viewdirs, global_step=global_step, **render_kwargs)
+        loss = fine_loss(ret, target, *self.loss_weights)
+        loss.backward()
+        self.optimizer.step(zero_grad=True)
+        return loss.detach(), ret

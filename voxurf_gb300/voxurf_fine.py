@@ -222,6 +222,7 @@ class _FineComposite(torch.autograd.Function):
         a.n_rays, a.s2_off, a.w2 = N, ptr(fr.s2_off), ptr(w2)
         a.logit, a.klogit, a.alphainv_last, a.bg = ptr(logit), ptr(klogit), ptr(alphainv_last), float(bg)
         a.rgb0, a.rgbk, a.rgbk_raw = ptr(rgb0), ptr(rgbk), ptr(rgbk_raw)
+        a.has_k = int(klogit is not None)
         if fr.render_extras:
             fr.normal_marched = torch.empty((N, 3), dtype=torch.float32, device=dev)
             fr.depth = torch.empty(N, dtype=torch.float32, device=dev)
@@ -249,6 +250,7 @@ class _FineComposite(torch.autograd.Function):
         g_rgbk = None if (g_rgbk is None or not ctx.has_k) else g_rgbk.contiguous()
         a.g_rgb0, a.g_rgbk, a.bg = ptr(g_rgb0), ptr(g_rgbk), ctx.bg
         a.d_logit, a.d_klogit, a.d_w2, a.d_last = ptr(d_logit), ptr(d_klogit), ptr(d_w2), ptr(d_last)
+        a.has_k = int(ctx.has_k)
         _abi.call_struct("vx_fine_composite_backward", a, stream_ptr())
         return d_w2, d_last, d_logit, d_klogit, None, None
 
