@@ -60,7 +60,16 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-bf16", action="store_true")
-    return p.parse_args()
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--grid", type=int, default=256, help="grid resolution (256 is the benchmark; smaller sizes "
+                                                         "serve profiler captures)")
+    args = p.parse_args()
+    global R, K0_ELEMS, MASK_VOXELS
+    if args.grid != R:
+        R = args.grid
+        K0_ELEMS = R ** 3 * 12
+        MASK_VOXELS = 0.05 / (2.0 / R)
+    return args
 
 
 def dist_setup(args):
@@ -220,18 +229,20 @@ def run_ours(args, world, rank, local):
     shaded = int(model._last_frame.S2)
 
     # ---- e2e: same step, batches from pinned host memory, loss read back -------
-    pinned = [torch.from_numpy(a).pin_memory() for a in host]
-    barrier()
-    w0 = time.perf_counter()
-    e2e_losses = []
-    for i in range(args.warmup, n_b):
-        xs = [p[i].to(dev, non_blocking=True) for p in pinned]
-        loss, _ = tr.step(xs[0], xs[1], xs[2], xs[3], rk)
-        e2e_losses.append(float(loss.item()))
-    barrier()
-    t_e2e = max_over_ranks(time.perf_counter() - w0)
-    e2e = world * N_RAYS * args.steps / t_e2e
-    h2d = sum(p[0].numel() * p[0].element_size() for p in pinned)
+    e2e, h2d = None, 0
+    if not args.no_e2e:
+        pinned = [torch.from_numpy(a).pin_memory() for a in host]
+        barrier()
+        w0 = time.perf_counter()
+        e2e_losses = []
+        for i in range(args.warmup, n_b):
+            xs = [p[i].to(dev, non_blocking=True) for p in pinned]
+            loss, _ = tr.step(xs[0], xs[1], xs[2], xs[3], rk)
+            e2e_losses.append(float(loss.item()))
+        barrier()
+        t_e2e = max_over_ranks(time.perf_counter() - w0)
+        e2e = world * N_RAYS * args.steps / t_e2e
+        h2d = sum(p[0].numel() * p[0].element_size() for p in pinned)
     del tr, model
     torch.cuda.empty_cache()
 
