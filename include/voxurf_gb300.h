@@ -327,6 +327,123 @@ typedef struct {
 } vx_fine_backward_args;
 int vx_fine_backward(const vx_fine_backward_args* args, void* stream);
 
+/* ---- dense SDF gradient grid (Voxurf.neus_sdf_gradient 'interpolate',
+ *      lib/voxurf_fine.py:440-450, lib/voxurf_coarse.py:323-332) ----------- */
+
+/* G = central differences / (2 voxel_size) on interior points, 0 on the
+ * boundary slab of each axis.  layout 0: [3,X,Y,Z]; layout 1: [X,Y,Z,4]. */
+int vx_sdf_gradient_grid(const float* sdf, float* G, int64_t X, int64_t Y, int64_t Z, float voxel_size, int layout,
+                         void* stream);
+/* d_sdf (+)= adjoint of vx_sdf_gradient_grid applied to dG. */
+int vx_sdf_gradient_grid_adjoint(const float* dG, float* d_sdf, int64_t X, int64_t Y, int64_t Z, float voxel_size,
+                                 int layout, int accumulate, void* stream);
+/* smooth_grad_tv (voxurf_fine.py:417-420, run.py:621-622) on a [X,Y,Z,4]
+ * gradient grid: dG = -grad_scale * (S(G) - G) on the non-empty voxels
+ * (mask bytes, NULL = all), S the normalised [1,2,1]^3 kernel with
+ * replicate padding; partial[b] = per-block sums of (S(G)-G)^2. */
+size_t vx_smooth_grad_tv_scratch_bytes(int64_t X, int64_t Y, int64_t Z);
+int vx_smooth_grad_tv(const float* G, const uint8_t* mask, int64_t X, int64_t Y, int64_t Z, float grad_scale,
+                      float* dG, double* partial, void* stream);
+
+/* ---- fused coarse-model rendering (lib/voxurf_coarse.py:513-619) ---------- */
+
+/* March with the coarse semantics: gradient from the [X,Y,Z,4] grid of the
+ * raw SDF, weights from a second Alphas2Weights over the weight > thres set
+ * (:540-550).  Records of that set go to the per-ray slots (all flagged);
+ * n1 = n2 = their count, n2b = the count up to the second scan's stop. */
+typedef struct {
+  vx_fine_march_args march;
+  const float* grad4;       /* [X,Y,Z,4] vx_sdf_gradient_grid(layout 1) of the raw SDF */
+  int32_t* n2b;             /* out [N]                                          */
+} vx_coarse_march_args;
+int vx_coarse_march(const vx_coarse_march_args* args, void* stream);
+
+typedef struct {
+  int32_t use_k0;           /* k0 columns first (rgbnet_full_implicit = False)  */
+  int32_t geo_rgb_dim;      /* 3: normalised gradient columns last, 0: none     */
+  int64_t posbase_pe, viewbase_pe;
+} vx_coarse_feature_cfg;
+
+/* rgbnet input [k0, PE(xyz), PE(viewdir), normal] (voxurf_coarse.py:552-569). */
+typedef struct {
+  int64_t n_rows;
+  const int32_t* ray2;
+  const float* pts2;
+  const float* viewdirs;
+  vx_grid_geom grid;
+  const float* grad4;
+  const float* k0_f32;
+  const void* k0_bf16;
+  vx_coarse_feature_cfg cfg;
+  int64_t ld;
+  void* X;
+  int32_t out_bf16;
+  float* normal_out;        /* optional [S2,3] interpolated gradient            */
+} vx_coarse_features_args;
+int vx_coarse_features(const vx_coarse_features_args* args, void* stream);
+
+/* rgb = clamp(sum w*sigmoid(logit) + (1 - sum w)*bg, 0, 1) (:575-584). */
+typedef struct {
+  int64_t n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;
+  float bg;
+  float* rgb;
+  float* rgb_raw;
+  const float* normal2;
+  const int32_t* step2;
+  float dist;
+  float* normal_out;
+  float* depth_out;
+  float* wsum_out;
+} vx_coarse_composite_args;
+int vx_coarse_composite(const vx_coarse_composite_args* args, void* stream);
+
+typedef struct {
+  int64_t n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;
+  const float* rgb_raw;
+  const float* g_rgb;
+  float bg;
+  float* d_logit;
+  float* d_w2;
+} vx_coarse_composite_bwd_args;
+int vx_coarse_composite_backward(const vx_coarse_composite_bwd_args* args, void* stream);
+
+typedef struct {
+  int64_t n_rays;
+  int64_t n_rows;
+  const float* rays_o;
+  const float* rays_d;
+  const float* viewdirs;
+  float near, stepdist;
+  vx_grid_geom grid;
+  const float* sdf_smooth;
+  const float* grad4;
+  float voxel_size;
+  float inv_s, dist;
+  int64_t max_steps;
+  const void* rec;
+  float* dw_slot;
+  const int32_t* n2b;
+  const float* alphainv_last;
+  const float* d_last;
+  const float* pts2;
+  const int32_t* slot2;
+  const float* dw2;
+  vx_coarse_feature_cfg cfg;
+  int64_t ld;
+  const void* dX;
+  int32_t in_bf16;
+  float* d_sdf_smooth;      /* [X,Y,Z] accumulated                              */
+  float* d_grad4;           /* [X,Y,Z,4] accumulated                            */
+  float* d_k0;              /* [X,Y,Z,12] accumulated                           */
+} vx_coarse_backward_args;
+int vx_coarse_backward(const vx_coarse_backward_args* args, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

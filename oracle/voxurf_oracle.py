@@ -225,6 +225,99 @@ class OracleFine(nn.Module):
         return out
 
 
+def neus_sdf_gradient(sdf, voxel_size):
+    """voxurf_coarse.py:323-332, 'interpolate' mode."""
+    g = torch.zeros([1, 3] + list(sdf.shape[-3:]), dtype=sdf.dtype)
+    g[:, 0, 1:-1, :, :] = (sdf[:, 0, 2:, :, :] - sdf[:, 0, :-2, :, :]) / 2 / voxel_size
+    g[:, 1, :, 1:-1, :] = (sdf[:, 0, :, 2:, :] - sdf[:, 0, :, :-2, :]) / 2 / voxel_size
+    g[:, 2, :, :, 1:-1] = (sdf[:, 0, :, :, 2:] - sdf[:, 0, :, :, :-2]) / 2 / voxel_size
+    return g
+
+
+class OracleCoarse(nn.Module):
+    """Reference coarse-stage step (voxurf_coarse.py:513-619) with parameters
+    copied from a voxurf_gb300 coarse model."""
+
+    def __init__(self, model, dtype=torch.float64):
+        super().__init__()
+        self.dtype = dtype
+        sd = {k: v.detach().cpu() for k, v in model.state_dict().items()}
+        self.sdf_grid = nn.Parameter(sd["sdf.grid"].contiguous().to(dtype))
+        self.full_implicit = model.rgbnet_full_implicit
+        self.k0_grid = nn.Parameter(sd["k0.grid"].contiguous().to(dtype))
+        self.rgbnet = copy.deepcopy(model.rgbnet).cpu().to(dtype)
+        self.xyz_min, self.xyz_max = sd["xyz_min"].to(dtype), sd["xyz_max"].to(dtype)
+        self.xyz_min32, self.xyz_max32 = sd["xyz_min"].float(), sd["xyz_max"].float()
+        self.voxel_size = f32(model.voxel_size)
+        self.fast_color_thres = model.fast_color_thres
+        self.smooth_sdf = model.smooth_sdf
+        if self.smooth_sdf:
+            self.kernel = torch.from_numpy(gaussian_kernel3d(model.smooth_ksize, model.smooth_sigma)).to(dtype)
+        self.posfreq, self.viewfreq = sd["posfreq"].to(dtype), sd["viewfreq"].to(dtype)
+        self.geo_rgb_dim = model.geo_rgb_dim
+        for k in ("s_ratio", "s_start", "s_learn", "step_start"):
+            setattr(self, k, getattr(model, k))
+        self.s_val = model.s_val.clone().float().cpu()
+        self.mask = None
+        if model.mask_cache is not None:
+            mc = model.mask_cache
+            self.mask = (mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
+
+    def forward(self, rays_o, rays_d, viewdirs, global_step=None, **rk):
+        dt = self.dtype
+        N = len(rays_o)
+        stepdist = f32(rk["stepsize"] * np.float32(self.voxel_size))
+        ru = RenderUtilsOracle
+        ray_pts, mask_outbbox, ray_id, step_id, _, _, _ = ru.sample_pts_on_rays(
+            rays_o.float().cpu(), rays_d.float().cpu(), self.xyz_min32, self.xyz_max32, rk["near"], 1e9, stepdist)
+        inb = ~mask_outbbox
+        ray_pts32, ray_id, step_id = ray_pts[inb], ray_id[inb], step_id[inb]
+        if self.mask is not None:
+            m = ru.maskcache_lookup(self.mask[0], ray_pts32, self.mask[1], self.mask[2])
+            ray_pts32, ray_id, step_id = ray_pts32[m], ray_id[m], step_id[m]
+        ray_pts = ray_pts32.to(dt)
+        viewdirs = viewdirs.cpu().to(dt)
+        sdf_grid = smooth3d(self.sdf_grid, self.kernel) if self.smooth_sdf else self.sdf_grid
+        sdf = grid_sample_pts(sdf_grid, ray_pts, self.xyz_min, self.xyz_max)[:, 0]
+        gradient_grid = neus_sdf_gradient(self.sdf_grid, self.voxel_size)
+        gradient = grid_sample_pts(gradient_grid, ray_pts, self.xyz_min, self.xyz_max)
+        dist = f32(rk["stepsize"] * np.float32(self.voxel_size))
+        if global_step is not None:
+            if not self.s_learn:
+                s_val = 1.0 / (global_step + self.s_ratio / self.s_start - self.step_start) * self.s_ratio
+                self.s_val = torch.ones(1) * s_val
+            else:
+                s_val = float(self.s_val.item())
+        else:
+            s_val = 0
+        inv_s = float((torch.ones(1) / self.s_val.float()).item())
+        alpha = neus_alpha(viewdirs, ray_id, dist, sdf, gradient, inv_s)
+        weights, _ = Alphas2WeightsOracle.apply(alpha, ray_id, N)
+        m = weights > self.fast_color_thres
+        ray_pts, ray_id, step_id, alpha, gradient = ray_pts[m], ray_id[m], step_id[m], alpha[m], gradient[m]
+        weights, alphainv_last = Alphas2WeightsOracle.apply(alpha, ray_id, N)
+        feats = []
+        if not self.full_implicit:
+            feats.append(grid_sample_pts(self.k0_grid, ray_pts, self.xyz_min, self.xyz_max))
+        rays_xyz = (ray_pts - self.xyz_min) / (self.xyz_max - self.xyz_min)
+        feats += [pe(rays_xyz, self.posfreq), pe(viewdirs, self.viewfreq)[ray_id]]
+        rgb_feat = torch.cat(feats, -1)
+        if self.geo_rgb_dim == 3:
+            normal = gradient / (gradient.norm(dim=-1, keepdim=True) + 1e-5)
+            rgb_feat = torch.cat([rgb_feat, normal], -1)
+        rgb = torch.sigmoid(self.rgbnet(rgb_feat))
+        rgb_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * rgb)
+        cum_w = torch.zeros([N, 1], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1))
+        rgb_marched = (rgb_marched + (1 - cum_w) * rk["bg"]).clamp(0, 1)
+        out = {"alphainv_cum": alphainv_last, "weights": weights, "rgb_marched": rgb_marched, "raw_rgb": rgb,
+               "raw_alpha": alpha, "gradient": gradient, "ray_id": ray_id, "step_id": step_id, "s_val": s_val,
+               "rgb_feat": rgb_feat}
+        if rk.get("render_grad", False):
+            nrm = gradient / (gradient.norm(2, -1, keepdim=True) + 1e-6)
+            out["normal_marched"] = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * nrm)
+        return out
+
+
 def train_loss(ret, target, weight_main=1.0, weight_entropy_last=0.001, weight_rgb0=0.5):
     """run.py:604-636 (the loss terms of the fine dtu_e2e stage)."""
     target = target.to(ret["rgb_marched"].dtype)

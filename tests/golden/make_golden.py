@@ -150,6 +150,51 @@ def fine_step_fixture(path, R=16, n_rays=128, width=64, mask_voxels=3.0, bg=1, s
     print("wrote", path, "shaded samples", ret["weights"].numel())
 
 
+def coarse_step_fixture(path, R=16, n_rays=128, width=32, bg=1, seed=4):
+    """One coarse-stage training step of the reference model in float64
+    (lib/voxurf_coarse.py:513-619, loss of run.py:604-610)."""
+    import lib.voxurf_coarse as rc
+    from voxurf_gb300 import configs, synthetic
+
+    ours = configs.build_coarse_model(R, "fp32", device="cpu", seed=seed, width=width)
+    kw = configs.coarse_model_kwargs(R, "fp32", width)
+    kw.pop("precision")
+    ref = rc.Voxurf(**kw)
+    sd = _state_from_ours(ours)
+    missing, unexpected = ref.load_state_dict(sd, strict=False)
+    assert not unexpected, unexpected
+    sd = {k: v for k, v in ref.state_dict().items()}
+    ref = ref.double()
+    ro, rd, vd = synthetic.random_rays(n_rays, seed=seed + 11)
+    tgt = configs.train_targets(n_rays, seed)
+    rk = dict(configs.COARSE_RENDER_KWARGS, bg=bg)
+    T = lambda a: torch.from_numpy(a).double()
+    # voxurf_coarse.py:329 allocates the gradient grid with the default dtype,
+    # so the float64 run needs float64 as the default (which also makes the
+    # reference's inv_s = ones(1)/s_val float64 here, voxurf_coarse.py:360)
+    torch.set_default_dtype(torch.float64)
+    try:
+        ret = ref(T(ro), T(rd), T(vd), global_step=1, **rk)
+    finally:
+        torch.set_default_dtype(torch.float32)
+    target = T(tgt)
+    loss = torch.nn.functional.mse_loss(ret["rgb_marched"], target)
+    pout = ret["alphainv_cum"][..., -1].clamp(1e-6, 1 - 1e-6)
+    loss = loss + 0.001 * (-(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean())
+    loss.backward()
+    out = {"R": R, "n_rays": n_rays, "width": width, "bg": bg, "seed": seed, "rays_o": ro, "rays_d": rd,
+           "viewdirs": vd, "target": tgt, "rgb_marched": ret["rgb_marched"].detach().numpy(),
+           "alphainv_cum": ret["alphainv_cum"].detach().numpy(), "weights": ret["weights"].detach().numpy(),
+           "loss": np.array(loss.item()), "grad_sdf": ref.sdf.grid.grad.numpy(), "grad_k0": ref.k0.grid.grad.numpy()}
+    for name, p in ref.rgbnet.named_parameters():
+        out["grad_mlp." + name] = p.grad.numpy()
+    for k, v in sd.items():
+        if v.dtype.is_floating_point:
+            out["state." + k] = v.float().numpy()
+    np.savez_compressed(path, **out)
+    print("wrote", path, "shaded samples", ret["weights"].numel())
+
+
 def ops_fixture(path, seed=5):
     """Reference torch code for individual pieces of the path."""
     import lib.grid as rgrid
@@ -205,6 +250,7 @@ def main():
     torch.set_default_dtype(torch.float32)
     ops_fixture(os.path.join(HERE, "ops_golden.npz"))
     fine_step_fixture(os.path.join(HERE, "fine_step_golden.npz"))
+    coarse_step_fixture(os.path.join(HERE, "coarse_step_golden.npz"))
 
 
 if __name__ == "__main__":

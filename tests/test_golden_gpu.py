@@ -86,3 +86,21 @@ def test_fine_step_vs_reference_golden(cuda):
         assert rel(p.grad.cpu().numpy(), FINE["grad_mlp." + n]) <= 1e-5, n
     for n, p in model.k_rgbnet.named_parameters():
         assert rel(p.grad.cpu().numpy(), FINE["grad_mlp.k." + n]) <= 1e-5, n
+
+
+def test_coarse_step_vs_reference_golden(cuda):
+    from test_oracle_golden import COARSE, coarse_fixture_inputs, coarse_model_from_fixture
+
+    model = coarse_model_from_fixture(device=cuda)
+    ro, rd, vd, tgt, rk = coarse_fixture_inputs()
+    T = lambda a: torch.from_numpy(a).to(cuda)
+    ret = model(T(ro), T(rd), T(vd), global_step=1, **rk)
+    loss = train_loss(ret, T(tgt), weight_rgb0=0)
+    loss.backward()
+    assert ret["weights"].numel() == COARSE["weights"].size
+    assert np.abs(ret["rgb_marched"].detach().cpu().numpy() - COARSE["rgb_marched"]).max() <= 1e-5
+    rel = lambda a, b: np.linalg.norm(a.reshape(-1) - b.reshape(-1)) / np.linalg.norm(b.reshape(-1))
+    assert rel(model.sdf.grid.grad.cpu().numpy(), COARSE["grad_sdf"]) <= 1e-5
+    assert rel(model.k0.grid.grad.contiguous().cpu().numpy(), COARSE["grad_k0"]) <= 1e-5
+    for n, p in model.rgbnet.named_parameters():
+        assert rel(p.grad.cpu().numpy(), COARSE["grad_mlp." + n]) <= 1e-5, n

@@ -62,7 +62,11 @@ def test_struct_sizes_match_c_layout():
                "vx_fine_compact_args": _abi.FineCompactArgs, "vx_fine_feature_cfg": _abi.FineFeatureCfg,
                "vx_fine_features_args": _abi.FineFeaturesArgs, "vx_fine_composite_args": _abi.FineCompositeArgs,
                "vx_fine_composite_bwd_args": _abi.FineCompositeBwdArgs,
-               "vx_fine_backward_args": _abi.FineBackwardArgs}
+               "vx_fine_backward_args": _abi.FineBackwardArgs, "vx_coarse_march_args": _abi.CoarseMarchArgs,
+               "vx_coarse_feature_cfg": _abi.CoarseFeatureCfg, "vx_coarse_features_args": _abi.CoarseFeaturesArgs,
+               "vx_coarse_composite_args": _abi.CoarseCompositeArgs,
+               "vx_coarse_composite_bwd_args": _abi.CoarseCompositeBwdArgs,
+               "vx_coarse_backward_args": _abi.CoarseBackwardArgs}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "voxurf_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -13,6 +13,7 @@ from oracle.voxurf_oracle import OracleFine, UtilsAdam, gaussian_kernel3d, grid_
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 OPS = np.load(os.path.join(HERE, "ops_golden.npz"))
 FINE = np.load(os.path.join(HERE, "fine_step_golden.npz"))
+COARSE = np.load(os.path.join(HERE, "coarse_step_golden.npz"))
 
 
 def test_alpha2weight_matches_reference_cumprod():
@@ -96,3 +97,40 @@ def test_fine_step_oracle_matches_reference():
         np.testing.assert_allclose(p.grad.numpy(), FINE["grad_mlp." + n], rtol=1e-9, atol=1e-15)
     for n, p in oracle.k_rgbnet.named_parameters():
         np.testing.assert_allclose(p.grad.numpy(), FINE["grad_mlp.k." + n], rtol=1e-9, atol=1e-15)
+
+
+def coarse_model_from_fixture(device="cpu"):
+    from voxurf_gb300 import configs
+
+    R, width = int(COARSE["R"]), int(COARSE["width"])
+    model = configs.build_coarse_model(R, "fp32", device="cpu", seed=int(COARSE["seed"]), width=width)
+    sd = {k[len("state."):]: torch.from_numpy(COARSE[k]) for k in COARSE.files if k.startswith("state.")}
+    model.load_state_dict(sd, strict=False)
+    return model.to(device)
+
+
+def coarse_fixture_inputs():
+    rk = dict(near=0.1, far=6.0, bg=float(COARSE["bg"]), stepsize=0.5)
+    return COARSE["rays_o"], COARSE["rays_d"], COARSE["viewdirs"], COARSE["target"], rk
+
+
+def test_coarse_step_oracle_matches_reference():
+    """The reference coarse run used float64 as torch's default dtype, which
+    makes its inv_s float64 (the oracle keeps float32 inv_s as the FP32
+    reference computes it): agreement to ~1e-7 relative."""
+    from oracle.voxurf_oracle import OracleCoarse
+
+    oracle = OracleCoarse(coarse_model_from_fixture())
+    ro, rd, vd, tgt, rk = coarse_fixture_inputs()
+    ret = oracle(torch.from_numpy(ro), torch.from_numpy(rd), torch.from_numpy(vd), global_step=1, **rk)
+    loss = train_loss(ret, torch.from_numpy(tgt).double(), weight_rgb0=0)
+    loss.backward()
+    assert ret["weights"].numel() == COARSE["weights"].size
+    np.testing.assert_allclose(ret["weights"].detach().numpy(), COARSE["weights"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(ret["rgb_marched"].detach().numpy(), COARSE["rgb_marched"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(ret["alphainv_cum"].detach().numpy(), COARSE["alphainv_cum"], rtol=1e-6)
+    rel = lambda a, b: np.linalg.norm((a - b).reshape(-1)) / np.linalg.norm(b.reshape(-1))
+    assert rel(oracle.sdf_grid.grad.numpy(), COARSE["grad_sdf"]) < 1e-6
+    assert rel(oracle.k0_grid.grad.numpy(), COARSE["grad_k0"]) < 1e-6
+    for n, p in oracle.rgbnet.named_parameters():
+        assert rel(p.grad.numpy(), COARSE["grad_mlp." + n]) < 1e-6, n

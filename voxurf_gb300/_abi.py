@@ -77,7 +77,52 @@ class FineBackwardArgs(C.Structure):
     ]
 
 
+class CoarseMarchArgs(C.Structure):
+    _fields_ = [("march", FineMarchArgs), ("grad4", P), ("n2b", P)]
+
+
+class CoarseFeatureCfg(C.Structure):
+    _fields_ = [("use_k0", I32), ("geo_rgb_dim", I32), ("posbase_pe", I64), ("viewbase_pe", I64)]
+
+
+class CoarseFeaturesArgs(C.Structure):
+    _fields_ = [
+        ("n_rows", I64), ("ray2", P), ("pts2", P), ("viewdirs", P), ("grid", GridGeom), ("grad4", P),
+        ("k0_f32", P), ("k0_bf16", P), ("cfg", CoarseFeatureCfg), ("ld", I64), ("X", P), ("out_bf16", I32),
+        ("normal_out", P),
+    ]
+
+
+class CoarseCompositeArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("s2_off", P), ("w2", P), ("logit", P), ("bg", F), ("rgb", P), ("rgb_raw", P),
+        ("normal2", P), ("step2", P), ("dist", F), ("normal_out", P), ("depth_out", P), ("wsum_out", P),
+    ]
+
+
+class CoarseCompositeBwdArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("s2_off", P), ("w2", P), ("logit", P), ("rgb_raw", P), ("g_rgb", P), ("bg", F),
+        ("d_logit", P), ("d_w2", P),
+    ]
+
+
+class CoarseBackwardArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("n_rows", I64), ("rays_o", P), ("rays_d", P), ("viewdirs", P), ("near", F),
+        ("stepdist", F), ("grid", GridGeom), ("sdf_smooth", P), ("grad4", P), ("voxel_size", F), ("inv_s", F),
+        ("dist", F), ("max_steps", I64), ("rec", P), ("dw_slot", P), ("n2b", P), ("alphainv_last", P),
+        ("d_last", P), ("pts2", P), ("slot2", P), ("dw2", P), ("cfg", CoarseFeatureCfg), ("ld", I64), ("dX", P),
+        ("in_bf16", I32), ("d_sdf_smooth", P), ("d_grad4", P), ("d_k0", P),
+    ]
+
+
 _STRUCT_FNS = {
+    "vx_coarse_march": CoarseMarchArgs,
+    "vx_coarse_features": CoarseFeaturesArgs,
+    "vx_coarse_composite": CoarseCompositeArgs,
+    "vx_coarse_composite_backward": CoarseCompositeBwdArgs,
+    "vx_coarse_backward": CoarseBackwardArgs,
     "vx_fine_march": FineMarchArgs,
     "vx_fine_compact": FineCompactArgs,
     "vx_fine_features": FineFeaturesArgs,
@@ -106,6 +151,14 @@ def _declare():
         fn = getattr(lib, name)
         fn.argtypes = [P, I64, C.c_int, C.POINTER(GridGeom), P, I64, P, P]
         fn.restype = C.c_int
+    lib.vx_sdf_gradient_grid.argtypes = [P, P, I64, I64, I64, F, C.c_int, P]
+    lib.vx_sdf_gradient_grid.restype = C.c_int
+    lib.vx_sdf_gradient_grid_adjoint.argtypes = [P, P, I64, I64, I64, F, C.c_int, C.c_int, P]
+    lib.vx_sdf_gradient_grid_adjoint.restype = C.c_int
+    lib.vx_smooth_grad_tv_scratch_bytes.argtypes = [I64, I64, I64]
+    lib.vx_smooth_grad_tv_scratch_bytes.restype = C.c_size_t
+    lib.vx_smooth_grad_tv.argtypes = [P, P, I64, I64, I64, F, P, P, P]
+    lib.vx_smooth_grad_tv.restype = C.c_int
     _declared = True
 
 
@@ -128,4 +181,6 @@ def call(name: str, *args) -> None:
 
 
 def struct_names() -> list[str]:
-    return list(_STRUCT_FNS) + ["vx_smooth3d", "vx_smooth3d_adjoint", "vx_grid_sample", "vx_grid_sample_backward"]
+    return list(_STRUCT_FNS) + ["vx_smooth3d", "vx_smooth3d_adjoint", "vx_grid_sample", "vx_grid_sample_backward",
+                                "vx_sdf_gradient_grid", "vx_sdf_gradient_grid_adjoint",
+                                "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv"]

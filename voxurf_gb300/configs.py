@@ -64,5 +64,38 @@ def build_fine_model(R: int = 256, precision: str = "fp32", device="cuda", seed:
     return model
 
 
+def coarse_model_kwargs(R: int = 96, precision: str = "fp32", width: int = 128) -> dict:
+    """Coarse stage (lib/voxurf_coarse.py) of the 96^3 configuration: rgbnet
+    input k0 12 + PE(xyz, 5) 33 + PE(viewdir, 4) 27 + normal 3 = 75, width
+    128, depth 3; smoothing 5^3 sigma 0.8; s_start 0.3 (s_ratio 50 as
+    configs/dtu_e2e/coarse.py:74)."""
+    return dict(
+        xyz_min=BBOX[0], xyz_max=BBOX[1], num_voxels=R ** 3, num_voxels_base=R ** 3, alpha_init=1e-2,
+        fast_color_thres=1e-4, rgbnet_dim=12, rgbnet_direct=True, rgbnet_full_implicit=False, rgbnet_depth=3,
+        rgbnet_width=width, posbase_pe=5, viewbase_pe=4, geo_rgb_dim=3, smooth_ksize=5, smooth_sigma=0.8,
+        s_ratio=50, s_start=0.3, precision=precision,
+    )
+
+
+def build_coarse_model(R: int = 96, precision: str = "fp32", device="cuda", seed: int = 0, width: int = 128,
+                       scene: str = "sphere"):
+    """Coarse Voxurf model with the sphere r=0.5 + N(0,0.01) scene loaded."""
+    from .voxurf_coarse import Voxurf
+
+    torch.manual_seed(seed)
+    model = Voxurf(**coarse_model_kwargs(R, precision, width))
+    with torch.no_grad():
+        model.sdf.grid.data = torch.from_numpy(synthetic.make_sdf(scene, R, seed=seed))[None, None].clone()
+        k0 = synthetic.make_k0(R, 12, seed=seed + 1)
+        model.k0.grid.data = k0.permute(3, 0, 1, 2)[None].contiguous(memory_format=torch.channels_last_3d)
+    model = model.to(device)
+    if precision == "bf16":
+        model.refresh_k0_shadow()
+    return model
+
+
+COARSE_RENDER_KWARGS = dict(near=0.1, far=6.0, bg=0, stepsize=0.5, inverse_y=True, flip_x=False, flip_y=False)
+
+
 def train_targets(n: int, seed: int = 0) -> np.ndarray:
     return np.random.default_rng(seed + 7).uniform(0, 1, size=(n, 3)).astype(np.float32)

@@ -757,6 +757,398 @@ __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P)
   }
 }
 
+// =============================================================================
+// Coarse model (lib/voxurf_coarse.py:513-619)
+//   sdf      : trilinear on the (smoothed) SDF grid
+//   gradient : trilinear on the central-difference gradient grid of the RAW
+//              SDF (neus_sdf_gradient, :323-332), stored [X,Y,Z,4]
+//   alpha    : as the fine model
+//   weights  : Alphas2Weights over all in-bbox samples (:540) only decides the
+//              weight > thres set; a second Alphas2Weights over that set
+//              (:550) gives the weights that are rendered and differentiated.
+// =============================================================================
+
+__device__ __forceinline__ void gather_grad4(const float* __restrict__ G4, const Corners& c, float g[3]) {
+  g[0] = g[1] = g[2] = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (c.off[q] < 0) continue;
+    const float4 v = __ldg(reinterpret_cast<const float4*>(G4) + c.off[q]);
+    g[0] += c.w[q] * v.x;
+    g[1] += c.w[q] * v.y;
+    g[2] += c.w[q] * v.z;
+  }
+}
+
+__device__ __forceinline__ void scatter_grad4(float* __restrict__ dG4, const Corners& c, const float d[3]) {
+  if (d[0] == 0.f && d[1] == 0.f && d[2] == 0.f) return;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (c.off[q] < 0 || c.w[q] == 0.f) continue;
+    red_add_v4(dG4 + 4 * (int64_t)c.off[q], c.w[q] * d[0], c.w[q] * d[1], c.w[q] * d[2], 0.f);
+  }
+}
+
+struct CoarseMarchParams {
+  MarchParams m;       // rays, frame, grids, mask, alpha constants, outputs
+  const float* G4;     // [X,Y,Z,4] gradient grid of the raw SDF
+  int* n2b;            // records up to the second scan's stop (backward range)
+};
+
+__global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) {
+  const MarchParams& P = C.m;
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  int64_t n_steps = f.n_steps;
+  if (n_steps > P.max_steps) {
+    if (lane == 0) set_device_error(P.err, VX_ERR_CAPACITY);
+    n_steps = P.max_steps;
+  }
+  const int64_t slot0 = (int64_t)r * P.max_steps;
+  double carry1 = 1.0, carry2 = 1.0, last2 = 1.0;
+  bool stop1 = false, stop2 = false;
+  int cnt = 0, cnt_b = 0;
+  for (int base = 0; base < n_steps && !stop1; base += 32) {
+    const int k = base + lane;
+    bool inb = false;
+    float alpha = 0.f;
+    if (k < n_steps) {
+      float p[3];
+      sample_point(f, P.stepdist, k, p);
+      inb = !outside_bbox(p, P.bmin, P.bmax);
+      if (inb && P.mask) inb = mask_hit(P, p);
+      if (inb) {
+        float ind[3], gr[3];
+        to_index(P.g, p, ind);
+        const Corners c = corners_of(P.g, ind[0], ind[1], ind[2]);
+        const float s = gather1(P.sdf, c);
+        gather_grad4(C.G4, c, gr);
+        alpha = neus_alpha(s, gr, v, P.inv_s, P.dist).alpha;
+      }
+    }
+    const unsigned in_mask = __ballot_sync(0xffffffffu, inb);
+    if (in_mask == 0u) continue;
+    // first scan: every in-bbox sample
+    const double f1 = inb ? 1.0 - (double)alpha : 1.0;
+    const double incl1 = warp_inclusive_prod(f1) * carry1;
+    double excl1 = __shfl_up_sync(0xffffffffu, incl1, 1);
+    if (lane == 0) excl1 = carry1;
+    const unsigned s1 = __ballot_sync(0xffffffffu, inb && incl1 < 1e-3);
+    unsigned live1 = in_mask;
+    if (s1) {
+      const int ks = __ffs(s1) - 1;
+      live1 &= (ks == 31) ? 0xffffffffu : ((2u << ks) - 1u);
+      stop1 = true;
+    } else {
+      carry1 = __shfl_sync(0xffffffffu, incl1, 31);
+    }
+    const float w1 = (float)excl1 * alpha;
+    const bool sel = ((live1 >> lane) & 1u) && (w1 > P.thres);
+    const unsigned sel_mask = __ballot_sync(0xffffffffu, sel);
+    if (sel_mask == 0u) continue;
+    // second scan: the selected samples only
+    float T2 = 1.f, w2 = 0.f;
+    unsigned live2 = 0u;
+    if (!stop2) {
+      const double f2 = sel ? 1.0 - (double)alpha : 1.0;
+      const double incl2 = warp_inclusive_prod(f2) * carry2;
+      double excl2 = __shfl_up_sync(0xffffffffu, incl2, 1);
+      if (lane == 0) excl2 = carry2;
+      const unsigned s2 = __ballot_sync(0xffffffffu, sel && incl2 < 1e-3);
+      live2 = sel_mask;
+      if (s2) {
+        const int ks = __ffs(s2) - 1;
+        live2 &= (ks == 31) ? 0xffffffffu : ((2u << ks) - 1u);
+        last2 = __shfl_sync(0xffffffffu, incl2, ks);
+        stop2 = true;
+      } else {
+        carry2 = __shfl_sync(0xffffffffu, incl2, 31);
+      }
+      if ((live2 >> lane) & 1u) {
+        T2 = (float)excl2;
+        w2 = T2 * alpha;
+      }
+    }
+    if (sel) {
+      const int64_t slot = slot0 + cnt + __popc(sel_mask & lt_mask);
+      const unsigned tag = (unsigned)k | 0x80000000u;
+      P.rec[slot] = make_float4(__uint_as_float(tag), alpha, T2, w2);
+      P.dw_slot[slot] = 0.f;
+    }
+    cnt += __popc(sel_mask);
+    cnt_b += __popc(live2);
+  }
+  if (lane == 0) {
+    P.n1[r] = cnt;
+    P.n2[r] = cnt;
+    C.n2b[r] = cnt_b;
+    P.alphainv_last[r] = (float)(stop2 ? last2 : carry2);
+  }
+}
+
+struct CoarseFeatParams {
+  int64_t n_rows;
+  const int* ray2;
+  const float* pts2;
+  const float* viewdirs;
+  GridGeom g;
+  const float* G4;
+  const float* k0f;
+  const __nv_bfloat16* k0h;
+  int use_k0, pos_pe, view_pe, geo_rgb_dim;
+  int ld;
+  void* X;
+  float* normal_out;  // [S2,3] interpolated gradient (unnormalised)
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128) features_coarse_kernel(CoarseFeatParams P) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= P.n_rows) return;
+  const int r = P.ray2[row];
+  const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
+  const float v[3] = {__ldg(P.viewdirs + 3 * r), __ldg(P.viewdirs + 3 * r + 1), __ldg(P.viewdirs + 3 * r + 2)};
+  float ind[3];
+  to_index(P.g, p, ind);
+  const Corners c = corners_of(P.g, ind[0], ind[1], ind[2]);
+  T* x = reinterpret_cast<T*>(P.X) + row * P.ld;
+  int col = 0;
+  if (P.use_k0) {
+    float k0v[12];
+    if (P.k0h)
+      gatherC<12>(P.k0h, c, k0v);
+    else
+      gatherC<12>(P.k0f, c, k0v);
+    for (int ch = 0; ch < 12; ++ch) put(x, col++, k0v[ch]);
+  }
+  float xyzn[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) xyzn[a] = (p[a] - P.g.mn[a]) / (P.g.mx[a] - P.g.mn[a]);
+  col = put_pe(x, col, xyzn, P.pos_pe);
+  col = put_pe(x, col, v, P.view_pe);
+  float gr[3];
+  gather_grad4(P.G4, c, gr);
+  if (P.geo_rgb_dim == 3) {
+    const float inv = 1.f / (sqrtf(gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]) + 1e-5f);
+    put(x, col++, gr[0] * inv);
+    put(x, col++, gr[1] * inv);
+    put(x, col++, gr[2] * inv);
+  }
+  if (P.normal_out) {
+    P.normal_out[3 * row + 0] = gr[0];
+    P.normal_out[3 * row + 1] = gr[1];
+    P.normal_out[3 * row + 2] = gr[2];
+  }
+}
+
+// rgb = clamp(sum w*sigmoid(logit) + (1 - sum w)*bg, 0, 1) (voxurf_coarse.py:575-584)
+struct CoarseCompositeParams {
+  int n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;
+  float bg;
+  float* rgb;
+  float* rgb_raw;
+  const float* normal2;
+  const int* step2;
+  float dist;
+  float* normal_out;
+  float* depth_out;
+  float* wsum_out;
+};
+
+__global__ void __launch_bounds__(256) composite_coarse_kernel(CoarseCompositeParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const int64_t b = P.s2_off[r], e = P.s2_off[r + 1];
+  float a0[3] = {0.f, 0.f, 0.f}, an[3] = {0.f, 0.f, 0.f}, ws = 0.f, dep = 0.f;
+  for (int64_t i = b + lane; i < e; i += 32) {
+    const float w = P.w2[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) a0[c] += w * sigmoidf_(P.logit[3 * i + c]);
+    ws += w;
+    if (P.normal2) {
+      const float nx = P.normal2[3 * i], ny = P.normal2[3 * i + 1], nz = P.normal2[3 * i + 2];
+      const float inv = 1.f / (sqrtf(nx * nx + ny * ny + nz * nz) + 1e-6f);
+      an[0] += w * nx * inv;
+      an[1] += w * ny * inv;
+      an[2] += w * nz * inv;
+    }
+    if (P.depth_out) dep += w * ((float)P.step2[i] * P.dist);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    a0[c] = warp_sum(a0[c]);
+    an[c] = warp_sum(an[c]);
+  }
+  ws = warp_sum(ws);
+  dep = warp_sum(dep);
+  if (lane == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float raw = a0[c] + (1.f - ws) * P.bg;
+      P.rgb_raw[3 * r + c] = raw;
+      P.rgb[3 * r + c] = fminf(fmaxf(raw, 0.f), 1.f);
+      if (P.normal_out) P.normal_out[3 * r + c] = an[c];
+    }
+    if (P.wsum_out) P.wsum_out[r] = ws;
+    if (P.depth_out) P.depth_out[r] = dep;
+  }
+}
+
+struct CoarseCompositeBwdParams {
+  int n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;
+  const float* rgb_raw;
+  const float* g_rgb;
+  float bg;
+  float* d_logit;
+  float* d_w2;
+};
+
+__global__ void __launch_bounds__(256) composite_coarse_bwd_kernel(CoarseCompositeBwdParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  float g[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float raw = P.rgb_raw[3 * r + c];
+    g[c] = (raw >= 0.f && raw <= 1.f) ? P.g_rgb[3 * r + c] : 0.f;
+  }
+  const float gbg = P.bg * (g[0] + g[1] + g[2]);
+  const int64_t b = P.s2_off[r], e = P.s2_off[r + 1];
+  for (int64_t i = b + lane; i < e; i += 32) {
+    const float w = P.w2[i];
+    float dw = -gbg;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float y = sigmoidf_(P.logit[3 * i + c]);
+      P.d_logit[3 * i + c] = (w * g[c]) * (1.f - y) * y;
+      dw += g[c] * y;
+    }
+    P.d_w2[i] = dw;
+  }
+}
+
+struct CoarseBwdParams {
+  GeomBwdParams gb;     // rays, frame, grid, sdf (smoothed), alpha constants, records
+  const int* n2b;       // backward range per ray
+  const float* G4;
+  float* dG4;           // [X,Y,Z,4] gradient of the gradient grid
+  // per-row feature backward
+  int64_t n_rows;
+  const float* pts2;
+  const int* slot2;
+  const float* dw2;
+  float* dw_slot;
+  int use_k0, pos_pe, view_pe, geo_rgb_dim, ld, in_bf16;
+  const void* dX;
+  float* d_k0;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128) features_coarse_bwd_kernel(CoarseBwdParams P) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= P.n_rows) return;
+  P.dw_slot[P.slot2[row]] = P.dw2[row];
+  const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
+  float ind[3];
+  to_index(P.gb.g, p, ind);
+  const Corners c = corners_of(P.gb.g, ind[0], ind[1], ind[2]);
+  const T* dx = reinterpret_cast<const T*>(P.dX) + row * P.ld;
+  if (P.use_k0) {
+    float dk0[12];
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) dk0[ch] = get(dx, ch);
+    scatterC<12>(P.d_k0, c, dk0);
+  }
+  if (P.geo_rgb_dim == 3) {
+    const int col = (P.use_k0 ? 12 : 0) + (3 + 6 * P.pos_pe) + (3 + 6 * P.view_pe);
+    float gr[3];
+    gather_grad4(P.G4, c, gr);
+    const float sn = sqrtf(gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
+    const float den = sn + 1e-5f;
+    const float dn[3] = {get(dx, col), get(dx, col + 1), get(dx, col + 2)};
+    const float gdn = gr[0] * dn[0] + gr[1] * dn[1] + gr[2] * dn[2];
+    const float corr = sn > 0.f ? gdn / (sn * den * den) : 0.f;
+    const float dg[3] = {dn[0] / den - gr[0] * corr, dn[1] / den - gr[1] * corr, dn[2] / den - gr[2] * corr};
+    scatter_grad4(P.dG4, c, dg);
+  }
+}
+
+__global__ void __launch_bounds__(256) geometry_coarse_bwd_kernel(CoarseBwdParams C) {
+  const GeomBwdParams& P = C.gb;
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const int n = C.n2b[r];
+  if (n == 0) return;
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  const int64_t slot0 = (int64_t)r * P.max_steps;
+  double carry = (double)(P.d_last[r] * P.alphainv_last[r]);
+  for (int top = n; top > 0; top -= 32) {
+    const int j = top - 32 + lane;
+    const bool valid = j >= 0;
+    float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float gw = 0.f;
+    if (valid) {
+      rc = P.rec[slot0 + j];
+      gw = P.dw_slot[slot0 + j];
+    }
+    const float alpha = rc.y, T = rc.z, w = rc.w;
+    const double term = valid ? (double)(gw * w) : 0.0;
+    const double suffix = warp_inclusive_suffix_sum(term);
+    double after = __shfl_down_sync(0xffffffffu, suffix, 1);
+    if (lane == 31) after = 0.0;
+    const double back = carry + after;
+    carry += __shfl_sync(0xffffffffu, suffix, 0);
+    if (!valid) continue;
+    const float d_alpha = (float)((double)(gw * T) - back / ((double)(1.f - alpha) + 1e-10));
+    if (d_alpha == 0.f) continue;
+    const int k = (int)(__float_as_uint(rc.x) & 0x7fffffffu);
+    float p[3], ind[3], gr[3];
+    sample_point(f, P.stepdist, k, p);
+    to_index(P.g, p, ind);
+    const Corners c = corners_of(P.g, ind[0], ind[1], ind[2]);
+    const float s = gather1(P.sdf, c);
+    gather_grad4(C.G4, c, gr);
+    const AlphaState a = neus_alpha(s, gr, v, P.inv_s, P.dist);
+    if (!(a.raw >= 0.f && a.raw <= 1.f)) continue;
+    const float den = a.P + 1e-5f;
+    const float dP = d_alpha * a.Q / (den * den);
+    const float dQ = -d_alpha / den;
+    const float d_prev = dP * a.P * a.nP * P.inv_s;
+    const float d_next = dQ * a.Q * a.nQ * P.inv_s;
+    const float d_ic = (d_next - d_prev) * P.dist * 0.5f;
+    const float d_cos = a.cosv < 0.f ? d_ic : 0.f;
+    scatter1(P.d_sdf, c, d_prev + d_next);
+    const float dg[3] = {d_cos * v[0], d_cos * v[1], d_cos * v[2]};
+    scatter_grad4(C.dG4, c, dg);
+  }
+}
+
 inline unsigned warp_blocks(int64_t n_items, int warps_per_block = 8) {
   return (unsigned)((n_items + warps_per_block - 1) / warps_per_block);
 }
@@ -1090,6 +1482,189 @@ int vx_fine_backward(const vx_fine_backward_args* A, void* stream) {
   G.d_last = A->d_last;
   G.d_sdf = A->d_sdf_smooth;
   geometry_fine_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, st>>>(G);
+  return launch_status();
+}
+
+// ---- coarse model ------------------------------------------------------------
+
+int vx_coarse_march(const vx_coarse_march_args* A, void* stream) {
+  if (!A) return VX_ERR_ARG;
+  const vx_fine_march_args* M = &A->march;
+  if (M->n_rays < 0 || M->max_steps <= 0) return VX_ERR_ARG;
+  if (M->n_rays == 0) return VX_OK;
+  if (!M->rays_o || !M->rays_d || !M->viewdirs || !M->sdf_smooth || !A->grad4 || !M->rec || !M->dw_slot ||
+      !M->n1 || !M->n2 || !A->n2b || !M->alphainv_last)
+    return VX_ERR_ARG;
+  if ((int64_t)M->n_rays * M->max_steps > INT32_MAX || (((uintptr_t)A->grad4) & 15)) return VX_ERR_ARG;
+  CoarseMarchParams C;
+  MarchParams& P = C.m;
+  P.rays_o = M->rays_o;
+  P.rays_d = M->rays_d;
+  P.viewdirs = M->viewdirs;
+  P.n_rays = (int)M->n_rays;
+  P.near = M->near;
+  P.stepdist = M->stepdist;
+  for (int a = 0; a < 3; ++a) {
+    P.bmin[a] = M->grid.xyz_min[a];
+    P.bmax[a] = M->grid.xyz_max[a];
+    P.mscale[a] = M->mask_scale[a];
+    P.mshift[a] = M->mask_shift[a];
+  }
+  P.g = geom_from(&M->grid);
+  P.sdf = M->sdf_smooth;
+  P.voxel_size = M->voxel_size;
+  P.mask = M->mask;
+  P.mX = (int)M->mask_X;
+  P.mY = (int)M->mask_Y;
+  P.mZ = (int)M->mask_Z;
+  P.inv_s = M->inv_s;
+  P.dist = M->dist;
+  P.thres = M->fast_color_thres;
+  P.max_steps = (int)M->max_steps;
+  P.rec = reinterpret_cast<float4*>(M->rec);
+  P.dw_slot = M->dw_slot;
+  P.n1 = M->n1;
+  P.n2 = M->n2;
+  P.alphainv_last = M->alphainv_last;
+  P.err = device_error_ptr();
+  C.G4 = A->grad4;
+  C.n2b = A->n2b;
+  march_coarse_kernel<<<warp_blocks(M->n_rays), 256, 0, as_stream(stream)>>>(C);
+  return launch_status();
+}
+
+static int64_t coarse_cols(const vx_coarse_feature_cfg* c) {
+  return (c->use_k0 ? 12 : 0) + (3 + 6 * c->posbase_pe) + (3 + 6 * c->viewbase_pe) + (c->geo_rgb_dim == 3 ? 3 : 0);
+}
+
+static bool coarse_cfg_ok(const vx_coarse_feature_cfg* c) {
+  return c->posbase_pe >= 0 && c->posbase_pe <= 16 && c->viewbase_pe >= 0 && c->viewbase_pe <= 16 &&
+         (c->geo_rgb_dim == 0 || c->geo_rgb_dim == 3);
+}
+
+int vx_coarse_features(const vx_coarse_features_args* A, void* stream) {
+  if (!A || A->n_rows < 0 || !coarse_cfg_ok(&A->cfg)) return VX_ERR_ARG;
+  if (A->n_rows == 0) return VX_OK;
+  if (A->ld != coarse_cols(&A->cfg) || !A->X || !A->grad4 || (A->cfg.use_k0 && !A->k0_f32 && !A->k0_bf16))
+    return VX_ERR_ARG;
+  CoarseFeatParams P;
+  P.n_rows = A->n_rows;
+  P.ray2 = A->ray2;
+  P.pts2 = A->pts2;
+  P.viewdirs = A->viewdirs;
+  P.g = geom_from(&A->grid);
+  P.G4 = A->grad4;
+  P.k0f = A->k0_f32;
+  P.k0h = reinterpret_cast<const __nv_bfloat16*>(A->k0_bf16);
+  P.use_k0 = A->cfg.use_k0;
+  P.pos_pe = (int)A->cfg.posbase_pe;
+  P.view_pe = (int)A->cfg.viewbase_pe;
+  P.geo_rgb_dim = A->cfg.geo_rgb_dim;
+  P.ld = (int)A->ld;
+  P.X = A->X;
+  P.normal_out = A->normal_out;
+  const unsigned b = (unsigned)((A->n_rows + 127) / 128);
+  if (A->out_bf16)
+    features_coarse_kernel<__nv_bfloat16><<<b, 128, 0, as_stream(stream)>>>(P);
+  else
+    features_coarse_kernel<float><<<b, 128, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_coarse_composite(const vx_coarse_composite_args* A, void* stream) {
+  if (!A || A->n_rays < 0) return VX_ERR_ARG;
+  if (A->n_rays == 0) return VX_OK;
+  CoarseCompositeParams P;
+  P.n_rays = (int)A->n_rays;
+  P.s2_off = A->s2_off;
+  P.w2 = A->w2;
+  P.logit = A->logit;
+  P.bg = A->bg;
+  P.rgb = A->rgb;
+  P.rgb_raw = A->rgb_raw;
+  P.normal2 = A->normal2;
+  P.step2 = A->step2;
+  P.dist = A->dist;
+  P.normal_out = A->normal_out;
+  P.depth_out = A->depth_out;
+  P.wsum_out = A->wsum_out;
+  composite_coarse_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_coarse_composite_backward(const vx_coarse_composite_bwd_args* A, void* stream) {
+  if (!A || A->n_rays < 0) return VX_ERR_ARG;
+  if (A->n_rays == 0) return VX_OK;
+  CoarseCompositeBwdParams P;
+  P.n_rays = (int)A->n_rays;
+  P.s2_off = A->s2_off;
+  P.w2 = A->w2;
+  P.logit = A->logit;
+  P.rgb_raw = A->rgb_raw;
+  P.g_rgb = A->g_rgb;
+  P.bg = A->bg;
+  P.d_logit = A->d_logit;
+  P.d_w2 = A->d_w2;
+  composite_coarse_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_coarse_backward(const vx_coarse_backward_args* A, void* stream) {
+  if (!A || A->n_rays < 0 || A->n_rows < 0 || !coarse_cfg_ok(&A->cfg)) return VX_ERR_ARG;
+  if (A->n_rows > 0 && A->ld != coarse_cols(&A->cfg)) return VX_ERR_ARG;
+  if ((((uintptr_t)A->grad4) | ((uintptr_t)A->d_grad4)) & 15) return VX_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  CoarseBwdParams C;
+  GeomBwdParams& G = C.gb;
+  G.rays_o = A->rays_o;
+  G.rays_d = A->rays_d;
+  G.viewdirs = A->viewdirs;
+  G.n_rays = (int)A->n_rays;
+  G.near = A->near;
+  G.stepdist = A->stepdist;
+  for (int a = 0; a < 3; ++a) {
+    G.bmin[a] = A->grid.xyz_min[a];
+    G.bmax[a] = A->grid.xyz_max[a];
+  }
+  G.g = geom_from(&A->grid);
+  G.sdf = A->sdf_smooth;
+  G.voxel_size = A->voxel_size;
+  G.inv_s = A->inv_s;
+  G.dist = A->dist;
+  G.max_steps = (int)A->max_steps;
+  G.rec = reinterpret_cast<const float4*>(A->rec);
+  G.dw_slot = A->dw_slot;
+  G.n1 = A->n2b;
+  G.alphainv_last = A->alphainv_last;
+  G.d_last = A->d_last;
+  G.d_sdf = A->d_sdf_smooth;
+  C.n2b = A->n2b;
+  C.G4 = A->grad4;
+  C.dG4 = A->d_grad4;
+  C.n_rows = A->n_rows;
+  C.pts2 = A->pts2;
+  C.slot2 = A->slot2;
+  C.dw2 = A->dw2;
+  C.dw_slot = A->dw_slot;
+  C.use_k0 = A->cfg.use_k0;
+  C.pos_pe = (int)A->cfg.posbase_pe;
+  C.view_pe = (int)A->cfg.viewbase_pe;
+  C.geo_rgb_dim = A->cfg.geo_rgb_dim;
+  C.ld = (int)A->ld;
+  C.in_bf16 = A->in_bf16;
+  C.dX = A->dX;
+  C.d_k0 = A->d_k0;
+  if (A->n_rows > 0) {
+    const unsigned b = (unsigned)((A->n_rows + 127) / 128);
+    if (A->in_bf16)
+      features_coarse_bwd_kernel<__nv_bfloat16><<<b, 128, 0, st>>>(C);
+    else
+      features_coarse_bwd_kernel<float><<<b, 128, 0, st>>>(C);
+    int s = launch_status();
+    if (s) return s;
+  }
+  if (A->n_rays == 0) return VX_OK;
+  geometry_coarse_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, st>>>(C);
   return launch_status();
 }
 
