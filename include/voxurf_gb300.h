@@ -136,6 +136,14 @@ int vx_adam_upd_with_perlr(float* param, const float* grad, float* exp_avg, floa
 int vx_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq, const float* per_lr, int64_t n,
                  double lr, double beta1, double beta2, double eps, int64_t step, int zero_grad, void* stream);
 
+/* Colour-MLP backward helper (rgbnet/k_rgbnet ReLU stacks,
+ * lib/voxurf_fine.py:132-187): dz = dh * (h > 0) and colsum += sum over rows
+ * of dz (the bias gradient), one pass; h == NULL skips the ReLU (bias
+ * gradient of the last layer).  dtype 0: float32, 1: bfloat16 for dh/h/dz;
+ * colsum [N] FP32, accumulated. */
+int vx_relu_bwd_colsum(const void* dh, const void* h, int64_t M, int64_t N, int dtype, void* dz, float* colsum,
+                       void* stream);
+
 /* Fused dense grid sweep: DenseGrid.total_variation_add_grad(w, w, w, dense)
  * (lib/grid.py:67-78; voxurf_fine.py:403-409; total_variation_kernel.cu:14-36)
  * followed by the utils.Adam update and the gradient reset, in one pass.

@@ -143,6 +143,19 @@ class OracleFine(nn.Module):
     def smoothed(self):
         return smooth3d(self.sdf_grid, self.kernel) if self.smooth_sdf else self.sdf_grid
 
+    def smooth_grad_tv(self, nonempty_mask, weight):
+        """density_total_variation(smooth_grad_tv=weight), voxurf_fine.py:417-420,
+        with tv_smooth_conv = the normalised [1,2,1]^3 kernel (:237-242, sigma 0)
+        and replicate padding."""
+        grad = neus_sdf_gradient(self.sdf_grid, self.voxel_size).permute(1, 0, 2, 3, 4)
+        k1 = torch.tensor([1.0, 2.0, 1.0], dtype=self.dtype)
+        k = (k1[:, None, None] * k1[None, :, None] * k1[None, None, :]) / 64.0
+        sm = F.conv3d(F.pad(grad, (1, 1, 1, 1, 1, 1), mode="replicate"), k[None, None])
+        err = (sm.detach() - grad)
+        if nonempty_mask is not None:
+            err = err[nonempty_mask.cpu().repeat(3, 1, 1, 1, 1)]
+        return (err ** 2).mean() * weight
+
     def forward(self, rays_o, rays_d, viewdirs, global_step=None, **rk):
         dt = self.dtype
         N = len(rays_o)

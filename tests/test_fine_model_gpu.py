@@ -105,3 +105,17 @@ def test_fine_forward_no_rays_hit(cuda):
     assert ret["weights"].numel() == 0
     assert torch.all(ret["alphainv_cum"] == 1)
     assert torch.all(ret["rgb_marched"] == 0)
+
+
+@pytest.mark.parametrize("masked", [True, False])
+def test_smooth_grad_tv_matches_oracle(cuda, masked):
+    """density_total_variation(smooth_grad_tv) (voxurf_fine.py:417-420): value
+    and SDF-grid gradient against the FP64 restatement."""
+    model = configs.build_fine_model(24, device=cuda, seed=5, mask_voxels=4.0 if masked else None)
+    oracle = OracleFine(model, dtype=torch.float64)
+    loss = model.density_total_variation(smooth_grad_tv=0.05)
+    loss.backward()
+    ol = oracle.smooth_grad_tv(model.nonempty_mask, 0.05)
+    ol.backward()
+    assert abs(loss.item() - ol.item()) <= 1e-5 * abs(ol.item())
+    assert _rel_l2(model.sdf.grid.grad, oracle.sdf_grid.grad) <= 1e-5

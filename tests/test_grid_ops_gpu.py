@@ -133,3 +133,30 @@ def test_fused_grid_tv_adam(cuda, C, R, dense):
     # the shadow is the round-to-nearest BF16 copy of the kernel's own FP32 result
     torch.testing.assert_close(shadow.float(), gout.bfloat16().float(), rtol=0, atol=0)
     assert torch.count_nonzero(gg) == 0
+
+
+@pytest.mark.parametrize("dense", [True, False])
+def test_row_sweep_bit_identical_to_generic_sweep(cuda, dense):
+    """The row-structured sweep (channel-last, 12 channels) and the generic
+    sweep (channel-first) apply the same operations in the same order."""
+    C, X, Y, Z = 12, 9, 14, 20
+    rng = np.random.default_rng(int(dense))
+    p = rng.normal(size=(C, X, Y, Z)).astype(np.float32)
+    g = rng.normal(scale=1e-3, size=p.shape).astype(np.float32)
+    g[rng.uniform(size=g.shape) < 0.4] = 0
+    m = rng.normal(scale=1e-3, size=p.shape).astype(np.float32)
+    v = rng.uniform(size=p.shape).astype(np.float32) * 1e-5
+    outs = []
+    for cl in (0, 1):
+        conv = (lambda a: np.ascontiguousarray(a.transpose(1, 2, 3, 0))) if cl else (lambda a: a.copy())
+        T = lambda a: torch.from_numpy(conv(a)).to(cuda)
+        pin, gg, gm, gv = T(p), T(g), T(m), T(v)
+        pout = torch.empty_like(pin)
+        _native.call("vx_grid_tv_adam_step", ptr(pin), ptr(pout), ptr(gg), ptr(gm), ptr(gv), None, None, C, X, Y, Z,
+                     cl, 1, 0.07, int(dense), 1e-2, 0.9, 0.99, 1e-8, 2, 0, stream_ptr())
+        res = [pout, gm, gv]
+        if cl:
+            res = [r.permute(3, 0, 1, 2) for r in res]
+        outs.append([r.cpu() for r in res])
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)

@@ -1,0 +1,55 @@
+"""Colour-MLP forward/backward (cuBLAS GEMMs + fused ReLU-backward/bias-grad
+kernel) against plain torch autograd of the reference nn.Sequential."""
+import pytest
+import torch
+import torch.nn as nn
+
+from voxurf_gb300.mlp import apply_mlp
+
+pytestmark = pytest.mark.gpu
+
+
+def _net(d_in, width, depth, seed):
+    torch.manual_seed(seed)
+    return nn.Sequential(nn.Linear(d_in, width), nn.ReLU(inplace=True),
+                         *[nn.Sequential(nn.Linear(width, width), nn.ReLU(inplace=True)) for _ in range(depth - 2)],
+                         nn.Linear(width, 3))
+
+
+@pytest.mark.parametrize("M,d_in,width,depth", [(3000, 70, 192, 4), (1037, 60, 192, 4), (513, 75, 128, 3), (0, 70, 64, 3)])
+def test_mlp_fp32_matches_autograd(cuda, M, d_in, width, depth):
+    net = _net(d_in, width, depth, M).to(cuda).double()
+    x = torch.randn(M, d_in, device=cuda, dtype=torch.float64, requires_grad=True)
+    gy = torch.randn(M, 3, device=cuda, dtype=torch.float64)
+    y_ref = net(x)
+    (y_ref * gy).sum().backward()
+    ref = [x.grad.clone()] + [p.grad.clone() for p in net.parameters()]
+    net32 = net.float()
+    for p in net32.parameters():
+        p.grad = None
+    x32 = x.detach().float().requires_grad_(True)
+    y = apply_mlp(net32, x32)
+    (y * gy.float()).sum().backward()
+    got = [x32.grad] + [p.grad for p in net32.parameters()]
+    assert torch.allclose(y.double(), y_ref.detach(), rtol=1e-5, atol=1e-5)
+    for g, r in zip(got, ref):
+        assert g.dtype == torch.float32
+        if r.numel():
+            assert float((g.double() - r).norm() / (r.norm() + 1e-30)) < 1e-5
+
+
+def test_mlp_bf16_close_to_fp32(cuda):
+    net = _net(70, 192, 4, 0).to(cuda)
+    x = torch.randn(4096, 70, device=cuda)
+    gy = torch.randn(4096, 3, device=cuda)
+    y32 = apply_mlp(net, x)
+    (y32 * gy).sum().backward()
+    g32 = [p.grad.clone() for p in net.parameters()]
+    for p in net.parameters():
+        p.grad = None
+    y16 = apply_mlp(net, x.bfloat16()).float()
+    (y16 * gy).sum().backward()
+    assert float((y16 - y32).abs().max()) < 5e-2
+    for p, r in zip(net.parameters(), g32):
+        assert p.grad.dtype == torch.float32
+        assert float((p.grad - r).norm() / r.norm()) < 5e-2

@@ -249,6 +249,105 @@ __global__ void __launch_bounds__(256) grid_tv_adam_kernel(const float* __restri
   }
 }
 
+// Row-structured variant of the fused sweep for the layouts the models use:
+// channel-last with C % 4 == 0 (k0, C = 12) and single-channel grids (sdf).
+// One CTA per (i, j) row: blockIdx.x = j, blockIdx.y = i, threads walk the
+// row's Z*C/4 float4 quads, so (i, j, k, c) need no integer division and
+// every TV neighbour is one float4 load (k +- 1 from the same row through
+// L1, j +- 1 and i +- 1 from rows other CTAs are streaming through L2).
+// Same operation order as grid_tv_adam_kernel, hence bit-identical results.
+template <int C>
+__device__ __forceinline__ float4 ld4(const float* __restrict__ p, int64_t q) {
+  return __ldg(reinterpret_cast<const float4*>(p) + q);
+}
+
+__device__ __forceinline__ float tv1(float c, float n, float w) { return fmul(w, clamp1(fsub(c, n))); }
+
+template <int C, bool TV, bool DENSE, bool SHADOW>
+__global__ void __launch_bounds__(256) grid_tv_adam_row_kernel(const float* __restrict__ param_in,
+                                                              float* __restrict__ param_out,
+                                                              float* __restrict__ grad,
+                                                              float* __restrict__ exp_avg,
+                                                              float* __restrict__ exp_avg_sq,
+                                                              const float* __restrict__ per_lr,
+                                                              __nv_bfloat16* __restrict__ shadow, int X, int Y,
+                                                              int Z, float wk, float wj, float wi, AdamParams a,
+                                                              int zero_grad) {
+  const int j = blockIdx.x, i = blockIdx.y;
+  const int row_q = Z * C / 4;  // float4 quads per row
+  const int64_t row0 = ((int64_t)i * Y + j) * row_q;
+  const int64_t sj = row_q, si = (int64_t)Y * row_q;
+  const bool h = per_lr != nullptr;
+  for (int t = threadIdx.x; t < row_q; t += blockDim.x) {
+    const int64_t q = row0 + t;
+    const float4 p = ld4<C>(param_in, q);
+    float4 gr = reinterpret_cast<const float4*>(grad)[q];
+    float gv[4] = {gr.x, gr.y, gr.z, gr.w};
+    const float pv[4] = {p.x, p.y, p.z, p.w};
+    if (TV) {
+      // neighbours of the 4 elements along each axis
+      float km[4], kp[4];
+      int kk[4];
+      if (C == 1) {
+        const float4 L = t > 0 ? ld4<C>(param_in, q - 1) : p;
+        const float4 Rr = t < row_q - 1 ? ld4<C>(param_in, q + 1) : p;
+        km[0] = L.w; km[1] = p.x; km[2] = p.y; km[3] = p.z;
+        kp[0] = p.y; kp[1] = p.z; kp[2] = p.w; kp[3] = Rr.x;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) kk[e] = 4 * t + e;
+      } else {
+        constexpr int QPV = C >= 4 ? C / 4 : 1;  // float4 quads per voxel
+        const int k = t / QPV;
+        const float4 L = k > 0 ? ld4<C>(param_in, q - QPV) : p;
+        const float4 Rr = k < Z - 1 ? ld4<C>(param_in, q + QPV) : p;
+        km[0] = L.x; km[1] = L.y; km[2] = L.z; km[3] = L.w;
+        kp[0] = Rr.x; kp[1] = Rr.y; kp[2] = Rr.z; kp[3] = Rr.w;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) kk[e] = k;
+      }
+      const float4 jm = j > 0 ? ld4<C>(param_in, q - sj) : p;
+      const float4 jp = j < Y - 1 ? ld4<C>(param_in, q + sj) : p;
+      const float4 im = i > 0 ? ld4<C>(param_in, q - si) : p;
+      const float4 ip = i < X - 1 ? ld4<C>(param_in, q + si) : p;
+      const float jmv[4] = {jm.x, jm.y, jm.z, jm.w}, jpv[4] = {jp.x, jp.y, jp.z, jp.w};
+      const float imv[4] = {im.x, im.y, im.z, im.w}, ipv[4] = {ip.x, ip.y, ip.z, ip.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (!(DENSE || gv[e] != 0.f)) continue;
+        const float c = pv[e];
+        float s = 0.f;
+        s = fadd(s, kk[e] == 0 ? 0.f : tv1(c, km[e], wk));
+        s = fadd(s, kk[e] == Z - 1 ? 0.f : tv1(c, kp[e], wk));
+        s = fadd(s, j == 0 ? 0.f : tv1(c, jmv[e], wj));
+        s = fadd(s, j == Y - 1 ? 0.f : tv1(c, jpv[e], wj));
+        s = fadd(s, i == 0 ? 0.f : tv1(c, imv[e], wi));
+        s = fadd(s, i == X - 1 ? 0.f : tv1(c, ipv[e], wi));
+        gv[e] = fadd(gv[e], s);
+      }
+    }
+    float4 m = reinterpret_cast<const float4*>(exp_avg)[q];
+    float4 v = reinterpret_cast<const float4*>(exp_avg_sq)[q];
+    const float4 l = h ? ld4<C>(per_lr, q) : make_float4(1.f, 1.f, 1.f, 1.f);
+    float mv[4] = {m.x, m.y, m.z, m.w}, vv[4] = {v.x, v.y, v.z, v.w};
+    const float lv[4] = {l.x, l.y, l.z, l.w};
+    float out[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) out[e] = adam_update(pv[e], gv[e], mv[e], vv[e], lv[e], h, a);
+    reinterpret_cast<float4*>(param_out)[q] = make_float4(out[0], out[1], out[2], out[3]);
+    reinterpret_cast<float4*>(exp_avg)[q] = make_float4(mv[0], mv[1], mv[2], mv[3]);
+    reinterpret_cast<float4*>(exp_avg_sq)[q] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+    if (zero_grad) reinterpret_cast<float4*>(grad)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (SHADOW) {
+      __nv_bfloat162 lo = __floats2bfloat162_rn(out[0], out[1]);
+      __nv_bfloat162 hi = __floats2bfloat162_rn(out[2], out[3]);
+      uint2 packed;
+      packed.x = *reinterpret_cast<uint32_t*>(&lo);
+      packed.y = *reinterpret_cast<uint32_t*>(&hi);
+      reinterpret_cast<uint2*>(shadow)[q] = packed;
+    }
+  }
+}
+
 inline unsigned sweep_blocks(int64_t work_items) {
   // Persistent-style grid: a multiple of the SM count, capped by the work.
   const int64_t per_wave = (int64_t)sm_count() * 8;  // 8 x 256-thread CTAs per SM
@@ -388,6 +487,36 @@ int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, f
   const int64_t n = C * X * Y * Z;
   cudaStream_t st = as_stream(stream);
   __nv_bfloat16* sh = reinterpret_cast<__nv_bfloat16*>(shadow_bf16);
+  // Row-structured kernel for k0 (channel-last, 12 channels) and 1-channel grids.
+  const bool row_c12 = channel_last && C == 12;
+  const bool row_c1 = C == 1 && (Z % 4) == 0;
+  if ((row_c12 || row_c1) && X <= 65535 && Y <= 2147483647LL && Z * C <= (1LL << 30)) {
+    const int row_q = (int)(Z * C / 4);
+    const int threads = row_q >= 256 ? 256 : ((row_q + 31) / 32) * 32;
+    dim3 grid((unsigned)Y, (unsigned)X);
+#define VX_ROW(CC, TV, DENSE, SH)                                                                             \
+  grid_tv_adam_row_kernel<CC, TV, DENSE, SH><<<grid, threads, 0, st>>>(param_in, param_out, grad, exp_avg,       \
+                                                                      exp_avg_sq, per_lr, sh, (int)X, (int)Y,   \
+                                                                      (int)Z, w6, w6, w6, a, zero_grad)
+#define VX_ROW_C(CC)                                                                                          \
+  if (tv_enabled) {                                                                                           \
+    if (tv_dense_mode) {                                                                                      \
+      if (sh) VX_ROW(CC, true, true, true); else VX_ROW(CC, true, true, false);                               \
+    } else {                                                                                                  \
+      if (sh) VX_ROW(CC, true, false, true); else VX_ROW(CC, true, false, false);                             \
+    }                                                                                                         \
+  } else {                                                                                                    \
+    if (sh) VX_ROW(CC, false, false, true); else VX_ROW(CC, false, false, false);                             \
+  }
+    if (row_c12) {
+      VX_ROW_C(12)
+    } else {
+      VX_ROW_C(1)
+    }
+#undef VX_ROW_C
+#undef VX_ROW
+    return launch_status();
+  }
   const unsigned b = sweep_blocks((n + 3) / 4);
 #define VX_LAUNCH_TVA(TV, DENSE, SH) \
   grid_tv_adam_kernel<TV, DENSE, SH><<<b, 256, 0, st>>>(param_in, param_out, grad, exp_avg, exp_avg_sq, per_lr, sh, \

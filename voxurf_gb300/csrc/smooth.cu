@@ -67,6 +67,116 @@ __global__ void smooth_axis_kernel(const float* __restrict__ in, float* __restri
   }
 }
 
+// ---- single-pass tiled version ----------------------------------------------
+// One CTA computes an 8 x 8 x 16 output tile: it stages the input tile plus a
+// 2-voxel halo (12 x 12 x 20) in shared memory and applies the three 1-D
+// passes there (z, then y, then x), so each voxel is read from DRAM about
+// once and written once.  Forward: the halo is read at clamped coordinates
+// (replicate padding).  Adjoint: the halo outside the grid is zero and each
+// axis applies the adjoint of the clamped 1-D convolution (boundary voxels
+// collect the taps that the forward clamped onto them).
+constexpr int TX = 8, TY = 8, TZ = 16, HALO = 2;
+constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO, SZ = TZ + 2 * HALO;
+
+// Adjoint of one clamped 1-D convolution at output position j of an axis of
+// length n, reading the gradient through get(i) for i in [j-h, j+h] (zero
+// outside [0, n)).
+template <typename Get>
+__device__ __forceinline__ float adjoint1d(const Taps& t, int j, int n, Get get) {
+  float acc = 0.f;
+  if (n == 1) {
+    float s = 0.f;
+    for (int tt = -t.h; tt <= t.h; ++tt) s += t.w[tt + t.h];
+    return s * get(0);
+  }
+  if (j == 0) {
+    for (int i = 0; i <= t.h && i < n; ++i) {
+      float s = 0.f;
+      for (int tt = -t.h; tt <= -i; ++tt) s += t.w[tt + t.h];
+      acc += s * get(i);
+    }
+  } else if (j == n - 1) {
+    for (int i = (n - 1 - t.h > 0 ? n - 1 - t.h : 0); i < n; ++i) {
+      float s = 0.f;
+      for (int tt = n - 1 - i; tt <= t.h; ++tt) s += t.w[tt + t.h];
+      acc += s * get(i);
+    }
+  } else {
+    for (int tt = -t.h; tt <= t.h; ++tt) {
+      const int i = j - tt;
+      if (i >= 0 && i < n) acc += t.w[tt + t.h] * get(i);
+    }
+  }
+  return acc;
+}
+
+template <bool ADJOINT, bool ACCUM>
+__global__ void __launch_bounds__(256) smooth_tile_kernel(const float* __restrict__ in, float* __restrict__ out,
+                                                         int X, int Y, int Z, Taps t) {
+  __shared__ float s_in[SX][SY][SZ];
+  __shared__ float s_z[SX][SY][TZ];
+  __shared__ float s_y[SX][TY][TZ];
+  const int x0 = blockIdx.z * TX, y0 = blockIdx.y * TY, z0 = blockIdx.x * TZ;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < SX * SY * SZ; e += blockDim.x) {
+    const int c = e % SZ, b = (e / SZ) % SY, a = e / (SZ * SY);
+    int gx = x0 + a - HALO, gy = y0 + b - HALO, gz = z0 + c - HALO;
+    float v;
+    if (!ADJOINT) {
+      gx = min(max(gx, 0), X - 1);
+      gy = min(max(gy, 0), Y - 1);
+      gz = min(max(gz, 0), Z - 1);
+      v = in[((int64_t)gx * Y + gy) * Z + gz];
+    } else {
+      const bool inside = gx >= 0 && gx < X && gy >= 0 && gy < Y && gz >= 0 && gz < Z;
+      v = inside ? in[((int64_t)gx * Y + gy) * Z + gz] : 0.f;
+    }
+    s_in[a][b][c] = v;
+  }
+  __syncthreads();
+  // z pass over all (a, b) of the halo'd tile
+  for (int e = tid; e < SX * SY * TZ; e += blockDim.x) {
+    const int c = e % TZ, b = (e / TZ) % SY, a = e / (TZ * SY);
+    float acc = 0.f;
+    if (!ADJOINT) {
+      for (int tt = -t.h; tt <= t.h; ++tt) acc += t.w[tt + t.h] * s_in[a][b][c + HALO + tt];
+    } else {
+      const int gz = z0 + c;
+      acc = adjoint1d(t, gz, Z, [&](int i) { return s_in[a][b][i - z0 + HALO]; });
+    }
+    s_z[a][b][c] = acc;
+  }
+  __syncthreads();
+  for (int e = tid; e < SX * TY * TZ; e += blockDim.x) {
+    const int c = e % TZ, b = (e / TZ) % TY, a = e / (TZ * TY);
+    float acc = 0.f;
+    if (!ADJOINT) {
+      for (int tt = -t.h; tt <= t.h; ++tt) acc += t.w[tt + t.h] * s_z[a][b + HALO + tt][c];
+    } else {
+      const int gy = y0 + b;
+      acc = adjoint1d(t, gy, Y, [&](int i) { return s_z[a][i - y0 + HALO][c]; });
+    }
+    s_y[a][b][c] = acc;
+  }
+  __syncthreads();
+  for (int e = tid; e < TX * TY * TZ; e += blockDim.x) {
+    const int c = e % TZ, b = (e / TZ) % TY, a = e / (TZ * TY);
+    const int gx = x0 + a, gy = y0 + b, gz = z0 + c;
+    if (gx >= X || gy >= Y || gz >= Z) continue;
+    float acc = 0.f;
+    if (!ADJOINT) {
+      for (int tt = -t.h; tt <= t.h; ++tt) acc += t.w[tt + t.h] * s_y[a + HALO + tt][b][c];
+    } else {
+      acc = adjoint1d(t, gx, X, [&](int i) { return s_y[i - x0 + HALO][b][c]; });
+    }
+    const int64_t o = ((int64_t)gx * Y + gy) * Z + gz;
+    if (ACCUM)
+      out[o] += acc;
+    else
+      out[o] = acc;
+  }
+}
+
 static unsigned pass_blocks(int64_t n) {
   int64_t b = (n + 255) / 256;
   const int64_t cap = (int64_t)sm_count() * 16;
@@ -88,6 +198,11 @@ int vx_smooth3d(const float* in, float* out, float* tmp1, float* tmp2, int64_t X
   t.h = ksize / 2;
   for (int i = 0; i < 9; ++i) t.w[i] = i < ksize ? taps_host[i] : 0.f;
   cudaStream_t st = as_stream(stream);
+  if (t.h <= HALO) {
+    dim3 grid((unsigned)((Z + TZ - 1) / TZ), (unsigned)((Y + TY - 1) / TY), (unsigned)((X + TX - 1) / TX));
+    smooth_tile_kernel<false, false><<<grid, 256, 0, st>>>(in, out, (int)X, (int)Y, (int)Z, t);
+    return launch_status();
+  }
   const unsigned b = pass_blocks(X * Y * Z);
   smooth_axis_kernel<false, false><<<b, 256, 0, st>>>(in, tmp1, (int)X, (int)Y, (int)Z, 0, t);
   int s = launch_status();
@@ -108,6 +223,14 @@ int vx_smooth3d_adjoint(const float* grad_out, float* grad_in, float* tmp1, floa
   t.h = ksize / 2;
   for (int i = 0; i < 9; ++i) t.w[i] = i < ksize ? taps_host[i] : 0.f;
   cudaStream_t st = as_stream(stream);
+  if (t.h <= HALO) {
+    dim3 grid((unsigned)((Z + TZ - 1) / TZ), (unsigned)((Y + TY - 1) / TY), (unsigned)((X + TX - 1) / TX));
+    if (accumulate)
+      smooth_tile_kernel<true, true><<<grid, 256, 0, st>>>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t);
+    else
+      smooth_tile_kernel<true, false><<<grid, 256, 0, st>>>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t);
+    return launch_status();
+  }
   const unsigned b = pass_blocks(X * Y * Z);
   smooth_axis_kernel<true, false><<<b, 256, 0, st>>>(grad_out, tmp1, (int)X, (int)Y, (int)Z, 2, t);
   int s = launch_status();

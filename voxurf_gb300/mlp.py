@@ -1,0 +1,76 @@
+"""Colour-MLP forward/backward for rgbnet / k_rgbnet (lib/voxurf_fine.py:
+132-187, lib/voxurf_coarse.py:116-123): Linear -> ReLU stacks applied to the
+feature rows written by the feature kernels.
+
+The GEMMs are cuBLAS calls (FP32, or BF16 with FP32 accumulation); the
+hidden layers use cuBLASLt's bias+ReLU epilogue (torch._addmm_activation);
+the backward fuses ReLU-backward with the bias gradient in one sm_103a pass
+(vx_relu_bwd_colsum) instead of torch's threshold_backward plus a strided
+column reduction.  Parameters stay FP32 masters; in BF16 mode they are cast
+per call and the weight gradients are returned in FP32.
+"""
+from __future__ import annotations
+
+import torch
+import torch.nn as nn
+
+from ._torch import call, ptr, stream_ptr
+
+
+def _colsum(dh: torch.Tensor, h: torch.Tensor | None, dz: torch.Tensor | None) -> torch.Tensor:
+    M, N = dh.shape
+    out = torch.zeros(N, dtype=torch.float32, device=dh.device)
+    dtype = 1 if dh.dtype == torch.bfloat16 else 0
+    call("vx_relu_bwd_colsum", ptr(dh), ptr(h), M, N, dtype, ptr(dz), ptr(out), stream_ptr())
+    return out
+
+
+class _MLP(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, *params):
+        n = len(params) // 2
+        dt = x.dtype
+        Ws = [params[2 * i].detach().to(dt) for i in range(n)]
+        bs = [params[2 * i + 1].detach().to(dt) for i in range(n)]
+        hs = [x]
+        h = x
+        for i in range(n):
+            if i < n - 1:
+                h = torch._addmm_activation(bs[i], h, Ws[i].t())
+            else:
+                h = torch.addmm(bs[i], h, Ws[i].t())
+            hs.append(h)
+        ctx.save_for_backward(*hs, *Ws)
+        ctx.n = n
+        return h
+
+    @staticmethod
+    def backward(ctx, dy):
+        n = ctx.n
+        saved = ctx.saved_tensors
+        hs, Ws = saved[: n + 1], saved[n + 1:]
+        dz = dy.to(hs[0].dtype).contiguous()
+        grads = [None] * (2 * n)
+        db = _colsum(dz, None, None)
+        dx = None
+        for i in reversed(range(n)):
+            grads[2 * i] = (dz.t() @ hs[i]).float()
+            grads[2 * i + 1] = db
+            if i > 0:
+                dh = dz @ Ws[i]
+                dz_prev = torch.empty_like(dh)
+                db = _colsum(dh, hs[i], dz_prev)
+                dz = dz_prev
+            elif ctx.needs_input_grad[0]:
+                dx = dz @ Ws[0]
+        return (dx, *grads)
+
+
+def mlp_params(net: nn.Sequential) -> list[torch.Tensor]:
+    """W1, b1, ..., Wn, bn of a Linear/ReLU stack (reference layout)."""
+    return list(net.parameters())
+
+
+def apply_mlp(net: nn.Sequential, x: torch.Tensor) -> torch.Tensor:
+    """net(x) with the fused backward; x float32 or bfloat16 (compute dtype)."""
+    return _MLP.apply(x.contiguous(), *mlp_params(net))

@@ -28,6 +28,12 @@ def fine_loss(ret, target, weight_main=1.0, weight_entropy_last=0.001, weight_rg
     return loss
 
 
+def eikonal_loss(gradient: torch.Tensor) -> torch.Tensor:
+    """mean((|grad| - 1)^2) over the shaded samples' finite-difference SDF
+    gradient (ret['gradient'], the d = 1 probes of voxurf_fine.py:524-526)."""
+    return ((gradient.float().norm(dim=-1) - 1.0) ** 2).mean()
+
+
 class FineTrainer:
     """Owns the optimizer of a fine Voxurf model and runs fused steps.
 
@@ -38,9 +44,15 @@ class FineTrainer:
     """
 
     def __init__(self, model, lr_sdf=1e-3, lr_k0=1e-3, lr_rgbnet=1e-3, lr_k_rgbnet=1e-3, tv_sdf=1e-4, tv_k0=1e-4,
-                 tv_dense=True, n_rays=8192, loss_weights=(1.0, 0.001, 0.5)):
+                 tv_dense=True, n_rays=8192, loss_weights=(1.0, 0.001, 0.5), weight_tv_density=0.0,
+                 smooth_grad_tv=0.0, weight_eikonal=0.0):
         self.model = model
         self.n_rays = n_rays
+        # run.py:617-622: loss += weight_tv_density * density_total_variation(smooth_grad_tv=...)
+        self.weight_tv_density, self.smooth_grad_tv = weight_tv_density, smooth_grad_tv
+        # eikonal term mean((|grad| - 1)^2) on the shaded samples' FD gradient
+        # (no counterpart in the reference loss; used by the differentiation workload)
+        self.weight_eikonal = weight_eikonal
         scale = float(model.world_size.max()) / 128  # voxurf_fine.py:404, 408
         shadow = None
         if model.precision == "bf16":
@@ -64,6 +76,11 @@ class FineTrainer:
             global_step = self.global_step
         ret = self.model(rays_o, rays_d, viewdirs, global_step=global_step, **render_kwargs)
         loss = fine_loss(ret, target, *self.loss_weights)
+        if self.weight_tv_density > 0 and self.smooth_grad_tv > 0:
+            loss = loss + self.weight_tv_density * self.model.density_total_variation(
+                smooth_grad_tv=self.smooth_grad_tv)
+        if self.weight_eikonal > 0 and ret["gradient"].numel() > 0:
+            loss = loss + self.weight_eikonal * eikonal_loss(ret["gradient"])
         loss.backward()
         self.optimizer.step(zero_grad=True)
         return loss.detach(), ret

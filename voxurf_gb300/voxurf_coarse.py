@@ -23,6 +23,7 @@ import torch.nn as nn
 from . import _abi, _native
 from . import grid as grid_mod
 from ._torch import ptr, stream_ptr
+from .mlp import apply_mlp
 from .voxurf_fine import FineFrame, gaussian_taps, max_steps_bound, smooth_grid, smooth_grid_adjoint
 
 
@@ -324,12 +325,7 @@ class Voxurf(nn.Module):
         fr.render_extras = bool(render_kwargs.get("render_depth", False) or render_kwargs.get("render_grad", False))
         Xf, w2, alphainv_last, normal2, alpha2 = _CoarseGeometry.apply(self.sdf.grid, self.k0.grid, fr)
         fr.normal2 = normal2
-        if fr.bf16:
-            with torch.autocast("cuda", dtype=torch.bfloat16):
-                rgb_logit = self.rgbnet(Xf)
-            rgb_logit = rgb_logit.float()
-        else:
-            rgb_logit = self.rgbnet(Xf)
+        rgb_logit = apply_mlp(self.rgbnet, Xf).float()
         rgb = torch.sigmoid(rgb_logit)
         rgb_marched = _CoarseComposite.apply(w2, rgb_logit, fr, float(render_kwargs["bg"]))
         normal_marched = None

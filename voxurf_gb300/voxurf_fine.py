@@ -35,6 +35,7 @@ import torch.nn.functional as F
 from . import _abi, _native
 from . import grid as grid_mod
 from ._torch import ptr, stream_ptr
+from .mlp import apply_mlp
 
 
 def gaussian_taps(ksize: int, sigma: float) -> np.ndarray:
@@ -255,6 +256,41 @@ class _FineComposite(torch.autograd.Function):
         return d_w2, d_last, d_logit, d_klogit, None, None
 
 
+class _SmoothGradTV(torch.autograd.Function):
+    """smooth_grad_tv term of Voxurf.density_total_variation
+    (voxurf_fine.py:417-420): mean over the non-empty voxels and the 3
+    channels of (tv_smooth_conv(G).detach() - G)^2, G the central-difference
+    gradient grid of the raw SDF (neus_sdf_gradient, 'interpolate')."""
+
+    @staticmethod
+    def forward(ctx, sdf_grid, mask_u8, voxel_size: float, n_voxels: int):
+        X, Y, Z = sdf_grid.shape[-3:]
+        dev = sdf_grid.device
+        st = stream_ptr()
+        G = torch.empty((X, Y, Z, 4), dtype=torch.float32, device=dev)
+        _abi.call("vx_sdf_gradient_grid", ptr(sdf_grid), ptr(G), X, Y, Z, float(voxel_size), 1, st)
+        count = 3 * n_voxels
+        partial = torch.empty(_abi_scratch_bytes(X, Y, Z) // 8, dtype=torch.float64, device=dev)
+        dG = torch.empty_like(G)
+        scale = 2.0 / max(count, 1)
+        _abi.call("vx_smooth_grad_tv", ptr(G), ptr(mask_u8), X, Y, Z, float(scale), ptr(dG), ptr(partial), st)
+        ctx.dG, ctx.shape, ctx.voxel_size = dG, sdf_grid.shape, float(voxel_size)
+        return (partial.sum() / max(count, 1)).float()
+
+    @staticmethod
+    def backward(ctx, g):
+        X, Y, Z = ctx.shape[-3:]
+        d_sdf = torch.zeros(ctx.shape, dtype=torch.float32, device=g.device)
+        dG = ctx.dG * g.float()
+        _abi.call("vx_sdf_gradient_grid_adjoint", ptr(dG), ptr(d_sdf), X, Y, Z, ctx.voxel_size, 1, 0, stream_ptr())
+        return d_sdf, None, None, None
+
+
+def _abi_scratch_bytes(X, Y, Z) -> int:
+    _abi._declare()
+    return int(_native.load().vx_smooth_grad_tv_scratch_bytes(X, Y, Z))
+
+
 def _mlp(d_in: int, width: int, depth: int, use_layer_norm: bool = False) -> nn.Sequential:
     """rgbnet / k_rgbnet layout of voxurf_fine.py:131-148, 167-184."""
     if use_layer_norm:
@@ -340,6 +376,7 @@ class Voxurf(nn.Module):
         # voxurf_fine.py:185 zeroes rgbnet's last bias a second time (not k_rgbnet's)
         nn.init.constant_(self.rgbnet[-1].bias, 0)
         self.dim0, self.k_dim0 = dim0, k_dim0
+        self._grad_col = self.k0_dim + (3 + 6 * k_posbase_pe) + (3 + 6 * k_viewbase_pe)
         # hierarchical displacement set (voxurf_fine.py:680-688)
         all_grad = sorted(set(self.grad_feat + self.k_grad_feat))
         all_sdf = sorted(set(self.sdf_feat + self.k_sdf_feat))
@@ -404,6 +441,26 @@ class Voxurf(nn.Module):
     def sdf_total_variation_add_grad(self, weight, dense_mode):
         w = weight * self.world_size.max() / 128
         self.sdf.total_variation_add_grad(w, w, w, dense_mode)
+
+    def density_total_variation(self, sdf_tv=0, smooth_grad_tv=0, grad_tv=0, smooth_sdf_tv=0):
+        """voxurf_fine.py:412-421.  smooth_grad_tv runs on the sm_103a kernels;
+        the masked-mean |diff| sdf_tv form (used only with ori_tv, never by
+        the fine configs) is not built.  Without a mask cache the reference
+        fails (nonempty_mask is None); here every voxel counts."""
+        if sdf_tv > 0:
+            raise NotImplementedError("sdf_tv (the ori_tv loss form) is not built; use sdf_total_variation_add_grad")
+        tv = 0
+        if smooth_grad_tv > 0:
+            nm = self.nonempty_mask
+            key = None if nm is None else (nm.data_ptr(), nm.numel())
+            if getattr(self, "_nonempty_key", "unset") != key:
+                self._nonempty_u8 = None if nm is None else nm.reshape(nm.shape[-3:]).to(torch.uint8).contiguous()
+                ws = self.sdf.grid.shape[-3:]
+                self._nonempty_count = int(ws[0] * ws[1] * ws[2]) if nm is None else int(nm.sum().item())
+                self._nonempty_key = key
+            tv = tv + _SmoothGradTV.apply(self.sdf.grid, self._nonempty_u8, float(self.voxel_size),
+                                          self._nonempty_count) * smooth_grad_tv
+        return tv
 
     def k0_total_variation_add_grad(self, weight, dense_mode):
         w = weight * self.world_size.max() / 128
@@ -498,7 +555,9 @@ class Voxurf(nn.Module):
             "disp": disp,
             "mask": None,          # per-sample masks are never materialised
             "mask_outbbox": None,
-            "gradient": normal2,
+            # differentiable FD gradient (xyz) of the shaded samples: the
+            # k_rgbnet input columns (voxurf_fine.py:733-739)
+            "gradient": X2a[:, self._grad_col:self._grad_col + 3].float(),
             "gradient_error": None,
             "s_val": s_val,
             "ray_id": fr.ray2,
@@ -509,8 +568,5 @@ class Voxurf(nn.Module):
         return ret
 
     def _run_mlp(self, net: nn.Sequential, x: torch.Tensor) -> torch.Tensor:
-        if self.precision == "bf16":
-            with torch.autocast("cuda", dtype=torch.bfloat16):
-                y = net(x)
-            return y.float()
-        return net(x)
+        # x is FP32 or BF16 (the compute dtype); logits come back in FP32
+        return apply_mlp(net, x).float()
