@@ -37,6 +37,10 @@ extern "C" {
 #define VX_ERR_LAUNCH 4      /* kernel launch failed                        */
 #define VX_ERR_CUDA 5        /* other CUDA runtime error                    */
 #define VX_ERR_UNSUPPORTED 6 /* configuration not supported by this build   */
+#define VX_ERR_TOO_LARGE 7   /* size above the fixed maximum of a no-allocation entry point */
+
+/* Largest ray count vx_sample_pts_count_noalloc accepts. */
+#define VX_NOALLOC_MAX_RAYS 4194304
 
 /* ---- library ------------------------------------------------------------ */
 int vx_version(void);
@@ -78,6 +82,23 @@ int vx_infer_ray_start_dir(const float* rays_o, const float* rays_d, const float
 int vx_sample_pts_count(const float* rays_o, const float* rays_d, const float* xyz_min, const float* xyz_max,
                         float near, float far, float stepdist, int64_t n_rays, float* t_min, float* t_max,
                         int64_t* n_steps, int64_t* offsets, void* scratch, size_t scratch_bytes, void* stream);
+
+/* No counterpart in the reference.  Phase 1 for callers that cannot
+ * allocate device memory: hosts that only receive device pointers for their
+ * inputs and outputs from another runtime (an FFI binding without access to
+ * a CUDA allocator) and render loops that reserve all device memory up
+ * front and must not allocate per frame.  Same outputs as
+ * vx_sample_pts_count; the scan scratch is a static array inside the library
+ * (16 KB per device, held until the process exits), so n_rays is limited to
+ * VX_NOALLOC_MAX_RAYS (larger sizes return VX_ERR_TOO_LARGE without touching
+ * the GPU).  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls on a device share the array: calls
+ * that overlap on the GPU race.  No cudaMalloc/cudaFree or other allocating
+ * call is made. */
+int vx_sample_pts_count_noalloc(const float* rays_o, const float* rays_d, const float* xyz_min,
+                                const float* xyz_max, float near, float far, float stepdist, int64_t n_rays,
+                                float* t_min, float* t_max, int64_t* n_steps, int64_t* offsets, void* stream);
 
 /* Phase 2: writes ray_pts [M,3], mask_outbbox [M] (0/1 bytes), ray_id [M],
  * step_id [M] for the offsets of phase 1.  Writes at or beyond `capacity` are

@@ -42,6 +42,8 @@ _SIGNATURES = {
                             c_ptr, c_size, c_ptr],
     "vx_sample_pts_fill": [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_i64, c_i64, c_ptr, c_ptr, c_ptr,
                            c_ptr, c_ptr],
+    "vx_sample_pts_count_noalloc": [c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_f32, c_f32, c_i64, c_ptr, c_ptr, c_ptr,
+                                    c_ptr, c_ptr],
     "vx_maskcache_lookup": [c_ptr, c_i64, c_i64, c_i64, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr],
     "vx_alpha2weight": [c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
     "vx_alpha2weight_backward": [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr,

@@ -12,9 +12,39 @@
 //     rounded once (no FMA contraction), so the CPU oracle reproduces the
 //     outputs bit for bit.
 #include <math.h>
+#include <mutex>
 #include "common.cuh"
 
 namespace vx {
+
+// Scan scratch of vx_sample_pts_count_noalloc: one int64 partial sum per
+// 2048-ray tile plus the grand total, for at most VX_NOALLOC_MAX_RAYS rays
+// (2049 entries, 16 KB).  Every GPU that loads the library holds this array
+// until the process exits.  Host code must not hand the symbol itself to a
+// kernel (on the host it is only a stand-in, not a device address); the
+// device address comes from cudaGetSymbolAddress, looked up once per device.
+static __device__ __align__(256) int64_t g_noalloc_scan[VX_NOALLOC_MAX_RAYS / 2048 + 8];
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of g_noalloc_scan on the current device (set-up on first
+// use per device).  Returns VX_OK or a CUDA error status.
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (dev < 0 || dev >= 64) return VX_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scan);
+    if (e != cudaSuccess) return cuda_status(e);
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return VX_OK;
+}
 
 struct RayClip {
   float t_min, t_max;
@@ -215,6 +245,33 @@ int vx_sample_pts_count(const float* rays_o, const float* rays_d, const float* x
     if (s) return s;
   }
   return exclusive_scan<int64_t, int64_t>(n_steps, n_rays, offsets, scratch, scratch_bytes, st);
+}
+
+// Same results as vx_sample_pts_count, for callers that cannot allocate
+// device memory: the scan scratch is the library's own static array.  The
+// array is shared by every call on a device and keeps the last call's
+// contents; every entry a call reads is written by that same call first, so
+// nothing needs clearing.  Calls that overlap on the GPU (different streams,
+// or threads without ordering) race on the array.
+int vx_sample_pts_count_noalloc(const float* rays_o, const float* rays_d, const float* xyz_min,
+                                const float* xyz_max, float near, float far, float stepdist, int64_t n_rays,
+                                float* t_min, float* t_max, int64_t* n_steps, int64_t* offsets, void* stream) {
+  if (n_rays < 0 || !offsets) return VX_ERR_ARG;
+  if (n_rays > VX_NOALLOC_MAX_RAYS) return VX_ERR_TOO_LARGE;
+  void* scratch = nullptr;
+  int s = noalloc_scratch(&scratch);
+  if (s) return s;
+  const size_t bytes = (size_t)(scan_n_tiles(n_rays) + 1) * sizeof(int64_t);
+  if (bytes > sizeof(g_noalloc_scan)) return VX_ERR_TOO_LARGE;
+  cudaStream_t st = as_stream(stream);
+  if (n_rays > 0) {
+    if (!rays_o || !rays_d || !xyz_min || !xyz_max || !t_min || !t_max || !n_steps) return VX_ERR_ARG;
+    sample_count_kernel<<<grid_for(n_rays), VX_THREADS, 0, st>>>(rays_o, rays_d, xyz_min, xyz_max, near, far,
+                                                               stepdist, n_rays, t_min, t_max, n_steps);
+    s = launch_status();
+    if (s) return s;
+  }
+  return exclusive_scan<int64_t, int64_t>(n_steps, n_rays, offsets, scratch, bytes, st);
 }
 
 int vx_sample_pts_fill(const float* rays_o, const float* rays_d, const float* xyz_min, const float* xyz_max,
