@@ -157,6 +157,14 @@ int vx_adam_upd_with_perlr(float* param, const float* grad, float* exp_avg, floa
 int vx_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq, const float* per_lr, int64_t n,
                  double lr, double beta1, double beta2, double eps, int64_t step, int zero_grad, void* stream);
 
+/* utils.Adam (utils.py:169-199) over up to 48 tensors in one launch (the
+ * MLP weights and biases).  params/grads/exp_avgs/exp_avg_sqs are HOST arrays
+ * of device pointers; sizes, lrs, steps (state['step'] after the increment)
+ * HOST arrays of n_tensors entries. */
+int vx_adam_step_multi(int n_tensors, float* const* params, float* const* grads, float* const* exp_avgs,
+                       float* const* exp_avg_sqs, const int64_t* sizes, const double* lrs, const int64_t* steps,
+                       double beta1, double beta2, double eps, void* stream);
+
 /* Colour-MLP backward helper (rgbnet/k_rgbnet ReLU stacks,
  * lib/voxurf_fine.py:132-187): dz = dh * (h > 0) and colsum += sum over rows
  * of dz (the bias gradient), one pass; h == NULL skips the ReLU (bias

@@ -160,3 +160,29 @@ def test_row_sweep_bit_identical_to_generic_sweep(cuda, dense):
         outs.append([r.cpu() for r in res])
     for a, b in zip(*outs):
         assert torch.equal(a, b)
+
+
+def test_adam_multi_matches_single(cuda):
+    """One multi-tensor launch == one vx_adam_step launch per tensor."""
+    import ctypes
+
+    torch.manual_seed(1)
+    sizes = [70 * 192, 192, 192 * 192, 192, 3 * 192, 3, 5000, 1]
+    lrs = [1e-3, 1e-3, 3e-3, 3e-3, 1e-2, 1e-2, 1e-3, 1e-3]
+    steps = [1, 1, 5, 5, 2, 2, 9, 9]
+    a = [[torch.randn(n, device=cuda) for n in sizes] for _ in range(4)]
+    b = [[t.clone() for t in grp] for grp in a]
+    b[2] = [t.abs() * 1e-3 for t in b[2]]
+    a[2] = [t.clone() for t in b[2]]
+    a[3] = [t.abs() * 1e-4 for t in a[3]]
+    b[3] = [t.clone() for t in a[3]]
+    for (p, g, m, v), n, lr, s in zip(zip(*a), sizes, lrs, steps):
+        _native.call("vx_adam_step", ptr(p), ptr(g), ptr(m), ptr(v), None, n, lr, 0.9, 0.99, 1e-8, s, 0, stream_ptr())
+    k = len(sizes)
+    P = ctypes.c_void_p * k
+    _native.call("vx_adam_step_multi", k, *[P(*[t.data_ptr() for t in grp]) for grp in b],
+                 (ctypes.c_int64 * k)(*sizes), (ctypes.c_double * k)(*lrs), (ctypes.c_int64 * k)(*steps), 0.9, 0.99,
+                 1e-8, stream_ptr())
+    for grp_a, grp_b in zip(a, b):
+        for x, y in zip(grp_a, grp_b):
+            assert torch.equal(x, y)

@@ -348,6 +348,52 @@ __global__ void __launch_bounds__(256) grid_tv_adam_row_kernel(const float* __re
   }
 }
 
+// Multi-tensor utils.Adam: up to VX_ADAM_MULTI_MAX small tensors (the MLP
+// weights and biases) in one launch.  The table is a by-value kernel
+// parameter; CTA b works on chunk b, mapped to (tensor, offset) through the
+// chunk prefix.
+constexpr int ADAM_MULTI_MAX = 48;
+constexpr int ADAM_CHUNK = 4096;
+
+struct AdamMultiTable {
+  int n;
+  float* p[ADAM_MULTI_MAX];
+  float* g[ADAM_MULTI_MAX];
+  float* m[ADAM_MULTI_MAX];
+  float* v[ADAM_MULTI_MAX];
+  int64_t len[ADAM_MULTI_MAX];
+  int chunk0[ADAM_MULTI_MAX + 1];
+  float step_size[ADAM_MULTI_MAX];
+  float sqrt_bc2[ADAM_MULTI_MAX];
+  float beta1, beta2, one_m_beta1, one_m_beta2, eps;
+};
+
+__global__ void __launch_bounds__(256) adam_multi_kernel(const AdamMultiTable T) {
+  const int b = blockIdx.x;
+  int t = 0;
+  while (t + 1 < T.n && T.chunk0[t + 1] <= b) ++t;
+  const int64_t off = (int64_t)(b - T.chunk0[t]) * ADAM_CHUNK;
+  const int64_t end = min(off + ADAM_CHUNK, T.len[t]);
+  AdamParams a;
+  a.beta1 = T.beta1;
+  a.beta2 = T.beta2;
+  a.one_m_beta1 = T.one_m_beta1;
+  a.one_m_beta2 = T.one_m_beta2;
+  a.step_size = T.step_size[t];
+  a.sqrt_bc2 = T.sqrt_bc2[t];
+  a.eps = T.eps;
+  float* p = T.p[t];
+  float* g = T.g[t];
+  float* m = T.m[t];
+  float* v = T.v[t];
+  for (int64_t i = off + threadIdx.x; i < end; i += blockDim.x) {
+    float mi = m[i], vi = v[i];
+    p[i] = adam_update(p[i], g[i], mi, vi, 1.f, false, a);
+    m[i] = mi;
+    v[i] = vi;
+  }
+}
+
 inline unsigned sweep_blocks(int64_t work_items) {
   // Persistent-style grid: a multiple of the SM count, capped by the work.
   const int64_t per_wave = (int64_t)sm_count() * 8;  // 8 x 256-thread CTAs per SM
@@ -457,6 +503,43 @@ int vx_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq, c
   a.eps = (float)eps;
   adam_step_kernel<<<sweep_blocks((n + 3) / 4), 256, 0, as_stream(stream)>>>(param, grad, exp_avg, exp_avg_sq,
                                                                            per_lr, n, a, zero_grad);
+  return launch_status();
+}
+
+int vx_adam_step_multi(int n_tensors, float* const* params, float* const* grads, float* const* exp_avgs,
+                       float* const* exp_avg_sqs, const int64_t* sizes, const double* lrs, const int64_t* steps,
+                       double beta1, double beta2, double eps, void* stream) {
+  if (n_tensors < 0 || n_tensors > ADAM_MULTI_MAX) return VX_ERR_ARG;
+  if (n_tensors == 0) return VX_OK;
+  if (!params || !grads || !exp_avgs || !exp_avg_sqs || !sizes || !lrs || !steps) return VX_ERR_ARG;
+  AdamMultiTable T;
+  T.n = n_tensors;
+  T.beta1 = (float)beta1;
+  T.beta2 = (float)beta2;
+  T.one_m_beta1 = (float)(1.0 - beta1);
+  T.one_m_beta2 = (float)(1.0 - beta2);
+  T.eps = (float)eps;
+  int64_t chunks = 0;
+  for (int t = 0; t < n_tensors; ++t) {
+    if (!params[t] || !grads[t] || !exp_avgs[t] || !exp_avg_sqs[t] || sizes[t] < 0 || steps[t] < 1)
+      return VX_ERR_ARG;
+    T.p[t] = params[t];
+    T.g[t] = grads[t];
+    T.m[t] = exp_avgs[t];
+    T.v[t] = exp_avg_sqs[t];
+    T.len[t] = sizes[t];
+    T.chunk0[t] = (int)chunks;
+    chunks += (sizes[t] + ADAM_CHUNK - 1) / ADAM_CHUNK;
+    // utils.py:177-194 scalars in double, cast to float
+    const double bc1 = 1.0 - pow(beta1, (double)steps[t]);
+    const double bc2 = 1.0 - pow(beta2, (double)steps[t]);
+    T.step_size[t] = (float)(lrs[t] / bc1);
+    T.sqrt_bc2[t] = (float)sqrt(bc2);
+  }
+  T.chunk0[n_tensors] = (int)chunks;
+  if (chunks == 0) return VX_OK;
+  if (chunks > INT32_MAX) return VX_ERR_ARG;
+  adam_multi_kernel<<<(unsigned)chunks, 256, 0, as_stream(stream)>>>(T);
   return launch_status();
 }
 

@@ -13,6 +13,8 @@ Differences by design:
 """
 from __future__ import annotations
 
+import weakref
+
 import torch
 import torch.nn as nn
 import torch.nn.functional as F
@@ -25,6 +27,24 @@ def create_grid(type, **kwargs):
     if type == "DenseGrid":
         return DenseGrid(**kwargs)
     raise NotImplementedError(f"{type} is not part of this build (the Voxurf models only create DenseGrid)")
+
+
+_HOST_CACHE: dict = {}
+
+
+def host_values(t: torch.Tensor) -> list:
+    """Host copy of a small device tensor (bbox, mask scale/shift), cached
+    per tensor storage and version: a per-step .tolist() would make the host
+    wait for all queued GPU work of the previous step."""
+    key = (t.data_ptr(), t._version, tuple(t.shape), str(t.device))
+    hit = _HOST_CACHE.get(id(t))
+    if hit is not None and hit[0] == key:
+        return hit[1]
+    vals = t.detach().cpu().tolist()
+    if id(t) not in _HOST_CACHE:
+        weakref.finalize(t, _HOST_CACHE.pop, id(t), None)
+    _HOST_CACHE[id(t)] = (key, vals)
+    return vals
 
 
 def grid_geom(world_size, xyz_min, xyz_max) -> _abi.GridGeom:
@@ -87,7 +107,7 @@ class DenseGrid(nn.Module):
         super()._load_from_state_dict(state_dict, prefix, *args, **kwargs)
 
     def geom(self) -> _abi.GridGeom:
-        return grid_geom(self.grid.shape[2:], self.xyz_min.tolist(), self.xyz_max.tolist())
+        return grid_geom(self.grid.shape[2:], host_values(self.xyz_min), host_values(self.xyz_max))
 
     def forward(self, xyz):
         shape = xyz.shape[:-1]

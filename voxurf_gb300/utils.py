@@ -15,6 +15,7 @@ BF16 shadow copy when ``shadow`` (a tensor) is given.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 
 import torch
@@ -52,6 +53,7 @@ class Adam(torch.optim.Optimizer):
             with torch.enable_grad():
                 loss = closure()
         st = stream_ptr()
+        batch = []  # small tensors without per-voxel lr: one multi-tensor launch
         for group in self.param_groups:
             beta1, beta2 = group["betas"]
             for p in group["params"]:
@@ -72,6 +74,11 @@ class Adam(torch.optim.Optimizer):
                 tv_w = group.get("tv_weight", 0.0)
                 if p.dim() == 5 and tv_w:
                     self._grid_step(p, g, state, per_lr, group, tv_w, zero_grad, st)
+                elif per_lr is None and group.get("shadow") is None and p.is_contiguous() and g.is_contiguous() \
+                        and group["betas"] == self.param_groups[0]["betas"] \
+                        and group["eps"] == self.param_groups[0]["eps"]:
+                    batch.append((p, g, state, float(group["lr"])))
+                    continue
                 else:
                     call("vx_adam_step", ptr(p), ptr(g), ptr(state["exp_avg"]), ptr(state["exp_avg_sq"]),
                          ptr(per_lr), p.numel(), float(group["lr"]), float(beta1), float(beta2),
@@ -80,6 +87,24 @@ class Adam(torch.optim.Optimizer):
                     if shadow is not None:
                         shadow.copy_(p.detach())
                 if zero_grad:
+                    p.grad = None
+        if batch:
+            b1, b2 = self.param_groups[0]["betas"]
+            eps = float(self.param_groups[0]["eps"])
+            for i in range(0, len(batch), 48):
+                part = batch[i:i + 48]
+                n = len(part)
+                P = ctypes.c_void_p * n
+                call("vx_adam_step_multi", n, P(*[p.data_ptr() for p, _, _, _ in part]),
+                     P(*[g.data_ptr() for _, g, _, _ in part]),
+                     P(*[s["exp_avg"].data_ptr() for _, _, s, _ in part]),
+                     P(*[s["exp_avg_sq"].data_ptr() for _, _, s, _ in part]),
+                     (ctypes.c_int64 * n)(*[p.numel() for p, _, _, _ in part]),
+                     (ctypes.c_double * n)(*[lr for _, _, _, lr in part]),
+                     (ctypes.c_int64 * n)(*[int(s["step"]) for _, _, s, _ in part]),
+                     float(b1), float(b2), eps, st)
+            if zero_grad:
+                for p, _, _, _ in batch:
                     p.grad = None
         return loss
 

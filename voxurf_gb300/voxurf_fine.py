@@ -504,13 +504,13 @@ class Voxurf(nn.Module):
         fr.voxel_size = float(vs)
         fr.inv_s = inv_s
         fr.thres = float(self.fast_color_thres)
-        fr.geom = grid_mod.grid_geom(self.sdf.grid.shape[2:], self.xyz_min.tolist(), self.xyz_max.tolist())
-        fr.max_steps = max_steps_bound(self.xyz_min.tolist(), self.xyz_max.tolist(), fr.stepdist)
+        fr.geom = grid_mod.grid_geom(self.sdf.grid.shape[2:], grid_mod.host_values(self.xyz_min), grid_mod.host_values(self.xyz_max))
+        fr.max_steps = max_steps_bound(grid_mod.host_values(self.xyz_min), grid_mod.host_values(self.xyz_max), fr.stepdist)
         fr.taps = self.smooth_taps if self.smooth_sdf else None
         fr.mask = None
         if self.mask_cache is not None:
             mc = self.mask_cache
-            fr.mask = (mc.mask, mc.xyz2ijk_scale.tolist(), mc.xyz2ijk_shift.tolist())
+            fr.mask = (mc.mask, grid_mod.host_values(mc.xyz2ijk_scale), grid_mod.host_values(mc.xyz2ijk_shift))
         fr.cfg = _feature_cfg(self)
         fr.bf16 = self.precision == "bf16"
         fr.k0_bf16 = None
