@@ -107,6 +107,13 @@ int vx_sample_pts_fill(const float* rays_o, const float* rays_d, const float* xy
                        const float* t_min, const int64_t* offsets, float stepdist, int64_t n_rays, int64_t capacity,
                        float* ray_pts, uint8_t* mask_outbbox, int64_t* ray_id, int64_t* step_id, void* stream);
 
+/* Rays of one pinhole view (get_rays + viewdirs, lib/voxurf_fine.py:1001-1029,
+ * 1062-1067): c2w_host is a HOST row-major 3x4 (or 4x4) camera-to-world
+ * matrix; pixel centres +0.5; inverse_y = 1 for OpenCV axes.  Outputs
+ * [H*W,3] each, row-major over (row j, column i). */
+int vx_camera_rays(const float* c2w_host, float fx, float fy, float cx, float cy, int64_t H, int64_t W,
+                   int inverse_y, float* rays_o, float* rays_d, float* viewdirs, void* stream);
+
 /* render_utils.cpp:109-118 / render_utils_kernel.cu:374-424 (grid.MaskGrid,
  * lib/grid.py:233-242).  world: [sz_i, sz_j, sz_k] bytes (0/1). */
 int vx_maskcache_lookup(const uint8_t* world, int64_t sz_i, int64_t sz_j, int64_t sz_k, const float* xyz,

@@ -164,3 +164,22 @@ def test_alpha2weight_empty(cuda):
 def test_inputs_must_be_cuda(cuda):
     with pytest.raises(RuntimeError):
         ru.alpha2weight(torch.zeros(3), torch.zeros(3, dtype=torch.int64), 1)
+
+
+@pytest.mark.parametrize("H,W,pose", [(120, 160, 3), (7, 5, 40), (1, 1, 0)])
+def test_camera_rays_match_get_rays(cuda, H, W, pose):
+    """vx_camera_rays == get_rays + viewdirs (OpenCV axes, pixel centres +0.5)."""
+    import ctypes
+    from voxurf_gb300 import _native
+    from voxurf_gb300._torch import ptr, stream_ptr
+
+    c2w = synthetic.fibonacci_poses()[pose]
+    K = synthetic.intrinsics(1200, 1600)
+    py, px = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    o, d, v = synthetic.rays_for_pixels(c2w, K, px.reshape(-1), py.reshape(-1))
+    out = [torch.empty(H * W, 3, device=cuda) for _ in range(3)]
+    m = (ctypes.c_float * 16)(*c2w.astype(np.float32).reshape(-1))
+    _native.call("vx_camera_rays", m, float(K[0, 0]), float(K[1, 1]), float(K[0, 2]), float(K[1, 2]), H, W, 1,
+                 *[ptr(t) for t in out], stream_ptr())
+    for got, want in zip(out, (o, d, v)):
+        np.testing.assert_allclose(got.cpu().numpy(), want, rtol=0, atol=2e-6)

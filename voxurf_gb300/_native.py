@@ -45,6 +45,7 @@ _SIGNATURES = {
     "vx_sample_pts_count_noalloc": [c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_f32, c_f32, c_i64, c_ptr, c_ptr, c_ptr,
                                     c_ptr, c_ptr],
     "vx_maskcache_lookup": [c_ptr, c_i64, c_i64, c_i64, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr],
+    "vx_camera_rays": [c_ptr, c_f32, c_f32, c_f32, c_f32, c_i64, c_i64, c_int, c_ptr, c_ptr, c_ptr, c_ptr],
     "vx_alpha2weight": [c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
     "vx_alpha2weight_backward": [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr,
                                  c_ptr],
