@@ -1,0 +1,276 @@
+// Device helpers shared by the training kernels (render.cu) and the render
+// server kernels (serve.cu): exact ray sample positions, SDF probes, NeuS
+// alpha and the MLP input encodings of the fine model.
+#pragma once
+#include <math.h>
+#include "common.cuh"
+#include "trilinear.cuh"
+
+namespace vx {
+
+constexpr int MAX_K = 4;  // hierarchical displacements (configs use <= 4)
+
+// ---- exact sample positions (shared with sampling.cu semantics) ------------
+struct RayFrame {
+  float st[3], dr[3];
+  int64_t n_steps;
+};
+
+__device__ __forceinline__ RayFrame ray_frame(const float* o, const float* d, const float* mn, const float* mx,
+                                              float near, float stepdist) {
+  const float far = 1e9f;  // voxurf_fine.py:605
+  const float vx = (d[0] == 0.f) ? 1e-6f : d[0];
+  const float vy = (d[1] == 0.f) ? 1e-6f : d[1];
+  const float vz = (d[2] == 0.f) ? 1e-6f : d[2];
+  const float ax = fdiv(fsub(mx[0], o[0]), vx), ay = fdiv(fsub(mx[1], o[1]), vy), az = fdiv(fsub(mx[2], o[2]), vz);
+  const float bx = fdiv(fsub(mn[0], o[0]), vx), by = fdiv(fsub(mn[1], o[1]), vy), bz = fdiv(fsub(mn[2], o[2]), vz);
+  const float t_min = fmaxf(fminf(fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz)), far), near);
+  const float t_max = fmaxf(fminf(fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)), far), near);
+  const float rn = __fsqrt_rn(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
+  RayFrame f;
+  const float c = ceilf(fdiv(fmul(fsub(t_max, t_min), rn), stepdist));
+  f.n_steps = (int64_t)fmax((double)c, 1.0);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    f.st[a] = fadd(o[a], fmul(d[a], t_min));
+    f.dr[a] = fdiv(d[a], rn);
+  }
+  return f;
+}
+
+__device__ __forceinline__ void sample_point(const RayFrame& f, float stepdist, int k, float p[3]) {
+  const float dist = fmul(stepdist, (float)k);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) p[a] = fadd(f.st[a], fmul(f.dr[a], dist));
+}
+
+// ---- SDF value + finite-difference gradient (sample_sdfs, one displacement) -
+struct Probe {
+  float fm, fp;     // values at index -d and +d (clamped)
+  float inv_diff;   // 1 / (clamped index difference)
+  Corners cm, cp;
+};
+
+__device__ __forceinline__ void probe_axis(const float* __restrict__ sdf, const GridGeom& g, const float ind[3],
+                                           int axis, float d, Probe& pr, bool keep_corners) {
+  float im[3] = {ind[0], ind[1], ind[2]};
+  float ip[3] = {ind[0], ind[1], ind[2]};
+  const float hi = (float)(gsize(g, axis) - 1);
+  im[axis] = fminf(fmaxf(ind[axis] - d, 0.f), hi);
+  ip[axis] = fminf(fmaxf(ind[axis] + d, 0.f), hi);
+  Corners cm = corners_of(g, im[0], im[1], im[2]);
+  Corners cp = corners_of(g, ip[0], ip[1], ip[2]);
+  pr.fm = gather1(sdf, cm);
+  pr.fp = gather1(sdf, cp);
+  pr.inv_diff = 1.f / (ip[axis] - im[axis]);
+  if (keep_corners) {
+    pr.cm = cm;
+    pr.cp = cp;
+  }
+}
+
+__device__ __forceinline__ void to_index(const GridGeom& g, const float p[3], float ind[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) ind[a] = world_to_index(g, a, p[a]);
+}
+
+// SDF and gradient (xyz order) at one point: centre + 6 probes at +-1 voxel.
+__device__ __forceinline__ void sdf_and_grad(const float* __restrict__ sdf, const GridGeom& g, float voxel_size,
+                                             const float ind[3], float* s, float gr[3]) {
+  *s = sample1(sdf, g, ind[0], ind[1], ind[2]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    Probe pr;
+    probe_axis(sdf, g, ind, a, 1.f, pr, false);
+    gr[a] = ((pr.fp - pr.fm) * pr.inv_diff) / voxel_size;
+  }
+}
+
+__device__ __forceinline__ float sigmoidf_(float x) { return 1.f / (1.f + expf(-x)); }
+
+// NeuS s-density alpha (voxurf_fine.py:475-499, cos_anneal_ratio = 1):
+//   P = sigmoid(prev*inv_s), Q = sigmoid(next*inv_s),
+//   alpha = clip((P - Q + 1e-5) / (P + 1e-5), 0, 1).
+// Away from the surface P and Q both approach 1 and the literal P - Q loses
+// all FP32 precision (about 1e-3 relative error at alpha ~ 1e-4, which flips
+// the fast_color_thres decisions against an FP64 evaluation).  The same
+// quantity is formed without cancellation:
+//   P - Q = sigmoid(a) * sigmoid(-b) * (-expm1(b - a)),  a = prev*inv_s,
+// b = next*inv_s (b <= a), and 1 - P, 1 - Q are taken as sigmoid(-a),
+// sigmoid(-b) in the backward.
+struct AlphaState {
+  float alpha, raw, P, Q, nP, nQ, cosv;
+};
+
+__device__ __forceinline__ AlphaState neus_alpha(float s, const float gr[3], const float v[3], float inv_s,
+                                                 float dist) {
+  AlphaState a;
+  a.cosv = v[0] * gr[0] + v[1] * gr[1] + v[2] * gr[2];
+  const float ic = fminf(a.cosv, 0.f);  // -relu(-cos)
+  const float h = ic * dist * 0.5f;
+  const float next = s + h, prev = s - h;
+  const float xa = prev * inv_s, xb = next * inv_s;
+  a.P = sigmoidf_(xa);
+  a.Q = sigmoidf_(xb);
+  a.nP = sigmoidf_(-xa);
+  a.nQ = sigmoidf_(-xb);
+  const float pmq = -(a.P * a.nQ) * expm1f(xb - xa);
+  a.raw = (pmq + 1e-5f) / (a.P + 1e-5f);
+  a.alpha = fminf(fmaxf(a.raw, 0.f), 1.f);
+  return a;
+}
+
+__device__ __forceinline__ bool outside_bbox(const float p[3], const float* mn, const float* mx) {
+  return (mn[0] > p[0]) | (mn[1] > p[1]) | (mn[2] > p[2]) | (mx[0] < p[0]) | (mx[1] < p[1]) | (mx[2] < p[2]);
+}
+
+// maskcache_lookup semantics (render_utils_kernel.cu:374-392): nearest voxel,
+// round half away from zero, false outside the grid.
+__device__ __forceinline__ bool mask_lookup(const uint8_t* __restrict__ mask, int mX, int mY, int mZ,
+                                            const float* scale, const float* shift, const float p[3]) {
+  int ijk[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) ijk[a] = (int)roundf(fadd(fmul(p[a], scale[a]), shift[a]));
+  if (ijk[0] < 0 || ijk[0] >= mX || ijk[1] < 0 || ijk[1] >= mY || ijk[2] < 0 || ijk[2] >= mZ) return false;
+  return mask[((int64_t)ijk[0] * mY + ijk[1]) * mZ + ijk[2]] != 0;
+}
+
+// ---- MLP input encodings ----------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void put(T* row, int c, float v);
+template <>
+__device__ __forceinline__ void put<float>(float* row, int c, float v) { row[c] = v; }
+template <>
+__device__ __forceinline__ void put<__nv_bfloat16>(__nv_bfloat16* row, int c, float v) {
+  row[c] = __float2bfloat16_rn(v);
+}
+
+template <typename T>
+__device__ __forceinline__ int put_pe(T* row, int c, const float x[3], int n_freq) {
+  // [x, sin(x*2^f) (axis-major), cos(...)] as torch.cat([x, emb.sin(), emb.cos()])
+  // with emb = (x.unsqueeze(-1) * freq).flatten(-2)  (voxurf_fine.py:694-698).
+#pragma unroll
+  for (int a = 0; a < 3; ++a) put(row, c + a, x[a]);
+  c += 3;
+  for (int a = 0; a < 3; ++a)
+    for (int q = 0; q < n_freq; ++q) put(row, c + a * n_freq + q, sinf(x[a] * (float)(1 << q)));
+  c += 3 * n_freq;
+  for (int a = 0; a < 3; ++a)
+    for (int q = 0; q < n_freq; ++q) put(row, c + a * n_freq + q, cosf(x[a] * (float)(1 << q)));
+  return c + 3 * n_freq;
+}
+
+// Hierarchical features of one point: feat[6K] (dir-major: z-,z+,y-,y+,x-,x+
+// each over K) and grad[3K] (pair-major z,y,x, normalised per K when
+// use_grad_norm), and the unnormalised d=1 gradient in xyz order.
+__device__ __forceinline__ void hier_features(const float* __restrict__ sdf, const GridGeom& g, float vs,
+                                              const float ind[3], int K, const float* disp, float feat[6 * MAX_K],
+                                              float graw[3 * MAX_K]) {
+  for (int kk = 0; kk < K; ++kk) {
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) {
+      const int axis = 2 - pair;  // zyx
+      Probe pr;
+      probe_axis(sdf, g, ind, axis, disp[kk], pr, false);
+      feat[(2 * pair + 0) * K + kk] = pr.fm;
+      feat[(2 * pair + 1) * K + kk] = pr.fp;
+      graw[pair * K + kk] = ((pr.fp - pr.fm) * pr.inv_diff) / vs;
+    }
+  }
+}
+
+// Column layout of the two colour-MLP inputs (voxurf_fine.py:694-739).
+struct FeatLayout {
+  int K;
+  float disp[MAX_K];
+  int k_unit;  // index of displacement 1.0 in disp
+  int pos_pe, view_pe, kpos_pe, kview_pe;
+  int center_sdf, use_rgbnet_k0, k_center_sdf;
+};
+
+// Host side: checks a feature configuration and converts it.
+inline int fill_feat_layout(const vx_fine_feature_cfg* c, FeatLayout& L) {
+  L.K = (int)c->K;
+  if (L.K < 1 || L.K > MAX_K) return VX_ERR_ARG;
+  L.k_unit = -1;
+  for (int i = 0; i < L.K; ++i) {
+    L.disp[i] = c->disp[i];
+    if (c->disp[i] == 1.0f) L.k_unit = i;
+  }
+  if (L.k_unit < 0) return VX_ERR_ARG;  // k_grad_feat = (1.0,) must be among the displacements
+  if (c->k0_channels != 12) return VX_ERR_UNSUPPORTED;
+  if (c->posbase_pe < 0 || c->posbase_pe > 16 || c->viewbase_pe < 0 || c->viewbase_pe > 16 ||
+      c->k_posbase_pe < 0 || c->k_posbase_pe > 16 || c->k_viewbase_pe < 0 || c->k_viewbase_pe > 16)
+    return VX_ERR_ARG;
+  L.pos_pe = (int)c->posbase_pe;
+  L.view_pe = (int)c->viewbase_pe;
+  L.kpos_pe = (int)c->k_posbase_pe;
+  L.kview_pe = (int)c->k_viewbase_pe;
+  L.center_sdf = c->center_sdf;
+  L.use_rgbnet_k0 = c->use_rgbnet_k0;
+  L.k_center_sdf = c->k_center_sdf;
+  return VX_OK;
+}
+
+// Column counts of the rows fine_feature_rows writes.
+inline int64_t x1_cols(const vx_fine_feature_cfg* c) {
+  return (c->use_rgbnet_k0 ? 12 : 0) + (3 + 6 * c->posbase_pe) + (3 + 6 * c->viewbase_pe) + (c->center_sdf ? 1 : 0) +
+         9 * c->K;
+}
+inline int64_t x2_cols(const vx_fine_feature_cfg* c) {
+  return 12 + (3 + 6 * c->k_posbase_pe) + (3 + 6 * c->k_viewbase_pe) + 3 + (c->k_center_sdf ? 1 : 0);
+}
+
+// One shaded point p seen along viewdir v: the rgbnet input row x1
+// ([k0], PE(xyz_n), PE(v), [sdf], 6K hierarchical values, 3K normalised
+// gradients) and the k_rgbnet input row x2 without its trailing logits
+// (k0, PE(xyz_n), PE(v), d=1 gradient, [sdf]); g1 = the d=1 gradient (xyz).
+template <typename T>
+__device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf, const GridGeom& g, float vs,
+                                                  const float* __restrict__ k0f,
+                                                  const __nv_bfloat16* __restrict__ k0h, const FeatLayout& L,
+                                                  const float p[3], const float v[3], T* x1, T* x2, float g1[3]) {
+  float ind[3];
+  to_index(g, p, ind);
+  const float s = sample1(sdf, g, ind[0], ind[1], ind[2]);
+  float feat[6 * MAX_K], graw[3 * MAX_K];
+  hier_features(sdf, g, vs, ind, L.K, L.disp, feat, graw);
+  // gradient for k_rgbnet: unnormalised, displacement 1.0, xyz order
+  g1[0] = graw[2 * L.K + L.k_unit];
+  g1[1] = graw[1 * L.K + L.k_unit];
+  g1[2] = graw[0 * L.K + L.k_unit];
+  float k0v[12];
+  const Corners c = corners_of(g, ind[0], ind[1], ind[2]);
+  if (k0h)
+    gatherC<12>(k0h, c, k0v);
+  else
+    gatherC<12>(k0f, c, k0v);
+  float xyzn[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) xyzn[a] = (p[a] - g.mn[a]) / (g.mx[a] - g.mn[a]);
+
+  int col = 0;
+  if (L.use_rgbnet_k0)
+    for (int ch = 0; ch < 12; ++ch) put(x1, col++, k0v[ch]);
+  col = put_pe(x1, col, xyzn, L.pos_pe);
+  col = put_pe(x1, col, v, L.view_pe);
+  if (L.center_sdf) put(x1, col++, s);
+  for (int q = 0; q < 6 * L.K; ++q) put(x1, col++, feat[q]);
+  for (int kk = 0; kk < L.K; ++kk) {
+    const float a = graw[0 * L.K + kk], b = graw[1 * L.K + kk], cc = graw[2 * L.K + kk];
+    const float nrm = sqrtf(a * a + b * b + cc * cc) + 1e-5f;
+    put(x1, col + 0 * L.K + kk, a / nrm);
+    put(x1, col + 1 * L.K + kk, b / nrm);
+    put(x1, col + 2 * L.K + kk, cc / nrm);
+  }
+  col = 0;
+  for (int ch = 0; ch < 12; ++ch) put(x2, col++, k0v[ch]);
+  col = put_pe(x2, col, xyzn, L.kpos_pe);
+  col = put_pe(x2, col, v, L.kview_pe);
+  put(x2, col++, g1[0]);
+  put(x2, col++, g1[1]);
+  put(x2, col++, g1[2]);
+  if (L.k_center_sdf) put(x2, col++, s);
+}
+
+}  // namespace vx
