@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-bf16", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-render", action="store_true", help="skip the render-server measurement")
+    p.add_argument("--render-requests", type=int, default=120)
     p.add_argument("--grid", type=int, default=256, help="grid resolution (256 is the benchmark; smaller sizes "
                                                          "serve profiler captures)")
     args = p.parse_args()
@@ -275,6 +277,10 @@ def run_ours(args, world, rank, local):
                 "bytes_per_launch": alg_bytes, "launch_ms": sweep_avg,
                 "traffic": SWEEP_NCU_TRAFFIC}
 
+    render = None
+    if not args.no_render:
+        render = run_render(args, dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline()
@@ -291,12 +297,91 @@ def run_ours(args, world, rank, local):
                        "l2": "no flush: ~10 GB of grids + Adam state swept per step (> 129 MB L2)"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4},
             "fused_bf16": bf16,
+            "render": render,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),
         }
         print(json.dumps(line))
+
+
+RENDER_SCENES = 4
+RENDER_RATE = 50.0          # requests per second (Poisson)
+RENDER_TICK_RAYS = 1 << 20  # rays packed per tick
+MLP_FLOPS_PER_ROW = 347136  # rgbnet + k_rgbnet forward FLOPs per shaded sample (70/60 -> 192 x3 -> 3)
+
+
+def run_render(args, dev):
+    """Render server on 4 resident 256^3 scenes (SDF FP32 + k0 BF16, MLPs
+    BF16): a Poisson stream at 50 req/s and a saturated stream (all requests
+    at t = 0), resolutions uniform over 160x120 .. 1600x1200, random poses
+    on the radius-3 sphere; latency is arrival -> RGB + depth in host memory.
+    Beside it, the plain per-request FP32 render (8192-ray chunks through
+    Voxurf.forward) of the first requests of the same stream."""
+    import numpy as np
+    import torch
+
+    from voxurf_gb300 import configs, serve
+
+    models = configs.build_serve_models(R, "bf16", device=dev, n=RENDER_SCENES, mask_voxels=MASK_VOXELS)
+    s_val = configs.trained_s_val()
+    scenes = [serve.ResidentScene(m, s_val=s_val, precision="bf16") for m in models]
+    for m in models:
+        m.s_val = torch.ones(1) * s_val
+        m.precision = "fp32"   # the plain render path
+        m._k0_shadow = None
+    server = serve.RenderServer(scenes, tick_rays=RENDER_TICK_RAYS, arena_pixels=32 << 20)
+    torch.cuda.synchronize()
+    serve.run_stream(server, serve.request_stream(6, float("inf"), RENDER_SCENES, seed=99))  # warm-up
+    n = args.render_requests
+    poisson = serve.run_stream(server, serve.request_stream(n, RENDER_RATE, RENDER_SCENES, seed=1))
+    rows0 = server.rows_shaded
+    saturated = serve.run_stream(server, serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2))
+    rows = server.rows_shaded - rows0
+    sat_wall = saturated["wall_s"]
+
+    # plain per-request FP32 render of the first requests of the saturated stream
+    stream = serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2)[:8]
+    torch.cuda.synchronize()
+    lat, px = [], 0
+    w0 = time.perf_counter()
+    err = 0.0
+    for t, s, c2w, H, W in stream:
+        a = time.perf_counter()
+        rgb, depth = serve.plain_render(models[s], c2w, H, W)
+        rgb_h = rgb.cpu().numpy()
+        lat.append(time.perf_counter() - a)
+        px += H * W
+        if (H, W) == (600, 800) and err == 0.0:
+            mine, _ = server.render(s, c2w, H, W)
+            err = float(np.abs(mine - rgb_h).max())
+    plain_wall = time.perf_counter() - w0
+    plain = {"requests": len(stream), "mpix_s": px / plain_wall / 1e6,
+             "p50_ms": float(np.percentile(np.array(lat) * 1000, 50)),
+             "p99_ms": float(np.percentile(np.array(lat) * 1000, 99))}
+    bf16_peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16_peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        bf16_peak = 1900.0
+    mlp_tflops = rows * MLP_FLOPS_PER_ROW / sat_wall / 1e12
+    del server, scenes, models
+    torch.cuda.empty_cache()
+    return {
+        "metric": "render Mpix/s and p50/p99 latency (4 resident 256^3 scenes)",
+        "workload": "4 scenes sdf 256^3 f32 + k0 256^3x12 bf16 + MLP bf16, mask |SDF|<0.05, s_val at step 20000, "
+                    "poses on r=3 sphere, res uniform {160x120,400x300,800x600,1600x1200}, "
+                    f"tick {RENDER_TICK_RAYS} rays",
+        "poisson_50_req_s": poisson,
+        "saturated": saturated,
+        "plain_fp32_per_request": plain,
+        "speedup_vs_plain": saturated["mpix_s"] / plain["mpix_s"],
+        "shaded_rows_per_pixel": rows / saturated["pixels"],
+        "mlp_tflops": mlp_tflops, "mlp_frac_of_bf16_peak": mlp_tflops / bf16_peak,
+        "rgb_max_abs_vs_plain_fp32_800x600": err,
+    }
 
 
 def cpu_baseline(seconds_hint=20.0):

@@ -488,6 +488,89 @@ typedef struct {
 } vx_coarse_backward_args;
 int vx_coarse_backward(const vx_coarse_backward_args* args, void* stream);
 
+/* ---- render server: the inference form of Voxurf.forward (global_step =
+ *      None, lib/voxurf_fine.py:620-802) for rays of several resident scenes
+ *      in one launch per stage.  The reference renders one scene per process,
+ *      chunk by chunk (run.py:81-126 render_viewpoints, 8192 rays per call);
+ *      these entry points have no one-to-one counterpart there. ------------ */
+
+#define VX_SERVE_MAX_SCENES 8
+
+/* One resident scene.  sdf_smooth is the SDF grid after the fine model's
+ * Gaussian smoothing (voxurf_fine.py:638), applied once at load time. */
+typedef struct {
+  vx_grid_geom grid;
+  const float* sdf_smooth;  /* [X,Y,Z] FP32                                      */
+  const void* k0;           /* [X,Y,Z,12] channel-last                           */
+  int32_t k0_bf16;          /* 1: k0 is BF16, 0: FP32                            */
+  float voxel_size;
+  const uint8_t* mask;      /* optional MaskGrid bool grid (NULL: none)          */
+  int64_t mask_X, mask_Y, mask_Z;
+  float mask_scale[3], mask_shift[3];
+  float inv_s;              /* 1 / s_val (s_val is per scene: not in checkpoints) */
+  float stepdist;           /* stepsize * voxel_size (also the NeuS dist)        */
+  float near;
+  float bg;
+  float fast_color_thres;
+} vx_scene_desc;
+
+/* A run of consecutive pixels of one view: rays [ray0, ray0 + n) of a tick
+ * come from pixels [pix0, pix0 + n) of an image W pixels wide (row-major)
+ * and their results go to pixels [out0, out0 + n) of the output arena. */
+typedef struct {
+  float c2w[12];            /* row-major 3x4 camera-to-world                     */
+  float fx, fy, cx, cy;
+  int32_t W;
+  int32_t inverse_y;        /* 1: OpenCV axes                                    */
+  int32_t scene;            /* index into the scene table                        */
+  int32_t reserved;
+  int64_t pix0, ray0, out0;
+} vx_view_chunk;
+
+/* Rays of a tick (get_rays + viewdirs, voxurf_fine.py:1001-1029, 1064) with
+ * their scene index and output pixel.  chunks: DEVICE array sorted by ray0,
+ * chunks[0].ray0 = 0. */
+int vx_serve_rays(const vx_view_chunk* chunks, int32_t n_chunks, int64_t n_rays, float* rays_o, float* rays_d,
+                  float* viewdirs, int32_t* ray_scene, int64_t* ray_out, void* stream);
+
+/* Per ray: exact samples (sample_pts_on_rays), mask lookup, SDF + FD normal,
+ * NeuS alpha, alpha > thres compaction, transmittance with the T < 1e-3
+ * stop, weight > thres test.  The shaded samples' (step, weight) go to
+ * rec[ray * max_steps + j] (8-byte records), their count to n2[ray].
+ * scenes_host: HOST array of n_scenes descriptors. */
+int vx_serve_march(const vx_scene_desc* scenes_host, int32_t n_scenes, const float* rays_o, const float* rays_d,
+                   const float* viewdirs, const int32_t* ray_scene, int64_t n_rays, int64_t max_steps, void* rec,
+                   int32_t* n2, float* alphainv_last, void* stream);
+
+/* ray2[s2_off[r] + j] = r for j < s2_off[r+1] - s2_off[r]. */
+int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, void* stream);
+
+/* MLP input rows of the shaded samples (the column layout of
+ * vx_fine_features; every scene of one call shares cfg).  Row strides:
+ * ld1 >= the rgbnet columns, ld2 >= the k_rgbnet columns + 3, the last 3
+ * being the rgbnet logits that vx_mlp_head writes. */
+int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const vx_fine_feature_cfg* cfg,
+                      const float* rays_o, const float* rays_d, const float* viewdirs, const int32_t* ray_scene,
+                      int64_t max_steps, const void* rec, const int64_t* s2_off, const int32_t* ray2, int64_t n_rows,
+                      int64_t ld1, int64_t ld2, void* X1, void* X2, int32_t out_bf16, void* stream);
+
+/* Output layer of a colour MLP (voxurf_fine.py:141-151): out[i,:] =
+ * H[i,:width] W^T + b (+ add[i,:]) with FP32 accumulation; when cols is
+ * given the result is also stored (BF16 when cols_bf16) at cols[i*ld_cols
+ * + 0..2].  H: [n_rows, ldh] BF16 (in_bf16) or FP32; W: [3,width] FP32. */
+int vx_mlp_head(const void* H, int64_t n_rows, int64_t width, int64_t ldh, int32_t in_bf16, const float* W,
+                const float* b, const float* add, float* out, void* cols, int64_t ld_cols, int32_t cols_bf16,
+                void* stream);
+
+/* Compositing (voxurf_fine.py:753-777) straight into the output images:
+ * rgb = sum w*sigmoid(logit) + alphainv_last*bg, or with klogit (the
+ * k-branch) the same sum clamped to [0,1]; depth = sum w*step*stepdist.
+ * Written to out_rgb[3*ray_out[r] + c] and out_depth[ray_out[r]] (optional). */
+int vx_serve_composite(const vx_scene_desc* scenes_host, int32_t n_scenes, const int32_t* ray_scene, int64_t n_rays,
+                       int64_t max_steps, const void* rec, const int64_t* s2_off, const float* logit,
+                       const float* klogit, const float* alphainv_last, const int64_t* ray_out, float* out_rgb,
+                       float* out_depth, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -238,6 +238,30 @@ class OracleFine(nn.Module):
         return out
 
 
+def camera_rays_f32(c2w, fx, fy, cx, cy, H, W, inverse_y=True):
+    """get_rays + viewdirs (voxurf_fine.py:1001-1029, 1064) in float32 with
+    one rounding per operation: pixel centres i+0.5, j+0.5; dir =
+    [(i-cx)/fx, +-(j-cy)/fy, +-1]; rays_d[a] = (dir0*R[a,0] + dir1*R[a,1]) +
+    dir2*R[a,2]; viewdir = rays_d / |rays_d|.  Row-major over (j, i)."""
+    f = np.float32
+    c = np.asarray(c2w, np.float32)
+    jj, ii = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    i = ii.reshape(-1).astype(np.float32) + f(0.5)
+    j = jj.reshape(-1).astype(np.float32) + f(0.5)
+    d0 = (i - f(cx)) / f(fx)
+    d1 = (j - f(cy)) / f(fy)
+    if inverse_y:
+        d2 = np.ones_like(d0)
+    else:
+        d1 = -d1
+        d2 = -np.ones_like(d0)
+    d = np.stack([(d0 * c[a, 0] + d1 * c[a, 1]) + d2 * c[a, 2] for a in range(3)], -1).astype(np.float32)
+    n = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2])
+    v = (d / n[:, None]).astype(np.float32)
+    o = np.broadcast_to(c[:3, 3], d.shape).astype(np.float32).copy()
+    return o, d, v
+
+
 def neus_sdf_gradient(sdf, voxel_size):
     """voxurf_coarse.py:323-332, 'interpolate' mode."""
     g = torch.zeros([1, 3] + list(sdf.shape[-3:]), dtype=sdf.dtype)

@@ -66,7 +66,8 @@ def test_struct_sizes_match_c_layout():
                "vx_coarse_feature_cfg": _abi.CoarseFeatureCfg, "vx_coarse_features_args": _abi.CoarseFeaturesArgs,
                "vx_coarse_composite_args": _abi.CoarseCompositeArgs,
                "vx_coarse_composite_bwd_args": _abi.CoarseCompositeBwdArgs,
-               "vx_coarse_backward_args": _abi.CoarseBackwardArgs}
+               "vx_coarse_backward_args": _abi.CoarseBackwardArgs, "vx_scene_desc": _abi.SceneDesc,
+               "vx_view_chunk": _abi.ViewChunk}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "voxurf_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -117,6 +117,21 @@ class CoarseBackwardArgs(C.Structure):
     ]
 
 
+class SceneDesc(C.Structure):
+    _fields_ = [
+        ("grid", GridGeom), ("sdf_smooth", P), ("k0", P), ("k0_bf16", I32), ("voxel_size", F), ("mask", P),
+        ("mask_X", I64), ("mask_Y", I64), ("mask_Z", I64), ("mask_scale", F * 3), ("mask_shift", F * 3),
+        ("inv_s", F), ("stepdist", F), ("near", F), ("bg", F), ("fast_color_thres", F),
+    ]
+
+
+class ViewChunk(C.Structure):
+    _fields_ = [
+        ("c2w", F * 12), ("fx", F), ("fy", F), ("cx", F), ("cy", F), ("W", I32), ("inverse_y", I32),
+        ("scene", I32), ("reserved", I32), ("pix0", I64), ("ray0", I64), ("out0", I64),
+    ]
+
+
 _STRUCT_FNS = {
     "vx_coarse_march": CoarseMarchArgs,
     "vx_coarse_features": CoarseFeaturesArgs,
@@ -129,6 +144,16 @@ _STRUCT_FNS = {
     "vx_fine_composite": FineCompositeArgs,
     "vx_fine_composite_backward": FineCompositeBwdArgs,
     "vx_fine_backward": FineBackwardArgs,
+}
+
+_SERVE_SIGNATURES = {
+    "vx_serve_rays": [P, I32, I64, P, P, P, P, P, P],
+    "vx_serve_march": ["scenes", I32, P, P, P, P, I64, I64, P, P, P, P],
+    "vx_serve_rows": [P, I64, P, P],
+    "vx_serve_features": ["scenes", I32, C.POINTER(FineFeatureCfg), P, P, P, P, I64, P, P, P, I64, I64, I64, P, P,
+                          I32, P],
+    "vx_mlp_head": [P, I64, I64, I64, I32, P, P, P, P, P, I64, I32, P],
+    "vx_serve_composite": ["scenes", I32, P, I64, I64, P, P, P, P, P, P, P, P, P],
 }
 
 _declared = False
@@ -159,6 +184,11 @@ def _declare():
     lib.vx_smooth_grad_tv_scratch_bytes.restype = C.c_size_t
     lib.vx_smooth_grad_tv.argtypes = [P, P, I64, I64, I64, F, P, P, P]
     lib.vx_smooth_grad_tv.restype = C.c_int
+    SP = C.POINTER(SceneDesc)
+    for name, args in _SERVE_SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = [SP if a == "scenes" else a for a in args]
+        fn.restype = C.c_int
     _declared = True
 
 
@@ -183,4 +213,4 @@ def call(name: str, *args) -> None:
 def struct_names() -> list[str]:
     return list(_STRUCT_FNS) + ["vx_smooth3d", "vx_smooth3d_adjoint", "vx_grid_sample", "vx_grid_sample_backward",
                                 "vx_sdf_gradient_grid", "vx_sdf_gradient_grid_adjoint",
-                                "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv"]
+                                "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv"] + list(_SERVE_SIGNATURES)

@@ -35,15 +35,17 @@ FINE_RENDER_KWARGS = dict(near=0.1, far=6.0, bg=0, stepsize=0.5, inverse_y=True,
 
 
 def build_fine_model(R: int = 256, precision: str = "fp32", device="cuda", seed: int = 0, scene: str = "sphere_torus",
-                     mask_voxels: float | None = None, width: int = 192, smooth: bool = True):
+                     mask_voxels: float | None = None, width: int = 192, smooth: bool = True,
+                     shape: tuple | None = None):
     """Fine Voxurf model with the synthetic scene loaded.  mask_voxels: if
     given, a MaskGrid of |SDF| < mask_voxels*voxel_size (the |SDF| < 0.05
-    mask of the 256^3 workload is mask_voxels = 6.4)."""
+    mask of the 256^3 workload is mask_voxels = 6.4).  shape: the
+    sphere_torus sizes (sphere r, torus R, torus r)."""
     from .grid import MaskGrid
     from .voxurf_fine import Voxurf
 
     torch.manual_seed(seed)
-    sdf = torch.from_numpy(synthetic.make_sdf(scene, R, seed=seed))
+    sdf = torch.from_numpy(synthetic.make_sdf(scene, R, seed=seed, shape=shape))
     mask = None
     if mask_voxels is not None:
         thr = mask_voxels * 2.0 / R
@@ -62,6 +64,25 @@ def build_fine_model(R: int = 256, precision: str = "fp32", device="cuda", seed:
     if precision == "bf16":
         model.refresh_k0_shadow()
     return model
+
+
+# Render-server scenes: sphere_torus with different sizes per scene
+# (sphere r, torus R, torus r), each with its own seed.
+SERVE_SHAPES = [(0.45, 0.6, 0.15), (0.40, 0.55, 0.12), (0.50, 0.65, 0.18), (0.35, 0.50, 0.10)]
+
+
+def trained_s_val(step: int = 20000, s_ratio: float = 50.0, s_start: float = 0.05, step_start: int = 0) -> float:
+    """s_val the fine stage reaches at `step` (voxurf_fine.py:466-469; the
+    dtu_e2e fine schedule ends at N_iters = 20000, configs/dtu_e2e/fine.py:32)."""
+    return 1.0 / (step + s_ratio / s_start - step_start) * s_ratio
+
+
+def build_serve_models(R: int = 256, precision: str = "bf16", device="cuda", n: int = 4, mask_voxels: float = 6.4,
+                       width: int = 192, seed: int = 100):
+    """The render server's resident scenes: fine models of SERVE_SHAPES[i]
+    (seed + i) with the |SDF| < mask_voxels voxel mask."""
+    return [build_fine_model(R, precision, device=device, seed=seed + i, mask_voxels=mask_voxels, width=width,
+                             shape=SERVE_SHAPES[i % len(SERVE_SHAPES)]) for i in range(n)]
 
 
 def coarse_model_kwargs(R: int = 96, precision: str = "fp32", width: int = 128) -> dict:

@@ -44,6 +44,32 @@ __device__ __forceinline__ void sample_point(const RayFrame& f, float stepdist, 
   for (int a = 0; a < 3; ++a) p[a] = fadd(f.st[a], fmul(f.dr[a], dist));
 }
 
+// Pinhole ray through pixel centre (i, j) (+0.5 already added) of a camera
+// with row-major 3x4 camera-to-world c2w (get_rays, voxurf_fine.py:1001-1029;
+// viewdir = d/|d|, :1064).  inverse_y selects OpenCV axes (+y down, +z fwd).
+// One rounding per operation, so the rays are reproducible bit for bit.
+__device__ __forceinline__ void pinhole_ray(const float* c2w, float fx, float fy, float cx, float cy, int inverse_y,
+                                            float i, float j, float o[3], float d[3], float v[3]) {
+  float dir[3];
+  dir[0] = fdiv(fsub(i, cx), fx);
+  if (inverse_y) {
+    dir[1] = fdiv(fsub(j, cy), fy);
+    dir[2] = 1.f;
+  } else {
+    dir[1] = -fdiv(fsub(j, cy), fy);
+    dir[2] = -1.f;
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    d[a] = fadd(fadd(fmul(dir[0], c2w[4 * a + 0]), fmul(dir[1], c2w[4 * a + 1])), fmul(dir[2], c2w[4 * a + 2]));
+  const float nrm = __fsqrt_rn(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = c2w[4 * a + 3];
+    v[a] = fdiv(d[a], nrm);
+  }
+}
+
 // ---- SDF value + finite-difference gradient (sample_sdfs, one displacement) -
 struct Probe {
   float fm, fp;     // values at index -d and +d (clamped)

@@ -196,41 +196,6 @@ __global__ void maskcache_lookup_kernel(const uint8_t* __restrict__ world, const
   out[p] = v;
 }
 
-// Rays of one pinhole view (get_rays + viewdirs, voxurf_fine.py:1001-1029,
-// 1064): pixel (i, j) -> dir = [(i+.5-cx)/fx, +-(j+.5-cy)/fy, +-1] rotated by
-// c2w[:3,:3]; origin c2w[:3,3].  inverse_y selects the OpenCV convention.
-struct CamParams {
-  float R[9], t[3];
-  float fx, fy, cx, cy;
-  int H, W, inverse_y;
-};
-
-__global__ void camera_rays_kernel(CamParams c, float* __restrict__ rays_o, float* __restrict__ rays_d,
-                                   float* __restrict__ viewdirs) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= (int64_t)c.H * c.W) return;
-  const float i = (float)(p % c.W) + 0.5f, j = (float)(p / c.W) + 0.5f;
-  float dir[3];
-  dir[0] = (i - c.cx) / c.fx;
-  if (c.inverse_y) {
-    dir[1] = (j - c.cy) / c.fy;
-    dir[2] = 1.f;
-  } else {
-    dir[1] = -(j - c.cy) / c.fy;
-    dir[2] = -1.f;
-  }
-  float d[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) d[a] = dir[0] * c.R[3 * a + 0] + dir[1] * c.R[3 * a + 1] + dir[2] * c.R[3 * a + 2];
-  const float inv = 1.f / sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    rays_o[3 * p + a] = c.t[a];
-    rays_d[3 * p + a] = d[a];
-    viewdirs[3 * p + a] = d[a] * inv;
-  }
-}
-
 }  // namespace vx
 
 using namespace vx;
@@ -322,27 +287,6 @@ int vx_sample_pts_fill(const float* rays_o, const float* rays_d, const float* xy
   sample_fill_kernel<<<blocks, VX_THREADS, 0, as_stream(stream)>>>(rays_o, rays_d, xyz_min, xyz_max, t_min, offsets,
                                                                   stepdist, n_rays, capacity, ray_pts, mask_outbbox,
                                                                   ray_id, step_id, device_error_ptr());
-  return launch_status();
-}
-
-int vx_camera_rays(const float* c2w_host, float fx, float fy, float cx, float cy, int64_t H, int64_t W,
-                   int inverse_y, float* rays_o, float* rays_d, float* viewdirs, void* stream) {
-  if (!c2w_host || H < 0 || W < 0 || H * W > INT32_MAX) return VX_ERR_ARG;
-  if (H * W == 0) return VX_OK;
-  if (!rays_o || !rays_d || !viewdirs) return VX_ERR_ARG;
-  CamParams c;
-  for (int a = 0; a < 3; ++a) {
-    for (int b = 0; b < 3; ++b) c.R[3 * a + b] = c2w_host[4 * a + b];
-    c.t[a] = c2w_host[4 * a + 3];
-  }
-  c.fx = fx;
-  c.fy = fy;
-  c.cx = cx;
-  c.cy = cy;
-  c.H = (int)H;
-  c.W = (int)W;
-  c.inverse_y = inverse_y;
-  camera_rays_kernel<<<grid_for(H * W), VX_THREADS, 0, as_stream(stream)>>>(c, rays_o, rays_d, viewdirs);
   return launch_status();
 }
 

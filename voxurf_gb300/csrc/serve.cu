@@ -1,0 +1,543 @@
+// Render-server kernels: the inference form of the fine model's forward
+// (lib/voxurf_fine.py:620-802 with global_step = None) over the rays of one
+// tick, which mixes requests for several resident scenes.  Every stage is
+// one launch for the whole tick; the scene of a ray selects its grids and
+// constants from a table that each block copies into shared memory.
+//
+//   rays      : per ray, its view chunk (binary search) -> get_rays.
+//   march     : per ray (one warp, 32 samples per iteration), exact samples,
+//               mask, SDF + FD normal, NeuS alpha, transmittance scan with the
+//               T < 1e-3 stop; only shaded samples (weight > thres) are kept,
+//               as 8-byte (step, weight) records.
+//   rows      : row -> ray map of the dense shaded rows.
+//   features  : MLP input rows (fine_feature_rows), BF16 or FP32.
+//   mlp_head  : the 192 -> 3 output layer with FP32 accumulation (the
+//               hidden layers are GEMMs issued by the host).
+//   composite : per ray, sum w*sigmoid(logit) + alphainv_last*bg (clamped in
+//               the k-branch) and depth, written into the output images.
+#include <math.h>
+#include "common.cuh"
+#include "fine_device.cuh"
+#include "trilinear.cuh"
+
+namespace vx {
+
+struct SceneK {
+  GridGeom g;
+  const float* sdf;
+  const float* k0f;
+  const __nv_bfloat16* k0h;
+  const uint8_t* mask;
+  int mX, mY, mZ;
+  float mscale[3], mshift[3];
+  float vs, inv_s, stepdist, near, bg, thres;
+};
+
+struct SceneTable {
+  SceneK s[VX_SERVE_MAX_SCENES];
+  int n;
+};
+
+static_assert(sizeof(SceneK) % 4 == 0, "scene table is copied as 32-bit words");
+
+// Cooperative copy of the (by-value) scene table into shared memory.
+__device__ __forceinline__ void load_scenes(const SceneTable& T, SceneK* sh) {
+  const int words = T.n * (int)(sizeof(SceneK) / 4);
+  const int* src = reinterpret_cast<const int*>(T.s);
+  int* dst = reinterpret_cast<int*>(sh);
+  for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+}
+
+// ---- rays of a tick ---------------------------------------------------------
+__global__ void serve_rays_kernel(const vx_view_chunk* __restrict__ ch, int n_chunks, int64_t n_rays,
+                                  float* __restrict__ rays_o, float* __restrict__ rays_d,
+                                  float* __restrict__ viewdirs, int* __restrict__ ray_scene,
+                                  int64_t* __restrict__ ray_out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rays) return;
+  int lo = 0, hi = n_chunks - 1;  // last chunk with ray0 <= r
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (ch[mid].ray0 <= r) lo = mid; else hi = mid - 1;
+  }
+  const vx_view_chunk& c = ch[lo];
+  const int64_t pix = c.pix0 + (r - c.ray0);
+  const float i = (float)(pix % c.W) + 0.5f, j = (float)(pix / c.W) + 0.5f;
+  float o[3], d[3], v[3];
+  pinhole_ray(c.c2w, c.fx, c.fy, c.cx, c.cy, c.inverse_y, i, j, o, d, v);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    rays_o[3 * r + a] = o[a];
+    rays_d[3 * r + a] = d[a];
+    viewdirs[3 * r + a] = v[a];
+  }
+  ray_scene[r] = c.scene;
+  ray_out[r] = c.out0 + (r - c.ray0);
+}
+
+__global__ void camera_rays_kernel(vx_view_chunk c, int64_t n, float* __restrict__ rays_o,
+                                   float* __restrict__ rays_d, float* __restrict__ viewdirs) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const float i = (float)(p % c.W) + 0.5f, j = (float)(p / c.W) + 0.5f;
+  float o[3], d[3], v[3];
+  pinhole_ray(c.c2w, c.fx, c.fy, c.cx, c.cy, c.inverse_y, i, j, o, d, v);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    rays_o[3 * p + a] = o[a];
+    rays_d[3 * p + a] = d[a];
+    viewdirs[3 * p + a] = v[a];
+  }
+}
+
+// ---- march ------------------------------------------------------------------
+struct ServeMarchParams {
+  SceneTable T;
+  const float* rays_o;
+  const float* rays_d;
+  const float* viewdirs;
+  const int* ray_scene;
+  int n_rays;
+  int max_steps;
+  uint2* rec;  // [n_rays*max_steps] {step, weight bits} of the shaded samples
+  int* n2;
+  float* alphainv_last;
+  int* err;
+};
+
+__global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
+  __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
+  load_scenes(P.T, sh);
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int sc = P.ray_scene[r];
+  if (sc < 0 || sc >= P.T.n) {
+    if (lane == 0) {
+      set_device_error(P.err, VX_ERR_BOUNDS);
+      P.n2[r] = 0;
+      P.alphainv_last[r] = 1.f;
+    }
+    return;
+  }
+  const SceneK& S = sh[sc];
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, S.g.mn, S.g.mx, S.near, S.stepdist);
+  int64_t n_steps = f.n_steps;
+  if (n_steps > P.max_steps) {
+    if (lane == 0) set_device_error(P.err, VX_ERR_CAPACITY);
+    n_steps = P.max_steps;
+  }
+  uint2* rec = P.rec + (int64_t)r * P.max_steps;
+  double carry = 1.0, last = 1.0;
+  int cnt2 = 0;
+  bool stopped = false;
+  for (int base = 0; base < n_steps && !stopped; base += 32) {
+    const int k = base + lane;
+    bool keep = false;
+    float alpha = 0.f;
+    if (k < n_steps) {
+      float p[3];
+      sample_point(f, S.stepdist, k, p);
+      bool inb = !outside_bbox(p, S.g.mn, S.g.mx);
+      if (inb && S.mask) inb = mask_lookup(S.mask, S.mX, S.mY, S.mZ, S.mscale, S.mshift, p);
+      if (inb) {
+        float ind[3], s, gr[3];
+        to_index(S.g, p, ind);
+        sdf_and_grad(S.sdf, S.g, S.vs, ind, &s, gr);
+        alpha = neus_alpha(s, gr, v, S.inv_s, S.stepdist).alpha;
+        keep = alpha > S.thres;
+      }
+    }
+    const unsigned keep_mask = __ballot_sync(0xffffffffu, keep);
+    if (keep_mask == 0u) continue;
+    const double fct = keep ? 1.0 - (double)alpha : 1.0;
+    const double incl = warp_inclusive_prod(fct) * carry;
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = carry;
+    const unsigned stop_mask = __ballot_sync(0xffffffffu, keep && incl < 1e-3);
+    unsigned live = keep_mask;
+    if (stop_mask) {
+      const int ks = __ffs(stop_mask) - 1;
+      live &= (ks == 31) ? 0xffffffffu : ((2u << ks) - 1u);
+      last = __shfl_sync(0xffffffffu, incl, ks);
+      stopped = true;
+    }
+    const bool mine = (live >> lane) & 1u;
+    const float w = (float)excl * alpha;
+    const bool s2 = mine && (w > S.thres);
+    const unsigned s2_mask = __ballot_sync(0xffffffffu, s2);
+    if (s2) rec[cnt2 + __popc(s2_mask & lt_mask)] = make_uint2((unsigned)k, __float_as_uint(w));
+    cnt2 += __popc(s2_mask);
+    if (!stopped) carry = __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) {
+    P.n2[r] = cnt2;
+    P.alphainv_last[r] = (float)(stopped ? last : carry);
+  }
+}
+
+// ---- row -> ray --------------------------------------------------------------
+__global__ void __launch_bounds__(256) serve_rows_kernel(const int64_t* __restrict__ s2_off, int n_rays,
+                                                         int* __restrict__ ray2) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= n_rays) return;
+  const int64_t b = s2_off[r], e = s2_off[r + 1];
+  for (int64_t i = b + lane_id(); i < e; i += 32) ray2[i] = r;
+}
+
+// ---- features ----------------------------------------------------------------
+struct ServeFeatParams {
+  SceneTable T;
+  FeatLayout L;
+  const float* rays_o;
+  const float* rays_d;
+  const float* viewdirs;
+  const int* ray_scene;
+  int max_steps;
+  const uint2* rec;
+  const int64_t* s2_off;
+  const int* ray2;
+  int64_t n_rows;
+  int64_t ld1, ld2;
+  void* X1;
+  void* X2;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) {
+  __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
+  load_scenes(P.T, sh);
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= P.n_rows) return;
+  const int r = P.ray2[row];
+  const SceneK& S = sh[P.ray_scene[r]];  // validated by the march
+  const int j = (int)(row - P.s2_off[r]);
+  const int k = (int)P.rec[(int64_t)r * P.max_steps + j].x;
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, S.g.mn, S.g.mx, S.near, S.stepdist);
+  float p[3];
+  sample_point(f, S.stepdist, k, p);
+  T* x1 = reinterpret_cast<T*>(P.X1) + row * P.ld1;
+  T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
+  float g1[3];
+  fine_feature_rows(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
+}
+
+// ---- output layer ------------------------------------------------------------
+constexpr int HEAD_MAX_WIDTH = 256;
+
+__device__ __forceinline__ float to_f(float x) { return x; }
+__device__ __forceinline__ float to_f(__nv_bfloat16 x) { return __bfloat162float(x); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) mlp_head_kernel(const T* __restrict__ H, int64_t n_rows, int width,
+                                                       int64_t ldh, const float* __restrict__ W,
+                                                       const float* __restrict__ b, const float* __restrict__ add,
+                                                       float* __restrict__ out, void* cols, int64_t ld_cols,
+                                                       int cols_bf16) {
+  constexpr int Q = HEAD_MAX_WIDTH / 32;
+  const int lane = lane_id();
+  float w0[Q], w1[Q], w2[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int c = lane + 32 * q;
+    const bool in = c < width;
+    w0[q] = in ? W[c] : 0.f;
+    w1[q] = in ? W[width + c] : 0.f;
+    w2[q] = in ? W[2 * width + c] : 0.f;
+  }
+  const float b0 = b ? b[0] : 0.f, b1 = b ? b[1] : 0.f, b2 = b ? b[2] : 0.f;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n_rows; row += warps) {
+    const T* h = H + row * ldh;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int c = lane + 32 * q;
+      if (c < width) {
+        const float x = to_f(h[c]);
+        a0 += x * w0[q];
+        a1 += x * w1[q];
+        a2 += x * w2[q];
+      }
+    }
+    a0 = warp_sum(a0);
+    a1 = warp_sum(a1);
+    a2 = warp_sum(a2);
+    if (lane == 0) {
+      a0 += b0;
+      a1 += b1;
+      a2 += b2;
+      if (add) {
+        a0 += add[3 * row + 0];
+        a1 += add[3 * row + 1];
+        a2 += add[3 * row + 2];
+      }
+      out[3 * row + 0] = a0;
+      out[3 * row + 1] = a1;
+      out[3 * row + 2] = a2;
+      if (cols) {
+        if (cols_bf16) {
+          __nv_bfloat16* cp = reinterpret_cast<__nv_bfloat16*>(cols) + row * ld_cols;
+          cp[0] = __float2bfloat16_rn(a0);
+          cp[1] = __float2bfloat16_rn(a1);
+          cp[2] = __float2bfloat16_rn(a2);
+        } else {
+          float* cp = reinterpret_cast<float*>(cols) + row * ld_cols;
+          cp[0] = a0;
+          cp[1] = a1;
+          cp[2] = a2;
+        }
+      }
+    }
+  }
+}
+
+// ---- composite -----------------------------------------------------------------
+struct ServeCompositeParams {
+  SceneTable T;
+  const int* ray_scene;
+  int n_rays;
+  int max_steps;
+  const uint2* rec;
+  const int64_t* s2_off;
+  const float* logit;
+  const float* klogit;  // null: no k-branch
+  const float* alphainv_last;
+  const int64_t* ray_out;
+  float* out_rgb;
+  float* out_depth;
+};
+
+__global__ void __launch_bounds__(256) serve_composite_kernel(ServeCompositeParams P) {
+  __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
+  load_scenes(P.T, sh);
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  const int sc = P.ray_scene[r];
+  if (sc < 0 || sc >= P.T.n) return;  // reported by the march
+  const SceneK& S = sh[sc];
+  const int64_t b = P.s2_off[r], e = P.s2_off[r + 1];
+  const uint2* rec = P.rec + (int64_t)r * P.max_steps;
+  const float* lg = P.klogit ? P.klogit : P.logit;
+  float acc[3] = {0.f, 0.f, 0.f}, dep = 0.f;
+  for (int64_t i = b + lane; i < e; i += 32) {
+    const uint2 rc = rec[i - b];
+    const float w = __uint_as_float(rc.y);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] += w * sigmoidf_(lg[3 * i + c]);
+    dep += w * ((float)rc.x * S.stepdist);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) acc[c] = warp_sum(acc[c]);
+  dep = warp_sum(dep);
+  if (lane == 0) {
+    const float bgt = P.alphainv_last[r] * S.bg;
+    const int64_t o = P.ray_out[r];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float x = acc[c] + bgt;
+      P.out_rgb[3 * o + c] = P.klogit ? fminf(fmaxf(x, 0.f), 1.f) : x;
+    }
+    if (P.out_depth) P.out_depth[o] = dep;
+  }
+}
+
+// ---- host helpers ----------------------------------------------------------------
+static int scene_table(const vx_scene_desc* D, int n, SceneTable& T) {
+  if (!D || n < 1 || n > VX_SERVE_MAX_SCENES) return VX_ERR_ARG;
+  T.n = n;
+  for (int i = 0; i < n; ++i) {
+    const vx_scene_desc& d = D[i];
+    SceneK& s = T.s[i];
+    if (!d.sdf_smooth || !d.k0 || d.grid.X < 2 || d.grid.Y < 2 || d.grid.Z < 2) return VX_ERR_ARG;
+    if (d.grid.X > INT32_MAX / d.grid.Y / d.grid.Z) return VX_ERR_TOO_LARGE;
+    if (!(d.stepdist > 0.f) || !(d.voxel_size > 0.f)) return VX_ERR_ARG;
+    s.g.X = (int)d.grid.X;
+    s.g.Y = (int)d.grid.Y;
+    s.g.Z = (int)d.grid.Z;
+    for (int a = 0; a < 3; ++a) {
+      s.g.mn[a] = d.grid.xyz_min[a];
+      s.g.mx[a] = d.grid.xyz_max[a];
+      s.mscale[a] = d.mask_scale[a];
+      s.mshift[a] = d.mask_shift[a];
+    }
+    s.sdf = d.sdf_smooth;
+    s.k0f = d.k0_bf16 ? nullptr : reinterpret_cast<const float*>(d.k0);
+    s.k0h = d.k0_bf16 ? reinterpret_cast<const __nv_bfloat16*>(d.k0) : nullptr;
+    s.mask = d.mask;
+    s.mX = (int)d.mask_X;
+    s.mY = (int)d.mask_Y;
+    s.mZ = (int)d.mask_Z;
+    s.vs = d.voxel_size;
+    s.inv_s = d.inv_s;
+    s.stepdist = d.stepdist;
+    s.near = d.near;
+    s.bg = d.bg;
+    s.thres = d.fast_color_thres;
+  }
+  for (int i = n; i < VX_SERVE_MAX_SCENES; ++i) T.s[i] = T.s[0];
+  return VX_OK;
+}
+
+static unsigned warp_blocks(int64_t n_warps) { return (unsigned)((n_warps + 7) / 8); }
+
+}  // namespace vx
+
+using namespace vx;
+
+extern "C" {
+
+int vx_camera_rays(const float* c2w_host, float fx, float fy, float cx, float cy, int64_t H, int64_t W,
+                   int inverse_y, float* rays_o, float* rays_d, float* viewdirs, void* stream) {
+  if (!c2w_host || H < 0 || W < 0 || H * W > INT32_MAX) return VX_ERR_ARG;
+  if (H * W == 0) return VX_OK;
+  if (!rays_o || !rays_d || !viewdirs) return VX_ERR_ARG;
+  vx_view_chunk c = {};
+  for (int q = 0; q < 12; ++q) c.c2w[q] = c2w_host[q];
+  c.fx = fx;
+  c.fy = fy;
+  c.cx = cx;
+  c.cy = cy;
+  c.W = (int32_t)W;
+  c.inverse_y = inverse_y;
+  camera_rays_kernel<<<grid_for(H * W), VX_THREADS, 0, as_stream(stream)>>>(c, H * W, rays_o, rays_d, viewdirs);
+  return launch_status();
+}
+
+int vx_serve_rays(const vx_view_chunk* chunks, int32_t n_chunks, int64_t n_rays, float* rays_o, float* rays_d,
+                  float* viewdirs, int32_t* ray_scene, int64_t* ray_out, void* stream) {
+  if (n_rays < 0 || n_rays > INT32_MAX) return VX_ERR_ARG;
+  if (n_rays == 0) return VX_OK;
+  if (!chunks || n_chunks < 1 || !rays_o || !rays_d || !viewdirs || !ray_scene || !ray_out) return VX_ERR_ARG;
+  serve_rays_kernel<<<grid_for(n_rays), VX_THREADS, 0, as_stream(stream)>>>(chunks, n_chunks, n_rays, rays_o, rays_d,
+                                                                           viewdirs, ray_scene, ray_out);
+  return launch_status();
+}
+
+int vx_serve_march(const vx_scene_desc* scenes_host, int32_t n_scenes, const float* rays_o, const float* rays_d,
+                   const float* viewdirs, const int32_t* ray_scene, int64_t n_rays, int64_t max_steps, void* rec,
+                   int32_t* n2, float* alphainv_last, void* stream) {
+  if (n_rays < 0 || n_rays > INT32_MAX || max_steps < 1 || max_steps > INT32_MAX) return VX_ERR_ARG;
+  if (n_rays == 0) return VX_OK;
+  ServeMarchParams P;
+  int s = scene_table(scenes_host, n_scenes, P.T);
+  if (s) return s;
+  if (!rays_o || !rays_d || !viewdirs || !ray_scene || !rec || !n2 || !alphainv_last) return VX_ERR_ARG;
+  P.rays_o = rays_o;
+  P.rays_d = rays_d;
+  P.viewdirs = viewdirs;
+  P.ray_scene = ray_scene;
+  P.n_rays = (int)n_rays;
+  P.max_steps = (int)max_steps;
+  P.rec = reinterpret_cast<uint2*>(rec);
+  P.n2 = n2;
+  P.alphainv_last = alphainv_last;
+  P.err = device_error_ptr();
+  serve_march_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, void* stream) {
+  if (n_rays < 0 || n_rays > INT32_MAX) return VX_ERR_ARG;
+  if (n_rays == 0) return VX_OK;
+  if (!s2_off || !ray2) return VX_ERR_ARG;
+  serve_rows_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(s2_off, (int)n_rays, ray2);
+  return launch_status();
+}
+
+int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const vx_fine_feature_cfg* cfg,
+                      const float* rays_o, const float* rays_d, const float* viewdirs, const int32_t* ray_scene,
+                      int64_t max_steps, const void* rec, const int64_t* s2_off, const int32_t* ray2, int64_t n_rows,
+                      int64_t ld1, int64_t ld2, void* X1, void* X2, int32_t out_bf16, void* stream) {
+  if (n_rows < 0 || !cfg || max_steps < 1 || max_steps > INT32_MAX) return VX_ERR_ARG;
+  if (n_rows == 0) return VX_OK;
+  ServeFeatParams P;
+  int s = scene_table(scenes_host, n_scenes, P.T);
+  if (s) return s;
+  s = fill_feat_layout(cfg, P.L);
+  if (s) return s;
+  if (ld1 < x1_cols(cfg) || ld2 < x2_cols(cfg) + 3) return VX_ERR_ARG;
+  if (!rays_o || !rays_d || !viewdirs || !ray_scene || !rec || !s2_off || !ray2 || !X1 || !X2) return VX_ERR_ARG;
+  P.rays_o = rays_o;
+  P.rays_d = rays_d;
+  P.viewdirs = viewdirs;
+  P.ray_scene = ray_scene;
+  P.max_steps = (int)max_steps;
+  P.rec = reinterpret_cast<const uint2*>(rec);
+  P.s2_off = s2_off;
+  P.ray2 = ray2;
+  P.n_rows = n_rows;
+  P.ld1 = ld1;
+  P.ld2 = ld2;
+  P.X1 = X1;
+  P.X2 = X2;
+  const unsigned b = (unsigned)((n_rows + 127) / 128);
+  if (out_bf16)
+    serve_features_kernel<__nv_bfloat16><<<b, 128, 0, as_stream(stream)>>>(P);
+  else
+    serve_features_kernel<float><<<b, 128, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+int vx_mlp_head(const void* H, int64_t n_rows, int64_t width, int64_t ldh, int32_t in_bf16, const float* W,
+                const float* b, const float* add, float* out, void* cols, int64_t ld_cols, int32_t cols_bf16,
+                void* stream) {
+  if (n_rows < 0 || width < 1 || ldh < width) return VX_ERR_ARG;
+  if (width > HEAD_MAX_WIDTH) return VX_ERR_UNSUPPORTED;
+  if (n_rows == 0) return VX_OK;
+  if (!H || !W || !out || (cols && ld_cols < 3)) return VX_ERR_ARG;
+  const int64_t blocks_needed = (n_rows + 7) / 8;
+  const unsigned blocks = (unsigned)(blocks_needed < (int64_t)sm_count() * 8 ? blocks_needed : sm_count() * 8);
+  if (in_bf16)
+    mlp_head_kernel<__nv_bfloat16><<<blocks, 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const __nv_bfloat16*>(H), n_rows, (int)width, ldh, W, b, add, out, cols, ld_cols, cols_bf16);
+  else
+    mlp_head_kernel<float><<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const float*>(H), n_rows,
+                                                                  (int)width, ldh, W, b, add, out, cols, ld_cols,
+                                                                  cols_bf16);
+  return launch_status();
+}
+
+int vx_serve_composite(const vx_scene_desc* scenes_host, int32_t n_scenes, const int32_t* ray_scene, int64_t n_rays,
+                       int64_t max_steps, const void* rec, const int64_t* s2_off, const float* logit,
+                       const float* klogit, const float* alphainv_last, const int64_t* ray_out, float* out_rgb,
+                       float* out_depth, void* stream) {
+  if (n_rays < 0 || n_rays > INT32_MAX || max_steps < 1 || max_steps > INT32_MAX) return VX_ERR_ARG;
+  if (n_rays == 0) return VX_OK;
+  ServeCompositeParams P;
+  int s = scene_table(scenes_host, n_scenes, P.T);
+  if (s) return s;
+  if (!ray_scene || !rec || !s2_off || !logit || !alphainv_last || !ray_out || !out_rgb) return VX_ERR_ARG;
+  P.ray_scene = ray_scene;
+  P.n_rays = (int)n_rays;
+  P.max_steps = (int)max_steps;
+  P.rec = reinterpret_cast<const uint2*>(rec);
+  P.s2_off = s2_off;
+  P.logit = logit;
+  P.klogit = klogit;
+  P.alphainv_last = alphainv_last;
+  P.ray_out = ray_out;
+  P.out_rgb = out_rgb;
+  P.out_depth = out_depth;
+  serve_composite_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+}  // extern "C"

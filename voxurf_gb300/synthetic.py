@@ -101,11 +101,12 @@ def sdf_torus(p, R=0.6, r=0.15):
     return np.sqrt(q * q + p[..., 2] ** 2) - r
 
 
-def make_sdf(kind: str, R: int, seed: int = 0, noise: float | None = None) -> np.ndarray:
+def make_sdf(kind: str, R: int, seed: int = 0, noise: float | None = None, shape: tuple | None = None) -> np.ndarray:
     """float32 [R, R, R] SDF grid.
 
     kind: 'sphere' (r=0.5, noise 0.01 -- coarse stage scene),
-          'sphere_torus' (min(sphere r=0.45, torus R=0.6 r=0.15), noise 0.005),
+          'sphere_torus' (min(sphere r=0.45, torus R=0.6 r=0.15), noise 0.005;
+                          shape = (sphere r, torus R, torus r) overrides the sizes),
           'spheres64' (64 spheres, centres U(-0.8,0.8)^3, radii U(0.05,0.2)).
     """
     rng = np.random.default_rng(seed)
@@ -114,7 +115,8 @@ def make_sdf(kind: str, R: int, seed: int = 0, noise: float | None = None) -> np
         s = sdf_sphere(p, 0.5)
         sd = 0.01 if noise is None else noise
     elif kind == "sphere_torus":
-        s = np.minimum(sdf_sphere(p, 0.45), sdf_torus(p, 0.6, 0.15))
+        rs, tR, tr = (0.45, 0.6, 0.15) if shape is None else shape
+        s = np.minimum(sdf_sphere(p, rs), sdf_torus(p, tR, tr))
         sd = 0.005 if noise is None else noise
     elif kind == "spheres64":
         c = rng.uniform(-0.8, 0.8, size=(64, 3))
