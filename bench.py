@@ -47,9 +47,11 @@ MASK_VOXELS = 6.4  # |SDF| < 0.05 at voxel size 2/256
 # p_new, exp_avg, exp_avg_sq (12 B) = 28 B (TV neighbour reads hit L1/L2).
 K0_ELEMS = R ** 3 * 12
 SWEEP_BYTES_PER_ELEM = 28
-# DRAM traffic of one k0 sweep launch from an ncu capture of this workload's
-# kernel (profiles/grid_tv_adam_k0.md); None until captured.
-SWEEP_NCU_TRAFFIC = None
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k0 sweep
+# launch: ncu capture at 128^3 (402.69 MB read + 253.78 MB written for
+# 25.17M elements, profiles/grid_tv_adam_row_k0.md) scaled by the element
+# count to 256^3 (x8).
+SWEEP_NCU_TRAFFIC = (402.692608e6 + 253.783552e6) * 8 if R == 256 else None
 
 
 def parse():
@@ -63,14 +65,17 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-render", action="store_true", help="skip the render-server measurement")
     p.add_argument("--render-requests", type=int, default=120)
+    p.add_argument("--render-only", action="store_true", help="only the render-server measurement (profiling)")
+    p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
     p.add_argument("--grid", type=int, default=256, help="grid resolution (256 is the benchmark; smaller sizes "
                                                          "serve profiler captures)")
     args = p.parse_args()
-    global R, K0_ELEMS, MASK_VOXELS
+    global R, K0_ELEMS, MASK_VOXELS, SWEEP_NCU_TRAFFIC
     if args.grid != R:
         R = args.grid
         K0_ELEMS = R ** 3 * 12
         MASK_VOXELS = 0.05 / (2.0 / R)
+        SWEEP_NCU_TRAFFIC = None
     return args
 
 
@@ -170,14 +175,17 @@ def run_ours(args, world, rank, local):
     from voxurf_gb300.train import FineTrainer
 
     dev = torch.device("cuda", local)
+    if args.render_only:
+        print(json.dumps({"render": run_render(args, dev)}))
+        return
     rk = dict(configs.FINE_RENDER_KWARGS)
     n_b = args.warmup + args.steps
     host = make_batches(n_b, seed=rank)
     dev_batches = [torch.from_numpy(a).to(dev) for a in host]
 
-    def build(precision):
+    def build(precision, graphed=False):
         model = configs.build_fine_model(R, precision, device=dev, seed=0, mask_voxels=MASK_VOXELS)
-        return model, FineTrainer(model, n_rays=N_RAYS)
+        return model, FineTrainer(model, n_rays=N_RAYS, graphed=graphed)
 
     def barrier():
         if world > 1:
@@ -251,10 +259,13 @@ def run_ours(args, world, rank, local):
     # ---- fused BF16 variant --------------------------------------------------
     bf16 = None
     if not args.no_bf16:
-        model, tr = build("bf16")
+        # k0 sampled from BF16, both MLPs in BF16 (FP32 accumulation), the
+        # step replayed from CUDA graphs (fused_step.GraphedFineStep)
+        model, tr = build("bf16", graphed=True)
         for i in range(args.warmup):
             tr.step(dev_batches[0][i], dev_batches[1][i], dev_batches[2][i], dev_batches[3][i], rk)
         barrier()
+        l0 = _native.launch_count() + tr._engine.launches_replayed
         b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         b0.record()
         for i in range(args.warmup, n_b):
@@ -263,7 +274,9 @@ def run_ours(args, world, rank, local):
         barrier()
         tb = max_over_ranks(b0.elapsed_time(b1) / 1000.0)
         bf16 = {"value": world * N_RAYS * args.steps / tb, "unit": UNIT, "ms_per_step": 1000 * tb / args.steps,
-                "speedup_vs_fp32": (world * N_RAYS * args.steps / tb) / value}
+                "speedup_vs_fp32": (world * N_RAYS * args.steps / tb) / value,
+                "execution": "cuda graphs per shaded-row bucket (8192 rows)", "graphs": len(tr._engine.graphs),
+                "gpu_launches": int(_native.launch_count() + tr._engine.launches_replayed - l0)}
         del tr, model
         torch.cuda.empty_cache()
 
@@ -342,24 +355,26 @@ def run_render(args, dev):
     sat_wall = saturated["wall_s"]
 
     # plain per-request FP32 render of the first requests of the saturated stream
-    stream = serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2)[:8]
+    stream = serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2)[:args.render_plain]
     torch.cuda.synchronize()
     lat, px = [], 0
     w0 = time.perf_counter()
-    err = 0.0
+    err = None
     for t, s, c2w, H, W in stream:
         a = time.perf_counter()
         rgb, depth = serve.plain_render(models[s], c2w, H, W)
         rgb_h = rgb.cpu().numpy()
         lat.append(time.perf_counter() - a)
         px += H * W
-        if (H, W) == (600, 800) and err == 0.0:
+        if (H, W) == (600, 800) and err is None:
             mine, _ = server.render(s, c2w, H, W)
             err = float(np.abs(mine - rgb_h).max())
     plain_wall = time.perf_counter() - w0
-    plain = {"requests": len(stream), "mpix_s": px / plain_wall / 1e6,
-             "p50_ms": float(np.percentile(np.array(lat) * 1000, 50)),
-             "p99_ms": float(np.percentile(np.array(lat) * 1000, 99))}
+    plain = None
+    if stream:
+        plain = {"requests": len(stream), "mpix_s": px / plain_wall / 1e6,
+                 "p50_ms": float(np.percentile(np.array(lat) * 1000, 50)),
+                 "p99_ms": float(np.percentile(np.array(lat) * 1000, 99))}
     bf16_peak = None
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -377,7 +392,7 @@ def run_render(args, dev):
         "poisson_50_req_s": poisson,
         "saturated": saturated,
         "plain_fp32_per_request": plain,
-        "speedup_vs_plain": saturated["mpix_s"] / plain["mpix_s"],
+        "speedup_vs_plain": saturated["mpix_s"] / plain["mpix_s"] if plain else None,
         "shaded_rows_per_pixel": rows / saturated["pixels"],
         "mlp_tflops": mlp_tflops, "mlp_frac_of_bf16_peak": mlp_tflops / bf16_peak,
         "rgb_max_abs_vs_plain_fp32_800x600": err,

@@ -290,11 +290,14 @@ typedef struct {
   const float* k0_f32;      /* [X,Y,Z,12] FP32, or NULL                        */
   const void* k0_bf16;      /* [X,Y,Z,12] BF16, or NULL                        */
   vx_fine_feature_cfg cfg;
-  int64_t ld1, ld2;         /* row strides (elements) of X1 and X2             */
+  int64_t ld1, ld2;         /* row strides (elements) of X1 and X2, >= their
+                               column counts; columns beyond them are zeroed */
   void* X1;                 /* out rgbnet input [S2, ld1]                      */
-  void* X2;                 /* out k_rgbnet input [S2, ld2] (last 3 = logits, filled by the caller) */
+  void* X2;                 /* out k_rgbnet input [S2, ld2] without the rgbnet logits */
   int32_t out_bf16;         /* X1/X2 element type: 0 FP32, 1 BF16              */
   float* normal_out;        /* optional [S2,3] FD gradient (render_grad)       */
+  const int64_t* n_rows_dev; /* optional DEVICE row count: rows at or beyond
+                               it are skipped (n_rows is then a capacity)    */
 } vx_fine_features_args;
 int vx_fine_features(const vx_fine_features_args* args, void* stream);
 
@@ -368,6 +371,8 @@ typedef struct {
   int32_t in_bf16;
   float* d_sdf_smooth;      /* [X,Y,Z] accumulated                              */
   float* d_k0;              /* [X,Y,Z,12] accumulated                           */
+  const int64_t* n_rows_dev; /* optional DEVICE row count (as vx_fine_features) */
+  const float* inv_s_dev;   /* optional DEVICE inv_s (overrides inv_s)          */
 } vx_fine_backward_args;
 int vx_fine_backward(const vx_fine_backward_args* args, void* stream);
 

@@ -47,7 +47,7 @@ class FineFeaturesArgs(C.Structure):
     _fields_ = [
         ("n_rows", I64), ("ray2", P), ("pts2", P), ("viewdirs", P), ("grid", GridGeom), ("sdf_smooth", P),
         ("voxel_size", F), ("k0_f32", P), ("k0_bf16", P), ("cfg", FineFeatureCfg), ("ld1", I64), ("ld2", I64),
-        ("X1", P), ("X2", P), ("out_bf16", I32), ("normal_out", P),
+        ("X1", P), ("X2", P), ("out_bf16", I32), ("normal_out", P), ("n_rows_dev", P),
     ]
 
 
@@ -73,7 +73,7 @@ class FineBackwardArgs(C.Structure):
         ("stepdist", F), ("grid", GridGeom), ("sdf_smooth", P), ("voxel_size", F), ("inv_s", F), ("dist", F),
         ("max_steps", I64), ("rec", P), ("dw_slot", P), ("n1", P), ("alphainv_last", P), ("d_last", P),
         ("pts2", P), ("slot2", P), ("dw2", P), ("cfg", FineFeatureCfg), ("ld1", I64), ("ld2", I64), ("dX1", P),
-        ("dX2", P), ("in_bf16", I32), ("d_sdf_smooth", P), ("d_k0", P),
+        ("dX2", P), ("in_bf16", I32), ("d_sdf_smooth", P), ("d_k0", P), ("n_rows_dev", P), ("inv_s_dev", P),
     ]
 
 

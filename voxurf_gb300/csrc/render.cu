@@ -211,12 +211,14 @@ struct FeatParams {
   int out_bf16;
   // optional per-row outputs for the render path
   float* normal_out;   // [S2,3] gradient (xyz, unnormalised) or null
+  int cols1, cols2;    // columns written; [cols, ld) is zero-filled
+  const int64_t* n_rows_dev;  // optional device row count (rows beyond it are skipped)
 };
 
 template <typename T>
 __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= P.n_rows) return;
+  if (row >= P.n_rows || (P.n_rows_dev && row >= *P.n_rows_dev)) return;
   const int r = P.ray2[row];
   const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
   const float v[3] = {__ldg(P.viewdirs + 3 * r), __ldg(P.viewdirs + 3 * r + 1), __ldg(P.viewdirs + 3 * r + 2)};
@@ -224,6 +226,8 @@ __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
   T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
   float g1[3];
   fine_feature_rows(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
+  for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
+  for (int c = P.cols2; c < P.ld2; ++c) put(x2, c, 0.f);
   if (P.normal_out) {
     P.normal_out[3 * row + 0] = g1[0];
     P.normal_out[3 * row + 1] = g1[1];
@@ -378,6 +382,7 @@ struct FeatBwdParams {
   float* dw_slot;
   float* d_sdf;          // [X,Y,Z] grad of the smoothed grid
   float* d_k0;           // [X,Y,Z,12] channel-last
+  const int64_t* n_rows_dev;  // optional device row count (rows beyond it are skipped)
 };
 
 template <typename T>
@@ -403,7 +408,7 @@ __device__ __forceinline__ void scatter_probe_axis(float* __restrict__ dgrid, co
 template <typename T>
 __global__ void __launch_bounds__(128) features_fine_bwd_kernel(FeatBwdParams P) {
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= P.n_rows) return;
+  if (row >= P.n_rows || (P.n_rows_dev && row >= *P.n_rows_dev)) return;
   P.dw_slot[P.slot2[row]] = P.dw2[row];
   const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
   float ind[3];
@@ -486,6 +491,7 @@ struct GeomBwdParams {
   const float* alphainv_last;
   const float* d_last;
   float* d_sdf;
+  const float* inv_s_dev;  // optional device copy of inv_s (overrides inv_s)
 };
 
 __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P) {
@@ -494,6 +500,7 @@ __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P)
   const int lane = lane_id();
   const int n = P.n1[r];
   if (n == 0) return;
+  const float inv_s = P.inv_s_dev ? *P.inv_s_dev : P.inv_s;
   float o[3], d[3], v[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -528,13 +535,13 @@ __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P)
     sample_point(f, P.stepdist, k, p);
     to_index(P.g, p, ind);
     sdf_and_grad(P.sdf, P.g, P.voxel_size, ind, &s, gr);
-    const AlphaState a = neus_alpha(s, gr, v, P.inv_s, P.dist);
+    const AlphaState a = neus_alpha(s, gr, v, inv_s, P.dist);
     if (!(a.raw >= 0.f && a.raw <= 1.f)) continue;  // clip backward
     const float den = a.P + 1e-5f;
     const float dP = d_alpha * a.Q / (den * den);
     const float dQ = -d_alpha / den;
-    const float d_prev = dP * a.P * a.nP * P.inv_s;
-    const float d_next = dQ * a.Q * a.nQ * P.inv_s;
+    const float d_prev = dP * a.P * a.nP * inv_s;
+    const float d_next = dQ * a.Q * a.nQ * inv_s;
     const float d_s = d_prev + d_next;
     const float d_ic = (d_next - d_prev) * P.dist * 0.5f;
     const float d_cos = a.cosv < 0.f ? d_ic : 0.f;
@@ -1122,7 +1129,10 @@ int vx_fine_features(const vx_fine_features_args* A, void* stream) {
   int s = fill_feat_layout(&A->cfg, P.L);
   if (s) return s;
   if ((!A->k0_f32 && !A->k0_bf16) || !A->sdf_smooth || !A->X1 || !A->X2) return VX_ERR_ARG;
-  if (A->ld1 != x1_cols(&A->cfg) || A->ld2 != x2_cols(&A->cfg)) return VX_ERR_ARG;
+  if (A->ld1 < x1_cols(&A->cfg) || A->ld2 < x2_cols(&A->cfg)) return VX_ERR_ARG;
+  P.cols1 = (int)x1_cols(&A->cfg);
+  P.cols2 = (int)x2_cols(&A->cfg);
+  P.n_rows_dev = A->n_rows_dev;
   P.n_rows = A->n_rows;
   P.ray2 = A->ray2;
   P.pts2 = A->pts2;
@@ -1201,8 +1211,9 @@ int vx_fine_backward(const vx_fine_backward_args* A, void* stream) {
     FeatBwdParams F;
     int s = fill_feat_common(&A->cfg, F.K, F.disp, F.k_unit);
     if (s) return s;
-    if (A->ld1 != x1_cols(&A->cfg) || A->ld2 != x2_cols(&A->cfg)) return VX_ERR_ARG;
+    if (A->ld1 < x1_cols(&A->cfg) || A->ld2 < x2_cols(&A->cfg)) return VX_ERR_ARG;
     F.n_rows = A->n_rows;
+    F.n_rows_dev = A->n_rows_dev;
     F.pts2 = A->pts2;
     F.g = geom_from(&A->grid);
     F.sdf = A->sdf_smooth;
@@ -1256,6 +1267,7 @@ int vx_fine_backward(const vx_fine_backward_args* A, void* stream) {
   G.alphainv_last = A->alphainv_last;
   G.d_last = A->d_last;
   G.d_sdf = A->d_sdf_smooth;
+  G.inv_s_dev = A->inv_s_dev;
   geometry_fine_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, st>>>(G);
   return launch_status();
 }

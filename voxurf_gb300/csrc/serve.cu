@@ -208,6 +208,7 @@ struct ServeFeatParams {
   const int* ray2;
   int64_t n_rows;
   int64_t ld1, ld2;
+  int cols1, cols2;  // feature columns; X1 [cols1, ld1) and X2 [cols2 + 3, ld2) are zero-filled
   void* X1;
   void* X2;
 };
@@ -236,6 +237,8 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
   T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
   float g1[3];
   fine_feature_rows(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
+  for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
+  for (int c = P.cols2 + 3; c < P.ld2; ++c) put(x2, c, 0.f);
 }
 
 // ---- output layer ------------------------------------------------------------
@@ -486,6 +489,8 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
   P.n_rows = n_rows;
   P.ld1 = ld1;
   P.ld2 = ld2;
+  P.cols1 = (int)x1_cols(cfg);
+  P.cols2 = (int)x2_cols(cfg);
   P.X1 = X1;
   P.X2 = X2;
   const unsigned b = (unsigned)((n_rows + 127) / 128);

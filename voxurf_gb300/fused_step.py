@@ -1,0 +1,332 @@
+"""The fine-stage training step replayed from CUDA graphs.
+
+FineTrainer.step runs the forward through two torch.autograd.Functions and
+lets autograd drive the hand-written backward: ~150 launches per step whose
+host-side cost (Python, autograd, allocation) exceeds the GPU time of the
+BF16 step.  GraphedFineStep runs the same kernels in the same order on
+static buffers:
+
+  part A (eager, 4 launches): Gaussian smoothing of the SDF grid, the ray
+      march, the scan of the per-ray shaded counts, then the one host sync
+      of the step (the shaded-row count S2, which sizes the MLP GEMMs);
+  part B (one CUDA graph per row bucket): compaction, MLP input rows,
+      rgbnet and k_rgbnet forward, compositing, the run.py loss and its
+      gradient, compositing backward, MLP backward, the march/feature
+      backward into the grid gradients and the smoothing adjoint;
+  optimizer (eager, 3 launches): the fused TV + Adam sweeps of the two
+      grids and one multi-tensor Adam launch for the MLPs.
+
+Part B is captured for a row capacity rounded up to `bucket_rows`; kernels
+that work per row read S2 from the device (s2_off[N]) and skip the rest,
+the GEMMs run over the whole capacity on rows that are finite but whose
+output gradients are zero, so the padding changes no result.  inv_s (which
+changes every step with s_val) reaches the captured backward through a
+device scalar refreshed from pinned host memory by the graph's first node.
+The first time a capacity is seen, part B runs eagerly (on a side stream,
+which also warms up cuBLAS for the capture), is captured, and is replayed;
+re-running part B is idempotent because it clears its accumulators first.
+
+The MLP input rows are padded to multiples of 8 columns (zero columns and
+zero weight columns) so that every GEMM gets 16-byte aligned operands.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from . import _abi, _native
+from . import grid as grid_mod
+from ._torch import ptr, stream_ptr
+from .mlp import mlp_backward, mlp_forward
+from .voxurf_fine import _feature_cfg, max_steps_bound
+
+
+def _round_up(x: int, m: int) -> int:
+    return (x + m - 1) // m * m
+
+
+class GraphedFineStep:
+    def __init__(self, trainer, render_kwargs: dict, bucket_rows: int = 8192, use_graphs: bool = True):
+        model = trainer.model
+        if trainer.weight_eikonal > 0 or (trainer.weight_tv_density > 0 and trainer.smooth_grad_tv > 0):
+            raise NotImplementedError("graphed step: eikonal / smooth_grad_tv terms run on the eager path")
+        if not model.use_rgb_k:
+            raise NotImplementedError("graphed step: the k-branch configuration (use_rgb_k) only")
+        self.tr, self.model, self.rk = trainer, model, dict(render_kwargs)
+        self.bucket = int(bucket_rows)
+        self.use_graphs = use_graphs
+        dev = model.sdf.grid.device
+        self.dev = dev
+        N = trainer.n_rays
+        self.N = N
+        X, Y, Z = (int(s) for s in model.sdf.grid.shape[2:])
+        self.XYZ = (X, Y, Z)
+        self.bf16 = model.precision == "bf16"
+        self.xdt = torch.bfloat16 if self.bf16 else torch.float32
+        xyz_min, xyz_max = grid_mod.host_values(model.xyz_min), grid_mod.host_values(model.xyz_max)
+        self.geom = grid_mod.grid_geom((X, Y, Z), xyz_min, xyz_max)
+        vs = model.voxel_size.float()
+        self.stepdist = float(self.rk["stepsize"] * vs)
+        self.voxel_size = float(vs)
+        self.near = float(self.rk["near"])
+        self.bg = float(self.rk["bg"])
+        self.thres = float(model.fast_color_thres)
+        self.max_steps = max_steps_bound(xyz_min, xyz_max, self.stepdist)
+        self.taps = np.ascontiguousarray(model.smooth_taps, np.float32) if model.smooth_sdf else None
+        self.cfg = _feature_cfg(model)
+        self.d1 = model.dim0
+        self.k_res = bool(model.k_res)
+        self.d2a = model.k_dim0 - (3 if self.k_res else 0)
+        self.ld1 = _round_up(self.d1, 8)
+        self.ld2 = _round_up(self.d2a + (3 if self.k_res else 0), 8)
+        f32, i32, i64 = torch.float32, torch.int32, torch.int64
+        # inputs
+        self.inp = torch.empty((4, N, 3), dtype=f32, device=dev)   # rays_o, rays_d, viewdirs, target
+        # part A
+        self.sdf_s = torch.empty((X, Y, Z), dtype=f32, device=dev)
+        self.tmp = torch.empty((2, X, Y, Z), dtype=f32, device=dev)
+        self.rec = torch.empty((N * self.max_steps, 4), dtype=f32, device=dev)
+        self.dw_slot = torch.empty(N * self.max_steps, dtype=f32, device=dev)
+        self.n1 = torch.empty(N, dtype=i32, device=dev)
+        self.n2 = torch.empty(N, dtype=i32, device=dev)
+        self.alast = torch.empty(N, dtype=f32, device=dev)
+        self.s2_off = torch.empty(N + 1, dtype=i64, device=dev)
+        self.scan_bytes = int(_native.load().vx_scan_scratch_bytes(N))
+        self.scan_tmp = torch.empty(max(self.scan_bytes, 16), dtype=torch.uint8, device=dev)
+        # gradients (the optimizer's p.grad) and per-step device scalars
+        self.d_sdf_s = torch.empty((X, Y, Z), dtype=f32, device=dev)
+        self.d_sdf = torch.zeros_like(model.sdf.grid)
+        self.d_k0 = torch.zeros_like(model.k0.grid)          # channels_last_3d like the parameter
+        self.dyn_host = torch.zeros(4, dtype=f32, pin_memory=True)
+        self.dyn = torch.zeros(4, dtype=f32, device=dev)
+        # padded first-layer weights (zero columns beyond the feature count)
+        w1 = model.rgbnet[0].weight
+        w2 = model.k_rgbnet[0].weight
+        self.W1p = torch.zeros((w1.shape[0], self.ld1), dtype=self.xdt, device=dev)
+        self.W2p = torch.zeros((w2.shape[0], self.ld2), dtype=self.xdt, device=dev)
+        self.rgb_params = list(model.rgbnet.parameters())
+        self.k_params = list(model.k_rgbnet.parameters())
+        self.cap = 0
+        self.graphs = {}
+        self.S2 = 0
+        # library kernels executed by graph replays (the launch counter of
+        # the C library only sees launches issued through its entry points)
+        self.launches_replayed = 0
+
+    # ---- buffers read beyond S2 (GEMM operands): static, zero-initialised --
+    def _ensure_rows(self, cap: int) -> None:
+        if cap <= self.cap:
+            return
+        cap = _round_up(int(cap * 1.25), self.bucket)
+        self.X1 = torch.zeros((cap, self.ld1), dtype=self.xdt, device=self.dev)
+        self.X2 = torch.zeros((cap, self.ld2), dtype=self.xdt, device=self.dev)
+        self.cap = cap
+        self.graphs.clear()   # captured graphs point at the old buffers
+
+    # ---- one step -------------------------------------------------------------
+    def step(self, rays_o, rays_d, viewdirs, target, global_step=None):
+        tr, model = self.tr, self.model
+        if global_step is None:
+            tr.global_step += 1
+            global_step = tr.global_step
+        _, inv_s = model.neus_s_val(global_step)
+        for i, t in enumerate((rays_o, rays_d, viewdirs, target)):
+            self.inp[i].copy_(t)
+        S2 = self._part_a(inv_s)
+        self.S2 = S2
+        cap = max(_round_up(S2, self.bucket), self.bucket)
+        self._ensure_rows(cap)
+        self.dyn_host[0] = inv_s
+        key = (cap, 0 if self.bf16 else model.k0.grid.data_ptr())
+        entry = self.graphs.get(key)
+        if entry is None:
+            entry = self._build(cap, key)
+        else:
+            entry["graph"].replay()
+            self.launches_replayed += entry["lib_launches"]
+        model.sdf.grid.grad = self.d_sdf
+        model.k0.grid.grad = self.d_k0
+        for p, g in zip(self.rgb_params + self.k_params, entry["grads"]):
+            p.grad = g
+        tr.optimizer.step(zero_grad=True)
+        return entry["loss"], S2
+
+    def _build(self, cap, key):
+        if not self.use_graphs:
+            return self._part_b(cap)
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            self._part_b(cap)            # warm-up (idempotent: accumulators are cleared first)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        c0 = _native.launch_count()
+        with torch.cuda.graph(g):
+            out = self._part_b(cap)
+        out["lib_launches"] = _native.launch_count() - c0   # library kernels in the graph
+        g.replay()
+        self.launches_replayed += out["lib_launches"]
+        out["graph"] = g
+        self.graphs[key] = out
+        return out
+
+    # ---- part A: smoothing, march, scan, S2 ------------------------------------
+    def _part_a(self, inv_s: float) -> int:
+        model = self.model
+        st = stream_ptr(self.dev)
+        X, Y, Z = self.XYZ
+        N = self.N
+        sdf = model.sdf.grid
+        if self.taps is not None:
+            _abi.call("vx_smooth3d", ptr(sdf), ptr(self.sdf_s), ptr(self.tmp[0]), ptr(self.tmp[1]), X, Y, Z,
+                      self.taps.ctypes.data, len(self.taps), st)
+        else:
+            self.sdf_s.copy_(sdf.reshape(X, Y, Z))
+        a = _abi.FineMarchArgs()
+        a.rays_o, a.rays_d, a.viewdirs = ptr(self.inp[0]), ptr(self.inp[1]), ptr(self.inp[2])
+        a.n_rays, a.near, a.stepdist = N, self.near, self.stepdist
+        a.grid = self.geom
+        a.sdf_smooth = ptr(self.sdf_s)
+        a.voxel_size = self.voxel_size
+        if model.mask_cache is not None:
+            mc = model.mask_cache
+            a.mask = ptr(mc.mask)
+            a.mask_X, a.mask_Y, a.mask_Z = mc.mask.shape
+            sc, sh = grid_mod.host_values(mc.xyz2ijk_scale), grid_mod.host_values(mc.xyz2ijk_shift)
+            for i in range(3):
+                a.mask_scale[i] = float(sc[i])
+                a.mask_shift[i] = float(sh[i])
+        a.inv_s, a.dist, a.fast_color_thres = inv_s, self.stepdist, self.thres
+        a.max_steps = self.max_steps
+        a.rec, a.dw_slot, a.n1, a.n2, a.alphainv_last = ptr(self.rec), ptr(self.dw_slot), ptr(self.n1), \
+            ptr(self.n2), ptr(self.alast)
+        _abi.call_struct("vx_fine_march", a, st)
+        _native.call("vx_exclusive_scan_i32", ptr(self.n2), N, ptr(self.s2_off), ptr(self.scan_tmp),
+                     self.scan_bytes, st)
+        return int(self.s2_off[N].item())
+
+    # ---- part B: everything that depends on the shaded rows -------------------
+    def _part_b(self, cap: int) -> dict:
+        model = self.model
+        dev, N, xdt = self.dev, self.N, self.xdt
+        st = stream_ptr(self.dev)
+        f32, i32 = torch.float32, torch.int32
+        n_rows_dev = self.s2_off[N:]          # device S2
+        self.dyn.copy_(self.dyn_host, non_blocking=True)
+        self.d_sdf_s.zero_()
+        self.d_k0.zero_()
+        o, d, v, target = self.inp[0], self.inp[1], self.inp[2], self.inp[3]
+        # compaction
+        ray2 = torch.empty(cap, dtype=i32, device=dev)
+        step2 = torch.empty(cap, dtype=i32, device=dev)
+        slot2 = torch.empty(cap, dtype=i32, device=dev)
+        w2 = torch.empty(cap, dtype=f32, device=dev)
+        alpha2 = torch.empty(cap, dtype=f32, device=dev)
+        pts2 = torch.empty((cap, 3), dtype=f32, device=dev)
+        c = _abi.FineCompactArgs()
+        c.rays_o, c.rays_d, c.n_rays, c.near, c.stepdist = ptr(o), ptr(d), N, self.near, self.stepdist
+        for i in range(3):
+            c.xyz_min[i] = self.geom.xyz_min[i]
+            c.xyz_max[i] = self.geom.xyz_max[i]
+        c.max_steps, c.rec, c.n1, c.s2_off = self.max_steps, ptr(self.rec), ptr(self.n1), ptr(self.s2_off)
+        c.ray2, c.step2, c.slot2, c.w2, c.alpha2, c.pts2 = ptr(ray2), ptr(step2), ptr(slot2), ptr(w2), \
+            ptr(alpha2), ptr(pts2)
+        _abi.call_struct("vx_fine_compact", c, st)
+        # MLP input rows
+        X1, X2 = self.X1[:cap], self.X2[:cap]
+        f = _abi.FineFeaturesArgs()
+        f.n_rows, f.ray2, f.pts2, f.viewdirs = cap, ptr(ray2), ptr(pts2), ptr(v)
+        f.grid, f.sdf_smooth, f.voxel_size = self.geom, ptr(self.sdf_s), self.voxel_size
+        if self.bf16:
+            f.k0_bf16 = ptr(model._k0_shadow)
+        else:
+            f.k0_f32 = ptr(model.k0.grid)
+        f.cfg = self.cfg
+        f.ld1, f.ld2 = self.ld1, self.ld2
+        f.X1, f.X2, f.out_bf16 = ptr(X1), ptr(X2), int(self.bf16)
+        f.n_rows_dev = ptr(n_rows_dev)
+        _abi.call_struct("vx_fine_features", f, st)
+        # colour MLPs (weights cast to the compute dtype, first layer padded)
+        W1 = [p for i, p in enumerate(self.rgb_params) if i % 2 == 0]
+        b1 = [p for i, p in enumerate(self.rgb_params) if i % 2 == 1]
+        W2 = [p for i, p in enumerate(self.k_params) if i % 2 == 0]
+        b2 = [p for i, p in enumerate(self.k_params) if i % 2 == 1]
+        self.W1p[:, :self.d1].copy_(W1[0].detach())
+        Ws1 = [self.W1p] + [w.detach().to(xdt) for w in W1[1:]]
+        bs1 = [b.detach().to(xdt) for b in b1]
+        hs1 = mlp_forward(X1, Ws1, bs1)
+        logit = hs1[-1].float()
+        if self.k_res:
+            X2[:, self.d2a:self.d2a + 3].copy_(logit)
+        d2 = self.d2a + (3 if self.k_res else 0)
+        self.W2p[:, :d2].copy_(W2[0].detach())
+        Ws2 = [self.W2p] + [w.detach().to(xdt) for w in W2[1:]]
+        bs2 = [b.detach().to(xdt) for b in b2]
+        hs2 = mlp_forward(X2, Ws2, bs2)
+        klogit = logit + hs2[-1].float()
+        # compositing
+        rgb0 = torch.empty((N, 3), dtype=f32, device=dev)
+        rgbk = torch.empty((N, 3), dtype=f32, device=dev)
+        rgbk_raw = torch.empty((N, 3), dtype=f32, device=dev)
+        a = _abi.FineCompositeArgs()
+        a.n_rays, a.s2_off, a.w2 = N, ptr(self.s2_off), ptr(w2)
+        a.logit, a.klogit, a.alphainv_last, a.bg = ptr(logit), ptr(klogit), ptr(self.alast), self.bg
+        a.rgb0, a.rgbk, a.rgbk_raw, a.has_k = ptr(rgb0), ptr(rgbk), ptr(rgbk_raw), 1
+        _abi.call_struct("vx_fine_composite", a, st)
+        # loss (run.py:604-636, fine dtu_e2e weights) and its gradient
+        wm, we, w0 = self.tr.loss_weights
+        dk = rgbk - target
+        d0 = rgb0 - target
+        loss = wm * (dk * dk).mean() + w0 * (d0 * d0).mean()
+        g_rgbk = dk * (2.0 * wm / dk.numel())
+        g_rgb0 = d0 * (2.0 * w0 / d0.numel())
+        g_last = torch.zeros(N, dtype=f32, device=dev)
+        if we > 0:
+            p_raw = self.alast[N - 1:]
+            pc = p_raw.clamp(1e-6, 1 - 1e-6)
+            loss = loss + we * (-(pc * torch.log(pc) + (1 - pc) * torch.log(1 - pc))).mean()
+            inside = ((p_raw >= 1e-6) & (p_raw <= 1 - 1e-6)).float()
+            g_last[N - 1:] = we * (torch.log(1 - pc) - torch.log(pc)) * inside
+        # compositing backward
+        d_logit = torch.zeros((cap, 3), dtype=f32, device=dev)
+        d_klogit = torch.zeros((cap, 3), dtype=f32, device=dev)
+        d_w2 = torch.empty(cap, dtype=f32, device=dev)
+        d_last = torch.empty(N, dtype=f32, device=dev)
+        b = _abi.FineCompositeBwdArgs()
+        b.n_rays, b.s2_off, b.w2, b.logit = N, ptr(self.s2_off), ptr(w2), ptr(logit)
+        b.klogit, b.rgbk_raw = ptr(klogit), ptr(rgbk_raw)
+        b.g_rgb0, b.g_rgbk, b.bg, b.g_last_in = ptr(g_rgb0), ptr(g_rgbk), self.bg, ptr(g_last)
+        b.d_logit, b.d_klogit, b.d_w2, b.d_last, b.has_k = ptr(d_logit), ptr(d_klogit), ptr(d_w2), ptr(d_last), 1
+        _abi.call_struct("vx_fine_composite_backward", b, st)
+        # MLP backward (k-branch first: its logit input may feed d_logit)
+        dX2, g2 = mlp_backward(d_klogit, hs2, Ws2, True)
+        if not model.k_detach_2:
+            d_logit = d_logit + d_klogit
+        if self.k_res and not model.k_detach_1:
+            d_logit = d_logit + dX2[:, self.d2a:self.d2a + 3].float()
+        dX1, g1 = mlp_backward(d_logit, hs1, Ws1, True)
+        g1[0] = g1[0][:, :self.d1].contiguous()
+        g2[0] = g2[0][:, :d2].contiguous()
+        # march / feature backward into the grid gradients
+        bw = _abi.FineBackwardArgs()
+        bw.n_rays, bw.n_rows = N, cap
+        bw.rays_o, bw.rays_d, bw.viewdirs = ptr(o), ptr(d), ptr(v)
+        bw.near, bw.stepdist, bw.grid = self.near, self.stepdist, self.geom
+        bw.sdf_smooth, bw.voxel_size, bw.inv_s, bw.dist = ptr(self.sdf_s), self.voxel_size, 1.0, self.stepdist
+        bw.max_steps, bw.rec, bw.dw_slot, bw.n1 = self.max_steps, ptr(self.rec), ptr(self.dw_slot), ptr(self.n1)
+        bw.alphainv_last, bw.d_last = ptr(self.alast), ptr(d_last)
+        bw.pts2, bw.slot2, bw.dw2 = ptr(pts2), ptr(slot2), ptr(d_w2)
+        bw.cfg, bw.ld1, bw.ld2 = self.cfg, self.ld1, self.ld2
+        bw.dX1, bw.dX2, bw.in_bf16 = ptr(dX1), ptr(dX2), int(self.bf16)
+        bw.d_sdf_smooth, bw.d_k0 = ptr(self.d_sdf_s), ptr(self.d_k0)
+        bw.n_rows_dev, bw.inv_s_dev = ptr(n_rows_dev), ptr(self.dyn)
+        _abi.call_struct("vx_fine_backward", bw, st)
+        X, Y, Z = self.XYZ
+        if self.taps is not None:
+            _abi.call("vx_smooth3d_adjoint", ptr(self.d_sdf_s), ptr(self.d_sdf), ptr(self.tmp[0]), ptr(self.tmp[1]),
+                      X, Y, Z, self.taps.ctypes.data, len(self.taps), 0, st)
+        else:
+            self.d_sdf.view(X, Y, Z).copy_(self.d_sdf_s)
+        return {"loss": loss.detach(), "grads": g1 + g2, "S2_cap": cap}

@@ -25,6 +25,43 @@ def _colsum(dh: torch.Tensor, h: torch.Tensor | None, dz: torch.Tensor | None) -
     return out
 
 
+def mlp_forward(x: torch.Tensor, Ws, bs) -> list[torch.Tensor]:
+    """Linear/ReLU stack on rows x (weights already in x's dtype): returns
+    the activations [x, h1, ..., logits]."""
+    n = len(Ws)
+    hs = [x]
+    h = x
+    for i in range(n):
+        if i < n - 1:
+            h = torch._addmm_activation(bs[i], h, Ws[i].t())
+        else:
+            h = torch.addmm(bs[i], h, Ws[i].t())
+        hs.append(h)
+    return hs
+
+
+def mlp_backward(dy: torch.Tensor, hs, Ws, need_dx: bool):
+    """Gradients of mlp_forward: (dx or None, [dW1, db1, ..., dWn, dbn]) with
+    FP32 weight gradients; ReLU backward and the bias gradient are one pass
+    (vx_relu_bwd_colsum)."""
+    n = len(Ws)
+    dz = dy.to(hs[0].dtype).contiguous()
+    grads = [None] * (2 * n)
+    db = _colsum(dz, None, None)
+    dx = None
+    for i in reversed(range(n)):
+        grads[2 * i] = (dz.t() @ hs[i]).float()
+        grads[2 * i + 1] = db
+        if i > 0:
+            dh = dz @ Ws[i]
+            dz_prev = torch.empty_like(dh)
+            db = _colsum(dh, hs[i], dz_prev)
+            dz = dz_prev
+        elif need_dx:
+            dx = dz @ Ws[0]
+    return dx, grads
+
+
 class _MLP(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, *params):
@@ -32,37 +69,17 @@ class _MLP(torch.autograd.Function):
         dt = x.dtype
         Ws = [params[2 * i].detach().to(dt) for i in range(n)]
         bs = [params[2 * i + 1].detach().to(dt) for i in range(n)]
-        hs = [x]
-        h = x
-        for i in range(n):
-            if i < n - 1:
-                h = torch._addmm_activation(bs[i], h, Ws[i].t())
-            else:
-                h = torch.addmm(bs[i], h, Ws[i].t())
-            hs.append(h)
+        hs = mlp_forward(x, Ws, bs)
         ctx.save_for_backward(*hs, *Ws)
         ctx.n = n
-        return h
+        return hs[-1]
 
     @staticmethod
     def backward(ctx, dy):
         n = ctx.n
         saved = ctx.saved_tensors
         hs, Ws = saved[: n + 1], saved[n + 1:]
-        dz = dy.to(hs[0].dtype).contiguous()
-        grads = [None] * (2 * n)
-        db = _colsum(dz, None, None)
-        dx = None
-        for i in reversed(range(n)):
-            grads[2 * i] = (dz.t() @ hs[i]).float()
-            grads[2 * i + 1] = db
-            if i > 0:
-                dh = dz @ Ws[i]
-                dz_prev = torch.empty_like(dh)
-                db = _colsum(dh, hs[i], dz_prev)
-                dz = dz_prev
-            elif ctx.needs_input_grad[0]:
-                dx = dz @ Ws[0]
+        dx, grads = mlp_backward(dy, hs, Ws, ctx.needs_input_grad[0])
         return (dx, *grads)
 
 

@@ -106,9 +106,17 @@ class ResidentScene:
         self.device = dev
 
     def _mlp(self, net):
-        lin = [m for m in net if isinstance(m, torch.nn.Linear)]
-        hidden = [(m.weight.detach().to(self.dtype).contiguous(), m.bias.detach().to(self.dtype).contiguous())
-                  for m in lin[:-1]]
+        """(hidden [(W, b)], head (W, b)); the first layer's W is padded with
+        zero columns to a multiple of 8 inputs (16-byte aligned GEMM rows)."""
+        lin = [m for m in net.modules() if isinstance(m, torch.nn.Linear)]
+        hidden = []
+        for i, m in enumerate(lin[:-1]):
+            W = m.weight.detach()
+            if i == 0:
+                Wp = torch.zeros((W.shape[0], _round_up(W.shape[1], 8)), dtype=self.dtype, device=W.device)
+                Wp[:, :W.shape[1]] = W
+                W = Wp
+            hidden.append((W.to(self.dtype).contiguous(), m.bias.detach().to(self.dtype).contiguous()))
         head = (lin[-1].weight.detach().float().contiguous(), lin[-1].bias.detach().float().contiguous())
         return hidden, head
 
@@ -186,6 +194,8 @@ class RenderServer:
                  hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None):
         if not 1 <= len(scenes) <= 8:
             raise ValueError("1 to 8 resident scenes")
+        if not all(s.use_rgb_k and s.k_res for s in scenes):
+            raise NotImplementedError("render server: fine models with the k-branch (use_rgb_k, k_res)")
         c0 = bytes(scenes[0].cfg)
         if any(bytes(s.cfg) != c0 or s.precision != scenes[0].precision for s in scenes):
             raise ValueError("resident scenes must share the feature layout and precision")
@@ -418,14 +428,13 @@ class RenderServer:
     def _shade(self, s: ResidentScene, a: int, b: int, st: int) -> None:
         n = b - a
         bf = int(self.bf16)
-        h = self._hidden(s.rgbnet[0], self.X1[a:b, :self.d1])
+        h = self._hidden(s.rgbnet[0], self.X1[a:b])
         W, bias = s.rgbnet[1]
         cols = self.X2[a:b, self.d2a:] if s.k_res else None
         _abi.call("vx_mlp_head", ptr(h), n, h.shape[1], h.stride(0), bf, ptr(W), ptr(bias), None,
                   ptr(self.logit[a:b]), ptr(cols), self.ld2, bf, st)
         if s.use_rgb_k:
-            width = self.d2a + (3 if s.k_res else 0)
-            h2 = self._hidden(s.k_rgbnet[0], self.X2[a:b, :width])
+            h2 = self._hidden(s.k_rgbnet[0], self.X2[a:b])
             W2, b2 = s.k_rgbnet[1]
             _abi.call("vx_mlp_head", ptr(h2), n, h2.shape[1], h2.stride(0), bf, ptr(W2), ptr(b2),
                       ptr(self.logit[a:b]), ptr(self.klogit[a:b]), None, 0, 0, st)

@@ -45,9 +45,13 @@ class FineTrainer:
 
     def __init__(self, model, lr_sdf=1e-3, lr_k0=1e-3, lr_rgbnet=1e-3, lr_k_rgbnet=1e-3, tv_sdf=1e-4, tv_k0=1e-4,
                  tv_dense=True, n_rays=8192, loss_weights=(1.0, 0.001, 0.5), weight_tv_density=0.0,
-                 smooth_grad_tv=0.0, weight_eikonal=0.0):
+                 smooth_grad_tv=0.0, weight_eikonal=0.0, graphed=False):
         self.model = model
         self.n_rays = n_rays
+        # graphed=True: steps replay CUDA graphs on static buffers
+        # (fused_step.GraphedFineStep); same kernels, same results
+        self.graphed = graphed
+        self._engine = None
         # run.py:617-622: loss += weight_tv_density * density_total_variation(smooth_grad_tv=...)
         self.weight_tv_density, self.smooth_grad_tv = weight_tv_density, smooth_grad_tv
         # eikonal term mean((|grad| - 1)^2) on the shaded samples' FD gradient
@@ -71,6 +75,15 @@ class FineTrainer:
         self.render_kwargs = None
 
     def step(self, rays_o, rays_d, viewdirs, target, render_kwargs, global_step=None):
+        """One training step; returns (loss, ret) -- in graphed mode ret is
+        {"S2": shaded rows} and the loss tensor lives until the next step."""
+        if self.graphed:
+            from .fused_step import GraphedFineStep
+
+            if self._engine is None or self._engine.rk != dict(render_kwargs):
+                self._engine = GraphedFineStep(self, render_kwargs)
+            loss, S2 = self._engine.step(rays_o, rays_d, viewdirs, target, global_step)
+            return loss, {"S2": S2}
         if global_step is None:
             self.global_step += 1
             global_step = self.global_step
