@@ -490,6 +490,8 @@ typedef struct {
   float* d_sdf_smooth;      /* [X,Y,Z] accumulated                              */
   float* d_grad4;           /* [X,Y,Z,4] accumulated                            */
   float* d_k0;              /* [X,Y,Z,12] accumulated                           */
+  const float* d_grad2;     /* optional [S2,3] gradient w.r.t. the shaded samples'
+                               raw interpolated SDF gradient (eikonal term)    */
 } vx_coarse_backward_args;
 int vx_coarse_backward(const vx_coarse_backward_args* args, void* stream);
 

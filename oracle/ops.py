@@ -16,6 +16,17 @@ import torch
 
 from . import cref
 
+# When set to a list, the branch taken by every non-smooth operation of the
+# oracle's step (thresholds, the transmittance stop, relu of the cosine, the
+# alpha clip, output clamps) is appended to it: gradient checks use it to
+# skip finite differences that straddle a kink.
+TRACE = None
+
+
+def trace(name, value):
+    if TRACE is not None:
+        TRACE.append((name, value.detach().clone()))
+
 
 def _np(t):
     return t.detach().cpu().numpy()
@@ -124,6 +135,7 @@ class Alphas2WeightsOracle(torch.autograd.Function):
     @staticmethod
     def forward(ctx, alpha, ray_id, N):
         w, T, last, i_s, i_e = RenderUtilsOracle.alpha2weight(alpha, ray_id, N)
+        trace("alpha2weight stop", i_e)
         ctx.save_for_backward(alpha, w, T, last, i_s, i_e)
         ctx.n_rays = N
         return w, last

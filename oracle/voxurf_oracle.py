@@ -23,7 +23,7 @@ import torch
 import torch.nn as nn
 import torch.nn.functional as F
 
-from .ops import Alphas2WeightsOracle, RenderUtilsOracle, tv_add_grad_torch, TotalVariationOracle
+from .ops import Alphas2WeightsOracle, RenderUtilsOracle, tv_add_grad_torch, TotalVariationOracle, trace
 
 
 def gaussian_kernel3d(ksize: int, sigma: float) -> np.ndarray:
@@ -85,6 +85,7 @@ def neus_alpha(viewdirs, ray_id, dist, sdf, gradients, inv_s):
     """voxurf_fine.py:475-499 (use_mid, cos_anneal_ratio = 1)."""
     dirs = viewdirs[ray_id]
     true_cos = (dirs * gradients).sum(-1, keepdim=True)
+    trace("cos<0", true_cos < 0)
     iter_cos = -(F.relu(-true_cos * 0.5 + 0.5) * 0.0 + F.relu(-true_cos) * 1.0)
     sdf = sdf.unsqueeze(-1)
     est_next = sdf + iter_cos * dist * 0.5
@@ -93,7 +94,9 @@ def neus_alpha(viewdirs, ray_id, dist, sdf, gradients, inv_s):
     next_cdf = torch.sigmoid(est_next * inv_s)
     p = prev_cdf - next_cdf
     c = prev_cdf
-    return ((p + 1e-5) / (c + 1e-5)).clip(0.0, 1.0).squeeze(-1)
+    raw = (p + 1e-5) / (c + 1e-5)
+    trace("alpha in [0,1]", (raw >= 0) & (raw <= 1))
+    return raw.clip(0.0, 1.0).squeeze(-1)
 
 
 def pe(x, freq):
@@ -139,6 +142,9 @@ class OracleFine(nn.Module):
         if model.mask_cache is not None:
             mc = model.mask_cache
             self.mask = (mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
+        # None, or a dict holding the detached rgbnet logits of a base
+        # forward (recorded on first use, then reused): see forward()
+        self.frozen = None
 
     def smoothed(self):
         return smooth3d(self.sdf_grid, self.kernel) if self.smooth_sdf else self.sdf_grid
@@ -188,11 +194,13 @@ class OracleFine(nn.Module):
         thr = self.fast_color_thres
         if thr > 0:
             m = alpha > thr
+            trace("alpha > thres", m)
             alpha, ray_id, ray_pts, step_id, gradient, sdf = alpha[m], ray_id[m], ray_pts[m], step_id[m], \
                 gradient[m], sdf[m]
         weights, alphainv_last = Alphas2WeightsOracle.apply(alpha, ray_id, N)
         if thr > 0:
             m = weights > thr
+            trace("weights > thres", m)
             weights, alpha, ray_pts, ray_id, step_id, gradient, sdf = weights[m], alpha[m], ray_pts[m], ray_id[m], \
                 step_id[m], gradient[m], sdf[m]
         k0 = grid_sample_pts(self.k0_grid, ray_pts, self.xyz_min, self.xyz_max)
@@ -215,12 +223,21 @@ class OracleFine(nn.Module):
         if self.use_rgb_k:
             k_feat = torch.cat([k0, pe(rays_xyz, self.k_posfreq), pe(viewdirs, self.k_viewfreq)[ray_id], gradient]
                                + ([sdf[:, None]] if self.k_center_sdf else []), -1)
+            # the detached rgbnet logits; a finite-difference check of the
+            # detached graph holds them at their unperturbed values (frozen)
+            detached = rgb_logit.detach()
+            if self.frozen is not None:
+                if "rgb_logit" in self.frozen:
+                    detached = self.frozen["rgb_logit"]
+                else:
+                    self.frozen["rgb_logit"] = detached
             if self.k_res:
-                k_feat = torch.cat([k_feat, rgb_logit.detach() if self.k_detach_1 else rgb_logit], -1)
-            base = rgb_logit.detach() if self.k_detach_2 else rgb_logit
+                k_feat = torch.cat([k_feat, detached if self.k_detach_1 else rgb_logit], -1)
+            base = detached if self.k_detach_2 else rgb_logit
             k_rgb = torch.sigmoid(base + self.k_rgbnet(k_feat))
             k_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * k_rgb) \
                 + alphainv_last[..., None] * bg
+            trace("k_rgb in [0,1]", (k_marched >= 0) & (k_marched <= 1))
             out["rgb_marched"] = k_marched.clamp(0, 1)
             out["k_rgb_feat"] = k_feat
         rgb_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * rgb) \
@@ -331,6 +348,7 @@ class OracleCoarse(nn.Module):
         alpha = neus_alpha(viewdirs, ray_id, dist, sdf, gradient, inv_s)
         weights, _ = Alphas2WeightsOracle.apply(alpha, ray_id, N)
         m = weights > self.fast_color_thres
+        trace("weights > thres", m)
         ray_pts, ray_id, step_id, alpha, gradient = ray_pts[m], ray_id[m], step_id[m], alpha[m], gradient[m]
         weights, alphainv_last = Alphas2WeightsOracle.apply(alpha, ray_id, N)
         feats = []
@@ -345,7 +363,9 @@ class OracleCoarse(nn.Module):
         rgb = torch.sigmoid(self.rgbnet(rgb_feat))
         rgb_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * rgb)
         cum_w = torch.zeros([N, 1], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1))
-        rgb_marched = (rgb_marched + (1 - cum_w) * rk["bg"]).clamp(0, 1)
+        rgb_marched = rgb_marched + (1 - cum_w) * rk["bg"]
+        trace("rgb in [0,1]", (rgb_marched >= 0) & (rgb_marched <= 1))
+        rgb_marched = rgb_marched.clamp(0, 1)
         out = {"alphainv_cum": alphainv_last, "weights": weights, "rgb_marched": rgb_marched, "raw_rgb": rgb,
                "raw_alpha": alpha, "gradient": gradient, "ray_id": ray_id, "step_id": step_id, "s_val": s_val,
                "rgb_feat": rgb_feat}
@@ -361,7 +381,9 @@ def train_loss(ret, target, weight_main=1.0, weight_entropy_last=0.001, weight_r
     loss = weight_main * F.mse_loss(ret["rgb_marched"], target)
     if weight_entropy_last > 0:
         # run.py:608 indexes [..., -1] of a 1-D tensor: the LAST RAY only
-        pout = ret["alphainv_cum"][..., -1].clamp(1e-6, 1 - 1e-6)
+        last = ret["alphainv_cum"][..., -1]
+        trace("pout in range", (last >= 1e-6) & (last <= 1 - 1e-6))
+        pout = last.clamp(1e-6, 1 - 1e-6)
         loss = loss + weight_entropy_last * (-(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean())
     if weight_rgb0 > 0 and "rgb_marched0" in ret:
         loss = loss + F.mse_loss(ret["rgb_marched0"], target) * weight_rgb0

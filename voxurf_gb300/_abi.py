@@ -113,7 +113,7 @@ class CoarseBackwardArgs(C.Structure):
         ("stepdist", F), ("grid", GridGeom), ("sdf_smooth", P), ("grad4", P), ("voxel_size", F), ("inv_s", F),
         ("dist", F), ("max_steps", I64), ("rec", P), ("dw_slot", P), ("n2b", P), ("alphainv_last", P),
         ("d_last", P), ("pts2", P), ("slot2", P), ("dw2", P), ("cfg", CoarseFeatureCfg), ("ld", I64), ("dX", P),
-        ("in_bf16", I32), ("d_sdf_smooth", P), ("d_grad4", P), ("d_k0", P),
+        ("in_bf16", I32), ("d_sdf_smooth", P), ("d_grad4", P), ("d_k0", P), ("d_grad2", P),
     ]
 
 

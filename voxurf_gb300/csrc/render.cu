@@ -863,6 +863,7 @@ struct CoarseBwdParams {
   int use_k0, pos_pe, view_pe, geo_rgb_dim, ld, in_bf16;
   const void* dX;
   float* d_k0;
+  const float* d_grad2;  // optional [S2,3] gradient of the raw interpolated gradient
 };
 
 template <typename T>
@@ -881,6 +882,7 @@ __global__ void __launch_bounds__(128) features_coarse_bwd_kernel(CoarseBwdParam
     for (int ch = 0; ch < 12; ++ch) dk0[ch] = get(dx, ch);
     scatterC<12>(P.d_k0, c, dk0);
   }
+  float dg[3] = {0.f, 0.f, 0.f};
   if (P.geo_rgb_dim == 3) {
     const int col = (P.use_k0 ? 12 : 0) + (3 + 6 * P.pos_pe) + (3 + 6 * P.view_pe);
     float gr[3];
@@ -890,9 +892,14 @@ __global__ void __launch_bounds__(128) features_coarse_bwd_kernel(CoarseBwdParam
     const float dn[3] = {get(dx, col), get(dx, col + 1), get(dx, col + 2)};
     const float gdn = gr[0] * dn[0] + gr[1] * dn[1] + gr[2] * dn[2];
     const float corr = sn > 0.f ? gdn / (sn * den * den) : 0.f;
-    const float dg[3] = {dn[0] / den - gr[0] * corr, dn[1] / den - gr[1] * corr, dn[2] / den - gr[2] * corr};
-    scatter_grad4(P.dG4, c, dg);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dg[a] = dn[a] / den - gr[a] * corr;
   }
+  if (P.d_grad2) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dg[a] += P.d_grad2[3 * row + a];
+  }
+  scatter_grad4(P.dG4, c, dg);
 }
 
 __global__ void __launch_bounds__(256) geometry_coarse_bwd_kernel(CoarseBwdParams C) {
@@ -1049,7 +1056,7 @@ int vx_fine_march(const vx_fine_march_args* A, void* stream) {
       !A->alphainv_last)
     return VX_ERR_ARG;
   if ((int64_t)A->n_rays * A->max_steps > INT32_MAX) return VX_ERR_ARG;
-  MarchParams P;
+  MarchParams P{};
   P.rays_o = A->rays_o;
   P.rays_d = A->rays_d;
   P.viewdirs = A->viewdirs;
@@ -1088,7 +1095,7 @@ int vx_fine_march(const vx_fine_march_args* A, void* stream) {
 int vx_fine_compact(const vx_fine_compact_args* A, void* stream) {
   if (!A || A->n_rays < 0) return VX_ERR_ARG;
   if (A->n_rays == 0) return VX_OK;
-  CompactParams P;
+  CompactParams P{};
   P.rays_o = A->rays_o;
   P.rays_d = A->rays_d;
   P.n_rays = (int)A->n_rays;
@@ -1125,7 +1132,7 @@ static int fill_feat_common(const vx_fine_feature_cfg* c, int& K, float* disp, i
 int vx_fine_features(const vx_fine_features_args* A, void* stream) {
   if (!A || A->n_rows < 0) return VX_ERR_ARG;
   if (A->n_rows == 0) return VX_OK;
-  FeatParams P;
+  FeatParams P{};
   int s = fill_feat_layout(&A->cfg, P.L);
   if (s) return s;
   if ((!A->k0_f32 && !A->k0_bf16) || !A->sdf_smooth || !A->X1 || !A->X2) return VX_ERR_ARG;
@@ -1159,7 +1166,7 @@ int vx_fine_features(const vx_fine_features_args* A, void* stream) {
 int vx_fine_composite(const vx_fine_composite_args* A, void* stream) {
   if (!A || A->n_rays < 0) return VX_ERR_ARG;
   if (A->n_rays == 0) return VX_OK;
-  CompositeParams P;
+  CompositeParams P{};
   P.n_rays = (int)A->n_rays;
   P.s2_off = A->s2_off;
   P.w2 = A->w2;
@@ -1184,7 +1191,7 @@ int vx_fine_composite(const vx_fine_composite_args* A, void* stream) {
 int vx_fine_composite_backward(const vx_fine_composite_bwd_args* A, void* stream) {
   if (!A || A->n_rays < 0) return VX_ERR_ARG;
   if (A->n_rays == 0) return VX_OK;
-  CompositeBwdParams P;
+  CompositeBwdParams P{};
   P.n_rays = (int)A->n_rays;
   P.s2_off = A->s2_off;
   P.w2 = A->w2;
@@ -1208,7 +1215,7 @@ int vx_fine_backward(const vx_fine_backward_args* A, void* stream) {
   if (!A || A->n_rays < 0 || A->n_rows < 0) return VX_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   if (A->n_rows > 0) {
-    FeatBwdParams F;
+    FeatBwdParams F{};
     int s = fill_feat_common(&A->cfg, F.K, F.disp, F.k_unit);
     if (s) return s;
     if (A->ld1 < x1_cols(&A->cfg) || A->ld2 < x2_cols(&A->cfg)) return VX_ERR_ARG;
@@ -1244,7 +1251,7 @@ int vx_fine_backward(const vx_fine_backward_args* A, void* stream) {
     if (s) return s;
   }
   if (A->n_rays == 0) return VX_OK;
-  GeomBwdParams G;
+  GeomBwdParams G{};
   G.rays_o = A->rays_o;
   G.rays_d = A->rays_d;
   G.viewdirs = A->viewdirs;
@@ -1283,7 +1290,7 @@ int vx_coarse_march(const vx_coarse_march_args* A, void* stream) {
       !M->n1 || !M->n2 || !A->n2b || !M->alphainv_last)
     return VX_ERR_ARG;
   if ((int64_t)M->n_rays * M->max_steps > INT32_MAX || (((uintptr_t)A->grad4) & 15)) return VX_ERR_ARG;
-  CoarseMarchParams C;
+  CoarseMarchParams C{};
   MarchParams& P = C.m;
   P.rays_o = M->rays_o;
   P.rays_d = M->rays_d;
@@ -1334,7 +1341,7 @@ int vx_coarse_features(const vx_coarse_features_args* A, void* stream) {
   if (A->n_rows == 0) return VX_OK;
   if (A->ld != coarse_cols(&A->cfg) || !A->X || !A->grad4 || (A->cfg.use_k0 && !A->k0_f32 && !A->k0_bf16))
     return VX_ERR_ARG;
-  CoarseFeatParams P;
+  CoarseFeatParams P{};
   P.n_rows = A->n_rows;
   P.ray2 = A->ray2;
   P.pts2 = A->pts2;
@@ -1361,7 +1368,7 @@ int vx_coarse_features(const vx_coarse_features_args* A, void* stream) {
 int vx_coarse_composite(const vx_coarse_composite_args* A, void* stream) {
   if (!A || A->n_rays < 0) return VX_ERR_ARG;
   if (A->n_rays == 0) return VX_OK;
-  CoarseCompositeParams P;
+  CoarseCompositeParams P{};
   P.n_rays = (int)A->n_rays;
   P.s2_off = A->s2_off;
   P.w2 = A->w2;
@@ -1382,7 +1389,7 @@ int vx_coarse_composite(const vx_coarse_composite_args* A, void* stream) {
 int vx_coarse_composite_backward(const vx_coarse_composite_bwd_args* A, void* stream) {
   if (!A || A->n_rays < 0) return VX_ERR_ARG;
   if (A->n_rays == 0) return VX_OK;
-  CoarseCompositeBwdParams P;
+  CoarseCompositeBwdParams P{};
   P.n_rays = (int)A->n_rays;
   P.s2_off = A->s2_off;
   P.w2 = A->w2;
@@ -1401,7 +1408,7 @@ int vx_coarse_backward(const vx_coarse_backward_args* A, void* stream) {
   if (A->n_rows > 0 && A->ld != coarse_cols(&A->cfg)) return VX_ERR_ARG;
   if ((((uintptr_t)A->grad4) | ((uintptr_t)A->d_grad4)) & 15) return VX_ERR_ARG;
   cudaStream_t st = as_stream(stream);
-  CoarseBwdParams C;
+  CoarseBwdParams C{};
   GeomBwdParams& G = C.gb;
   G.rays_o = A->rays_o;
   G.rays_d = A->rays_d;
@@ -1441,6 +1448,7 @@ int vx_coarse_backward(const vx_coarse_backward_args* A, void* stream) {
   C.in_bf16 = A->in_bf16;
   C.dX = A->dX;
   C.d_k0 = A->d_k0;
+  C.d_grad2 = A->d_grad2;
   if (A->n_rows > 0) {
     const unsigned b = (unsigned)((A->n_rows + 127) / 128);
     if (A->in_bf16)

@@ -439,7 +439,7 @@ int vx_serve_march(const vx_scene_desc* scenes_host, int32_t n_scenes, const flo
                    int32_t* n2, float* alphainv_last, void* stream) {
   if (n_rays < 0 || n_rays > INT32_MAX || max_steps < 1 || max_steps > INT32_MAX) return VX_ERR_ARG;
   if (n_rays == 0) return VX_OK;
-  ServeMarchParams P;
+  ServeMarchParams P{};
   int s = scene_table(scenes_host, n_scenes, P.T);
   if (s) return s;
   if (!rays_o || !rays_d || !viewdirs || !ray_scene || !rec || !n2 || !alphainv_last) return VX_ERR_ARG;
@@ -471,7 +471,7 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
                       int64_t ld1, int64_t ld2, void* X1, void* X2, int32_t out_bf16, void* stream) {
   if (n_rows < 0 || !cfg || max_steps < 1 || max_steps > INT32_MAX) return VX_ERR_ARG;
   if (n_rows == 0) return VX_OK;
-  ServeFeatParams P;
+  ServeFeatParams P{};
   int s = scene_table(scenes_host, n_scenes, P.T);
   if (s) return s;
   s = fill_feat_layout(cfg, P.L);
@@ -526,7 +526,7 @@ int vx_serve_composite(const vx_scene_desc* scenes_host, int32_t n_scenes, const
                        float* out_depth, void* stream) {
   if (n_rays < 0 || n_rays > INT32_MAX || max_steps < 1 || max_steps > INT32_MAX) return VX_ERR_ARG;
   if (n_rays == 0) return VX_OK;
-  ServeCompositeParams P;
+  ServeCompositeParams P{};
   int s = scene_table(scenes_host, n_scenes, P.T);
   if (s) return s;
   if (!ray_scene || !rec || !s2_off || !logit || !alphainv_last || !ray_out || !out_rgb) return VX_ERR_ARG;

@@ -111,11 +111,13 @@ class _CoarseGeometry(torch.autograd.Function):
         fr.rec, fr.dw_slot, fr.n2b, fr.alphainv_last = rec, dw_slot, n2b, alphainv_last
         fr.s2_off, fr.ray2, fr.step2, fr.slot2, fr.w2, fr.alpha2, fr.pts2 = s2_off, ray2, step2, slot2, w2, alpha2, pts2
         ctx.fr, ctx.k0_like, ctx.sdf_shape = fr, k0_grid, sdf_grid.shape
-        ctx.mark_non_differentiable(normal2, alpha2)
+        ctx.mark_non_differentiable(alpha2)
+        # normal2 = the shaded samples' raw interpolated gradient (differentiable:
+        # an eikonal term on it reaches the gradient grid through d_grad2)
         return Xf, w2, alphainv_last, normal2, alpha2
 
     @staticmethod
-    def backward(ctx, dX, dw2, dlast, _dn, _da):
+    def backward(ctx, dX, dw2, dlast, d_grad2, _da):
         fr = ctx.fr
         dev = fr.w2.device
         st = stream_ptr()
@@ -139,6 +141,9 @@ class _CoarseGeometry(torch.autograd.Function):
         b.pts2, b.slot2, b.dw2 = ptr(fr.pts2), ptr(fr.slot2), ptr(dw2)
         b.cfg, b.ld, b.dX, b.in_bf16 = fr.cfg, fr.d1, ptr(dX), int(fr.bf16)
         b.d_sdf_smooth, b.d_grad4, b.d_k0 = ptr(d_sdf_s), ptr(dG4), ptr(d_k0)
+        if d_grad2 is not None:
+            d_grad2 = d_grad2.float().contiguous()
+            b.d_grad2 = ptr(d_grad2)
         _abi.call_struct("vx_coarse_backward", b, st)
         d_sdf = smooth_grid_adjoint(d_sdf_s, fr.taps) if fr.taps is not None else d_sdf_s
         _abi.call("vx_sdf_gradient_grid_adjoint", ptr(dG4), ptr(d_sdf), X, Y, Z, float(fr.voxel_size), 1, 1, st)
