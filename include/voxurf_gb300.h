@@ -519,7 +519,21 @@ typedef struct {
   float near;
   float bg;
   float fast_color_thres;
+  const uint8_t* occ;       /* optional occupancy of the mask (vx_mask_occupancy):
+                               the march skips runs of samples in empty cells */
+  int64_t occ_X, occ_Y, occ_Z;
+  int32_t occ_block;
 } vx_scene_desc;
+
+/* Block occupancy of a mask grid for empty-space skipping: cell (I,J,K) of
+ * an [occ_X, occ_Y, occ_Z] = [ceil(mX/block)+2, ...] grid (one border cell
+ * on each side) is 1 iff a mask voxel lies in its block of voxels
+ * [block*(I-1), block*I) (per axis) widened by one voxel on both sides.
+ * The widening makes a skip decision taken on a float model of the sample
+ * positions safe: a sample the model places in an empty cell has its exact
+ * voxel within one voxel of that cell, where the mask is 0. */
+int vx_mask_occupancy(const uint8_t* mask, int64_t mX, int64_t mY, int64_t mZ, int32_t block, uint8_t* occ,
+                      void* stream);
 
 /* A run of consecutive pixels of one view: rays [ray0, ray0 + n) of a tick
  * come from pixels [pix0, pix0 + n) of an image W pixels wide (row-major)

@@ -108,6 +108,27 @@ def test_same_alone_and_in_mix(cuda):
         assert np.abs(r.depth - depth).max() <= 1e-3 * max(1.0, np.abs(depth).max())
 
 
+def test_empty_space_skipping_is_exact(cuda):
+    """Skipping the samples that lie in empty blocks of the mask leaves every
+    result unchanged (same shaded rows; RGB equal up to the grouping of the
+    FP64 transmittance products)."""
+    models = _models(cuda, "fp32", n=2)
+    views = [(0, _pose(40), 48, 64), (1, _pose(41), 40, 40), (0, _pose(42), 33, 17)]
+    out = []
+    for block in (0, 4, 8):
+        scenes = [serve.ResidentScene(m, s_val=S_VAL, precision="fp32", skip_block=block) for m in models]
+        srv = serve.RenderServer(scenes, tick_rays=1500, arena_pixels=1 << 16)
+        reqs = [srv.submit(*v) for v in views]
+        srv.run_until_idle()
+        out.append((srv.rows_shaded, [r.rgb for r in reqs], [r.depth for r in reqs]))
+    for rows, rgbs, depths in out[1:]:
+        assert rows == out[0][0]
+        for a, b in zip(rgbs, out[0][1]):
+            assert np.abs(a - b).max() <= 1e-6
+        for a, b in zip(depths, out[0][2]):
+            assert np.abs(a - b).max() <= 1e-6
+
+
 def test_admission_waits_for_arena(cuda):
     """With an arena of 2 x 40x40 pixels the third request waits for a free
     range; every request still completes with the result it has alone."""

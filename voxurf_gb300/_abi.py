@@ -121,7 +121,8 @@ class SceneDesc(C.Structure):
     _fields_ = [
         ("grid", GridGeom), ("sdf_smooth", P), ("k0", P), ("k0_bf16", I32), ("voxel_size", F), ("mask", P),
         ("mask_X", I64), ("mask_Y", I64), ("mask_Z", I64), ("mask_scale", F * 3), ("mask_shift", F * 3),
-        ("inv_s", F), ("stepdist", F), ("near", F), ("bg", F), ("fast_color_thres", F),
+        ("inv_s", F), ("stepdist", F), ("near", F), ("bg", F), ("fast_color_thres", F), ("occ", P),
+        ("occ_X", I64), ("occ_Y", I64), ("occ_Z", I64), ("occ_block", I32),
     ]
 
 
@@ -150,6 +151,7 @@ _SERVE_SIGNATURES = {
     "vx_serve_rays": [P, I32, I64, P, P, P, P, P, P],
     "vx_serve_march": ["scenes", I32, P, P, P, P, I64, I64, P, P, P, P],
     "vx_serve_rows": [P, I64, P, P],
+    "vx_mask_occupancy": [P, I64, I64, I64, I32, P, P],
     "vx_serve_features": ["scenes", I32, C.POINTER(FineFeatureCfg), P, P, P, P, I64, P, P, P, I64, I64, I64, P, P,
                           I32, P],
     "vx_mlp_head": [P, I64, I64, I64, I32, P, P, P, P, P, I64, I32, P],

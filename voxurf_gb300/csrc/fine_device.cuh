@@ -247,11 +247,32 @@ inline int64_t x2_cols(const vx_fine_feature_cfg* c) {
   return 12 + (3 + 6 * c->k_posbase_pe) + (3 + 6 * c->k_viewbase_pe) + 3 + (c->k_center_sdf ? 1 : 0);
 }
 
+// hier_features with the number of displacements known at compile time, so
+// the value arrays stay in registers.
+template <int KK>
+__device__ __forceinline__ void hier_features_k(const float* __restrict__ sdf, const GridGeom& g, float vs,
+                                                const float ind[3], const float* disp, float feat[6 * KK],
+                                                float graw[3 * KK]) {
+#pragma unroll
+  for (int kk = 0; kk < KK; ++kk) {
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) {
+      const int axis = 2 - pair;  // zyx
+      Probe pr;
+      probe_axis(sdf, g, ind, axis, disp[kk], pr, false);
+      feat[(2 * pair + 0) * KK + kk] = pr.fm;
+      feat[(2 * pair + 1) * KK + kk] = pr.fp;
+      graw[pair * KK + kk] = ((pr.fp - pr.fm) * pr.inv_diff) / vs;
+    }
+  }
+}
+
 // One shaded point p seen along viewdir v: the rgbnet input row x1
 // ([k0], PE(xyz_n), PE(v), [sdf], 6K hierarchical values, 3K normalised
 // gradients) and the k_rgbnet input row x2 without its trailing logits
 // (k0, PE(xyz_n), PE(v), d=1 gradient, [sdf]); g1 = the d=1 gradient (xyz).
-template <typename T>
+// KK = L.K (instantiated per displacement count).
+template <typename T, int KK>
 __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf, const GridGeom& g, float vs,
                                                   const float* __restrict__ k0f,
                                                   const __nv_bfloat16* __restrict__ k0h, const FeatLayout& L,
@@ -259,12 +280,23 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
   float ind[3];
   to_index(g, p, ind);
   const float s = sample1(sdf, g, ind[0], ind[1], ind[2]);
-  float feat[6 * MAX_K], graw[3 * MAX_K];
-  hier_features(sdf, g, vs, ind, L.K, L.disp, feat, graw);
+  float feat[6 * KK], graw[3 * KK];
+  float disp[KK];
+#pragma unroll
+  for (int kk = 0; kk < KK; ++kk) disp[kk] = L.disp[kk];
+  hier_features_k<KK>(sdf, g, vs, ind, disp, feat, graw);
   // gradient for k_rgbnet: unnormalised, displacement 1.0, xyz order
-  g1[0] = graw[2 * L.K + L.k_unit];
-  g1[1] = graw[1 * L.K + L.k_unit];
-  g1[2] = graw[0 * L.K + L.k_unit];
+  float gu[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int kk = 0; kk < KK; ++kk)
+    if (kk == L.k_unit) {
+      gu[0] = graw[2 * KK + kk];
+      gu[1] = graw[1 * KK + kk];
+      gu[2] = graw[0 * KK + kk];
+    }
+  g1[0] = gu[0];
+  g1[1] = gu[1];
+  g1[2] = gu[2];
   float k0v[12];
   const Corners c = corners_of(g, ind[0], ind[1], ind[2]);
   if (k0h)
@@ -276,21 +308,28 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
   for (int a = 0; a < 3; ++a) xyzn[a] = (p[a] - g.mn[a]) / (g.mx[a] - g.mn[a]);
 
   int col = 0;
-  if (L.use_rgbnet_k0)
-    for (int ch = 0; ch < 12; ++ch) put(x1, col++, k0v[ch]);
+  if (L.use_rgbnet_k0) {
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) put(x1, ch, k0v[ch]);
+    col = 12;
+  }
   col = put_pe(x1, col, xyzn, L.pos_pe);
   col = put_pe(x1, col, v, L.view_pe);
   if (L.center_sdf) put(x1, col++, s);
-  for (int q = 0; q < 6 * L.K; ++q) put(x1, col++, feat[q]);
-  for (int kk = 0; kk < L.K; ++kk) {
-    const float a = graw[0 * L.K + kk], b = graw[1 * L.K + kk], cc = graw[2 * L.K + kk];
+#pragma unroll
+  for (int q = 0; q < 6 * KK; ++q) put(x1, col + q, feat[q]);
+  col += 6 * KK;
+#pragma unroll
+  for (int kk = 0; kk < KK; ++kk) {
+    const float a = graw[0 * KK + kk], b = graw[1 * KK + kk], cc = graw[2 * KK + kk];
     const float nrm = sqrtf(a * a + b * b + cc * cc) + 1e-5f;
-    put(x1, col + 0 * L.K + kk, a / nrm);
-    put(x1, col + 1 * L.K + kk, b / nrm);
-    put(x1, col + 2 * L.K + kk, cc / nrm);
+    put(x1, col + 0 * KK + kk, a / nrm);
+    put(x1, col + 1 * KK + kk, b / nrm);
+    put(x1, col + 2 * KK + kk, cc / nrm);
   }
-  col = 0;
-  for (int ch = 0; ch < 12; ++ch) put(x2, col++, k0v[ch]);
+  col = 12;
+#pragma unroll
+  for (int ch = 0; ch < 12; ++ch) put(x2, ch, k0v[ch]);
   col = put_pe(x2, col, xyzn, L.kpos_pe);
   col = put_pe(x2, col, v, L.kview_pe);
   put(x2, col++, g1[0]);

@@ -215,7 +215,7 @@ struct FeatParams {
   const int64_t* n_rows_dev;  // optional device row count (rows beyond it are skipped)
 };
 
-template <typename T>
+template <typename T, int KK>
 __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= P.n_rows || (P.n_rows_dev && row >= *P.n_rows_dev)) return;
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
   T* x1 = reinterpret_cast<T*>(P.X1) + row * P.ld1;
   T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
   float g1[3];
-  fine_feature_rows(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
+  fine_feature_rows<T, KK>(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
   for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
   for (int c = P.cols2; c < P.ld2; ++c) put(x2, c, 0.f);
   if (P.normal_out) {
@@ -1156,10 +1156,22 @@ int vx_fine_features(const vx_fine_features_args* A, void* stream) {
   P.out_bf16 = A->out_bf16;
   P.normal_out = A->normal_out;
   const unsigned b = (unsigned)((A->n_rows + 127) / 128);
-  if (A->out_bf16)
-    features_fine_kernel<__nv_bfloat16><<<b, 128, 0, as_stream(stream)>>>(P);
-  else
-    features_fine_kernel<float><<<b, 128, 0, as_stream(stream)>>>(P);
+  cudaStream_t st = as_stream(stream);
+#define VX_FEAT_LAUNCH(T, KK) features_fine_kernel<T, KK><<<b, 128, 0, st>>>(P)
+#define VX_FEAT_SWITCH(T)        \
+  switch (P.L.K) {               \
+    case 1: VX_FEAT_LAUNCH(T, 1); break; \
+    case 2: VX_FEAT_LAUNCH(T, 2); break; \
+    case 3: VX_FEAT_LAUNCH(T, 3); break; \
+    default: VX_FEAT_LAUNCH(T, 4); break; \
+  }
+  if (A->out_bf16) {
+    VX_FEAT_SWITCH(__nv_bfloat16)
+  } else {
+    VX_FEAT_SWITCH(float)
+  }
+#undef VX_FEAT_SWITCH
+#undef VX_FEAT_LAUNCH
   return launch_status();
 }
 

@@ -31,6 +31,8 @@ struct SceneK {
   int mX, mY, mZ;
   float mscale[3], mshift[3];
   float vs, inv_s, stepdist, near, bg, thres;
+  const uint8_t* occ;  // optional block occupancy of the mask (padded by one cell)
+  int oX, oY, oZ, oB;
 };
 
 struct SceneTable {
@@ -91,6 +93,77 @@ __global__ void camera_rays_kernel(vx_view_chunk c, int64_t n, float* __restrict
   }
 }
 
+// ---- empty-space skipping ------------------------------------------------------
+// Block occupancy: padded cell (I,J,K) <- any mask voxel in
+// [B(I-1) - 1, B I + 1) x ... (the block widened by one voxel).
+__global__ void mask_occupancy_kernel(const uint8_t* __restrict__ mask, int mX, int mY, int mZ, int B,
+                                      uint8_t* __restrict__ occ, int oX, int oY, int oZ) {
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= (int64_t)oX * oY * oZ) return;
+  const int K = (int)(cell % oZ), J = (int)((cell / oZ) % oY), I = (int)(cell / ((int64_t)oY * oZ));
+  const int i0 = max(B * (I - 1) - 1, 0), i1 = min(B * I + 1, mX);
+  const int j0 = max(B * (J - 1) - 1, 0), j1 = min(B * J + 1, mY);
+  const int k0 = max(B * (K - 1) - 1, 0), k1 = min(B * K + 1, mZ);
+  uint8_t any = 0;
+  for (int i = i0; i < i1 && !any; ++i)
+    for (int j = j0; j < j1 && !any; ++j)
+      for (int k = k0; k < k1; ++k)
+        if (mask[((int64_t)i * mY + j) * mZ + k]) {
+          any = 1;
+          break;
+        }
+  occ[cell] = any;
+}
+
+// Mask-index coordinates of sample k on a float model of the march:
+// u(k) = u0 + du * k (the exact positions differ by far less than a voxel).
+struct SkipModel {
+  float u0[3], du[3];
+};
+
+__device__ __forceinline__ SkipModel skip_model(const RayFrame& f, const SceneK& S) {
+  SkipModel m;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    m.u0[a] = f.st[a] * S.mscale[a] + S.mshift[a];
+    m.du[a] = f.dr[a] * S.stepdist * S.mscale[a];
+  }
+  return m;
+}
+
+// First k' >= k whose sample the model places in an occupied cell (cells
+// outside the padded grid are empty), or n_steps.  Every sample skipped lies
+// in an empty widened cell, so its mask lookup would have been false.
+__device__ __forceinline__ int skip_empty(const SkipModel& m, int k, int n_steps, const SceneK& S) {
+  const int dims[3] = {S.oX, S.oY, S.oZ};
+  const float invB = 1.f / (float)S.oB;
+  for (int it = 0; it < 4096 && k < n_steps; ++it) {
+    int c[3];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float u = m.u0[a] + m.du[a] * (float)k;
+      const float cf = floorf((u + 0.5f) * invB) + 1.f;
+      // beyond the padded grid and moving away from it: no later sample can hit the mask
+      if ((cf < 0.f && m.du[a] <= 0.f) || (cf >= (float)dims[a] && m.du[a] >= 0.f)) return n_steps;
+      c[a] = (int)fminf(fmaxf(cf, -1.f), (float)dims[a]);
+      inside &= (c[a] >= 0) & (c[a] < dims[a]);
+    }
+    if (inside && __ldg(S.occ + ((int64_t)c[0] * S.oY + c[1]) * S.oZ + c[2])) return k;
+    float t = 3.0e9f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (m.du[a] > 0.f)
+        t = fminf(t, ((float)(S.oB * c[a]) - 0.5f - m.u0[a]) / m.du[a]);
+      else if (m.du[a] < 0.f)
+        t = fminf(t, ((float)(S.oB * (c[a] - 1)) - 0.5f - m.u0[a]) / m.du[a]);
+    }
+    if (!(t < (float)n_steps)) return n_steps;
+    k = max(k + 1, (int)ceilf(t));
+  }
+  return k;
+}
+
 // ---- march ------------------------------------------------------------------
 struct ServeMarchParams {
   SceneTable T;
@@ -140,7 +213,10 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
   double carry = 1.0, last = 1.0;
   int cnt2 = 0;
   bool stopped = false;
-  for (int base = 0; base < n_steps && !stopped; base += 32) {
+  const SkipModel sm = skip_model(f, S);
+  for (int base = 0; !stopped; base += 32) {
+    if (S.occ && S.mask) base = skip_empty(sm, base, (int)n_steps, S);  // warp-uniform
+    if (base >= n_steps) break;
     const int k = base + lane;
     bool keep = false;
     float alpha = 0.f;
@@ -213,7 +289,7 @@ struct ServeFeatParams {
   void* X2;
 };
 
-template <typename T>
+template <typename T, int KK>
 __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
   load_scenes(P.T, sh);
@@ -236,7 +312,7 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
   T* x1 = reinterpret_cast<T*>(P.X1) + row * P.ld1;
   T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
   float g1[3];
-  fine_feature_rows(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
+  fine_feature_rows<T, KK>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
   for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
   for (int c = P.cols2 + 3; c < P.ld2; ++c) put(x2, c, 0.f);
 }
@@ -247,65 +323,83 @@ constexpr int HEAD_MAX_WIDTH = 256;
 __device__ __forceinline__ float to_f(float x) { return x; }
 __device__ __forceinline__ float to_f(__nv_bfloat16 x) { return __bfloat162float(x); }
 
-template <typename T>
+// 16-byte row chunks: 8 BF16 or 4 FP32 values.
+__device__ __forceinline__ void chunk_to_f(const uint4& u, const __nv_bfloat16*, float x[8]) {
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __bfloat1622float2(h[i]);
+    x[2 * i] = f.x;
+    x[2 * i + 1] = f.y;
+  }
+}
+__device__ __forceinline__ void chunk_to_f(const uint4& u, const float*, float x[8]) {
+  x[0] = __uint_as_float(u.x);
+  x[1] = __uint_as_float(u.y);
+  x[2] = __uint_as_float(u.z);
+  x[3] = __uint_as_float(u.w);
+}
+
+// One thread per row; the 3 x width weights in shared memory (broadcast
+// reads); VEC: rows read in 16-byte chunks (width and the row stride are
+// multiples of the chunk, the base 16-byte aligned).
+template <typename T, bool VEC>
 __global__ void __launch_bounds__(256) mlp_head_kernel(const T* __restrict__ H, int64_t n_rows, int width,
                                                        int64_t ldh, const float* __restrict__ W,
                                                        const float* __restrict__ b, const float* __restrict__ add,
                                                        float* __restrict__ out, void* cols, int64_t ld_cols,
                                                        int cols_bf16) {
-  constexpr int Q = HEAD_MAX_WIDTH / 32;
-  const int lane = lane_id();
-  float w0[Q], w1[Q], w2[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const int c = lane + 32 * q;
-    const bool in = c < width;
-    w0[q] = in ? W[c] : 0.f;
-    w1[q] = in ? W[width + c] : 0.f;
-    w2[q] = in ? W[2 * width + c] : 0.f;
-  }
+  __shared__ float sw[3 * HEAD_MAX_WIDTH];
+  for (int i = threadIdx.x; i < 3 * width; i += blockDim.x) sw[i] = W[i];
+  __syncthreads();
+  constexpr int PER = 16 / (int)sizeof(T);
   const float b0 = b ? b[0] : 0.f, b1 = b ? b[1] : 0.f, b2 = b ? b[2] : 0.f;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n_rows; row += warps) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n_rows; row += stride) {
     const T* h = H + row * ldh;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    if (VEC) {
+      const uint4* hv = reinterpret_cast<const uint4*>(h);
+      for (int c0 = 0; c0 < width; c0 += PER) {
+        float x[8];
+        chunk_to_f(__ldg(hv + c0 / PER), h, x);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int c = lane + 32 * q;
-      if (c < width) {
+        for (int i = 0; i < PER; ++i) {
+          a0 += x[i] * sw[c0 + i];
+          a1 += x[i] * sw[width + c0 + i];
+          a2 += x[i] * sw[2 * width + c0 + i];
+        }
+      }
+    } else {
+      for (int c = 0; c < width; ++c) {
         const float x = to_f(h[c]);
-        a0 += x * w0[q];
-        a1 += x * w1[q];
-        a2 += x * w2[q];
+        a0 += x * sw[c];
+        a1 += x * sw[width + c];
+        a2 += x * sw[2 * width + c];
       }
     }
-    a0 = warp_sum(a0);
-    a1 = warp_sum(a1);
-    a2 = warp_sum(a2);
-    if (lane == 0) {
-      a0 += b0;
-      a1 += b1;
-      a2 += b2;
-      if (add) {
-        a0 += add[3 * row + 0];
-        a1 += add[3 * row + 1];
-        a2 += add[3 * row + 2];
-      }
-      out[3 * row + 0] = a0;
-      out[3 * row + 1] = a1;
-      out[3 * row + 2] = a2;
-      if (cols) {
-        if (cols_bf16) {
-          __nv_bfloat16* cp = reinterpret_cast<__nv_bfloat16*>(cols) + row * ld_cols;
-          cp[0] = __float2bfloat16_rn(a0);
-          cp[1] = __float2bfloat16_rn(a1);
-          cp[2] = __float2bfloat16_rn(a2);
-        } else {
-          float* cp = reinterpret_cast<float*>(cols) + row * ld_cols;
-          cp[0] = a0;
-          cp[1] = a1;
-          cp[2] = a2;
-        }
+    a0 += b0;
+    a1 += b1;
+    a2 += b2;
+    if (add) {
+      a0 += add[3 * row + 0];
+      a1 += add[3 * row + 1];
+      a2 += add[3 * row + 2];
+    }
+    out[3 * row + 0] = a0;
+    out[3 * row + 1] = a1;
+    out[3 * row + 2] = a2;
+    if (cols) {
+      if (cols_bf16) {
+        __nv_bfloat16* cp = reinterpret_cast<__nv_bfloat16*>(cols) + row * ld_cols;
+        cp[0] = __float2bfloat16_rn(a0);
+        cp[1] = __float2bfloat16_rn(a1);
+        cp[2] = __float2bfloat16_rn(a2);
+      } else {
+        float* cp = reinterpret_cast<float*>(cols) + row * ld_cols;
+        cp[0] = a0;
+        cp[1] = a1;
+        cp[2] = a2;
       }
     }
   }
@@ -394,6 +488,15 @@ static int scene_table(const vx_scene_desc* D, int n, SceneTable& T) {
     s.near = d.near;
     s.bg = d.bg;
     s.thres = d.fast_color_thres;
+    s.occ = d.occ;
+    s.oX = (int)d.occ_X;
+    s.oY = (int)d.occ_Y;
+    s.oZ = (int)d.occ_Z;
+    s.oB = d.occ_block;
+    if (d.occ && (!d.mask || d.occ_block < 1 || d.occ_X != (d.mask_X + d.occ_block - 1) / d.occ_block + 2 ||
+                  d.occ_Y != (d.mask_Y + d.occ_block - 1) / d.occ_block + 2 ||
+                  d.occ_Z != (d.mask_Z + d.occ_block - 1) / d.occ_block + 2))
+      return VX_ERR_ARG;
   }
   for (int i = n; i < VX_SERVE_MAX_SCENES; ++i) T.s[i] = T.s[0];
   return VX_OK;
@@ -457,6 +560,18 @@ int vx_serve_march(const vx_scene_desc* scenes_host, int32_t n_scenes, const flo
   return launch_status();
 }
 
+int vx_mask_occupancy(const uint8_t* mask, int64_t mX, int64_t mY, int64_t mZ, int32_t block, uint8_t* occ,
+                      void* stream) {
+  if (!mask || !occ || mX < 1 || mY < 1 || mZ < 1 || block < 1 || block > 64) return VX_ERR_ARG;
+  if (mX > INT32_MAX / mY / mZ) return VX_ERR_TOO_LARGE;
+  const int oX = (int)((mX + block - 1) / block + 2), oY = (int)((mY + block - 1) / block + 2),
+            oZ = (int)((mZ + block - 1) / block + 2);
+  const int64_t n = (int64_t)oX * oY * oZ;
+  mask_occupancy_kernel<<<grid_for(n), VX_THREADS, 0, as_stream(stream)>>>(mask, (int)mX, (int)mY, (int)mZ, block, occ,
+                                                                          oX, oY, oZ);
+  return launch_status();
+}
+
 int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, void* stream) {
   if (n_rays < 0 || n_rays > INT32_MAX) return VX_ERR_ARG;
   if (n_rays == 0) return VX_OK;
@@ -494,10 +609,22 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
   P.X1 = X1;
   P.X2 = X2;
   const unsigned b = (unsigned)((n_rows + 127) / 128);
-  if (out_bf16)
-    serve_features_kernel<__nv_bfloat16><<<b, 128, 0, as_stream(stream)>>>(P);
-  else
-    serve_features_kernel<float><<<b, 128, 0, as_stream(stream)>>>(P);
+  cudaStream_t st = as_stream(stream);
+#define VX_FEAT_LAUNCH(T, KK) serve_features_kernel<T, KK><<<b, 128, 0, st>>>(P)
+#define VX_FEAT_SWITCH(T)        \
+  switch (P.L.K) {               \
+    case 1: VX_FEAT_LAUNCH(T, 1); break; \
+    case 2: VX_FEAT_LAUNCH(T, 2); break; \
+    case 3: VX_FEAT_LAUNCH(T, 3); break; \
+    default: VX_FEAT_LAUNCH(T, 4); break; \
+  }
+  if (out_bf16) {
+    VX_FEAT_SWITCH(__nv_bfloat16)
+  } else {
+    VX_FEAT_SWITCH(float)
+  }
+#undef VX_FEAT_SWITCH
+#undef VX_FEAT_LAUNCH
   return launch_status();
 }
 
@@ -508,15 +635,29 @@ int vx_mlp_head(const void* H, int64_t n_rows, int64_t width, int64_t ldh, int32
   if (width > HEAD_MAX_WIDTH) return VX_ERR_UNSUPPORTED;
   if (n_rows == 0) return VX_OK;
   if (!H || !W || !out || (cols && ld_cols < 3)) return VX_ERR_ARG;
-  const int64_t blocks_needed = (n_rows + 7) / 8;
+  const int64_t blocks_needed = (n_rows + 255) / 256;
   const unsigned blocks = (unsigned)(blocks_needed < (int64_t)sm_count() * 8 ? blocks_needed : sm_count() * 8);
-  if (in_bf16)
-    mlp_head_kernel<__nv_bfloat16><<<blocks, 256, 0, as_stream(stream)>>>(
-        reinterpret_cast<const __nv_bfloat16*>(H), n_rows, (int)width, ldh, W, b, add, out, cols, ld_cols, cols_bf16);
-  else
-    mlp_head_kernel<float><<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const float*>(H), n_rows,
-                                                                  (int)width, ldh, W, b, add, out, cols, ld_cols,
-                                                                  cols_bf16);
+  const int64_t esz = in_bf16 ? 2 : 4, per = 16 / esz;
+  const bool vec = (width % per == 0) && (ldh % per == 0) && ((reinterpret_cast<uintptr_t>(H) & 15) == 0);
+  cudaStream_t st = as_stream(stream);
+  const int w = (int)width;
+  if (in_bf16) {
+    const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(H);
+    if (vec)
+      mlp_head_kernel<__nv_bfloat16, true><<<blocks, 256, 0, st>>>(h, n_rows, w, ldh, W, b, add, out, cols, ld_cols,
+                                                                   cols_bf16);
+    else
+      mlp_head_kernel<__nv_bfloat16, false><<<blocks, 256, 0, st>>>(h, n_rows, w, ldh, W, b, add, out, cols, ld_cols,
+                                                                    cols_bf16);
+  } else {
+    const float* h = reinterpret_cast<const float*>(H);
+    if (vec)
+      mlp_head_kernel<float, true><<<blocks, 256, 0, st>>>(h, n_rows, w, ldh, W, b, add, out, cols, ld_cols,
+                                                           cols_bf16);
+    else
+      mlp_head_kernel<float, false><<<blocks, 256, 0, st>>>(h, n_rows, w, ldh, W, b, add, out, cols, ld_cols,
+                                                            cols_bf16);
+  }
   return launch_status();
 }
 

@@ -53,7 +53,7 @@ class ResidentScene:
     compute dtype, output layers FP32) and the scene's s_val."""
 
     def __init__(self, model, s_val: float | None = None, stepsize: float = 0.5, near: float = 0.1,
-                 bg: float = 0.0, precision: str = "bf16"):
+                 bg: float = 0.0, precision: str = "bf16", skip_block: int = 8):
         if precision not in ("bf16", "fp32"):
             raise ValueError(precision)
         dev = model.sdf.grid.device
@@ -88,6 +88,7 @@ class ResidentScene:
         d.k0_bf16 = int(precision == "bf16")
         d.voxel_size = vs
         self.mask = None
+        self.occ = None
         if model.mask_cache is not None:
             mc = model.mask_cache
             self.mask = mc.mask.contiguous()
@@ -97,6 +98,15 @@ class ResidentScene:
             for a in range(3):
                 d.mask_scale[a] = float(sc[a])
                 d.mask_shift[a] = float(sh[a])
+            if skip_block:
+                # block occupancy of the mask: the march jumps over empty blocks
+                B = int(skip_block)
+                oshape = tuple(-(-int(s) // B) + 2 for s in self.mask.shape)
+                self.occ = torch.empty(oshape, dtype=torch.uint8, device=dev)
+                _abi.call("vx_mask_occupancy", ptr(self.mask), *self.mask.shape, B, ptr(self.occ), stream_ptr(dev))
+                d.occ = self.occ.data_ptr()
+                d.occ_X, d.occ_Y, d.occ_Z = oshape
+                d.occ_block = B
         d.inv_s = inv_s_of(self.s_val)
         d.stepdist = self.stepdist
         d.near = float(near)

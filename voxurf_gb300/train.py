@@ -35,7 +35,9 @@ def eikonal_loss(gradient: torch.Tensor) -> torch.Tensor:
 
 
 class FineTrainer:
-    """Owns the optimizer of a fine Voxurf model and runs fused steps.
+    """Owns the optimizer of a Voxurf model and runs fused steps (the fine
+    model; the coarse model too, which has no k_rgbnet group and no
+    rgb_marched0 term).
 
     lr_* are the per-group learning rates (utils.create_optimizer_or_freeze_model
     groups sdf / k0 / rgbnet / k_rgbnet); tv_sdf / tv_k0 are the weights
@@ -67,8 +69,9 @@ class FineTrainer:
             {"params": [model.k0.grid], "lr": lr_k0, "name": "k0", "tv_weight": tv_k0 / n_rays * scale,
              "tv_dense": tv_dense, "shadow": shadow},
             {"params": list(model.rgbnet.parameters()), "lr": lr_rgbnet, "name": "rgbnet"},
-            {"params": list(model.k_rgbnet.parameters()), "lr": lr_k_rgbnet, "name": "k_rgbnet"},
         ]
+        if getattr(model, "k_rgbnet", None) is not None:   # the coarse model has no k-branch
+            groups.append({"params": list(model.k_rgbnet.parameters()), "lr": lr_k_rgbnet, "name": "k_rgbnet"})
         self.optimizer = Adam(groups, betas=(0.9, 0.99))
         self.loss_weights = loss_weights
         self.global_step = 0
