@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--no-bf16", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-render", action="store_true", help="skip the render-server measurement")
+    p.add_argument("--no-long", action="store_true", help="skip the long-ray (384^3, stepsize 0.25) measurement")
     p.add_argument("--render-requests", type=int, default=120)
     p.add_argument("--render-only", action="store_true", help="only the render-server measurement (profiling)")
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
@@ -293,6 +294,9 @@ def run_ours(args, world, rank, local):
     render = None
     if not args.no_render:
         render = run_render(args, dev)
+    long_rays = None
+    if not args.no_long and R == 256:
+        long_rays = run_long_rays(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -311,12 +315,61 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4},
             "fused_bf16": bf16,
             "render": render,
+            "long_rays": long_rays,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),
         }
         print(json.dumps(line))
+
+
+LONG_R = 384               # long-ray workload: 64 spheres, stepsize 0.25, 65536 rays, s = 0.05
+LONG_RAYS = 65536
+LONG_STEPS = 5
+
+
+def run_long_rays(args, dev):
+    """Long-ray stress workload (SDF 384^3 holding 64 random spheres + noise,
+    k0 384^3 x 12, 65536 rays per step at stepsize 0.25 voxel = up to ~2660
+    samples per ray, s-density 0.05): the plain FP32 step against the fused
+    BF16 graph-replayed step, both full training steps."""
+    import numpy as np
+    import torch
+
+    from voxurf_gb300 import configs, synthetic
+    from voxurf_gb300.train import FineTrainer
+
+    rk = dict(configs.FINE_RENDER_KWARGS, stepsize=0.25)
+    n_b = 3 + LONG_STEPS
+    o, d, v = synthetic.random_rays(LONG_RAYS * n_b, seed=11)
+    t = configs.train_targets(LONG_RAYS * n_b, 11)
+    batches = [torch.from_numpy(np.ascontiguousarray(a.reshape(n_b, LONG_RAYS, 3))).to(dev) for a in (o, d, v, t)]
+    out = {"workload": f"SDF {LONG_R}^3 64 spheres + k0 {LONG_R}^3x12, {LONG_RAYS} rays/step, stepsize 0.25, "
+                       "s 0.05, mask |SDF|<0.05", "rays_per_step": LONG_RAYS}
+    for name, precision, graphed in (("fp32", "fp32", False), ("bf16_graphed", "bf16", True)):
+        model = configs.build_fine_model(LONG_R, precision, device=dev, seed=7, scene="spheres64",
+                                         mask_voxels=0.05 / (2.0 / LONG_R))
+        tr = FineTrainer(model, n_rays=LONG_RAYS, graphed=graphed)
+        for i in range(3):
+            tr.step(batches[0][i], batches[1][i], batches[2][i], batches[3][i], rk, global_step=0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(3, n_b):
+            tr.step(batches[0][i], batches[1][i], batches[2][i], batches[3][i], rk, global_step=0)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / LONG_STEPS
+        out[name] = {"rays_per_s": LONG_RAYS / (ms / 1000.0), "ms_per_step": ms}
+        if not graphed:
+            fr = model._last_frame
+            out["shaded_rows_last_step"] = int(fr.S2)
+            out["max_steps_bound"] = int(fr.max_steps)
+        del tr, model
+        torch.cuda.empty_cache()
+    out["speedup_bf16_vs_fp32"] = out["bf16_graphed"]["rays_per_s"] / out["fp32"]["rays_per_s"]
+    return out
 
 
 RENDER_SCENES = 4

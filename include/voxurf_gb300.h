@@ -38,6 +38,7 @@ extern "C" {
 #define VX_ERR_CUDA 5        /* other CUDA runtime error                    */
 #define VX_ERR_UNSUPPORTED 6 /* configuration not supported by this build   */
 #define VX_ERR_TOO_LARGE 7   /* size above the fixed maximum of a no-allocation entry point */
+#define VX_ERR_TIMEOUT 8     /* a bounded on-device wait expired (reported via vx_device_error) */
 
 /* Largest ray count vx_sample_pts_count_noalloc accepts. */
 #define VX_NOALLOC_MAX_RAYS 4194304
@@ -494,6 +495,42 @@ typedef struct {
                                raw interpolated SDF gradient (eikonal term)    */
 } vx_coarse_backward_args;
 int vx_coarse_backward(const vx_coarse_backward_args* args, void* stream);
+
+/* ---- fused colour-MLP forward on the tcgen05 tensor cores (the rgbnet /
+ *      k_rgbnet stacks of lib/voxurf_fine.py:132-187, three 192-wide hidden
+ *      layers with ReLU and a 3-output layer) --------------------------------- */
+
+/* Packs W [N,K] (row-major FP32, nn.Linear.weight) into the BF16 operand
+ * layout of vx_mlp_tc_forward: [Kp/8][N][8], K zero-padded to Kp (multiple
+ * of 8). */
+int vx_mlp_tc_pack(const float* W, int64_t N, int64_t K, int64_t Kp, void* out, void* stream);
+
+typedef struct {
+  const void* X;            /* [n_rows, ldx] BF16 input rows, 16-byte aligned, ldx % 8 == 0 */
+  int64_t ldx;
+  int64_t K0;               /* first-layer inputs (multiple of 16, <= 80); X columns [K0_real, K0) must
+                               be zero or meet zero weight columns                   */
+  int64_t n_rows;
+  int64_t width;            /* hidden width: 192                                    */
+  const void* W0p;          /* vx_mlp_tc_pack(W0, 192, K, K0)                        */
+  const void* W1p;          /* vx_mlp_tc_pack(W1, 192, 192, 192)                     */
+  const void* W2p;
+  const float* b0;          /* [192] hidden biases (FP32)                           */
+  const float* b1;
+  const float* b2;
+  const float* Wh;          /* [3,192] output layer (FP32)                          */
+  const float* bh;          /* [3]                                                  */
+  const float* add;         /* optional [n_rows,3] added to the output (k_rgbnet's residual logits) */
+  float* out;               /* [n_rows,3] logits                                    */
+  void* cols;               /* optional: the logits also stored as BF16 at cols[row*ld_cols + 0..2] */
+  int64_t ld_cols;
+} vx_mlp_tc_args;
+
+/* out = Wh relu(W2 relu(W1 relu(W0 x + b0) + b1) + b2) + bh (+ add) for every
+ * row: BF16 operands, FP32 accumulation in tensor memory, hidden activations
+ * rounded to BF16 between layers, output layer in FP32.  One persistent CTA
+ * per SM holds the hidden weights in shared memory. */
+int vx_mlp_tc_forward(const vx_mlp_tc_args* args, void* stream);
 
 /* ---- render server: the inference form of Voxurf.forward (global_step =
  *      None, lib/voxurf_fine.py:620-802) for rays of several resident scenes

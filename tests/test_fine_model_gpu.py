@@ -119,3 +119,32 @@ def test_smooth_grad_tv_matches_oracle(cuda, masked):
     ol.backward()
     assert abs(loss.item() - ol.item()) <= 1e-5 * abs(ol.item())
     assert _rel_l2(model.sdf.grid.grad, oracle.sdf_grid.grad) <= 1e-5
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("bf16", 1e-3)])
+def test_long_rays_match_fp64_oracle(cuda, precision, tol):
+    """Long-ray workload at a size the oracle finishes quickly: 64 random
+    spheres on a 128^3 grid, stepsize 0.25 voxel (up to 700 samples per ray,
+    74 of the 192 rays beyond 512), s-density 0.05 (global_step 0).  Same
+    shaded-sample set, RGB within tol; FP32 gradients rel-L2 <= 1e-5."""
+    R = 128
+    model = configs.build_fine_model(R, precision, device=cuda, seed=7, scene="spheres64", width=32)
+    oracle = OracleFine(model, dtype=torch.float64)
+    ro, rd, vd = synthetic.random_rays(192, seed=31)
+    rays = (ro, rd, vd, configs.train_targets(192, 31))
+    rk = dict(RK, stepsize=0.25)
+    g, gl = _run_gpu(model, rays, rk, step=0)
+    o, ol = _run_oracle(oracle, rays, rk, step=0)
+    from oracle.ops import RenderUtilsOracle
+
+    stepdist = float(np.float32(0.25) * np.float32(model.voxel_size.item()))
+    n_steps = RenderUtilsOracle.sample_pts_on_rays(torch.from_numpy(ro), torch.from_numpy(rd), oracle.xyz_min32,
+                                                   oracle.xyz_max32, rk["near"], 1e9, stepdist)[4]
+    assert int(n_steps.max()) > 512, int(n_steps.max())   # rays marched beyond 512 samples
+    if precision == "fp32":
+        assert torch.equal(g["ray_id"].long().cpu(), o["ray_id"])
+    err = (g["rgb_marched"].detach().double().cpu() - o["rgb_marched"].detach()).abs().max().item()
+    assert err <= tol, err
+    if precision == "fp32":
+        assert _rel_l2(model.sdf.grid.grad, oracle.sdf_grid.grad) <= 1e-5
+        assert _rel_l2(model.k0.grid.grad, oracle.k0_grid.grad) <= 1e-5

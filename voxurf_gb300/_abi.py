@@ -117,6 +117,14 @@ class CoarseBackwardArgs(C.Structure):
     ]
 
 
+class MlpTcArgs(C.Structure):
+    _fields_ = [
+        ("X", P), ("ldx", I64), ("K0", I64), ("n_rows", I64), ("width", I64), ("W0p", P), ("W1p", P), ("W2p", P),
+        ("b0", P), ("b1", P), ("b2", P), ("Wh", P), ("bh", P), ("add", P), ("out", P), ("cols", P),
+        ("ld_cols", I64),
+    ]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [
         ("grid", GridGeom), ("sdf_smooth", P), ("k0", P), ("k0_bf16", I32), ("voxel_size", F), ("mask", P),
@@ -145,6 +153,7 @@ _STRUCT_FNS = {
     "vx_fine_composite": FineCompositeArgs,
     "vx_fine_composite_backward": FineCompositeBwdArgs,
     "vx_fine_backward": FineBackwardArgs,
+    "vx_mlp_tc_forward": MlpTcArgs,
 }
 
 _SERVE_SIGNATURES = {

@@ -1,0 +1,342 @@
+// Fused colour-MLP forward on the 5th-generation tensor cores (tcgen05).
+//
+// One persistent CTA per SM keeps all three 192-wide hidden layers of one
+// colour MLP (rgbnet or k_rgbnet, voxurf_fine.py:132-187) resident in shared
+// memory (BF16, 30 + 72 + 72 KB) and streams 128-row tiles of its input
+// rows through them:
+//
+//   X tile (128 x K0, BF16) --tcgen05.mma--> TMEM (128 x 192 FP32)
+//     --tcgen05.ld--> +bias, ReLU, BF16 --st.shared--> A tile --mma--> ...
+//   last hidden layer: +bias, ReLU in registers, then the 192 -> 3 output
+//   layer on the CUDA cores (FP32), + optional residual logits.
+//
+// Hidden activations never leave the SM; HBM traffic per row is the input
+// row and 12 bytes of logits.  Operands use the canonical K-major layout
+// without swizzle: 8 x 16-byte core matrices, chunk c of K (8 elements) of
+// all R rows stored contiguously ([K/8][R][8]), so LBO = R * 16 bytes (next
+// core matrix along K) and SBO = 128 bytes (next 8 rows).  Weights are
+// packed into that layout by the caller (vx_mlp_tc_pack) and copied to
+// shared memory once per CTA.
+//
+// Thread roles: 4 warps; warp w owns TMEM lanes / tile rows [32w, 32w+32)
+// in the epilogue; thread 0 issues the MMAs and the commit.  Every wait on
+// an mbarrier is bounded: on expiry the kernel records VX_ERR_TIMEOUT,
+// releases its TMEM and returns.
+#include "common.cuh"
+
+namespace vx {
+
+constexpr int TC_M = 128;       // rows per tile (one cta_group::1 MMA)
+constexpr int TC_N = 192;       // hidden width
+constexpr int TC_KMAX0 = 80;    // largest first-layer K (shared memory: 30 + 144 + 48 KB)
+constexpr int TC_TMEM_COLS = 256;
+
+struct MlpTcParams {
+  const __nv_bfloat16* X;  // [n_rows, ldx] input rows (columns K0.. zero or ignored via zero weights)
+  int64_t ldx;
+  int K0;                  // first-layer K (multiple of 16, <= TC_KMAX0)
+  int64_t n_rows;
+  const __nv_bfloat16* W0p;  // packed [K0/8][192][8]
+  const __nv_bfloat16* W1p;  // packed [24][192][8]
+  const __nv_bfloat16* W2p;
+  const float* b0;
+  const float* b1;
+  const float* b2;
+  const float* Wh;   // [3,192] output layer (FP32)
+  const float* bh;   // [3]
+  const float* add;  // optional [n,3] added to the logits
+  float* out;        // [n,3]
+  __nv_bfloat16* cols;  // optional: logits also stored (BF16) at cols[row*ld_cols + 0..2]
+  int64_t ld_cols;
+  int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// tcgen05 shared-memory matrix descriptor, K-major, no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);            // bits 0-13: start address >> 4
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;         // bits 16-29: leading byte offset >> 4
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;         // bits 32-45: stride byte offset >> 4
+  d |= (uint64_t)1 << 46;                             // bits 46-48: fixed 0b001
+  // base offset 0, absolute-LBO mode off, swizzle mode 0 (none)
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = FP32, both K-major.
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) {
+  return (1u << 4)            // D format F32
+         | (1u << 7)          // A format BF16
+         | (1u << 10)         // B format BF16
+         | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Bounded wait for the phase `parity` of an mbarrier; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t it = 0; it < (1u << 26); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"((uint32_t)acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float v[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// All K/16 MMAs of one layer (issued by one thread) and the commit.
+__device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_s, uint32_t b_s, int K, uint64_t* bar) {
+  constexpr uint32_t idesc = umma_idesc(TC_M, TC_N);
+  for (int ks = 0; ks < K / 16; ++ks) {
+    const uint64_t ad = umma_desc(a_s + (uint32_t)(2 * ks) * (TC_M * 16), TC_M * 16, 128);
+    const uint64_t bd = umma_desc(b_s + (uint32_t)(2 * ks) * (TC_N * 16), TC_N * 16, 128);
+    tc_mma(tmem, ad, bd, idesc, ks > 0);
+  }
+  tc_commit(bar);
+}
+
+__global__ void __launch_bounds__(128, 1) mlp_tc_kernel(MlpTcParams P) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int K0 = P.K0;
+  __nv_bfloat16* W0s = reinterpret_cast<__nv_bfloat16*>(smem);
+  __nv_bfloat16* W1s = W0s + (size_t)K0 * TC_N;
+  __nv_bfloat16* W2s = W1s + (size_t)TC_N * TC_N;
+  __nv_bfloat16* As = W2s + (size_t)TC_N * TC_N;  // [24][128][8] (the input tile uses [K0/8][128][8])
+  uint64_t* bar = reinterpret_cast<uint64_t*>(As + (size_t)TC_N * TC_M);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // weights -> shared memory (already packed), 16-byte copies
+  {
+    const uint4* src[3] = {reinterpret_cast<const uint4*>(P.W0p), reinterpret_cast<const uint4*>(P.W1p),
+                           reinterpret_cast<const uint4*>(P.W2p)};
+    uint4* dst[3] = {reinterpret_cast<uint4*>(W0s), reinterpret_cast<uint4*>(W1s), reinterpret_cast<uint4*>(W2s)};
+    const int n16[3] = {K0 * TC_N / 8, TC_N * TC_N / 8, TC_N * TC_N / 8};
+    for (int m = 0; m < 3; ++m)
+      for (int i = tid; i < n16[m]; i += blockDim.x) dst[m][i] = __ldg(src[m] + i);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) mbar_init(bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tmem_warp = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 lanes
+  const uint32_t a_s = smem_u32(As), w_s[3] = {smem_u32(W0s), smem_u32(W1s), smem_u32(W2s)};
+  const float* bias[3] = {P.b0, P.b1, P.b2};
+  uint32_t phase = 0;
+  bool ok = true;
+
+  const int64_t n_tiles = (P.n_rows + TC_M - 1) / TC_M;
+  for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+    const int64_t row0 = tile * TC_M;
+    // input tile -> As in core-matrix layout (rows beyond n_rows are zero)
+    const int chunks = K0 / 8;
+    for (int i = tid; i < chunks * TC_M; i += blockDim.x) {
+      const int c = i / TC_M, r = i % TC_M;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (row0 + r < P.n_rows)
+        v = __ldg(reinterpret_cast<const uint4*>(P.X + (row0 + r) * P.ldx) + c);
+      reinterpret_cast<uint4*>(As)[(size_t)c * TC_M + r] = v;
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const int64_t row = row0 + 32 * warp + lane;
+    for (int layer = 0; layer < 3 && ok; ++layer) {
+      if (tid == 0) tc_layer(tmem, a_s, w_s[layer], layer == 0 ? K0 : TC_N, bar);
+      ok = mbar_wait(bar, phase);
+      phase ^= 1u;
+      tc_fence_after();
+      if (!ok) break;
+      if (layer < 2) {
+        // +bias, ReLU, BF16 -> As (the next layer's A operand)
+        for (int j = 0; j < TC_N / 32; ++j) {
+          float v[32];
+          tc_ld32(tmem_warp + 32 * j, v);
+          uint4* dst = reinterpret_cast<uint4*>(As);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            float h[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) h[e] = fmaxf(v[8 * q + e] + __ldg(bias[layer] + 32 * j + 8 * q + e), 0.f);
+            dst[(size_t)(4 * j + q) * TC_M + 32 * warp + lane] =
+                make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+          }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+      } else {
+        // last hidden layer: +bias, ReLU (rounded to BF16 like the GEMM path's
+        // output), then the FP32 output layer
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int j = 0; j < TC_N / 32; ++j) {
+          float v[32];
+          tc_ld32(tmem_warp + 32 * j, v);
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            const int col = 32 * j + e;
+            const float h = __bfloat162float(__float2bfloat16_rn(fmaxf(v[e] + __ldg(P.b2 + col), 0.f)));
+            a0 += h * __ldg(P.Wh + col);
+            a1 += h * __ldg(P.Wh + TC_N + col);
+            a2 += h * __ldg(P.Wh + 2 * TC_N + col);
+          }
+        }
+        if (row < P.n_rows) {
+          a0 += __ldg(P.bh + 0);
+          a1 += __ldg(P.bh + 1);
+          a2 += __ldg(P.bh + 2);
+          if (P.add) {
+            a0 += P.add[3 * row + 0];
+            a1 += P.add[3 * row + 1];
+            a2 += P.add[3 * row + 2];
+          }
+          P.out[3 * row + 0] = a0;
+          P.out[3 * row + 1] = a1;
+          P.out[3 * row + 2] = a2;
+          if (P.cols) {
+            __nv_bfloat16* cp = P.cols + row * P.ld_cols;
+            cp[0] = __float2bfloat16_rn(a0);
+            cp[1] = __float2bfloat16_rn(a1);
+            cp[2] = __float2bfloat16_rn(a2);
+          }
+        }
+        tc_fence_before();
+        __syncthreads();  // TMEM and As are reused by the next tile
+        tc_fence_after();
+      }
+    }
+  }
+  if (!ok && tid == 0) set_device_error(P.err, VX_ERR_TIMEOUT);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
+// [N, K] row-major FP32 weights -> [K/8][N][8] BF16 (K padded with zeros to Kp).
+__global__ void mlp_tc_pack_kernel(const float* __restrict__ W, int N, int K, int Kp, __nv_bfloat16* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)N * Kp) return;
+  const int e = (int)(i % 8), n = (int)((i / 8) % N), c = (int)(i / (8 * (int64_t)N));
+  const int k = 8 * c + e;
+  out[i] = __float2bfloat16_rn(k < K ? W[(int64_t)n * K + k] : 0.f);
+}
+
+static size_t mlp_tc_smem_bytes(int K0) {
+  return (size_t)K0 * TC_N * 2 + 2 * (size_t)TC_N * TC_N * 2 + (size_t)TC_N * TC_M * 2 + 16;
+}
+
+}  // namespace vx
+
+using namespace vx;
+
+extern "C" {
+
+int vx_mlp_tc_pack(const float* W, int64_t N, int64_t K, int64_t Kp, void* out, void* stream) {
+  if (!W || !out || N < 1 || K < 1 || Kp < K || Kp % 8) return VX_ERR_ARG;
+  mlp_tc_pack_kernel<<<grid_for(N * Kp), VX_THREADS, 0, as_stream(stream)>>>(W, (int)N, (int)K, (int)Kp,
+                                                                          reinterpret_cast<__nv_bfloat16*>(out));
+  return launch_status();
+}
+
+int vx_mlp_tc_forward(const vx_mlp_tc_args* A, void* stream) {
+  if (!A || A->n_rows < 0) return VX_ERR_ARG;
+  if (A->n_rows == 0) return VX_OK;
+  if (A->width != TC_N || A->K0 < 16 || A->K0 > TC_KMAX0 || A->K0 % 16) return VX_ERR_UNSUPPORTED;
+  if (!A->X || !A->W0p || !A->W1p || !A->W2p || !A->b0 || !A->b1 || !A->b2 || !A->Wh || !A->bh || !A->out)
+    return VX_ERR_ARG;
+  if (A->ldx < A->K0 || (A->ldx % 8) || (reinterpret_cast<uintptr_t>(A->X) & 15)) return VX_ERR_ARG;
+  if ((reinterpret_cast<uintptr_t>(A->W0p) | reinterpret_cast<uintptr_t>(A->W1p) |
+       reinterpret_cast<uintptr_t>(A->W2p)) & 15)
+    return VX_ERR_ARG;
+  MlpTcParams P{};
+  P.X = reinterpret_cast<const __nv_bfloat16*>(A->X);
+  P.ldx = A->ldx;
+  P.K0 = (int)A->K0;
+  P.n_rows = A->n_rows;
+  P.W0p = reinterpret_cast<const __nv_bfloat16*>(A->W0p);
+  P.W1p = reinterpret_cast<const __nv_bfloat16*>(A->W1p);
+  P.W2p = reinterpret_cast<const __nv_bfloat16*>(A->W2p);
+  P.b0 = A->b0;
+  P.b1 = A->b1;
+  P.b2 = A->b2;
+  P.Wh = A->Wh;
+  P.bh = A->bh;
+  P.add = A->add;
+  P.out = A->out;
+  P.cols = reinterpret_cast<__nv_bfloat16*>(A->cols);
+  P.ld_cols = A->ld_cols;
+  P.err = device_error_ptr();
+  const size_t smem = mlp_tc_smem_bytes(P.K0);
+  cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_status(e);
+  const int64_t tiles = (A->n_rows + TC_M - 1) / TC_M;
+  const unsigned grid = (unsigned)(tiles < sm_count() ? tiles : sm_count());
+  mlp_tc_kernel<<<grid, 128, smem, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+}  // extern "C"

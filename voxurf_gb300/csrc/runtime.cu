@@ -48,6 +48,7 @@ const char* vx_status_string(int status) {
     case VX_ERR_CUDA: return "CUDA runtime error";
     case VX_ERR_UNSUPPORTED: return "unsupported configuration";
     case VX_ERR_TOO_LARGE: return "size above the fixed maximum of the no-allocation entry point";
+    case VX_ERR_TIMEOUT: return "bounded device wait expired";
     default: return "unknown status";
   }
 }

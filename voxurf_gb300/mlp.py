@@ -91,3 +91,51 @@ def mlp_params(net: nn.Sequential) -> list[torch.Tensor]:
 def apply_mlp(net: nn.Sequential, x: torch.Tensor) -> torch.Tensor:
     """net(x) with the fused backward; x float32 or bfloat16 (compute dtype)."""
     return _MLP.apply(x.contiguous(), *mlp_params(net))
+
+
+class TensorCoreMLP:
+    """A rgbnet / k_rgbnet stack (Linear(K,192), ReLU, 2 x [Linear(192,192),
+    ReLU], Linear(192,3)) packed for the fused tcgen05 forward
+    (vx_mlp_tc_forward): hidden weights BF16 in the operand layout, first
+    layer K zero-padded to K0 (multiple of 16), biases rounded to BF16 like
+    the GEMM path, output layer FP32.  Inference only (no autograd)."""
+
+    WIDTH = 192
+
+    @staticmethod
+    def supports(net: nn.Sequential, K0: int) -> bool:
+        lin = [m for m in net.modules() if isinstance(m, nn.Linear)]
+        return (len(lin) == 4 and all(m.out_features == TensorCoreMLP.WIDTH for m in lin[:3])
+                and lin[3].out_features == 3 and lin[0].in_features <= K0 <= 80 and K0 % 16 == 0)
+
+    def __init__(self, net: nn.Sequential, K0: int):
+        if not self.supports(net, K0):
+            raise ValueError("the fused tensor-core MLP needs Linear(K<=80,192), 2 x Linear(192,192), "
+                             "Linear(192,3)")
+        lin = [m for m in net.modules() if isinstance(m, nn.Linear)]
+        dev = lin[0].weight.device
+        st = stream_ptr(dev)
+        self.K0 = K0
+        self.packed = []
+        for i, m in enumerate(lin[:3]):
+            Kp = K0 if i == 0 else self.WIDTH
+            out = torch.empty((Kp // 8) * self.WIDTH * 8, dtype=torch.bfloat16, device=dev)
+            W = m.weight.detach().float().contiguous()
+            call("vx_mlp_tc_pack", ptr(W), self.WIDTH, W.shape[1], Kp, ptr(out), st)
+            self.packed.append(out)
+        self.biases = [m.bias.detach().to(torch.bfloat16).float().contiguous() for m in lin[:3]]
+        self.Wh = lin[3].weight.detach().float().contiguous()
+        self.bh = lin[3].bias.detach().float().contiguous()
+
+    def forward(self, X: torch.Tensor, out: torch.Tensor, add: torch.Tensor | None = None,
+                cols: torch.Tensor | None = None, ld_cols: int = 0) -> None:
+        """out[i] = MLP(X[i, :K0]) (+ add[i]); X [n, ldx] BF16 rows, out [n,3] FP32."""
+        from . import _abi
+
+        a = _abi.MlpTcArgs()
+        a.X, a.ldx, a.K0, a.n_rows, a.width = ptr(X), X.stride(0), self.K0, X.shape[0], self.WIDTH
+        a.W0p, a.W1p, a.W2p = (ptr(t) for t in self.packed)
+        a.b0, a.b1, a.b2 = (ptr(t) for t in self.biases)
+        a.Wh, a.bh, a.add, a.out = ptr(self.Wh), ptr(self.bh), ptr(add), ptr(out)
+        a.cols, a.ld_cols = ptr(cols), ld_cols
+        _abi.call_struct("vx_mlp_tc_forward", a, stream_ptr(X.device))

@@ -33,6 +33,7 @@ import torch
 from . import _abi
 from . import grid as grid_mod
 from ._torch import ptr, scratch, stream_ptr
+from .mlp import TensorCoreMLP
 from .voxurf_fine import _feature_cfg, max_steps_bound, smooth_grid
 
 _BYTES_PER_PIXEL = 16  # rgb f32 + depth f32 (device and pinned host)
@@ -78,8 +79,16 @@ class ResidentScene:
         self.k_res = bool(model.k_res)
         self.use_rgb_k = bool(model.use_rgb_k)
         self.d2a = model.k_dim0 - (3 if self.k_res else 0)
-        self.rgbnet = self._mlp(model.rgbnet)
-        self.k_rgbnet = self._mlp(model.k_rgbnet) if self.use_rgb_k else None
+        # MLP input rows padded to 16 columns (the tensor-core K step)
+        self.ld1 = _round_up(self.d1, 16)
+        self.ld2 = _round_up(self.d2a + 3, 16)
+        self.rgbnet = self._mlp(model.rgbnet, self.ld1)
+        self.k_rgbnet = self._mlp(model.k_rgbnet, self.ld2) if self.use_rgb_k else None
+        # fused tcgen05 forward of both MLPs (BF16 scenes of the 192-wide layout)
+        self.tc = None
+        if precision == "bf16" and self.use_rgb_k and TensorCoreMLP.supports(model.rgbnet, self.ld1) \
+                and TensorCoreMLP.supports(model.k_rgbnet, self.ld2):
+            self.tc = (TensorCoreMLP(model.rgbnet, self.ld1), TensorCoreMLP(model.k_rgbnet, self.ld2))
 
         d = _abi.SceneDesc()
         d.grid = grid_mod.grid_geom(self.sdf.shape, xyz_min, xyz_max)
@@ -115,15 +124,15 @@ class ResidentScene:
         self.desc = d
         self.device = dev
 
-    def _mlp(self, net):
-        """(hidden [(W, b)], head (W, b)); the first layer's W is padded with
-        zero columns to a multiple of 8 inputs (16-byte aligned GEMM rows)."""
+    def _mlp(self, net, ld: int):
+        """(hidden [(W, b)], head (W, b)) for the GEMM path; the first layer's
+        W is padded with zero columns to the row stride ld of its input."""
         lin = [m for m in net.modules() if isinstance(m, torch.nn.Linear)]
         hidden = []
         for i, m in enumerate(lin[:-1]):
             W = m.weight.detach()
             if i == 0:
-                Wp = torch.zeros((W.shape[0], _round_up(W.shape[1], 8)), dtype=self.dtype, device=W.device)
+                Wp = torch.zeros((W.shape[0], ld), dtype=self.dtype, device=W.device)
                 Wp[:, :W.shape[1]] = W
                 W = Wp
             hidden.append((W.to(self.dtype).contiguous(), m.bias.detach().to(self.dtype).contiguous()))
@@ -201,7 +210,10 @@ class OutputArena:
 
 class RenderServer:
     def __init__(self, scenes: list[ResidentScene], tick_rays: int = 1 << 19, arena_pixels: int | None = None,
-                 hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None):
+                 hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None, mlp: str = "tc"):
+        """mlp: "tc" runs each scene's two colour MLPs as fused tcgen05
+        launches where the scene supports it (BF16, 192-wide), "gemm" as
+        per-layer cuBLAS GEMMs plus vx_mlp_head."""
         if not 1 <= len(scenes) <= 8:
             raise ValueError("1 to 8 resident scenes")
         if not all(s.use_rgb_k and s.k_res for s in scenes):
@@ -221,8 +233,11 @@ class RenderServer:
         self.cfg = scenes[0].cfg
         self.d1 = scenes[0].d1
         self.d2a = scenes[0].d2a
-        self.ld1 = _round_up(self.d1, 8)
-        self.ld2 = _round_up(self.d2a + 3, 8)
+        self.ld1 = scenes[0].ld1
+        self.ld2 = scenes[0].ld2
+        if mlp not in ("tc", "gemm"):
+            raise ValueError(mlp)
+        self.mlp = mlp
         dev = self.device
         N = self.tick_rays
         # per-tick workspace (fixed size)
@@ -438,6 +453,12 @@ class RenderServer:
     def _shade(self, s: ResidentScene, a: int, b: int, st: int) -> None:
         n = b - a
         bf = int(self.bf16)
+        if s.tc is not None and self.mlp == "tc":
+            # rgbnet -> logits (also into the k_rgbnet input's last columns), then
+            # k_rgbnet with the logits as residual, each one fused tcgen05 launch
+            s.tc[0].forward(self.X1[a:b], self.logit[a:b], cols=self.X2[a:b, self.d2a:], ld_cols=self.ld2)
+            s.tc[1].forward(self.X2[a:b], self.klogit[a:b], add=self.logit[a:b])
+            return
         h = self._hidden(s.rgbnet[0], self.X1[a:b])
         W, bias = s.rgbnet[1]
         cols = self.X2[a:b, self.d2a:] if s.k_res else None
