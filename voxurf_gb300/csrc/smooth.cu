@@ -110,12 +110,34 @@ __device__ __forceinline__ float adjoint1d(const Taps& t, int j, int n, Get get)
   return acc;
 }
 
-template <bool ADJOINT, bool ACCUM>
+// 1-D pass at global position j of an axis of length n, reading the staged
+// values through get(k) for k in [j-H, j+H] (staged coordinates are
+// clamped for the forward, zero outside the grid for the adjoint).  The
+// adjoint is the transposed convolution (flipped taps) except at the two
+// boundary positions, which also collect the taps the forward clamped.
+template <bool ADJOINT, int H, typename Get>
+__device__ __forceinline__ float pass1d(const Taps& t, const float w[2 * H + 1], int j, int n, Get get) {
+  float acc = 0.f;
+  if (ADJOINT) {
+    if (j == 0 || j == n - 1) return adjoint1d(t, j, n, get);
+#pragma unroll
+    for (int tt = H; tt >= -H; --tt) acc += w[H - tt] * get(j + tt);  // the order of adjoint1d
+  } else {
+#pragma unroll
+    for (int tt = -H; tt <= H; ++tt) acc += w[tt + H] * get(j + tt);
+  }
+  return acc;
+}
+
+template <bool ADJOINT, bool ACCUM, int H>
 __global__ void __launch_bounds__(256) smooth_tile_kernel(const float* __restrict__ in, float* __restrict__ out,
                                                          int X, int Y, int Z, Taps t) {
   __shared__ float s_in[SX][SY][SZ];
   __shared__ float s_z[SX][SY][TZ];
   __shared__ float s_y[SX][TY][TZ];
+  float w[2 * H + 1];
+#pragma unroll
+  for (int i = 0; i < 2 * H + 1; ++i) w[i] = t.w[i];
   const int x0 = blockIdx.z * TX, y0 = blockIdx.y * TY, z0 = blockIdx.x * TZ;
   const int tid = threadIdx.x;
   for (int e = tid; e < SX * SY * SZ; e += blockDim.x) {
@@ -137,44 +159,36 @@ __global__ void __launch_bounds__(256) smooth_tile_kernel(const float* __restric
   // z pass over all (a, b) of the halo'd tile
   for (int e = tid; e < SX * SY * TZ; e += blockDim.x) {
     const int c = e % TZ, b = (e / TZ) % SY, a = e / (TZ * SY);
-    float acc = 0.f;
-    if (!ADJOINT) {
-      for (int tt = -t.h; tt <= t.h; ++tt) acc += t.w[tt + t.h] * s_in[a][b][c + HALO + tt];
-    } else {
-      const int gz = z0 + c;
-      acc = adjoint1d(t, gz, Z, [&](int i) { return s_in[a][b][i - z0 + HALO]; });
-    }
-    s_z[a][b][c] = acc;
+    s_z[a][b][c] = pass1d<ADJOINT, H>(t, w, z0 + c, Z, [&](int i) { return s_in[a][b][i - z0 + HALO]; });
   }
   __syncthreads();
   for (int e = tid; e < SX * TY * TZ; e += blockDim.x) {
     const int c = e % TZ, b = (e / TZ) % TY, a = e / (TZ * TY);
-    float acc = 0.f;
-    if (!ADJOINT) {
-      for (int tt = -t.h; tt <= t.h; ++tt) acc += t.w[tt + t.h] * s_z[a][b + HALO + tt][c];
-    } else {
-      const int gy = y0 + b;
-      acc = adjoint1d(t, gy, Y, [&](int i) { return s_z[a][i - y0 + HALO][c]; });
-    }
-    s_y[a][b][c] = acc;
+    s_y[a][b][c] = pass1d<ADJOINT, H>(t, w, y0 + b, Y, [&](int i) { return s_z[a][i - y0 + HALO][c]; });
   }
   __syncthreads();
   for (int e = tid; e < TX * TY * TZ; e += blockDim.x) {
     const int c = e % TZ, b = (e / TZ) % TY, a = e / (TZ * TY);
     const int gx = x0 + a, gy = y0 + b, gz = z0 + c;
     if (gx >= X || gy >= Y || gz >= Z) continue;
-    float acc = 0.f;
-    if (!ADJOINT) {
-      for (int tt = -t.h; tt <= t.h; ++tt) acc += t.w[tt + t.h] * s_y[a + HALO + tt][b][c];
-    } else {
-      acc = adjoint1d(t, gx, X, [&](int i) { return s_y[i - x0 + HALO][b][c]; });
-    }
+    const float acc = pass1d<ADJOINT, H>(t, w, gx, X, [&](int i) { return s_y[i - x0 + HALO][b][c]; });
     const int64_t o = ((int64_t)gx * Y + gy) * Z + gz;
     if (ACCUM)
       out[o] += acc;
     else
       out[o] = acc;
   }
+}
+
+template <bool ADJOINT, bool ACCUM>
+static void launch_tile(const float* in, float* out, int X, int Y, int Z, const Taps& t, cudaStream_t st) {
+  dim3 grid((unsigned)((Z + TZ - 1) / TZ), (unsigned)((Y + TY - 1) / TY), (unsigned)((X + TX - 1) / TX));
+  if (t.h == 2)
+    smooth_tile_kernel<ADJOINT, ACCUM, 2><<<grid, 256, 0, st>>>(in, out, X, Y, Z, t);
+  else if (t.h == 1)
+    smooth_tile_kernel<ADJOINT, ACCUM, 1><<<grid, 256, 0, st>>>(in, out, X, Y, Z, t);
+  else
+    smooth_tile_kernel<ADJOINT, ACCUM, 0><<<grid, 256, 0, st>>>(in, out, X, Y, Z, t);
 }
 
 static unsigned pass_blocks(int64_t n) {
@@ -199,8 +213,7 @@ int vx_smooth3d(const float* in, float* out, float* tmp1, float* tmp2, int64_t X
   for (int i = 0; i < 9; ++i) t.w[i] = i < ksize ? taps_host[i] : 0.f;
   cudaStream_t st = as_stream(stream);
   if (t.h <= HALO) {
-    dim3 grid((unsigned)((Z + TZ - 1) / TZ), (unsigned)((Y + TY - 1) / TY), (unsigned)((X + TX - 1) / TX));
-    smooth_tile_kernel<false, false><<<grid, 256, 0, st>>>(in, out, (int)X, (int)Y, (int)Z, t);
+    launch_tile<false, false>(in, out, (int)X, (int)Y, (int)Z, t, st);
     return launch_status();
   }
   const unsigned b = pass_blocks(X * Y * Z);
@@ -224,11 +237,10 @@ int vx_smooth3d_adjoint(const float* grad_out, float* grad_in, float* tmp1, floa
   for (int i = 0; i < 9; ++i) t.w[i] = i < ksize ? taps_host[i] : 0.f;
   cudaStream_t st = as_stream(stream);
   if (t.h <= HALO) {
-    dim3 grid((unsigned)((Z + TZ - 1) / TZ), (unsigned)((Y + TY - 1) / TY), (unsigned)((X + TX - 1) / TX));
     if (accumulate)
-      smooth_tile_kernel<true, true><<<grid, 256, 0, st>>>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t);
+      launch_tile<true, true>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t, st);
     else
-      smooth_tile_kernel<true, false><<<grid, 256, 0, st>>>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t);
+      launch_tile<true, false>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t, st);
     return launch_status();
   }
   const unsigned b = pass_blocks(X * Y * Z);

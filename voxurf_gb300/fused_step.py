@@ -136,10 +136,11 @@ class GraphedFineStep:
             self.inp[i].copy_(t)
         S2 = self._part_a(inv_s)
         self.S2 = S2
-        cap = max(_round_up(S2, self.bucket), self.bucket)
+        kptr = 0 if self.bf16 else model.k0.grid.data_ptr()
+        cap = self._pick_capacity(S2, kptr)
         self._ensure_rows(cap)
         self.dyn_host[0] = inv_s
-        key = (cap, 0 if self.bf16 else model.k0.grid.data_ptr())
+        key = (cap, kptr)
         entry = self.graphs.get(key)
         if entry is None:
             entry = self._build(cap, key)
@@ -152,6 +153,16 @@ class GraphedFineStep:
             p.grad = g
         tr.optimizer.step(zero_grad=True)
         return entry["loss"], S2
+
+    def _pick_capacity(self, S2: int, kptr: int) -> int:
+        """Row capacity for S2 shaded rows: the smallest captured capacity in
+        [S2, 1.3 S2 + bucket] (S2 drifts by a few percent between steps, and a
+        capture costs tens of milliseconds), else S2 + 8% rounded up to the
+        bucket, so that the next steps reuse the new graph."""
+        fits = [c for (c, p) in self.graphs if p == kptr and S2 <= c <= 1.3 * S2 + self.bucket]
+        if fits:
+            return min(fits)
+        return max(_round_up(int(S2 * 1.08) + 1, self.bucket), self.bucket)
 
     def _build(self, cap, key):
         if not self.use_graphs:
