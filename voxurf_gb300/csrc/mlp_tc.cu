@@ -145,80 +145,123 @@ __device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_s, uint32_t b
   tc_commit(bar);
 }
 
-__global__ void __launch_bounds__(128, 1) mlp_tc_kernel(MlpTcParams P) {
+// Global -> shared bulk copy (async proxy) completing on an mbarrier.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 16-byte asynchronous copy with zero fill of the bytes beyond src_bytes.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Input tile rows [row0, row0+128) -> As chunks [0, K0/8) (zero rows past n).
+__device__ __forceinline__ void load_x_tile(const MlpTcParams& P, __nv_bfloat16* As, int64_t row0, int tid,
+                                            int nthreads) {
+  const int chunks = P.K0 / 8;
+  for (int i = tid; i < chunks * TC_M; i += nthreads) {
+    const int c = i / TC_M, r = i % TC_M;
+    const bool in = row0 + r < P.n_rows;
+    const __nv_bfloat16* src = P.X + (in ? (row0 + r) * P.ldx + 8 * c : 0);
+    cp_async16(As + ((size_t)c * TC_M + r) * 8, src, in ? 16u : 0u);
+  }
+  cp_async_commit();
+}
+
+constexpr int TC_THREADS = 256;  // 8 warps: warps w and w+4 share TMEM lanes 32(w%4).., split the columns
+
+__global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int K0 = P.K0;
   __nv_bfloat16* W0s = reinterpret_cast<__nv_bfloat16*>(smem);
   __nv_bfloat16* W1s = W0s + (size_t)K0 * TC_N;
   __nv_bfloat16* W2s = W1s + (size_t)TC_N * TC_N;
-  __nv_bfloat16* As = W2s + (size_t)TC_N * TC_N;  // [24][128][8] (the input tile uses [K0/8][128][8])
-  uint64_t* bar = reinterpret_cast<uint64_t*>(As + (size_t)TC_N * TC_M);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  __nv_bfloat16* As = W2s + (size_t)TC_N * TC_N;                  // [24][128][8]
+  float* bias_s = reinterpret_cast<float*>(As + (size_t)TC_N * TC_M);  // [3][192]
+  float* wh_s = bias_s + 3 * TC_N;                                  // [3][192]
+  uint64_t* bar_w = reinterpret_cast<uint64_t*>(wh_s + 3 * TC_N);
+  uint64_t* bar_mma = bar_w + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_mma + 1);
+  float* partial = reinterpret_cast<float*>(As + 16 * TC_M * 8);    // [128][3] in A chunks >= 16
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // weights -> shared memory (already packed), 16-byte copies
-  {
-    const uint4* src[3] = {reinterpret_cast<const uint4*>(P.W0p), reinterpret_cast<const uint4*>(P.W1p),
-                           reinterpret_cast<const uint4*>(P.W2p)};
-    uint4* dst[3] = {reinterpret_cast<uint4*>(W0s), reinterpret_cast<uint4*>(W1s), reinterpret_cast<uint4*>(W2s)};
-    const int n16[3] = {K0 * TC_N / 8, TC_N * TC_N / 8, TC_N * TC_N / 8};
-    for (int m = 0; m < 3; ++m)
-      for (int i = tid; i < n16[m]; i += blockDim.x) dst[m][i] = __ldg(src[m] + i);
-  }
+  const int quarter = warp & 3, half = warp >> 2;  // TMEM lanes 32*quarter.., columns [96*half, +96)
+  const int64_t n_tiles = (P.n_rows + TC_M - 1) / TC_M;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(TC_TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  if (tid == 0) mbar_init(bar, 1);
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  fence_async_smem();
+  if (tid == 0) {
+    mbar_init(bar_w, 1);
+    mbar_init(bar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // weights, biases and the output layer: bulk copies on the async proxy
+    const uint32_t w0b = (uint32_t)K0 * TC_N * 2, w1b = (uint32_t)TC_N * TC_N * 2, bb = TC_N * 4;
+    mbar_expect_tx(bar_w, w0b + 2 * w1b + 3 * bb + 3 * bb);
+    bulk_g2s(W0s, P.W0p, w0b, bar_w);
+    bulk_g2s(W1s, P.W1p, w1b, bar_w);
+    bulk_g2s(W2s, P.W2p, w1b, bar_w);
+    bulk_g2s(bias_s, P.b0, bb, bar_w);
+    bulk_g2s(bias_s + TC_N, P.b1, bb, bar_w);
+    bulk_g2s(bias_s + 2 * TC_N, P.b2, bb, bar_w);
+    bulk_g2s(wh_s, P.Wh, 3 * bb, bar_w);
+  }
+  if (blockIdx.x < n_tiles) load_x_tile(P, As, (int64_t)blockIdx.x * TC_M, tid, TC_THREADS);
+  bool ok = mbar_wait(bar_w, 0);
+  const float bh0 = __ldg(P.bh + 0), bh1 = __ldg(P.bh + 1), bh2 = __ldg(P.bh + 2);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tmem_warp = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's 32 lanes
+  const uint32_t tmem_row = tmem + ((uint32_t)(32 * quarter) << 16);
   const uint32_t a_s = smem_u32(As), w_s[3] = {smem_u32(W0s), smem_u32(W1s), smem_u32(W2s)};
-  const float* bias[3] = {P.b0, P.b1, P.b2};
   uint32_t phase = 0;
-  bool ok = true;
 
-  const int64_t n_tiles = (P.n_rows + TC_M - 1) / TC_M;
   for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
     const int64_t row0 = tile * TC_M;
-    // input tile -> As in core-matrix layout (rows beyond n_rows are zero)
-    const int chunks = K0 / 8;
-    for (int i = tid; i < chunks * TC_M; i += blockDim.x) {
-      const int c = i / TC_M, r = i % TC_M;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (row0 + r < P.n_rows)
-        v = __ldg(reinterpret_cast<const uint4*>(P.X + (row0 + r) * P.ldx) + c);
-      reinterpret_cast<uint4*>(As)[(size_t)c * TC_M + r] = v;
-    }
+    const int64_t row = row0 + 32 * quarter + lane;
+    // this tile's input rows (prefetched during the previous tile)
+    cp_async_wait_all();
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const int64_t row = row0 + 32 * warp + lane;
-    for (int layer = 0; layer < 3 && ok; ++layer) {
-      if (tid == 0) tc_layer(tmem, a_s, w_s[layer], layer == 0 ? K0 : TC_N, bar);
-      ok = mbar_wait(bar, phase);
+#pragma unroll 1
+    for (int layer = 0; layer < 3; ++layer) {
+      if (tid == 0) tc_layer(tmem, a_s, w_s[layer], layer == 0 ? K0 : TC_N, bar_mma);
+      ok = mbar_wait(bar_mma, phase);
       phase ^= 1u;
       tc_fence_after();
       if (!ok) break;
+      const float* b = bias_s + layer * TC_N;
       if (layer < 2) {
-        // +bias, ReLU, BF16 -> As (the next layer's A operand)
-        for (int j = 0; j < TC_N / 32; ++j) {
+        // +bias, ReLU, BF16 -> As (the next layer's A operand): this thread's
+        // row, columns [96*half, 96*half + 96)
+        uint4* dst = reinterpret_cast<uint4*>(As);
+#pragma unroll 1
+        for (int j = 0; j < 3; ++j) {
+          const int col0 = 96 * half + 32 * j;
           float v[32];
-          tc_ld32(tmem_warp + 32 * j, v);
-          uint4* dst = reinterpret_cast<uint4*>(As);
+          tc_ld32(tmem_row + col0, v);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             float h[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) h[e] = fmaxf(v[8 * q + e] + __ldg(bias[layer] + 32 * j + 8 * q + e), 0.f);
-            dst[(size_t)(4 * j + q) * TC_M + 32 * warp + lane] =
+            for (int e = 0; e < 8; ++e) h[e] = fmaxf(v[8 * q + e] + b[col0 + 8 * q + e], 0.f);
+            dst[(size_t)(col0 / 8 + q) * TC_M + 32 * quarter + lane] =
                 make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
           }
         }
@@ -227,25 +270,39 @@ __global__ void __launch_bounds__(128, 1) mlp_tc_kernel(MlpTcParams P) {
         __syncthreads();
         tc_fence_after();
       } else {
-        // last hidden layer: +bias, ReLU (rounded to BF16 like the GEMM path's
-        // output), then the FP32 output layer
+        // As is free (all MMAs of this tile are done): prefetch the next tile
+        const int64_t next = tile + gridDim.x;
+        if (next < n_tiles) load_x_tile(P, As, next * TC_M, tid, TC_THREADS);
+        // last hidden layer: +bias, ReLU, rounded to BF16 like the GEMM path,
+        // then this thread's share of the FP32 output layer
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        for (int j = 0; j < TC_N / 32; ++j) {
+#pragma unroll 1
+        for (int j = 0; j < 3; ++j) {
+          const int col0 = 96 * half + 32 * j;
           float v[32];
-          tc_ld32(tmem_warp + 32 * j, v);
+          tc_ld32(tmem_row + col0, v);
 #pragma unroll
           for (int e = 0; e < 32; ++e) {
-            const int col = 32 * j + e;
-            const float h = __bfloat162float(__float2bfloat16_rn(fmaxf(v[e] + __ldg(P.b2 + col), 0.f)));
-            a0 += h * __ldg(P.Wh + col);
-            a1 += h * __ldg(P.Wh + TC_N + col);
-            a2 += h * __ldg(P.Wh + 2 * TC_N + col);
+            const int col = col0 + e;
+            const float h = __bfloat162float(__float2bfloat16_rn(fmaxf(v[e] + b[col], 0.f)));
+            a0 += h * wh_s[col];
+            a1 += h * wh_s[TC_N + col];
+            a2 += h * wh_s[2 * TC_N + col];
           }
         }
-        if (row < P.n_rows) {
-          a0 += __ldg(P.bh + 0);
-          a1 += __ldg(P.bh + 1);
-          a2 += __ldg(P.bh + 2);
+        const int r = 32 * quarter + lane;
+        if (half == 1) {
+          partial[3 * r + 0] = a0;
+          partial[3 * r + 1] = a1;
+          partial[3 * r + 2] = a2;
+        }
+        tc_fence_before();
+        __syncthreads();  // partials written; TMEM free for the next tile
+        tc_fence_after();
+        if (half == 0 && row < P.n_rows) {
+          a0 += partial[3 * r + 0] + bh0;
+          a1 += partial[3 * r + 1] + bh1;
+          a2 += partial[3 * r + 2] + bh2;
           if (P.add) {
             a0 += P.add[3 * row + 0];
             a1 += P.add[3 * row + 1];
@@ -261,12 +318,10 @@ __global__ void __launch_bounds__(128, 1) mlp_tc_kernel(MlpTcParams P) {
             cp[2] = __float2bfloat16_rn(a2);
           }
         }
-        tc_fence_before();
-        __syncthreads();  // TMEM and As are reused by the next tile
-        tc_fence_after();
       }
     }
   }
+  cp_async_wait_all();
   if (!ok && tid == 0) set_device_error(P.err, VX_ERR_TIMEOUT);
   tc_fence_before();
   __syncthreads();
@@ -286,7 +341,7 @@ __global__ void mlp_tc_pack_kernel(const float* __restrict__ W, int N, int K, in
 }
 
 static size_t mlp_tc_smem_bytes(int K0) {
-  return (size_t)K0 * TC_N * 2 + 2 * (size_t)TC_N * TC_N * 2 + (size_t)TC_N * TC_M * 2 + 16;
+  return (size_t)K0 * TC_N * 2 + 2 * (size_t)TC_N * TC_N * 2 + (size_t)TC_N * TC_M * 2 + 6 * TC_N * 4 + 24;
 }
 
 }  // namespace vx
@@ -335,7 +390,7 @@ int vx_mlp_tc_forward(const vx_mlp_tc_args* A, void* stream) {
   if (e != cudaSuccess) return cuda_status(e);
   const int64_t tiles = (A->n_rows + TC_M - 1) / TC_M;
   const unsigned grid = (unsigned)(tiles < sm_count() ? tiles : sm_count());
-  mlp_tc_kernel<<<grid, 128, smem, as_stream(stream)>>>(P);
+  mlp_tc_kernel<<<grid, TC_THREADS, smem, as_stream(stream)>>>(P);
   return launch_status();
 }
 
