@@ -212,6 +212,7 @@ struct FeatLayout {
   int k_unit;  // index of displacement 1.0 in disp
   int pos_pe, view_pe, kpos_pe, kview_pe;
   int center_sdf, use_rgbnet_k0, k_center_sdf;
+  int planes;  // every displacement in (0, 2]: probes from shared planes
 };
 
 // Host side: checks a feature configuration and converts it.
@@ -219,9 +220,11 @@ inline int fill_feat_layout(const vx_fine_feature_cfg* c, FeatLayout& L) {
   L.K = (int)c->K;
   if (L.K < 1 || L.K > MAX_K) return VX_ERR_ARG;
   L.k_unit = -1;
+  L.planes = 1;
   for (int i = 0; i < L.K; ++i) {
     L.disp[i] = c->disp[i];
     if (c->disp[i] == 1.0f) L.k_unit = i;
+    if (!(c->disp[i] > 0.f && c->disp[i] <= 2.f)) L.planes = 0;
   }
   if (L.k_unit < 0) return VX_ERR_ARG;  // k_grad_feat = (1.0,) must be among the displacements
   if (c->k0_channels != 12) return VX_ERR_UNSUPPORTED;
@@ -245,6 +248,91 @@ inline int64_t x1_cols(const vx_fine_feature_cfg* c) {
 }
 inline int64_t x2_cols(const vx_fine_feature_cfg* c) {
   return 12 + (3 + 6 * c->k_posbase_pe) + (3 + 6 * c->k_viewbase_pe) + 3 + (c->k_center_sdf ? 1 : 0);
+}
+
+// ---- axis probes from shared planes -------------------------------------------
+// Every probe of a point along axis a moves only that coordinate, so it is a
+// linear interpolation between two planes perpendicular to a, each a
+// bilinear interpolation at the point's other two coordinates.  The planes
+// i0-2 .. i0+3 cover every probe at |d| <= 2: 6 planes x 4 voxels per axis
+// instead of 8 voxels per probe.  Voxels outside the grid are zero
+// (grid_sample padding 'zeros'); a probe at floor fl with fraction t reads
+// planes fl and fl+1, as its own trilinear lookup would.
+template <int A>
+__device__ __forceinline__ float plane_bilerp(const float* __restrict__ sdf, const GridGeom& g, int p,
+                                              const int i0[3], const float t[3]) {
+  constexpr int B = A == 0 ? 1 : 0, C = A == 2 ? 1 : 2;
+  if (p < 0 || p >= gsize(g, A)) return 0.f;
+  float acc = 0.f;
+#pragma unroll
+  for (int db = 0; db < 2; ++db)
+#pragma unroll
+    for (int dc = 0; dc < 2; ++dc) {
+      const int ib = i0[B] + db, ic = i0[C] + dc;
+      if (ib < 0 || ib >= gsize(g, B) || ic < 0 || ic >= gsize(g, C)) continue;
+      int idx[3];
+      idx[A] = p;
+      idx[B] = ib;
+      idx[C] = ic;
+      const float w = (db ? t[B] : 1.f - t[B]) * (dc ? t[C] : 1.f - t[C]);
+      acc += w * __ldg(sdf + ((int64_t)idx[0] * g.Y + idx[1]) * g.Z + idx[2]);
+    }
+  return acc;
+}
+
+// Value at coordinate q along the axis from planes P[0..5] = i0-2 .. i0+3.
+__device__ __forceinline__ float plane_lerp(const float P[6], int i0, float q) {
+  const float fl = floorf(q);
+  const float tq = q - fl;
+  const int p = (int)fl - (i0 - 2);  // in [0, 4] for |q - coordinate| <= 2
+  float lo = P[0], hi = P[1];
+#pragma unroll
+  for (int k = 1; k < 5; ++k)
+    if (p == k) {
+      lo = P[k];
+      hi = P[k + 1];
+    }
+  return (1.f - tq) * lo + tq * hi;
+}
+
+// Centre value and the hierarchical probes of hier_features (same outputs:
+// feat[6K] dir-major z-,z+,y-,y+,x-,x+; graw[3K] pair-major z,y,x) from
+// shared planes; requires every displacement <= 2.
+template <int KK>
+__device__ __forceinline__ void hier_features_planes(const float* __restrict__ sdf, const GridGeom& g, float vs,
+                                                     const float ind[3], const float* disp, float* s,
+                                                     float feat[6 * KK], float graw[3 * KK]) {
+  int i0[3];
+  float t[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float fl = floorf(ind[a]);
+    i0[a] = (int)fl;
+    t[a] = ind[a] - fl;
+  }
+  float P[3][6];
+#pragma unroll
+  for (int p = 0; p < 6; ++p) {
+    P[0][p] = plane_bilerp<0>(sdf, g, i0[0] - 2 + p, i0, t);
+    P[1][p] = plane_bilerp<1>(sdf, g, i0[1] - 2 + p, i0, t);
+    P[2][p] = plane_bilerp<2>(sdf, g, i0[2] - 2 + p, i0, t);
+  }
+  *s = (1.f - t[0]) * P[0][2] + t[0] * P[0][3];
+#pragma unroll
+  for (int kk = 0; kk < KK; ++kk) {
+#pragma unroll
+    for (int pair = 0; pair < 3; ++pair) {
+      const int axis = 2 - pair;  // zyx
+      const float hi = (float)(gsize(g, axis) - 1);
+      const float qm = fminf(fmaxf(ind[axis] - disp[kk], 0.f), hi);
+      const float qp = fminf(fmaxf(ind[axis] + disp[kk], 0.f), hi);
+      const float fm = plane_lerp(P[axis], i0[axis], qm);
+      const float fp = plane_lerp(P[axis], i0[axis], qp);
+      feat[(2 * pair + 0) * KK + kk] = fm;
+      feat[(2 * pair + 1) * KK + kk] = fp;
+      graw[pair * KK + kk] = ((fp - fm) * (1.f / (qp - qm))) / vs;
+    }
+  }
 }
 
 // hier_features with the number of displacements known at compile time, so
@@ -279,12 +367,17 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
                                                   const float p[3], const float v[3], T* x1, T* x2, float g1[3]) {
   float ind[3];
   to_index(g, p, ind);
-  const float s = sample1(sdf, g, ind[0], ind[1], ind[2]);
+  float s;
   float feat[6 * KK], graw[3 * KK];
   float disp[KK];
 #pragma unroll
   for (int kk = 0; kk < KK; ++kk) disp[kk] = L.disp[kk];
-  hier_features_k<KK>(sdf, g, vs, ind, disp, feat, graw);
+  if (L.planes) {
+    hier_features_planes<KK>(sdf, g, vs, ind, disp, &s, feat, graw);
+  } else {
+    s = sample1(sdf, g, ind[0], ind[1], ind[2]);
+    hier_features_k<KK>(sdf, g, vs, ind, disp, feat, graw);
+  }
   // gradient for k_rgbnet: unnormalised, displacement 1.0, xyz order
   float gu[3] = {0.f, 0.f, 0.f};
 #pragma unroll
