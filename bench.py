@@ -68,6 +68,10 @@ def parse():
     p.add_argument("--render-requests", type=int, default=120)
     p.add_argument("--render-only", action="store_true", help="only the render-server measurement (profiling)")
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
+    p.add_argument("--render-grid", type=int, default=256, help="scene grid size (256 is the benchmark)")
+    p.add_argument("--render-tick", type=int, default=1 << 20, help="rays packed per tick")
+    p.add_argument("--render-grid", type=int, default=256, help="scene grid size (256 is the benchmark)")
+    p.add_argument("--render-tick", type=int, default=1 << 20, help="rays packed per tick")
     p.add_argument("--grid", type=int, default=256, help="grid resolution (256 is the benchmark; smaller sizes "
                                                          "serve profiler captures)")
     args = p.parse_args()
@@ -374,7 +378,6 @@ def run_long_rays(args, dev):
 
 RENDER_SCENES = 4
 RENDER_RATE = 50.0          # requests per second (Poisson)
-RENDER_TICK_RAYS = 1 << 20  # rays packed per tick
 MLP_FLOPS_PER_ROW = 347136  # rgbnet + k_rgbnet forward FLOPs per shaded sample (70/60 -> 192 x3 -> 3)
 
 
@@ -390,14 +393,15 @@ def run_render(args, dev):
 
     from voxurf_gb300 import configs, serve
 
-    models = configs.build_serve_models(R, "bf16", device=dev, n=RENDER_SCENES, mask_voxels=MASK_VOXELS)
+    RR = args.render_grid
+    models = configs.build_serve_models(RR, "bf16", device=dev, n=RENDER_SCENES, mask_voxels=0.05 / (2.0 / RR))
     s_val = configs.trained_s_val()
     scenes = [serve.ResidentScene(m, s_val=s_val, precision="bf16") for m in models]
     for m in models:
         m.s_val = torch.ones(1) * s_val
         m.precision = "fp32"   # the plain render path
         m._k0_shadow = None
-    server = serve.RenderServer(scenes, tick_rays=RENDER_TICK_RAYS, arena_pixels=32 << 20)
+    server = serve.RenderServer(scenes, tick_rays=args.render_tick, arena_pixels=32 << 20)
     torch.cuda.synchronize()
     serve.run_stream(server, serve.request_stream(6, float("inf"), RENDER_SCENES, seed=99))  # warm-up
     n = args.render_requests
@@ -439,9 +443,9 @@ def run_render(args, dev):
     torch.cuda.empty_cache()
     return {
         "metric": "render Mpix/s and p50/p99 latency (4 resident 256^3 scenes)",
-        "workload": "4 scenes sdf 256^3 f32 + k0 256^3x12 bf16 + MLP bf16, mask |SDF|<0.05, s_val at step 20000, "
-                    "poses on r=3 sphere, res uniform {160x120,400x300,800x600,1600x1200}, "
-                    f"tick {RENDER_TICK_RAYS} rays",
+        "workload": f"4 scenes sdf {RR}^3 f32 + k0 {RR}^3x12 bf16 + MLP bf16 (fused tcgen05), mask |SDF|<0.05, "
+                    "s_val at step 20000, poses on r=3 sphere, res uniform {160x120,400x300,800x600,1600x1200}, "
+                    f"tick {args.render_tick} rays",
         "poisson_50_req_s": poisson,
         "saturated": saturated,
         "plain_fp32_per_request": plain,

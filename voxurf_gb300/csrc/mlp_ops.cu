@@ -50,6 +50,78 @@ __global__ void relu_bwd_colsum_kernel(const T* __restrict__ dh, const T* __rest
   }
 }
 
+// Vectorised form for rows of 16-byte chunks (N % (16/sizeof(T)) == 0, 16-byte
+// aligned rows): thread (rl, g) of a block of G*RL threads owns chunk g of the
+// rows r0 + rl, r0 + rl + RL, ...; the RL partial sums of a column are added
+// in shared memory, then one atomic per column and block.
+__device__ __forceinline__ void unpack16(const uint4& u, const float*, float x[4]) {
+  x[0] = __uint_as_float(u.x);
+  x[1] = __uint_as_float(u.y);
+  x[2] = __uint_as_float(u.z);
+  x[3] = __uint_as_float(u.w);
+}
+__device__ __forceinline__ void unpack16(const uint4& u, const __nv_bfloat16*, float x[8]) {
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __bfloat1622float2(h[i]);
+    x[2 * i] = f.x;
+    x[2 * i + 1] = f.y;
+  }
+}
+__device__ __forceinline__ uint4 pack16(const float x[4], const float*) {
+  return make_uint4(__float_as_uint(x[0]), __float_as_uint(x[1]), __float_as_uint(x[2]), __float_as_uint(x[3]));
+}
+__device__ __forceinline__ uint4 pack16(const float x[8], const __nv_bfloat16*) {
+  uint32_t w[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x[2 * i], x[2 * i + 1]);
+    w[i] = *reinterpret_cast<const uint32_t*>(&h);
+  }
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+constexpr int VEC_ROWS_PER_BLOCK = 256;
+
+template <typename T, bool RELU>
+__global__ void relu_bwd_colsum_vec_kernel(const T* __restrict__ dh, const T* __restrict__ h, int64_t M, int N,
+                                           T* __restrict__ dz, float* __restrict__ colsum) {
+  constexpr int PER = 16 / (int)sizeof(T);
+  extern __shared__ float part[];  // [RL][N]
+  const int G = N / PER, RL = blockDim.x / G;
+  const int tid = threadIdx.x, rl = tid / G, g = tid % G;
+  float s[PER];
+#pragma unroll
+  for (int e = 0; e < PER; ++e) s[e] = 0.f;
+  if (rl < RL) {
+    const int64_t r0 = (int64_t)blockIdx.x * VEC_ROWS_PER_BLOCK;
+    const int64_t r1 = min(r0 + VEC_ROWS_PER_BLOCK, M);
+    for (int64_t r = r0 + rl; r < r1; r += RL) {
+      const int64_t i = r * (N / PER) + g;
+      float v[PER];
+      unpack16(__ldg(reinterpret_cast<const uint4*>(dh) + i), dh, v);
+      if (RELU) {
+        float hv[PER];
+        unpack16(__ldg(reinterpret_cast<const uint4*>(h) + i), h, hv);
+#pragma unroll
+        for (int e = 0; e < PER; ++e) v[e] = hv[e] > 0.f ? v[e] : 0.f;
+        reinterpret_cast<uint4*>(dz)[i] = pack16(v, dz);
+      }
+#pragma unroll
+      for (int e = 0; e < PER; ++e) s[e] += v[e];
+    }
+#pragma unroll
+    for (int e = 0; e < PER; ++e) part[rl * N + g * PER + e] = s[e];
+  }
+  __syncthreads();
+  for (int c = tid; c < N; c += blockDim.x) {
+    float acc = 0.f;
+    for (int q = 0; q < RL; ++q) acc += part[q * N + c];
+    atomicAdd(colsum + c, acc);
+  }
+}
+
 }  // namespace vx
 
 using namespace vx;
@@ -63,6 +135,38 @@ int vx_relu_bwd_colsum(const void* dh, const void* h, int64_t M, int64_t N, int 
   if (M < 0 || N <= 0 || N > INT32_MAX || !colsum || (dtype != 0 && dtype != 1)) return VX_ERR_ARG;
   if (M == 0) return VX_OK;
   if (!dh || (h && !dz)) return VX_ERR_ARG;
+  {
+    const int per = dtype == 0 ? 4 : 8;
+    const uintptr_t al = reinterpret_cast<uintptr_t>(dh) | reinterpret_cast<uintptr_t>(h) |
+                         reinterpret_cast<uintptr_t>(dz);
+    const int G = (int)(N / per);
+    if (N % per == 0 && (al & 15) == 0 && G <= 256) {
+      const int RL = 256 / G;  // row lanes per block
+      const int threads = RL * G;
+      const size_t shm = (size_t)RL * N * sizeof(float);
+      if (shm <= 48 * 1024) {
+        const unsigned vb = (unsigned)((M + VEC_ROWS_PER_BLOCK - 1) / VEC_ROWS_PER_BLOCK);
+        cudaStream_t vst = as_stream(stream);
+        using B = __nv_bfloat16;
+        if (dtype == 0) {
+          if (h)
+            relu_bwd_colsum_vec_kernel<float, true><<<vb, threads, shm, vst>>>((const float*)dh, (const float*)h, M,
+                                                                                (int)N, (float*)dz, colsum);
+          else
+            relu_bwd_colsum_vec_kernel<float, false><<<vb, threads, shm, vst>>>((const float*)dh, nullptr, M, (int)N,
+                                                                                 nullptr, colsum);
+        } else {
+          if (h)
+            relu_bwd_colsum_vec_kernel<B, true><<<vb, threads, shm, vst>>>((const B*)dh, (const B*)h, M, (int)N,
+                                                                            (B*)dz, colsum);
+          else
+            relu_bwd_colsum_vec_kernel<B, false><<<vb, threads, shm, vst>>>((const B*)dh, nullptr, M, (int)N,
+                                                                             nullptr, colsum);
+        }
+        return launch_status();
+      }
+    }
+  }
   const unsigned blocks = (unsigned)((M + ROWS_PER_BLOCK - 1) / ROWS_PER_BLOCK);
   const int threads = N >= 256 ? 256 : (int)((N + 31) / 32) * 32;
   cudaStream_t st = as_stream(stream);
