@@ -70,8 +70,6 @@ def parse():
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
     p.add_argument("--render-grid", type=int, default=256, help="scene grid size (256 is the benchmark)")
     p.add_argument("--render-tick", type=int, default=1 << 20, help="rays packed per tick")
-    p.add_argument("--render-grid", type=int, default=256, help="scene grid size (256 is the benchmark)")
-    p.add_argument("--render-tick", type=int, default=1 << 20, help="rays packed per tick")
     p.add_argument("--grid", type=int, default=256, help="grid resolution (256 is the benchmark; smaller sizes "
                                                          "serve profiler captures)")
     args = p.parse_args()
