@@ -181,6 +181,14 @@ int vx_adam_step_multi(int n_tensors, float* const* params, float* const* grads,
 int vx_relu_bwd_colsum(const void* dh, const void* h, int64_t M, int64_t N, int dtype, void* dz, float* colsum,
                        void* stream);
 
+/* Backward of a colour MLP's 3-output layer (out = W h + b over [M,N] rows
+ * h of the last ReLU layer) fused with that ReLU's backward: dW [3,N] +=
+ * dout^T h, db [3] += column sums of dout, dz = (h > 0) * (dout W) [M,N]
+ * and db_prev [N] += column sums of dz.  dout FP32 [M,3]; h, dz in dtype
+ * (0 FP32, 1 BF16), N a multiple of 16 bytes / element size, <= 256. */
+int vx_mlp_head_backward(const float* dout, const void* h, const float* W, int64_t M, int64_t N, int dtype, void* dz,
+                         float* dW, float* db, float* db_prev, void* stream);
+
 /* Fused dense grid sweep: DenseGrid.total_variation_add_grad(w, w, w, dense)
  * (lib/grid.py:67-78; voxurf_fine.py:403-409; total_variation_kernel.cu:14-36)
  * followed by the utils.Adam update and the gradient reset, in one pass.

@@ -122,11 +122,118 @@ __global__ void relu_bwd_colsum_vec_kernel(const T* __restrict__ dh, const T* __
   }
 }
 
+// Backward of the 3-output layer of a colour MLP fused with the ReLU backward
+// of the hidden layer feeding it (out = W h + b, h = relu(.)):
+//   dW[j][c] += sum_rows g_j h_c,  db[j] += sum_rows g_j,
+//   dz_c = (h_c > 0) * sum_j g_j W[j][c],  db_prev[c] += sum_rows dz_c.
+// g = dout [M,3] FP32; h, dz [M,N] (T); W [3,N] FP32.  Replaces three GEMMs
+// with a 3-wide dimension (which map to slow unaligned kernels), a ReLU
+// backward and a bias reduction.  Rows in 16-byte chunks as the kernel above.
+constexpr int HEAD_MAX_N = 256;
+
+template <typename T>
+__global__ void head_backward_kernel(const float* __restrict__ dout, const T* __restrict__ h,
+                                     const float* __restrict__ W, int64_t M, int N, T* __restrict__ dz,
+                                     float* __restrict__ dW, float* __restrict__ db, float* __restrict__ db_prev) {
+  constexpr int PER = 16 / (int)sizeof(T);
+  extern __shared__ float sh[];  // W [3][N] | partials [RL][4][N] | db partials [RL][3]
+  const int G = N / PER, RL = blockDim.x / G;
+  const int tid = threadIdx.x, rl = tid / G, g = tid % G;
+  float* Ws = sh;
+  float* part = sh + 3 * N;
+  float* dbp = part + (size_t)RL * 4 * N;
+  for (int i = tid; i < 3 * N; i += blockDim.x) Ws[i] = W[i];
+  __syncthreads();
+  float w[3][PER], aw[3][PER], ab[PER], a3[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int e = 0; e < PER; ++e) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      w[j][e] = Ws[j * N + g * PER + e];
+      aw[j][e] = 0.f;
+    }
+    ab[e] = 0.f;
+  }
+  if (rl < RL) {
+    const int64_t r0 = (int64_t)blockIdx.x * VEC_ROWS_PER_BLOCK;
+    const int64_t r1 = min(r0 + VEC_ROWS_PER_BLOCK, M);
+    for (int64_t r = r0 + rl; r < r1; r += RL) {
+      const float g0 = dout[3 * r], g1 = dout[3 * r + 1], g2 = dout[3 * r + 2];
+      const int64_t i = r * (N / PER) + g;
+      float hv[PER], d[PER];
+      unpack16(__ldg(reinterpret_cast<const uint4*>(h) + i), h, hv);
+#pragma unroll
+      for (int e = 0; e < PER; ++e) {
+        aw[0][e] += g0 * hv[e];
+        aw[1][e] += g1 * hv[e];
+        aw[2][e] += g2 * hv[e];
+        const float dh = g0 * w[0][e] + g1 * w[1][e] + g2 * w[2][e];
+        d[e] = hv[e] > 0.f ? dh : 0.f;
+        ab[e] += d[e];
+      }
+      reinterpret_cast<uint4*>(dz)[i] = pack16(d, dz);
+      if (g == 0) {
+        a3[0] += g0;
+        a3[1] += g1;
+        a3[2] += g2;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+      const int c = g * PER + e;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) part[((size_t)rl * 4 + j) * N + c] = aw[j][e];
+      part[((size_t)rl * 4 + 3) * N + c] = ab[e];
+    }
+    if (g == 0) {
+      dbp[3 * rl + 0] = a3[0];
+      dbp[3 * rl + 1] = a3[1];
+      dbp[3 * rl + 2] = a3[2];
+    }
+  }
+  __syncthreads();
+  for (int k = tid; k < 4 * N; k += blockDim.x) {
+    const int j = k / N, c = k % N;
+    float acc = 0.f;
+    for (int q = 0; q < RL; ++q) acc += part[((size_t)q * 4 + j) * N + c];
+    if (j < 3)
+      atomicAdd(dW + j * N + c, acc);
+    else
+      atomicAdd(db_prev + c, acc);
+  }
+  if (tid < 3) {
+    float acc = 0.f;
+    for (int q = 0; q < RL; ++q) acc += dbp[3 * q + tid];
+    atomicAdd(db + tid, acc);
+  }
+}
+
 }  // namespace vx
 
 using namespace vx;
 
 extern "C" {
+
+int vx_mlp_head_backward(const float* dout, const void* h, const float* W, int64_t M, int64_t N, int dtype, void* dz,
+                         float* dW, float* db, float* db_prev, void* stream) {
+  if (M < 0 || N <= 0 || N > HEAD_MAX_N || (dtype != 0 && dtype != 1)) return VX_ERR_ARG;
+  if (!dW || !db || !db_prev || !W) return VX_ERR_ARG;
+  if (M == 0) return VX_OK;
+  if (!dout || !h || !dz) return VX_ERR_ARG;
+  const int per = dtype == 0 ? 4 : 8;
+  if (N % per || ((reinterpret_cast<uintptr_t>(h) | reinterpret_cast<uintptr_t>(dz)) & 15)) return VX_ERR_UNSUPPORTED;
+  const int G = (int)(N / per), RL = 256 / G, threads = RL * G;
+  const size_t shm = ((size_t)3 * N + (size_t)RL * 4 * N + 3 * RL) * sizeof(float);
+  const unsigned blocks = (unsigned)((M + VEC_ROWS_PER_BLOCK - 1) / VEC_ROWS_PER_BLOCK);
+  cudaStream_t st = as_stream(stream);
+  if (dtype == 0)
+    head_backward_kernel<float><<<blocks, threads, shm, st>>>(dout, (const float*)h, W, M, (int)N, (float*)dz, dW, db,
+                                                              db_prev);
+  else
+    head_backward_kernel<__nv_bfloat16><<<blocks, threads, shm, st>>>(
+        dout, (const __nv_bfloat16*)h, W, M, (int)N, (__nv_bfloat16*)dz, dW, db, db_prev);
+  return launch_status();
+}
 
 // dtype: 0 float32, 1 bfloat16 (dh, h, dz).  h == NULL: no ReLU (dz unused),
 // only the column sums.  colsum [N] is accumulated (callers zero it).

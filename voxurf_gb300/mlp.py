@@ -25,15 +25,34 @@ def _colsum(dh: torch.Tensor, h: torch.Tensor | None, dz: torch.Tensor | None) -
     return out
 
 
+def _head_layer(Ws, hs_last) -> bool:
+    """The last layer is a colour head (3 outputs from a ReLU layer of at
+    most 256 columns in 16-byte row chunks) that the fused head kernels take."""
+    W = Ws[-1]
+    N = W.shape[1]
+    per = 8 if hs_last.dtype == torch.bfloat16 else 4
+    return (len(Ws) >= 2 and W.shape[0] == 3 and N <= 256 and N % per == 0 and hs_last.is_contiguous()
+            and hs_last.data_ptr() % 16 == 0)
+
+
 def mlp_forward(x: torch.Tensor, Ws, bs) -> list[torch.Tensor]:
     """Linear/ReLU stack on rows x (weights already in x's dtype): returns
-    the activations [x, h1, ..., logits]."""
+    the activations [x, h1, ..., logits].  A 3-output last layer runs in
+    vx_mlp_head (FP32 accumulation and FP32 logits) instead of a GEMM with a
+    3-wide dimension."""
     n = len(Ws)
     hs = [x]
     h = x
     for i in range(n):
         if i < n - 1:
             h = torch._addmm_activation(bs[i], h, Ws[i].t())
+        elif _head_layer(Ws, h):
+            M, N = h.shape
+            out = torch.empty((M, 3), dtype=torch.float32, device=h.device)
+            W, b = Ws[i].float().contiguous(), bs[i].float().contiguous()
+            call("vx_mlp_head", ptr(h), M, N, N, int(h.dtype == torch.bfloat16), ptr(W), ptr(b), None, ptr(out),
+                 None, 0, 0, stream_ptr(h.device))
+            h = out
         else:
             h = torch.addmm(bs[i], h, Ws[i].t())
         hs.append(h)
@@ -43,13 +62,31 @@ def mlp_forward(x: torch.Tensor, Ws, bs) -> list[torch.Tensor]:
 def mlp_backward(dy: torch.Tensor, hs, Ws, need_dx: bool):
     """Gradients of mlp_forward: (dx or None, [dW1, db1, ..., dWn, dbn]) with
     FP32 weight gradients; ReLU backward and the bias gradient are one pass
-    (vx_relu_bwd_colsum)."""
+    (vx_relu_bwd_colsum); a 3-output head's weight and bias gradients, its
+    input gradient and the ReLU backward below it are one pass
+    (vx_mlp_head_backward)."""
     n = len(Ws)
-    dz = dy.to(hs[0].dtype).contiguous()
     grads = [None] * (2 * n)
-    db = _colsum(dz, None, None)
     dx = None
-    for i in reversed(range(n)):
+    top = n
+    if _head_layer(Ws, hs[n - 1]):
+        h = hs[n - 1]
+        M, N = h.shape
+        dev = h.device
+        dW = torch.zeros((3, N), dtype=torch.float32, device=dev)
+        dbh = torch.zeros(3, dtype=torch.float32, device=dev)
+        db = torch.zeros(N, dtype=torch.float32, device=dev)
+        dz = torch.empty_like(h)
+        W = Ws[n - 1].float().contiguous()
+        call("vx_mlp_head_backward", ptr(dy.float().contiguous()), ptr(h), ptr(W), M, N,
+             int(h.dtype == torch.bfloat16), ptr(dz), ptr(dW), ptr(dbh), ptr(db), stream_ptr(dev))
+        grads[2 * (n - 1)] = dW
+        grads[2 * (n - 1) + 1] = dbh
+        top = n - 1
+    else:
+        dz = dy.to(hs[0].dtype).contiguous()
+        db = _colsum(dz, None, None)
+    for i in reversed(range(top)):
         grads[2 * i] = (dz.t() @ hs[i]).float()
         grads[2 * i + 1] = db
         if i > 0:
