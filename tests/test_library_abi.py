@@ -85,3 +85,20 @@ def test_struct_sizes_match_c_layout():
         assert int(got[cname]) == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
+
+
+def test_every_called_entry_point_has_a_signature():
+    """ctypes would pass undeclared arguments as 32-bit ints (truncating
+    pointers): every vx_* name the package or bench.py uses is declared."""
+    import glob
+    import re
+
+    from voxurf_gb300 import _abi, _native
+
+    lib = _native.load()
+    _abi._declare()
+    names = set()
+    for f in glob.glob(os.path.join(ROOT, "voxurf_gb300", "*.py")) + [os.path.join(ROOT, "bench.py")]:
+        names |= set(re.findall(r'["\'](vx_[a-z0-9_]+)["\']', open(f).read()))
+    undeclared = [n for n in sorted(names) if hasattr(lib, n) and getattr(lib, n).argtypes is None]
+    assert not undeclared, undeclared

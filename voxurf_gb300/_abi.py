@@ -163,7 +163,6 @@ _SERVE_SIGNATURES = {
     "vx_mask_occupancy": [P, I64, I64, I64, I32, P, P],
     "vx_serve_features": ["scenes", I32, C.POINTER(FineFeatureCfg), P, P, P, P, I64, P, P, P, I64, I64, I64, P, P,
                           I32, P],
-    "vx_mlp_head": [P, I64, I64, I64, I32, P, P, P, P, P, I64, I32, P],
     "vx_serve_composite": ["scenes", I32, P, I64, I64, P, P, P, P, P, P, P, P, P],
 }
 

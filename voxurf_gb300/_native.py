@@ -61,6 +61,7 @@ _SIGNATURES = {
     "vx_relu_bwd_colsum": [c_ptr, c_ptr, c_i64, c_i64, c_int, c_ptr, c_ptr, c_ptr],
     "vx_mlp_tc_pack": [c_ptr, c_i64, c_i64, c_i64, c_ptr, c_ptr],
     "vx_mlp_head_backward": [c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr],
+    "vx_mlp_head": [c_ptr, c_i64, c_i64, c_i64, c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_int, c_ptr],
     "vx_adam_step_multi": [c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_f64, c_f64, c_f64, c_ptr],
     "vx_grid_tv_adam_step": [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_i64, c_i64, c_int,
                              c_int, c_f32, c_int, c_f64, c_f64, c_f64, c_f64, c_i64, c_int, c_ptr],
@@ -120,8 +121,16 @@ def check(status: int, what: str) -> None:
 
 
 def call(name: str, *args) -> None:
-    """Calls entry point `name` and raises on a non-zero status."""
+    """Calls entry point `name` and raises on a non-zero status.  An entry
+    point without declared argument types is never called (ctypes would pass
+    Python ints as 32-bit C ints and truncate pointers)."""
     fn = getattr(load(), name)
+    if fn.argtypes is None:
+        from . import _abi  # declares the struct-based entry points
+
+        _abi._declare()
+        if fn.argtypes is None:
+            raise VxError(f"{name}: entry point has no declared signature")
     check(fn(*args), name)
 
 

@@ -78,8 +78,9 @@ def mlp_backward(dy: torch.Tensor, hs, Ws, need_dx: bool):
         db = torch.zeros(N, dtype=torch.float32, device=dev)
         dz = torch.empty_like(h)
         W = Ws[n - 1].float().contiguous()
-        call("vx_mlp_head_backward", ptr(dy.float().contiguous()), ptr(h), ptr(W), M, N,
-             int(h.dtype == torch.bfloat16), ptr(dz), ptr(dW), ptr(dbh), ptr(db), stream_ptr(dev))
+        dout = dy.float().contiguous()  # kept alive until the kernel is enqueued
+        call("vx_mlp_head_backward", ptr(dout), ptr(h), ptr(W), M, N, int(h.dtype == torch.bfloat16), ptr(dz),
+             ptr(dW), ptr(dbh), ptr(db), stream_ptr(dev))
         grads[2 * (n - 1)] = dW
         grads[2 * (n - 1) + 1] = dbh
         top = n - 1

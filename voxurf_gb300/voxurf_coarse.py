@@ -180,7 +180,8 @@ class _CoarseComposite(torch.autograd.Function):
         d_w2 = torch.empty(fr.S2, dtype=torch.float32, device=dev)
         a = _abi.CoarseCompositeBwdArgs()
         a.n_rays, a.s2_off, a.w2, a.logit, a.rgb_raw = fr.n_rays, ptr(fr.s2_off), ptr(w2), ptr(logit), ptr(raw)
-        a.g_rgb, a.bg = ptr(g_rgb.contiguous()), ctx.bg
+        g_rgb = g_rgb.contiguous()
+        a.g_rgb, a.bg = ptr(g_rgb), ctx.bg
         a.d_logit, a.d_w2 = ptr(d_logit), ptr(d_w2)
         _abi.call_struct("vx_coarse_composite_backward", a, stream_ptr())
         return d_w2, d_logit, None, None
