@@ -215,6 +215,19 @@ struct FeatLayout {
   int planes;  // every displacement in (0, 2]: probes from shared planes
 };
 
+// Rows of a block staged in shared memory ([rows][ld] elements, written by
+// one thread each) copied to global memory as one contiguous range of
+// 16-byte chunks (coalesced; one thread per row writing 2-byte values would
+// touch a different cache line per thread and per column).  Requires
+// ld * sizeof(T) % 16 == 0 and a 16-byte aligned destination.
+template <typename T>
+__device__ __forceinline__ void copy_rows_out(const T* stage, T* dst, int n_rows, int64_t ld) {
+  const int64_t n16 = (int64_t)n_rows * ld * (int64_t)sizeof(T) / 16;
+  const uint4* s = reinterpret_cast<const uint4*>(stage);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int64_t i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+}
+
 // Host side: checks a feature configuration and converts it.
 inline int fill_feat_layout(const vx_fine_feature_cfg* c, FeatLayout& L) {
   L.K = (int)c->K;

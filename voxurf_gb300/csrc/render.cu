@@ -215,23 +215,39 @@ struct FeatParams {
   const int64_t* n_rows_dev;  // optional device row count (rows beyond it are skipped)
 };
 
-template <typename T, int KK>
+// STAGE: the block's rows are assembled in shared memory and written out as
+// contiguous 16-byte chunks (row strides of 16-byte multiples).
+template <typename T, int KK, bool STAGE>
 __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
-  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= P.n_rows || (P.n_rows_dev && row >= *P.n_rows_dev)) return;
-  const int r = P.ray2[row];
-  const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
-  const float v[3] = {__ldg(P.viewdirs + 3 * r), __ldg(P.viewdirs + 3 * r + 1), __ldg(P.viewdirs + 3 * r + 2)};
-  T* x1 = reinterpret_cast<T*>(P.X1) + row * P.ld1;
-  T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
-  float g1[3];
-  fine_feature_rows<T, KK>(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
-  for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
-  for (int c = P.cols2; c < P.ld2; ++c) put(x2, c, 0.f);
-  if (P.normal_out) {
-    P.normal_out[3 * row + 0] = g1[0];
-    P.normal_out[3 * row + 1] = g1[1];
-    P.normal_out[3 * row + 2] = g1[2];
+  extern __shared__ __align__(16) unsigned char feat_stage[];
+  const int64_t row0 = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t row = row0 + threadIdx.x;
+  int64_t n = P.n_rows;
+  if (P.n_rows_dev) n = min(n, *P.n_rows_dev);
+  const bool valid = row < n;
+  T* s1 = reinterpret_cast<T*>(feat_stage);
+  T* s2 = s1 + (int64_t)blockDim.x * P.ld1;
+  if (valid) {
+    const int r = P.ray2[row];
+    const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
+    const float v[3] = {__ldg(P.viewdirs + 3 * r), __ldg(P.viewdirs + 3 * r + 1), __ldg(P.viewdirs + 3 * r + 2)};
+    T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * P.ld1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
+    T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * P.ld2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
+    float g1[3];
+    fine_feature_rows<T, KK>(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
+    for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
+    for (int c = P.cols2; c < P.ld2; ++c) put(x2, c, 0.f);
+    if (P.normal_out) {
+      P.normal_out[3 * row + 0] = g1[0];
+      P.normal_out[3 * row + 1] = g1[1];
+      P.normal_out[3 * row + 2] = g1[2];
+    }
+  }
+  if (STAGE) {
+    __syncthreads();
+    const int nv = (int)max((int64_t)0, min((int64_t)blockDim.x, n - row0));
+    copy_rows_out(s1, reinterpret_cast<T*>(P.X1) + row0 * P.ld1, nv, P.ld1);
+    copy_rows_out(s2, reinterpret_cast<T*>(P.X2) + row0 * P.ld2, nv, P.ld2);
   }
 }
 
@@ -1157,7 +1173,16 @@ int vx_fine_features(const vx_fine_features_args* A, void* stream) {
   P.normal_out = A->normal_out;
   const unsigned b = (unsigned)((A->n_rows + 127) / 128);
   cudaStream_t st = as_stream(stream);
-#define VX_FEAT_LAUNCH(T, KK) features_fine_kernel<T, KK><<<b, 128, 0, st>>>(P)
+  // staged rows: strides of 16-byte multiples, aligned bases, <= 48 KB of shared memory
+  const size_t esz = A->out_bf16 ? 2 : 4;
+  const size_t shm = 128 * (size_t)(A->ld1 + A->ld2) * esz;
+  const bool stage = (A->ld1 * esz) % 16 == 0 && (A->ld2 * esz) % 16 == 0 && shm <= 48 * 1024 &&
+                     ((reinterpret_cast<uintptr_t>(A->X1) | reinterpret_cast<uintptr_t>(A->X2)) & 15) == 0;
+#define VX_FEAT_LAUNCH(T, KK)                                           \
+  if (stage)                                                            \
+    features_fine_kernel<T, KK, true><<<b, 128, shm, st>>>(P);          \
+  else                                                                  \
+    features_fine_kernel<T, KK, false><<<b, 128, 0, st>>>(P)
 #define VX_FEAT_SWITCH(T)        \
   switch (P.L.K) {               \
     case 1: VX_FEAT_LAUNCH(T, 1); break; \

@@ -289,32 +289,46 @@ struct ServeFeatParams {
   void* X2;
 };
 
-template <typename T, int KK>
+// STAGE: rows assembled in shared memory, written out as contiguous 16-byte
+// chunks (the logit columns [cols2, cols2+3) are zero until the rgbnet
+// output layer fills them).
+template <typename T, int KK, bool STAGE>
 __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
+  extern __shared__ __align__(16) unsigned char feat_stage[];
   load_scenes(P.T, sh);
-  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= P.n_rows) return;
-  const int r = P.ray2[row];
-  const SceneK& S = sh[P.ray_scene[r]];  // validated by the march
-  const int j = (int)(row - P.s2_off[r]);
-  const int k = (int)P.rec[(int64_t)r * P.max_steps + j].x;
-  float o[3], d[3], v[3];
+  const int64_t row0 = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t row = row0 + threadIdx.x;
+  T* s1 = reinterpret_cast<T*>(feat_stage);
+  T* s2 = s1 + (int64_t)blockDim.x * P.ld1;
+  if (row < P.n_rows) {
+    const int r = P.ray2[row];
+    const SceneK& S = sh[P.ray_scene[r]];  // validated by the march
+    const int j = (int)(row - P.s2_off[r]);
+    const int k = (int)P.rec[(int64_t)r * P.max_steps + j].x;
+    float o[3], d[3], v[3];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    o[a] = __ldg(P.rays_o + 3 * r + a);
-    d[a] = __ldg(P.rays_d + 3 * r + a);
-    v[a] = __ldg(P.viewdirs + 3 * r + a);
+    for (int a = 0; a < 3; ++a) {
+      o[a] = __ldg(P.rays_o + 3 * r + a);
+      d[a] = __ldg(P.rays_d + 3 * r + a);
+      v[a] = __ldg(P.viewdirs + 3 * r + a);
+    }
+    const RayFrame f = ray_frame(o, d, S.g.mn, S.g.mx, S.near, S.stepdist);
+    float p[3];
+    sample_point(f, S.stepdist, k, p);
+    T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * P.ld1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
+    T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * P.ld2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
+    float g1[3];
+    fine_feature_rows<T, KK>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
+    for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
+    for (int c = STAGE ? P.cols2 : P.cols2 + 3; c < P.ld2; ++c) put(x2, c, 0.f);
   }
-  const RayFrame f = ray_frame(o, d, S.g.mn, S.g.mx, S.near, S.stepdist);
-  float p[3];
-  sample_point(f, S.stepdist, k, p);
-  T* x1 = reinterpret_cast<T*>(P.X1) + row * P.ld1;
-  T* x2 = reinterpret_cast<T*>(P.X2) + row * P.ld2;
-  float g1[3];
-  fine_feature_rows<T, KK>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
-  for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
-  for (int c = P.cols2 + 3; c < P.ld2; ++c) put(x2, c, 0.f);
+  if (STAGE) {
+    __syncthreads();
+    const int nv = (int)max((int64_t)0, min((int64_t)blockDim.x, P.n_rows - row0));
+    copy_rows_out(s1, reinterpret_cast<T*>(P.X1) + row0 * P.ld1, nv, P.ld1);
+    copy_rows_out(s2, reinterpret_cast<T*>(P.X2) + row0 * P.ld2, nv, P.ld2);
+  }
 }
 
 // ---- output layer ------------------------------------------------------------
@@ -610,7 +624,18 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
   P.X2 = X2;
   const unsigned b = (unsigned)((n_rows + 127) / 128);
   cudaStream_t st = as_stream(stream);
-#define VX_FEAT_LAUNCH(T, KK) serve_features_kernel<T, KK><<<b, 128, 0, st>>>(P)
+  // staged rows: strides of 16-byte multiples, aligned bases, static + dynamic
+  // shared memory within the default 48 KB
+  const size_t esz = out_bf16 ? 2 : 4;
+  const size_t shm = 128 * (size_t)(ld1 + ld2) * esz;
+  const bool stage = ((size_t)ld1 * esz) % 16 == 0 && ((size_t)ld2 * esz) % 16 == 0 &&
+                     shm + sizeof(SceneK) * VX_SERVE_MAX_SCENES <= 48 * 1024 &&
+                     ((reinterpret_cast<uintptr_t>(X1) | reinterpret_cast<uintptr_t>(X2)) & 15) == 0;
+#define VX_FEAT_LAUNCH(T, KK)                                    \
+  if (stage)                                                     \
+    serve_features_kernel<T, KK, true><<<b, 128, shm, st>>>(P);  \
+  else                                                           \
+    serve_features_kernel<T, KK, false><<<b, 128, 0, st>>>(P)
 #define VX_FEAT_SWITCH(T)        \
   switch (P.L.K) {               \
     case 1: VX_FEAT_LAUNCH(T, 1); break; \
