@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-render", action="store_true", help="skip the render-server measurement")
     p.add_argument("--no-long", action="store_true", help="skip the long-ray (384^3, stepsize 0.25) measurement")
+    p.add_argument("--no-eikonal", action="store_true",
+                   help="skip the eikonal-training (coarse 96^3, 8192/32768 rays) measurement")
     p.add_argument("--render-requests", type=int, default=120)
     p.add_argument("--render-only", action="store_true", help="only the render-server measurement (profiling)")
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
@@ -299,6 +301,9 @@ def run_ours(args, world, rank, local):
     long_rays = None
     if not args.no_long and R == 256:
         long_rays = run_long_rays(args, dev)
+    eikonal = None
+    if not args.no_eikonal and R == 256:
+        eikonal = run_eikonal(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -318,6 +323,7 @@ def run_ours(args, world, rank, local):
             "fused_bf16": bf16,
             "render": render,
             "long_rays": long_rays,
+            "eikonal_train": eikonal,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -371,6 +377,62 @@ def run_long_rays(args, dev):
         del tr, model
         torch.cuda.empty_cache()
     out["speedup_bf16_vs_fp32"] = out["bf16_graphed"]["rays_per_s"] / out["fp32"]["rays_per_s"]
+    return out
+
+
+EIK_R = 96                 # differentiation workload: coarse grids/MLP, eikonal 0.1
+EIK_RAYS = (8192, 32768)
+EIK_STEPS = 5
+EIK_WEIGHT = 0.1
+
+
+def run_eikonal(args, dev):
+    """Differentiation workload: the coarse model (SDF 96^3 f32, k0 96^3x12,
+    MLP 75 -> 128 x3 -> 3, Gaussian smoothing 5^3) trained with an eikonal
+    term 0.1 * mean((|grad| - 1)^2) on the sampled points' finite-difference
+    SDF gradient, at 8192 and 32768 rays per step: plain FP32 against BF16
+    k0 + MLP (FP32 accumulation), both through the hand-written backward
+    and full Adam steps.  Also the BF16 run's RGB / loss deviation from the
+    FP32 run on the same batch (the FP64-oracle errors of both are checked
+    by the test suite)."""
+    import numpy as np
+    import torch
+
+    from voxurf_gb300 import configs, synthetic
+    from voxurf_gb300.train import FineTrainer
+
+    rk = dict(configs.COARSE_RENDER_KWARGS)
+    n_b = 3 + EIK_STEPS
+    out = {"workload": f"coarse SDF {EIK_R}^3 f32 + k0 {EIK_R}^3x12, MLP 75->128x3->3, sphere r=0.5, "
+                       f"smoothing 5^3 s=0.8, eikonal {EIK_WEIGHT}, TV 1e-4, Adam 1e-3"}
+    for n in EIK_RAYS:
+        o, d, v = synthetic.random_rays(n * n_b, seed=13)
+        t = configs.train_targets(n * n_b, 13)
+        batches = [torch.from_numpy(np.ascontiguousarray(a.reshape(n_b, n, 3))).to(dev) for a in (o, d, v, t)]
+        res, first = {}, {}
+        for precision in ("fp32", "bf16"):
+            model = configs.build_coarse_model(EIK_R, precision, device=dev, seed=0)
+            tr = FineTrainer(model, n_rays=n, weight_eikonal=EIK_WEIGHT)
+            loss, ret = tr.step(batches[0][0], batches[1][0], batches[2][0], batches[3][0], rk, global_step=1)
+            first[precision] = (float(loss), ret["rgb_marched"].detach().clone())
+            for i in range(1, 3):
+                tr.step(batches[0][i], batches[1][i], batches[2][i], batches[3][i], rk, global_step=i + 1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for i in range(3, n_b):
+                tr.step(batches[0][i], batches[1][i], batches[2][i], batches[3][i], rk, global_step=i + 1)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / EIK_STEPS
+            res[precision] = {"rays_per_s": n / (ms / 1000.0), "ms_per_step": ms,
+                              "shaded_rows_last_step": int(ret["weights"].numel())}
+            del tr, model, ret
+            torch.cuda.empty_cache()
+        res["speedup_bf16_vs_fp32"] = res["bf16"]["rays_per_s"] / res["fp32"]["rays_per_s"]
+        res["bf16_vs_fp32_rgb_max_abs"] = float((first["bf16"][1] - first["fp32"][1]).abs().max())
+        res["bf16_vs_fp32_loss_rel"] = abs(first["bf16"][0] - first["fp32"][0]) / max(abs(first["fp32"][0]), 1e-30)
+        out[f"rays_{n}"] = res
     return out
 
 

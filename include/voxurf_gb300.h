@@ -199,13 +199,27 @@ int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, f
                          const float* per_lr, void* shadow_bf16, int64_t C, int64_t X, int64_t Y, int64_t Z,
                          int channel_last, int tv_enabled, float tv_weight, int tv_dense_mode, double lr,
                          double beta1, double beta2, double eps, int64_t step, int zero_grad, void* stream);
+/* The same sweep for a gradient that is zero outside the voxels marked in
+ * touched [X*Y*Z] (uint8, 4-byte aligned; channel-last 12-channel grids
+ * and 1-channel grids with Z % 4 == 0): unmarked voxels take gradient 0
+ * without reading it, and zero_grad resets only the marked ones.  The
+ * result equals vx_grid_tv_adam_step on the same (dense) gradient. */
+int vx_grid_tv_adam_step_touched(const float* param_in, float* param_out, float* grad, float* exp_avg,
+                                 float* exp_avg_sq, const float* per_lr, void* shadow_bf16, int64_t C, int64_t X,
+                                 int64_t Y, int64_t Z, int channel_last, int tv_enabled, float tv_weight,
+                                 int tv_dense_mode, double lr, double beta1, double beta2, double eps, int64_t step,
+                                 int zero_grad, const uint8_t* touched, void* stream);
+/* Zeroes the C gradient values of every voxel marked in touched [n_vox]
+ * (16-byte aligned) and clears the marks: the reset of a gradient that is
+ * nonzero only at marked voxels, at the cost of one read of the marks. */
+int vx_grid_clear_touched(float* grad, uint8_t* touched, int64_t n_vox, int64_t C, void* stream);
 
 /* ---- Gaussian smoothing (Voxurf._gaussian_3dconv, lib/voxurf_fine.py:246-258,
  *      used at voxurf_fine.py:638 / voxurf_coarse.py:531) ------------------- */
 
 /* out = G * in on an [X,Y,Z] grid with replicate padding; taps_host: the
  * normalised 1-D kernel (ksize odd, <= 9; the 3-D kernel is its cube).
- * tmp1/tmp2: two [X,Y,Z] scratch grids. */
+ * tmp1/tmp2: unused (the three passes run in one sweep); may be NULL. */
 int vx_smooth3d(const float* in, float* out, float* tmp1, float* tmp2, int64_t X, int64_t Y, int64_t Z,
                 const float* taps_host, int ksize, void* stream);
 /* grad_in (+)= G^T grad_out (exact adjoint of the clamped convolution). */
@@ -382,6 +396,8 @@ typedef struct {
   float* d_k0;              /* [X,Y,Z,12] accumulated                           */
   const int64_t* n_rows_dev; /* optional DEVICE row count (as vx_fine_features) */
   const float* inv_s_dev;   /* optional DEVICE inv_s (overrides inv_s)          */
+  uint8_t* k0_touched;      /* optional [X*Y*Z]: set to 1 at every k0 voxel the
+                               scatter adds to (vx_grid_tv_adam_step_touched) */
 } vx_fine_backward_args;
 int vx_fine_backward(const vx_fine_backward_args* args, void* stream);
 

@@ -42,6 +42,49 @@ def test_coarse_step_fp32_matches_fp64_oracle(cuda, bg, R):
         assert _rel_l2(p.grad, q.grad) <= 1e-5, n
 
 
+@pytest.mark.parametrize("precision,rgb_tol,loss_tol,grad_tol", [("fp32", 1e-5, 1e-6, 1e-5),
+                                                                  ("bf16", 1e-3, 2e-3, 5e-2)])
+def test_coarse_eikonal_step_vs_fp64_oracle(cuda, precision, rgb_tol, loss_tol, grad_tol):
+    """Differentiation workload: coarse grids and MLP at R = 96 (SDF FP32; k0
+    and MLP FP32 or BF16 with FP32 accumulation), the trainer's loss plus
+    0.1 * mean((|grad| - 1)^2) on the sampled points' FD gradient, 1024 rays
+    from the 49-camera rig.  Each output against the FP64 oracle: RGB max
+    abs error, loss, eikonal term, and the gradients of the SDF grid, the k0
+    grid and every MLP tensor (rel-L2; the BF16 bound covers k0 and MLP
+    weights rounded to BF16)."""
+    from voxurf_gb300.train import eikonal_loss, fine_loss
+
+    model = configs.build_coarse_model(96, precision, device=cuda, seed=0)
+    oracle = OracleCoarse(model)
+    ro, rd, vd = synthetic.random_rays(1024, seed=13)
+    tgt = configs.train_targets(1024, 13)
+    rk = dict(configs.COARSE_RENDER_KWARGS)
+    T = lambda a: torch.from_numpy(a).to(cuda)
+    g = model(T(ro), T(rd), T(vd), global_step=1, **rk)
+    g_eik = eikonal_loss(g["gradient"])
+    gl = fine_loss(g, T(tgt)) + 0.1 * g_eik
+    gl.backward()
+    o = oracle(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, **rk)
+    o_eik = ((o["gradient"].norm(dim=-1) - 1.0) ** 2).mean()
+    ol = train_loss(o, torch.from_numpy(tgt).double(), weight_rgb0=0) + 0.1 * o_eik
+    ol.backward()
+    assert g["gradient"].shape[0] == o["gradient"].shape[0] > 1000
+    rgb_err = (g["rgb_marched"].double().detach().cpu() - o["rgb_marched"].detach()).abs().max().item()
+    errs = {"rgb_max_abs": rgb_err,
+            "loss_rel": abs(gl.item() - ol.item()) / abs(ol.item()),
+            "eikonal_rel": abs(g_eik.item() - o_eik.item()) / abs(o_eik.item()),
+            "sdf_grad": _rel_l2(model.sdf.grid.grad, oracle.sdf_grid.grad),
+            "k0_grad": _rel_l2(model.k0.grid.grad, oracle.k0_grid.grad)}
+    for (n, p), (_, q) in zip(model.rgbnet.named_parameters(), oracle.rgbnet.named_parameters()):
+        errs["rgbnet." + n] = _rel_l2(p.grad, q.grad)
+    print(precision, errs)
+    assert errs["rgb_max_abs"] <= rgb_tol
+    assert errs["loss_rel"] <= loss_tol and errs["eikonal_rel"] <= loss_tol
+    for k, v in errs.items():
+        if k.endswith("grad") or k.startswith("rgbnet."):
+            assert v <= grad_tol, (k, v)
+
+
 def test_sdf_gradient_grid_vs_reference(cuda):
     from test_oracle_golden import OPS
     from voxurf_gb300.voxurf_coarse import sdf_gradient_grid

@@ -51,6 +51,38 @@ def test_smoothing_adjoint_identity(cuda):
         assert abs(lhs - rhs) <= 1e-5 * max(1.0, abs(lhs)), shape
 
 
+@pytest.mark.parametrize("ksize", [1, 3, 5, 7, 9])
+def test_smoothing_and_adjoint_vs_oracle_conv(cuda, ksize):
+    """Forward against the oracle's replicate-padded conv3d in FP64 and the
+    adjoint against its autograd, on grids with ragged tiles (sizes that are
+    not multiples of the 16 x 32 column tile or the x chunk), degenerate axes
+    and the accumulate mode."""
+    from oracle.voxurf_oracle import gaussian_kernel3d, smooth3d
+    from voxurf_gb300.voxurf_fine import smooth_grid_adjoint
+
+    sigma = 0.8
+    taps = gaussian_taps(ksize, sigma)
+    k3 = torch.from_numpy(np.einsum("i,j,k->ijk", *(taps.astype(np.float64),) * 3))
+    gen = torch.Generator().manual_seed(ksize)
+    for shape in [(40, 20, 37), (9, 33, 65), (1, 1, 1), (2, 3, 1), (17, 5, 2), (70, 17, 33)]:
+        a = torch.randn(shape, generator=gen, dtype=torch.float64)
+        g = torch.randn(shape, generator=gen, dtype=torch.float64)
+        ad = a.clone().requires_grad_(True)
+        ref = smooth3d(ad[None, None], k3)[0, 0]
+        (ref * g).sum().backward()
+        out = smooth_grid(a.float().to(cuda), taps)
+        np.testing.assert_allclose(out.cpu().double().numpy(), ref.detach().numpy(), rtol=1e-5, atol=1e-6,
+                                   err_msg=str(shape))
+        adj = smooth_grid_adjoint(g.float().to(cuda), taps)
+        np.testing.assert_allclose(adj.cpu().double().numpy(), ad.grad.numpy(), rtol=1e-5, atol=2e-6,
+                                   err_msg=str(shape))
+        base = torch.randn(shape, generator=gen).to(cuda)
+        acc = smooth_grid_adjoint(g.float().to(cuda), taps, out=base.clone(), accumulate=True)
+        np.testing.assert_allclose(acc.cpu().numpy(), (base + adj).cpu().numpy(), rtol=1e-6, atol=1e-6)
+    # the 3-D kernel the oracle builds (float32 exponentials, normalised) is the taps' cube
+    np.testing.assert_allclose(gaussian_kernel3d(ksize, sigma), k3.numpy(), rtol=1e-6, atol=1e-8)
+
+
 def test_utils_adam_vs_reference(cuda):
     p0 = torch.from_numpy(OPS["adam_p0"]).to(cuda).contiguous()
     p1 = torch.from_numpy(OPS["adam_p1"]).to(cuda).contiguous()

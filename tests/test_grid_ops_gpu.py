@@ -162,6 +162,49 @@ def test_row_sweep_bit_identical_to_generic_sweep(cuda, dense):
         assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("C,dense,shadow", [(12, True, True), (12, False, False), (1, True, False),
+                                            (1, False, False)])
+def test_touched_sweep_bit_identical_to_dense_sweep(cuda, C, dense, shadow):
+    """A gradient that is zero outside marked voxels: the sweep that reads it
+    only at the marks gives bit-identical parameters, moments and shadow to
+    the dense sweep; zero_grad resets exactly the marked voxels; the clear
+    kernel then zeroes marked rows and the marks (incl. a ragged tail)."""
+    X, Y, Z = 7, 11, 36
+    rng = np.random.default_rng(C + 2 * int(dense))
+    p = rng.normal(size=(X, Y, Z, C)).astype(np.float32)
+    marks = rng.uniform(size=(X, Y, Z)) < 0.15
+    g = rng.normal(scale=1e-3, size=p.shape).astype(np.float32) * marks[..., None]
+    g[rng.uniform(size=g.shape) < 0.1] = 0           # marked voxels may hold exact zeros
+    m = rng.normal(scale=1e-3, size=p.shape).astype(np.float32)
+    v = rng.uniform(size=p.shape).astype(np.float32) * 1e-5
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    touched = torch.zeros(_round16(X * Y * Z), dtype=torch.uint8, device=cuda)
+    touched[:X * Y * Z] = T(marks.reshape(-1).astype(np.uint8))
+    outs = []
+    for fn in ("vx_grid_tv_adam_step", "vx_grid_tv_adam_step_touched"):
+        pin, gg, gm, gv = T(p), T(g), T(m), T(v)
+        pout = torch.empty_like(pin)
+        sh = torch.empty(pin.shape, dtype=torch.bfloat16, device=cuda) if shadow else None
+        extra = (ptr(touched),) if fn.endswith("touched") else ()
+        _native.call(fn, ptr(pin), ptr(pout), ptr(gg), ptr(gm), ptr(gv), None, ptr(sh), C, X, Y, Z, int(C > 1), 1,
+                     0.07, int(dense), 1e-2, 0.9, 0.99, 1e-8, 2, 1, *extra, stream_ptr())
+        outs.append([pout.cpu(), gm.cpu(), gv.cpu(), gg.cpu()] + ([sh.float().cpu()] if shadow else []))
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+    assert torch.count_nonzero(outs[1][3]) == 0
+    # clear kernel
+    gg = T(g)
+    n_vox = X * Y * Z
+    _native.call("vx_grid_clear_touched", ptr(gg), ptr(touched), n_vox, C, stream_ptr())
+    assert torch.count_nonzero(gg) == 0 and torch.count_nonzero(touched) == 0
+    with pytest.raises(RuntimeError):
+        _native.call("vx_grid_clear_touched", ptr(gg), ptr(touched[1:]), n_vox - 1, C, stream_ptr())
+
+
+def _round16(n):
+    return (n + 15) // 16 * 16
+
+
 def test_adam_multi_matches_single(cuda):
     """One multi-tensor launch == one vx_adam_step launch per tensor."""
     import ctypes

@@ -74,6 +74,7 @@ class FineBackwardArgs(C.Structure):
         ("max_steps", I64), ("rec", P), ("dw_slot", P), ("n1", P), ("alphainv_last", P), ("d_last", P),
         ("pts2", P), ("slot2", P), ("dw2", P), ("cfg", FineFeatureCfg), ("ld1", I64), ("ld2", I64), ("dX1", P),
         ("dX2", P), ("in_bf16", I32), ("d_sdf_smooth", P), ("d_k0", P), ("n_rows_dev", P), ("inv_s_dev", P),
+        ("k0_touched", P),
     ]
 
 

@@ -65,6 +65,10 @@ _SIGNATURES = {
     "vx_adam_step_multi": [c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_f64, c_f64, c_f64, c_ptr],
     "vx_grid_tv_adam_step": [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_i64, c_i64, c_int,
                              c_int, c_f32, c_int, c_f64, c_f64, c_f64, c_f64, c_i64, c_int, c_ptr],
+    "vx_grid_tv_adam_step_touched": [c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_i64, c_i64,
+                                     c_int, c_int, c_f32, c_int, c_f64, c_f64, c_f64, c_f64, c_i64, c_int, c_ptr,
+                                     c_ptr],
+    "vx_grid_clear_touched": [c_ptr, c_ptr, c_i64, c_i64, c_ptr],
 }
 
 _RESTYPES = {

@@ -272,16 +272,26 @@ __global__ void __launch_bounds__(256) grid_tv_adam_row_kernel(const float* __re
                                                               const float* __restrict__ per_lr,
                                                               __nv_bfloat16* __restrict__ shadow, int X, int Y,
                                                               int Z, float wk, float wj, float wi, AdamParams a,
-                                                              int zero_grad) {
+                                                              int zero_grad, const uint8_t* __restrict__ touched) {
   const int j = blockIdx.x, i = blockIdx.y;
   const int row_q = Z * C / 4;  // float4 quads per row
   const int64_t row0 = ((int64_t)i * Y + j) * row_q;
   const int64_t sj = row_q, si = (int64_t)Y * row_q;
   const bool h = per_lr != nullptr;
+  const int64_t vox0 = ((int64_t)i * Y + j) * Z;  // first voxel of the row
   for (int t = threadIdx.x; t < row_q; t += blockDim.x) {
     const int64_t q = row0 + t;
     const float4 p = ld4<C>(param_in, q);
-    float4 gr = reinterpret_cast<const float4*>(grad)[q];
+    // touched map: the gradient is zero outside the marked voxels, so
+    // unmarked quads are not read
+    bool use_g = true;
+    if (touched) {
+      if (C == 1)
+        use_g = *reinterpret_cast<const uint32_t*>(touched + vox0 + 4 * t) != 0u;
+      else
+        use_g = touched[vox0 + t / (C >= 4 ? C / 4 : 1)] != 0;
+    }
+    float4 gr = use_g ? reinterpret_cast<const float4*>(grad)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
     float gv[4] = {gr.x, gr.y, gr.z, gr.w};
     const float pv[4] = {p.x, p.y, p.z, p.w};
     if (TV) {
@@ -336,7 +346,7 @@ __global__ void __launch_bounds__(256) grid_tv_adam_row_kernel(const float* __re
     reinterpret_cast<float4*>(param_out)[q] = make_float4(out[0], out[1], out[2], out[3]);
     reinterpret_cast<float4*>(exp_avg)[q] = make_float4(mv[0], mv[1], mv[2], mv[3]);
     reinterpret_cast<float4*>(exp_avg_sq)[q] = make_float4(vv[0], vv[1], vv[2], vv[3]);
-    if (zero_grad) reinterpret_cast<float4*>(grad)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (zero_grad && use_g) reinterpret_cast<float4*>(grad)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (SHADOW) {
       __nv_bfloat162 lo = __floats2bfloat162_rn(out[0], out[1]);
       __nv_bfloat162 hi = __floats2bfloat162_rn(out[2], out[3]);
@@ -391,6 +401,36 @@ __global__ void __launch_bounds__(256) adam_multi_kernel(const AdamMultiTable T)
     p[i] = adam_update(p[i], g[i], mi, vi, 1.f, false, a);
     m[i] = mi;
     v[i] = vi;
+  }
+}
+
+// Resets a gradient grid that is nonzero only at marked voxels: zeroes the
+// C values of every marked voxel and clears the marks (16 marks per thread
+// and chunk; unmarked chunks cost one 16-byte read).
+__global__ void __launch_bounds__(256) clear_touched_kernel(float* __restrict__ grad, uint8_t* __restrict__ touched,
+                                                           int64_t n_vox, int C) {
+  const int64_t chunks = (n_vox + 15) / 16;
+  for (int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ch < chunks;
+       ch += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v0 = ch * 16;
+    if (v0 + 16 <= n_vox) {
+      const uint4 m = reinterpret_cast<const uint4*>(touched)[ch];
+      if ((m.x | m.y | m.z | m.w) == 0u) continue;
+      const uint32_t w[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+      for (int b = 0; b < 16; ++b) {
+        if (((w[b >> 2] >> (8 * (b & 3))) & 0xffu) == 0u) continue;
+        float* g = grad + (v0 + b) * C;
+        for (int c = 0; c < C; ++c) g[c] = 0.f;
+      }
+      reinterpret_cast<uint4*>(touched)[ch] = make_uint4(0u, 0u, 0u, 0u);
+    } else {
+      for (int64_t v = v0; v < n_vox; ++v) {
+        if (!touched[v]) continue;
+        for (int c = 0; c < C; ++c) grad[v * C + c] = 0.f;
+        touched[v] = 0;
+      }
+    }
   }
 }
 
@@ -543,16 +583,17 @@ int vx_adam_step_multi(int n_tensors, float* const* params, float* const* grads,
   return launch_status();
 }
 
-int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, float* exp_avg, float* exp_avg_sq,
-                         const float* per_lr, void* shadow_bf16, int64_t C, int64_t X, int64_t Y, int64_t Z,
-                         int channel_last, int tv_enabled, float tv_weight, int tv_dense_mode, double lr,
-                         double beta1, double beta2, double eps, int64_t step, int zero_grad, void* stream) {
+static int grid_tv_adam_impl(const float* param_in, float* param_out, float* grad, float* exp_avg,
+                             float* exp_avg_sq, const float* per_lr, void* shadow_bf16, int64_t C, int64_t X,
+                             int64_t Y, int64_t Z, int channel_last, int tv_enabled, float tv_weight,
+                             int tv_dense_mode, double lr, double beta1, double beta2, double eps, int64_t step,
+                             int zero_grad, const uint8_t* touched, void* stream) {
   if (!shape_ok(C, X, Y, Z) || step < 1) return VX_ERR_ARG;
   if (!param_in || !param_out || !grad || !exp_avg || !exp_avg_sq) return VX_ERR_ARG;
   if (tv_enabled && param_in == param_out) return VX_ERR_ARG;
   const uintptr_t al = ((uintptr_t)param_in) | ((uintptr_t)param_out) | ((uintptr_t)grad) | ((uintptr_t)exp_avg) |
                        ((uintptr_t)exp_avg_sq) | ((uintptr_t)per_lr);
-  if ((al & 15) || (((uintptr_t)shadow_bf16) & 7)) return VX_ERR_ARG;
+  if ((al & 15) || (((uintptr_t)shadow_bf16) & 7) || (((uintptr_t)touched) & 3)) return VX_ERR_ARG;
   const double bc1 = 1.0 - pow(beta1, (double)step);
   const double bc2 = 1.0 - pow(beta2, (double)step);
   AdamParams a;
@@ -580,8 +621,8 @@ int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, f
 #define VX_ROW(CC, TV, DENSE, SH)                                                                             \
   grid_tv_adam_row_kernel<CC, TV, DENSE, SH><<<grid, threads, 0, st>>>(param_in, param_out, grad, exp_avg,       \
                                                                       exp_avg_sq, per_lr, sh, (int)X, (int)Y,   \
-                                                                      (int)Z, w6, w6, w6, a, zero_grad)
-#define VX_ROW_C(CC)                                                                                          \
+                                                                      (int)Z, w6, w6, w6, a, zero_grad, touched)
+#define VX_ROW_C(CC)                                                                                       \
   if (tv_enabled) {                                                                                           \
     if (tv_dense_mode) {                                                                                      \
       if (sh) VX_ROW(CC, true, true, true); else VX_ROW(CC, true, true, false);                               \
@@ -600,6 +641,7 @@ int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, f
 #undef VX_ROW
     return launch_status();
   }
+  if (touched) return VX_ERR_UNSUPPORTED;  // the map is read by the row kernel only
   const unsigned b = sweep_blocks((n + 3) / 4);
 #define VX_LAUNCH_TVA(TV, DENSE, SH) \
   grid_tv_adam_kernel<TV, DENSE, SH><<<b, 256, 0, st>>>(param_in, param_out, grad, exp_avg, exp_avg_sq, per_lr, sh, \
@@ -614,6 +656,35 @@ int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, f
     if (sh) VX_LAUNCH_TVA(false, false, true); else VX_LAUNCH_TVA(false, false, false);
   }
 #undef VX_LAUNCH_TVA
+  return launch_status();
+}
+
+int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, float* exp_avg, float* exp_avg_sq,
+                         const float* per_lr, void* shadow_bf16, int64_t C, int64_t X, int64_t Y, int64_t Z,
+                         int channel_last, int tv_enabled, float tv_weight, int tv_dense_mode, double lr,
+                         double beta1, double beta2, double eps, int64_t step, int zero_grad, void* stream) {
+  return grid_tv_adam_impl(param_in, param_out, grad, exp_avg, exp_avg_sq, per_lr, shadow_bf16, C, X, Y, Z,
+                           channel_last, tv_enabled, tv_weight, tv_dense_mode, lr, beta1, beta2, eps, step,
+                           zero_grad, nullptr, stream);
+}
+
+int vx_grid_tv_adam_step_touched(const float* param_in, float* param_out, float* grad, float* exp_avg,
+                                 float* exp_avg_sq, const float* per_lr, void* shadow_bf16, int64_t C, int64_t X,
+                                 int64_t Y, int64_t Z, int channel_last, int tv_enabled, float tv_weight,
+                                 int tv_dense_mode, double lr, double beta1, double beta2, double eps, int64_t step,
+                                 int zero_grad, const uint8_t* touched, void* stream) {
+  if (!touched) return VX_ERR_ARG;
+  return grid_tv_adam_impl(param_in, param_out, grad, exp_avg, exp_avg_sq, per_lr, shadow_bf16, C, X, Y, Z,
+                           channel_last, tv_enabled, tv_weight, tv_dense_mode, lr, beta1, beta2, eps, step,
+                           zero_grad, touched, stream);
+}
+
+int vx_grid_clear_touched(float* grad, uint8_t* touched, int64_t n_vox, int64_t C, void* stream) {
+  if (n_vox < 0 || C < 1 || C > 64) return VX_ERR_ARG;
+  if (n_vox == 0) return VX_OK;
+  if (!grad || !touched || (((uintptr_t)touched) & 15)) return VX_ERR_ARG;
+  const int64_t chunks = (n_vox + 15) / 16;
+  clear_touched_kernel<<<sweep_blocks(chunks), 256, 0, as_stream(stream)>>>(grad, touched, n_vox, (int)C);
   return launch_status();
 }
 

@@ -399,6 +399,7 @@ struct FeatBwdParams {
   float* d_sdf;          // [X,Y,Z] grad of the smoothed grid
   float* d_k0;           // [X,Y,Z,12] channel-last
   const int64_t* n_rows_dev;  // optional device row count (rows beyond it are skipped)
+  uint8_t* k0_touched;        // optional [X*Y*Z] marks of the k0 voxels scattered to
 };
 
 template <typename T>
@@ -451,6 +452,7 @@ __global__ void __launch_bounds__(128) features_fine_bwd_kernel(FeatBwdParams P)
 #pragma unroll
     for (int ch = 0; ch < 12; ++ch) dk0[ch] += get(dx1, ch);
   scatterC<12>(P.d_k0, cc, dk0);
+  if (P.k0_touched) mark_corners(P.k0_touched, cc);
   // hierarchical probes
   for (int kk = 0; kk < P.K; ++kk) {
     float fm[3], fp[3], invd[3], gr[3];
@@ -1258,6 +1260,7 @@ int vx_fine_backward(const vx_fine_backward_args* A, void* stream) {
     if (A->ld1 < x1_cols(&A->cfg) || A->ld2 < x2_cols(&A->cfg)) return VX_ERR_ARG;
     F.n_rows = A->n_rows;
     F.n_rows_dev = A->n_rows_dev;
+    F.k0_touched = A->k0_touched;
     F.pts2 = A->pts2;
     F.g = geom_from(&A->grid);
     F.sdf = A->sdf_smooth;

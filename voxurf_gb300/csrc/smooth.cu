@@ -4,9 +4,21 @@
 // normalised Gaussian of Voxurf._gaussian_3dconv (lib/voxurf_fine.py:246-258,
 // applied every step at voxurf_fine.py:638; voxurf_coarse.py:180-198, 531).
 // exp(-(x^2+y^2+z^2)/(2 s^2)) / sum factorises exactly into three normalised
-// 1-D kernels, so the 125-tap convolution becomes three 5-tap passes with
+// 1-D kernels, so the k^3-tap convolution becomes three k-tap passes with
 // clamped (replicate) indices.  The backward is the exact adjoint of each
-// clamped pass, applied in reverse order.
+// clamped pass.
+//
+// One kernel does all three passes in one sweep of the grid.  A CTA owns a
+// 16 (y) x 32 (z) column tile and a chunk of x; it streams the chunk's
+// x-planes (plus an H-plane halo on each side) through a 4-deep ring of
+// shared-memory stages filled by 4-byte cp.async copies (clamped source
+// coordinates for the forward, zero fill outside the grid for the adjoint),
+// applies the z pass and the y pass in shared memory, and keeps the last
+// 2H+1 y-passed values of each of its two output columns in registers, from
+// which it forms the x pass and writes the output plane with 128-byte
+// coalesced stores.  Each input voxel is read from DRAM about once; the
+// halos are mostly L2 hits because the chunks of one tile are neighbouring
+// CTAs.
 #include "common.cuh"
 
 namespace vx {
@@ -16,112 +28,74 @@ struct Taps {
   int h;  // half width, ksize = 2h+1 (<= 9)
 };
 
-// One separable pass along `axis` (0: X, stride Y*Z; 1: Y, stride Z; 2: Z).
-template <bool ADJOINT, bool ACCUM>
-__global__ void smooth_axis_kernel(const float* __restrict__ in, float* __restrict__ out, int X, int Y, int Z,
-                                   int axis, Taps t) {
-  const int64_t n = (int64_t)X * Y * Z;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t astride = axis == 0 ? (int64_t)Y * Z : (axis == 1 ? (int64_t)Z : 1);
-  const int len = axis == 0 ? X : (axis == 1 ? Y : Z);
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += stride) {
-    const int pos = (int)((idx / astride) % len);
-    const float* base = in + (idx - (int64_t)pos * astride);
-    float acc = 0.f;
-    if (!ADJOINT) {
-      // out[i] = sum_t w_t * in[clamp(i+t)]
-      for (int tt = -t.h; tt <= t.h; ++tt) {
-        int q = pos + tt;
-        q = q < 0 ? 0 : (q > len - 1 ? len - 1 : q);
-        acc += t.w[tt + t.h] * base[(int64_t)q * astride];
-      }
-    } else {
-      // out[j] = sum_i sum_t w_t * g[i] * [clamp(i+t) == j]
-      if (len == 1) {
-        float s = 0.f;
-        for (int tt = -t.h; tt <= t.h; ++tt) s += t.w[tt + t.h];
-        acc = s * base[0];
-      } else if (pos == 0) {
-        for (int i = 0; i <= t.h && i < len; ++i) {
-          float s = 0.f;
-          for (int tt = -t.h; tt <= -i; ++tt) s += t.w[tt + t.h];
-          acc += s * base[(int64_t)i * astride];
-        }
-      } else if (pos == len - 1) {
-        for (int i = (len - 1 - t.h > 0 ? len - 1 - t.h : 0); i < len; ++i) {
-          float s = 0.f;
-          for (int tt = len - 1 - i; tt <= t.h; ++tt) s += t.w[tt + t.h];
-          acc += s * base[(int64_t)i * astride];
-        }
-      } else {
-        for (int tt = -t.h; tt <= t.h; ++tt) {
-          const int i = pos - tt;
-          if (i >= 0 && i < len) acc += t.w[tt + t.h] * base[(int64_t)i * astride];
-        }
-      }
-    }
-    if (ACCUM)
-      out[idx] += acc;
-    else
-      out[idx] = acc;
-  }
+constexpr int SM_TY = 16, SM_TZ = 32, SM_THREADS = 256, SM_STAGES = 4;
+static_assert(SM_TY == 2 * (SM_THREADS / 32), "two y rows per warp");
+static_assert(SM_TZ == 32, "one z column per lane");
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// 4-byte asynchronous global->shared copy; src_bytes 0 writes a zero.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_group() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// ---- single-pass tiled version ----------------------------------------------
-// One CTA computes an 8 x 8 x 16 output tile: it stages the input tile plus a
-// 2-voxel halo (12 x 12 x 20) in shared memory and applies the three 1-D
-// passes there (z, then y, then x), so each voxel is read from DRAM about
-// once and written once.  Forward: the halo is read at clamped coordinates
-// (replicate padding).  Adjoint: the halo outside the grid is zero and each
-// axis applies the adjoint of the clamped 1-D convolution (boundary voxels
-// collect the taps that the forward clamped onto them).
-constexpr int TX = 8, TY = 8, TZ = 16, HALO = 2;
-constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO, SZ = TZ + 2 * HALO;
-
-// Adjoint of one clamped 1-D convolution at output position j of an axis of
-// length n, reading the gradient through get(i) for i in [j-h, j+h] (zero
-// outside [0, n)).
-template <typename Get>
-__device__ __forceinline__ float adjoint1d(const Taps& t, int j, int n, Get get) {
+// Adjoint of one clamped 1-D convolution at output position j (0 or n-1) of
+// an axis of length n, reading the gradient at position j+d through rel(d)
+// for d in [-H, H] (zero outside [0, n)).  Only the two boundary positions
+// take this path: they also collect the taps that the forward clamped onto
+// them.  The offsets are compile-time after unrolling, so rel may index a
+// register array.
+template <int H, typename Rel>
+__device__ __forceinline__ float adjoint_boundary(const float (&w)[2 * H + 1], int j, int n, Rel rel) {
   float acc = 0.f;
   if (n == 1) {
     float s = 0.f;
-    for (int tt = -t.h; tt <= t.h; ++tt) s += t.w[tt + t.h];
-    return s * get(0);
+#pragma unroll
+    for (int tt = -H; tt <= H; ++tt) s += w[tt + H];
+    return s * rel(0);
   }
   if (j == 0) {
-    for (int i = 0; i <= t.h && i < n; ++i) {
-      float s = 0.f;
-      for (int tt = -t.h; tt <= -i; ++tt) s += t.w[tt + t.h];
-      acc += s * get(i);
+#pragma unroll
+    for (int i = 0; i <= H; ++i) {  // gradient positions i = 0 .. H
+      if (i < n) {
+        float s = 0.f;
+#pragma unroll
+        for (int tt = -H; tt <= -i; ++tt) s += w[tt + H];
+        acc += s * rel(i);
+      }
     }
-  } else if (j == n - 1) {
-    for (int i = (n - 1 - t.h > 0 ? n - 1 - t.h : 0); i < n; ++i) {
-      float s = 0.f;
-      for (int tt = n - 1 - i; tt <= t.h; ++tt) s += t.w[tt + t.h];
-      acc += s * get(i);
-    }
-  } else {
-    for (int tt = -t.h; tt <= t.h; ++tt) {
-      const int i = j - tt;
-      if (i >= 0 && i < n) acc += t.w[tt + t.h] * get(i);
+  } else {  // j == n - 1
+#pragma unroll
+    for (int d = -H; d <= 0; ++d) {  // gradient positions n-1+d, ascending
+      if (n - 1 + d >= 0) {
+        float s = 0.f;
+#pragma unroll
+        for (int tt = -d; tt <= H; ++tt) s += w[tt + H];
+        acc += s * rel(d);
+      }
     }
   }
   return acc;
 }
 
-// 1-D pass at global position j of an axis of length n, reading the staged
-// values through get(k) for k in [j-H, j+H] (staged coordinates are
-// clamped for the forward, zero outside the grid for the adjoint).  The
-// adjoint is the transposed convolution (flipped taps) except at the two
-// boundary positions, which also collect the taps the forward clamped.
+// 1-D pass at global position j of an axis of length n; get(i) reads the
+// value at global index i in [j-H, j+H] (clamped copies for the forward,
+// zero outside the grid for the adjoint).  The adjoint is the transposed
+// convolution (flipped taps) except at the two boundary positions.
 template <bool ADJOINT, int H, typename Get>
-__device__ __forceinline__ float pass1d(const Taps& t, const float w[2 * H + 1], int j, int n, Get get) {
+__device__ __forceinline__ float pass1d(const float (&w)[2 * H + 1], int j, int n, Get get) {
   float acc = 0.f;
   if (ADJOINT) {
-    if (j == 0 || j == n - 1) return adjoint1d(t, j, n, get);
+    if (j == 0 || j == n - 1) return adjoint_boundary<H>(w, j, n, [&](int d) { return get(j + d); });
 #pragma unroll
-    for (int tt = H; tt >= -H; --tt) acc += w[H - tt] * get(j + tt);  // the order of adjoint1d
+    for (int tt = H; tt >= -H; --tt) acc += w[H - tt] * get(j + tt);
   } else {
 #pragma unroll
     for (int tt = -H; tt <= H; ++tt) acc += w[tt + H] * get(j + tt);
@@ -129,72 +103,143 @@ __device__ __forceinline__ float pass1d(const Taps& t, const float w[2 * H + 1],
   return acc;
 }
 
-template <bool ADJOINT, bool ACCUM, int H>
-__global__ void __launch_bounds__(256) smooth_tile_kernel(const float* __restrict__ in, float* __restrict__ out,
-                                                         int X, int Y, int Z, Taps t) {
-  __shared__ float s_in[SX][SY][SZ];
-  __shared__ float s_z[SX][SY][TZ];
-  __shared__ float s_y[SX][TY][TZ];
-  float w[2 * H + 1];
-#pragma unroll
-  for (int i = 0; i < 2 * H + 1; ++i) w[i] = t.w[i];
-  const int x0 = blockIdx.z * TX, y0 = blockIdx.y * TY, z0 = blockIdx.x * TZ;
-  const int tid = threadIdx.x;
-  for (int e = tid; e < SX * SY * SZ; e += blockDim.x) {
-    const int c = e % SZ, b = (e / SZ) % SY, a = e / (SZ * SY);
-    int gx = x0 + a - HALO, gy = y0 + b - HALO, gz = z0 + c - HALO;
-    float v;
+// Copies input plane gx of the (y0, z0) tile, with its H halo in y and z,
+// into one shared-memory stage.
+template <bool ADJOINT, int H>
+__device__ __forceinline__ void issue_plane(float (*dst)[SM_TZ + 2 * H], const float* __restrict__ in, int gx, int X,
+                                            int Y, int Z, int y0, int z0) {
+  constexpr int PY = SM_TY + 2 * H, PZ = SM_TZ + 2 * H;
+  const bool xin = gx >= 0 && gx < X;
+  const int cx = min(max(gx, 0), X - 1);
+  for (int e = threadIdx.x; e < PY * PZ; e += SM_THREADS) {
+    const int b = e / PZ, c = e - b * PZ;
+    int gy = y0 + b - H, gz = z0 + c - H;
     if (!ADJOINT) {
-      gx = min(max(gx, 0), X - 1);
       gy = min(max(gy, 0), Y - 1);
       gz = min(max(gz, 0), Z - 1);
-      v = in[((int64_t)gx * Y + gy) * Z + gz];
+      cp_async4(&dst[b][c], in + ((int64_t)cx * Y + gy) * Z + gz, 4u);
     } else {
-      const bool inside = gx >= 0 && gx < X && gy >= 0 && gy < Y && gz >= 0 && gz < Z;
-      v = inside ? in[((int64_t)gx * Y + gy) * Z + gz] : 0.f;
+      const bool inside = xin && gy >= 0 && gy < Y && gz >= 0 && gz < Z;
+      cp_async4(&dst[b][c], inside ? in + ((int64_t)gx * Y + gy) * Z + gz : in, inside ? 4u : 0u);
     }
-    s_in[a][b][c] = v;
   }
-  __syncthreads();
-  // z pass over all (a, b) of the halo'd tile
-  for (int e = tid; e < SX * SY * TZ; e += blockDim.x) {
-    const int c = e % TZ, b = (e / TZ) % SY, a = e / (TZ * SY);
-    s_z[a][b][c] = pass1d<ADJOINT, H>(t, w, z0 + c, Z, [&](int i) { return s_in[a][b][i - z0 + HALO]; });
+}
+
+template <bool ADJOINT, bool ACCUM, int H>
+__global__ void __launch_bounds__(SM_THREADS) smooth_march_kernel(const float* __restrict__ in,
+                                                                  float* __restrict__ out, int X, int Y, int Z,
+                                                                  int CX, int n_xc, int n_zt, Taps t) {
+  constexpr int PY = SM_TY + 2 * H, PZ = SM_TZ + 2 * H, R = 2 * H + 1;
+  __shared__ __align__(16) float s_in[SM_STAGES][PY][PZ];
+  __shared__ float s_zq[PY][SM_TZ];
+  float w[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) w[i] = t.w[i];
+  const int xc = blockIdx.x % n_xc, tile = blockIdx.x / n_xc;
+  const int y0 = (tile / n_zt) * SM_TY, z0 = (tile % n_zt) * SM_TZ;
+  const int x0 = xc * CX, x1 = min(X, x0 + CX);
+  const int NP = x1 - x0 + 2 * H;  // input planes x0-H .. x1-1+H
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int gz = z0 + lane;
+
+#pragma unroll
+  for (int s = 0; s < SM_STAGES - 1; ++s) {
+    if (s < NP) issue_plane<ADJOINT, H>(s_in[s], in, x0 - H + s, X, Y, Z, y0, z0);
+    cp_async_commit_group();
   }
-  __syncthreads();
-  for (int e = tid; e < SX * TY * TZ; e += blockDim.x) {
-    const int c = e % TZ, b = (e / TZ) % TY, a = e / (TZ * TY);
-    s_y[a][b][c] = pass1d<ADJOINT, H>(t, w, y0 + b, Y, [&](int i) { return s_z[a][i - y0 + HALO][c]; });
+  float ring[2][R];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int k = 0; k < R; ++k) ring[r][k] = 0.f;
+
+  for (int p = 0; p < NP; ++p) {
+    cp_async_wait_group<SM_STAGES - 2>();  // plane p has landed
+    __syncthreads();
+    {
+      const int q = p + SM_STAGES - 1;  // refill the stage plane p-1 used
+      if (q < NP) issue_plane<ADJOINT, H>(s_in[q % SM_STAGES], in, x0 - H + q, X, Y, Z, y0, z0);
+      cp_async_commit_group();
+    }
+    const int st = p % SM_STAGES;
+    // z pass over all PY rows of the plane
+    for (int e = tid; e < PY * SM_TZ; e += SM_THREADS) {
+      const int b = e >> 5, c = e & 31;
+      s_zq[b][c] = pass1d<ADJOINT, H>(w, z0 + c, Z, [&](int i) { return s_in[st][b][i - z0 + H]; });
+    }
+    __syncthreads();
+    // y pass for this thread's two output rows; shift them into the x ring
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int gy = y0 + 2 * warp + r;
+      const float v = pass1d<ADJOINT, H>(w, gy, Y, [&](int i) { return s_zq[i - y0 + H][lane]; });
+#pragma unroll
+      for (int k = 0; k < R - 1; ++k) ring[r][k] = ring[r][k + 1];
+      ring[r][R - 1] = v;
+    }
+    // x pass: ring[k] holds input plane gxo - H + k of output plane gxo
+    const int gxo = x0 + p - 2 * H;
+    if (gxo < x0 || gz >= Z) continue;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int gy = y0 + 2 * warp + r;
+      if (gy >= Y) continue;
+      float acc;
+      if (ADJOINT) {
+        if (gxo == 0 || gxo == X - 1) {
+          acc = adjoint_boundary<H>(w, gxo, X, [&](int d) { return ring[r][d + H]; });
+        } else {
+          acc = 0.f;
+#pragma unroll
+          for (int tt = H; tt >= -H; --tt) acc += w[H - tt] * ring[r][tt + H];
+        }
+      } else {
+        acc = 0.f;
+#pragma unroll
+        for (int tt = -H; tt <= H; ++tt) acc += w[tt + H] * ring[r][tt + H];
+      }
+      const int64_t o = ((int64_t)gxo * Y + gy) * Z + gz;
+      if (ACCUM)
+        out[o] += acc;
+      else
+        out[o] = acc;
+    }
   }
-  __syncthreads();
-  for (int e = tid; e < TX * TY * TZ; e += blockDim.x) {
-    const int c = e % TZ, b = (e / TZ) % TY, a = e / (TZ * TY);
-    const int gx = x0 + a, gy = y0 + b, gz = z0 + c;
-    if (gx >= X || gy >= Y || gz >= Z) continue;
-    const float acc = pass1d<ADJOINT, H>(t, w, gx, X, [&](int i) { return s_y[i - x0 + HALO][b][c]; });
-    const int64_t o = ((int64_t)gx * Y + gy) * Z + gz;
-    if (ACCUM)
-      out[o] += acc;
-    else
-      out[o] = acc;
-  }
+  cp_async_wait_group<0>();
+}
+
+// x chunking: about two waves of 8 resident CTAs per SM, chunks of >= 8 planes.
+template <bool ADJOINT, bool ACCUM, int H>
+static void launch_march(const float* in, float* out, int X, int Y, int Z, const Taps& t, cudaStream_t st) {
+  const int n_zt = (Z + SM_TZ - 1) / SM_TZ, n_yt = (Y + SM_TY - 1) / SM_TY;
+  const int64_t tiles = (int64_t)n_zt * n_yt;
+  const int64_t want = (int64_t)sm_count() * 8 * 2;
+  int64_t nx = (want + tiles - 1) / tiles;
+  const int64_t nx_max = (X + 7) / 8;
+  nx = nx < 1 ? 1 : (nx > nx_max ? nx_max : nx);
+  int n_xc = (int)nx;
+  const int CX = (X + n_xc - 1) / n_xc;
+  n_xc = (X + CX - 1) / CX;
+  const unsigned blocks = (unsigned)(tiles * n_xc);
+  smooth_march_kernel<ADJOINT, ACCUM, H><<<blocks, SM_THREADS, 0, st>>>(in, out, X, Y, Z, CX, n_xc, n_zt, t);
 }
 
 template <bool ADJOINT, bool ACCUM>
-static void launch_tile(const float* in, float* out, int X, int Y, int Z, const Taps& t, cudaStream_t st) {
-  dim3 grid((unsigned)((Z + TZ - 1) / TZ), (unsigned)((Y + TY - 1) / TY), (unsigned)((X + TX - 1) / TX));
-  if (t.h == 2)
-    smooth_tile_kernel<ADJOINT, ACCUM, 2><<<grid, 256, 0, st>>>(in, out, X, Y, Z, t);
-  else if (t.h == 1)
-    smooth_tile_kernel<ADJOINT, ACCUM, 1><<<grid, 256, 0, st>>>(in, out, X, Y, Z, t);
-  else
-    smooth_tile_kernel<ADJOINT, ACCUM, 0><<<grid, 256, 0, st>>>(in, out, X, Y, Z, t);
+static void launch_h(const float* in, float* out, int X, int Y, int Z, const Taps& t, cudaStream_t st) {
+  switch (t.h) {
+    case 0: launch_march<ADJOINT, ACCUM, 0>(in, out, X, Y, Z, t, st); break;
+    case 1: launch_march<ADJOINT, ACCUM, 1>(in, out, X, Y, Z, t, st); break;
+    case 2: launch_march<ADJOINT, ACCUM, 2>(in, out, X, Y, Z, t, st); break;
+    case 3: launch_march<ADJOINT, ACCUM, 3>(in, out, X, Y, Z, t, st); break;
+    default: launch_march<ADJOINT, ACCUM, 4>(in, out, X, Y, Z, t, st); break;
+  }
 }
 
-static unsigned pass_blocks(int64_t n) {
-  int64_t b = (n + 255) / 256;
-  const int64_t cap = (int64_t)sm_count() * 16;
-  return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+static int make_taps(const float* taps_host, int ksize, Taps& t) {
+  if (ksize < 1 || ksize > 9 || (ksize % 2) == 0) return VX_ERR_ARG;
+  t.h = ksize / 2;
+  for (int i = 0; i < 9; ++i) t.w[i] = i < ksize ? taps_host[i] : 0.f;
+  return VX_OK;
 }
 
 }  // namespace vx
@@ -205,55 +250,31 @@ extern "C" {
 
 int vx_smooth3d(const float* in, float* out, float* tmp1, float* tmp2, int64_t X, int64_t Y, int64_t Z,
                 const float* taps_host, int ksize, void* stream) {
-  if (X <= 0 || Y <= 0 || Z <= 0 || ksize < 1 || ksize > 9 || (ksize % 2) == 0) return VX_ERR_ARG;
-  if (!in || !out || !tmp1 || !tmp2 || !taps_host) return VX_ERR_ARG;
+  (void)tmp1;
+  (void)tmp2;
+  if (X <= 0 || Y <= 0 || Z <= 0 || !in || !out || !taps_host) return VX_ERR_ARG;
   if (X * Y * Z > INT32_MAX) return VX_ERR_ARG;
   Taps t;
-  t.h = ksize / 2;
-  for (int i = 0; i < 9; ++i) t.w[i] = i < ksize ? taps_host[i] : 0.f;
-  cudaStream_t st = as_stream(stream);
-  if (t.h <= HALO) {
-    launch_tile<false, false>(in, out, (int)X, (int)Y, (int)Z, t, st);
-    return launch_status();
-  }
-  const unsigned b = pass_blocks(X * Y * Z);
-  smooth_axis_kernel<false, false><<<b, 256, 0, st>>>(in, tmp1, (int)X, (int)Y, (int)Z, 0, t);
-  int s = launch_status();
+  const int s = make_taps(taps_host, ksize, t);
   if (s) return s;
-  smooth_axis_kernel<false, false><<<b, 256, 0, st>>>(tmp1, tmp2, (int)X, (int)Y, (int)Z, 1, t);
-  s = launch_status();
-  if (s) return s;
-  smooth_axis_kernel<false, false><<<b, 256, 0, st>>>(tmp2, out, (int)X, (int)Y, (int)Z, 2, t);
+  launch_h<false, false>(in, out, (int)X, (int)Y, (int)Z, t, as_stream(stream));
   return launch_status();
 }
 
 int vx_smooth3d_adjoint(const float* grad_out, float* grad_in, float* tmp1, float* tmp2, int64_t X, int64_t Y,
                         int64_t Z, const float* taps_host, int ksize, int accumulate, void* stream) {
-  if (X <= 0 || Y <= 0 || Z <= 0 || ksize < 1 || ksize > 9 || (ksize % 2) == 0) return VX_ERR_ARG;
-  if (!grad_out || !grad_in || !tmp1 || !tmp2 || !taps_host) return VX_ERR_ARG;
+  (void)tmp1;
+  (void)tmp2;
+  if (X <= 0 || Y <= 0 || Z <= 0 || !grad_out || !grad_in || !taps_host) return VX_ERR_ARG;
   if (X * Y * Z > INT32_MAX) return VX_ERR_ARG;
   Taps t;
-  t.h = ksize / 2;
-  for (int i = 0; i < 9; ++i) t.w[i] = i < ksize ? taps_host[i] : 0.f;
+  const int s = make_taps(taps_host, ksize, t);
+  if (s) return s;
   cudaStream_t st = as_stream(stream);
-  if (t.h <= HALO) {
-    if (accumulate)
-      launch_tile<true, true>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t, st);
-    else
-      launch_tile<true, false>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t, st);
-    return launch_status();
-  }
-  const unsigned b = pass_blocks(X * Y * Z);
-  smooth_axis_kernel<true, false><<<b, 256, 0, st>>>(grad_out, tmp1, (int)X, (int)Y, (int)Z, 2, t);
-  int s = launch_status();
-  if (s) return s;
-  smooth_axis_kernel<true, false><<<b, 256, 0, st>>>(tmp1, tmp2, (int)X, (int)Y, (int)Z, 1, t);
-  s = launch_status();
-  if (s) return s;
   if (accumulate)
-    smooth_axis_kernel<true, true><<<b, 256, 0, st>>>(tmp2, grad_in, (int)X, (int)Y, (int)Z, 0, t);
+    launch_h<true, true>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t, st);
   else
-    smooth_axis_kernel<true, false><<<b, 256, 0, st>>>(tmp2, grad_in, (int)X, (int)Y, (int)Z, 0, t);
+    launch_h<true, false>(grad_out, grad_in, (int)X, (int)Y, (int)Z, t, st);
   return launch_status();
 }
 

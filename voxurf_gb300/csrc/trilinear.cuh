@@ -134,4 +134,14 @@ __device__ __forceinline__ void scatterC(float* __restrict__ grid, const Corners
   }
 }
 
+// Marks the voxels scatterC adds to (every writer stores the same byte, so
+// plain stores suffice).
+__device__ __forceinline__ void mark_corners(uint8_t* __restrict__ touched, const Corners& c) {
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (c.off[q] < 0 || c.w[q] == 0.f) continue;
+    touched[c.off[q]] = 1;
+  }
+}
+
 }  // namespace vx

@@ -86,7 +86,6 @@ class GraphedFineStep:
         self.inp = torch.empty((4, N, 3), dtype=f32, device=dev)   # rays_o, rays_d, viewdirs, target
         # part A
         self.sdf_s = torch.empty((X, Y, Z), dtype=f32, device=dev)
-        self.tmp = torch.empty((2, X, Y, Z), dtype=f32, device=dev)
         self.rec = torch.empty((N * self.max_steps, 4), dtype=f32, device=dev)
         self.dw_slot = torch.empty(N * self.max_steps, dtype=f32, device=dev)
         self.n1 = torch.empty(N, dtype=i32, device=dev)
@@ -99,6 +98,10 @@ class GraphedFineStep:
         self.d_sdf_s = torch.empty((X, Y, Z), dtype=f32, device=dev)
         self.d_sdf = torch.zeros_like(model.sdf.grid)
         self.d_k0 = torch.zeros_like(model.k0.grid)          # channels_last_3d like the parameter
+        # marks of the k0 voxels the backward scatters to: part B resets only
+        # those gradient rows, the optimizer sweep reads only those
+        self.k0_touched = torch.zeros(_round_up(X * Y * Z, 16), dtype=torch.uint8, device=dev)
+        self.k0_group = next(g for g in trainer.optimizer.param_groups if g.get("name") == "k0")
         self.dyn_host = torch.zeros(4, dtype=f32, pin_memory=True)
         self.dyn = torch.zeros(4, dtype=f32, device=dev)
         # padded first-layer weights (zero columns beyond the feature count)
@@ -151,7 +154,11 @@ class GraphedFineStep:
         model.k0.grid.grad = self.d_k0
         for p, g in zip(self.rgb_params + self.k_params, entry["grads"]):
             p.grad = g
-        tr.optimizer.step(zero_grad=True)
+        self.k0_group["touched"] = self.k0_touched
+        try:
+            tr.optimizer.step(zero_grad=True)
+        finally:
+            self.k0_group.pop("touched", None)
         return entry["loss"], S2
 
     def _pick_capacity(self, S2: int, kptr: int) -> int:
@@ -191,7 +198,7 @@ class GraphedFineStep:
         N = self.N
         sdf = model.sdf.grid
         if self.taps is not None:
-            _abi.call("vx_smooth3d", ptr(sdf), ptr(self.sdf_s), ptr(self.tmp[0]), ptr(self.tmp[1]), X, Y, Z,
+            _abi.call("vx_smooth3d", ptr(sdf), ptr(self.sdf_s), None, None, X, Y, Z,
                       self.taps.ctypes.data, len(self.taps), st)
         else:
             self.sdf_s.copy_(sdf.reshape(X, Y, Z))
@@ -227,7 +234,8 @@ class GraphedFineStep:
         n_rows_dev = self.s2_off[N:]          # device S2
         self.dyn.copy_(self.dyn_host, non_blocking=True)
         self.d_sdf_s.zero_()
-        self.d_k0.zero_()
+        X, Y, Z = self.XYZ
+        _native.call("vx_grid_clear_touched", ptr(self.d_k0), ptr(self.k0_touched), X * Y * Z, 12, st)
         o, d, v, target = self.inp[0], self.inp[1], self.inp[2], self.inp[3]
         # compaction
         ray2 = torch.empty(cap, dtype=i32, device=dev)
@@ -333,10 +341,10 @@ class GraphedFineStep:
         bw.dX1, bw.dX2, bw.in_bf16 = ptr(dX1), ptr(dX2), int(self.bf16)
         bw.d_sdf_smooth, bw.d_k0 = ptr(self.d_sdf_s), ptr(self.d_k0)
         bw.n_rows_dev, bw.inv_s_dev = ptr(n_rows_dev), ptr(self.dyn)
+        bw.k0_touched = ptr(self.k0_touched)
         _abi.call_struct("vx_fine_backward", bw, st)
-        X, Y, Z = self.XYZ
         if self.taps is not None:
-            _abi.call("vx_smooth3d_adjoint", ptr(self.d_sdf_s), ptr(self.d_sdf), ptr(self.tmp[0]), ptr(self.tmp[1]),
+            _abi.call("vx_smooth3d_adjoint", ptr(self.d_sdf_s), ptr(self.d_sdf), None, None,
                       X, Y, Z, self.taps.ctypes.data, len(self.taps), 0, st)
         else:
             self.d_sdf.view(X, Y, Z).copy_(self.d_sdf_s)

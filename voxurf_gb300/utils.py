@@ -11,7 +11,9 @@ DenseGrid.total_variation_add_grad, already scaled) and ``tv_dense``; for
 such 5-D grid parameters the step runs TV add-grad + Adam + gradient reset
 in a single sweep (vx_grid_tv_adam_step), reading the old parameter buffer
 and writing a second one that is swapped in (ping-pong), and refreshes a
-BF16 shadow copy when ``shadow`` (a tensor) is given.
+BF16 shadow copy when ``shadow`` (a tensor) is given.  A group may also
+carry ``touched``: uint8 marks of the voxels where the gradient can be
+nonzero (vx_grid_tv_adam_step_touched reads the gradient only there).
 """
 from __future__ import annotations
 
@@ -116,10 +118,15 @@ class Adam(torch.optim.Optimizer):
         C, X, Y, Z = p.size(1), p.size(2), p.size(3), p.size(4)
         cl = C > 1 and not p.is_contiguous()
         shadow = group.get("shadow")
-        call("vx_grid_tv_adam_step", ptr(p), ptr(spare), ptr(g), ptr(state["exp_avg"]), ptr(state["exp_avg_sq"]),
-             ptr(per_lr), ptr(shadow), C, X, Y, Z, int(cl), 1, float(tv_w), int(bool(group.get("tv_dense", True))),
-             float(group["lr"]), float(beta1), float(beta2), float(group["eps"]), int(state["step"]),
-             0 if zero_grad else 0, st)
+        args = (ptr(p), ptr(spare), ptr(g), ptr(state["exp_avg"]), ptr(state["exp_avg_sq"]), ptr(per_lr),
+                ptr(shadow), C, X, Y, Z, int(cl), 1, float(tv_w), int(bool(group.get("tv_dense", True))),
+                float(group["lr"]), float(beta1), float(beta2), float(group["eps"]), int(state["step"]), 0)
+        touched = group.get("touched")
+        if touched is not None:
+            # the gradient is zero outside the marked voxels (the fused step's scatter)
+            call("vx_grid_tv_adam_step_touched", *args, ptr(touched), st)
+        else:
+            call("vx_grid_tv_adam_step", *args, st)
         old = p.data
         p.data = spare
         state["spare"] = old

@@ -50,10 +50,8 @@ def smooth_grid(src: torch.Tensor, taps: np.ndarray) -> torch.Tensor:
     """[X,Y,Z]-shaped smoothing through vx_smooth3d (returns a new tensor)."""
     X, Y, Z = src.shape[-3:]
     out = torch.empty((X, Y, Z), dtype=torch.float32, device=src.device)
-    t1 = torch.empty_like(out)
-    t2 = torch.empty_like(out)
     th = np.ascontiguousarray(taps, np.float32)
-    _abi.call("vx_smooth3d", ptr(src), ptr(out), ptr(t1), ptr(t2), X, Y, Z, th.ctypes.data, len(th), stream_ptr())
+    _abi.call("vx_smooth3d", ptr(src), ptr(out), None, None, X, Y, Z, th.ctypes.data, len(th), stream_ptr())
     return out
 
 
@@ -62,10 +60,8 @@ def smooth_grid_adjoint(grad_out: torch.Tensor, taps: np.ndarray, out: torch.Ten
     X, Y, Z = grad_out.shape[-3:]
     if out is None:
         out = torch.empty((X, Y, Z), dtype=torch.float32, device=grad_out.device)
-    t1 = torch.empty((X, Y, Z), dtype=torch.float32, device=grad_out.device)
-    t2 = torch.empty_like(t1)
     th = np.ascontiguousarray(taps, np.float32)
-    _abi.call("vx_smooth3d_adjoint", ptr(grad_out), ptr(out), ptr(t1), ptr(t2), X, Y, Z, th.ctypes.data, len(th),
+    _abi.call("vx_smooth3d_adjoint", ptr(grad_out), ptr(out), None, None, X, Y, Z, th.ctypes.data, len(th),
               int(accumulate), stream_ptr())
     return out
 
