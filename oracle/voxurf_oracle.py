@@ -6,7 +6,10 @@ run.py:600-659, the TV add-grad of grid.py:67-78 and lib/utils.py:Adam),
 runnable in float64 (the correctness oracle) or float32 (the timed CPU
 baseline).  The reference's CUDA ops come from oracle/ops.py.  Ray sampling
 and the mask lookup always run in float32 with the kernels' operation order
-so that sample sets are bit-identical to the GPU's.
+so that sample sets are bit-identical to the GPU's.  Threshold decisions
+downstream (fast_color_thres on FP64 weights) can meet ties at FP32
+precision; OracleCoarse.forward(device_keep=...) resolves those (weights
+within 1e-5 relative of the threshold) with the device's decision.
 
 The module takes its parameters from a voxurf_gb300 model's state (converted
 to channel-first layout and the oracle dtype), so both sides start from the
@@ -317,7 +320,11 @@ class OracleCoarse(nn.Module):
             mc = model.mask_cache
             self.mask = (mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
 
-    def forward(self, rays_o, rays_d, viewdirs, global_step=None, **rk):
+    def forward(self, rays_o, rays_d, viewdirs, global_step=None, device_keep=None, **rk):
+        """device_keep: optional set of (ray_id, step_id) pairs that a device
+        run kept after the fast_color_thres test.  A sample whose weight is
+        within 1e-5 relative of the threshold (a tie at FP32 precision) then
+        takes the device's decision, so that both sides shade the same set."""
         dt = self.dtype
         N = len(rays_o)
         stepdist = f32(rk["stepsize"] * np.float32(self.voxel_size))
@@ -348,6 +355,11 @@ class OracleCoarse(nn.Module):
         alpha = neus_alpha(viewdirs, ray_id, dist, sdf, gradient, inv_s)
         weights, _ = Alphas2WeightsOracle.apply(alpha, ray_id, N)
         m = weights > self.fast_color_thres
+        if device_keep is not None:
+            near = ((weights.detach() - self.fast_color_thres).abs() <= 1e-5 * self.fast_color_thres).nonzero()
+            for i in near.reshape(-1).tolist():
+                m[i] = (int(ray_id[i]), int(step_id[i])) in device_keep
+            self.ties = int(near.numel())
         trace("weights > thres", m)
         ray_pts, ray_id, step_id, alpha, gradient = ray_pts[m], ray_id[m], step_id[m], alpha[m], gradient[m]
         weights, alphainv_last = Alphas2WeightsOracle.apply(alpha, ray_id, N)
