@@ -215,17 +215,26 @@ struct FeatLayout {
   int planes;  // every displacement in (0, 2]: probes from shared planes
 };
 
-// Rows of a block staged in shared memory ([rows][ld] elements, written by
-// one thread each) copied to global memory as one contiguous range of
-// 16-byte chunks (coalesced; one thread per row writing 2-byte values would
-// touch a different cache line per thread and per column).  Requires
-// ld * sizeof(T) % 16 == 0 and a 16-byte aligned destination.
+// Rows of a block staged in shared memory, written by one thread each, then
+// copied to global memory one row per warp (coalesced 4-byte words; one
+// thread per row writing 2-byte values straight to global memory would touch
+// a different cache line per thread and per column).  The staged row stride
+// is the global stride plus one 4-byte word: an odd number of words, so the
+// 32 threads of a warp writing the same column of 32 rows hit 32 different
+// banks.  Requires ld * sizeof(T) % 4 == 0 and a 4-byte aligned destination.
+template <typename T>
+__host__ __device__ constexpr int64_t stage_ld(int64_t ld) {
+  return ld + 4 / (int64_t)sizeof(T);
+}
+
 template <typename T>
 __device__ __forceinline__ void copy_rows_out(const T* stage, T* dst, int n_rows, int64_t ld) {
-  const int64_t n16 = (int64_t)n_rows * ld * (int64_t)sizeof(T) / 16;
-  const uint4* s = reinterpret_cast<const uint4*>(stage);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-  for (int64_t i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+  const int words = (int)(ld * (int64_t)sizeof(T) / 4), swords = words + 1;
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(stage);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int r = warp; r < n_rows; r += nw)
+    for (int w = lane; w < words; w += 32) d[(int64_t)r * words + w] = s[r * swords + w];
 }
 
 // Host side: checks a feature configuration and converts it.

@@ -18,9 +18,13 @@
 // packed into that layout by the caller (vx_mlp_tc_pack) and copied to
 // shared memory once per CTA.
 //
-// Thread roles: 4 warps; warp w owns TMEM lanes / tile rows [32w, 32w+32)
-// in the epilogue; thread 0 issues the MMAs and the commit.  Every wait on
-// an mbarrier is bounded: on expiry the kernel records VX_ERR_TIMEOUT,
+// Thread roles: 8 warps; warps w and w+4 own TMEM lanes / tile rows
+// [32(w%4), +32) in the epilogue and split the 192 columns in halves;
+// thread 0 issues the MMAs and the commit.  Weights, biases and the output
+// layer arrive by bulk copies on the async proxy (one mbarrier); the next
+// input tile is prefetched with 16-byte cp.async (zero fill past the last
+// row) while the current tile's last layer runs.  Every wait on an
+// mbarrier is bounded: on expiry the kernel records VX_ERR_TIMEOUT,
 // releases its TMEM and returns.
 #include "common.cuh"
 
@@ -112,9 +116,9 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                : "memory");
 }
 
-// 32 consecutive FP32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, float v[32]) {
-  uint32_t r[32];
+// 32 consecutive FP32 columns of this thread's TMEM lane (raw bits; valid
+// after tc_wait_ld).
+__device__ __forceinline__ void tc_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
       "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -124,9 +128,22 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float v[32]) {
         "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
         "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// This thread's 96 columns [col0, col0 + 96) of its TMEM lane: three loads
+// in flight, one wait.
+__device__ __forceinline__ void tc_ld96(uint32_t taddr, uint32_t (&r)[3][32]) {
+  tc_ld32_async(taddr, r[0]);
+  tc_ld32_async(taddr + 32, r[1]);
+  tc_ld32_async(taddr + 64, r[2]);
+  tc_wait_ld();
+  // order every use of the loaded registers after the wait (empty volatile
+  // asms stay in program order with the wait and carry the dependency)
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 32; ++i) asm volatile("" : "+r"(r[j][i]));
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -251,16 +268,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
         // +bias, ReLU, BF16 -> As (the next layer's A operand): this thread's
         // row, columns [96*half, 96*half + 96)
         uint4* dst = reinterpret_cast<uint4*>(As);
-#pragma unroll 1
+        uint32_t v[3][32];
+        tc_ld96(tmem_row + 96 * half, v);
+#pragma unroll
         for (int j = 0; j < 3; ++j) {
           const int col0 = 96 * half + 32 * j;
-          float v[32];
-          tc_ld32(tmem_row + col0, v);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
+            const float4 bl = *reinterpret_cast<const float4*>(b + col0 + 8 * q);
+            const float4 bu = *reinterpret_cast<const float4*>(b + col0 + 8 * q + 4);
+            const float bb[8] = {bl.x, bl.y, bl.z, bl.w, bu.x, bu.y, bu.z, bu.w};
             float h[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) h[e] = fmaxf(v[8 * q + e] + b[col0 + 8 * q + e], 0.f);
+            for (int e = 0; e < 8; ++e) h[e] = fmaxf(__uint_as_float(v[j][8 * q + e]) + bb[e], 0.f);
             dst[(size_t)(col0 / 8 + q) * TC_M + 32 * quarter + lane] =
                 make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
           }
@@ -276,18 +296,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
         // last hidden layer: +bias, ReLU, rounded to BF16 like the GEMM path,
         // then this thread's share of the FP32 output layer
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-#pragma unroll 1
-        for (int j = 0; j < 3; ++j) {
-          const int col0 = 96 * half + 32 * j;
-          float v[32];
-          tc_ld32(tmem_row + col0, v);
+        uint32_t v[3][32];
+        tc_ld96(tmem_row + 96 * half, v);
 #pragma unroll
-          for (int e = 0; e < 32; ++e) {
-            const int col = col0 + e;
-            const float h = __bfloat162float(__float2bfloat16_rn(fmaxf(v[e] + b[col], 0.f)));
-            a0 += h * wh_s[col];
-            a1 += h * wh_s[TC_N + col];
-            a2 += h * wh_s[2 * TC_N + col];
+        for (int j = 0; j < 3; ++j) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int col = 96 * half + 32 * j + 4 * q;
+            const float4 bq = *reinterpret_cast<const float4*>(b + col);
+            const float4 w0 = *reinterpret_cast<const float4*>(wh_s + col);
+            const float4 w1 = *reinterpret_cast<const float4*>(wh_s + TC_N + col);
+            const float4 w2 = *reinterpret_cast<const float4*>(wh_s + 2 * TC_N + col);
+            const float bb[4] = {bq.x, bq.y, bq.z, bq.w};
+            const float x0[4] = {w0.x, w0.y, w0.z, w0.w}, x1[4] = {w1.x, w1.y, w1.z, w1.w};
+            const float x2[4] = {w2.x, w2.y, w2.z, w2.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float h =
+                  __bfloat162float(__float2bfloat16_rn(fmaxf(__uint_as_float(v[j][4 * q + e]) + bb[e], 0.f)));
+              a0 += h * x0[e];
+              a1 += h * x1[e];
+              a2 += h * x2[e];
+            }
           }
         }
         const int r = 32 * quarter + lane;

@@ -215,8 +215,8 @@ struct FeatParams {
   const int64_t* n_rows_dev;  // optional device row count (rows beyond it are skipped)
 };
 
-// STAGE: the block's rows are assembled in shared memory and written out as
-// contiguous 16-byte chunks (row strides of 16-byte multiples).
+// STAGE: the block's rows are assembled in shared memory (bank-conflict-free
+// padded stride) and written out one row per warp in coalesced words.
 template <typename T, int KK, bool STAGE>
 __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
   extern __shared__ __align__(16) unsigned char feat_stage[];
@@ -226,13 +226,14 @@ __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
   if (P.n_rows_dev) n = min(n, *P.n_rows_dev);
   const bool valid = row < n;
   T* s1 = reinterpret_cast<T*>(feat_stage);
-  T* s2 = s1 + (int64_t)blockDim.x * P.ld1;
+  const int64_t sl1 = stage_ld<T>(P.ld1), sl2 = stage_ld<T>(P.ld2);
+  T* s2 = s1 + (int64_t)blockDim.x * sl1;
   if (valid) {
     const int r = P.ray2[row];
     const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
     const float v[3] = {__ldg(P.viewdirs + 3 * r), __ldg(P.viewdirs + 3 * r + 1), __ldg(P.viewdirs + 3 * r + 2)};
-    T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * P.ld1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
-    T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * P.ld2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
+    T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * sl1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
+    T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * sl2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
     float g1[3];
     fine_feature_rows<T, KK>(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
     for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
@@ -1177,9 +1178,9 @@ int vx_fine_features(const vx_fine_features_args* A, void* stream) {
   cudaStream_t st = as_stream(stream);
   // staged rows: strides of 16-byte multiples, aligned bases, <= 48 KB of shared memory
   const size_t esz = A->out_bf16 ? 2 : 4;
-  const size_t shm = 128 * (size_t)(A->ld1 + A->ld2) * esz;
-  const bool stage = (A->ld1 * esz) % 16 == 0 && (A->ld2 * esz) % 16 == 0 && shm <= 48 * 1024 &&
-                     ((reinterpret_cast<uintptr_t>(A->X1) | reinterpret_cast<uintptr_t>(A->X2)) & 15) == 0;
+  const size_t shm = 128 * (size_t)(A->ld1 + A->ld2 + 2 * (4 / esz)) * esz;
+  const bool stage = (A->ld1 * esz) % 4 == 0 && (A->ld2 * esz) % 4 == 0 && shm <= 48 * 1024 &&
+                     ((reinterpret_cast<uintptr_t>(A->X1) | reinterpret_cast<uintptr_t>(A->X2)) & 3) == 0;
 #define VX_FEAT_LAUNCH(T, KK)                                           \
   if (stage)                                                            \
     features_fine_kernel<T, KK, true><<<b, 128, shm, st>>>(P);          \

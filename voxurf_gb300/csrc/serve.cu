@@ -289,9 +289,9 @@ struct ServeFeatParams {
   void* X2;
 };
 
-// STAGE: rows assembled in shared memory, written out as contiguous 16-byte
-// chunks (the logit columns [cols2, cols2+3) are zero until the rgbnet
-// output layer fills them).
+// STAGE: rows assembled in shared memory (bank-conflict-free padded stride),
+// written out one row per warp in coalesced words (the logit columns
+// [cols2, cols2+3) are zero until the rgbnet output layer fills them).
 template <typename T, int KK, bool STAGE>
 __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
@@ -300,7 +300,8 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
   const int64_t row0 = (int64_t)blockIdx.x * blockDim.x;
   const int64_t row = row0 + threadIdx.x;
   T* s1 = reinterpret_cast<T*>(feat_stage);
-  T* s2 = s1 + (int64_t)blockDim.x * P.ld1;
+  const int64_t sl1 = stage_ld<T>(P.ld1), sl2 = stage_ld<T>(P.ld2);
+  T* s2 = s1 + (int64_t)blockDim.x * sl1;
   if (row < P.n_rows) {
     const int r = P.ray2[row];
     const SceneK& S = sh[P.ray_scene[r]];  // validated by the march
@@ -316,8 +317,8 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
     const RayFrame f = ray_frame(o, d, S.g.mn, S.g.mx, S.near, S.stepdist);
     float p[3];
     sample_point(f, S.stepdist, k, p);
-    T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * P.ld1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
-    T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * P.ld2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
+    T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * sl1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
+    T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * sl2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
     float g1[3];
     fine_feature_rows<T, KK>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
     for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
@@ -624,13 +625,13 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
   P.X2 = X2;
   const unsigned b = (unsigned)((n_rows + 127) / 128);
   cudaStream_t st = as_stream(stream);
-  // staged rows: strides of 16-byte multiples, aligned bases, static + dynamic
+  // staged rows: strides of 4-byte multiples, aligned bases, static + dynamic
   // shared memory within the default 48 KB
   const size_t esz = out_bf16 ? 2 : 4;
-  const size_t shm = 128 * (size_t)(ld1 + ld2) * esz;
-  const bool stage = ((size_t)ld1 * esz) % 16 == 0 && ((size_t)ld2 * esz) % 16 == 0 &&
+  const size_t shm = 128 * (size_t)(ld1 + ld2 + 2 * (4 / esz)) * esz;
+  const bool stage = ((size_t)ld1 * esz) % 4 == 0 && ((size_t)ld2 * esz) % 4 == 0 &&
                      shm + sizeof(SceneK) * VX_SERVE_MAX_SCENES <= 48 * 1024 &&
-                     ((reinterpret_cast<uintptr_t>(X1) | reinterpret_cast<uintptr_t>(X2)) & 15) == 0;
+                     ((reinterpret_cast<uintptr_t>(X1) | reinterpret_cast<uintptr_t>(X2)) & 3) == 0;
 #define VX_FEAT_LAUNCH(T, KK)                                    \
   if (stage)                                                     \
     serve_features_kernel<T, KK, true><<<b, 128, shm, st>>>(P);  \
