@@ -67,6 +67,10 @@ def parse():
     p.add_argument("--no-long", action="store_true", help="skip the long-ray (384^3, stepsize 0.25) measurement")
     p.add_argument("--no-eikonal", action="store_true",
                    help="skip the eikonal-training (coarse 96^3, 8192/32768 rays) measurement")
+    p.add_argument("--no-mesh", action="store_true", help="skip the 512^3 mesh-extraction field measurement")
+    p.add_argument("--micro", choices=["smooth", "mlp_tc"], default=None,
+                   help="single-kernel timing instead of the step (profiling): the Gaussian smoothing sweep "
+                        "on a --grid^3 grid, or the fused tensor-core MLP against the GEMM path")
     p.add_argument("--render-requests", type=int, default=120)
     p.add_argument("--render-only", action="store_true", help="only the render-server measurement (profiling)")
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
@@ -182,6 +186,9 @@ def run_ours(args, world, rank, local):
     dev = torch.device("cuda", local)
     if args.render_only:
         print(json.dumps({"render": run_render(args, dev)}))
+        return
+    if args.micro:
+        print(json.dumps({"micro": run_micro(args, dev)}))
         return
     rk = dict(configs.FINE_RENDER_KWARGS)
     n_b = args.warmup + args.steps
@@ -304,6 +311,9 @@ def run_ours(args, world, rank, local):
     eikonal = None
     if not args.no_eikonal and R == 256:
         eikonal = run_eikonal(args, dev)
+    mesh = None
+    if not args.no_mesh and R == 256:
+        mesh = run_mesh_query(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -324,6 +334,7 @@ def run_ours(args, world, rank, local):
             "render": render,
             "long_rays": long_rays,
             "eikonal_train": eikonal,
+            "mesh_query": mesh,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -378,6 +389,117 @@ def run_long_rays(args, dev):
         torch.cuda.empty_cache()
     out["speedup_bf16_vs_fp32"] = out["bf16_graphed"]["rays_per_s"] / out["fp32"]["rays_per_s"]
     return out
+
+
+def _event_ms(fn, warmup, steps):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_micro(args, dev):
+    """One kernel in isolation (CUDA events on the launching stream, warm-up
+    launches first): `smooth` = vx_smooth3d / vx_smooth3d_adjoint (5^3,
+    sigma 0.8) on a --grid^3 FP32 grid, 8 algorithmic bytes per voxel (12
+    with accumulation); `mlp_tc` = the fused tcgen05 colour MLP
+    (70(80) -> 192 x3 -> 3, BF16 rows) against the cuBLAS GEMM path with
+    the head kernel, at 131,072 and 2,097,152 rows."""
+    import numpy as np
+    import torch
+    import torch.nn as nn
+
+    from voxurf_gb300 import _abi
+    from voxurf_gb300._torch import ptr, stream_ptr
+
+    W, S = max(args.warmup, 3), max(args.steps, 10)
+    out = {"kind": args.micro}
+    if args.micro == "smooth":
+        from voxurf_gb300.voxurf_fine import gaussian_taps, smooth_grid, smooth_grid_adjoint
+
+        R = args.grid
+        a = torch.randn((R, R, R), device=dev, generator=torch.Generator(dev).manual_seed(0))
+        o = torch.empty_like(a)
+        taps = gaussian_taps(5, 0.8)
+        for name, fn, b in (("forward", lambda: smooth_grid(a, taps), 8),
+                            ("adjoint", lambda: smooth_grid_adjoint(a, taps, out=o), 8),
+                            ("adjoint_accumulate", lambda: smooth_grid_adjoint(a, taps, out=o, accumulate=True), 12)):
+            ms = _event_ms(fn, W, S)
+            out[name] = {"us": ms * 1000, "gbs": R ** 3 * b / ms / 1e6}
+        out["grid"] = R
+        return out
+    gen = torch.Generator().manual_seed(0)
+    net = nn.Sequential(nn.Linear(70, 192), nn.ReLU(), nn.Sequential(nn.Linear(192, 192), nn.ReLU()),
+                        nn.Sequential(nn.Linear(192, 192), nn.ReLU()), nn.Linear(192, 3))
+    for m in net.modules():
+        if isinstance(m, nn.Linear):
+            m.weight.data = torch.randn(m.weight.shape, generator=gen) * (1.0 / np.sqrt(m.in_features))
+            m.bias.data = torch.randn(m.bias.shape, generator=gen) * 0.1
+    net = net.to(dev)
+    from voxurf_gb300.mlp import TensorCoreMLP
+
+    tc = TensorCoreMLP(net, 80)
+    lin = [m for m in net.modules() if isinstance(m, nn.Linear)]
+    W0 = torch.zeros((192, 80), dtype=torch.bfloat16, device=dev)
+    W0[:, :70] = lin[0].weight.to(torch.bfloat16)
+    Ws = [W0, lin[1].weight.to(torch.bfloat16), lin[2].weight.to(torch.bfloat16)]
+    bs = [m.bias.to(torch.bfloat16) for m in lin[:3]]
+    Wh, bh = lin[3].weight.float().contiguous(), lin[3].bias.float().contiguous()
+    for n in (131072, 2097152):
+        X = torch.zeros((n, 80), dtype=torch.bfloat16, device=dev)
+        X[:, :70] = torch.randn((n, 70), generator=gen).to(dev, torch.bfloat16)
+        res = torch.empty((n, 3), device=dev)
+
+        def gemm():
+            h = X
+            for Wl, bl in zip(Ws, bs):
+                h = torch._addmm_activation(bl, h, Wl.t())
+            _abi.call("vx_mlp_head", ptr(h), n, 192, 192, 1, ptr(Wh), ptr(bh), None, ptr(res), None, 0, 0,
+                      stream_ptr())
+
+        flops = n * 2 * (80 * 192 + 2 * 192 * 192 + 3 * 192)
+        row = {}
+        for name, fn in (("gemm", gemm), ("tc", lambda: tc.forward(X, res))):
+            ms = _event_ms(fn, W, S)
+            row[name] = {"ms": ms, "tflops": flops / ms / 1e9}
+        out[f"rows_{n}"] = row
+    return out
+
+
+MESH_R = 512               # extract_geometry resolution of the reference's final mesh (run.py:798-799)
+
+
+def run_mesh_query(args, dev):
+    """Dense field for mesh extraction on the 256^3 fine model: the 512^3
+    lattice over the bbox (smoothing of the SDF grid + one field launch,
+    537 MB written), CUDA events around model.extract_fields."""
+    import torch
+
+    from voxurf_gb300 import configs
+
+    model = configs.build_fine_model(R, "fp32", device=dev, seed=0, mask_voxels=MASK_VOXELS)
+    bmin, bmax = model.xyz_min, model.xyz_max
+    ms = _event_ms(lambda: model.extract_fields(bmin, bmax, MESH_R), 2, 5)
+    grid = model.mesh_sdf_grid()
+    from voxurf_gb300.voxurf_fine import extract_fields
+
+    ms_field = _event_ms(lambda: extract_fields(grid, model.xyz_min, model.xyz_max, bmin, bmax, MESH_R), 2, 5)
+    peak, _ = measured_peaks()
+    field_bytes = MESH_R ** 3 * 4
+    del model, grid
+    torch.cuda.empty_cache()
+    return {"workload": f"extract_fields {MESH_R}^3 over the bbox of the 256^3 fine model (-smoothed SDF)",
+            "ms": ms, "field_ms": ms_field, "points_per_s": MESH_R ** 3 / (ms / 1000.0),
+            "field_write_gbs": field_bytes / (ms_field / 1000.0) / 1e9,
+            "field_frac_of_hbm": field_bytes / (ms_field / 1000.0) / 1e9 / peak}
 
 
 EIK_R = 96                 # differentiation workload: coarse grids/MLP, eikonal 0.1

@@ -244,6 +244,15 @@ int vx_grid_sample(const float* grid, int64_t C, int channel_last, const vx_grid
 int vx_grid_sample_backward(const float* grad_out, int64_t C, int channel_last, const vx_grid_geom* geom,
                             const float* xyz, int64_t n_pts, float* grad_grid, void* stream);
 
+/* Dense field for mesh extraction: extract_fields (lib/dvgo_ori.py:679-693)
+ * with query_func = grid_sampler(pts, sign * sdf) (voxurf_fine.py:894-910,
+ * voxurf_coarse.py:652-665).  out [R,R,R] (z fastest) = sign x trilinear
+ * lookup of the 1-channel [X,Y,Z] grid at the lattice point
+ * (linspace(bound_min[a], bound_max[a], R) per axis, as torch.linspace
+ * forms it).  R <= 2048. */
+int vx_sdf_field(const float* sdf, const vx_grid_geom* grid, const float* bound_min, const float* bound_max,
+                 int64_t R, float sign, float* out, void* stream);
+
 /* Ray march: sample_ray (voxurf_fine.py:593-617) + mask (:631-636) +
  * grid_sampler with FD gradient (:640, 502-534) + neus alpha (:643, 463-500)
  * + alpha/weight compaction (:647-676) + Alphas2Weights (:667, 981-988). */

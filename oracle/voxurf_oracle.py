@@ -53,6 +53,18 @@ def grid_sample_pts(grid, xyz, xyz_min, xyz_max):
     return out.reshape(C, -1).T
 
 
+def extract_fields(grid, xyz_min, xyz_max, bound_min, bound_max, resolution, sign=-1.0):
+    """extract_fields (dvgo_ori.py:679-693) with the mesh query of
+    Voxurf.extract_geometry (voxurf_fine.py:903, voxurf_coarse.py:658):
+    grid_sampler(pts, sign * grid) on the lattice linspace(bound_min,
+    bound_max, R) per axis (meshgrid 'ij'), all chunks at once."""
+    axes = [torch.linspace(float(bound_min[a]), float(bound_max[a]), int(resolution)) for a in range(3)]
+    xx, yy, zz = torch.meshgrid(*axes, indexing="ij")
+    pts = torch.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], -1).to(grid.dtype)
+    val = grid_sample_pts(sign * grid, pts, xyz_min.to(grid.dtype), xyz_max.to(grid.dtype))
+    return val.reshape(int(resolution), int(resolution), int(resolution))
+
+
 def sample_sdfs(xyz, grid, displace_list, xyz_min, xyz_max, voxel_size, use_grad_norm):
     """voxurf_fine.py:537-577."""
     n = xyz.shape[0]

@@ -15,7 +15,7 @@ script stubs them:
   * Tensor.cuda / Module.cuda -> no-ops.
 PYTHONDONTWRITEBYTECODE keeps the read-only reference tree clean.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh]   (default: all)
 """
 from __future__ import annotations
 
@@ -245,12 +245,41 @@ def ops_fixture(path, seed=5):
     print("wrote", path)
 
 
+def mesh_fixture(path, seed=6):
+    """extract_fields (lib/dvgo_ori.py:679-693) with the fine model's mesh
+    query (voxurf_fine.py:894-910: grid_sampler(pts, -sdf_grid) on the grid
+    smoothed by init_smooth_conv_test_k3, sigma 0.5), in FP32 as the
+    reference runs it, with 8^3 chunks so that chunk borders are covered."""
+    import lib.dvgo_ori as rdvgo
+    import lib.voxurf_fine as rf
+
+    g = torch.Generator().manual_seed(seed)
+    sdf = torch.randn((1, 1, 11, 13, 9), generator=g)
+    holder = types.SimpleNamespace(sdf=types.SimpleNamespace(grid=sdf), nearest=False,
+                                   xyz_min=torch.tensor([-1.0, -0.8, -1.2]), xyz_max=torch.tensor([1.1, 0.9, 0.7]))
+    conv = rf.Voxurf._gaussian_3dconv(holder, ksize=3, sigma=0.5)
+    with torch.no_grad():
+        grid_s = conv(sdf)
+    bmin, bmax = torch.tensor([-0.9, -0.7, -1.0]), torch.tensor([1.0, 0.85, 0.6])
+    u = rdvgo.extract_fields(bmin, bmax, 21, lambda pts: rf.Voxurf.grid_sampler(holder, pts, -grid_s), N=8)
+    np.savez_compressed(path, sdf=sdf.numpy(), xyz_min=holder.xyz_min.numpy(), xyz_max=holder.xyz_max.numpy(),
+                        bound_min=bmin.numpy(), bound_max=bmax.numpy(), resolution=np.array(21), sigma=np.array(0.5),
+                        field=u)
+    print("wrote", path)
+
+
 def main():
     install_stubs()
     torch.set_default_dtype(torch.float32)
-    ops_fixture(os.path.join(HERE, "ops_golden.npz"))
-    fine_step_fixture(os.path.join(HERE, "fine_step_golden.npz"))
-    coarse_step_fixture(os.path.join(HERE, "coarse_step_golden.npz"))
+    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh"]
+    if "ops" in which:
+        ops_fixture(os.path.join(HERE, "ops_golden.npz"))
+    if "fine" in which:
+        fine_step_fixture(os.path.join(HERE, "fine_step_golden.npz"))
+    if "coarse" in which:
+        coarse_step_fixture(os.path.join(HERE, "coarse_step_golden.npz"))
+    if "mesh" in which:
+        mesh_fixture(os.path.join(HERE, "mesh_golden.npz"))
 
 
 if __name__ == "__main__":

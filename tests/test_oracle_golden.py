@@ -51,6 +51,19 @@ def test_dense_grid_restatement():
     np.testing.assert_array_equal(out.numpy(), OPS["dg_out"])
 
 
+def test_extract_fields_restatement():
+    """The oracle's extract_fields + mesh query against the reference's own
+    dvgo_ori.extract_fields with Voxurf.grid_sampler (FP32, 8^3 chunks)."""
+    from oracle.voxurf_oracle import extract_fields
+
+    M = np.load(os.path.join(HERE, "mesh_golden.npz"))
+    k = torch.from_numpy(gaussian_kernel3d(3, float(M["sigma"])))
+    grid = smooth3d(torch.from_numpy(M["sdf"]), k)
+    u = extract_fields(grid, torch.from_numpy(M["xyz_min"]), torch.from_numpy(M["xyz_max"]), M["bound_min"],
+                       M["bound_max"], int(M["resolution"]))
+    np.testing.assert_allclose(u.numpy(), M["field"], rtol=1e-6, atol=1e-7)
+
+
 def test_smoothing_restatement():
     k = torch.from_numpy(gaussian_kernel3d(5, 0.8))
     out = smooth3d(torch.from_numpy(OPS["smooth_in"]), k)

@@ -187,6 +187,8 @@ def _declare():
         fn = getattr(lib, name)
         fn.argtypes = [P, I64, C.c_int, C.POINTER(GridGeom), P, I64, P, P]
         fn.restype = C.c_int
+    lib.vx_sdf_field.argtypes = [P, C.POINTER(GridGeom), P, P, I64, F, P, P]
+    lib.vx_sdf_field.restype = C.c_int
     lib.vx_sdf_gradient_grid.argtypes = [P, P, I64, I64, I64, F, C.c_int, P]
     lib.vx_sdf_gradient_grid.restype = C.c_int
     lib.vx_sdf_gradient_grid_adjoint.argtypes = [P, P, I64, I64, I64, F, C.c_int, C.c_int, P]
@@ -224,4 +226,5 @@ def call(name: str, *args) -> None:
 def struct_names() -> list[str]:
     return list(_STRUCT_FNS) + ["vx_smooth3d", "vx_smooth3d_adjoint", "vx_grid_sample", "vx_grid_sample_backward",
                                 "vx_sdf_gradient_grid", "vx_sdf_gradient_grid_adjoint",
-                                "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv"] + list(_SERVE_SIGNATURES)
+                                "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv",
+                                "vx_sdf_field"] + list(_SERVE_SIGNATURES)

@@ -24,7 +24,8 @@ from . import _abi, _native
 from . import grid as grid_mod
 from ._torch import ptr, stream_ptr
 from .mlp import apply_mlp
-from .voxurf_fine import FineFrame, gaussian_taps, max_steps_bound, smooth_grid, smooth_grid_adjoint
+from .voxurf_fine import FineFrame, gaussian_taps, marching_cubes, max_steps_bound, smooth_grid, smooth_grid_adjoint
+from .voxurf_fine import extract_fields as _extract_fields
 
 
 def sdf_gradient_grid(sdf: torch.Tensor, voxel_size: float) -> torch.Tensor:
@@ -292,6 +293,27 @@ class Voxurf(nn.Module):
     def sdf_total_variation_add_grad(self, weight, dense_mode):
         w = weight * self.world_size.max() / 128
         self.sdf.total_variation_add_grad(w, w, w, dense_mode)
+
+    # -- mesh extraction (voxurf_coarse.py:652-665) ---------------------------
+    @torch.no_grad()
+    def mesh_sdf_grid(self) -> torch.Tensor:
+        g = self.sdf.grid.detach()
+        if self.smooth_sdf:
+            return smooth_grid(g, self.smooth_taps)
+        return g.reshape(g.shape[-3:]).float().contiguous()
+
+    @torch.no_grad()
+    def extract_fields(self, bound_min, bound_max, resolution=128) -> torch.Tensor:
+        """[R, R, R] field -sdf on the lattice (device tensor)."""
+        if resolution is None:
+            resolution = int(self.world_size[0])
+        return _extract_fields(self.mesh_sdf_grid(), self.xyz_min, self.xyz_max, bound_min, bound_max, resolution)
+
+    def extract_geometry(self, bound_min, bound_max, resolution=128, threshold=0.0, **kwargs):
+        if resolution is None:
+            resolution = int(self.world_size[0])
+        u = self.extract_fields(bound_min, bound_max, resolution).cpu().numpy()
+        return marching_cubes(u, threshold, bound_min, bound_max, resolution)
 
     def k0_total_variation_add_grad(self, weight, dense_mode):
         w = weight * self.world_size.max() / 128

@@ -24,6 +24,7 @@ the SDF grid, alpha, normals and the transmittance stay FP32 (FP64 carry).
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from copy import deepcopy
 
@@ -64,6 +65,41 @@ def smooth_grid_adjoint(grad_out: torch.Tensor, taps: np.ndarray, out: torch.Ten
     _abi.call("vx_smooth3d_adjoint", ptr(grad_out), ptr(out), None, None, X, Y, Z, th.ctypes.data, len(th),
               int(accumulate), stream_ptr())
     return out
+
+
+@torch.no_grad()
+def extract_fields(sdf_grid: torch.Tensor, xyz_min, xyz_max, bound_min, bound_max, resolution: int,
+                   sign: float = -1.0) -> torch.Tensor:
+    """extract_fields (lib/dvgo_ori.py:679-693) with query_func =
+    grid_sampler(pts, sign * sdf_grid): the [R, R, R] field over the lattice
+    linspace(bound_min, bound_max, R)^3 in one launch (vx_sdf_field), left
+    on the device."""
+    X, Y, Z = sdf_grid.shape[-3:]
+    src = sdf_grid.reshape(X, Y, Z).float().contiguous()
+    geom = grid_mod.grid_geom((X, Y, Z), grid_mod.host_values(xyz_min), grid_mod.host_values(xyz_max))
+    R = int(resolution)
+    out = torch.empty((R, R, R), dtype=torch.float32, device=src.device)
+    bmin = np.ascontiguousarray([float(v) for v in bound_min], np.float32)
+    bmax = np.ascontiguousarray([float(v) for v in bound_max], np.float32)
+    _abi.call("vx_sdf_field", ptr(src), ctypes.byref(geom), bmin.ctypes.data, bmax.ctypes.data, R, float(sign),
+              ptr(out), stream_ptr(src.device))
+    return out
+
+
+def marching_cubes(u: np.ndarray, threshold: float, bound_min, bound_max, resolution: int):
+    """extract_geometry (lib/dvgo_ori.py:695-703): marching cubes of the host
+    copy of the field (PyMCubes, as the reference), vertices mapped back to
+    [bound_min, bound_max]."""
+    try:
+        import mcubes
+    except ImportError as e:  # the field itself comes from extract_fields
+        raise RuntimeError("marching cubes needs PyMCubes (mcubes), which is not installed; "
+                           "extract_fields returns the [R,R,R] field for any host-side mesher") from e
+    vertices, triangles = mcubes.marching_cubes(u, threshold)
+    b_max = np.asarray([float(v) for v in bound_max], np.float64)
+    b_min = np.asarray([float(v) for v in bound_min], np.float64)
+    vertices = vertices / (resolution - 1.0) * (b_max - b_min)[None, :] + b_min[None, :]
+    return vertices, triangles
 
 
 def max_steps_bound(xyz_min, xyz_max, stepdist: float) -> int:
@@ -437,6 +473,34 @@ class Voxurf(nn.Module):
     def sdf_total_variation_add_grad(self, weight, dense_mode):
         w = weight * self.world_size.max() / 128
         self.sdf.total_variation_add_grad(w, w, w, dense_mode)
+
+    # -- mesh extraction (voxurf_fine.py:894-910) ----------------------------
+    @torch.no_grad()
+    def mesh_sdf_grid(self, smooth: bool = True, sigma: float = 0.5) -> torch.Tensor:
+        """The grid extract_geometry queries: smooth_conv(sdf) when the model
+        smooths, else the 3^3 Gaussian test kernel (init_smooth_conv_test_k3)
+        when `smooth`, else the raw grid."""
+        g = self.sdf.grid.detach()
+        if self.smooth_sdf:
+            return smooth_grid(g, self.smooth_taps)
+        if smooth:
+            return smooth_grid(g, gaussian_taps(3, sigma))
+        return g.reshape(g.shape[-3:]).float().contiguous()
+
+    @torch.no_grad()
+    def extract_fields(self, bound_min, bound_max, resolution=128, smooth=True, sigma=0.5) -> torch.Tensor:
+        """[R, R, R] field -sdf on the lattice (device tensor)."""
+        if resolution is None:
+            resolution = int(self.world_size[0])
+        return extract_fields(self.mesh_sdf_grid(smooth, sigma), self.xyz_min, self.xyz_max, bound_min, bound_max,
+                              resolution)
+
+    def extract_geometry(self, bound_min, bound_max, resolution=128, threshold=0.0, smooth=True, sigma=0.5,
+                         **kwargs):
+        if resolution is None:
+            resolution = int(self.world_size[0])
+        u = self.extract_fields(bound_min, bound_max, resolution, smooth, sigma).cpu().numpy()
+        return marching_cubes(u, threshold, bound_min, bound_max, resolution)
 
     def density_total_variation(self, sdf_tv=0, smooth_grad_tv=0, grad_tv=0, smooth_sdf_tv=0):
         """voxurf_fine.py:412-421.  smooth_grad_tv runs on the sm_103a kernels;
