@@ -278,8 +278,25 @@ typedef struct {
   int32_t* n1;              /* out [N] kept samples (alpha > thres, to stop)   */
   int32_t* n2;              /* out [N] shaded samples (weight > thres)         */
   float* alphainv_last;     /* out [N]                                         */
+  /* optional MaskCache density mask (voxurf_fine.py:917-942; exclusive with
+     `mask`): a sample is kept when 1 - exp(-softplus(trilinear(
+     mask_density) + mask_act_shift) * mask_voxel_size_ratio) >= mask_thres */
+  const float* mask_density; /* [X,Y,Z] max-pooled density (NULL: none)       */
+  vx_grid_geom mask_dgrid;
+  float mask_act_shift, mask_voxel_size_ratio, mask_thres;
 } vx_fine_march_args;
 int vx_fine_march(const vx_fine_march_args* args, void* stream);
+
+/* MaskCache.forward (voxurf_fine.py:930-942): out[i] = 1 when
+ * 1 - exp(-softplus(trilinear(density, xyz[i]) + act_shift) *
+ * voxel_size_ratio) >= thres.  density [X,Y,Z] (already max-pooled). */
+int vx_density_mask(const float* density, const vx_grid_geom* dgrid, float act_shift, float voxel_size_ratio,
+                    float thres, const float* xyz, int64_t n, uint8_t* out, void* stream);
+/* Voxurf.hit_coarse_geo (voxurf_fine.py:579-591): hit[r] = 1 when any
+ * in-bbox sample of ray r (sample_pts_on_rays with far = 1e9) lies in the
+ * mask of `args` (bool `mask` or `mask_density`; one of them is required).
+ * Reads rays_o, rays_d, n_rays, near, stepdist, grid and the mask fields. */
+int vx_hit_coarse_geo(const vx_fine_march_args* args, uint8_t* hit, void* stream);
 
 /* Dense rows of the shaded samples, ray-major (s2_off = exclusive scan of n2,
  * [N+1], e.g. from vx_exclusive_scan_i32). */
@@ -593,6 +610,11 @@ typedef struct {
                                the march skips runs of samples in empty cells */
   int64_t occ_X, occ_Y, occ_Z;
   int32_t occ_block;
+  /* optional MaskCache density mask (as in vx_fine_march_args; exclusive
+     with `mask` and `occ`) */
+  const float* mask_density;
+  vx_grid_geom mask_dgrid;
+  float mask_act_shift, mask_voxel_size_ratio, mask_thres;
 } vx_scene_desc;
 
 /* Block occupancy of a mask grid for empty-space skipping: cell (I,J,K) of

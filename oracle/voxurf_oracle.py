@@ -53,6 +53,33 @@ def grid_sample_pts(grid, xyz, xyz_min, xyz_max):
     return out.reshape(C, -1).T
 
 
+def maskcache_query(density, xyz_min, xyz_max, act_shift, voxel_size_ratio, thres, xyz):
+    """MaskCache.forward (voxurf_fine.py:930-942, bilinear mode) in FP32 on
+    the already max-pooled density [1,1,X,Y,Z]: alpha >= thres."""
+    d = grid_sample_pts(density.float(), xyz.float(), xyz_min.float(), xyz_max.float())[:, 0]
+    alpha = 1 - torch.exp(-F.softplus(d + act_shift) * voxel_size_ratio)
+    return alpha >= thres
+
+
+def _mask_state(model):
+    """The oracle's copy of a model's mask cache: ('grid', mask, scale,
+    shift) for a MaskGrid, ('density', density, xyz_min, xyz_max, act_shift,
+    voxel_size_ratio, thres) for a MaskCache, or None."""
+    mc = model.mask_cache
+    if mc is None:
+        return None
+    if hasattr(mc, "density"):
+        return ("density", mc.density.detach().cpu().float(), mc.xyz_min.cpu().float(), mc.xyz_max.cpu().float(),
+                float(mc.act_shift), float(mc.voxel_size_ratio), float(mc.mask_cache_thres))
+    return ("grid", mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
+
+
+def _apply_mask(mask, pts32):
+    if mask[0] == "grid":
+        return RenderUtilsOracle.maskcache_lookup(mask[1], pts32, mask[2], mask[3])
+    return maskcache_query(*mask[1:], pts32)
+
+
 def extract_fields(grid, xyz_min, xyz_max, bound_min, bound_max, resolution, sign=-1.0):
     """extract_fields (dvgo_ori.py:679-693) with the mesh query of
     Voxurf.extract_geometry (voxurf_fine.py:903, voxurf_coarse.py:658):
@@ -153,10 +180,7 @@ class OracleFine(nn.Module):
                   "sdf_feat", "k_sdf_feat"):
             setattr(self, k, getattr(model, k))
         self.s_val = model.s_val.clone().float().cpu()
-        self.mask = None
-        if model.mask_cache is not None:
-            mc = model.mask_cache
-            self.mask = (mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
+        self.mask = _mask_state(model)
         # None, or a dict holding the detached rgbnet logits of a base
         # forward (recorded on first use, then reused): see forward()
         self.frozen = None
@@ -187,7 +211,7 @@ class OracleFine(nn.Module):
         inb = ~mask_outbbox
         ray_pts32, ray_id, step_id = ray_pts[inb], ray_id[inb], step_id[inb]
         if self.mask is not None:
-            m = ru.maskcache_lookup(self.mask[0], ray_pts32, self.mask[1], self.mask[2])
+            m = _apply_mask(self.mask, ray_pts32)
             ray_pts32, ray_id, step_id = ray_pts32[m], ray_id[m], step_id[m]
         ray_pts = ray_pts32.to(dt)
         viewdirs = viewdirs.cpu().to(dt)
@@ -327,10 +351,7 @@ class OracleCoarse(nn.Module):
         for k in ("s_ratio", "s_start", "s_learn", "step_start"):
             setattr(self, k, getattr(model, k))
         self.s_val = model.s_val.clone().float().cpu()
-        self.mask = None
-        if model.mask_cache is not None:
-            mc = model.mask_cache
-            self.mask = (mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
+        self.mask = _mask_state(model)
 
     def forward(self, rays_o, rays_d, viewdirs, global_step=None, device_keep=None, **rk):
         """device_keep: optional set of (ray_id, step_id) pairs that a device
@@ -346,7 +367,7 @@ class OracleCoarse(nn.Module):
         inb = ~mask_outbbox
         ray_pts32, ray_id, step_id = ray_pts[inb], ray_id[inb], step_id[inb]
         if self.mask is not None:
-            m = ru.maskcache_lookup(self.mask[0], ray_pts32, self.mask[1], self.mask[2])
+            m = _apply_mask(self.mask, ray_pts32)
             ray_pts32, ray_id, step_id = ray_pts32[m], ray_id[m], step_id[m]
         ray_pts = ray_pts32.to(dt)
         viewdirs = viewdirs.cpu().to(dt)

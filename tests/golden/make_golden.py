@@ -12,10 +12,12 @@ script stubs them:
     out.index_add(0, index, src) (same sum);
   * torch.utils.cpp_extension.load -> the oracle's restatement of the CUDA
     ops (oracle/ops.py), since no GPU exists here;
-  * Tensor.cuda / Module.cuda -> no-ops.
+  * Tensor.cuda / Module.cuda -> no-ops;
+  * torch.load -> weights_only=False (the torch 1.10 behaviour the
+    reference's checkpoint loading relies on).
 PYTHONDONTWRITEBYTECODE keeps the read-only reference tree clean.
 
-    python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh]   (default: all)
+    python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt]   (default: all)
 """
 from __future__ import annotations
 
@@ -89,6 +91,10 @@ def install_stubs():
     # and float32 under model.double(), voxurf_fine.py:61)
     torch.Tensor.cuda = lambda self, *a, **k: self.data if isinstance(self, torch.nn.Parameter) else self
     torch.nn.Module.cuda = lambda self, *a, **k: self
+    # the reference targets torch 1.10, whose torch.load unpickles the numpy
+    # arrays run.py stores in checkpoints (MaskCache_kwargs['xyz_min'], ...)
+    _load = torch.load
+    torch.load = lambda *a, **k: _load(*a, **{"weights_only": False, **k})
     sys.path.insert(0, REF)
 
 
@@ -268,10 +274,71 @@ def mesh_fixture(path, seed=6):
     print("wrote", path)
 
 
+def ckpt_fixture(dirpath, R=16, seed=7):
+    """Checkpoints in run.py's format (run.py:786-793) written by the
+    reference models, and the reference's answers on them:
+      coarse_last.tar  a coarse model (lib/voxurf_coarse.py) whose density
+                       is high within |sdf| < 0.3 (the mask cache source);
+      fine_last.tar    a fine model (lib/voxurf_fine.py) built with
+                       mask_cache_path = coarse_last.tar (MaskCache,
+                       _set_nonempty_mask applied to its SDF);
+      ckpt_golden.npz  MaskCache point queries (and the alphas, for ties),
+                       hit_coarse_geo of 256 rays, and a FP32 forward of
+                       the fine model (rgb, shaded-sample count)."""
+    import lib.voxurf_coarse as rc
+    import lib.voxurf_fine as rf
+    from voxurf_gb300 import configs, synthetic
+
+    torch.manual_seed(seed)
+    kw = configs.coarse_model_kwargs(R, "fp32", 32)
+    kw.pop("precision")
+    coarse = rc.Voxurf(**kw)
+    ours = configs.build_coarse_model(R, "fp32", device="cpu", seed=seed, width=32)
+    coarse.load_state_dict(_state_from_ours(ours), strict=False)
+    with torch.no_grad():
+        coarse.density.data = (10.0 * (0.3 - coarse.sdf.grid.detach().abs())).clone()
+    ckpt_c = os.path.join(dirpath, "coarse_last.tar")
+    torch.save({"global_step": 1000, "model_kwargs": coarse.get_kwargs(),
+                "MaskCache_kwargs": coarse.get_MaskCache_kwargs(), "model_state_dict": coarse.state_dict(),
+                "optimizer_state_dict": {}}, ckpt_c)
+    fkw = configs.fine_model_kwargs(R, "fp32", 32)
+    fkw.pop("precision")
+    fkw.update(mask_cache_path=ckpt_c, mask_cache_thres=1e-3)
+    fine = rf.Voxurf(**fkw)
+    fours = configs.build_fine_model(R, "fp32", device="cpu", seed=seed, width=32)
+    sd = _state_from_ours(fours)
+    fine.load_state_dict({k: v for k, v in sd.items() if not k.startswith("mask_cache")}, strict=False)
+    fine._set_nonempty_mask()
+    ckpt_f = os.path.join(dirpath, "fine_last.tar")
+    torch.save({"global_step": 1000, "model_kwargs": fine.get_kwargs(),
+                "MaskCache_kwargs": fine.get_MaskCache_kwargs(), "model_state_dict": fine.state_dict(),
+                "optimizer_state_dict": {}}, ckpt_f)
+    g = torch.Generator().manual_seed(seed)
+    pts = torch.rand((4000, 3), generator=g) * 2.2 - 1.1
+    mc = fine.mask_cache
+    with torch.no_grad():
+        inside = mc(pts)
+        xyz = pts.reshape(1, 1, 1, -1, 3)
+        ind_norm = ((xyz - mc.xyz_min) / (mc.xyz_max - mc.xyz_min)).flip((-1,)) * 2 - 1
+        dens = torch.nn.functional.grid_sample(mc.density, ind_norm, align_corners=True)
+        alpha = (1 - torch.exp(-torch.nn.functional.softplus(dens + mc.act_shift) * mc.voxel_size_ratio)).reshape(-1)
+    ro, rd, vd = synthetic.random_rays(256, seed=seed + 1)
+    T = lambda a: torch.from_numpy(a)
+    rk = dict(configs.FINE_RENDER_KWARGS)
+    with torch.no_grad():
+        hit = fine.hit_coarse_geo(T(ro), T(rd), **rk)
+        ret = fine(T(ro), T(rd), T(vd), global_step=1, **rk)
+    np.savez_compressed(os.path.join(dirpath, "ckpt_golden.npz"), pts=pts.numpy(), inside=inside.numpy(),
+                        alpha=alpha.numpy(), rays_o=ro, rays_d=rd, viewdirs=vd, hit=hit.numpy(),
+                        rgb_marched=ret["rgb_marched"].numpy(), n_shaded=np.array(ret["weights"].numel()),
+                        mask_cache_thres=np.array(1e-3))
+    print("wrote", ckpt_c, ckpt_f, "shaded samples", ret["weights"].numel(), "hits", int(hit.sum()))
+
+
 def main():
     install_stubs()
     torch.set_default_dtype(torch.float32)
-    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh"]
+    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt"]
     if "ops" in which:
         ops_fixture(os.path.join(HERE, "ops_golden.npz"))
     if "fine" in which:
@@ -280,6 +347,8 @@ def main():
         coarse_step_fixture(os.path.join(HERE, "coarse_step_golden.npz"))
     if "mesh" in which:
         mesh_fixture(os.path.join(HERE, "mesh_golden.npz"))
+    if "ckpt" in which:
+        ckpt_fixture(HERE)
 
 
 if __name__ == "__main__":

@@ -64,6 +64,25 @@ def test_extract_fields_restatement():
     np.testing.assert_allclose(u.numpy(), M["field"], rtol=1e-6, atol=1e-7)
 
 
+def test_maskcache_restatement():
+    """MaskCache (voxurf_fine.py:917-942) restated: max-pool 3^3 of the
+    coarse checkpoint's density at load, then the FP32 alpha test, against
+    the reference MaskCache's own answers on 4,000 points."""
+    import torch.nn.functional as F
+
+    from oracle.voxurf_oracle import maskcache_query
+
+    C = np.load(os.path.join(HERE, "ckpt_golden.npz"))
+    st = torch.load(os.path.join(HERE, "coarse_last.tar"), map_location="cpu", weights_only=False)
+    kw = st["MaskCache_kwargs"]
+    dens = F.max_pool3d(st["model_state_dict"]["density"], kernel_size=3, padding=1, stride=1)
+    inside = maskcache_query(dens, torch.as_tensor(kw["xyz_min"]), torch.as_tensor(kw["xyz_max"]),
+                             float(kw["act_shift"]), float(kw["voxel_size_ratio"]), float(C["mask_cache_thres"]),
+                             torch.from_numpy(C["pts"]))
+    np.testing.assert_array_equal(inside.numpy(), C["inside"])
+    assert 0 < C["inside"].sum() < len(C["inside"])
+
+
 def test_smoothing_restatement():
     k = torch.from_numpy(gaussian_kernel3d(5, 0.8))
     out = smooth3d(torch.from_numpy(OPS["smooth_in"]), k)

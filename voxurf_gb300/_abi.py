@@ -24,6 +24,8 @@ class FineMarchArgs(C.Structure):
         ("mask", P), ("mask_X", I64), ("mask_Y", I64), ("mask_Z", I64), ("mask_scale", F * 3), ("mask_shift", F * 3),
         ("inv_s", F), ("dist", F), ("fast_color_thres", F), ("max_steps", I64),
         ("rec", P), ("dw_slot", P), ("n1", P), ("n2", P), ("alphainv_last", P),
+        ("mask_density", P), ("mask_dgrid", GridGeom), ("mask_act_shift", F), ("mask_voxel_size_ratio", F),
+        ("mask_thres", F),
     ]
 
 
@@ -132,6 +134,8 @@ class SceneDesc(C.Structure):
         ("mask_X", I64), ("mask_Y", I64), ("mask_Z", I64), ("mask_scale", F * 3), ("mask_shift", F * 3),
         ("inv_s", F), ("stepdist", F), ("near", F), ("bg", F), ("fast_color_thres", F), ("occ", P),
         ("occ_X", I64), ("occ_Y", I64), ("occ_Z", I64), ("occ_block", I32),
+        ("mask_density", P), ("mask_dgrid", GridGeom), ("mask_act_shift", F), ("mask_voxel_size_ratio", F),
+        ("mask_thres", F),
     ]
 
 
@@ -189,6 +193,10 @@ def _declare():
         fn.restype = C.c_int
     lib.vx_sdf_field.argtypes = [P, C.POINTER(GridGeom), P, P, I64, F, P, P]
     lib.vx_sdf_field.restype = C.c_int
+    lib.vx_density_mask.argtypes = [P, C.POINTER(GridGeom), F, F, F, P, I64, P, P]
+    lib.vx_density_mask.restype = C.c_int
+    lib.vx_hit_coarse_geo.argtypes = [C.POINTER(FineMarchArgs), P, P]
+    lib.vx_hit_coarse_geo.restype = C.c_int
     lib.vx_sdf_gradient_grid.argtypes = [P, P, I64, I64, I64, F, C.c_int, P]
     lib.vx_sdf_gradient_grid.restype = C.c_int
     lib.vx_sdf_gradient_grid_adjoint.argtypes = [P, P, I64, I64, I64, F, C.c_int, C.c_int, P]
@@ -227,4 +235,4 @@ def struct_names() -> list[str]:
     return list(_STRUCT_FNS) + ["vx_smooth3d", "vx_smooth3d_adjoint", "vx_grid_sample", "vx_grid_sample_backward",
                                 "vx_sdf_gradient_grid", "vx_sdf_gradient_grid_adjoint",
                                 "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv",
-                                "vx_sdf_field"] + list(_SERVE_SIGNATURES)
+                                "vx_sdf_field", "vx_density_mask", "vx_hit_coarse_geo"] + list(_SERVE_SIGNATURES)

@@ -14,10 +14,61 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "fine_device.cuh"
 #include "trilinear.cuh"
 
 namespace vx {
 
+// ---- MaskCache queries -------------------------------------------------------
+__global__ void __launch_bounds__(256) density_mask_kernel(DensityMask m, const float* __restrict__ xyz, int64_t n,
+                                                           uint8_t* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    out[i] = density_mask_hit(m, p) ? 1 : 0;
+  }
+}
+
+struct HitParams {
+  const float* rays_o;
+  const float* rays_d;
+  int n_rays;
+  float near, stepdist;
+  float bmin[3], bmax[3];
+  const uint8_t* mask;
+  int mX, mY, mZ;
+  float mscale[3], mshift[3];
+  DensityMask dm;
+  uint8_t* hit;
+};
+
+// One warp per ray, 32 samples per step, stop at the first sample in the mask.
+__global__ void __launch_bounds__(256) hit_coarse_geo_kernel(HitParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  float o[3], d[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  bool any = false;
+  for (int64_t base = 0; base < f.n_steps && !any; base += 32) {
+    const int64_t k = base + lane;
+    bool h = false;
+    if (k < f.n_steps) {
+      float p[3];
+      sample_point(f, P.stepdist, (int)k, p);
+      h = !outside_bbox(p, P.bmin, P.bmax);
+      if (h) h = P.mask ? mask_lookup(P.mask, P.mX, P.mY, P.mZ, P.mscale, P.mshift, p) : density_mask_hit(P.dm, p);
+    }
+    any = __any_sync(0xffffffffu, h);
+  }
+  if (lane == 0) P.hit[r] = any ? 1 : 0;
+}
+
+// ---- dense field ---------------------------------------------------------------
 struct FieldAxis {
   float start, end, step;
   int half;  // first index computed from the end
@@ -114,6 +165,49 @@ int vx_sdf_field(const float* sdf, const vx_grid_geom* grid, const float* bound_
   const int64_t cap = (int64_t)sm_count() * 64;
   const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((rows + 7) / 8, cap));
   sdf_field_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(sdf, g, ax, ay, az, (int)R, sign, out);
+  return launch_status();
+}
+
+int vx_density_mask(const float* density, const vx_grid_geom* dgrid, float act_shift, float voxel_size_ratio,
+                    float thres, const float* xyz, int64_t n, uint8_t* out, void* stream) {
+  if (n < 0 || !dgrid) return VX_ERR_ARG;
+  if (n == 0) return VX_OK;
+  if (!density || !xyz || !out) return VX_ERR_ARG;
+  DensityMask m;
+  const int s = fill_density_mask(density, *dgrid, act_shift, voxel_size_ratio, thres, false, m);
+  if (s) return s;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 32);
+  density_mask_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(m, xyz, n, out);
+  return launch_status();
+}
+
+int vx_hit_coarse_geo(const vx_fine_march_args* A, uint8_t* hit, void* stream) {
+  if (!A || A->n_rays < 0 || A->n_rays > INT32_MAX) return VX_ERR_ARG;
+  if (A->n_rays == 0) return VX_OK;
+  if (!A->rays_o || !A->rays_d || !hit || !(A->stepdist > 0.f)) return VX_ERR_ARG;
+  if (!A->mask && !A->mask_density) return VX_ERR_ARG;
+  HitParams P{};
+  P.rays_o = A->rays_o;
+  P.rays_d = A->rays_d;
+  P.n_rays = (int)A->n_rays;
+  P.near = A->near;
+  P.stepdist = A->stepdist;
+  for (int a = 0; a < 3; ++a) {
+    P.bmin[a] = A->grid.xyz_min[a];
+    P.bmax[a] = A->grid.xyz_max[a];
+    P.mscale[a] = A->mask_scale[a];
+    P.mshift[a] = A->mask_shift[a];
+  }
+  P.mask = A->mask;
+  P.mX = (int)A->mask_X;
+  P.mY = (int)A->mask_Y;
+  P.mZ = (int)A->mask_Z;
+  const int s = fill_density_mask(A->mask_density, A->mask_dgrid, A->mask_act_shift, A->mask_voxel_size_ratio,
+                                  A->mask_thres, A->mask != nullptr, P.dm);
+  if (s) return s;
+  P.hit = hit;
+  const int64_t blocks = (A->n_rays + 7) / 8;
+  hit_coarse_geo_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(P);
   return launch_status();
 }
 

@@ -161,6 +161,27 @@ __device__ __forceinline__ bool mask_lookup(const uint8_t* __restrict__ mask, in
   return mask[((int64_t)ijk[0] * mY + ijk[1]) * mZ + ijk[2]] != 0;
 }
 
+// MaskCache (voxurf_fine.py:917-942, voxurf_coarse.py:671-696): the coarse
+// model's density, max-pooled 3^3 at load time, sampled trilinearly
+// (grid_sample, align_corners, zero padding) and thresholded as an alpha:
+// 1 - exp(-softplus(d + act_shift) * voxel_size_ratio) >= thres, softplus
+// with torch's default threshold 20.
+struct DensityMask {
+  const float* dens;  // [X,Y,Z]; null: no density mask
+  GridGeom g;
+  float shift, ratio, thres;
+};
+
+__device__ __forceinline__ bool density_mask_hit(const DensityMask& m, const float p[3]) {
+  float ind[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) ind[a] = world_to_index(m.g, a, p[a]);
+  const float d = sample1(m.dens, m.g, ind[0], ind[1], ind[2]);
+  const float x = d + m.shift;
+  const float sp = x > 20.f ? x : log1pf(expf(x));
+  return 1.f - expf(-sp * m.ratio) >= m.thres;
+}
+
 // ---- MLP input encodings ----------------------------------------------------
 template <typename T>
 __device__ __forceinline__ void put(T* row, int c, float v);
@@ -238,6 +259,27 @@ __device__ __forceinline__ void copy_rows_out(const T* stage, T* dst, int n_rows
 }
 
 // Host side: checks a feature configuration and converts it.
+// Host side: the density mask of a march descriptor (none when dens is
+// null; a bool mask and a density mask together are an argument error).
+inline int fill_density_mask(const float* dens, const vx_grid_geom& g, float shift, float ratio, float thres,
+                             bool has_bool_mask, DensityMask& m) {
+  m.dens = dens;
+  if (!dens) return VX_OK;
+  if (has_bool_mask) return VX_ERR_ARG;
+  if (g.X < 1 || g.Y < 1 || g.Z < 1 || g.X * g.Y * g.Z > INT32_MAX) return VX_ERR_ARG;
+  m.g.X = (int)g.X;
+  m.g.Y = (int)g.Y;
+  m.g.Z = (int)g.Z;
+  for (int a = 0; a < 3; ++a) {
+    m.g.mn[a] = g.xyz_min[a];
+    m.g.mx[a] = g.xyz_max[a];
+  }
+  m.shift = shift;
+  m.ratio = ratio;
+  m.thres = thres;
+  return VX_OK;
+}
+
 inline int fill_feat_layout(const vx_fine_feature_cfg* c, FeatLayout& L) {
   L.K = (int)c->K;
   if (L.K < 1 || L.K > MAX_K) return VX_ERR_ARG;

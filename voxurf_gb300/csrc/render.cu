@@ -50,12 +50,14 @@ struct MarchParams {
   int* n2;            // of which weight > thres
   float* alphainv_last;
   int* err;
+  DensityMask dm;     // optional MaskCache density mask (DENS instantiation)
 };
 
 __device__ __forceinline__ bool mask_hit(const MarchParams& P, const float p[3]) {
   return mask_lookup(P.mask, P.mX, P.mY, P.mZ, P.mscale, P.mshift, p);
 }
 
+template <bool DENS>
 __global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= P.n_rays) return;
@@ -88,6 +90,7 @@ __global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
       sample_point(f, P.stepdist, k, p);
       bool inb = !outside_bbox(p, P.bmin, P.bmax);
       if (inb && P.mask) inb = mask_hit(P, p);
+      if (DENS && inb) inb = density_mask_hit(P.dm, p);
       if (inb) {
         float ind[3], s, gr[3];
         to_index(P.g, p, ind);
@@ -618,6 +621,7 @@ struct CoarseMarchParams {
   int* n2b;            // records up to the second scan's stop (backward range)
 };
 
+template <bool DENS>
 __global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) {
   const MarchParams& P = C.m;
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -650,6 +654,7 @@ __global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) 
       sample_point(f, P.stepdist, k, p);
       inb = !outside_bbox(p, P.bmin, P.bmax);
       if (inb && P.mask) inb = mask_hit(P, p);
+      if (DENS && inb) inb = density_mask_hit(P.dm, p);
       if (inb) {
         float ind[3], gr[3];
         to_index(P.g, p, ind);
@@ -1107,7 +1112,13 @@ int vx_fine_march(const vx_fine_march_args* A, void* stream) {
   P.n2 = A->n2;
   P.alphainv_last = A->alphainv_last;
   P.err = device_error_ptr();
-  march_fine_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  const int s = fill_density_mask(A->mask_density, A->mask_dgrid, A->mask_act_shift, A->mask_voxel_size_ratio,
+                                  A->mask_thres, A->mask != nullptr, P.dm);
+  if (s) return s;
+  if (P.dm.dens)
+    march_fine_kernel<true><<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  else
+    march_fine_kernel<false><<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
   return launch_status();
 }
 
@@ -1364,7 +1375,13 @@ int vx_coarse_march(const vx_coarse_march_args* A, void* stream) {
   P.err = device_error_ptr();
   C.G4 = A->grad4;
   C.n2b = A->n2b;
-  march_coarse_kernel<<<warp_blocks(M->n_rays), 256, 0, as_stream(stream)>>>(C);
+  const int s = fill_density_mask(M->mask_density, M->mask_dgrid, M->mask_act_shift, M->mask_voxel_size_ratio,
+                                  M->mask_thres, M->mask != nullptr, P.dm);
+  if (s) return s;
+  if (P.dm.dens)
+    march_coarse_kernel<true><<<warp_blocks(M->n_rays), 256, 0, as_stream(stream)>>>(C);
+  else
+    march_coarse_kernel<false><<<warp_blocks(M->n_rays), 256, 0, as_stream(stream)>>>(C);
   return launch_status();
 }
 

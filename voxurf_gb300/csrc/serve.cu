@@ -33,6 +33,7 @@ struct SceneK {
   float vs, inv_s, stepdist, near, bg, thres;
   const uint8_t* occ;  // optional block occupancy of the mask (padded by one cell)
   int oX, oY, oZ, oB;
+  DensityMask dm;      // optional MaskCache density mask (dm.dens null: none)
 };
 
 struct SceneTable {
@@ -179,6 +180,7 @@ struct ServeMarchParams {
   int* err;
 };
 
+template <bool DENS>  // some scene carries a MaskCache density mask
 __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
   load_scenes(P.T, sh);
@@ -225,6 +227,7 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
       sample_point(f, S.stepdist, k, p);
       bool inb = !outside_bbox(p, S.g.mn, S.g.mx);
       if (inb && S.mask) inb = mask_lookup(S.mask, S.mX, S.mY, S.mZ, S.mscale, S.mshift, p);
+      if (DENS && inb && S.dm.dens) inb = density_mask_hit(S.dm, p);
       if (inb) {
         float ind[3], s, gr[3];
         to_index(S.g, p, ind);
@@ -512,6 +515,9 @@ static int scene_table(const vx_scene_desc* D, int n, SceneTable& T) {
                   d.occ_Y != (d.mask_Y + d.occ_block - 1) / d.occ_block + 2 ||
                   d.occ_Z != (d.mask_Z + d.occ_block - 1) / d.occ_block + 2))
       return VX_ERR_ARG;
+    const int sd = fill_density_mask(d.mask_density, d.mask_dgrid, d.mask_act_shift, d.mask_voxel_size_ratio,
+                                     d.mask_thres, d.mask != nullptr, s.dm);
+    if (sd) return sd;
   }
   for (int i = n; i < VX_SERVE_MAX_SCENES; ++i) T.s[i] = T.s[0];
   return VX_OK;
@@ -571,7 +577,12 @@ int vx_serve_march(const vx_scene_desc* scenes_host, int32_t n_scenes, const flo
   P.n2 = n2;
   P.alphainv_last = alphainv_last;
   P.err = device_error_ptr();
-  serve_march_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(P);
+  bool dens = false;
+  for (int i = 0; i < P.T.n; ++i) dens |= P.T.s[i].dm.dens != nullptr;
+  if (dens)
+    serve_march_kernel<true><<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(P);
+  else
+    serve_march_kernel<false><<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(P);
   return launch_status();
 }
 

@@ -209,13 +209,7 @@ class GraphedFineStep:
         a.sdf_smooth = ptr(self.sdf_s)
         a.voxel_size = self.voxel_size
         if model.mask_cache is not None:
-            mc = model.mask_cache
-            a.mask = ptr(mc.mask)
-            a.mask_X, a.mask_Y, a.mask_Z = mc.mask.shape
-            sc, sh = grid_mod.host_values(mc.xyz2ijk_scale), grid_mod.host_values(mc.xyz2ijk_shift)
-            for i in range(3):
-                a.mask_scale[i] = float(sc[i])
-                a.mask_shift[i] = float(sh[i])
+            model.mask_cache.fill_march(a)
         a.inv_s, a.dist, a.fast_color_thres = inv_s, self.stepdist, self.thres
         a.max_steps = self.max_steps
         a.rec, a.dw_slot, a.n1, a.n2, a.alphainv_last = ptr(self.rec), ptr(self.dw_slot), ptr(self.n1), \

@@ -1,4 +1,5 @@
-"""Host-side mirror of lib/grid.py: DenseGrid and MaskGrid.
+"""Host-side mirror of lib/grid.py: DenseGrid and MaskGrid, and the
+MaskCache of lib/voxurf_fine.py / lib/voxurf_coarse.py.
 
 Same constructor arguments, attribute names (``grid``, ``xyz_min``,
 ``xyz_max``, ``mask``, ``xyz2ijk_scale``, ``xyz2ijk_shift``), methods and
@@ -15,6 +16,7 @@ from __future__ import annotations
 
 import weakref
 
+import numpy as np
 import torch
 import torch.nn as nn
 import torch.nn.functional as F
@@ -188,5 +190,73 @@ class MaskGrid(nn.Module):
         mask = render_utils_cuda.maskcache_lookup(self.mask, xyz, self.xyz2ijk_scale, self.xyz2ijk_shift)
         return mask.reshape(shape)
 
+    def fill_march(self, a) -> None:
+        """Mask fields of a vx_fine_march_args / vx_scene_desc mirror."""
+        sc, sh = host_values(self.xyz2ijk_scale), host_values(self.xyz2ijk_shift)
+        a.mask = self.mask.data_ptr()
+        a.mask_X, a.mask_Y, a.mask_Z = (int(s) for s in self.mask.shape)
+        for i in range(3):
+            a.mask_scale[i] = float(sc[i])
+            a.mask_shift[i] = float(sh[i])
+
     def extra_repr(self):
         return f"mask.shape={list(self.mask.shape)}"
+
+
+class MaskCache(nn.Module):
+    """The searched coarse geometry of the fine stage (voxurf_fine.py:913-942,
+    voxurf_coarse.py:668-696): a coarse checkpoint's density, max-pooled
+    ks^3 (stride 1) at load time; a point is inside when
+    1 - exp(-softplus(trilinear(density) + act_shift) * voxel_size_ratio)
+    >= mask_cache_thres.  The march kernels evaluate the test per sample
+    (vx_fine_march_args.mask_density); forward() answers point queries
+    (vx_density_mask) and needs the CUDA library.
+
+    `path` is a checkpoint saved by run.py (model_state_dict['density'] and
+    MaskCache_kwargs); `state` the same dict already in memory."""
+
+    def __init__(self, path=None, mask_cache_thres=1e-3, ks=3, state=None):
+        super().__init__()
+        st = torch.load(path, map_location="cpu", weights_only=False) if path is not None else state
+        if st is None:
+            raise ValueError("MaskCache needs a checkpoint path or its state dict")
+        kw = st["MaskCache_kwargs"]
+        self.mask_cache_thres = float(mask_cache_thres)
+        self.register_buffer("xyz_min", torch.as_tensor(np.asarray(kw["xyz_min"], np.float32)).clone())
+        self.register_buffer("xyz_max", torch.as_tensor(np.asarray(kw["xyz_max"], np.float32)).clone())
+        dens = st["model_state_dict"]["density"].detach().float()
+        self.register_buffer("density", F.max_pool3d(dens, kernel_size=ks, padding=ks // 2, stride=1).contiguous())
+        self.act_shift = float(kw["act_shift"])
+        self.voxel_size_ratio = float(torch.as_tensor(kw["voxel_size_ratio"]))
+        self.nearest = bool(kw.get("nearest", False))
+        if self.nearest:
+            raise NotImplementedError("nearest MaskCache sampling is not used by the Voxurf configs and is not built")
+
+    def _geom(self):
+        return grid_geom(self.density.shape[2:], host_values(self.xyz_min), host_values(self.xyz_max))
+
+    @torch.no_grad()
+    def forward(self, xyz):
+        """Boolean [...] for points xyz [..., 3] (computed on the mask's device)."""
+        if not self.density.is_cuda:
+            raise RuntimeError("MaskCache queries run on the GPU: move the module to a CUDA device first")
+        shape = xyz.shape[:-1]
+        pts = xyz.reshape(-1, 3).to(self.density.device, torch.float32).contiguous()
+        out = torch.empty(pts.shape[0], dtype=torch.uint8, device=pts.device)
+        import ctypes
+
+        _abi.call("vx_density_mask", self.density.data_ptr(), ctypes.byref(self._geom()), self.act_shift,
+                  self.voxel_size_ratio, self.mask_cache_thres, pts.data_ptr(), pts.shape[0], out.data_ptr(),
+                  stream_ptr(pts.device))
+        return out.bool().reshape(shape).to(xyz.device)
+
+    def fill_march(self, a) -> None:
+        """Density-mask fields of a vx_fine_march_args / vx_scene_desc mirror."""
+        a.mask_density = self.density.data_ptr()
+        a.mask_dgrid = self._geom()
+        a.mask_act_shift = self.act_shift
+        a.mask_voxel_size_ratio = self.voxel_size_ratio
+        a.mask_thres = self.mask_cache_thres
+
+    def extra_repr(self):
+        return f"density.shape={list(self.density.shape)}, thres={self.mask_cache_thres}"

@@ -102,7 +102,11 @@ class ResidentScene:
         d.voxel_size = vs
         self.mask = None
         self.occ = None
-        if model.mask_cache is not None:
+        if isinstance(model.mask_cache, grid_mod.MaskCache):
+            # trilinear density mask: evaluated per sample, no block skipping
+            self.mask = model.mask_cache.density
+            model.mask_cache.fill_march(d)
+        elif model.mask_cache is not None:
             mc = model.mask_cache
             self.mask = mc.mask.contiguous()
             d.mask = self.mask.data_ptr()

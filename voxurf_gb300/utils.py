@@ -1,4 +1,5 @@
-"""Host-side mirror of the optimizer part of lib/utils.py.
+"""Host-side mirror of the optimizer and checkpoint parts of lib/utils.py
+(load_checkpoint / load_model read run.py's checkpoints into these models).
 
 ``Adam`` keeps the reference's interface (utils.py:54-151: param groups with
 ``lr``, ``betas``, ``eps``, per-voxel learning rate through
@@ -159,3 +160,59 @@ def create_optimizer_or_freeze_model(model, cfg_train, global_step):
         else:
             param.requires_grad = False
     return Adam(param_group, betas=(0.9, 0.99))
+
+
+# ---- checkpoints (utils.py:234-300) -------------------------------------------
+def _load_ckpt(ckpt_path):
+    # run.py stores numpy arrays in model_kwargs / MaskCache_kwargs
+    return torch.load(ckpt_path, map_location="cpu", weights_only=False)
+
+
+def _load_state(model, state, strict):
+    """load_state_dict that keeps the model's storage (channel-last grids,
+    device) and, when not strict, skips keys the model does not hold (the
+    reference registers `nonempty_mask` as a buffer; here it is recomputed)."""
+    own = model.state_dict()
+    if strict:
+        model.load_state_dict(state, strict=True)
+        return
+    model.load_state_dict({k: v for k, v in state.items() if k in own and own[k].shape == v.shape}, strict=False)
+
+
+def load_checkpoint(model, optimizer, ckpt_path, no_reload_optimizer, strict=True):
+    """utils.py:234-250: model (and optimizer) state from a run.py checkpoint;
+    a narrower rgbnet input layer in the checkpoint is zero-padded."""
+    ckpt = _load_ckpt(ckpt_path)
+    start = ckpt["global_step"]
+    sd = dict(ckpt["model_state_dict"])
+    w = sd.get("rgbnet.0.weight")
+    if w is not None and model.rgbnet[0].weight.shape != w.shape:
+        tmp = torch.zeros(model.rgbnet[0].weight.shape)
+        tmp[:, :w.shape[-1]] = w
+        sd["rgbnet.0.weight"] = tmp
+    model.load_state_dict(sd, strict=strict)
+    if not no_reload_optimizer:
+        try:
+            optimizer.load_state_dict(ckpt["optimizer_state_dict"])
+        except Exception:
+            if strict:
+                raise ValueError("failed to load the optimizer state dict")
+    return model, optimizer, start
+
+
+def load_model(model_class, ckpt_path, new_kwargs=None, strict=False):
+    """utils.py:279-300: model_class(**ckpt['model_kwargs'] updated by
+    new_kwargs) with the checkpoint's state (a MaskCache named by
+    mask_cache_path is loaded from its own checkpoint on construction)."""
+    ckpt = _load_ckpt(ckpt_path)
+    kwargs = dict(ckpt["model_kwargs"])
+    if new_kwargs is not None:
+        kwargs.update(new_kwargs)
+    model = model_class(**kwargs)
+    try:
+        _load_state(model, ckpt["model_state_dict"], strict=True)
+    except RuntimeError:
+        if strict:
+            raise
+        _load_state(model, ckpt["model_state_dict"], strict=False)
+    return model

@@ -26,6 +26,7 @@ from ._torch import ptr, stream_ptr
 from .mlp import apply_mlp
 from .voxurf_fine import FineFrame, gaussian_taps, marching_cubes, max_steps_bound, smooth_grid, smooth_grid_adjoint
 from .voxurf_fine import extract_fields as _extract_fields
+from .voxurf_fine import query_mask
 
 
 def sdf_gradient_grid(sdf: torch.Tensor, voxel_size: float) -> torch.Tensor:
@@ -65,12 +66,8 @@ class _CoarseGeometry(torch.autograd.Function):
         m.rays_o, m.rays_d, m.viewdirs = ptr(fr.rays_o), ptr(fr.rays_d), ptr(fr.viewdirs)
         m.n_rays, m.near, m.stepdist, m.grid = N, fr.near, fr.stepdist, fr.geom
         m.sdf_smooth, m.voxel_size = ptr(fr.sdf_s), fr.voxel_size
-        if fr.mask is not None:
-            mk, sc, sh = fr.mask
-            m.mask = ptr(mk)
-            m.mask_X, m.mask_Y, m.mask_Z = mk.shape
-            for i in range(3):
-                m.mask_scale[i], m.mask_shift[i] = float(sc[i]), float(sh[i])
+        if fr.mask_cache is not None:
+            fr.mask_cache.fill_march(m)
         m.inv_s, m.dist, m.fast_color_thres, m.max_steps = fr.inv_s, fr.dist, fr.thres, ms
         m.rec, m.dw_slot, m.n1, m.n2, m.alphainv_last = ptr(rec), ptr(dw_slot), ptr(n1), ptr(n2), ptr(alphainv_last)
         a.grad4, a.n2b = ptr(fr.G4), ptr(n2b)
@@ -251,10 +248,13 @@ class Voxurf(nn.Module):
         )
         nn.init.constant_(self.rgbnet[-1].bias, 0)
         self.mask_cache_path, self.mask_cache_thres = mask_cache_path, mask_cache_thres
-        if mask_cache_path:
-            raise NotImplementedError("path-based MaskCache (trilinear density) is not built yet; pass mask_grid")
-        self.mask_cache = mask_grid
         self.nonempty_mask = None
+        if mask_cache_path:
+            # voxurf_coarse.py:128-137: known free space from an earlier checkpoint
+            self.mask_cache = grid_mod.MaskCache(path=mask_cache_path, mask_cache_thres=mask_cache_thres)
+            self._set_nonempty_mask()
+        else:
+            self.mask_cache = mask_grid
         self.grad_mode = grad_mode
         if grad_mode != "interpolate":
             raise NotImplementedError("only grad_mode='interpolate' (the configs' default) is built")
@@ -293,6 +293,23 @@ class Voxurf(nn.Module):
     def sdf_total_variation_add_grad(self, weight, dense_mode):
         w = weight * self.world_size.max() / 128
         self.sdf.total_variation_add_grad(w, w, w, dense_mode)
+
+    def get_MaskCache_kwargs(self):
+        return {"xyz_min": self.xyz_min.cpu().numpy(), "xyz_max": self.xyz_max.cpu().numpy(),
+                "act_shift": self.act_shift, "voxel_size_ratio": self.voxel_size_ratio, "nearest": self.nearest}
+
+    @torch.no_grad()
+    def _set_nonempty_mask(self):
+        # grid points inside known non-empty space (voxurf_coarse.py:255-270)
+        ws = self.sdf.grid.shape[2:]
+        pts = torch.stack(torch.meshgrid(
+            torch.linspace(float(self.xyz_min[0]), float(self.xyz_max[0]), ws[0]),
+            torch.linspace(float(self.xyz_min[1]), float(self.xyz_max[1]), ws[1]),
+            torch.linspace(float(self.xyz_min[2]), float(self.xyz_max[2]), ws[2]), indexing="ij"), -1)
+        nonempty = query_mask(self.mask_cache, pts)[None, None].contiguous()
+        self.nonempty_mask = nonempty
+        self.density.data[~nonempty.to(self.density.device)] = -100
+        self.sdf.grid.data[~nonempty.to(self.sdf.grid.device)] = 1
 
     # -- mesh extraction (voxurf_coarse.py:652-665) ---------------------------
     @torch.no_grad()
@@ -337,10 +354,7 @@ class Voxurf(nn.Module):
         fr.geom = grid_mod.grid_geom(self.sdf.grid.shape[2:], grid_mod.host_values(self.xyz_min), grid_mod.host_values(self.xyz_max))
         fr.max_steps = max_steps_bound(grid_mod.host_values(self.xyz_min), grid_mod.host_values(self.xyz_max), fr.stepdist)
         fr.taps = self.smooth_taps if self.smooth_sdf else None
-        fr.mask = None
-        if self.mask_cache is not None:
-            mc = self.mask_cache
-            fr.mask = (mc.mask, grid_mod.host_values(mc.xyz2ijk_scale), grid_mod.host_values(mc.xyz2ijk_shift))
+        fr.mask_cache = self.mask_cache  # MaskGrid (bool) or MaskCache (density), or None
         fr.cfg = _coarse_cfg(self)
         fr.use_k0 = not self.rgbnet_full_implicit
         fr.bf16 = self.precision == "bf16"

@@ -102,6 +102,47 @@ def marching_cubes(u: np.ndarray, threshold: float, bound_min, bound_max, resolu
     return vertices, triangles
 
 
+@torch.no_grad()
+def get_training_rays_in_maskcache_sampling(rgb_tr_ori, train_poses, HW, Ks, ndc, inverse_y, flip_x, flip_y, model,
+                                            render_kwargs, rgbnet_sup_reduce=1):
+    """voxurf_fine.py:1127-1164: the training rays of every view that hit
+    the mask cache (model.hit_coarse_geo), with their colours, packed in view
+    order.  Rays per view come from vx_camera_rays (pinhole, pixel centres
+    +0.5); returns (rgb_tr, rays_o_tr, rays_d_tr, viewdirs_tr, imsz)."""
+    if ndc or flip_x or flip_y:
+        raise NotImplementedError("ndc / flipped cameras are not used by the Voxurf configs")
+    dev = model.sdf.grid.device
+    out = [[], [], [], []]
+    imsz = []
+    for c2w, img, (H, W), K in zip(train_poses, rgb_tr_ori, HW, Ks):
+        H, W = int(H), int(W)
+        K = np.asarray(K.cpu() if torch.is_tensor(K) else K, np.float32)
+        o = torch.empty((H * W, 3), dtype=torch.float32, device=dev)
+        d = torch.empty_like(o)
+        v = torch.empty_like(o)
+        m = (ctypes.c_float * 12)(*np.asarray(c2w.cpu() if torch.is_tensor(c2w) else c2w, np.float32)[:3, :4].reshape(-1))
+        _abi.call("vx_camera_rays", m, float(K[0, 0]), float(K[1, 1]), float(K[0, 2]), float(K[1, 2]), H, W,
+                  int(inverse_y), ptr(o), ptr(d), ptr(v), stream_ptr(dev))
+        hit = model.hit_coarse_geo(o, d, **render_kwargs)
+        out[0].append(img.reshape(H * W, -1).to(dev)[hit])
+        out[1].append(o[hit])
+        out[2].append(d[hit])
+        out[3].append(v[hit])
+        imsz.append(int(hit.sum()))
+    rgb_tr, rays_o_tr, rays_d_tr, viewdirs_tr = (torch.cat(x, 0) for x in out)
+    return rgb_tr, rays_o_tr, rays_d_tr, viewdirs_tr, imsz
+
+
+@torch.no_grad()
+def query_mask(mask_cache, pts: torch.Tensor) -> torch.Tensor:
+    """Point query of a MaskGrid / MaskCache on the GPU (a device copy of a
+    module that still sits on the host, as during model construction)."""
+    buf = mask_cache.mask if isinstance(mask_cache, grid_mod.MaskGrid) else mask_cache.density
+    mc = mask_cache if buf.is_cuda else deepcopy(mask_cache).to("cuda")
+    dev = (mc.mask if isinstance(mc, grid_mod.MaskGrid) else mc.density).device
+    return mc(pts.to(dev))
+
+
 def max_steps_bound(xyz_min, xyz_max, stepdist: float) -> int:
     """Upper bound of N_steps for any ray: the bbox diagonal in steps, +2."""
     diag = math.sqrt(sum((float(b) - float(a)) ** 2 for a, b in zip(xyz_min, xyz_max)))
@@ -150,13 +191,8 @@ class _FineGeometry(torch.autograd.Function):
         a.grid = fr.geom
         a.sdf_smooth = ptr(fr.sdf_s)
         a.voxel_size = fr.voxel_size
-        if fr.mask is not None:
-            m, sc, sh = fr.mask
-            a.mask = ptr(m)
-            a.mask_X, a.mask_Y, a.mask_Z = m.shape
-            for i in range(3):
-                a.mask_scale[i] = float(sc[i])
-                a.mask_shift[i] = float(sh[i])
+        if fr.mask_cache is not None:
+            fr.mask_cache.fill_march(a)
         a.inv_s, a.dist, a.fast_color_thres = fr.inv_s, fr.dist, fr.thres
         a.max_steps = ms
         a.rec, a.dw_slot, a.n1, a.n2, a.alphainv_last = ptr(rec), ptr(dw_slot), ptr(n1), ptr(n2), ptr(alphainv_last)
@@ -425,10 +461,12 @@ class Voxurf(nn.Module):
             raise NotImplementedError("use_grad_norm=False is not used by the Voxurf configs")
         self.mask_cache_path, self.mask_cache_thres = mask_cache_path, mask_cache_thres
         if mask_cache_path:
-            raise NotImplementedError("path-based MaskCache (trilinear density) is not built yet; pass mask_grid")
-        self.mask_cache = mask_grid
+            # the coarse checkpoint's density (voxurf_fine.py:189-195)
+            self.mask_cache = grid_mod.MaskCache(path=mask_cache_path, mask_cache_thres=mask_cache_thres)
+        else:
+            self.mask_cache = mask_grid
         self.nonempty_mask = None
-        if mask_grid is not None:
+        if self.mask_cache is not None:
             self._set_nonempty_mask()
         self.grad_mode = grad_mode
         if precision not in ("fp32", "bf16"):
@@ -448,6 +486,31 @@ class Voxurf(nn.Module):
         self.smooth_ksize, self.smooth_sigma = ksize, sigma
         self.smooth_taps = gaussian_taps(ksize, sigma) if self.smooth_sdf else None
 
+    def get_MaskCache_kwargs(self):
+        return {"xyz_min": self.xyz_min.cpu().numpy(), "xyz_max": self.xyz_max.cpu().numpy(),
+                "act_shift": self.act_shift, "voxel_size_ratio": self.voxel_size_ratio, "nearest": self.nearest}
+
+    @torch.no_grad()
+    def hit_coarse_geo(self, rays_o, rays_d, near, far, stepsize, **render_kwargs):
+        """voxurf_fine.py:579-591: whether each ray has an in-bbox sample
+        (sample_pts_on_rays, far = 1e9) inside the mask cache; one warp per
+        ray stops at the first such sample (vx_hit_coarse_geo)."""
+        if self.mask_cache is None:
+            raise RuntimeError("hit_coarse_geo needs a mask cache")
+        shape = rays_o.shape[:-1]
+        dev = self.sdf.grid.device
+        o = rays_o.reshape(-1, 3).to(dev, torch.float32).contiguous()
+        d = rays_d.reshape(-1, 3).to(dev, torch.float32).contiguous()
+        a = _abi.FineMarchArgs()
+        a.rays_o, a.rays_d, a.n_rays, a.near = ptr(o), ptr(d), o.shape[0], float(near)
+        a.stepdist = float(stepsize * self.voxel_size.float())
+        a.grid = grid_mod.grid_geom(self.sdf.grid.shape[2:], grid_mod.host_values(self.xyz_min),
+                                    grid_mod.host_values(self.xyz_max))
+        self.mask_cache.fill_march(a)
+        hit = torch.empty(o.shape[0], dtype=torch.uint8, device=dev)
+        _abi.call("vx_hit_coarse_geo", ctypes.byref(a), ptr(hit), stream_ptr(dev))
+        return hit.bool().reshape(shape)
+
     def get_kwargs(self):
         return {"xyz_min": self.xyz_min.cpu().numpy(), "xyz_max": self.xyz_max.cpu().numpy(),
                 "num_voxels": self.num_voxels, "num_voxels_base": self.num_voxels_base,
@@ -464,8 +527,7 @@ class Voxurf(nn.Module):
             torch.linspace(float(self.xyz_min[0]), float(self.xyz_max[0]), ws[0]),
             torch.linspace(float(self.xyz_min[1]), float(self.xyz_max[1]), ws[1]),
             torch.linspace(float(self.xyz_min[2]), float(self.xyz_max[2]), ws[2]), indexing="ij"), -1)
-        dev = self.mask_cache.mask.device
-        nonempty = self.mask_cache(pts.to(dev))[None, None].contiguous()
+        nonempty = query_mask(self.mask_cache, pts)[None, None].contiguous()
         self.nonempty_mask = nonempty
         self.density.data[~nonempty.to(self.density.device)] = -100
         self.sdf.grid.data[~nonempty.to(self.sdf.grid.device)] = 1
@@ -567,10 +629,7 @@ class Voxurf(nn.Module):
         fr.geom = grid_mod.grid_geom(self.sdf.grid.shape[2:], grid_mod.host_values(self.xyz_min), grid_mod.host_values(self.xyz_max))
         fr.max_steps = max_steps_bound(grid_mod.host_values(self.xyz_min), grid_mod.host_values(self.xyz_max), fr.stepdist)
         fr.taps = self.smooth_taps if self.smooth_sdf else None
-        fr.mask = None
-        if self.mask_cache is not None:
-            mc = self.mask_cache
-            fr.mask = (mc.mask, grid_mod.host_values(mc.xyz2ijk_scale), grid_mod.host_values(mc.xyz2ijk_shift))
+        fr.mask_cache = self.mask_cache  # MaskGrid (bool) or MaskCache (density), or None
         fr.cfg = _feature_cfg(self)
         fr.bf16 = self.precision == "bf16"
         fr.k0_bf16 = None
