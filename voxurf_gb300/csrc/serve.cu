@@ -180,6 +180,35 @@ struct ServeMarchParams {
   int* err;
 };
 
+// First sample of each ray that can lie in its scene's mask (scenes with an
+// occupancy grid; 0 otherwise), written to n2[r] for the march to start at.
+// One thread per ray: the block walk is serial per ray, so 32 rays share a
+// warp's instruction stream (a warp-per-ray walk would spend 32x the issue
+// slots).  Exact: skip_empty only passes cells of the one-voxel-widened
+// occupancy that hold no mask voxel.
+__global__ void __launch_bounds__(256) serve_first_kernel(ServeMarchParams P) {
+  __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
+  load_scenes(P.T, sh);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= P.n_rays) return;
+  const int sc = P.ray_scene[r];
+  if (sc < 0 || sc >= P.T.n) return;  // reported by the march
+  const SceneK& S = sh[sc];
+  if (!S.occ) {
+    P.n2[r] = 0;
+    return;
+  }
+  float o[3], d[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, S.g.mn, S.g.mx, S.near, S.stepdist);
+  const int n_steps = (int)min(f.n_steps, (int64_t)P.max_steps);
+  P.n2[r] = skip_empty(skip_model(f, S), 0, n_steps, S);
+}
+
 template <bool DENS>  // some scene carries a MaskCache density mask
 __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
@@ -215,9 +244,10 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
   double carry = 1.0, last = 1.0;
   int cnt2 = 0;
   bool stopped = false;
-  const SkipModel sm = skip_model(f, S);
-  for (int base = 0; !stopped; base += 32) {
-    if (S.occ && S.mask) base = skip_empty(sm, base, (int)n_steps, S);  // warp-uniform
+  // with an occupancy grid, serve_first_kernel left the first sample that
+  // can lie in the mask in n2[r]: every earlier sample is masked out
+  const int k0 = S.occ ? P.n2[r] : 0;
+  for (int base = k0; !stopped; base += 32) {
     if (base >= n_steps) break;
     const int k = base + lane;
     bool keep = false;
@@ -577,8 +607,16 @@ int vx_serve_march(const vx_scene_desc* scenes_host, int32_t n_scenes, const flo
   P.n2 = n2;
   P.alphainv_last = alphainv_last;
   P.err = device_error_ptr();
-  bool dens = false;
-  for (int i = 0; i < P.T.n; ++i) dens |= P.T.s[i].dm.dens != nullptr;
+  bool dens = false, occ = false;
+  for (int i = 0; i < P.T.n; ++i) {
+    dens |= P.T.s[i].dm.dens != nullptr;
+    occ |= P.T.s[i].occ != nullptr;
+  }
+  if (occ) {
+    serve_first_kernel<<<(unsigned)((n_rays + 255) / 256), 256, 0, as_stream(stream)>>>(P);
+    s = launch_status();
+    if (s) return s;
+  }
   if (dens)
     serve_march_kernel<true><<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(P);
   else
