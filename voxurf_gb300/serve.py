@@ -6,10 +6,14 @@ Voxurf.forward call (run.py:81-126, render_viewpoints).  Here each tick
 packs rays from every admitted request (oldest first, up to ``tick_rays``)
 and runs the inference form of the forward (voxurf_fine.py:620-802 with
 global_step=None) over them with one launch per stage for all scenes
-(vx_serve_rays / _march / _rows / _features / _composite); only the hidden
-MLP layers are issued per scene, as GEMMs on the scene's contiguous rows,
-with the 192 -> 3 output layers in vx_mlp_head (FP32 accumulation).  The
-composite writes straight into each request's range of an output arena.
+(vx_serve_rays / _march / _rows / _features / _composite); only the colour
+MLPs are issued per scene, on the scene's contiguous rows: for BF16 scenes
+the fused tcgen05 kernel (vx_mlp_tc_forward, hidden activations never leave
+the SM), otherwise GEMMs with the 192 -> 3 output layers in vx_mlp_head
+(FP32 accumulation).  With a bool mask, a thread-per-ray pass over the
+mask's block occupancy starts each ray's march at its first sample that can
+lie in the mask.  The composite writes straight into each request's range
+of an output arena.
 
 Admission is by device memory: a request is admitted once the arena (sized
 from free HBM when the server starts) has room for its pixels and fewer
