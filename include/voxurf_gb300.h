@@ -568,7 +568,9 @@ typedef struct {
   const float* b0;          /* [192] hidden biases (FP32)                           */
   const float* b1;
   const float* b2;
-  const float* Wh;          /* [3,192] output layer (FP32)                          */
+  const void* Whp;          /* output layer as vx_mlp_tc_pack(Wsplit, 16, 192, 192) of
+                               Wsplit [16,192] FP32: rows 0-2 = BF16(Wh), rows 3-5 =
+                               BF16(Wh - BF16(Wh)), rows 6-15 = 0 (Wh [3,192])     */
   const float* bh;          /* [3]                                                  */
   const float* add;         /* optional [n_rows,3] added to the output (k_rgbnet's residual logits) */
   float* out;               /* [n_rows,3] logits                                    */
@@ -578,8 +580,9 @@ typedef struct {
 
 /* out = Wh relu(W2 relu(W1 relu(W0 x + b0) + b1) + b2) + bh (+ add) for every
  * row: BF16 operands, FP32 accumulation in tensor memory, hidden activations
- * rounded to BF16 between layers, output layer in FP32.  One persistent CTA
- * per SM holds the hidden weights in shared memory. */
+ * rounded to BF16 between layers; the output layer also on the tensor cores,
+ * its FP32 weights split into two BF16 parts (hi + lo, relative error below
+ * 2^-16).  One persistent CTA per SM holds all weights in shared memory. */
 int vx_mlp_tc_forward(const vx_mlp_tc_args* args, void* stream);
 
 /* ---- render server: the inference form of Voxurf.forward (global_step =

@@ -123,7 +123,7 @@ class CoarseBackwardArgs(C.Structure):
 class MlpTcArgs(C.Structure):
     _fields_ = [
         ("X", P), ("ldx", I64), ("K0", I64), ("n_rows", I64), ("width", I64), ("W0p", P), ("W1p", P), ("W2p", P),
-        ("b0", P), ("b1", P), ("b2", P), ("Wh", P), ("bh", P), ("add", P), ("out", P), ("cols", P),
+        ("b0", P), ("b1", P), ("b2", P), ("Whp", P), ("bh", P), ("add", P), ("out", P), ("cols", P),
         ("ld_cols", I64),
     ]
 

@@ -1,17 +1,18 @@
 // Fused colour-MLP forward on the 5th-generation tensor cores (tcgen05).
 //
-// One persistent CTA per SM keeps all three 192-wide hidden layers of one
-// colour MLP (rgbnet or k_rgbnet, voxurf_fine.py:132-187) resident in shared
-// memory (BF16, 30 + 72 + 72 KB) and streams 128-row tiles of its input
-// rows through them:
+// One persistent CTA per SM keeps all layers of one colour MLP (rgbnet or
+// k_rgbnet, voxurf_fine.py:132-187) resident in shared memory (BF16, 30 +
+// 72 + 72 KB hidden, 6 KB output layer) and streams 128-row tiles of its
+// input rows through them:
 //
-//   X tile (128 x K0, BF16) --tcgen05.mma--> TMEM (128 x 192 FP32)
-//     --tcgen05.ld--> +bias, ReLU, BF16 --st.shared--> A tile --mma--> ...
-//   last hidden layer: +bias, ReLU in registers, then the 192 -> 3 output
-//   layer on the CUDA cores (FP32), + optional residual logits.
+//   X tile (128 x K0, BF16, shared) --tcgen05.mma--> TMEM acc (128 x 192 FP32)
+//     --tcgen05.ld--> +bias, ReLU, BF16 --tcgen05.st--> TMEM A operand
+//     --tcgen05.mma (A from tensor memory)--> acc ... (layers 1, 2)
+//   output layer: one more MMA (N = 16) from the TMEM A operand against the
+//   FP32 output weights split into BF16 hi + lo rows; logit = hi + lo + b.
 //
-// Hidden activations never leave the SM; HBM traffic per row is the input
-// row and 12 bytes of logits.  Operands use the canonical K-major layout
+// Hidden activations never leave tensor memory; HBM traffic per row is the
+// input row and 12 bytes of logits.  Shared-memory operands use the canonical K-major layout
 // without swizzle: 8 x 16-byte core matrices, chunk c of K (8 elements) of
 // all R rows stored contiguously ([K/8][R][8]), so LBO = R * 16 bytes (next
 // core matrix along K) and SBO = 128 bytes (next 8 rows).  Weights are
@@ -23,7 +24,9 @@
 // thread 0 issues the MMAs and the commit.  Weights, biases and the output
 // layer arrive by bulk copies on the async proxy (one mbarrier); the next
 // input tile is prefetched with 16-byte cp.async (zero fill past the last
-// row) while the current tile's last layer runs.  Every wait on an
+// row) as soon as the first layer's MMAs have read the current one.  Tensor
+// memory: 512 columns (accumulator 0-191, output layer 192-207, A operand
+// 256-351; one CTA per SM).  Every wait on an
 // mbarrier is bounded: on expiry the kernel records VX_ERR_TIMEOUT,
 // releases its TMEM and returns.
 #include "common.cuh"
@@ -32,8 +35,8 @@ namespace vx {
 
 constexpr int TC_M = 128;       // rows per tile (one cta_group::1 MMA)
 constexpr int TC_N = 192;       // hidden width
-constexpr int TC_KMAX0 = 80;    // largest first-layer K (shared memory: 30 + 144 + 48 KB)
-constexpr int TC_TMEM_COLS = 256;
+constexpr int TC_KMAX0 = 80;    // largest first-layer K (shared memory: 30 + 144 + 20 + 6 + 2 KB)
+constexpr int TC_TMEM_COLS = 512;
 
 struct MlpTcParams {
   const __nv_bfloat16* X;  // [n_rows, ldx] input rows (columns K0.. zero or ignored via zero weights)
@@ -46,7 +49,7 @@ struct MlpTcParams {
   const float* b0;
   const float* b1;
   const float* b2;
-  const float* Wh;   // [3,192] output layer (FP32)
+  const __nv_bfloat16* Whp;  // packed [24][16][8] output layer: rows 0-2 hi, 3-5 lo parts
   const float* bh;   // [3]
   const float* add;  // optional [n,3] added to the logits
   float* out;        // [n,3]
@@ -193,7 +196,58 @@ __device__ __forceinline__ void load_x_tile(const MlpTcParams& P, __nv_bfloat16*
   cp_async_commit();
 }
 
+// ---- A operand in tensor memory ------------------------------------------
+// Hidden activations of layers 1 and 2 and of the output layer stay in
+// tensor memory: row m in lane m, K element k in column k/2 (two BF16 per
+// 32-bit column, the lower k in the lower half, as pack_bf16 packs them).
+__device__ __forceinline__ void tc_mma_ta(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc, bool acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(dtmem),
+      "r"(atmem), "l"(bdesc), "r"(idesc), "r"((uint32_t)acc)
+      : "memory");
+}
+
+// All K/16 MMAs of a layer with A in tensor memory (8 columns per K step)
+// and B [K/8][N][8] in shared memory, then the commit.
+__device__ __forceinline__ void tc_layer_ta(uint32_t dtmem, uint32_t atmem, uint32_t b_s, int N, int K,
+                                            uint64_t* bar) {
+  const uint32_t idesc = umma_idesc(TC_M, N);
+  for (int ks = 0; ks < K / 16; ++ks) {
+    const uint64_t bd = umma_desc(b_s + (uint32_t)(2 * ks) * (uint32_t)(N * 16), (uint32_t)(N * 16), 128);
+    tc_mma_ta(dtmem, atmem + (uint32_t)(8 * ks), bd, idesc, ks > 0);
+  }
+  tc_commit(bar);
+}
+
+// 16 consecutive 32-bit columns of this thread's TMEM lane <- r.
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+      "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  tc_wait_ld();
+#pragma unroll
+  for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(r[i]));
+}
+
 constexpr int TC_THREADS = 256;  // 8 warps: warps w and w+4 share TMEM lanes 32(w%4).., split the columns
+constexpr int TC_NH = 16;        // output-layer tile: rows 0-2 hi, 3-5 lo, rest zero
+// tensor-memory columns: hidden accumulator, output-layer accumulator, A operand
+constexpr uint32_t TM_ACC = 0, TM_HEAD = 192, TM_A = 256;
 
 __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -201,13 +255,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   __nv_bfloat16* W0s = reinterpret_cast<__nv_bfloat16*>(smem);
   __nv_bfloat16* W1s = W0s + (size_t)K0 * TC_N;
   __nv_bfloat16* W2s = W1s + (size_t)TC_N * TC_N;
-  __nv_bfloat16* As = W2s + (size_t)TC_N * TC_N;                  // [24][128][8]
-  float* bias_s = reinterpret_cast<float*>(As + (size_t)TC_N * TC_M);  // [3][192]
-  float* wh_s = bias_s + 3 * TC_N;                                  // [3][192]
-  uint64_t* bar_w = reinterpret_cast<uint64_t*>(wh_s + 3 * TC_N);
+  __nv_bfloat16* Xs = W2s + (size_t)TC_N * TC_N;                    // [K0/8][128][8] input tile
+  __nv_bfloat16* WHs = Xs + (size_t)K0 * TC_M;                      // [24][16][8] output layer
+  float* bias_s = reinterpret_cast<float*>(WHs + (size_t)TC_NH * TC_N);  // [3][192]
+  uint64_t* bar_w = reinterpret_cast<uint64_t*>(bias_s + 3 * TC_N);
   uint64_t* bar_mma = bar_w + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_mma + 1);
-  float* partial = reinterpret_cast<float*>(As + 16 * TC_M * 8);    // [128][3] in A chunks >= 16
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3, half = warp >> 2;  // TMEM lanes 32*quarter.., columns [96*half, +96)
@@ -225,18 +278,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   }
   __syncthreads();
   if (tid == 0) {
-    // weights, biases and the output layer: bulk copies on the async proxy
-    const uint32_t w0b = (uint32_t)K0 * TC_N * 2, w1b = (uint32_t)TC_N * TC_N * 2, bb = TC_N * 4;
-    mbar_expect_tx(bar_w, w0b + 2 * w1b + 3 * bb + 3 * bb);
+    // weights and biases: bulk copies on the async proxy
+    const uint32_t w0b = (uint32_t)K0 * TC_N * 2, w1b = (uint32_t)TC_N * TC_N * 2, bb = TC_N * 4,
+                   whb = (uint32_t)TC_NH * TC_N * 2;
+    mbar_expect_tx(bar_w, w0b + 2 * w1b + whb + 3 * bb);
     bulk_g2s(W0s, P.W0p, w0b, bar_w);
     bulk_g2s(W1s, P.W1p, w1b, bar_w);
     bulk_g2s(W2s, P.W2p, w1b, bar_w);
+    bulk_g2s(WHs, P.Whp, whb, bar_w);
     bulk_g2s(bias_s, P.b0, bb, bar_w);
     bulk_g2s(bias_s + TC_N, P.b1, bb, bar_w);
     bulk_g2s(bias_s + 2 * TC_N, P.b2, bb, bar_w);
-    bulk_g2s(wh_s, P.Wh, 3 * bb, bar_w);
   }
-  if (blockIdx.x < n_tiles) load_x_tile(P, As, (int64_t)blockIdx.x * TC_M, tid, TC_THREADS);
+  if (blockIdx.x < n_tiles) load_x_tile(P, Xs, (int64_t)blockIdx.x * TC_M, tid, TC_THREADS);
   bool ok = mbar_wait(bar_w, 0);
   const float bh0 = __ldg(P.bh + 0), bh1 = __ldg(P.bh + 1), bh2 = __ldg(P.bh + 2);
   tc_fence_before();
@@ -244,7 +298,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const uint32_t tmem_row = tmem + ((uint32_t)(32 * quarter) << 16);
-  const uint32_t a_s = smem_u32(As), w_s[3] = {smem_u32(W0s), smem_u32(W1s), smem_u32(W2s)};
+  const uint32_t x_s = smem_u32(Xs), w_s[3] = {smem_u32(W0s), smem_u32(W1s), smem_u32(W2s)}, wh_s = smem_u32(WHs);
   uint32_t phase = 0;
 
   for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
@@ -257,82 +311,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
     __syncthreads();
     tc_fence_after();
 #pragma unroll 1
-    for (int layer = 0; layer < 3; ++layer) {
-      if (tid == 0) tc_layer(tmem, a_s, w_s[layer], layer == 0 ? K0 : TC_N, bar_mma);
+    for (int layer = 0; layer < 4; ++layer) {
+      if (tid == 0) {
+        if (layer == 0)
+          tc_layer(tmem + TM_ACC, x_s, w_s[0], K0, bar_mma);
+        else if (layer < 3)
+          tc_layer_ta(tmem + TM_ACC, tmem + TM_A, w_s[layer], TC_N, TC_N, bar_mma);
+        else
+          tc_layer_ta(tmem + TM_HEAD, tmem + TM_A, wh_s, TC_NH, TC_N, bar_mma);
+      }
       ok = mbar_wait(bar_mma, phase);
       phase ^= 1u;
       tc_fence_after();
       if (!ok) break;
-      const float* b = bias_s + layer * TC_N;
-      if (layer < 2) {
-        // +bias, ReLU, BF16 -> As (the next layer's A operand): this thread's
-        // row, columns [96*half, 96*half + 96)
-        uint4* dst = reinterpret_cast<uint4*>(As);
+      if (layer == 0) {
+        // the input tile is consumed: prefetch the next one
+        const int64_t next = tile + gridDim.x;
+        if (next < n_tiles) load_x_tile(P, Xs, next * TC_M, tid, TC_THREADS);
+      }
+      if (layer < 3) {
+        // +bias, ReLU, BF16 -> the A operand in tensor memory: this thread's
+        // row, columns [96*half, 96*half + 96) -> TMEM columns [48*half, +48)
+        const float* b = bias_s + layer * TC_N;
         uint32_t v[3][32];
-        tc_ld96(tmem_row + 96 * half, v);
+        tc_ld96(tmem_row + TM_ACC + 96 * half, v);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           const int col0 = 96 * half + 32 * j;
+          uint32_t pk[16];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float4 bl = *reinterpret_cast<const float4*>(b + col0 + 8 * q);
-            const float4 bu = *reinterpret_cast<const float4*>(b + col0 + 8 * q + 4);
-            const float bb[8] = {bl.x, bl.y, bl.z, bl.w, bu.x, bu.y, bu.z, bu.w};
-            float h[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) h[e] = fmaxf(__uint_as_float(v[j][8 * q + e]) + bb[e], 0.f);
-            dst[(size_t)(col0 / 8 + q) * TC_M + 32 * quarter + lane] =
-                make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+          for (int q = 0; q < 8; ++q) {
+            const float4 bq = *reinterpret_cast<const float4*>(b + col0 + 4 * q);
+            const float h0 = fmaxf(__uint_as_float(v[j][4 * q + 0]) + bq.x, 0.f);
+            const float h1 = fmaxf(__uint_as_float(v[j][4 * q + 1]) + bq.y, 0.f);
+            const float h2 = fmaxf(__uint_as_float(v[j][4 * q + 2]) + bq.z, 0.f);
+            const float h3 = fmaxf(__uint_as_float(v[j][4 * q + 3]) + bq.w, 0.f);
+            pk[2 * q] = pack_bf16(h0, h1);
+            pk[2 * q + 1] = pack_bf16(h2, h3);
           }
+          tc_st16(tmem_row + TM_A + (uint32_t)(48 * half + 16 * j), pk);
         }
-        fence_async_smem();
+        tc_wait_st();
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-      } else {
-        // As is free (all MMAs of this tile are done): prefetch the next tile
-        const int64_t next = tile + gridDim.x;
-        if (next < n_tiles) load_x_tile(P, As, next * TC_M, tid, TC_THREADS);
-        // last hidden layer: +bias, ReLU, rounded to BF16 like the GEMM path,
-        // then this thread's share of the FP32 output layer
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        uint32_t v[3][32];
-        tc_ld96(tmem_row + 96 * half, v);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int col = 96 * half + 32 * j + 4 * q;
-            const float4 bq = *reinterpret_cast<const float4*>(b + col);
-            const float4 w0 = *reinterpret_cast<const float4*>(wh_s + col);
-            const float4 w1 = *reinterpret_cast<const float4*>(wh_s + TC_N + col);
-            const float4 w2 = *reinterpret_cast<const float4*>(wh_s + 2 * TC_N + col);
-            const float bb[4] = {bq.x, bq.y, bq.z, bq.w};
-            const float x0[4] = {w0.x, w0.y, w0.z, w0.w}, x1[4] = {w1.x, w1.y, w1.z, w1.w};
-            const float x2[4] = {w2.x, w2.y, w2.z, w2.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const float h =
-                  __bfloat162float(__float2bfloat16_rn(fmaxf(__uint_as_float(v[j][4 * q + e]) + bb[e], 0.f)));
-              a0 += h * x0[e];
-              a1 += h * x1[e];
-              a2 += h * x2[e];
-            }
-          }
-        }
-        const int r = 32 * quarter + lane;
-        if (half == 1) {
-          partial[3 * r + 0] = a0;
-          partial[3 * r + 1] = a1;
-          partial[3 * r + 2] = a2;
-        }
-        tc_fence_before();
-        __syncthreads();  // partials written; TMEM free for the next tile
-        tc_fence_after();
-        if (half == 0 && row < P.n_rows) {
-          a0 += partial[3 * r + 0] + bh0;
-          a1 += partial[3 * r + 1] + bh1;
-          a2 += partial[3 * r + 2] + bh2;
+      } else if (half == 0) {
+        // output layer: hi + lo parts of each logit, + bias (+ residual)
+        uint32_t hv[16];
+        tc_ld16(tmem_row + TM_HEAD, hv);
+        if (row < P.n_rows) {
+          float a0 = (__uint_as_float(hv[0]) + __uint_as_float(hv[3])) + bh0;
+          float a1 = (__uint_as_float(hv[1]) + __uint_as_float(hv[4])) + bh1;
+          float a2 = (__uint_as_float(hv[2]) + __uint_as_float(hv[5])) + bh2;
           if (P.add) {
             a0 += P.add[3 * row + 0];
             a1 += P.add[3 * row + 1];
@@ -371,7 +401,8 @@ __global__ void mlp_tc_pack_kernel(const float* __restrict__ W, int N, int K, in
 }
 
 static size_t mlp_tc_smem_bytes(int K0) {
-  return (size_t)K0 * TC_N * 2 + 2 * (size_t)TC_N * TC_N * 2 + (size_t)TC_N * TC_M * 2 + 6 * TC_N * 4 + 24;
+  return (size_t)K0 * TC_N * 2 + 2 * (size_t)TC_N * TC_N * 2 + (size_t)K0 * TC_M * 2 + (size_t)TC_NH * TC_N * 2 +
+         3 * TC_N * 4 + 24;
 }
 
 }  // namespace vx
@@ -391,11 +422,13 @@ int vx_mlp_tc_forward(const vx_mlp_tc_args* A, void* stream) {
   if (!A || A->n_rows < 0) return VX_ERR_ARG;
   if (A->n_rows == 0) return VX_OK;
   if (A->width != TC_N || A->K0 < 16 || A->K0 > TC_KMAX0 || A->K0 % 16) return VX_ERR_UNSUPPORTED;
-  if (!A->X || !A->W0p || !A->W1p || !A->W2p || !A->b0 || !A->b1 || !A->b2 || !A->Wh || !A->bh || !A->out)
+  if (!A->X || !A->W0p || !A->W1p || !A->W2p || !A->b0 || !A->b1 || !A->b2 || !A->Whp || !A->bh || !A->out)
     return VX_ERR_ARG;
   if (A->ldx < A->K0 || (A->ldx % 8) || (reinterpret_cast<uintptr_t>(A->X) & 15)) return VX_ERR_ARG;
   if ((reinterpret_cast<uintptr_t>(A->W0p) | reinterpret_cast<uintptr_t>(A->W1p) |
-       reinterpret_cast<uintptr_t>(A->W2p)) & 15)
+       reinterpret_cast<uintptr_t>(A->W2p) | reinterpret_cast<uintptr_t>(A->Whp) |
+       reinterpret_cast<uintptr_t>(A->b0) | reinterpret_cast<uintptr_t>(A->b1) | reinterpret_cast<uintptr_t>(A->b2)) &
+      15)
     return VX_ERR_ARG;
   MlpTcParams P{};
   P.X = reinterpret_cast<const __nv_bfloat16*>(A->X);
@@ -408,7 +441,7 @@ int vx_mlp_tc_forward(const vx_mlp_tc_args* A, void* stream) {
   P.b0 = A->b0;
   P.b1 = A->b1;
   P.b2 = A->b2;
-  P.Wh = A->Wh;
+  P.Whp = reinterpret_cast<const __nv_bfloat16*>(A->Whp);
   P.bh = A->bh;
   P.add = A->add;
   P.out = A->out;

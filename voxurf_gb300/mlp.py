@@ -136,7 +136,8 @@ class TensorCoreMLP:
     ReLU], Linear(192,3)) packed for the fused tcgen05 forward
     (vx_mlp_tc_forward): hidden weights BF16 in the operand layout, first
     layer K zero-padded to K0 (multiple of 16), biases rounded to BF16 like
-    the GEMM path, output layer FP32.  Inference only (no autograd)."""
+    the GEMM path, the FP32 output layer as BF16 hi + lo rows of a 16-wide
+    tensor-core tile.  Inference only (no autograd)."""
 
     WIDTH = 192
 
@@ -162,7 +163,16 @@ class TensorCoreMLP:
             call("vx_mlp_tc_pack", ptr(W), self.WIDTH, W.shape[1], Kp, ptr(out), st)
             self.packed.append(out)
         self.biases = [m.bias.detach().to(torch.bfloat16).float().contiguous() for m in lin[:3]]
-        self.Wh = lin[3].weight.detach().float().contiguous()
+        # output layer on the tensor cores: FP32 weights as BF16 hi + lo parts
+        Wh = lin[3].weight.detach().float()
+        hi = Wh.to(torch.bfloat16).float()
+        lo = (Wh - hi).to(torch.bfloat16).float()
+        Wsplit = torch.zeros((16, self.WIDTH), dtype=torch.float32, device=dev)
+        Wsplit[0:3] = hi
+        Wsplit[3:6] = lo
+        self.Whp = torch.empty(16 * self.WIDTH, dtype=torch.bfloat16, device=dev)
+        call("vx_mlp_tc_pack", ptr(Wsplit), 16, self.WIDTH, self.WIDTH, ptr(self.Whp), st)
+        self._Wsplit = Wsplit  # kept alive until the pack kernel has run
         self.bh = lin[3].bias.detach().float().contiguous()
 
     def forward(self, X: torch.Tensor, out: torch.Tensor, add: torch.Tensor | None = None,
@@ -174,6 +184,6 @@ class TensorCoreMLP:
         a.X, a.ldx, a.K0, a.n_rows, a.width = ptr(X), X.stride(0), self.K0, X.shape[0], self.WIDTH
         a.W0p, a.W1p, a.W2p = (ptr(t) for t in self.packed)
         a.b0, a.b1, a.b2 = (ptr(t) for t in self.biases)
-        a.Wh, a.bh, a.add, a.out = ptr(self.Wh), ptr(self.bh), ptr(add), ptr(out)
+        a.Whp, a.bh, a.add, a.out = ptr(self.Whp), ptr(self.bh), ptr(add), ptr(out)
         a.cols, a.ld_cols = ptr(cols), ld_cols
         _abi.call_struct("vx_mlp_tc_forward", a, stream_ptr(X.device))
