@@ -196,15 +196,40 @@ template <typename T>
 __device__ __forceinline__ int put_pe(T* row, int c, const float x[3], int n_freq) {
   // [x, sin(x*2^f) (axis-major), cos(...)] as torch.cat([x, emb.sin(), emb.cos()])
   // with emb = (x.unsqueeze(-1) * freq).flatten(-2)  (voxurf_fine.py:694-698).
+  // FP32 rows: sincosf of every frequency.  BF16 rows: sincosf of the base
+  // frequency and the double-angle recurrence above it (error ~2^q ulp of
+  // FP32 at frequency 2^q, far below the BF16 rounding of the row).
 #pragma unroll
   for (int a = 0; a < 3; ++a) put(row, c + a, x[a]);
   c += 3;
-  for (int a = 0; a < 3; ++a)
-    for (int q = 0; q < n_freq; ++q) put(row, c + a * n_freq + q, sinf(x[a] * (float)(1 << q)));
-  c += 3 * n_freq;
-  for (int a = 0; a < 3; ++a)
-    for (int q = 0; q < n_freq; ++q) put(row, c + a * n_freq + q, cosf(x[a] * (float)(1 << q)));
-  return c + 3 * n_freq;
+  const int cs = c, cc = c + 3 * n_freq;
+  for (int a = 0; a < 3; ++a) {
+    if (sizeof(T) == 2) {
+      float s, co;
+      sincosf(x[a], &s, &co);
+      for (int q = 0; q < n_freq; ++q) {
+        put(row, cs + a * n_freq + q, s);
+        put(row, cc + a * n_freq + q, co);
+        const float s2 = 2.f * s * co, c2 = (co - s) * (co + s);
+        s = s2;
+        co = c2;
+      }
+    } else {
+      for (int q = 0; q < n_freq; ++q) {
+        float s, co;
+        sincosf(x[a] * (float)(1 << q), &s, &co);
+        put(row, cs + a * n_freq + q, s);
+        put(row, cc + a * n_freq + q, co);
+      }
+    }
+  }
+  return cc + 3 * n_freq;
+}
+
+// Columns [c_src, c_src + n) of a staged row copied to [c_dst, ...) of another.
+template <typename T>
+__device__ __forceinline__ void copy_cols(const T* src, int c_src, T* dst, int c_dst, int n) {
+  for (int i = 0; i < n; ++i) dst[c_dst + i] = src[c_src + i];
 }
 
 // Hierarchical features of one point: feat[6K] (dir-major: z-,z+,y-,y+,x-,x+
@@ -423,8 +448,10 @@ __device__ __forceinline__ void hier_features_k(const float* __restrict__ sdf, c
 // ([k0], PE(xyz_n), PE(v), [sdf], 6K hierarchical values, 3K normalised
 // gradients) and the k_rgbnet input row x2 without its trailing logits
 // (k0, PE(xyz_n), PE(v), d=1 gradient, [sdf]); g1 = the d=1 gradient (xyz).
-// KK = L.K (instantiated per displacement count).
-template <typename T, int KK>
+// KK = L.K (instantiated per displacement count).  REUSE: x1 and x2 are
+// rows staged in shared memory, so x2's positional encodings are copied
+// from x1 when both use the same frequencies.
+template <typename T, int KK, bool REUSE = false>
 __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf, const GridGeom& g, float vs,
                                                   const float* __restrict__ k0f,
                                                   const __nv_bfloat16* __restrict__ k0h, const FeatLayout& L,
@@ -470,6 +497,7 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
     for (int ch = 0; ch < 12; ++ch) put(x1, ch, k0v[ch]);
     col = 12;
   }
+  const int pe1 = col;  // the two encodings of x1 start here
   col = put_pe(x1, col, xyzn, L.pos_pe);
   col = put_pe(x1, col, v, L.view_pe);
   if (L.center_sdf) put(x1, col++, s);
@@ -487,8 +515,15 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
   col = 12;
 #pragma unroll
   for (int ch = 0; ch < 12; ++ch) put(x2, ch, k0v[ch]);
-  col = put_pe(x2, col, xyzn, L.kpos_pe);
-  col = put_pe(x2, col, v, L.kview_pe);
+  if (REUSE && L.kpos_pe == L.pos_pe && L.kview_pe == L.view_pe) {
+    // same encodings as x1 (rows staged in shared memory): copy, do not recompute
+    const int n = (3 + 6 * L.pos_pe) + (3 + 6 * L.view_pe);
+    copy_cols(x1, pe1, x2, col, n);
+    col += n;
+  } else {
+    col = put_pe(x2, col, xyzn, L.kpos_pe);
+    col = put_pe(x2, col, v, L.kview_pe);
+  }
   put(x2, col++, g1[0]);
   put(x2, col++, g1[1]);
   put(x2, col++, g1[2]);

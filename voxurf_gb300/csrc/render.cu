@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(128) features_fine_kernel(FeatParams P) {
     T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * sl1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
     T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * sl2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
     float g1[3];
-    fine_feature_rows<T, KK>(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
+    fine_feature_rows<T, KK, STAGE>(P.sdf, P.g, P.voxel_size, P.k0f, P.k0h, P.L, p, v, x1, x2, g1);
     for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
     for (int c = P.cols2; c < P.ld2; ++c) put(x2, c, 0.f);
     if (P.normal_out) {

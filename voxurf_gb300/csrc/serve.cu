@@ -5,14 +5,17 @@
 // constants from a table that each block copies into shared memory.
 //
 //   rays      : per ray, its view chunk (binary search) -> get_rays.
+//   first     : per ray (one thread), the first sample that can lie in the
+//               mask, from the mask's block occupancy (scenes that have one).
 //   march     : per ray (one warp, 32 samples per iteration), exact samples,
 //               mask, SDF + FD normal, NeuS alpha, transmittance scan with the
 //               T < 1e-3 stop; only shaded samples (weight > thres) are kept,
 //               as 8-byte (step, weight) records.
 //   rows      : row -> ray map of the dense shaded rows.
 //   features  : MLP input rows (fine_feature_rows), BF16 or FP32.
-//   mlp_head  : the 192 -> 3 output layer with FP32 accumulation (the
-//               hidden layers are GEMMs issued by the host).
+//   mlp_head  : the 192 -> 3 output layer with FP32 accumulation, for the
+//               FP32 scenes whose hidden layers are GEMMs issued by the host
+//               (BF16 scenes run the whole MLP in the fused tcgen05 kernel).
 //   composite : per ray, sum w*sigmoid(logit) + alphainv_last*bg (clamped in
 //               the k-branch) and depth, written into the output images.
 #include <math.h>
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
     T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * sl1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
     T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * sl2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
     float g1[3];
-    fine_feature_rows<T, KK>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
+    fine_feature_rows<T, KK, STAGE>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
     for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
     for (int c = STAGE ? P.cols2 : P.cols2 + 3; c < P.ld2; ++c) put(x2, c, 0.f);
   }
