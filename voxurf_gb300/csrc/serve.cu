@@ -183,12 +183,14 @@ struct ServeMarchParams {
   int* err;
 };
 
-// First sample of each ray that can lie in its scene's mask (scenes with an
-// occupancy grid; 0 otherwise), written to n2[r] for the march to start at.
-// One thread per ray: the block walk is serial per ray, so 32 rays share a
-// warp's instruction stream (a warp-per-ray walk would spend 32x the issue
-// slots).  Exact: skip_empty only passes cells of the one-voxel-widened
-// occupancy that hold no mask voxel.
+// First and last sample of each ray that can lie in its scene's mask
+// (scenes with an occupancy grid), written to n2[r] and (as int bits)
+// alphainv_last[r] for the march to start and end at; both outputs are
+// overwritten by the march.  One thread per ray: the block walk is serial
+// per ray, so 32 rays share a warp's instruction stream (a warp-per-ray walk
+// would spend 32x the issue slots).  Exact: skip_empty only passes cells of
+// the one-voxel-widened occupancy that hold no mask voxel, and either walk's
+// float model is within far less than the widening of the exact samples.
 __global__ void __launch_bounds__(256) serve_first_kernel(ServeMarchParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
   load_scenes(P.T, sh);
@@ -209,7 +211,21 @@ __global__ void __launch_bounds__(256) serve_first_kernel(ServeMarchParams P) {
   }
   const RayFrame f = ray_frame(o, d, S.g.mn, S.g.mx, S.near, S.stepdist);
   const int n_steps = (int)min(f.n_steps, (int64_t)P.max_steps);
-  P.n2[r] = skip_empty(skip_model(f, S), 0, n_steps, S);
+  const SkipModel fwd = skip_model(f, S);
+  const int first = skip_empty(fwd, 0, n_steps, S);
+  // last possible sample: the same walk from the far end (model reversed)
+  int last = -1;
+  if (first < n_steps) {
+    SkipModel rev;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      rev.u0[a] = fwd.u0[a] + fwd.du[a] * (float)(n_steps - 1);
+      rev.du[a] = -fwd.du[a];
+    }
+    last = (n_steps - 1) - skip_empty(rev, 0, n_steps - first, S);
+  }
+  P.n2[r] = first;
+  P.alphainv_last[r] = __int_as_float(last);  // stashed for the march, which overwrites it
 }
 
 template <bool DENS>  // some scene carries a MaskCache density mask
@@ -247,10 +263,12 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
   double carry = 1.0, last = 1.0;
   int cnt2 = 0;
   bool stopped = false;
-  // with an occupancy grid, serve_first_kernel left the first sample that
-  // can lie in the mask in n2[r]: every earlier sample is masked out
+  // with an occupancy grid, serve_first_kernel left the first and the last
+  // sample that can lie in the mask in n2[r] and alphainv_last[r]: every
+  // sample outside [k0, kl] is masked out
   const int k0 = S.occ ? P.n2[r] : 0;
-  for (int base = k0; !stopped; base += 32) {
+  const int kl = S.occ ? __float_as_int(P.alphainv_last[r]) : INT_MAX;
+  for (int base = k0; !stopped && base <= kl; base += 32) {
     if (base >= n_steps) break;
     const int k = base + lane;
     bool keep = false;
