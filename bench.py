@@ -106,6 +106,32 @@ def dist_setup(args):
     return world, rank, local
 
 
+def rank_barrier(world, dev):
+    """All replicas reach this point, with their device work finished."""
+    import torch
+
+    if world > 1:
+        torch.distributed.barrier()
+    if dev.type == "cuda":
+        torch.cuda.synchronize(dev)
+
+
+def max_over_ranks_of(x: float, world: int, dev) -> float:
+    """The slowest replica's time (max over ranks; gloo on CPU, NCCL on GPU)."""
+    import torch
+
+    if world > 1:
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+    return x
+
+
+def whole_job_rays_per_s(world: int, rays_per_step: int, steps: int, t_max: float) -> float:
+    """Rays of all replicas over the slowest replica's timed region."""
+    return world * rays_per_step * steps / t_max
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
 
@@ -200,16 +226,10 @@ def run_ours(args, world, rank, local):
         return model, FineTrainer(model, n_rays=N_RAYS, graphed=graphed)
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
+        rank_barrier(world, dev)
 
     def max_over_ranks(x):
-        if world > 1:
-            t = torch.tensor([x], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return x
+        return max_over_ranks_of(x, world, dev)
 
     # ---- plain FP32, device-resident batches ---------------------------------
     model, tr = build("fp32")
@@ -247,7 +267,7 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
     sweep_ms = [a.elapsed_time(b) for a, b in timing["events"]]
     t_total = max_over_ranks(ms / 1000.0)
-    value = world * N_RAYS * args.steps / t_total
+    value = whole_job_rays_per_s(world, N_RAYS, args.steps, t_total)
     shaded = int(model._last_frame.S2)
 
     # ---- e2e: same step, batches from pinned host memory, loss read back -------
@@ -263,7 +283,7 @@ def run_ours(args, world, rank, local):
             e2e_losses.append(float(loss.item()))
         barrier()
         t_e2e = max_over_ranks(time.perf_counter() - w0)
-        e2e = world * N_RAYS * args.steps / t_e2e
+        e2e = whole_job_rays_per_s(world, N_RAYS, args.steps, t_e2e)
         h2d = sum(p[0].numel() * p[0].element_size() for p in pinned)
     del tr, model
     torch.cuda.empty_cache()

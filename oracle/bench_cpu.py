@@ -40,7 +40,7 @@ def build_cpu_oracle(R: int, seed: int = 0, mask_voxels: float | None = 6.4, wid
     if mask is not None:
         scale = ((np.array(mask.shape, np.float32) - 1) / np.float32(2.0)).astype(np.float32)
         shift = (np.float32(1.0) * scale).astype(np.float32)
-        oracle.mask = (torch.from_numpy(mask), torch.from_numpy(scale), torch.from_numpy(shift))
+        oracle.mask = ("grid", torch.from_numpy(mask), torch.from_numpy(scale), torch.from_numpy(shift))
     return oracle, float(model.world_size.max())
 
 
