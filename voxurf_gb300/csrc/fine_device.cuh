@@ -347,27 +347,45 @@ inline int64_t x2_cols(const vx_fine_feature_cfg* c) {
 // instead of 8 voxels per probe.  Voxels outside the grid are zero
 // (grid_sample padding 'zeros'); a probe at floor fl with fraction t reads
 // planes fl and fl+1, as its own trilinear lookup would.
+// The 2x2 cross-section of the point perpendicular to axis A: the flat
+// offsets of its four voxels without the A term, their validity and
+// bilinear weights, formed once and reused for every plane p along A (the
+// flat index is p * stride(A) + off).
 template <int A>
-__device__ __forceinline__ float plane_bilerp(const float* __restrict__ sdf, const GridGeom& g, int p,
-                                              const int i0[3], const float t[3]) {
-  constexpr int B = A == 0 ? 1 : 0, C = A == 2 ? 1 : 2;
-  if (p < 0 || p >= gsize(g, A)) return 0.f;
-  float acc = 0.f;
+struct CrossSection {
+  int off[4];
+  bool ok[4];
+  float w[4];
+  int stride, n;
+
+  __device__ __forceinline__ CrossSection(const GridGeom& g, const int i0[3], const float t[3]) {
+    constexpr int B = A == 0 ? 1 : 0, C = A == 2 ? 1 : 2;
+    const int strides[3] = {g.Y * g.Z, g.Z, 1};
+    stride = strides[A];
+    n = gsize(g, A);
 #pragma unroll
-  for (int db = 0; db < 2; ++db)
+    for (int db = 0; db < 2; ++db)
 #pragma unroll
-    for (int dc = 0; dc < 2; ++dc) {
-      const int ib = i0[B] + db, ic = i0[C] + dc;
-      if (ib < 0 || ib >= gsize(g, B) || ic < 0 || ic >= gsize(g, C)) continue;
-      int idx[3];
-      idx[A] = p;
-      idx[B] = ib;
-      idx[C] = ic;
-      const float w = (db ? t[B] : 1.f - t[B]) * (dc ? t[C] : 1.f - t[C]);
-      acc += w * __ldg(sdf + ((int64_t)idx[0] * g.Y + idx[1]) * g.Z + idx[2]);
-    }
-  return acc;
-}
+      for (int dc = 0; dc < 2; ++dc) {
+        const int q = 2 * db + dc;
+        const int ib = i0[B] + db, ic = i0[C] + dc;
+        ok[q] = ib >= 0 && ib < gsize(g, B) && ic >= 0 && ic < gsize(g, C);
+        off[q] = ib * strides[B] + ic * strides[C];
+        w[q] = (db ? t[B] : 1.f - t[B]) * (dc ? t[C] : 1.f - t[C]);
+      }
+  }
+
+  // bilinear value on plane p (zero outside the grid)
+  __device__ __forceinline__ float plane(const float* __restrict__ sdf, int p) const {
+    if (p < 0 || p >= n) return 0.f;
+    const float* base = sdf + (int64_t)p * stride;
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (ok[q]) acc += w[q] * __ldg(base + off[q]);
+    return acc;
+  }
+};
 
 // Value at coordinate q along the axis from planes P[0..5] = i0-2 .. i0+3.
 __device__ __forceinline__ float plane_lerp(const float P[6], int i0, float q) {
@@ -400,11 +418,20 @@ __device__ __forceinline__ void hier_features_planes(const float* __restrict__ s
     t[a] = ind[a] - fl;
   }
   float P[3][6];
+  {
+    const CrossSection<0> cs(g, i0, t);
 #pragma unroll
-  for (int p = 0; p < 6; ++p) {
-    P[0][p] = plane_bilerp<0>(sdf, g, i0[0] - 2 + p, i0, t);
-    P[1][p] = plane_bilerp<1>(sdf, g, i0[1] - 2 + p, i0, t);
-    P[2][p] = plane_bilerp<2>(sdf, g, i0[2] - 2 + p, i0, t);
+    for (int p = 0; p < 6; ++p) P[0][p] = cs.plane(sdf, i0[0] - 2 + p);
+  }
+  {
+    const CrossSection<1> cs(g, i0, t);
+#pragma unroll
+    for (int p = 0; p < 6; ++p) P[1][p] = cs.plane(sdf, i0[1] - 2 + p);
+  }
+  {
+    const CrossSection<2> cs(g, i0, t);
+#pragma unroll
+    for (int p = 0; p < 6; ++p) P[2][p] = cs.plane(sdf, i0[2] - 2 + p);
   }
   *s = (1.f - t[0]) * P[0][2] + t[0] * P[0][3];
 #pragma unroll
