@@ -68,6 +68,8 @@ def parse():
     p.add_argument("--no-eikonal", action="store_true",
                    help="skip the eikonal-training (coarse 96^3, 8192/32768 rays) measurement")
     p.add_argument("--no-mesh", action="store_true", help="skip the 512^3 mesh-extraction field measurement")
+    p.add_argument("--no-background", action="store_true",
+                   help="skip the background-sample generator measurement (scenes without an object mask)")
     p.add_argument("--micro", choices=["smooth", "mlp_tc"], default=None,
                    help="single-kernel timing instead of the step (profiling): the Gaussian smoothing sweep "
                         "on a --grid^3 grid, or the fused tensor-core MLP against the GEMM path")
@@ -334,6 +336,9 @@ def run_ours(args, world, rank, local):
     mesh = None
     if not args.no_mesh and R == 256:
         mesh = run_mesh_query(args, dev)
+    bg_samples = None
+    if not args.no_background and R == 256:
+        bg_samples = run_background(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -355,6 +360,7 @@ def run_ours(args, world, rank, local):
             "long_rays": long_rays,
             "eikonal_train": eikonal,
             "mesh_query": mesh,
+            "background_samples": bg_samples,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -520,6 +526,32 @@ def run_mesh_query(args, dev):
             "ms": ms, "field_ms": ms_field, "points_per_s": MESH_R ** 3 / (ms / 1000.0),
             "field_write_gbs": field_bytes / (ms_field / 1000.0) / 1e9,
             "field_frac_of_hbm": field_bytes / (ms_field / 1000.0) / 1e9 / peak}
+
+
+def run_background(args, dev):
+    """Background samples of a scene without an object mask (the womask
+    fine model's sample_ray_ori + inversion + cumdist_thres + compaction) for
+    8192 training rays (with jitter) on the 256^3 grid's 891 candidates per
+    ray: count launch, device scan, one 8-byte read of the total, fill
+    launch; CUDA events around the public call."""
+    import numpy as np
+    import torch
+
+    from voxurf_gb300 import background, synthetic
+
+    o, d, _ = synthetic.random_rays(N_RAYS, seed=21)
+    o, d = torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev)
+    jit = torch.rand(N_RAYS, device=dev, generator=torch.Generator(dev).manual_seed(0))
+    vs = np.float32(2.0 / R)
+    S = background.n_samples_for([R, R, R], 0.5)
+    mn, mx = [-1.0] * 3, [1.0] * 3
+    fn = lambda: background.background_samples(o, d, mn, mx, 0.2, 1e9, 0.5, vs, S, jit)  # noqa: E731
+    ms = _event_ms(fn, 3, 10)
+    kept = int(fn()[0].shape[0])
+    return {"workload": f"womask background samples: {N_RAYS} rays x {S} candidates (256^3 grid, stepsize 0.5, "
+                        "jitter), inversion + cumdist_thres + compaction",
+            "ms": ms, "candidates_per_s": N_RAYS * S / (ms / 1000.0), "kept_samples": kept,
+            "bytes_written": kept * 64}
 
 
 EIK_R = 96                 # differentiation workload: coarse grids/MLP, eikonal 0.1

@@ -687,6 +687,56 @@ int vx_serve_composite(const vx_scene_desc* scenes_host, int32_t n_scenes, const
                        const float* klogit, const float* alphainv_last, const int64_t* ray_out, float* out_rgb,
                        float* out_depth, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Background branch of the scenes without an object mask
+ * (lib/voxurf_womask_fine.py, lib/voxurf_womask_coarse.py).
+ * ------------------------------------------------------------------------ */
+
+/* ub360_utils.cpp / ub360_utils_kernel.cu:13-31 (ub360_utils_cuda.
+ * cumdist_thres, called at voxurf_womask_fine.py:867 and
+ * voxurf_womask_coarse.py:645): mask[r, i] = 1 where the running sum of
+ * dist[r, :i+1] since the last mark exceeds thres; the sum restarts from 0
+ * after a mark.  dist and mask: [n_rays, n_pts] row-major, float32 / bytes. */
+int vx_cumdist_thres(const float* dist, int64_t n_rays, int64_t n_pts, float thres, uint8_t* mask, void* stream);
+
+/* Background samples of voxurf_womask_fine.py:857-870 (sample_ray_ori at
+ * :789-818 with use_bg=False, outside_sphere_trans(filtered=True) at
+ * :820-825, the inverted-sample distances and cumdist_thres, then the
+ * compaction by bg_mask) and of voxurf_womask_coarse.py:633-650.  Sample k
+ * of ray r (k < n_samples) is p = o + d*(t_min + stepdist*(k + jitter[r])/|d|)
+ * with t_min the slab entry clamped to [near, far]; it is kept when |p| >= 1,
+ * when (outbbox_only) it lies outside the bbox or its ray misses the bbox
+ * (the coarse model's bg_mask & mask_outbbox), and when k = 0 or the running
+ * distance between consecutive inverted points p/|p|^2 exceeds dist_thres.
+ * jitter: [n_rays] device floats (the training-time torch.rand of :808) or
+ * NULL. */
+typedef struct {
+  const float* rays_o;      /* [n_rays,3] */
+  const float* rays_d;      /* [n_rays,3] */
+  const float* jitter;      /* [n_rays] or NULL */
+  float xyz_min[3];
+  float xyz_max[3];
+  float near;
+  float far;
+  float stepdist;           /* stepsize * voxel size (float32, as the reference's tensor) */
+  float dist_thres;         /* voxel_size * stepsize * 0.5 (fine) or * 0.95 (coarse), float32 */
+  int32_t n_samples;        /* int(|grid shape + 1| / stepsize) + 1 */
+  int32_t outbbox_only;     /* 1: the coarse model's additional mask_outbbox test */
+  int64_t n_rays;
+} vx_bg_sample_args;
+
+/* Phase 1: counts [n_rays] kept samples per ray and offsets [n_rays+1]
+ * (offsets[n_rays] = M); scratch: vx_scan_scratch_bytes(n_rays) bytes. */
+int vx_bg_samples_count(const vx_bg_sample_args* args, int64_t* counts, int64_t* offsets, void* scratch,
+                        size_t scratch_bytes, void* stream);
+
+/* Phase 2: the kept samples in ray order: outer_pts [M,3] (inverted),
+ * pts_org [M,3], ray_id [M], step_id [M] (k).  Writes at or beyond
+ * `capacity` are skipped and reported as VX_ERR_CAPACITY through
+ * vx_device_error(). */
+int vx_bg_samples_fill(const vx_bg_sample_args* args, const int64_t* offsets, int64_t capacity, float* outer_pts,
+                       float* pts_org, int64_t* ray_id, int64_t* step_id, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

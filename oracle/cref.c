@@ -296,3 +296,72 @@ void vxo_adam_upd(int mode, float* param, const float* grad, float* exp_avg, flo
       param[i] -= step_size * exp_avg[i] / (sqrtf(exp_avg_sq[i]) + eps);
   }
 }
+
+/* ---- ub360_utils_kernel.cu:13-31 (cumdist_thres) ----------------------------- */
+void vxo_cumdist_thres(const float* dist, int64_t n_rays, int64_t n_pts, float thres, uint8_t* mask) {
+  for (int64_t r = 0; r < n_rays; ++r) {
+    float cum = 0.f;
+    for (int64_t i = r * n_pts; i < (r + 1) * n_pts; ++i) {
+      cum += dist[i];
+      const int over = cum > thres;
+      cum *= (float)(!over);
+      mask[i] = (uint8_t)over;
+    }
+  }
+}
+
+/* |v| as torch's norm reduction forms it (fused multiply-add accumulation). */
+static float norm3_fma(float x, float y, float z) { return sqrtf(fmaf(z, z, fmaf(y, y, x * x))); }
+
+/* ---- background samples, lib/voxurf_womask_fine.py:789-818 (sample_ray_ori),
+ * :820-825 (outside_sphere_trans, filtered), :857-868 (bg_mask with the
+ * cumdist_thres of consecutive inverted points); coarse variant
+ * voxurf_womask_coarse.py:633-646 (outbbox_only).  Dense outputs over all
+ * [n_rays, n_samples] candidates: pts [.,3], inv [.,3], keep [.]. */
+void vxo_bg_samples(const float* rays_o, const float* rays_d, const float* jitter, const float* mn, const float* mx,
+                    float near, float far, float stepdist, float dist_thres, int n_samples, int outbbox_only,
+                    int64_t n_rays, float* pts, float* inv, uint8_t* keep) {
+  for (int64_t r = 0; r < n_rays; ++r) {
+    const float* o = rays_o + 3 * r;
+    const float* d = rays_d + 3 * r;
+    float tmin = -INFINITY, tmax = INFINITY;
+    for (int i = 0; i < 3; ++i) {
+      const float v = d[i] == 0.f ? 1e-6f : d[i];
+      const float ra = (mx[i] - o[i]) / v;
+      const float rb = (mn[i] - o[i]) / v;
+      tmin = fmaxf(tmin, fminf(ra, rb));
+      tmax = fminf(tmax, fmaxf(ra, rb));
+    }
+    tmin = fminf(fmaxf(tmin, near), far);
+    tmax = fminf(fmaxf(tmax, near), far);
+    const int miss = tmax <= tmin;
+    const float dn = norm3_fma(d[0], d[1], d[2]);
+    float cum = 0.f;
+    for (int k = 0; k < n_samples; ++k) {
+      const int64_t s = r * n_samples + k;
+      const float rng = jitter ? (float)k + jitter[r] : (float)k;
+      const float t = tmin + (stepdist * rng) / dn;
+      float* p = pts + 3 * s;
+      float* q = inv + 3 * s;
+      for (int i = 0; i < 3; ++i) p[i] = o[i] + d[i] * t;
+      const float n = norm3_fma(p[0], p[1], p[2]);
+      const float n2 = n * n;
+      for (int i = 0; i < 3; ++i) q[i] = p[i] / n2;
+      int kp = !(n < 1.f);
+      if (outbbox_only) {
+        int out = miss;
+        for (int i = 0; i < 3; ++i) out = out || (mn[i] > p[i]) || (p[i] > mx[i]);
+        kp = kp && out;
+      }
+      if (k > 0) {
+        const float* qp = q - 3;
+        const float dx = q[0] - qp[0], dy = q[1] - qp[1], dz = q[2] - qp[2];
+        cum += norm3_fma(dx, dy, dz);
+        const int over = cum > dist_thres;
+        cum *= (float)(!over);
+        kp = kp && over;
+      }
+      keep[s] = (uint8_t)kp;
+    }
+  }
+}

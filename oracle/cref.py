@@ -165,3 +165,37 @@ def adam_upd(mode, param, grad, exp_avg, exp_avg_sq, step, beta1, beta2, lr, eps
     lib().vxo_adam_upd(C.c_int(mode), _p(param), _p(grad), _p(exp_avg), _p(exp_avg_sq),
                        None if pl is None else _p(pl), C.c_int64(param.size), C.c_int(step), C.c_float(beta1),
                        C.c_float(beta2), C.c_float(lr), C.c_float(eps))
+
+
+def cumdist_thres(dist, thres):
+    """ub360_utils_kernel.cu:13-31 -> bool [n_rays, n_pts]."""
+    dist = _f32(dist)
+    n_rays, n_pts = dist.shape
+    mask = np.zeros((n_rays, n_pts), np.uint8)
+    lib().vxo_cumdist_thres(_p(dist), C.c_int64(n_rays), C.c_int64(n_pts), C.c_float(thres), _p(mask))
+    return mask.astype(bool)
+
+
+def bg_samples_dense(rays_o, rays_d, xyz_min, xyz_max, near, far, stepdist, dist_thres, n_samples, jitter=None,
+                     outbbox_only=False):
+    """Background candidates of voxurf_womask_fine.py:857-868 (coarse variant
+    with outbbox_only) over all [N, S] samples -> (pts, inverted pts, keep)."""
+    rays_o, rays_d, mn, mx = _f32(rays_o), _f32(rays_d), _f32(xyz_min), _f32(xyz_max)
+    n = rays_o.shape[0]
+    jit = None if jitter is None else _f32(jitter)
+    pts = np.zeros((n, n_samples, 3), np.float32)
+    inv = np.zeros((n, n_samples, 3), np.float32)
+    keep = np.zeros((n, n_samples), np.uint8)
+    lib().vxo_bg_samples(_p(rays_o), _p(rays_d), None if jit is None else _p(jit), _p(mn), _p(mx), C.c_float(near),
+                         C.c_float(far), C.c_float(stepdist), C.c_float(dist_thres), C.c_int(n_samples),
+                         C.c_int(int(bool(outbbox_only))), C.c_int64(n), _p(pts), _p(inv), _p(keep))
+    return pts, inv, keep.astype(bool)
+
+
+def bg_samples(rays_o, rays_d, xyz_min, xyz_max, near, far, stepdist, dist_thres, n_samples, jitter=None,
+               outbbox_only=False):
+    """Compacted like :868-870 -> (outer_pts, outer_pts_org, ray_id, step_id)."""
+    pts, inv, keep = bg_samples_dense(rays_o, rays_d, xyz_min, xyz_max, near, far, stepdist, dist_thres, n_samples,
+                                      jitter, outbbox_only)
+    ray_id, step_id = np.nonzero(keep)
+    return inv[keep], pts[keep], ray_id.astype(np.int64), step_id.astype(np.int64)

@@ -38,6 +38,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 REF = os.environ.get("VOXURF_REFERENCE", "/root/reference")
 sys.path.insert(0, REPO)
 
+from oracle import cref  # noqa: E402
 from oracle.ops import RenderUtilsOracle, TotalVariationOracle  # noqa: E402
 
 STUBS = ("cv2", "mcubes", "matplotlib", "matplotlib.pyplot", "matplotlib.cm", "plyfile", "imageio", "skimage",
@@ -83,6 +84,9 @@ def install_stubs():
             return RenderUtilsOracle
         if name == "total_variation_cuda":
             return TotalVariationOracle
+        if name == "ub360_utils_cuda":
+            return types.SimpleNamespace(
+                cumdist_thres=lambda dist, thres: torch.from_numpy(cref.cumdist_thres(dist.numpy(), float(thres))))
         return types.SimpleNamespace()
 
     cpp.load = fake_load
@@ -335,10 +339,71 @@ def ckpt_fixture(dirpath, R=16, seed=7):
     print("wrote", ckpt_c, ckpt_f, "shaded samples", ret["weights"].numel(), "hits", int(hit.sum()))
 
 
+def bg_fixture(path, seed=8):
+    """Background samples of the models without an object mask: the
+    reference's sample_ray_ori and outside_sphere_trans (womask fine
+    :789-825, womask coarse :568-604) called on a holder object, then the
+    mask and compaction statements of voxurf_womask_fine.py:860-870 and
+    voxurf_womask_coarse.py:637-650 as written there, with cumdist_thres from
+    the oracle (its CUDA source cannot run on the host).  The per-ray
+    training jitter (torch.rand_like at :808) is fixed by the fixture."""
+    import lib.voxurf_womask_coarse as wc
+    import lib.voxurf_womask_fine as wf
+
+    from oracle import cref
+
+    g = torch.Generator().manual_seed(seed)
+    n = 96
+    o = torch.rand((n, 3), generator=g) * 3.2 - 1.6
+    d = torch.randn((n, 3), generator=g)
+    d[:6, 0] = 0.0   # zero direction components (the 1e-6 substitution)
+    d[6:10, 1:] = 0.0
+    d[10:14] = -o[10:14] + 0.05 * torch.randn((4, 3), generator=g)   # towards the centre
+    jit = torch.rand((n,), generator=g)
+    xyz_min, xyz_max = torch.tensor([-1.0, -1.0, -1.0]), torch.tensor([1.0, 1.0, 1.0])
+    R, Rb, stepsize, near, far = 24, 20, 0.5, 0.2, 6.0
+    vs = ((xyz_max - xyz_min).prod() / R ** 3).pow(1 / 3)
+    vs_bg = ((xyz_max - xyz_min).prod() / Rb ** 3).pow(1 / 3)
+    holder = types.SimpleNamespace(xyz_min=xyz_min, xyz_max=xyz_max, voxel_size=vs, voxel_size_bg=vs_bg,
+                                   sdf=types.SimpleNamespace(grid=torch.zeros((1, 1, R, R, R))),
+                                   bg_density=types.SimpleNamespace(grid=torch.zeros((1, 1, Rb, Rb, Rb))))
+    ub = types.SimpleNamespace(cumdist_thres=lambda dist, thres: torch.from_numpy(
+        cref.cumdist_thres(dist.numpy(), float(thres))))
+    out = {"rays_o": o.numpy(), "rays_d": d.numpy(), "jitter": jit.numpy(), "xyz_min": xyz_min.numpy(),
+           "xyz_max": xyz_max.numpy(), "near": np.float32(near), "far": np.float32(far),
+           "stepsize": np.float32(stepsize), "voxel_size": vs.numpy(), "voxel_size_bg": vs_bg.numpy()}
+    rand_like = torch.rand_like
+    try:
+        torch.rand_like = lambda x: jit[:, None].clone()
+        for tag, mod, train in (("fine", wf, False), ("fine_train", wf, True), ("coarse", wc, True)):
+            cls = mod.Voxurf
+            use_bg = tag == "coarse"
+            pts_org, mask_outbbox, _ = cls.sample_ray_ori(holder, o, d, near, far, stepsize, is_train=train,
+                                                          use_bg=use_bg)
+            # womask fine :860-868 / womask coarse :637-646
+            pn = torch.linalg.norm(pts_org, ord=2, dim=-1, keepdim=True)
+            inside = (pn < 1.0)[..., 0]
+            inv = cls.outside_sphere_trans(holder, pts_org, pn, filtered=True)
+            if use_bg:
+                bg_mask = ~inside & mask_outbbox
+                dist_thres = vs * stepsize * 0.95
+            else:
+                bg_mask = ~inside
+                dist_thres = vs * stepsize * 0.5
+            dist = (inv[:, 1:] - inv[:, :-1]).norm(dim=-1)
+            bg_mask[:, 1:] &= ub.cumdist_thres(dist, dist_thres)
+            out.update({f"{tag}_pts": pts_org.numpy(), f"{tag}_inv": inv.numpy(), f"{tag}_keep": bg_mask.numpy(),
+                        f"{tag}_dist": dist.numpy(), f"{tag}_thres": np.float32(dist_thres)})
+    finally:
+        torch.rand_like = rand_like
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
 def main():
     install_stubs()
     torch.set_default_dtype(torch.float32)
-    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt"]
+    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg"]
     if "ops" in which:
         ops_fixture(os.path.join(HERE, "ops_golden.npz"))
     if "fine" in which:
@@ -349,6 +414,8 @@ def main():
         mesh_fixture(os.path.join(HERE, "mesh_golden.npz"))
     if "ckpt" in which:
         ckpt_fixture(HERE)
+    if "bg" in which:
+        bg_fixture(os.path.join(HERE, "bg_golden.npz"))
 
 
 if __name__ == "__main__":

@@ -166,3 +166,42 @@ def test_coarse_step_oracle_matches_reference():
     assert rel(oracle.k0_grid.grad.numpy(), COARSE["grad_k0"]) < 1e-6
     for n, p in oracle.rgbnet.named_parameters():
         assert rel(p.grad.numpy(), COARSE["grad_mlp." + n]) < 1e-6, n
+
+
+def _bg_case(z, tag):
+    coarse = tag == "coarse"
+    vs = np.float32(z["voxel_size_bg"] if coarse else z["voxel_size"])
+    return dict(near=float(z["near"]), far=float(z["far"]), stepdist=float(np.float32(z["stepsize"]) * vs),
+                dist_thres=float(z[f"{tag}_thres"]), n_samples=z[f"{tag}_pts"].shape[1],
+                jitter=None if tag == "fine" else z["jitter"], outbbox_only=coarse)
+
+
+@pytest.mark.parametrize("tag", ["fine", "fine_train", "coarse"])
+def test_background_samples_restatement(tag):
+    """The oracle's background candidates (points, inverted points, kept
+    mask) equal the reference's sample_ray_ori / outside_sphere_trans /
+    cumdist_thres composition bit for bit (womask fine and coarse)."""
+    z = np.load(os.path.join(HERE, "bg_golden.npz"))
+    pts, inv, keep = cref.bg_samples_dense(z["rays_o"], z["rays_d"], z["xyz_min"], z["xyz_max"], **_bg_case(z, tag))
+    assert np.array_equal(pts, z[f"{tag}_pts"])
+    assert np.array_equal(inv, z[f"{tag}_inv"])
+    assert np.array_equal(keep, z[f"{tag}_keep"])
+    assert 0 < keep.sum() < keep.size
+
+
+def test_cumdist_thres_restatement():
+    """cumdist_thres on the reference's own distances: marks where the
+    running sum since the last mark first exceeds the threshold."""
+    z = np.load(os.path.join(HERE, "bg_golden.npz"))
+    dist, thres = z["fine_dist"], float(z["fine_thres"])
+    m = cref.cumdist_thres(dist, thres)
+    # the same recurrence written out in float32 numpy
+    want = np.zeros_like(m)
+    for r in range(dist.shape[0]):
+        cum = np.float32(0)
+        for i in range(dist.shape[1]):
+            cum = np.float32(cum + dist[r, i])
+            want[r, i] = cum > np.float32(thres)
+            if want[r, i]:
+                cum = np.float32(0)
+    assert np.array_equal(m, want)

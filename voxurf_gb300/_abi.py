@@ -84,6 +84,14 @@ class CoarseMarchArgs(C.Structure):
     _fields_ = [("march", FineMarchArgs), ("grad4", P), ("n2b", P)]
 
 
+class BgSampleArgs(C.Structure):
+    _fields_ = [
+        ("rays_o", P), ("rays_d", P), ("jitter", P), ("xyz_min", F * 3), ("xyz_max", F * 3), ("near", F),
+        ("far", F), ("stepdist", F), ("dist_thres", F), ("n_samples", I32), ("outbbox_only", I32),
+        ("n_rays", I64),
+    ]
+
+
 class CoarseFeatureCfg(C.Structure):
     _fields_ = [("use_k0", I32), ("geo_rgb_dim", I32), ("posbase_pe", I64), ("viewbase_pe", I64)]
 
@@ -197,6 +205,10 @@ def _declare():
     lib.vx_density_mask.restype = C.c_int
     lib.vx_hit_coarse_geo.argtypes = [C.POINTER(FineMarchArgs), P, P]
     lib.vx_hit_coarse_geo.restype = C.c_int
+    lib.vx_bg_samples_count.argtypes = [C.POINTER(BgSampleArgs), P, P, P, C.c_size_t, P]
+    lib.vx_bg_samples_count.restype = C.c_int
+    lib.vx_bg_samples_fill.argtypes = [C.POINTER(BgSampleArgs), P, I64, P, P, P, P, P]
+    lib.vx_bg_samples_fill.restype = C.c_int
     lib.vx_sdf_gradient_grid.argtypes = [P, P, I64, I64, I64, F, C.c_int, P]
     lib.vx_sdf_gradient_grid.restype = C.c_int
     lib.vx_sdf_gradient_grid_adjoint.argtypes = [P, P, I64, I64, I64, F, C.c_int, C.c_int, P]
@@ -235,4 +247,5 @@ def struct_names() -> list[str]:
     return list(_STRUCT_FNS) + ["vx_smooth3d", "vx_smooth3d_adjoint", "vx_grid_sample", "vx_grid_sample_backward",
                                 "vx_sdf_gradient_grid", "vx_sdf_gradient_grid_adjoint",
                                 "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv",
-                                "vx_sdf_field", "vx_density_mask", "vx_hit_coarse_geo"] + list(_SERVE_SIGNATURES)
+                                "vx_sdf_field", "vx_density_mask", "vx_hit_coarse_geo", "vx_bg_samples_count",
+                                "vx_bg_samples_fill"] + list(_SERVE_SIGNATURES)
