@@ -202,9 +202,10 @@ int vx_cumdist_thres(const float* dist, int64_t n_rays, int64_t n_pts, float thr
 
 int vx_bg_samples_count(const vx_bg_sample_args* args, int64_t* counts, int64_t* offsets, void* scratch,
                         size_t scratch_bytes, void* stream) {
-  if (!bg_args_ok(args) || !counts || !offsets) return VX_ERR_ARG;
+  if (!bg_args_ok(args) || !offsets) return VX_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   if (args->n_rays > 0) {
+    if (!counts) return VX_ERR_ARG;
     bg_samples_kernel<false><<<grid_for(args->n_rays, 128), 128, 0, st>>>(*args, counts, nullptr, 0, nullptr,
                                                                             nullptr, nullptr, nullptr, nullptr);
     const int s = launch_status();
