@@ -13,7 +13,7 @@
 //     it and the compaction of the kept samples.  The reference materialises
 //     [N, S, 3] points, their norms, the inverted points, the [N, S-1]
 //     distances and the masks in HBM (about 60 bytes per candidate sample)
-//     before compacting with boolean indexing; here one thread walks one ray
+//     before compacting with boolean indexing; here one warp walks one ray
 //     in registers and only the kept samples are written.
 // Every float operation is rounded as the reference's torch expressions
 // round it (one rounding per elementwise operation; the norms accumulate with
@@ -120,65 +120,99 @@ __device__ __forceinline__ bool bg_point(const vx_bg_sample_args& a, const BgRay
   return n < 1.f;
 }
 
-// One pass over the ray's samples; FILL writes the kept ones from `base`.
+// One warp per ray; the lanes take 32 consecutive samples at a time.  Each
+// lane forms its point, the inverted point and the distance to the previous
+// inverted point (shuffled up from the neighbouring lane); the cumdist
+// recurrence is serial along the ray, so every lane runs it over the 32
+// shuffled distances in order (the running sum is identical in all lanes)
+// and picks its own mark.  The kept samples of the 32 are compacted with a
+// ballot, so the fill pass writes consecutive records from consecutive lanes.
+constexpr int BG_THREADS = 256;
+
 template <bool FILL>
-__global__ void bg_samples_kernel(const vx_bg_sample_args a, int64_t* __restrict__ counts,
-                                  const int64_t* __restrict__ offsets, int64_t capacity, float* __restrict__ outer_pts,
-                                  float* __restrict__ pts_org, int64_t* __restrict__ ray_id,
-                                  int64_t* __restrict__ step_id, int* err) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.n_rays) return;
+__global__ void __launch_bounds__(BG_THREADS) bg_samples_kernel(
+    const vx_bg_sample_args a, int64_t* __restrict__ counts, const int64_t* __restrict__ offsets, int64_t capacity,
+    float* __restrict__ outer_pts, float* __restrict__ pts_org, int64_t* __restrict__ ray_id,
+    int64_t* __restrict__ step_id, int* err) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * BG_THREADS + threadIdx.x) >> 5;
+  if (r >= a.n_rays) return;  // r is uniform over the warp
   const BgRay R = bg_ray(a, r);
   int64_t idx = FILL ? offsets[r] : 0;
   const int64_t end = FILL ? offsets[r + 1] : 0;
-  if (FILL && end > capacity) set_device_error(err, VX_ERR_CAPACITY);
+  if (FILL && lane == 0 && end > capacity) set_device_error(err, VX_ERR_CAPACITY);
   int64_t n = 0;
-  float prev[3] = {0.f, 0.f, 0.f};
   float cum = 0.f;
-  for (int k = 0; k < a.n_samples; ++k) {
-    float p[3], q[3];
-    const bool inside = bg_point(a, R, k, p, q);
-    bool keep = !inside;
-    if (a.outbbox_only) {
-      // voxurf_womask_coarse.py:641 keeps only samples outside the bbox
-      // (sample_ray_ori's mask_outbbox, voxurf_womask_fine.py:814)
-      bool out = R.miss;
+  float lastq[3] = {0.f, 0.f, 0.f};  // inverted point of the previous chunk's last sample
+  for (int k0 = 0; k0 < a.n_samples; k0 += 32) {
+    const int k = k0 + lane;
+    const bool valid = k < a.n_samples;
+    float p[3] = {0.f, 0.f, 0.f}, q[3] = {0.f, 0.f, 0.f};
+    bool keep = false;
+    if (valid) {
+      keep = !bg_point(a, R, k, p, q);
+      if (a.outbbox_only) {
+        // voxurf_womask_coarse.py:641 keeps only samples outside the bbox
+        // (sample_ray_ori's mask_outbbox, voxurf_womask_fine.py:814)
+        bool out = R.miss;
 #pragma unroll
-      for (int i = 0; i < 3; ++i) out = out || (a.xyz_min[i] > p[i]) || (p[i] > a.xyz_max[i]);
-      keep = keep && out;
-    }
-    if (k > 0) {
-      // dist of :866 and the cumdist_thres recurrence over it
-      const float dx = fsub(q[0], prev[0]), dy = fsub(q[1], prev[1]), dz = fsub(q[2], prev[2]);
-      const float dd = norm3(dx, dy, dz);
-      cum = fadd(cum, dd);
-      const bool over = cum > a.dist_thres;
-      cum = fmul(cum, (float)(!over));
-      keep = keep && over;
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i) prev[i] = q[i];
-    if (!keep) continue;
-    if (FILL) {
-      if (idx < capacity && idx < end) {
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          outer_pts[3 * idx + i] = q[i];
-          pts_org[3 * idx + i] = p[i];
-        }
-        ray_id[idx] = r;
-        step_id[idx] = k;
+        for (int i = 0; i < 3; ++i) out = out || (a.xyz_min[i] > p[i]) || (p[i] > a.xyz_max[i]);
+        keep = keep && out;
       }
-      ++idx;
+    }
+    // dist of :866 between this sample's and the previous inverted point
+    float prevq[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float up = __shfl_up_sync(FULL, q[i], 1);
+      prevq[i] = lane == 0 ? lastq[i] : up;
+      lastq[i] = __shfl_sync(FULL, q[i], 31);
+    }
+    float dd = 0.f;
+    if (valid && k > 0) dd = norm3(fsub(q[0], prevq[0]), fsub(q[1], prevq[1]), fsub(q[2], prevq[2]));
+    // cumdist_thres over the chunk, in sample order
+    const int cnt = a.n_samples - k0 < 32 ? a.n_samples - k0 : 32;
+    unsigned marks = 0;
+    for (int j = 0; j < cnt; ++j) {
+      const float v = __shfl_sync(FULL, dd, j);
+      if (k0 + j > 0) {
+        cum = fadd(cum, v);
+        const bool over = cum > a.dist_thres;
+        cum = fmul(cum, (float)(!over));
+        marks |= (unsigned)over << j;
+      }
+    }
+    if (k > 0) keep = keep && ((marks >> lane) & 1u);
+    const unsigned ball = __ballot_sync(FULL, keep);
+    if (FILL) {
+      if (keep) {
+        const int64_t o = idx + __popc(ball & ((1u << lane) - 1u));
+        if (o < capacity && o < end) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            outer_pts[3 * o + i] = q[i];
+            pts_org[3 * o + i] = p[i];
+          }
+          ray_id[o] = r;
+          step_id[o] = k;
+        }
+      }
+      idx += __popc(ball);
     } else {
-      ++n;
+      n += __popc(ball);
     }
   }
-  if (!FILL) counts[r] = n;
+  if (!FILL && lane == 0) counts[r] = n;
+}
+
+inline unsigned bg_blocks(int64_t n_rays) {
+  return (unsigned)((n_rays * 32 + BG_THREADS - 1) / BG_THREADS);
 }
 
 bool bg_args_ok(const vx_bg_sample_args* a) {
   if (!a || a->n_rays < 0 || a->n_samples < 0) return false;
+  if (a->n_rays > ((int64_t)INT32_MAX * BG_THREADS) / 32) return false;
   if (a->n_rays > 0 && (!a->rays_o || !a->rays_d)) return false;
   return true;
 }
@@ -206,8 +240,8 @@ int vx_bg_samples_count(const vx_bg_sample_args* args, int64_t* counts, int64_t*
   cudaStream_t st = as_stream(stream);
   if (args->n_rays > 0) {
     if (!counts) return VX_ERR_ARG;
-    bg_samples_kernel<false><<<grid_for(args->n_rays, 128), 128, 0, st>>>(*args, counts, nullptr, 0, nullptr,
-                                                                            nullptr, nullptr, nullptr, nullptr);
+    bg_samples_kernel<false><<<bg_blocks(args->n_rays), BG_THREADS, 0, st>>>(*args, counts, nullptr, 0, nullptr,
+                                                                              nullptr, nullptr, nullptr, nullptr);
     const int s = launch_status();
     if (s) return s;
   }
@@ -219,7 +253,7 @@ int vx_bg_samples_fill(const vx_bg_sample_args* args, const int64_t* offsets, in
   if (!bg_args_ok(args) || capacity < 0) return VX_ERR_ARG;
   if (args->n_rays == 0 || capacity == 0) return VX_OK;
   if (!offsets || !outer_pts || !pts_org || !ray_id || !step_id) return VX_ERR_ARG;
-  bg_samples_kernel<true><<<grid_for(args->n_rays, 128), 128, 0, as_stream(stream)>>>(
+  bg_samples_kernel<true><<<bg_blocks(args->n_rays), BG_THREADS, 0, as_stream(stream)>>>(
       *args, nullptr, offsets, capacity, outer_pts, pts_org, ray_id, step_id, device_error_ptr());
   return launch_status();
 }

@@ -19,16 +19,21 @@
 // packed into that layout by the caller (vx_mlp_tc_pack) and copied to
 // shared memory once per CTA.
 //
-// Thread roles: 8 warps; warps w and w+4 own TMEM lanes / tile rows
-// [32(w%4), +32) in the epilogue and split the 192 columns in halves;
-// thread 0 issues the MMAs and the commit.  Weights, biases and the output
+// Thread roles: 8 epilogue warps (warps w and w+4 own TMEM lanes / tile rows
+// [32(w%4), +32) and split each 64-column step in halves; 16 warps splitting
+// it in four measured the same) and one warp
+// whose lane 0 issues the MMAs and the commits.  The epilogue hands each
+// layer's activations to the next layer in three steps of 64 columns, so
+// the next layer's first MMAs overlap the conversion of the last columns
+// (layers alternate between two accumulators), and the next tile's first
+// layer overlaps the output-layer epilogue.  Weights, biases and the output
 // layer arrive by bulk copies on the async proxy (one mbarrier); the next
 // input tile is prefetched with 16-byte cp.async (zero fill past the last
 // row) as soon as the first layer's MMAs have read the current one.  Tensor
-// memory: 512 columns (accumulator 0-191, output layer 192-207, A operand
-// 256-351; one CTA per SM).  Every wait on an
-// mbarrier is bounded: on expiry the kernel records VX_ERR_TIMEOUT,
-// releases its TMEM and returns.
+// memory: 512 columns (accumulators 0-191 and 192-383, A operand 384-479,
+// output layer 480-495; one CTA per SM).  Every wait on an mbarrier is
+// bounded: on expiry the kernel records VX_ERR_TIMEOUT, waits (bounded) for
+// its issued MMAs, releases its TMEM and returns.
 #include "common.cuh"
 
 namespace vx {
@@ -244,11 +249,79 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(r[i]));
 }
 
-constexpr int TC_THREADS = 256;  // 8 warps: warps w and w+4 share TMEM lanes 32(w%4).., split the columns
+constexpr int TC_EPI_WARPS = 8;                 // epilogue warps (w, w+4, .. share TMEM lanes 32(w%4)..)
+constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);  // + one warp that issues the MMAs
 constexpr int TC_NH = 16;        // output-layer tile: rows 0-2 hi, 3-5 lo, rest zero
-// tensor-memory columns: hidden accumulator, output-layer accumulator, A operand
-constexpr uint32_t TM_ACC = 0, TM_HEAD = 192, TM_A = 256;
+// tensor-memory columns: two hidden accumulators (layers alternate between
+// them), the A operand (192 BF16 = 96 columns), the output-layer accumulator
+constexpr uint32_t TM_ACC0 = 0, TM_ACC1 = 192, TM_A = 384, TM_HEAD = 480;
+constexpr int TC_STEPS = 3;      // epilogue hand-off steps per layer
+constexpr int TC_SW = TC_N / TC_STEPS;          // hidden columns per step (64)
+constexpr int TC_KPS = TC_SW / 16;              // MMA K steps per hand-off step
+constexpr int TC_PARTS = TC_EPI_WARPS / 4;      // warps sharing one lane quarter
+constexpr int TC_CPW = TC_SW / TC_PARTS;        // hidden columns per thread per step
+static_assert(TC_CPW == 16 || TC_CPW == 32, "epilogue split");
 
+// 8 consecutive 32-bit columns of this thread's TMEM lane <- r.
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
+               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+               : "memory");
+}
+
+// N consecutive FP32 columns of this thread's TMEM lane (complete on return).
+template <int N>
+__device__ __forceinline__ void tc_ld_cols(uint32_t taddr, uint32_t (&r)[N]) {
+  if constexpr (N == 32) {
+    tc_ld32_async(taddr, r);
+    tc_wait_ld();
+  } else {
+    tc_ld16(taddr, r);
+  }
+}
+// N consecutive 32-bit columns of this thread's TMEM lane <- r (N = 16 or 8).
+template <int N>
+__device__ __forceinline__ void tc_st_cols(uint32_t taddr, const uint32_t (&r)[N]) {
+  if constexpr (N == 16)
+    tc_st16(taddr, r);
+  else
+    tc_st8(taddr, r);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// MMAs of K steps [KPS s, KPS (s + 1)) (K = SW s .. SW (s + 1) - 1) of a
+// layer whose A operand is in tensor memory.
+__device__ __forceinline__ void tc_layer_ta_step(uint32_t dtmem, uint32_t atmem, uint32_t b_s, int N, int s) {
+  const uint32_t idesc = umma_idesc(TC_M, N);
+#pragma unroll
+  for (int ks = TC_KPS * s; ks < TC_KPS * (s + 1); ++ks) {
+    const uint64_t bd = umma_desc(b_s + (uint32_t)(2 * ks) * (uint32_t)(N * 16), (uint32_t)(N * 16), 128);
+    tc_mma_ta(dtmem, atmem + (uint32_t)(8 * ks), bd, idesc, ks > 0);
+  }
+}
+
+// Pipeline of one CTA (one tile of 128 rows at a time):
+//   MMA warp:      L0 (A = X tile in shared memory) -> ACC0, commit bar_acc;
+//                  then for L1 (-> ACC1), L2 (-> ACC0) and the output layer
+//                  (-> HEAD): for each step s, wait bar_a[s] and issue the K
+//                  steps of the activations that step made; commit.
+//   epilogue warps: for L0, L1, L2: wait bar_acc; in 3 steps, hidden columns
+//                  [64s, 64s + 64) (split between the warps of a lane quarter):
+//                  tcgen05.ld, +bias, ReLU, BF16, tcgen05.st into the A
+//                  operand, arrive on bar_a[s].  After L2 the next X tile is
+//                  complete (bar_x); the output layer's logits follow
+//                  bar_head.
+// So the next layer's first MMAs run while the epilogue still converts the
+// last columns of the current one (they write the other accumulator), and
+// the next tile's first layer runs during the output-layer epilogue.
+// Ordering: an accumulator is rewritten two layers later, after all of its
+// reader's steps; the A operand's columns of step s are rewritten only after
+// the commit of the layer reading them (every epilogue wait on bar_acc
+// follows that commit); each barrier runs at most one phase ahead of its
+// waiter (the producer of phase k+1 itself waits on the consumer of phase k).
 __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int K0 = P.K0;
@@ -259,11 +332,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   __nv_bfloat16* WHs = Xs + (size_t)K0 * TC_M;                      // [24][16][8] output layer
   float* bias_s = reinterpret_cast<float*>(WHs + (size_t)TC_NH * TC_N);  // [3][192]
   uint64_t* bar_w = reinterpret_cast<uint64_t*>(bias_s + 3 * TC_N);
-  uint64_t* bar_mma = bar_w + 1;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_mma + 1);
+  uint64_t* bar_acc = bar_w + 1;
+  uint64_t* bar_head = bar_w + 2;
+  uint64_t* bar_x = bar_w + 3;
+  uint64_t* bar_fin = bar_w + 4;
+  uint64_t* bar_a = bar_w + 5;  // [TC_STEPS]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_a + TC_STEPS);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2;  // TMEM lanes 32*quarter.., columns [96*half, +96)
+  const bool mma_warp = warp == TC_EPI_WARPS;
+  const int quarter = warp & 3, part = (warp >> 2) % TC_PARTS;  // TMEM lanes 32*quarter..
+  const int epi_threads = 32 * TC_EPI_WARPS;
   const int64_t n_tiles = (P.n_rows + TC_M - 1) / TC_M;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -273,7 +352,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   }
   if (tid == 0) {
     mbar_init(bar_w, 1);
-    mbar_init(bar_mma, 1);
+    mbar_init(bar_acc, 1);
+    mbar_init(bar_head, 1);
+    mbar_init(bar_x, TC_EPI_WARPS);
+    mbar_init(bar_fin, 1);
+    for (int s = 0; s < TC_STEPS; ++s) mbar_init(bar_a + s, TC_EPI_WARPS);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -290,7 +373,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
     bulk_g2s(bias_s + TC_N, P.b1, bb, bar_w);
     bulk_g2s(bias_s + 2 * TC_N, P.b2, bb, bar_w);
   }
-  if (blockIdx.x < n_tiles) load_x_tile(P, Xs, (int64_t)blockIdx.x * TC_M, tid, TC_THREADS);
+  if (!mma_warp && blockIdx.x < n_tiles) {
+    load_x_tile(P, Xs, (int64_t)blockIdx.x * TC_M, tid, epi_threads);
+    cp_async_wait_all();
+    fence_async_smem();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(bar_x);
+  }
   bool ok = mbar_wait(bar_w, 0);
   const float bh0 = __ldg(P.bh + 0), bh1 = __ldg(P.bh + 1), bh2 = __ldg(P.bh + 2);
   tc_fence_before();
@@ -299,64 +388,98 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   const uint32_t tmem = *tmem_slot;
   const uint32_t tmem_row = tmem + ((uint32_t)(32 * quarter) << 16);
   const uint32_t x_s = smem_u32(Xs), w_s[3] = {smem_u32(W0s), smem_u32(W1s), smem_u32(W2s)}, wh_s = smem_u32(WHs);
-  uint32_t phase = 0;
 
-  for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-    const int64_t row0 = tile * TC_M;
-    const int64_t row = row0 + 32 * quarter + lane;
-    // this tile's input rows (prefetched during the previous tile)
-    cp_async_wait_all();
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-#pragma unroll 1
-    for (int layer = 0; layer < 4; ++layer) {
-      if (tid == 0) {
-        if (layer == 0)
-          tc_layer(tmem + TM_ACC, x_s, w_s[0], K0, bar_mma);
-        else if (layer < 3)
-          tc_layer_ta(tmem + TM_ACC, tmem + TM_A, w_s[layer], TC_N, TC_N, bar_mma);
-        else
-          tc_layer_ta(tmem + TM_HEAD, tmem + TM_A, wh_s, TC_NH, TC_N, bar_mma);
-      }
-      ok = mbar_wait(bar_mma, phase);
-      phase ^= 1u;
+  if (mma_warp) {
+    uint32_t ph_x = 0, ph_a = 0;
+    for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+      ok = mbar_wait(bar_x, ph_x);
+      ph_x ^= 1u;
       tc_fence_after();
       if (!ok) break;
-      if (layer == 0) {
-        // the input tile is consumed: prefetch the next one
-        const int64_t next = tile + gridDim.x;
-        if (next < n_tiles) load_x_tile(P, Xs, next * TC_M, tid, TC_THREADS);
+      if (lane == 0) tc_layer(tmem + TM_ACC0, x_s, w_s[0], K0, bar_acc);
+      __syncwarp();
+#pragma unroll 1
+      for (int layer = 1; layer < 4 && ok; ++layer) {
+        const uint32_t d = layer == 1 ? TM_ACC1 : layer == 2 ? TM_ACC0 : TM_HEAD;
+        const uint32_t b = layer == 1 ? w_s[1] : layer == 2 ? w_s[2] : wh_s;
+        const int N = layer < 3 ? TC_N : TC_NH;
+#pragma unroll 1
+        for (int s = 0; s < TC_STEPS; ++s) {
+          ok = mbar_wait(bar_a + s, ph_a);
+          tc_fence_after();
+          if (!ok) break;
+          if (lane == 0) tc_layer_ta_step(tmem + d, tmem + TM_A, b, N, s);
+          __syncwarp();
+        }
+        ph_a ^= 1u;
+        if (ok && lane == 0) tc_commit(layer < 3 ? bar_acc : bar_head);
+        __syncwarp();
       }
-      if (layer < 3) {
-        // +bias, ReLU, BF16 -> the A operand in tensor memory: this thread's
-        // row, columns [96*half, 96*half + 96) -> TMEM columns [48*half, +48)
-        const float* b = bias_s + layer * TC_N;
-        uint32_t v[3][32];
-        tc_ld96(tmem_row + TM_ACC + 96 * half, v);
+    }
+    // nothing of this CTA's may still be in flight when the tensor memory is
+    // released
+    if (lane == 0) {
+      tc_commit(bar_fin);
+      if (!mbar_wait(bar_fin, 0)) ok = false;
+    }
+    __syncwarp();
+  } else {
+    uint32_t ph_acc = 0, ph_head = 0;
+    for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+      const int64_t row = tile * TC_M + 32 * quarter + lane;
+#pragma unroll 1
+      for (int layer = 0; layer < 3; ++layer) {
+        ok = mbar_wait(bar_acc, ph_acc);
+        ph_acc ^= 1u;
+        tc_fence_after();
+        if (!ok) break;
+        if (layer == 0) {
+          // the input tile is consumed: prefetch the next one
+          const int64_t next = tile + gridDim.x;
+          if (next < n_tiles) load_x_tile(P, Xs, next * TC_M, tid, epi_threads);
+        }
+        const uint32_t acc = layer == 1 ? TM_ACC1 : TM_ACC0;
+        const float* bl = bias_s + layer * TC_N;
+#pragma unroll 1
+        for (int s = 0; s < TC_STEPS; ++s) {
+          // +bias, ReLU, BF16 -> the A operand: this thread's row, hidden
+          // columns [SW s + CPW part, +CPW) -> TMEM columns (the same) / 2
+          const int col0 = TC_SW * s + TC_CPW * part;
+          uint32_t v[TC_CPW];
+          tc_ld_cols<TC_CPW>(tmem_row + acc + (uint32_t)col0, v);
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          const int col0 = 96 * half + 32 * j;
-          uint32_t pk[16];
+          for (int i = 0; i < TC_CPW; ++i) asm volatile("" : "+r"(v[i]));
+          uint32_t pk[TC_CPW / 2];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const float4 bq = *reinterpret_cast<const float4*>(b + col0 + 4 * q);
-            const float h0 = fmaxf(__uint_as_float(v[j][4 * q + 0]) + bq.x, 0.f);
-            const float h1 = fmaxf(__uint_as_float(v[j][4 * q + 1]) + bq.y, 0.f);
-            const float h2 = fmaxf(__uint_as_float(v[j][4 * q + 2]) + bq.z, 0.f);
-            const float h3 = fmaxf(__uint_as_float(v[j][4 * q + 3]) + bq.w, 0.f);
+          for (int q = 0; q < TC_CPW / 4; ++q) {
+            const float4 bq = *reinterpret_cast<const float4*>(bl + col0 + 4 * q);
+            const float h0 = fmaxf(__uint_as_float(v[4 * q + 0]) + bq.x, 0.f);
+            const float h1 = fmaxf(__uint_as_float(v[4 * q + 1]) + bq.y, 0.f);
+            const float h2 = fmaxf(__uint_as_float(v[4 * q + 2]) + bq.z, 0.f);
+            const float h3 = fmaxf(__uint_as_float(v[4 * q + 3]) + bq.w, 0.f);
             pk[2 * q] = pack_bf16(h0, h1);
             pk[2 * q + 1] = pack_bf16(h2, h3);
           }
-          tc_st16(tmem_row + TM_A + (uint32_t)(48 * half + 16 * j), pk);
+          tc_st_cols<TC_CPW / 2>(tmem_row + TM_A + (uint32_t)(col0 / 2), pk);
+          tc_wait_st();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(bar_a + s);
         }
-        tc_wait_st();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-      } else if (half == 0) {
+        if (layer == 2) {
+          // the next input tile (if any) is in shared memory
+          cp_async_wait_all();
+          fence_async_smem();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(bar_x);
+        }
+      }
+      if (!ok) break;
+      if (part == 0) {
         // output layer: hi + lo parts of each logit, + bias (+ residual)
+        ok = mbar_wait(bar_head, ph_head);
+        tc_fence_after();
+        if (!ok) break;
         uint32_t hv[16];
         tc_ld16(tmem_row + TM_HEAD, hv);
         if (row < P.n_rows) {
@@ -378,11 +501,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
             cp[2] = __float2bfloat16_rn(a2);
           }
         }
+        tc_fence_before();
       }
+      ph_head ^= 1u;
     }
+    cp_async_wait_all();
   }
-  cp_async_wait_all();
-  if (!ok && tid == 0) set_device_error(P.err, VX_ERR_TIMEOUT);
+  if (!ok) set_device_error(P.err, VX_ERR_TIMEOUT);
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -402,7 +527,7 @@ __global__ void mlp_tc_pack_kernel(const float* __restrict__ W, int N, int K, in
 
 static size_t mlp_tc_smem_bytes(int K0) {
   return (size_t)K0 * TC_N * 2 + 2 * (size_t)TC_N * TC_N * 2 + (size_t)K0 * TC_M * 2 + (size_t)TC_NH * TC_N * 2 +
-         3 * TC_N * 4 + 24;
+         3 * TC_N * 4 + (5 + TC_STEPS) * 8 + 8;
 }
 
 }  // namespace vx
