@@ -15,6 +15,15 @@ mask's block occupancy starts each ray's march at its first sample that can
 lie in the mask.  The composite writes straight into each request's range
 of an output arena.
 
+A tick has a front half (rays, march, row scan; on the front stream) and a
+back half (rows, features, MLPs, compositing; on the back stream), and the
+two halves of consecutive ticks overlap: the host launches the front half
+of tick t+1 and the back half of tick t before it waits for tick t+1's row
+counts (the tick's one host synchronisation), so the march of one tick
+runs beside the MLPs of the previous one.  Two workspace slots alternate
+between ticks; a slot is reused once its previous tick's compositing is
+done (an event).
+
 Admission is by device memory: a request is admitted once the arena (sized
 from free HBM when the server starts) has room for its pixels and fewer
 than ``max_active`` requests are in flight; until then it waits in FIFO
@@ -221,6 +230,41 @@ class OutputArena:
         return self.capacity - sum(ln for _, ln in self.free)
 
 
+class _TickSlot:
+    """Device workspace of one tick in flight (rays, per-ray sample records,
+    row offsets) and its pinned host staging."""
+
+    def __init__(self, N: int, max_steps: int, scan_bytes: int, max_chunks: int, dev):
+        self.rays = torch.empty((3, N, 3), dtype=torch.float32, device=dev)
+        self.ray_scene = torch.empty(N, dtype=torch.int32, device=dev)
+        self.ray_out = torch.empty(N, dtype=torch.int64, device=dev)
+        self.n2 = torch.empty(N, dtype=torch.int32, device=dev)
+        self.alast = torch.empty(N, dtype=torch.float32, device=dev)
+        self.s2_off = torch.empty(N + 1, dtype=torch.int64, device=dev)
+        self.scan_tmp = scratch(scan_bytes, dev)
+        self.rec = torch.empty(N * max_steps * 8, dtype=torch.uint8, device=dev)
+        self.chunk_host = torch.empty(max_chunks * ctypes.sizeof(_abi.ViewChunk), dtype=torch.uint8,
+                                      pin_memory=True)
+        self.chunk_dev = torch.empty_like(self.chunk_host, device=dev)
+        self.chunk_ready = torch.cuda.Event()
+        self.bounds_host = torch.empty(16, dtype=torch.int64, pin_memory=True)
+        self.ev_back = None   # recorded after the back half of the slot's last tick
+
+
+class _Tick:
+    """One tick between its front and back halves."""
+
+    def __init__(self, slot: int):
+        self.slot = slot
+        self.N = 0
+        self.S2 = 0
+        self.scene_ids: list[int] = []
+        self.bounds: list[int] = []
+        self.row_bounds: list[int] = []
+        self.finished: list = []
+        self.ev_front = None
+
+
 class RenderServer:
     def __init__(self, scenes: list[ResidentScene], tick_rays: int = 1 << 19, arena_pixels: int | None = None,
                  hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None, mlp: str = "tc"):
@@ -253,21 +297,17 @@ class RenderServer:
         self.mlp = mlp
         dev = self.device
         N = self.tick_rays
-        # per-tick workspace (fixed size)
-        self.rays = torch.empty((3, N, 3), dtype=torch.float32, device=dev)
-        self.ray_scene = torch.empty(N, dtype=torch.int32, device=dev)
-        self.ray_out = torch.empty(N, dtype=torch.int64, device=dev)
-        self.n2 = torch.empty(N, dtype=torch.int32, device=dev)
-        self.alast = torch.empty(N, dtype=torch.float32, device=dev)
-        self.s2_off = torch.empty(N + 1, dtype=torch.int64, device=dev)
+        # per-tick workspace (fixed size), two slots: while the back half of
+        # tick t (features, MLPs, compositing) runs on the back stream, the
+        # front half of tick t+1 (rays, march, scan) runs on the front stream
         lib = _abi._native.load()
         self.scan_bytes = int(lib.vx_scan_scratch_bytes(N))
-        self.scan_tmp = scratch(self.scan_bytes, dev)
-        self.rec = torch.empty(N * self.max_steps * 8, dtype=torch.uint8, device=dev)
         self.max_chunks = 4 * max_active + 8
-        self.chunk_host = torch.empty(self.max_chunks * ctypes.sizeof(_abi.ViewChunk), dtype=torch.uint8,
-                                      pin_memory=True)
-        self.chunk_dev = torch.empty_like(self.chunk_host, device=dev)
+        self.slots = [_TickSlot(N, self.max_steps, self.scan_bytes, self.max_chunks, dev) for _ in range(2)]
+        torch.cuda.current_stream(dev).synchronize()   # scene uploads are complete
+        self.front_stream = torch.cuda.Stream(dev)
+        self.back_stream = torch.cuda.Stream(dev)
+        self.pending = None   # the tick whose back half is not launched yet
         self.rows_cap = 0
         self._grow_rows(N * 4)
         # output arena (device) and its pinned host mirror
@@ -333,15 +373,16 @@ class RenderServer:
         return out
 
     def idle(self) -> bool:
-        return not (self.queue or self.active or self.finishing)
+        return not (self.queue or self.active or self.finishing or self.pending)
 
     def has_work(self) -> bool:
-        return bool(self.queue or self.active)
+        return bool(self.queue or self.active or self.pending)
 
     # ---- one tick -----------------------------------------------------------
     def tick(self) -> int:
-        """Admits what fits, launches one tick of rays, harvests finished
-        requests.  Returns the number of rays launched."""
+        """Admits what fits, launches the front half of one tick of rays and
+        the back half of the previous tick, harvests finished requests.
+        Returns the number of rays launched."""
         self.poll()
         self._admit()
         budget = self.tick_rays
@@ -354,22 +395,20 @@ class RenderServer:
                 batch.append((r, r.next_pix, n))
                 r.next_pix += n
                 budget -= n
-        if not batch:
+        new = self._front(batch) if batch else None
+        if new is not None:
+            new.finished = [r for r in self.active if r.next_pix == r.n_pix]
+            self.active = [r for r in self.active if r.next_pix < r.n_pix]
+        if self.pending is not None:
+            self._back(self.pending)
+        self.pending = None
+        if new is None:
             return 0
-        n_rays = self._launch(batch)
-        finished = [r for r in self.active if r.next_pix == r.n_pix]
-        self.active = [r for r in self.active if r.next_pix < r.n_pix]
-        st = torch.cuda.current_stream(self.device)
-        for r in finished:
-            a, b = r.off, r.off + r.n_pix
-            self.host_rgb[a:b].copy_(self.out_rgb[a:b], non_blocking=True)
-            self.host_depth[a:b].copy_(self.out_depth[a:b], non_blocking=True)
-            r.event = torch.cuda.Event()
-            r.event.record(st)
-            self.finishing.append(r)
+        self._row_bounds(new)   # the tick's one host sync (front stream only)
+        self.pending = new
         self.ticks += 1
-        self.rays_launched += n_rays
-        return n_rays
+        self.rays_launched += new.N
+        return new.N
 
     def run_until_idle(self, sleep: float = 0.0) -> None:
         while not self.idle():
@@ -396,6 +435,8 @@ class RenderServer:
         if n <= self.rows_cap:
             return
         dev = self.device
+        if self.rows_cap:
+            self.back_stream.synchronize()   # the old rows are no longer read
         self.rows_cap = n
         self.ray2 = torch.empty(n, dtype=torch.int32, device=dev)
         self.X1 = torch.empty((n, self.ld1), dtype=self.dtype, device=dev)
@@ -403,9 +444,15 @@ class RenderServer:
         self.logit = torch.empty((n, 3), dtype=torch.float32, device=dev)
         self.klogit = torch.empty((n, 3), dtype=torch.float32, device=dev)
 
-    def _launch(self, batch) -> int:
+    def _front(self, batch) -> "_Tick":
+        """Rays, march and the row scan of one tick on the front stream."""
         batch = sorted(batch, key=lambda t: t[0].scene)   # rows grouped by scene
-        st = stream_ptr(self.device)
+        t = _Tick(self.ticks % 2)
+        sl = self.slots[t.slot]
+        fs = self.front_stream
+        if sl.ev_back is not None:
+            fs.wait_event(sl.ev_back)   # the slot's previous tick is composited
+        st = fs.cuda_stream
         chunks = (_abi.ViewChunk * len(batch))()
         ray0 = 0
         bounds, scene_ids = [0], []
@@ -424,38 +471,70 @@ class RenderServer:
             else:
                 scene_ids.append(r.scene)
                 bounds.append(ray0)
+        t.N, t.scene_ids, t.bounds = ray0, scene_ids, bounds
         N = ray0
         nbytes = ctypes.sizeof(chunks)
-        ctypes.memmove(self.chunk_host.data_ptr(), ctypes.addressof(chunks), nbytes)
-        self.chunk_dev[:nbytes].copy_(self.chunk_host[:nbytes], non_blocking=True)
-        o, d, v = self.rays[0], self.rays[1], self.rays[2]
-        tab, ns = self.table, len(self.scenes)
-        _abi.call("vx_serve_rays", ptr(self.chunk_dev), len(batch), N, ptr(o), ptr(d), ptr(v), ptr(self.ray_scene),
-                  ptr(self.ray_out), st)
-        _abi.call("vx_serve_march", tab, ns, ptr(o), ptr(d), ptr(v), ptr(self.ray_scene), N, self.max_steps,
-                  ptr(self.rec), ptr(self.n2), ptr(self.alast), st)
-        _abi.call("vx_exclusive_scan_i32", ptr(self.n2), N, ptr(self.s2_off), ptr(self.scan_tmp), self.scan_bytes, st)
-        idx = torch.tensor(bounds, dtype=torch.int64).to(self.device, non_blocking=True)
-        row_bounds = self.s2_off.index_select(0, idx).cpu().tolist()   # the tick's one host sync
-        S2 = row_bounds[-1]
-        self.rows_shaded += S2
-        if S2 > self.rows_cap:
-            self._grow_rows(S2)
-        if S2 > 0:
-            _abi.call("vx_serve_rows", ptr(self.s2_off), N, ptr(self.ray2), st)
-            _abi.call("vx_serve_features", tab, ns, ctypes.byref(self.cfg), ptr(o), ptr(d), ptr(v),
-                      ptr(self.ray_scene), self.max_steps, ptr(self.rec), ptr(self.s2_off), ptr(self.ray2), S2,
-                      self.ld1, self.ld2, ptr(self.X1), ptr(self.X2), int(self.bf16), st)
-            with torch.no_grad():
-                for g, sc in enumerate(scene_ids):
-                    a, b = row_bounds[g], row_bounds[g + 1]
-                    if b > a:
-                        self._shade(self.scenes[sc], a, b, st)
-        use_k = self.scenes[0].use_rgb_k
-        _abi.call("vx_serve_composite", tab, ns, ptr(self.ray_scene), N, self.max_steps, ptr(self.rec),
-                  ptr(self.s2_off), ptr(self.logit), ptr(self.klogit) if use_k else None, ptr(self.alast),
-                  ptr(self.ray_out), ptr(self.out_rgb), ptr(self.out_depth), st)
-        return N
+        with torch.cuda.stream(fs):
+            sl.chunk_ready.synchronize()   # the pinned table's previous upload is done
+            ctypes.memmove(sl.chunk_host.data_ptr(), ctypes.addressof(chunks), nbytes)
+            sl.chunk_dev[:nbytes].copy_(sl.chunk_host[:nbytes], non_blocking=True)
+            sl.chunk_ready.record(fs)
+            o, d, v = sl.rays[0], sl.rays[1], sl.rays[2]
+            tab, ns = self.table, len(self.scenes)
+            _abi.call("vx_serve_rays", ptr(sl.chunk_dev), len(batch), N, ptr(o), ptr(d), ptr(v),
+                      ptr(sl.ray_scene), ptr(sl.ray_out), st)
+            _abi.call("vx_serve_march", tab, ns, ptr(o), ptr(d), ptr(v), ptr(sl.ray_scene), N, self.max_steps,
+                      ptr(sl.rec), ptr(sl.n2), ptr(sl.alast), st)
+            _abi.call("vx_exclusive_scan_i32", ptr(sl.n2), N, ptr(sl.s2_off), ptr(sl.scan_tmp), self.scan_bytes,
+                      st)
+            idx = torch.tensor(bounds, dtype=torch.int64).to(self.device, non_blocking=True)
+            sl.bounds_host[:len(bounds)].copy_(sl.s2_off.index_select(0, idx), non_blocking=True)
+            t.ev_front = torch.cuda.Event()
+            t.ev_front.record(fs)
+        return t
+
+    def _row_bounds(self, t: "_Tick") -> None:
+        t.ev_front.synchronize()
+        t.row_bounds = self.slots[t.slot].bounds_host[:len(t.bounds)].tolist()
+        t.S2 = t.row_bounds[-1]
+        self.rows_shaded += t.S2
+
+    def _back(self, t: "_Tick") -> None:
+        """Rows, features, MLPs and compositing of a tick on the back stream,
+        then the copies of the requests it finished."""
+        sl = self.slots[t.slot]
+        bs = self.back_stream
+        st = bs.cuda_stream
+        with torch.cuda.stream(bs):
+            bs.wait_event(t.ev_front)
+            S2, N = t.S2, t.N
+            o, d, v = sl.rays[0], sl.rays[1], sl.rays[2]
+            tab, ns = self.table, len(self.scenes)
+            if S2 > self.rows_cap:
+                self._grow_rows(S2)
+            if S2 > 0:
+                _abi.call("vx_serve_rows", ptr(sl.s2_off), N, ptr(self.ray2), st)
+                _abi.call("vx_serve_features", tab, ns, ctypes.byref(self.cfg), ptr(o), ptr(d), ptr(v),
+                          ptr(sl.ray_scene), self.max_steps, ptr(sl.rec), ptr(sl.s2_off), ptr(self.ray2), S2,
+                          self.ld1, self.ld2, ptr(self.X1), ptr(self.X2), int(self.bf16), st)
+                with torch.no_grad():
+                    for g, sc in enumerate(t.scene_ids):
+                        a, b = t.row_bounds[g], t.row_bounds[g + 1]
+                        if b > a:
+                            self._shade(self.scenes[sc], a, b, st)
+            use_k = self.scenes[0].use_rgb_k
+            _abi.call("vx_serve_composite", tab, ns, ptr(sl.ray_scene), N, self.max_steps, ptr(sl.rec),
+                      ptr(sl.s2_off), ptr(self.logit), ptr(self.klogit) if use_k else None, ptr(sl.alast),
+                      ptr(sl.ray_out), ptr(self.out_rgb), ptr(self.out_depth), st)
+            sl.ev_back = torch.cuda.Event()
+            sl.ev_back.record(bs)
+            for r in t.finished:
+                a, b = r.off, r.off + r.n_pix
+                self.host_rgb[a:b].copy_(self.out_rgb[a:b], non_blocking=True)
+                self.host_depth[a:b].copy_(self.out_depth[a:b], non_blocking=True)
+                r.event = torch.cuda.Event()
+                r.event.record(bs)
+                self.finishing.append(r)
 
     def _hidden(self, layers, x):
         h = x
