@@ -687,6 +687,17 @@ int vx_serve_composite(const vx_scene_desc* scenes_host, int32_t n_scenes, const
                        const float* klogit, const float* alphainv_last, const int64_t* ray_out, float* out_rgb,
                        float* out_depth, void* stream);
 
+/* FP32 GEMM of the colour-MLP backward (the weight and input gradients that
+ * autograd forms for voxurf_fine.py:132-187's nn.Linear layers): cuBLAS
+ * SGEMM, column-major, C = alpha op(A) op(B) + beta C, on `stream`, with the
+ * caller's workspace (may be NULL: cuBLAS's own).  emulate = 1 selects
+ * cuBLAS's BF16x9 FP32 emulation on the tensor cores.  Uses one cuBLAS
+ * handle per device, created on first use (cublasCreate allocates its own
+ * small state: the one device allocation this library makes). */
+int vx_gemm_f32(int transa, int transb, int64_t m, int64_t n, int64_t k, float alpha, const float* A, int64_t lda,
+                const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int emulate, void* workspace,
+                size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------------------
  * Background branch of the scenes without an object mask
  * (lib/voxurf_womask_fine.py, lib/voxurf_womask_coarse.py).
