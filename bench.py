@@ -70,9 +70,10 @@ def parse():
     p.add_argument("--no-mesh", action="store_true", help="skip the 512^3 mesh-extraction field measurement")
     p.add_argument("--no-background", action="store_true",
                    help="skip the background-sample generator measurement (scenes without an object mask)")
-    p.add_argument("--micro", choices=["smooth", "mlp_tc"], default=None,
+    p.add_argument("--micro", choices=["smooth", "mlp_tc", "background"], default=None,
                    help="single-kernel timing instead of the step (profiling): the Gaussian smoothing sweep "
-                        "on a --grid^3 grid, or the fused tensor-core MLP against the GEMM path")
+                        "on a --grid^3 grid, the fused tensor-core MLP against the GEMM path, or the "
+                        "background-sample generator and cumdist_thres")
     p.add_argument("--render-requests", type=int, default=120)
     p.add_argument("--render-only", action="store_true", help="only the render-server measurement (profiling)")
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
@@ -448,6 +449,15 @@ def run_micro(args, dev):
 
     W, S = max(args.warmup, 3), max(args.steps, 10)
     out = {"kind": args.micro}
+    if args.micro == "background":
+        from voxurf_gb300 import ub360_utils_cuda
+
+        out["generator"] = run_background(args, dev)
+        d = torch.rand((N_RAYS, 890), device=dev, generator=torch.Generator(dev).manual_seed(1)) * 0.02
+        ms = _event_ms(lambda: ub360_utils_cuda.cumdist_thres(d, 0.0208), W, S)
+        out["cumdist_thres"] = {"shape": [N_RAYS, 890], "ms": ms, "gbs": d.numel() * 5 / (ms / 1000.0) / 1e9}
+        print(json.dumps({"micro": out}))
+        return
     if args.micro == "smooth":
         from voxurf_gb300.voxurf_fine import gaussian_taps, smooth_grid, smooth_grid_adjoint
 
