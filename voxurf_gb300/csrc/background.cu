@@ -29,7 +29,8 @@ namespace {
 // cumdist_thres.  A CTA of 32 threads owns 32 rays; the rows are moved
 // through shared memory in [32 rays x 32 samples] tiles so that the loads
 // and stores are coalesced (a thread walking its own row would touch a new
-// 128-byte line per sample), and each thread scans its ray's row of the tile.
+// 128-byte line per sample), and each thread scans its ray's row of the
+// tile while the next tile is in flight.
 constexpr int CD_RAYS = 32;
 constexpr int CD_COLS = 32;
 
@@ -41,13 +42,25 @@ __global__ void __launch_bounds__(CD_RAYS) cumdist_thres_kernel(const float* __r
   const int lane = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.x * CD_RAYS;
   float cum = 0.f;
+  // the next tile's 32 values of this lane's column are loaded into
+  // registers while the current tile is scanned
+  float nxt[CD_RAYS];
+#pragma unroll
+  for (int rr = 0; rr < CD_RAYS; ++rr) {
+    const int64_t r = r0 + rr;
+    nxt[rr] = (r < n_rays && lane < n_pts) ? dist[r * n_pts + lane] : 0.f;
+  }
   for (int64_t c0 = 0; c0 < n_pts; c0 += CD_COLS) {
     const int64_t c = c0 + lane;
+#pragma unroll
+    for (int rr = 0; rr < CD_RAYS; ++rr) tile[rr][lane] = nxt[rr];
+    __syncwarp();
+    const int64_t cn = c + CD_COLS;
+#pragma unroll
     for (int rr = 0; rr < CD_RAYS; ++rr) {
       const int64_t r = r0 + rr;
-      tile[rr][lane] = (r < n_rays && c < n_pts) ? dist[r * n_pts + c] : 0.f;
+      nxt[rr] = (r < n_rays && cn < n_pts) ? dist[r * n_pts + cn] : 0.f;
     }
-    __syncwarp();
     const int cols = n_pts - c0 < CD_COLS ? (int)(n_pts - c0) : CD_COLS;
     for (int j = 0; j < cols; ++j) {
       cum = fadd(cum, tile[lane][j]);
