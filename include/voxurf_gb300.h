@@ -698,15 +698,6 @@ int vx_gemm_f32(int transa, int transb, int64_t m, int64_t n, int64_t k, float a
                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int emulate, void* workspace,
                 size_t workspace_bytes, void* stream);
 
-/* Weight gradient of one colour-MLP layer in FP32, dW [n_out, k_in]
- * (row-major) = dz^T h with dz [S, n_out] and h [S, k_in] row-major: the
- * S rows are cut into chunks of rows_per_chunk, one strided-batched SGEMM
- * (plus one for the remainder) writes a partial product per chunk into
- * `partials` (ceil(S / rows_per_chunk) x n_out x k_in floats) and a kernel
- * sums them in chunk order; S <= rows_per_chunk is one SGEMM into dW. */
-int vx_gemm_f32_wgrad(const float* dz, const float* h, int64_t S, int64_t n_out, int64_t k_in, int64_t rows_per_chunk,
-                      float* partials, float* dW, int emulate, void* stream);
-
 /* ------------------------------------------------------------------------
  * Background branch of the scenes without an object mask
  * (lib/voxurf_womask_fine.py, lib/voxurf_womask_coarse.py).

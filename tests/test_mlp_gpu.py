@@ -83,24 +83,3 @@ def test_gemm_f32_matches_fp64(cuda, emulate, ta, tb, m, n, k):
     else:
         err = float((C.double() - want).abs().max() / want.abs().max())
         assert err < 1e-6, err
-
-
-@pytest.mark.parametrize("S", [0, 100, 4096, 10001])
-def test_gemm_f32_wgrad_matches_fp64(cuda, S):
-    """Chunked weight gradient dz^T h (partials per 4096 rows, summed in
-    order) against an FP64 product."""
-    from voxurf_gb300._torch import call, ptr, stream_ptr
-
-    g = torch.Generator(device=cuda).manual_seed(S + 3)
-    dz = torch.randn((S, 192), device=cuda, generator=g)
-    h = torch.relu(torch.randn((S, 70), device=cuda, generator=g))
-    parts = -(-S // 4096)
-    partials = torch.empty((parts, 192, 70), device=cuda) if parts > 1 else None
-    dW = torch.full((192, 70), float("nan"), device=cuda)
-    call("vx_gemm_f32_wgrad", ptr(dz), ptr(h), S, 192, 70, 4096, ptr(partials), ptr(dW), 0, stream_ptr())
-    torch.cuda.synchronize()
-    want = dz.double().t() @ h.double()
-    if S == 0:
-        assert torch.equal(dW, torch.zeros_like(dW))
-    else:
-        assert float((dW.double() - want).abs().max() / want.abs().max()) < 1e-6

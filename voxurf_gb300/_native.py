@@ -72,7 +72,6 @@ _SIGNATURES = {
     "vx_cumdist_thres": [c_ptr, c_i64, c_i64, c_f32, c_ptr, c_ptr],
     "vx_gemm_f32": [c_int, c_int, c_i64, c_i64, c_i64, c_f32, c_ptr, c_i64, c_ptr, c_i64, c_f32, c_ptr, c_i64,
                     c_int, c_ptr, c_size, c_ptr],
-    "vx_gemm_f32_wgrad": [c_ptr, c_ptr, c_i64, c_i64, c_i64, c_i64, c_ptr, c_ptr, c_int, c_ptr],
 }
 
 _RESTYPES = {

@@ -27,18 +27,7 @@ int handle_for_current_device(cublasHandle_t* out) {
   return VX_OK;
 }
 
-// out[i] = sum over b of part[b * n + i], b in order.
-__global__ void sum_partials_kernel(const float* __restrict__ part, int64_t n, int nb, float* __restrict__ out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float acc = 0.f;
-  for (int b = 0; b < nb; ++b) acc += part[(int64_t)b * n + i];
-  out[i] = acc;
-}
-
 }  // namespace
-
-using namespace vx;
 
 extern "C" {
 
@@ -66,39 +55,6 @@ int vx_gemm_f32(int transa, int transb, int64_t m, int64_t n, int64_t k, float a
                   &alpha, A, (int)lda, B, (int)ldb, &beta, C, (int)ldc);
   if (st != CUBLAS_STATUS_SUCCESS) return st == CUBLAS_STATUS_NOT_SUPPORTED ? VX_ERR_UNSUPPORTED : VX_ERR_CUDA;
   return VX_OK;
-}
-
-int vx_gemm_f32_wgrad(const float* dz, const float* h, int64_t S, int64_t n_out, int64_t k_in, int64_t rows_per_chunk,
-                      float* partials, float* dW, int emulate, void* stream) {
-  if (S < 0 || n_out <= 0 || k_in <= 0 || rows_per_chunk <= 0 || !dW) return VX_ERR_ARG;
-  if (S <= rows_per_chunk)
-    return vx_gemm_f32(0, 1, k_in, n_out, S, 1.f, h, k_in, dz, n_out, 0.f, dW, k_in, emulate, nullptr, 0, stream);
-  if (!dz || !h || !partials) return VX_ERR_ARG;
-  const int64_t nb = S / rows_per_chunk, rem = S - nb * rows_per_chunk, n = n_out * k_in;
-  if (nb + 1 > INT32_MAX || rows_per_chunk > INT32_MAX || n_out > INT32_MAX || k_in > INT32_MAX) return VX_ERR_ARG;
-  cublasHandle_t hd = nullptr;
-  int s = handle_for_current_device(&hd);
-  if (s) return s;
-  {
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (cublasSetStream(hd, reinterpret_cast<cudaStream_t>(stream)) != CUBLAS_STATUS_SUCCESS) return VX_ERR_CUDA;
-    if (cublasSetMathMode(hd, emulate ? CUBLAS_FP32_EMULATED_BF16X9_MATH : CUBLAS_DEFAULT_MATH) !=
-        CUBLAS_STATUS_SUCCESS)
-      return VX_ERR_UNSUPPORTED;
-    const float one = 1.f, zero = 0.f;
-    // chunk b: partials[b] (k_in x n_out, column-major) = h_b^T dz_b
-    cublasStatus_t st = cublasSgemmStridedBatched(
-        hd, CUBLAS_OP_N, CUBLAS_OP_T, (int)k_in, (int)n_out, (int)rows_per_chunk, &one, h, (int)k_in,
-        rows_per_chunk * k_in, dz, (int)n_out, rows_per_chunk * n_out, &zero, partials, (int)k_in, n, (int)nb);
-    if (st == CUBLAS_STATUS_SUCCESS && rem > 0)
-      st = cublasSgemm(hd, CUBLAS_OP_N, CUBLAS_OP_T, (int)k_in, (int)n_out, (int)rem, &one,
-                       h + nb * rows_per_chunk * k_in, (int)k_in, dz + nb * rows_per_chunk * n_out, (int)n_out,
-                       &zero, partials + nb * n, (int)k_in);
-    if (st != CUBLAS_STATUS_SUCCESS) return st == CUBLAS_STATUS_NOT_SUPPORTED ? VX_ERR_UNSUPPORTED : VX_ERR_CUDA;
-  }
-  const int parts = (int)(nb + (rem > 0 ? 1 : 0));
-  sum_partials_kernel<<<grid_for(n), VX_THREADS, 0, as_stream(stream)>>>(partials, n, parts, dW);
-  return launch_status();
 }
 
 }  // extern "C"

@@ -24,7 +24,6 @@ from ._torch import call, ptr, stream_ptr
 # FP32 emulation on the tensor cores (another 5%; meets the FP32 parity
 # bars), "torch" = torch.matmul.
 FP32_GEMM = os.environ.get("VX_FP32_GEMM", "native")
-WGRAD_ROWS = 4096   # rows per partial product of a weight gradient
 
 
 def _gemm_f32(dz: torch.Tensor, other: torch.Tensor, wgrad: bool) -> torch.Tensor:
@@ -37,12 +36,9 @@ def _gemm_f32(dz: torch.Tensor, other: torch.Tensor, wgrad: bool) -> torch.Tenso
         h = other
         k_in = h.shape[1]
         out = torch.empty((n_out, k_in), dtype=torch.float32, device=dev)
-        # chunks of WGRAD_ROWS rows, one partial product each (a batched
-        # GEMM keeps every SM busy on the 192 x 192 output), summed in order
-        parts = -(-S // WGRAD_ROWS)
-        partials = torch.empty((parts, n_out, k_in), dtype=torch.float32, device=dev) if parts > 1 else None
-        call("vx_gemm_f32_wgrad", ptr(dz), ptr(h), S, n_out, k_in, WGRAD_ROWS, ptr(partials), ptr(out), emulate,
-             stream_ptr(dev))
+        # column-major: out^T (k_in x n_out) = h^T (k_in x S) . dz (S x n_out)
+        call("vx_gemm_f32", 0, 1, k_in, n_out, S, 1.0, ptr(h), k_in, ptr(dz), n_out, 0.0, ptr(out), k_in, emulate,
+             None, 0, stream_ptr(dev))
     else:
         W = other
         k_in = W.shape[1]
