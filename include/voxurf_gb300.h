@@ -698,6 +698,22 @@ int vx_gemm_f32(int transa, int transb, int64_t m, int64_t n, int64_t k, float a
                 const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int emulate, void* workspace,
                 size_t workspace_bytes, void* stream);
 
+/* Per-step FP32 -> BF16 casts of the colour-MLP weights and biases of the
+ * mixed-precision step (the reference keeps FP32 parameters; the BF16
+ * copies feed the GEMMs), all in one launch: job j copies rows x cols
+ * elements from src (row stride src_ld floats) to dst (row stride dst_ld
+ * BF16 elements). */
+#define VX_CAST_MAX_JOBS 16
+typedef struct {
+  const float* src;
+  void* dst;
+  int32_t rows;
+  int32_t cols;
+  int32_t src_ld;
+  int32_t dst_ld;
+} vx_cast_job;
+int vx_cast_rows_bf16(const vx_cast_job* jobs_host, int32_t n_jobs, void* stream);
+
 /* ------------------------------------------------------------------------
  * Background branch of the scenes without an object mask
  * (lib/voxurf_womask_fine.py, lib/voxurf_womask_coarse.py).

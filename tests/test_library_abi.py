@@ -68,7 +68,7 @@ def test_struct_sizes_match_c_layout():
                "vx_coarse_composite_bwd_args": _abi.CoarseCompositeBwdArgs,
                "vx_coarse_backward_args": _abi.CoarseBackwardArgs, "vx_scene_desc": _abi.SceneDesc,
                "vx_view_chunk": _abi.ViewChunk, "vx_mlp_tc_args": _abi.MlpTcArgs,
-               "vx_bg_sample_args": _abi.BgSampleArgs}
+               "vx_bg_sample_args": _abi.BgSampleArgs, "vx_cast_job": _abi.CastJob}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "voxurf_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -92,6 +92,10 @@ class BgSampleArgs(C.Structure):
     ]
 
 
+class CastJob(C.Structure):
+    _fields_ = [("src", P), ("dst", P), ("rows", I32), ("cols", I32), ("src_ld", I32), ("dst_ld", I32)]
+
+
 class CoarseFeatureCfg(C.Structure):
     _fields_ = [("use_k0", I32), ("geo_rgb_dim", I32), ("posbase_pe", I64), ("viewbase_pe", I64)]
 
@@ -205,6 +209,8 @@ def _declare():
     lib.vx_density_mask.restype = C.c_int
     lib.vx_hit_coarse_geo.argtypes = [C.POINTER(FineMarchArgs), P, P]
     lib.vx_hit_coarse_geo.restype = C.c_int
+    lib.vx_cast_rows_bf16.argtypes = [C.POINTER(CastJob), I32, P]
+    lib.vx_cast_rows_bf16.restype = C.c_int
     lib.vx_bg_samples_count.argtypes = [C.POINTER(BgSampleArgs), P, P, P, C.c_size_t, P]
     lib.vx_bg_samples_count.restype = C.c_int
     lib.vx_bg_samples_fill.argtypes = [C.POINTER(BgSampleArgs), P, I64, P, P, P, P, P]
@@ -248,4 +254,4 @@ def struct_names() -> list[str]:
                                 "vx_sdf_gradient_grid", "vx_sdf_gradient_grid_adjoint",
                                 "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv",
                                 "vx_sdf_field", "vx_density_mask", "vx_hit_coarse_geo", "vx_bg_samples_count",
-                                "vx_bg_samples_fill"] + list(_SERVE_SIGNATURES)
+                                "vx_bg_samples_fill", "vx_cast_rows_bf16"] + list(_SERVE_SIGNATURES)

@@ -210,9 +210,52 @@ __global__ void head_backward_kernel(const float* __restrict__ dout, const T* __
 
 }  // namespace vx
 
+namespace vx {
+
+// Several FP32 -> BF16 row-block copies in one launch (the per-step casts of
+// the colour-MLP weights and biases in the mixed-precision step).  Block b
+// belongs to the job whose [first_block, first_block + blocks) holds b.
+struct CastJobs {
+  vx_cast_job job[VX_CAST_MAX_JOBS];
+  int first_block[VX_CAST_MAX_JOBS + 1];
+  int n;
+};
+
+__global__ void __launch_bounds__(256) cast_rows_bf16_kernel(const CastJobs J) {
+  int j = 0;
+  while (j + 1 < J.n && (int)blockIdx.x >= J.first_block[j + 1]) ++j;
+  const vx_cast_job& c = J.job[j];
+  const int64_t i = (int64_t)(blockIdx.x - J.first_block[j]) * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)c.rows * c.cols) return;
+  const int64_t r = i / c.cols, k = i - r * c.cols;
+  reinterpret_cast<__nv_bfloat16*>(c.dst)[r * c.dst_ld + k] = __float2bfloat16_rn(c.src[r * c.src_ld + k]);
+}
+
+}  // namespace vx
+
 using namespace vx;
 
 extern "C" {
+
+int vx_cast_rows_bf16(const vx_cast_job* jobs_host, int32_t n_jobs, void* stream) {
+  if (n_jobs < 0 || n_jobs > VX_CAST_MAX_JOBS || (n_jobs > 0 && !jobs_host)) return VX_ERR_ARG;
+  CastJobs J{};
+  int blocks = 0;
+  for (int j = 0; j < n_jobs; ++j) {
+    const vx_cast_job& c = jobs_host[j];
+    if (c.rows < 0 || c.cols < 0 || c.src_ld < c.cols || c.dst_ld < c.cols) return VX_ERR_ARG;
+    if (c.rows > 0 && c.cols > 0 && (!c.src || !c.dst)) return VX_ERR_ARG;
+    J.job[j] = c;
+    J.first_block[j] = blocks;
+    blocks += (int)((((int64_t)c.rows * c.cols) + 255) / 256);
+  }
+  J.first_block[n_jobs] = blocks;
+  J.n = n_jobs;
+  if (blocks == 0) return VX_OK;
+  cast_rows_bf16_kernel<<<blocks, 256, 0, as_stream(stream)>>>(J);
+  return launch_status();
+}
+
 
 int vx_mlp_head_backward(const float* dout, const void* h, const float* W, int64_t M, int64_t N, int dtype, void* dz,
                          float* dW, float* db, float* db_prev, void* stream) {

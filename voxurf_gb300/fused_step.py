@@ -111,6 +111,26 @@ class GraphedFineStep:
         self.W2p = torch.zeros((w2.shape[0], self.ld2), dtype=self.xdt, device=dev)
         self.rgb_params = list(model.rgbnet.parameters())
         self.k_params = list(model.k_rgbnet.parameters())
+        self.cast_jobs = None
+        if self.bf16:
+            # persistent BF16 copies of the MLP weights and biases, refreshed
+            # by one multi-job cast launch per step
+            jobs = []
+
+            def job(src, dst, cols, dst_ld):
+                rows = src.shape[0] if src.dim() == 2 else 1
+                jobs.append(_abi.CastJob(src.data_ptr(), dst.data_ptr(), rows, cols, cols, dst_ld))
+
+            self.bf_rgb = [torch.empty_like(p, dtype=torch.bfloat16) for p in self.rgb_params]
+            self.bf_k = [torch.empty_like(p, dtype=torch.bfloat16) for p in self.k_params]
+            job(w1, self.W1p, w1.shape[1], self.ld1)
+            job(w2, self.W2p, w2.shape[1], self.ld2)
+            for params, bufs in ((self.rgb_params, self.bf_rgb), (self.k_params, self.bf_k)):
+                for i, (p, b) in enumerate(zip(params, bufs)):
+                    if i > 0:   # the first layer's weight goes to the padded W1p / W2p
+                        job(p, b, p.shape[-1], p.shape[-1])
+            if len(jobs) <= 16 and all(p.is_contiguous() for p in self.rgb_params + self.k_params):
+                self.cast_jobs = (_abi.CastJob * len(jobs))(*jobs)
         self.cap = 0
         self.graphs = {}
         self.S2 = 0
@@ -266,17 +286,25 @@ class GraphedFineStep:
         b1 = [p for i, p in enumerate(self.rgb_params) if i % 2 == 1]
         W2 = [p for i, p in enumerate(self.k_params) if i % 2 == 0]
         b2 = [p for i, p in enumerate(self.k_params) if i % 2 == 1]
-        self.W1p[:, :self.d1].copy_(W1[0].detach())
-        Ws1 = [self.W1p] + [w.detach().to(xdt) for w in W1[1:]]
-        bs1 = [b.detach().to(xdt) for b in b1]
+        if self.cast_jobs is not None:
+            _abi.call("vx_cast_rows_bf16", self.cast_jobs, len(self.cast_jobs), st)
+            Ws1 = [self.W1p] + [self.bf_rgb[i] for i in range(2, len(self.bf_rgb), 2)]
+            bs1 = [self.bf_rgb[i] for i in range(1, len(self.bf_rgb), 2)]
+            Ws2 = [self.W2p] + [self.bf_k[i] for i in range(2, len(self.bf_k), 2)]
+            bs2 = [self.bf_k[i] for i in range(1, len(self.bf_k), 2)]
+        else:
+            self.W1p[:, :self.d1].copy_(W1[0].detach())
+            Ws1 = [self.W1p] + [w.detach().to(xdt) for w in W1[1:]]
+            bs1 = [b.detach().to(xdt) for b in b1]
         hs1 = mlp_forward(X1, Ws1, bs1)
         logit = hs1[-1].float()
         if self.k_res:
             X2[:, self.d2a:self.d2a + 3].copy_(logit)
         d2 = self.d2a + (3 if self.k_res else 0)
-        self.W2p[:, :d2].copy_(W2[0].detach())
-        Ws2 = [self.W2p] + [w.detach().to(xdt) for w in W2[1:]]
-        bs2 = [b.detach().to(xdt) for b in b2]
+        if self.cast_jobs is None:
+            self.W2p[:, :d2].copy_(W2[0].detach())
+            Ws2 = [self.W2p] + [w.detach().to(xdt) for w in W2[1:]]
+            bs2 = [b.detach().to(xdt) for b in b2]
         hs2 = mlp_forward(X2, Ws2, bs2)
         klogit = logit + hs2[-1].float()
         # compositing
