@@ -49,9 +49,11 @@ def _gemm_f32(dz: torch.Tensor, other: torch.Tensor, wgrad: bool) -> torch.Tenso
     return out
 
 
-def _colsum(dh: torch.Tensor, h: torch.Tensor | None, dz: torch.Tensor | None) -> torch.Tensor:
+def _colsum(dh: torch.Tensor, h: torch.Tensor | None, dz: torch.Tensor | None,
+            out: torch.Tensor | None = None) -> torch.Tensor:
     M, N = dh.shape
-    out = torch.zeros(N, dtype=torch.float32, device=dh.device)
+    if out is None:
+        out = torch.zeros(N, dtype=torch.float32, device=dh.device)
     dtype = 1 if dh.dtype == torch.bfloat16 else 0
     call("vx_relu_bwd_colsum", ptr(dh), ptr(h), M, N, dtype, ptr(dz), ptr(out), stream_ptr())
     return out
@@ -101,13 +103,24 @@ def mlp_backward(dy: torch.Tensor, hs, Ws, need_dx: bool):
     grads = [None] * (2 * n)
     dx = None
     top = n
-    if _head_layer(Ws, hs[n - 1]):
+    head = _head_layer(Ws, hs[n - 1])
+    # every accumulator of the pass (head dW, dbh, db; the bias gradients of
+    # the layers below) comes from one zero-filled buffer, 16-byte aligned
+    sizes = [3 * hs[n - 1].shape[1], 3, hs[n - 1].shape[1]] if head else [dy.shape[1]]
+    sizes += [Ws[i].shape[1] for i in reversed(range(1, n - 1 if head else n))]
+    offs, total = [], 0
+    for sz in sizes:
+        offs.append(total)
+        total += (sz + 3) // 4 * 4
+    acc = torch.zeros(total, dtype=torch.float32, device=dy.device)
+    views = iter([acc[o:o + sz] for o, sz in zip(offs, sizes)])
+    if head:
         h = hs[n - 1]
         M, N = h.shape
         dev = h.device
-        dW = torch.zeros((3, N), dtype=torch.float32, device=dev)
-        dbh = torch.zeros(3, dtype=torch.float32, device=dev)
-        db = torch.zeros(N, dtype=torch.float32, device=dev)
+        dW = next(views).view(3, N)
+        dbh = next(views)
+        db = next(views)
         dz = torch.empty_like(h)
         W = Ws[n - 1].float().contiguous()
         dout = dy.float().contiguous()  # kept alive until the kernel is enqueued
@@ -118,7 +131,7 @@ def mlp_backward(dy: torch.Tensor, hs, Ws, need_dx: bool):
         top = n - 1
     else:
         dz = dy.to(hs[0].dtype).contiguous()
-        db = _colsum(dz, None, None)
+        db = _colsum(dz, None, None, next(views))
     lib_gemm = dz.dtype == torch.float32 and FP32_GEMM != "torch"
     for i in reversed(range(top)):
         if lib_gemm:
@@ -130,7 +143,7 @@ def mlp_backward(dy: torch.Tensor, hs, Ws, need_dx: bool):
         if i > 0:
             dh = _gemm_f32(dz, W, False) if lib_gemm else dz @ Ws[i]
             dz_prev = torch.empty_like(dh)
-            db = _colsum(dh, hs[i], dz_prev)
+            db = _colsum(dh, hs[i], dz_prev, next(views))
             dz = dz_prev
         elif need_dx:
             dx = _gemm_f32(dz, W, False) if lib_gemm else dz @ Ws[0]
