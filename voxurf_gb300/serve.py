@@ -248,6 +248,8 @@ class _TickSlot:
         self.chunk_dev = torch.empty_like(self.chunk_host, device=dev)
         self.chunk_ready = torch.cuda.Event()
         self.bounds_host = torch.empty(16, dtype=torch.int64, pin_memory=True)
+        self.idx_host = torch.empty(16, dtype=torch.int64, pin_memory=True)   # scene bounds, staged
+        self.idx_dev = torch.empty(16, dtype=torch.int64, device=dev)
         self.ev_back = None   # recorded after the back half of the slot's last tick
 
 
@@ -475,9 +477,12 @@ class RenderServer:
         N = ray0
         nbytes = ctypes.sizeof(chunks)
         with torch.cuda.stream(fs):
-            sl.chunk_ready.synchronize()   # the pinned table's previous upload is done
+            sl.chunk_ready.synchronize()   # the slot's pinned staging is free again
             ctypes.memmove(sl.chunk_host.data_ptr(), ctypes.addressof(chunks), nbytes)
             sl.chunk_dev[:nbytes].copy_(sl.chunk_host[:nbytes], non_blocking=True)
+            nb = len(bounds)
+            sl.idx_host[:nb].copy_(torch.tensor(bounds, dtype=torch.int64))
+            sl.idx_dev[:nb].copy_(sl.idx_host[:nb], non_blocking=True)
             sl.chunk_ready.record(fs)
             o, d, v = sl.rays[0], sl.rays[1], sl.rays[2]
             tab, ns = self.table, len(self.scenes)
@@ -487,8 +492,7 @@ class RenderServer:
                       ptr(sl.rec), ptr(sl.n2), ptr(sl.alast), st)
             _abi.call("vx_exclusive_scan_i32", ptr(sl.n2), N, ptr(sl.s2_off), ptr(sl.scan_tmp), self.scan_bytes,
                       st)
-            idx = torch.tensor(bounds, dtype=torch.int64).to(self.device, non_blocking=True)
-            sl.bounds_host[:len(bounds)].copy_(sl.s2_off.index_select(0, idx), non_blocking=True)
+            sl.bounds_host[:nb].copy_(sl.s2_off.index_select(0, sl.idx_dev[:nb]), non_blocking=True)
             t.ev_front = torch.cuda.Event()
             t.ev_front.record(fs)
         return t
