@@ -383,9 +383,9 @@ class RenderServer:
     # ---- one tick -----------------------------------------------------------
     def tick(self) -> int:
         """Admits what fits, launches the front half of one tick of rays and
-        the back half of the previous tick, harvests finished requests.
+        the back half of the previous tick, then harvests finished requests
+        (their host copies overlap the launched work).
         Returns the number of rays launched."""
-        self.poll()
         self._admit()
         budget = self.tick_rays
         batch = []
@@ -404,6 +404,9 @@ class RenderServer:
         if self.pending is not None:
             self._back(self.pending)
         self.pending = None
+        # completed requests are copied out of the pinned arena while the
+        # GPU runs what was just launched
+        self.poll()
         if new is None:
             return 0
         self._row_bounds(new)   # the tick's one host sync (front stream only)
