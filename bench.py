@@ -651,7 +651,29 @@ def run_render(args, dev):
     n = args.render_requests
     poisson = serve.run_stream(server, serve.request_stream(n, RENDER_RATE, RENDER_SCENES, seed=1))
     rows0 = server.rows_shaded
+    # host time per tick of the saturated stream, by server method
+    host = {"_front": 0.0, "_back": 0.0, "_row_bounds": 0.0, "poll": 0.0}
+
+    def timed(name, fn):
+        def call(*a, **k):
+            t0 = time.perf_counter()
+            try:
+                return fn(*a, **k)
+            finally:
+                host[name] += time.perf_counter() - t0
+        return call
+
+    for name in host:
+        setattr(server, name, timed(name, getattr(server, name)))
+    ticks0 = server.ticks
     saturated = serve.run_stream(server, serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2))
+    for name in host:
+        delattr(server, name)   # back to the class methods
+    ticks = max(server.ticks - ticks0, 1)
+    saturated["host_ms_per_tick"] = {
+        "ticks": ticks, "wall": saturated["wall_s"] * 1e3 / ticks, "launch_front": host["_front"] * 1e3 / ticks,
+        "launch_back": host["_back"] * 1e3 / ticks, "harvest": host["poll"] * 1e3 / ticks,
+        "wait_row_counts": host["_row_bounds"] * 1e3 / ticks}
     rows = server.rows_shaded - rows0
     sat_wall = saturated["wall_s"]
 
