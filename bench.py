@@ -49,9 +49,16 @@ K0_ELEMS = R ** 3 * 12
 SWEEP_BYTES_PER_ELEM = 28
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k0 sweep
 # launch: ncu capture at 128^3 (402.69 MB read + 253.78 MB written for
-# 25.17M elements, profiles/grid_tv_adam_row_k0.md) scaled by the element
-# count to 256^3 (x8).
+# 25.17M elements) scaled by the element count to 256^3 (x8).
 SWEEP_NCU_TRAFFIC = (402.692608e6 + 253.783552e6) * 8 if R == 256 else None
+
+
+def bench_config() -> dict:
+    """The workload, identical in both arms."""
+    return {"workload": "voxurf fine stage train step: SDF 256^3 f32 + k0 256^3x12 f32, 8192 rays/step, "
+                        "stepsize 0.5, mask |SDF|<0.05, MLP 192x4 (x2), TV 1e-4, Adam 1e-3",
+            "rays_per_step": N_RAYS, "grid": R,
+            "l2": "no flush: ~10 GB of grids + Adam state swept per step (> 129 MB L2)"}
 
 
 def parse():
@@ -350,11 +357,8 @@ def run_ours(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_total * 1000 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "voxurf fine stage train step: SDF 256^3 f32 + k0 256^3x12 f32, 8192 rays/step, "
-                                   "stepsize 0.5, mask |SDF|<0.05, MLP 192x4 (x2), TV 1e-4, Adam 1e-3",
-                       "rays_per_step": N_RAYS, "grid": R, "shaded_samples_last_step": shaded,
-                       "parallelism": f"replicas x{world}",
-                       "l2": "no flush: ~10 GB of grids + Adam state swept per step (> 129 MB L2)"},
+            "config": bench_config(),
+            "parallelism": f"replicas x{world}", "shaded_samples_last_step": shaded,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4},
             "fused_bf16": bf16,
             "render": render,
@@ -366,8 +370,26 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),
+            # the sub-results that matter most, last (a reader of the output's
+            # tail sees them)
+            "headline": headline(value, e2e, bf16, render, long_rays),
         }
         print(json.dumps(line))
+
+
+def headline(value, e2e, bf16, render, long_rays) -> dict:
+    h = {"fp32_rays_s": value, "fp32_e2e_rays_s": e2e}
+    if bf16:
+        h["bf16_rays_s"] = bf16["value"]
+        h["bf16_ms_per_step"] = bf16["ms_per_step"]
+        h["bf16_speedup_vs_fp32"] = bf16["speedup_vs_fp32"]
+    if render:
+        h["render_saturated_mpix_s"] = render["saturated"]["mpix_s"]
+        h["render_poisson_p99_ms_800x600"] = render["poisson_50_req_s"].get("p99_ms_800x600")
+        h["render_poisson_p50_ms"] = render["poisson_50_req_s"].get("p50_ms")
+    if long_rays:
+        h["long_rays_bf16_speedup_vs_fp32"] = long_rays["speedup_bf16_vs_fp32"]
+    return h
 
 
 LONG_R = 384               # long-ray workload: 64 spheres, stepsize 0.25, 65536 rays, s = 0.05
@@ -651,7 +673,11 @@ def run_render(args, dev):
     n = args.render_requests
     poisson = serve.run_stream(server, serve.request_stream(n, RENDER_RATE, RENDER_SCENES, seed=1))
     rows0 = server.rows_shaded
-    # host time per tick of the saturated stream, by server method
+    saturated = serve.run_stream(server, serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2))
+    rows = server.rows_shaded - rows0
+    sat_wall = saturated["wall_s"]
+    # host time per tick by server method, on a second saturated stream
+    # (timed wrappers around the methods: not part of the figures above)
     host = {"_front": 0.0, "_back": 0.0, "_row_bounds": 0.0, "poll": 0.0}
 
     def timed(name, fn):
@@ -666,16 +692,14 @@ def run_render(args, dev):
     for name in host:
         setattr(server, name, timed(name, getattr(server, name)))
     ticks0 = server.ticks
-    saturated = serve.run_stream(server, serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2))
+    probe = serve.run_stream(server, serve.request_stream(n, float("inf"), RENDER_SCENES, seed=3))
     for name in host:
         delattr(server, name)   # back to the class methods
     ticks = max(server.ticks - ticks0, 1)
-    saturated["host_ms_per_tick"] = {
-        "ticks": ticks, "wall": saturated["wall_s"] * 1e3 / ticks, "launch_front": host["_front"] * 1e3 / ticks,
-        "launch_back": host["_back"] * 1e3 / ticks, "harvest": host["poll"] * 1e3 / ticks,
-        "wait_row_counts": host["_row_bounds"] * 1e3 / ticks}
-    rows = server.rows_shaded - rows0
-    sat_wall = saturated["wall_s"]
+    saturated["host_ms_per_tick_probe"] = {
+        "ticks": ticks, "wall": probe["wall_s"] * 1e3 / ticks, "probe_mpix_s": probe["mpix_s"],
+        "launch_front": host["_front"] * 1e3 / ticks, "launch_back": host["_back"] * 1e3 / ticks,
+        "harvest": host["poll"] * 1e3 / ticks, "wait_row_counts": host["_row_bounds"] * 1e3 / ticks}
 
     # plain per-request FP32 render of the first requests of the saturated stream
     stream = serve.request_stream(n, float("inf"), RENDER_SCENES, seed=2)[:args.render_plain]
@@ -722,40 +746,40 @@ def run_render(args, dev):
     }
 
 
-def cpu_baseline(seconds_hint=20.0):
+def cpu_baseline():
     """The reference step on the host CPU (oracle restatement, FP32, all
-    threads): full steps at 1024 and 4096 rays on the 256^3 grids, fitted
-    t(n) = a + b n and evaluated at 8192 rays (the dense TV/Adam/smoothing
-    work is the constant a)."""
+    threads), a bounded sample of the benchmark workload: one warm-up and
+    three timed full steps of 8192 rays on the 256^3 grids (~20 s)."""
     import torch
 
-    from oracle.bench_cpu import time_reference_step
+    from oracle.bench_cpu import time_reference_steps
 
     cores = os.cpu_count() or 1
     torch.set_num_threads(cores)
-    res = time_reference_step(R, [1024, 4096], N_RAYS)
-    return {"value": res["rays_per_s"], "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": res["sample"]}
+    res = time_reference_steps(R, N_RAYS, 1, 3)
+    return {"value": res["rays_per_s"], "unit": UNIT, "cores": cores, "kind": "port", "sample": res["sample"]}
 
 
 def run_reference(args, world, rank):
+    """The reference arm: --warmup untimed and --steps timed full reference
+    steps (8192 rays on the 256^3 grids each, ~5 s of CPU per step) on all
+    host cores, rank 0 only."""
     if rank != 0:
         return
     import torch
 
-    from oracle.bench_cpu import time_reference_step
+    from oracle.bench_cpu import time_reference_steps
 
     cores = os.cpu_count() or 1
     torch.set_num_threads(cores)
-    res = time_reference_step(R, [1024, 4096], N_RAYS, repeats=max(1, min(args.steps, 2)))
+    res = time_reference_steps(R, N_RAYS, args.warmup, args.steps)
     v = res["rays_per_s"]
+    t_total = sum(res["times"])
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * N_RAYS / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": "voxurf fine stage train step: SDF 256^3 f32 + k0 256^3x12 f32, 8192 rays/step, "
-                               "stepsize 0.5, mask |SDF|<0.05, MLP 192x4 (x2), TV 1e-4, Adam 1e-3",
-                   "rays_per_step": N_RAYS, "grid": R},
+        "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": bench_config(),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": res["sample"]},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

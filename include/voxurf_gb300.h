@@ -94,9 +94,11 @@ int vx_sample_pts_count(const float* rays_o, const float* rays_d, const float* x
  * VX_NOALLOC_MAX_RAYS (larger sizes return VX_ERR_TOO_LARGE without touching
  * the GPU).  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls on a device share the array: calls
- * that overlap on the GPU race.  No cudaMalloc/cudaFree or other allocating
- * call is made. */
+ * before any stream capture.  The address is kept for the life of the
+ * process: a caller that destroys and recreates the device's primary
+ * context (cudaDeviceReset) must not call this entry point afterwards.  All
+ * calls on a device share the array: calls that overlap on the GPU race.  No
+ * cudaMalloc/cudaFree or other allocating call is made. */
 int vx_sample_pts_count_noalloc(const float* rays_o, const float* rays_d, const float* xyz_min,
                                 const float* xyz_max, float near, float far, float stepdist, int64_t n_rays,
                                 float* t_min, float* t_max, int64_t* n_steps, int64_t* offsets, void* stream);

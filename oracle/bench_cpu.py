@@ -60,7 +60,11 @@ def reference_step(oracle, opt, world_max, rays, rk, global_step, tv_weight=1e-4
     return float(loss.item())
 
 
-def time_reference_step(R: int, ray_counts, n_target: int, repeats: int = 1, seed: int = 0):
+def time_reference_steps(R: int, n_rays: int, warmup: int, steps: int, seed: int = 0):
+    """Full reference training steps on the host CPU at the benchmark's own
+    size (R^3 grids, n_rays rays per step, a fresh seeded batch per step):
+    `warmup` untimed steps, then `steps` timed ones.  Returns the per-step
+    wall times (s) and a one-line description of the sample."""
     from voxurf_gb300 import configs, synthetic
 
     from .voxurf_oracle import UtilsAdam
@@ -69,31 +73,18 @@ def time_reference_step(R: int, ray_counts, n_target: int, repeats: int = 1, see
     opt = UtilsAdam([([oracle.sdf_grid], 1e-3), ([oracle.k0_grid], 1e-3), (list(oracle.rgbnet.parameters()), 1e-3),
                      (list(oracle.k_rgbnet.parameters()), 1e-3)], betas=(0.9, 0.99))
     rk = dict(configs.FINE_RENDER_KWARGS)
-    times = {}
-    step = 1
-    for n in ray_counts:
-        o, d, v = synthetic.random_rays(n, seed=seed + n)
-        t = configs.train_targets(n, seed + n)
-        rays = tuple(torch.from_numpy(a) for a in (o, d, v, t))
-        reference_step(oracle, opt, world_max, rays, rk, step)  # warm-up
-        step += 1
-        ts = []
-        for _ in range(repeats):
-            t0 = time.perf_counter()
-            reference_step(oracle, opt, world_max, rays, rk, step)
-            ts.append(time.perf_counter() - t0)
-            step += 1
-        times[n] = float(np.median(ts))
-    ns = sorted(times)
-    if len(ns) >= 2:
-        b = (times[ns[-1]] - times[ns[0]]) / (ns[-1] - ns[0])
-        a = times[ns[0]] - b * ns[0]
-        b = max(b, 0.0)
-        a = max(a, 0.0)
-        t_target = a + b * n_target
-    else:
-        t_target = times[ns[0]] * n_target / ns[0]
-    sample = (f"full reference steps (fwd+bwd+TV+Adam, FP32 torch on CPU) on the {R}^3 grids at "
-              + ", ".join(f"{n} rays: {times[n]:.2f} s" for n in ns)
-              + f"; t(n) = a + b*n fitted, evaluated at {n_target} rays = {t_target:.2f} s")
-    return {"rays_per_s": n_target / t_target, "sample": sample, "times": times, "t_target": t_target}
+    total = warmup + steps
+    o, d, v = synthetic.random_rays(n_rays * total, seed=seed + 1)
+    t = configs.train_targets(n_rays * total, seed + 1)
+    times = []
+    for i in range(total):
+        sl = slice(i * n_rays, (i + 1) * n_rays)
+        rays = tuple(torch.from_numpy(np.ascontiguousarray(a[sl])) for a in (o, d, v, t))
+        t0 = time.perf_counter()
+        reference_step(oracle, opt, world_max, rays, rk, i + 1)
+        if i >= warmup:
+            times.append(time.perf_counter() - t0)
+    sample = (f"{steps} full reference steps of {n_rays} rays (fwd+bwd+TV+Adam, FP32 torch on CPU, the {R}^3 "
+              f"grids) after {warmup} warm-up: median {float(np.median(times)):.2f} s, "
+              f"total {sum(times):.1f} s")
+    return {"times": times, "sample": sample, "rays_per_s": n_rays * steps / sum(times)}

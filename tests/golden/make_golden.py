@@ -2,8 +2,8 @@
 Voxurf Python code (lib/voxurf_fine.py, lib/voxurf_coarse.py, lib/grid.py,
 lib/utils.py) on the CPU in float64.
 
-Run in a container that has the reference sources (default path below, or
-$VOXURF_REFERENCE); the GPU machine never runs this.  The reference imports
+Run in a container that has the reference sources, with their path in
+$VOXURF_REFERENCE; the GPU machine never runs this.  The reference imports
 several packages that are absent here and JIT-builds CUDA extensions; this
 script stubs them:
   * cv2, mcubes, matplotlib, plyfile, imageio, skimage, trimesh, lpips ->
@@ -17,7 +17,8 @@ script stubs them:
     reference's checkpoint loading relies on).
 PYTHONDONTWRITEBYTECODE keeps the read-only reference tree clean.
 
-    python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt]   (default: all)
+    VOXURF_REFERENCE=<reference checkout> python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt]
+    (default: all)
 """
 from __future__ import annotations
 
@@ -35,7 +36,7 @@ import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("VOXURF_REFERENCE", "/root/reference")
+REF = os.environ.get("VOXURF_REFERENCE")
 sys.path.insert(0, REPO)
 
 from oracle import cref  # noqa: E402
@@ -99,6 +100,8 @@ def install_stubs():
     # arrays run.py stores in checkpoints (MaskCache_kwargs['xyz_min'], ...)
     _load = torch.load
     torch.load = lambda *a, **k: _load(*a, **{"weights_only": False, **k})
+    if not REF or not os.path.isdir(os.path.join(REF, "lib")):
+        raise SystemExit("set VOXURF_REFERENCE to a checkout of the reference (the directory holding lib/)")
     sys.path.insert(0, REF)
 
 

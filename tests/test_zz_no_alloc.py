@@ -60,6 +60,31 @@ def test_noalloc_count_matches_allocating_entry_point(cuda):
         assert got[3][-1] == got[2].sum()
 
 
+def test_noalloc_count_empty_and_largest(cuda):
+    """n_rays = 0 (only offsets[0] = 0 is written) and n_rays exactly at the
+    maximum, the call that uses every entry of the static scratch."""
+    lib = _native.load()
+    bmin = torch.tensor([-1.0, -1.0, -1.0], device=cuda)
+    bmax = torch.tensor([1.0, 1.0, 1.0], device=cuda)
+    offsets = torch.full((1,), -1, dtype=torch.int64, device=cuda)
+    null = ctypes.c_void_p(0)
+    status = lib.vx_sample_pts_count_noalloc(null, null, null, null, 0.1, 1e9, 0.01, 0, null, null, null,
+                                             ptr(offsets), stream_ptr())
+    assert status == 0, lib.vx_status_string(status)
+    torch.cuda.synchronize()
+    assert int(offsets.item()) == 0
+    n = VX_NOALLOC_MAX_RAYS
+    g = torch.Generator(cuda).manual_seed(3)
+    rays_o = (torch.rand((n, 3), device=cuda, generator=g) * 2 - 1) * 3
+    rays_d = -rays_o + (torch.rand((n, 3), device=cuda, generator=g) - 0.5)
+    stepdist = float(np.float32(0.5 * 2.0 / 128))
+    ref = _count(lib, "vx_sample_pts_count", rays_o, rays_d, bmin, bmax, stepdist, cuda)
+    got = _count(lib, "vx_sample_pts_count_noalloc", rays_o, rays_d, bmin, bmax, stepdist, cuda)
+    for a, b in zip(got, ref):
+        np.testing.assert_array_equal(a, b)
+    assert got[3][-1] == got[2].sum()
+
+
 def test_noalloc_rejects_sizes_above_the_maximum(cuda):
     lib = _native.load()
     # rejected on the host before any pointer is used or any kernel launched

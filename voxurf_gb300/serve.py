@@ -325,6 +325,7 @@ class RenderServer:
         self.queue: deque[RenderRequest] = deque()   # waiting for admission
         self.active: list[RenderRequest] = []        # admitted, pixels left to launch
         self.finishing: list[RenderRequest] = []     # all pixels launched, copy in flight
+        self.reaped: list[RenderRequest] = []        # in the pinned arena, host copy pending
         self.done: list[RenderRequest] = []
         self._next_id = 0
         self.ticks = 0
@@ -355,37 +356,49 @@ class RenderServer:
             r.t_admit = time.perf_counter()
             self.active.append(r)
 
-    def poll(self) -> list[RenderRequest]:
-        """Completes the requests whose results have reached host memory."""
-        out = []
+    def _reap(self) -> None:
+        """Requests whose results have reached the pinned arena give back
+        their arena range and their seat (an event query each; no copy).
+        Their pinned range stays intact until poll() copies it out: a request
+        admitted into it now is copied to host memory only after it has been
+        rendered, ticks later."""
         still = []
         for r in self.finishing:
             if r.event.query():
-                r.t_done = time.perf_counter()
-                a, b = r.off, r.off + r.n_pix
-                r.rgb = self.host_rgb[a:b].numpy().reshape(r.H, r.W, 3).copy()
-                r.depth = self.host_depth[a:b].numpy().reshape(r.H, r.W).copy()
                 self.arena.release(r.off, r.n_pix)
                 r.event = None
-                out.append(r)
+                self.reaped.append(r)
             else:
                 still.append(r)
         self.finishing = still
+
+    def poll(self) -> list[RenderRequest]:
+        """Completes the requests whose results have reached host memory."""
+        self._reap()
+        out = self.reaped
+        self.reaped = []
+        for r in out:
+            a, b = r.off, r.off + r.n_pix
+            r.rgb = self.host_rgb[a:b].numpy().reshape(r.H, r.W, 3).copy()
+            r.depth = self.host_depth[a:b].numpy().reshape(r.H, r.W).copy()
+            r.t_done = time.perf_counter()
         self.done.extend(out)
         return out
 
     def idle(self) -> bool:
-        return not (self.queue or self.active or self.finishing or self.pending)
+        return not (self.queue or self.active or self.finishing or self.reaped or self.pending)
 
     def has_work(self) -> bool:
         return bool(self.queue or self.active or self.pending)
 
     # ---- one tick -----------------------------------------------------------
     def tick(self) -> int:
-        """Admits what fits, launches the front half of one tick of rays and
-        the back half of the previous tick, then harvests finished requests
-        (their host copies overlap the launched work).
+        """Frees the seats and arena ranges of finished requests, admits what
+        fits, launches the front half of one tick of rays and the back half
+        of the previous tick, then copies finished requests out of the pinned
+        arena (those host copies overlap the launched work).
         Returns the number of rays launched."""
+        self._reap()
         self._admit()
         budget = self.tick_rays
         batch = []
