@@ -353,11 +353,12 @@ class OracleCoarse(nn.Module):
         self.s_val = model.s_val.clone().float().cpu()
         self.mask = _mask_state(model)
 
-    def forward(self, rays_o, rays_d, viewdirs, global_step=None, device_keep=None, **rk):
+    def forward(self, rays_o, rays_d, viewdirs, global_step=None, device_keep=None, tie_rel=1e-5, **rk):
         """device_keep: optional set of (ray_id, step_id) pairs that a device
         run kept after the fast_color_thres test.  A sample whose weight is
-        within 1e-5 relative of the threshold (a tie at FP32 precision) then
-        takes the device's decision, so that both sides shade the same set."""
+        within tie_rel (relative) of the threshold (a tie at FP32 precision)
+        then takes the device's decision, so that both sides shade the same
+        set."""
         dt = self.dtype
         N = len(rays_o)
         stepdist = f32(rk["stepsize"] * np.float32(self.voxel_size))
@@ -389,7 +390,7 @@ class OracleCoarse(nn.Module):
         weights, _ = Alphas2WeightsOracle.apply(alpha, ray_id, N)
         m = weights > self.fast_color_thres
         if device_keep is not None:
-            near = ((weights.detach() - self.fast_color_thres).abs() <= 1e-5 * self.fast_color_thres).nonzero()
+            near = ((weights.detach() - self.fast_color_thres).abs() <= tie_rel * self.fast_color_thres).nonzero()
             for i in near.reshape(-1).tolist():
                 m[i] = (int(ray_id[i]), int(step_id[i])) in device_keep
             self.ties = int(near.numel())

@@ -92,14 +92,22 @@ def fine256(cuda):
     rays = tuple(a[:SUB] for a in full)
     orc = OracleFine(model, dtype=torch.float64)
     world_max = float(model.world_size.max())
+    model32 = model
     del model
-    torch.cuda.empty_cache()
     before = _params(orc.sdf_grid, orc.k0_grid, orc.rgbnet, orc.k_rgbnet)
     ro, rd, vd, tgt = (torch.from_numpy(a) for a in rays)
     ret = orc(ro, rd, vd, global_step=1, **RK)
     loss = train_loss(ret, tgt.double())
     loss.backward()
     grads = _oracle_grads(orc)
+    # the reference algorithm's own FP32 error on this batch (same step in
+    # FP32): the FP32 bars are max(1e-5, 3x this)
+    orc32 = OracleFine(model32, dtype=torch.float32)
+    del model32
+    torch.cuda.empty_cache()
+    train_loss(orc32(ro, rd, vd, global_step=1, **RK), tgt).backward()
+    ref32 = {k: _rel_l2(v, grads[k]) for k, v in _oracle_grads(orc32).items()}
+    del orc32
     tv_add_grad(orc.sdf_grid, 1e-4 / SUB, world_max, True)
     tv_add_grad(orc.k0_grid, 1e-4 / SUB, world_max, True)
     opt = UtilsAdam([([orc.sdf_grid], 1e-3), ([orc.k0_grid], 1e-3), (list(orc.rgbnet.parameters()), 1e-3),
@@ -108,7 +116,7 @@ def fine256(cuda):
     after = _params(orc.sdf_grid, orc.k0_grid, orc.rgbnet, orc.k_rgbnet)
     delta = {k: after[k] - before[k] for k in before}
     out = {"rays": rays, "full": full, "ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in ret.items()},
-           "loss": float(loss.item()), "grads": grads, "before": before, "delta": delta}
+           "loss": float(loss.item()), "grads": grads, "ref32": ref32, "before": before, "delta": delta}
     del orc, opt, after
     return out
 
@@ -132,14 +140,15 @@ def test_fine256_fp32_step_matches_fp64_oracle(cuda, fine256):
     torch.cuda.synchronize()
     assert ret["weights"].numel() == o["weights"].numel() > 2000
     assert torch.equal(ret["ray_id"].long().cpu(), o["ray_id"])
-    assert torch.equal(ret["step_id"].long().cpu(), o["step_id"])
+    assert torch.equal(model._last_frame.step2.long().cpu(), o["step_id"])
     for key in ("rgb_marched", "rgb_marched0"):
         err = (ret[key].double().detach().cpu() - o[key]).abs().max().item()
         assert err <= 1e-5, (key, err)
     assert abs(float(loss) - fine256["loss"]) <= 1e-6 * abs(fine256["loss"])
-    for name, ref in fine256["grads"].items():
-        err = _rel_l2(grads[name], ref)
-        assert err <= 1e-5, (name, err)
+    errs = {name: _rel_l2(grads[name], ref) for name, ref in fine256["grads"].items()}
+    print("fp32 step vs FP64 (256^3 bench workload):", errs, "reference fp32:", fine256["ref32"])
+    for name, err in errs.items():
+        assert err <= max(1e-5, 3 * fine256["ref32"][name]), (name, err, fine256["ref32"][name])
     # the update of the whole step, against the oracle's updated parameters
     # rounded to the FP32 storage both sides keep them in (otherwise one ulp
     # of a parameter near 1, 6e-8, would count against a 1e-3 Adam step)
@@ -148,14 +157,15 @@ def test_fine256_fp32_step_matches_fp64_oracle(cuda, fine256):
         p0 = fine256["before"][name]
         ref32 = (p0 + ref).float().double() - p0
         err = _rel_l2(after[name] - p0, ref32)
-        assert err <= 1e-5, ("update", name, err)
+        assert err <= max(1e-5, 3 * fine256["ref32"][name]), ("update", name, err)
 
 
-# Measured errors of the BF16 graph-replayed step against FP64 on this batch
-# bound the checks below at about three times their size (the k0 grid and the
-# MLP run in BF16 with FP32 accumulation; the SDF grid, alpha and normals in
-# FP32).
-BF16_BOUNDS = {"rgb": 1e-3, "loss": 2e-3, "sdf": 1e-1, "k0": 1e-1, "mlp": 1e-1}
+# Bounds of the BF16 graph-replayed step against FP64 on this batch, about
+# 2-3x the measured errors (RGB 1.5e-4, loss 3.5e-6, SDF gradient 7.4e-4, k0
+# gradient 4.4e-2, MLP weight gradients <= 2.1e-2): the k0 grid and the MLP
+# run in BF16 with FP32 accumulation, the SDF grid, alpha and normals in
+# FP32; the k0 gradient sums many BF16 input gradients of either sign.
+BF16_BOUNDS = {"rgb": 1e-3, "loss": 1e-5, "sdf": 2e-3, "k0": 1e-1, "mlp": 5e-2}
 
 
 def test_fine256_bf16_graphed_step_vs_fp64_oracle(cuda, fine256):
@@ -221,11 +231,22 @@ def long384(cuda):
     o = orc(*(torch.from_numpy(a) for a in rays[:3]), global_step=0, **rk)
     ol = train_loss(o, torch.from_numpy(rays[3]).double())
     ol.backward()
-    out = {"rays": rays, "rk": rk, "ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in o.items()},
-           "grads": {"sdf": orc.sdf_grid.grad, "k0": orc.k0_grid.grad,
-                     "rgbnet": [q.grad for q in orc.rgbnet.parameters()],
-                     "k_rgbnet": [q.grad for q in orc.k_rgbnet.parameters()]}}
-    return out
+    grads = {"sdf": orc.sdf_grid.grad, "k0": orc.k0_grid.grad,
+             "rgbnet": [q.grad for q in orc.rgbnet.parameters()],
+             "k_rgbnet": [q.grad for q in orc.k_rgbnet.parameters()]}
+    # the reference algorithm's own FP32 error on this batch
+    model = _long_model(cuda, "fp32")
+    orc32 = OracleFine(model, dtype=torch.float32)
+    del model
+    torch.cuda.empty_cache()
+    train_loss(orc32(*(torch.from_numpy(a) for a in rays[:3]), global_step=0, **rk),
+               torch.from_numpy(rays[3])).backward()
+    ref32 = {"sdf": _rel_l2(orc32.sdf_grid.grad, grads["sdf"]), "k0": _rel_l2(orc32.k0_grid.grad, grads["k0"])}
+    for net in ("rgbnet", "k_rgbnet"):
+        for (n, q), r in zip(getattr(orc32, net).named_parameters(), grads[net]):
+            ref32[net + "." + n] = _rel_l2(q.grad, r)
+    return {"rays": rays, "rk": rk, "ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in o.items()},
+            "grads": grads, "ref32": ref32}
 
 
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
@@ -243,14 +264,15 @@ def test_long_rays_384_vs_fp64_oracle(cuda, precision, long384):
     for net in ("rgbnet", "k_rgbnet"):
         for (n, p), q in zip(getattr(model, net).named_parameters(), og[net]):
             errs[net + "." + n] = _rel_l2(p.grad, q)
-    print(precision, "384^3 long rays vs FP64:", errs, "shaded", o["weights"].numel())
+    print(precision, "384^3 long rays vs FP64:", errs, "shaded", o["weights"].numel(), "reference fp32:",
+          long384["ref32"])
     assert o["weights"].numel() > 1000
     if precision == "fp32":
         assert torch.equal(g["ray_id"].long().cpu(), o["ray_id"])
         assert err <= 1e-5
         for k, v in errs.items():
             if k != "rgb":
-                assert v <= 1e-5, (k, v)
+                assert v <= max(1e-5, 3 * long384["ref32"][k]), (k, v, long384["ref32"][k])
     else:
         assert err <= 1e-3
         assert errs["sdf"] <= BF16_BOUNDS["sdf"] and errs["k0"] <= BF16_BOUNDS["k0"]
@@ -283,14 +305,15 @@ def test_coarse_eikonal_bench_batch_vs_fp64_oracle(cuda, precision, rgb_tol, los
 
     def run_oracle(dtype):
         orc = OracleCoarse(model, dtype=dtype)
-        o = orc(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, device_keep=keep, **rk)
+        o = orc(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, device_keep=keep, tie_rel=1e-4, **rk)
         o_eik = ((o["gradient"].norm(dim=-1) - 1.0) ** 2).mean()
         ol = train_loss(o, torch.from_numpy(tgt).to(dtype), weight_rgb0=0) + 0.1 * o_eik
         ol.backward()
         # threshold ties (FP32 vs FP64 decide a weight within rounding of
         # fast_color_thres differently): a few per thousand rays at most
         assert orc.ties <= max(4, n // 256), orc.ties
-        assert set(zip(o["ray_id"].tolist(), o["step_id"].tolist())) == keep
+        got = set(zip(o["ray_id"].tolist(), o["step_id"].tolist()))
+        assert got == keep, (sorted(got - keep)[:8], sorted(keep - got)[:8])
         grads = {"sdf": orc.sdf_grid.grad, "k0": orc.k0_grid.grad}
         for nm, q in orc.rgbnet.named_parameters():
             grads["rgbnet." + nm] = q.grad
