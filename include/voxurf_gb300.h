@@ -477,7 +477,8 @@ typedef struct {
   const float* k0_f32;
   const void* k0_bf16;
   vx_coarse_feature_cfg cfg;
-  int64_t ld;
+  int64_t ld;               /* row stride of X, >= the feature count; columns
+                               beyond the features are written as zero       */
   void* X;
   int32_t out_bf16;
   float* normal_out;        /* optional [S2,3] interpolated gradient            */
@@ -587,6 +588,177 @@ typedef struct {
  * 2^-16).  One persistent CTA per SM holds all weights in shared memory. */
 int vx_mlp_tc_forward(const vx_mlp_tc_args* args, void* stream);
 
+/* ---- colour-MLP training on the tensor cores (tcgen05, BF16 operands, FP32
+ *      accumulation): forward + backward of the rgbnet / k_rgbnet stacks
+ *      (lib/voxurf_fine.py:132-187, applied at :718-752) and of the coarse
+ *      rgbnet (lib/voxurf_coarse.py:116-123, applied at :571-573), i.e. what
+ *      torch autograd runs for nn.Linear/ReLU in the reference.  Hidden width
+ *      32, 64, 128 or 192; 2 or 3 hidden layers; first-layer K0 a multiple of
+ *      16 up to 80; a 3-wide output layer.  Intermediate tensors are "T-tiles"
+ *      (128-row tiles of a [rows, C] BF16 matrix as 8x8 core matrices,
+ *      element (r, c) of tile t at t*128*C + ((r/8)*(C/8) + c/8)*64 + (r%8)*8
+ *      + c%8); rows_cap (a multiple of 128 >= n_rows) sizes them. ---- */
+
+/* One operand-preparation job of vx_mlp_train_pack.  mode 0: BF16 [Kp/8][Np][8]
+ * of B[n][k] = src[n*ld + k] (transpose 0) or src[k*ld + n] (transpose 1),
+ * zero beyond N x K; mode 1: the 3-row output layer as BF16 hi rows 0-2 and
+ * lo rows 3-5 (hi + lo = the FP32 weight to 2^-16), [Kp/8][Np][8]; mode 2:
+ * FP32 copy of the [N, K] matrix into dst contiguous; mode 3: FP32 [Kp][Np]
+ * of Bt[k][n] = src[n*ld + k] (transpose 1) or src[k*ld + n] (transpose 0),
+ * zero beyond N x K. */
+typedef struct {
+  const float* src;
+  int64_t ld, N, K, Np, Kp;
+  int32_t transpose, mode;
+  void* dst;
+} vx_mlp_pack_job;
+
+/* Up to 32 jobs in one launch (the per-step operand refresh of both MLPs). */
+int vx_mlp_train_pack(const vx_mlp_pack_job* jobs, int n_jobs, void* stream);
+
+typedef struct {
+  int64_t n_rows;            /* rows of X                                          */
+  const int64_t* n_rows_dev; /* optional device row count <= n_rows (graph replay) */
+  int64_t rows_cap;          /* row capacity of H / relu (multiple of 128)         */
+  int64_t width, n_hidden, K0;
+  const void* X;             /* BF16 [n_rows, ldx], 16-byte aligned rows            */
+  int64_t ldx;
+  const void* W0p;           /* pack mode 0 of W_0 [width, K]: N = width, Kp = K0   */
+  const void* Wp;            /* hidden W_1..W_{L-1}: pack mode 0, N = Kp = width    */
+  const float* bias;         /* [n_hidden][width] FP32 (pack mode 2)                */
+  const void* Whp;           /* output layer: pack mode 1, Np = 16, Kp = width      */
+  const float* bh;           /* [3]                                                 */
+  float* out;                /* [n_rows, 3] logits                                  */
+  void* cols;                /* optional BF16 copy of the logits: cols[row*ld_cols]  */
+  int64_t ld_cols;
+  void* H;                   /* T-tiles of h_1..h_L, each rows_cap*width BF16; null
+                                for inference                                       */
+  void* relu;                /* ReLU bits [L][rows_cap][width/16] uint16; null with H */
+} vx_mlp_train_fwd_args;
+
+/* Forward: logits = MLP(X); with H/relu set, keeps what the backward needs. */
+int vx_mlp_train_forward(const vx_mlp_train_fwd_args* args, void* stream);
+
+typedef struct {
+  int64_t n_rows;
+  const int64_t* n_rows_dev;
+  int64_t rows_cap, width, n_hidden, K0;
+  const float* dY;           /* [n_rows, 3] gradient of the logits                  */
+  const float* Wh;           /* [3, width] output-layer weights (FP32)              */
+  const void* relu;          /* from the forward                                    */
+  const void* WTp;           /* hidden W_1..W_{L-1} transposed: pack mode 0 with
+                                transpose 1, N = Kp = width                          */
+  const void* W0Tp;          /* W_0 [width, K] transposed: pack mode 0, transpose 1,
+                                N = Np = K0 (zero beyond K), K = Kp = width          */
+  void* dZ;                  /* out: T-tiles of dz_1..dz_L, each rows_cap*width     */
+  void* dYT;                 /* out: T-tiles (width 16) of dy as BF16 hi, lo        */
+  void* dX;                  /* out: [n_rows, ld_dx] input gradient, columns < K0   */
+  int64_t ld_dx;
+  int32_t dx_bf16;
+  float* dbh_part;           /* out: [grid][4] per-CTA column sums of dy            */
+  int64_t dbh_part_cap;      /* rows of dbh_part (>= vx_mlp_wgrad_grid(n_rows))     */
+} vx_mlp_train_bwd_args;
+
+/* Backward, input-gradient chain (dz of every hidden layer, dX). */
+int vx_mlp_train_backward(const vx_mlp_train_bwd_args* args, void* stream);
+
+/* CTAs (= partials) of vx_mlp_train_wgrad and vx_mlp_train_backward for n_rows. */
+size_t vx_mlp_wgrad_grid(int64_t n_rows);
+
+typedef struct {
+  int64_t n_rows;
+  const int64_t* n_rows_dev;
+  const void* A;             /* T-tiles of width WA (the M side)                     */
+  int64_t WA;                /* multiple of 16, <= 256                               */
+  const void* B;             /* T-tiles of width WB, or BF16 rows [n_rows, ldb]      */
+  int64_t WB, ldb;           /* WB multiple of 16, <= 240                            */
+  int32_t b_rows;            /* 1: B is rows                                         */
+  int32_t ones;              /* 1: 16 more partial columns, column WB = sum_rows A   */
+  float* part;               /* out: [grid][WA][WB + 16 ones] FP32 partials          */
+  int64_t part_cap;          /* floats available at part                            */
+} vx_mlp_wgrad_args;
+
+/* part[cta][m][n] = sum over the CTA's rows of A[row][m] * B[row][n]. */
+int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* args, void* stream);
+
+/* One ordered sum of vx_mlp_train_wgrad partials.  kind 0: w[m][n] = sum
+ * part[.][m][n] for n < n_out (ld n_out), b[m] = sum part[.][m][WB]; kind 1
+ * (output layer, A = h_L, B = dYT): w[c][m] = sum part[.][m][c] +
+ * part[.][m][c + 3] for c < 3, b[c] = sum bh_part[.][c]. */
+typedef struct {
+  const float* part;
+  int64_t n_part, WA, NC;
+  int32_t kind, reserved;
+  int64_t WB, n_out;
+  float* w;
+  float* b;
+  const float* bh_part;
+  int64_t n_bh;
+} vx_mlp_reduce_job;
+
+/* Up to 8 jobs in one launch. */
+int vx_mlp_train_reduce(const vx_mlp_reduce_job* jobs, int n_jobs, void* stream);
+
+/* ---- colour-MLP training in plain FP32 on the CUDA cores (the same layers
+ *      as above with FP32 operands and FP32 fused multiply-adds; the output
+ *      layer runs in vx_mlp_head / vx_mlp_head_backward).  Weights enter as
+ *      Bt [Kp][Np] FP32 (vx_mlp_train_pack mode 3), Np in {32, 64, 80, 128,
+ *      192}. ---- */
+typedef struct {
+  int64_t M;                 /* rows                                                */
+  const int64_t* m_dev;      /* optional device row count <= M                      */
+  int64_t K;                 /* inner dimension (columns of A used)                 */
+  const float* A;            /* [M, lda]                                            */
+  int64_t lda;
+  const float* Bt;           /* [round_up(K,16)][Np], zero rows beyond K            */
+  int64_t Np;
+  int32_t mode;              /* 0: C = relu(A Bt + bias)   (hidden layer, forward)
+                                1: C = (A Bt) * [H > 0], colsum[cta][n] = column sums
+                                   of C over the CTA's rows (hidden layer, backward)
+                                2: C = A Bt               (input gradient)          */
+  int32_t reserved;
+  const float* bias;         /* mode 0: [Np]                                        */
+  const float* H;            /* mode 1: [M, ldh] the layer's post-ReLU activation   */
+  int64_t ldh;
+  float* C;                  /* [M, ldc], columns < n_store                         */
+  int64_t ldc, n_store;
+  float* colsum;             /* mode 1: [vx_mlp_f32_rowgemm_grid(M)][Np]            */
+  int64_t colsum_cap;        /* floats available at colsum                          */
+} vx_mlp_f32_rowgemm_args;
+
+size_t vx_mlp_f32_rowgemm_grid(int64_t M);
+/* C = A Bt with the epilogue of `mode` (lib/voxurf_fine.py:132-151 forward,
+ * and its autograd backward). */
+int vx_mlp_f32_rowgemm(const vx_mlp_f32_rowgemm_args* args, void* stream);
+
+typedef struct {
+  int64_t rows;
+  const int64_t* rows_dev;
+  const float* A;            /* [rows, lda], columns < M (dz of the layer's output) */
+  int64_t lda;
+  const float* B;            /* [rows, ldb], columns < N (the layer's input)        */
+  int64_t ldb;
+  int64_t M, N;              /* each <= 192                                         */
+  float* part;               /* out: [grid][MP][NP] (MP, NP = M, N padded up to 32, 64,
+                                80, 128 or 192)                                      */
+  int64_t part_cap;
+} vx_mlp_f32_wgrad_args;
+
+size_t vx_mlp_f32_wgrad_grid(int64_t rows);
+/* part[cta][m][n] = sum over the CTA's rows of A[r][m] B[r][n] (dW = dz^T h). */
+int vx_mlp_f32_wgrad(const vx_mlp_f32_wgrad_args* args, void* stream);
+
+/* out[m*out_ld + n] = sum_k part[k*part_stride + m*part_ld + n], k in order. */
+typedef struct {
+  const float* part;
+  int64_t n_part, part_stride, part_ld, rows, cols;
+  float* out;
+  int64_t out_ld;
+} vx_mlp_sum_job;
+
+/* Up to 16 jobs in one launch. */
+int vx_mlp_f32_reduce(const vx_mlp_sum_job* jobs, int n_jobs, void* stream);
+
 /* ---- render server: the inference form of Voxurf.forward (global_step =
  *      None, lib/voxurf_fine.py:620-802) for rays of several resident scenes
  *      in one launch per stage.  The reference renders one scene per process,
@@ -688,17 +860,6 @@ int vx_serve_composite(const vx_scene_desc* scenes_host, int32_t n_scenes, const
                        int64_t max_steps, const void* rec, const int64_t* s2_off, const float* logit,
                        const float* klogit, const float* alphainv_last, const int64_t* ray_out, float* out_rgb,
                        float* out_depth, void* stream);
-
-/* FP32 GEMM of the colour-MLP backward (the weight and input gradients that
- * autograd forms for voxurf_fine.py:132-187's nn.Linear layers): cuBLAS
- * SGEMM, column-major, C = alpha op(A) op(B) + beta C, on `stream`, with the
- * caller's workspace (may be NULL: cuBLAS's own).  emulate = 1 selects
- * cuBLAS's BF16x9 FP32 emulation on the tensor cores.  Uses one cuBLAS
- * handle per device, created on first use (cublasCreate allocates its own
- * small state: the one device allocation this library makes). */
-int vx_gemm_f32(int transa, int transb, int64_t m, int64_t n, int64_t k, float alpha, const float* A, int64_t lda,
-                const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int emulate, void* workspace,
-                size_t workspace_bytes, void* stream);
 
 /* Per-step FP32 -> BF16 casts of the colour-MLP weights and biases of the
  * mixed-precision step (the reference keeps FP32 parameters; the BF16

@@ -107,6 +107,11 @@ def fine256(cuda):
     torch.cuda.empty_cache()
     train_loss(orc32(ro, rd, vd, global_step=1, **RK), tgt).backward()
     ref32 = {k: _rel_l2(v, grads[k]) for k, v in _oracle_grads(orc32).items()}
+    tv_add_grad(orc32.sdf_grid, 1e-4 / SUB, world_max, True)
+    tv_add_grad(orc32.k0_grid, 1e-4 / SUB, world_max, True)
+    UtilsAdam([([orc32.sdf_grid], 1e-3), ([orc32.k0_grid], 1e-3), (list(orc32.rgbnet.parameters()), 1e-3),
+               (list(orc32.k_rgbnet.parameters()), 1e-3)], betas=(0.9, 0.99)).step()
+    after32 = _params(orc32.sdf_grid, orc32.k0_grid, orc32.rgbnet, orc32.k_rgbnet)
     del orc32
     tv_add_grad(orc.sdf_grid, 1e-4 / SUB, world_max, True)
     tv_add_grad(orc.k0_grid, 1e-4 / SUB, world_max, True)
@@ -115,8 +120,14 @@ def fine256(cuda):
     opt.step()
     after = _params(orc.sdf_grid, orc.k0_grid, orc.rgbnet, orc.k_rgbnet)
     delta = {k: after[k] - before[k] for k in before}
+    # the reference algorithm's own FP32 update error, measured like the GPU's
+    # (against the FP64 update rounded to FP32 storage)
+    ref32_update = {k: _rel_l2(after32[k] - before[k], (before[k] + delta[k]).float().double() - before[k])
+                    for k in before}
+    del after32
     out = {"rays": rays, "full": full, "ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in ret.items()},
-           "loss": float(loss.item()), "grads": grads, "ref32": ref32, "before": before, "delta": delta}
+           "loss": float(loss.item()), "grads": grads, "ref32": ref32, "ref32_update": ref32_update,
+           "before": before, "delta": delta}
     del orc, opt, after
     return out
 
@@ -153,11 +164,13 @@ def test_fine256_fp32_step_matches_fp64_oracle(cuda, fine256):
     # rounded to the FP32 storage both sides keep them in (otherwise one ulp
     # of a parameter near 1, 6e-8, would count against a 1e-3 Adam step)
     after = _params(model.sdf.grid, model.k0.grid, model.rgbnet, model.k_rgbnet)
+    uerr = {}
     for name, ref in fine256["delta"].items():
         p0 = fine256["before"][name]
-        ref32 = (p0 + ref).float().double() - p0
-        err = _rel_l2(after[name] - p0, ref32)
-        assert err <= max(1e-5, 3 * fine256["ref32"][name]), ("update", name, err)
+        uerr[name] = _rel_l2(after[name] - p0, (p0 + ref).float().double() - p0)
+    print("fp32 update vs FP64:", uerr, "reference fp32:", fine256["ref32_update"])
+    for name, err in uerr.items():
+        assert err <= max(1e-5, 3 * fine256["ref32_update"][name]), ("update", name, err)
 
 
 # Bounds of the BF16 graph-replayed step against FP64 on this batch, about
@@ -305,12 +318,14 @@ def test_coarse_eikonal_bench_batch_vs_fp64_oracle(cuda, precision, rgb_tol, los
 
     def run_oracle(dtype):
         orc = OracleCoarse(model, dtype=dtype)
-        o = orc(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, device_keep=keep, tie_rel=1e-4, **rk)
+        o = orc(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, device_keep=keep, tie_rel=1e-3, **rk)
         o_eik = ((o["gradient"].norm(dim=-1) - 1.0) ** 2).mean()
         ol = train_loss(o, torch.from_numpy(tgt).to(dtype), weight_rgb0=0) + 0.1 * o_eik
         ol.backward()
-        # threshold ties (FP32 vs FP64 decide a weight within rounding of
-        # fast_color_thres differently): a few per thousand rays at most
+        # threshold ties: FP32 and FP64 decide a weight within 1e-3 (relative)
+        # of fast_color_thres differently (behind a nearly opaque sample FP32
+        # keeps 1 - alpha only to ~1e-4, so T does too); a few per thousand
+        # rays at most
         assert orc.ties <= max(4, n // 256), orc.ties
         got = set(zip(o["ray_id"].tolist(), o["step_id"].tolist()))
         assert got == keep, (sorted(got - keep)[:8], sorted(keep - got)[:8])

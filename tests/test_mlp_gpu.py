@@ -1,5 +1,6 @@
-"""Colour-MLP forward/backward (cuBLAS GEMMs + fused ReLU-backward/bias-grad
-kernel) against plain torch autograd of the reference nn.Sequential."""
+"""Colour-MLP forward/backward through apply_mlp (the FP32 CUDA-core engine
+for FP32 rows, the tcgen05 engine for BF16 rows) against plain torch autograd
+of the reference nn.Sequential (FP64) and torch's BF16 autocast."""
 import pytest
 import torch
 import torch.nn as nn
@@ -56,30 +57,3 @@ def test_mlp_bf16_matches_torch_autocast(cuda):
     for p, r in zip(net.parameters(), g_ref):
         assert p.grad.dtype == torch.float32
         assert float((p.grad - r).norm() / r.norm()) < 3e-2
-
-
-@pytest.mark.parametrize("emulate", [0, 1])
-@pytest.mark.parametrize("ta,tb,m,n,k", [(0, 1, 70, 192, 3001), (0, 0, 192, 1037, 192), (0, 1, 16, 8, 0),
-                                         (1, 0, 33, 65, 129)])
-def test_gemm_f32_matches_fp64(cuda, emulate, ta, tb, m, n, k):
-    """vx_gemm_f32 (column-major C = op(A) op(B)) against an FP64 product;
-    the BF16x9 emulation is held to the same FP32 bound."""
-    from voxurf_gb300._torch import call, ptr, stream_ptr
-
-    g = torch.Generator(device=cuda).manual_seed(m * 7 + n + k)
-    # column-major storage = row-major tensors of the transposed shapes
-    A = torch.randn((m, k) if ta else (k, m), device=cuda, generator=g)   # op(A) is m x k
-    B = torch.randn((k, n) if tb else (n, k), device=cuda, generator=g)   # op(B) is k x n
-    C = torch.full((n, m), float("nan"), device=cuda)
-    lda, ldb = A.shape[1], B.shape[1]
-    call("vx_gemm_f32", ta, tb, m, n, k, 1.0, ptr(A) if k else None, lda, ptr(B) if k else None, ldb, 0.0, ptr(C),
-         m, emulate, None, 0, stream_ptr())
-    torch.cuda.synchronize()
-    opA = (A.double() if ta else A.double().t())          # m x k
-    opB = (B.double() if tb else B.double().t())          # k x n
-    want = (opA @ opB).t()                                  # stored column-major = [n, m] row-major
-    if k == 0:
-        assert torch.equal(C, torch.zeros_like(C))
-    else:
-        err = float((C.double() - want).abs().max() / want.abs().max())
-        assert err < 1e-6, err

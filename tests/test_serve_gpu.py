@@ -110,7 +110,7 @@ def test_same_alone_and_in_mix(cuda):
 
 def test_tensor_core_mlp_path_matches_oracle(cuda):
     """192-wide BF16 scenes shade through the fused tcgen05 MLP: same result
-    as the per-layer GEMM path and within the BF16 bound of the oracle."""
+    as the per-layer MLP engines and within the BF16 bound of the oracle."""
     models = configs.build_serve_models(32, "bf16", device=cuda, n=2, mask_voxels=3.0, width=192)
     for m in models:
         m.s_val = torch.ones(1) * S_VAL
@@ -118,12 +118,12 @@ def test_tensor_core_mlp_path_matches_oracle(cuda):
     assert all(s.tc is not None for s in scenes)
     views = [(0, _pose(50), 24, 32), (1, _pose(51), 20, 20)]
     res = {}
-    for mlp in ("tc", "gemm"):
+    for mlp in ("tc", "layers"):
         srv = serve.RenderServer(scenes, tick_rays=600, arena_pixels=1 << 16, mlp=mlp)
         reqs = [srv.submit(*v) for v in views]
         srv.run_until_idle()
         res[mlp] = [r.rgb for r in reqs]
-    for (s, c2w, H, W), a, b in zip(views, res["tc"], res["gemm"]):
+    for (s, c2w, H, W), a, b in zip(views, res["tc"], res["layers"]):
         assert np.abs(a - b).max() <= 1e-3
         rgb, _ = _oracle_view(models[s], c2w, H, W)
         assert np.abs(a - rgb).max() <= 1e-3

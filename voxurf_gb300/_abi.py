@@ -140,6 +140,61 @@ class MlpTcArgs(C.Structure):
     ]
 
 
+class MlpPackJob(C.Structure):
+    _fields_ = [("src", P), ("ld", I64), ("N", I64), ("K", I64), ("Np", I64), ("Kp", I64), ("transpose", I32),
+                ("mode", I32), ("dst", P)]
+
+
+class MlpTrainFwdArgs(C.Structure):
+    _fields_ = [
+        ("n_rows", I64), ("n_rows_dev", P), ("rows_cap", I64), ("width", I64), ("n_hidden", I64), ("K0", I64),
+        ("X", P), ("ldx", I64), ("W0p", P), ("Wp", P), ("bias", P), ("Whp", P), ("bh", P), ("out", P),
+        ("cols", P), ("ld_cols", I64), ("H", P), ("relu", P),
+    ]
+
+
+class MlpTrainBwdArgs(C.Structure):
+    _fields_ = [
+        ("n_rows", I64), ("n_rows_dev", P), ("rows_cap", I64), ("width", I64), ("n_hidden", I64), ("K0", I64),
+        ("dY", P), ("Wh", P), ("relu", P), ("WTp", P), ("W0Tp", P), ("dZ", P), ("dYT", P), ("dX", P),
+        ("ld_dx", I64), ("dx_bf16", I32), ("dbh_part", P), ("dbh_part_cap", I64),
+    ]
+
+
+class MlpWgradArgs(C.Structure):
+    _fields_ = [
+        ("n_rows", I64), ("n_rows_dev", P), ("A", P), ("WA", I64), ("B", P), ("WB", I64), ("ldb", I64),
+        ("b_rows", I32), ("ones", I32), ("part", P), ("part_cap", I64),
+    ]
+
+
+class MlpReduceJob(C.Structure):
+    _fields_ = [
+        ("part", P), ("n_part", I64), ("WA", I64), ("NC", I64), ("kind", I32), ("reserved", I32), ("WB", I64),
+        ("n_out", I64), ("w", P), ("b", P), ("bh_part", P), ("n_bh", I64),
+    ]
+
+
+class MlpF32RowGemmArgs(C.Structure):
+    _fields_ = [
+        ("M", I64), ("m_dev", P), ("K", I64), ("A", P), ("lda", I64), ("Bt", P), ("Np", I64), ("mode", I32),
+        ("reserved", I32), ("bias", P), ("H", P), ("ldh", I64), ("C", P), ("ldc", I64), ("n_store", I64),
+        ("colsum", P), ("colsum_cap", I64),
+    ]
+
+
+class MlpF32WgradArgs(C.Structure):
+    _fields_ = [
+        ("rows", I64), ("rows_dev", P), ("A", P), ("lda", I64), ("B", P), ("ldb", I64), ("M", I64), ("N", I64),
+        ("part", P), ("part_cap", I64),
+    ]
+
+
+class MlpSumJob(C.Structure):
+    _fields_ = [("part", P), ("n_part", I64), ("part_stride", I64), ("part_ld", I64), ("rows", I64), ("cols", I64),
+                ("out", P), ("out_ld", I64)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [
         ("grid", GridGeom), ("sdf_smooth", P), ("k0", P), ("k0_bf16", I32), ("voxel_size", F), ("mask", P),
@@ -171,6 +226,11 @@ _STRUCT_FNS = {
     "vx_fine_composite_backward": FineCompositeBwdArgs,
     "vx_fine_backward": FineBackwardArgs,
     "vx_mlp_tc_forward": MlpTcArgs,
+    "vx_mlp_train_forward": MlpTrainFwdArgs,
+    "vx_mlp_train_backward": MlpTrainBwdArgs,
+    "vx_mlp_train_wgrad": MlpWgradArgs,
+    "vx_mlp_f32_rowgemm": MlpF32RowGemmArgs,
+    "vx_mlp_f32_wgrad": MlpF32WgradArgs,
 }
 
 _SERVE_SIGNATURES = {
@@ -211,6 +271,18 @@ def _declare():
     lib.vx_hit_coarse_geo.restype = C.c_int
     lib.vx_cast_rows_bf16.argtypes = [C.POINTER(CastJob), I32, P]
     lib.vx_cast_rows_bf16.restype = C.c_int
+    lib.vx_mlp_train_pack.argtypes = [C.POINTER(MlpPackJob), C.c_int, P]
+    lib.vx_mlp_train_pack.restype = C.c_int
+    lib.vx_mlp_train_reduce.argtypes = [C.POINTER(MlpReduceJob), C.c_int, P]
+    lib.vx_mlp_train_reduce.restype = C.c_int
+    lib.vx_mlp_wgrad_grid.argtypes = [I64]
+    lib.vx_mlp_wgrad_grid.restype = C.c_size_t
+    lib.vx_mlp_f32_rowgemm_grid.argtypes = [I64]
+    lib.vx_mlp_f32_rowgemm_grid.restype = C.c_size_t
+    lib.vx_mlp_f32_wgrad_grid.argtypes = [I64]
+    lib.vx_mlp_f32_wgrad_grid.restype = C.c_size_t
+    lib.vx_mlp_f32_reduce.argtypes = [C.POINTER(MlpSumJob), C.c_int, P]
+    lib.vx_mlp_f32_reduce.restype = C.c_int
     lib.vx_bg_samples_count.argtypes = [C.POINTER(BgSampleArgs), P, P, P, C.c_size_t, P]
     lib.vx_bg_samples_count.restype = C.c_int
     lib.vx_bg_samples_fill.argtypes = [C.POINTER(BgSampleArgs), P, I64, P, P, P, P, P]
@@ -254,4 +326,6 @@ def struct_names() -> list[str]:
                                 "vx_sdf_gradient_grid", "vx_sdf_gradient_grid_adjoint",
                                 "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv",
                                 "vx_sdf_field", "vx_density_mask", "vx_hit_coarse_geo", "vx_bg_samples_count",
-                                "vx_bg_samples_fill", "vx_cast_rows_bf16"] + list(_SERVE_SIGNATURES)
+                                "vx_bg_samples_fill", "vx_cast_rows_bf16", "vx_mlp_train_pack",
+                                "vx_mlp_train_reduce", "vx_mlp_wgrad_grid", "vx_mlp_f32_rowgemm_grid",
+                                "vx_mlp_f32_wgrad_grid", "vx_mlp_f32_reduce"] + list(_SERVE_SIGNATURES)

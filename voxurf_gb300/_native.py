@@ -70,8 +70,6 @@ _SIGNATURES = {
                                      c_ptr],
     "vx_grid_clear_touched": [c_ptr, c_ptr, c_i64, c_i64, c_ptr],
     "vx_cumdist_thres": [c_ptr, c_i64, c_i64, c_f32, c_ptr, c_ptr],
-    "vx_gemm_f32": [c_int, c_int, c_i64, c_i64, c_i64, c_f32, c_ptr, c_i64, c_ptr, c_i64, c_f32, c_ptr, c_i64,
-                    c_int, c_ptr, c_size, c_ptr],
 }
 
 _RESTYPES = {

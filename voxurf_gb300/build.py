@@ -85,7 +85,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None, e
             if verbose and log.strip():
                 print(f"[{os.path.basename(futs[f])}]\n{log}", file=sys.stderr)
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-Xcompiler", "-fPIC", *sorted(objs), "-lcublas", "-o", tmp]
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-Xcompiler", "-fPIC", *sorted(objs), "-o", tmp]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")

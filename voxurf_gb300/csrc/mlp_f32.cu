@@ -1,0 +1,363 @@
+// Colour-MLP training in plain FP32 on the CUDA cores: the hidden layers of
+// rgbnet / k_rgbnet (lib/voxurf_fine.py:132-187) and of the coarse rgbnet
+// (lib/voxurf_coarse.py:116-123), forward and backward, with FP32 operands
+// and FP32 fused multiply-adds (the arithmetic of the reference's FP32
+// nn.Linear under autograd).  The 3-wide output layer has kernels of its own
+// (vx_mlp_head, vx_mlp_head_backward in mlp_ops.cu).
+//
+//   rowgemm_kernel   C[m][n] = sum_k A[m][k] Bt[k][n] over a 64-row tile and
+//                    all N columns (N = 16 TN), with one of three epilogues:
+//                    +bias and ReLU (forward), times the ReLU mask of the
+//                    layer's activation plus per-CTA column sums (backward,
+//                    hidden layer), none (backward, input gradient).  Bt is
+//                    the layer's weight, transposed or not, zero-padded to
+//                    [Kp][Np] by vx_mlp_train_pack (mode 3).
+//   wgrad_kernel     D[m][n] = sum over a CTA's rows of A[r][m] B[r][n] (the
+//                    weight gradient dz^T h, summed over rows), one FP32
+//                    partial per CTA; vx_mlp_f32_reduce sums the partials in a
+//                    fixed order.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace vx {
+namespace mf {
+
+constexpr int BM = 64;       // rows per rowgemm tile
+constexpr int KC = 16;       // K per shared-memory stage
+constexpr int THREADS = 256; // 16 x 16 threads
+
+struct RowGemmParams {
+  const float* A;            // [M, lda]
+  int64_t lda;
+  int64_t M;
+  const int64_t* m_dev;      // optional device row count (<= M)
+  int K;                     // columns of A used
+  const float* Bt;           // [Kp][Np] (Kp = round_up(K, 16), zero rows beyond K)
+  int Np;
+  int mode;                  // 0: relu(acc + bias); 1: acc * [H > 0] + column sums; 2: acc
+  const float* bias;         // mode 0: [Np]
+  const float* H;            // mode 1: [M, ldh] post-ReLU activation of the layer
+  int64_t ldh;
+  float* C;                  // [M, ldc], columns < n_store
+  int64_t ldc;
+  int n_store;
+  float* colsum;             // mode 1: [gridDim.x][Np] per-CTA column sums
+};
+
+__device__ __forceinline__ int64_t rows_of(int64_t n, const int64_t* n_dev) {
+  if (n_dev) {
+    const int64_t d = *n_dev;
+    if (d < n) n = d < 0 ? 0 : d;
+  }
+  return n;
+}
+
+template <int TN>
+__global__ void __launch_bounds__(THREADS) rowgemm_kernel(RowGemmParams P) {
+  constexpr int NP = 16 * TN;
+  __shared__ __align__(16) float As[2][KC][BM];
+  __shared__ __align__(16) float Bs[2][KC][NP];
+  __shared__ float red[16][NP];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t M = rows_of(P.M, P.m_dev);
+  const int64_t m0 = (int64_t)blockIdx.x * BM;
+  if (m0 >= M && P.mode != 1) return;
+  const int nk = (P.K + KC - 1) / KC;
+  // A tile loader: row am, k columns [4 aq, 4 aq + 4) of the stage
+  const int am = tid & 63, aq = tid >> 6;
+  const int64_t arow = m0 + am;
+  const bool arow_ok = arow < M;
+  const float* Arow = P.A + (arow_ok ? arow : 0) * P.lda;
+  const bool avec = (P.lda & 3) == 0 && (reinterpret_cast<uintptr_t>(P.A) & 15) == 0;
+
+  auto load_a = [&](int kt, float (&r)[4]) {
+    const int k = kt * KC + 4 * aq;
+    if (arow_ok && avec && k + 4 <= P.K) {
+      const float4 v = *reinterpret_cast<const float4*>(Arow + k);
+      r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) r[i] = (arow_ok && k + i < P.K) ? Arow[k + i] : 0.f;
+    }
+  };
+  auto store_a = [&](int s, const float (&r)[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) As[s][4 * aq + i][am] = r[i];
+  };
+  // B stage: KC x NP floats, contiguous in Bt
+  auto load_b = [&](int kt, int s) {
+    const float4* src = reinterpret_cast<const float4*>(P.Bt + (int64_t)kt * KC * NP);
+    float4* dst = reinterpret_cast<float4*>(&Bs[s][0][0]);
+    for (int i = tid; i < KC * NP / 4; i += THREADS) dst[i] = src[i];
+  };
+
+  float acc[4][TN];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+
+  float ra[4];
+  load_a(0, ra);
+  store_a(0, ra);
+  load_b(0, 0);
+  __syncthreads();
+  for (int kt = 0; kt < nk; ++kt) {
+    const int s = kt & 1;
+    if (kt + 1 < nk) {
+      load_a(kt + 1, ra);
+      load_b(kt + 1, s ^ 1);
+    }
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      const float4 a4 = *reinterpret_cast<const float4*>(&As[s][k][4 * ty]);
+      const float a[4] = {a4.x, a4.y, a4.z, a4.w};
+      float b[TN];
+      if constexpr (TN % 4 == 0) {
+#pragma unroll
+        for (int j = 0; j < TN / 4; ++j) {
+          const float4 b4 = *reinterpret_cast<const float4*>(&Bs[s][k][TN * tx + 4 * j]);
+          b[4 * j] = b4.x; b[4 * j + 1] = b4.y; b[4 * j + 2] = b4.z; b[4 * j + 3] = b4.w;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < TN; ++j) b[j] = Bs[s][k][TN * tx + j];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    if (kt + 1 < nk) store_a(s ^ 1, ra);
+    __syncthreads();
+  }
+  // epilogue
+  float cs[TN];
+#pragma unroll
+  for (int j = 0; j < TN; ++j) cs[j] = 0.f;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t m = m0 + 4 * ty + i;
+    if (m >= M) continue;
+    float* crow = P.C + m * P.ldc;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int n = TN * tx + j;
+      float v = acc[i][j];
+      if (P.mode == 0) {
+        v = fmaxf(v + P.bias[n], 0.f);
+      } else if (P.mode == 1) {
+        v = P.H[m * P.ldh + n] > 0.f ? v : 0.f;
+        cs[j] += v;
+      }
+      if (n < P.n_store) crow[n] = v;
+    }
+  }
+  if (P.mode == 1) {
+#pragma unroll
+    for (int j = 0; j < TN; ++j) red[ty][TN * tx + j] = cs[j];
+    __syncthreads();
+    for (int n = tid; n < NP; n += THREADS) {
+      float s = 0.f;
+      for (int r = 0; r < 16; ++r) s += red[r][n];
+      P.colsum[(int64_t)blockIdx.x * NP + n] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct WgradParams {
+  const float* A;            // [rows, lda] (dz of the layer's output), columns < M
+  int64_t lda;
+  const float* B;            // [rows, ldb] (the layer's input), columns < N
+  int64_t ldb;
+  int M, N;                  // N <= 16 TN, M <= 16 TM
+  int64_t rows;
+  const int64_t* rows_dev;
+  float* part;               // [gridDim.x][16 TM][16 TN]
+};
+
+constexpr int WG_KC = 16;    // rows per stage
+
+template <int TM, int TN>
+__global__ void __launch_bounds__(THREADS, 1) wgrad_kernel(WgradParams P) {
+  constexpr int MP = 16 * TM, NP = 16 * TN;
+  __shared__ __align__(16) float As[2][WG_KC][MP];
+  __shared__ __align__(16) float Bs[2][WG_KC][NP];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t rows = rows_of(P.rows, P.rows_dev);
+  // this CTA's rows: a contiguous range, in stages of WG_KC
+  const int64_t per = (rows + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = std::min<int64_t>(rows, (int64_t)blockIdx.x * per);
+  const int64_t r1 = std::min<int64_t>(rows, r0 + per);
+  const int nst = (int)((r1 - r0 + WG_KC - 1) / WG_KC);
+
+  auto load = [&](int st, int s) {
+    const int64_t rb = r0 + (int64_t)st * WG_KC;
+    for (int i = tid; i < WG_KC * MP; i += THREADS) {
+      const int rr = i / MP, c = i % MP;
+      const int64_t r = rb + rr;
+      As[s][rr][c] = (r < r1 && c < P.M) ? P.A[r * P.lda + c] : 0.f;
+    }
+    for (int i = tid; i < WG_KC * NP; i += THREADS) {
+      const int rr = i / NP, c = i % NP;
+      const int64_t r = rb + rr;
+      Bs[s][rr][c] = (r < r1 && c < P.N) ? P.B[r * P.ldb + c] : 0.f;
+    }
+  };
+
+  float acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+  if (nst > 0) load(0, 0);
+  __syncthreads();
+  for (int st = 0; st < nst; ++st) {
+    const int s = st & 1;
+    if (st + 1 < nst) load(st + 1, s ^ 1);
+#pragma unroll 4
+    for (int k = 0; k < WG_KC; ++k) {
+      float a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[s][k][TM * ty + i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[s][k][TN * tx + j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  float* part = P.part + (size_t)blockIdx.x * MP * NP;
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) part[(TM * ty + i) * NP + TN * tx + j] = acc[i][j];
+}
+
+struct SumJob {
+  const float* part;         // [n_part][part_stride], element (m, n) at m * part_ld + n
+  int64_t n_part, part_stride, part_ld;
+  int64_t rows, cols;
+  float* out;                // out[m * out_ld + n]
+  int64_t out_ld;
+};
+constexpr int MAX_SUM_JOBS = 16;
+struct SumJobs {
+  SumJob j[MAX_SUM_JOBS];
+  int n;
+};
+
+__global__ void sum_partials_kernel(SumJobs J) {
+  const SumJob& S = J.j[blockIdx.y];
+  const int64_t total = S.rows * S.cols;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = i / S.cols, n = i % S.cols;
+    const float* p = S.part + m * S.part_ld + n;
+    float s = 0.f;
+    for (int64_t k = 0; k < S.n_part; ++k) s += p[k * S.part_stride];
+    S.out[m * S.out_ld + n] = s;
+  }
+}
+
+}  // namespace mf
+}  // namespace vx
+
+using namespace vx;
+using namespace vx::mf;
+
+extern "C" {
+
+size_t vx_mlp_f32_rowgemm_grid(int64_t M) { return (size_t)std::max<int64_t>(1, (M + BM - 1) / BM); }
+
+int vx_mlp_f32_rowgemm(const vx_mlp_f32_rowgemm_args* a, void* stream) {
+  if (!a || a->M < 0 || a->K < 1 || !a->A || !a->Bt || !a->C) return VX_ERR_ARG;
+  if (a->mode < 0 || a->mode > 2 || a->lda < a->K || a->n_store < 1 || a->n_store > a->Np || a->ldc < a->n_store)
+    return VX_ERR_ARG;
+  if ((reinterpret_cast<uintptr_t>(a->Bt) & 15) || (a->mode == 0 && !a->bias) ||
+      (a->mode == 1 && (!a->H || !a->colsum || a->ldh < a->Np || a->colsum_cap < (int64_t)vx_mlp_f32_rowgemm_grid(a->M) * a->Np)))
+    return VX_ERR_ARG;
+  if (a->M == 0 && a->mode != 1) return VX_OK;   // mode 1 still writes its (zero) column sums
+  RowGemmParams P{};
+  P.A = a->A;
+  P.lda = a->lda;
+  P.M = a->M;
+  P.m_dev = a->m_dev;
+  P.K = (int)a->K;
+  P.Bt = a->Bt;
+  P.Np = (int)a->Np;
+  P.mode = a->mode;
+  P.bias = a->bias;
+  P.H = a->H;
+  P.ldh = a->ldh;
+  P.C = a->C;
+  P.ldc = a->ldc;
+  P.n_store = (int)a->n_store;
+  P.colsum = a->colsum;
+  const unsigned grid = (unsigned)vx_mlp_f32_rowgemm_grid(a->M);
+  cudaStream_t st = as_stream(stream);
+  switch (a->Np) {
+    case 32: rowgemm_kernel<2><<<grid, THREADS, 0, st>>>(P); break;
+    case 64: rowgemm_kernel<4><<<grid, THREADS, 0, st>>>(P); break;
+    case 80: rowgemm_kernel<5><<<grid, THREADS, 0, st>>>(P); break;
+    case 128: rowgemm_kernel<8><<<grid, THREADS, 0, st>>>(P); break;
+    case 192: rowgemm_kernel<12><<<grid, THREADS, 0, st>>>(P); break;
+    default: return VX_ERR_UNSUPPORTED;
+  }
+  return launch_status();
+}
+
+size_t vx_mlp_f32_wgrad_grid(int64_t rows) {
+  // about 1024 rows per CTA, at most one CTA per SM
+  return (size_t)std::max<int64_t>(1, std::min<int64_t>(sm_count(), (rows + 1023) / 1024));
+}
+
+int vx_mlp_f32_wgrad(const vx_mlp_f32_wgrad_args* a, void* stream) {
+  if (!a || a->rows < 0 || !a->A || !a->B || !a->part || a->M < 1 || a->N < 1 || a->lda < a->M || a->ldb < a->N)
+    return VX_ERR_ARG;
+  auto pad = [](int64_t x) -> int64_t { return x <= 32 ? 32 : x <= 64 ? 64 : x <= 80 ? 80 : x <= 128 ? 128 : x <= 192 ? 192 : -1; };
+  const int64_t MP = pad(a->M), NP = pad(a->N);
+  if (MP < 0 || NP < 0) return VX_ERR_UNSUPPORTED;
+  const unsigned grid = (unsigned)vx_mlp_f32_wgrad_grid(a->rows);
+  if (a->part_cap < (int64_t)grid * MP * NP) return VX_ERR_ARG;
+  WgradParams P{};
+  P.A = a->A;
+  P.lda = a->lda;
+  P.B = a->B;
+  P.ldb = a->ldb;
+  P.M = (int)a->M;
+  P.N = (int)a->N;
+  P.rows = a->rows;
+  P.rows_dev = a->rows_dev;
+  P.part = a->part;
+  cudaStream_t st = as_stream(stream);
+#define VX_WG(TM_, TN_)                                            \
+  if (MP == 16 * TM_ && NP == 16 * TN_) {                          \
+    wgrad_kernel<TM_, TN_><<<grid, THREADS, 0, st>>>(P);           \
+    return launch_status();                                        \
+  }
+  VX_WG(12, 12) VX_WG(12, 5) VX_WG(12, 4) VX_WG(8, 8) VX_WG(8, 5) VX_WG(8, 4) VX_WG(4, 4) VX_WG(4, 5) VX_WG(2, 2)
+  VX_WG(2, 5) VX_WG(2, 4) VX_WG(4, 2)
+#undef VX_WG
+  return VX_ERR_UNSUPPORTED;
+}
+
+int vx_mlp_f32_reduce(const vx_mlp_sum_job* jobs, int n_jobs, void* stream) {
+  if (!jobs || n_jobs < 1 || n_jobs > MAX_SUM_JOBS) return VX_ERR_ARG;
+  SumJobs J{};
+  for (int i = 0; i < n_jobs; ++i) {
+    const vx_mlp_sum_job& s = jobs[i];
+    if (!s.part || !s.out || s.n_part < 1 || s.rows < 1 || s.cols < 1 || s.part_ld < s.cols || s.out_ld < s.cols)
+      return VX_ERR_ARG;
+    J.j[i] = SumJob{s.part, s.n_part, s.part_stride, s.part_ld, s.rows, s.cols, s.out, s.out_ld};
+  }
+  J.n = n_jobs;
+  dim3 grid(32, (unsigned)n_jobs);
+  sum_partials_kernel<<<grid, 256, 0, as_stream(stream)>>>(J);
+  return launch_status();
+}
+
+}  // extern "C"

@@ -772,6 +772,7 @@ __global__ void __launch_bounds__(128) features_coarse_kernel(CoarseFeatParams P
     put(x, col++, gr[1] * inv);
     put(x, col++, gr[2] * inv);
   }
+  for (; col < P.ld; ++col) put(x, col, 0.f);   // pad columns of the MLP row stride
   if (P.normal_out) {
     P.normal_out[3 * row + 0] = gr[0];
     P.normal_out[3 * row + 1] = gr[1];
@@ -1397,7 +1398,7 @@ static bool coarse_cfg_ok(const vx_coarse_feature_cfg* c) {
 int vx_coarse_features(const vx_coarse_features_args* A, void* stream) {
   if (!A || A->n_rows < 0 || !coarse_cfg_ok(&A->cfg)) return VX_ERR_ARG;
   if (A->n_rows == 0) return VX_OK;
-  if (A->ld != coarse_cols(&A->cfg) || !A->X || !A->grad4 || (A->cfg.use_k0 && !A->k0_f32 && !A->k0_bf16))
+  if (A->ld < coarse_cols(&A->cfg) || !A->X || !A->grad4 || (A->cfg.use_k0 && !A->k0_f32 && !A->k0_bf16))
     return VX_ERR_ARG;
   CoarseFeatParams P{};
   P.n_rows = A->n_rows;
@@ -1463,7 +1464,7 @@ int vx_coarse_composite_backward(const vx_coarse_composite_bwd_args* A, void* st
 
 int vx_coarse_backward(const vx_coarse_backward_args* A, void* stream) {
   if (!A || A->n_rays < 0 || A->n_rows < 0 || !coarse_cfg_ok(&A->cfg)) return VX_ERR_ARG;
-  if (A->n_rows > 0 && A->ld != coarse_cols(&A->cfg)) return VX_ERR_ARG;
+  if (A->n_rows > 0 && A->ld < coarse_cols(&A->cfg)) return VX_ERR_ARG;
   if ((((uintptr_t)A->grad4) | ((uintptr_t)A->d_grad4)) & 15) return VX_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   CoarseBwdParams C{};

@@ -18,16 +18,17 @@ static buffers:
 
 Part B is captured for a row capacity rounded up to `bucket_rows`; kernels
 that work per row read S2 from the device (s2_off[N]) and skip the rest,
-the GEMMs run over the whole capacity on rows that are finite but whose
-output gradients are zero, so the padding changes no result.  inv_s (which
+the MLP engines too.  inv_s (which
 changes every step with s_val) reaches the captured backward through a
 device scalar refreshed from pinned host memory by the graph's first node.
-The first time a capacity is seen, part B runs eagerly (on a side stream,
-which also warms up cuBLAS for the capture), is captured, and is replayed;
-re-running part B is idempotent because it clears its accumulators first.
+The first time a capacity is seen, part B runs eagerly (on a side stream),
+is captured, and is replayed; re-running part B is idempotent because it
+clears its accumulators first.
 
-The MLP input rows are padded to multiples of 8 columns (zero columns and
-zero weight columns) so that every GEMM gets 16-byte aligned operands.
+The colour MLPs run on the engines of mlp.py (the tcgen05 kernels for BF16
+rows, the FP32 CUDA-core kernels for FP32 rows); their input rows are padded
+to the engine's row stride, and the rgbnet forward writes its logits straight
+into the k-branch rows (k_res).
 """
 from __future__ import annotations
 
@@ -39,7 +40,7 @@ import torch
 from . import _abi, _native
 from . import grid as grid_mod
 from ._torch import ptr, stream_ptr
-from .mlp import mlp_backward, mlp_forward
+from .mlp import F32TrainMLP, TcTrainMLP, row_stride
 from .voxurf_fine import _feature_cfg, max_steps_bound
 
 
@@ -79,8 +80,8 @@ class GraphedFineStep:
         self.d1 = model.dim0
         self.k_res = bool(model.k_res)
         self.d2a = model.k_dim0 - (3 if self.k_res else 0)
-        self.ld1 = _round_up(self.d1, 8)
-        self.ld2 = _round_up(self.d2a + (3 if self.k_res else 0), 8)
+        self.ld1 = row_stride(self.d1, self.xdt)
+        self.ld2 = row_stride(self.d2a + (3 if self.k_res else 0), self.xdt)
         f32, i32, i64 = torch.float32, torch.int32, torch.int64
         # inputs
         self.inp = torch.empty((4, N, 3), dtype=f32, device=dev)   # rays_o, rays_d, viewdirs, target
@@ -104,33 +105,20 @@ class GraphedFineStep:
         self.k0_group = next(g for g in trainer.optimizer.param_groups if g.get("name") == "k0")
         self.dyn_host = torch.zeros(4, dtype=f32, pin_memory=True)
         self.dyn = torch.zeros(4, dtype=f32, device=dev)
-        # padded first-layer weights (zero columns beyond the feature count)
-        w1 = model.rgbnet[0].weight
-        w2 = model.k_rgbnet[0].weight
-        self.W1p = torch.zeros((w1.shape[0], self.ld1), dtype=self.xdt, device=dev)
-        self.W2p = torch.zeros((w2.shape[0], self.ld2), dtype=self.xdt, device=dev)
+        # the MLP engines (their operand buffers follow the FP32 parameters)
+        if self.bf16:
+            self.eng1 = TcTrainMLP(model.rgbnet, self.ld1)
+            self.eng2 = TcTrainMLP(model.k_rgbnet, self.ld2)
+        else:
+            self.eng1 = F32TrainMLP(model.rgbnet)
+            self.eng2 = F32TrainMLP(model.k_rgbnet)
         self.rgb_params = list(model.rgbnet.parameters())
         self.k_params = list(model.k_rgbnet.parameters())
-        self.cast_jobs = None
-        if self.bf16:
-            # persistent BF16 copies of the MLP weights and biases, refreshed
-            # by one multi-job cast launch per step
-            jobs = []
-
-            def job(src, dst, cols, dst_ld):
-                rows = src.shape[0] if src.dim() == 2 else 1
-                jobs.append(_abi.CastJob(src.data_ptr(), dst.data_ptr(), rows, cols, cols, dst_ld))
-
-            self.bf_rgb = [torch.empty_like(p, dtype=torch.bfloat16) for p in self.rgb_params]
-            self.bf_k = [torch.empty_like(p, dtype=torch.bfloat16) for p in self.k_params]
-            job(w1, self.W1p, w1.shape[1], self.ld1)
-            job(w2, self.W2p, w2.shape[1], self.ld2)
-            for params, bufs in ((self.rgb_params, self.bf_rgb), (self.k_params, self.bf_k)):
-                for i, (p, b) in enumerate(zip(params, bufs)):
-                    if i > 0:   # the first layer's weight goes to the padded W1p / W2p
-                        job(p, b, p.shape[-1], p.shape[-1])
-            if len(jobs) <= 16 and all(p.is_contiguous() for p in self.rgb_params + self.k_params):
-                self.cast_jobs = (_abi.CastJob * len(jobs))(*jobs)
+        # static FP32 gradients (the optimizer's p.grad) and per-capacity
+        # engine state (saved activations, backward scratch)
+        self.g1 = self.eng1.grad_buffers()
+        self.g2 = self.eng2.grad_buffers()
+        self.mlp_state = {}
         self.cap = 0
         self.graphs = {}
         self.S2 = 0
@@ -147,6 +135,7 @@ class GraphedFineStep:
         self.X2 = torch.zeros((cap, self.ld2), dtype=self.xdt, device=self.dev)
         self.cap = cap
         self.graphs.clear()   # captured graphs point at the old buffers
+        self.mlp_state.clear()
 
     # ---- one step -------------------------------------------------------------
     def step(self, rays_o, rays_d, viewdirs, target, global_step=None):
@@ -281,32 +270,15 @@ class GraphedFineStep:
         f.X1, f.X2, f.out_bf16 = ptr(X1), ptr(X2), int(self.bf16)
         f.n_rows_dev = ptr(n_rows_dev)
         _abi.call_struct("vx_fine_features", f, st)
-        # colour MLPs (weights cast to the compute dtype, first layer padded)
-        W1 = [p for i, p in enumerate(self.rgb_params) if i % 2 == 0]
-        b1 = [p for i, p in enumerate(self.rgb_params) if i % 2 == 1]
-        W2 = [p for i, p in enumerate(self.k_params) if i % 2 == 0]
-        b2 = [p for i, p in enumerate(self.k_params) if i % 2 == 1]
-        if self.cast_jobs is not None:
-            _abi.call("vx_cast_rows_bf16", self.cast_jobs, len(self.cast_jobs), st)
-            Ws1 = [self.W1p] + [self.bf_rgb[i] for i in range(2, len(self.bf_rgb), 2)]
-            bs1 = [self.bf_rgb[i] for i in range(1, len(self.bf_rgb), 2)]
-            Ws2 = [self.W2p] + [self.bf_k[i] for i in range(2, len(self.bf_k), 2)]
-            bs2 = [self.bf_k[i] for i in range(1, len(self.bf_k), 2)]
-        else:
-            self.W1p[:, :self.d1].copy_(W1[0].detach())
-            Ws1 = [self.W1p] + [w.detach().to(xdt) for w in W1[1:]]
-            bs1 = [b.detach().to(xdt) for b in b1]
-        hs1 = mlp_forward(X1, Ws1, bs1)
-        logit = hs1[-1].float()
-        if self.k_res:
-            X2[:, self.d2a:self.d2a + 3].copy_(logit)
-        d2 = self.d2a + (3 if self.k_res else 0)
-        if self.cast_jobs is None:
-            self.W2p[:, :d2].copy_(W2[0].detach())
-            Ws2 = [self.W2p] + [w.detach().to(xdt) for w in W2[1:]]
-            bs2 = [b.detach().to(xdt) for b in b2]
-        hs2 = mlp_forward(X2, Ws2, bs2)
-        klogit = logit + hs2[-1].float()
+        # colour MLPs: one pack launch for both engines' operands, then the
+        # rgbnet forward (its logits also land in the k-branch rows, k_res)
+        # and the k_rgbnet forward, over the device row count S2
+        sv = self.mlp_state.setdefault(cap, ({}, {}, {}, {}))
+        TcTrainMLP.pack_many([self.eng1, self.eng2], st)
+        cols = X2[:, self.d2a:self.d2a + 3] if self.k_res else None
+        logit, st1 = self.eng1.forward(X1, train=True, cols=cols, n_rows_dev=n_rows_dev, saved=sv[0])
+        kout, st2 = self.eng2.forward(X2, train=True, n_rows_dev=n_rows_dev, saved=sv[1])
+        klogit = logit + kout
         # compositing
         rgb0 = torch.empty((N, 3), dtype=f32, device=dev)
         rgbk = torch.empty((N, 3), dtype=f32, device=dev)
@@ -342,14 +314,12 @@ class GraphedFineStep:
         b.d_logit, b.d_klogit, b.d_w2, b.d_last, b.has_k = ptr(d_logit), ptr(d_klogit), ptr(d_w2), ptr(d_last), 1
         _abi.call_struct("vx_fine_composite_backward", b, st)
         # MLP backward (k-branch first: its logit input may feed d_logit)
-        dX2, g2 = mlp_backward(d_klogit, hs2, Ws2, True)
+        dX2, g2 = self.eng2.backward(st2, d_klogit, dx_dtype=xdt, grads=self.g2, work=sv[3])
         if not model.k_detach_2:
             d_logit = d_logit + d_klogit
         if self.k_res and not model.k_detach_1:
             d_logit = d_logit + dX2[:, self.d2a:self.d2a + 3].float()
-        dX1, g1 = mlp_backward(d_logit, hs1, Ws1, True)
-        g1[0] = g1[0][:, :self.d1].contiguous()
-        g2[0] = g2[0][:, :d2].contiguous()
+        dX1, g1 = self.eng1.backward(st1, d_logit, dx_dtype=xdt, grads=self.g1, work=sv[2])
         # march / feature backward into the grid gradients
         bw = _abi.FineBackwardArgs()
         bw.n_rays, bw.n_rows = N, cap

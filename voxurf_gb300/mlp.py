@@ -1,174 +1,91 @@
 """Colour-MLP forward/backward for rgbnet / k_rgbnet (lib/voxurf_fine.py:
-132-187, lib/voxurf_coarse.py:116-123): Linear -> ReLU stacks applied to the
-feature rows written by the feature kernels.
+132-187, applied at :718-752) and the coarse rgbnet (lib/voxurf_coarse.py:
+116-123): Linear -> ReLU stacks applied to the feature rows written by the
+feature kernels, then a 3-wide output layer.
 
-The GEMMs are cuBLAS calls (FP32, or BF16 with FP32 accumulation); the
-hidden layers use cuBLASLt's bias+ReLU epilogue (torch._addmm_activation);
-the backward fuses ReLU-backward with the bias gradient in one sm_103a pass
-(vx_relu_bwd_colsum) instead of torch's threshold_backward plus a strided
-column reduction.  Parameters stay FP32 masters; in BF16 mode they are cast
-per call and the weight gradients are returned in FP32.
+Two native engines, both hand-written sm_103a kernels:
+* BF16 rows (the mixed-precision path): TcTrainMLP, the tcgen05 tensor-core
+  kernels of mlp_train.cu (BF16 operands, FP32 accumulation);
+* FP32 rows (the plain path): F32TrainMLP, FP32 CUDA-core kernels
+  (mlp_f32.cu) for the hidden layers and the fused output-layer kernels of
+  mlp_ops.cu (vx_mlp_head, vx_mlp_head_backward).
+Parameters stay FP32 masters (the reference's nn.Linear parameters, same
+names and shapes); each forward refreshes the engine's operand copies of
+them with one pack launch, and the backward returns FP32 gradients.
 """
 from __future__ import annotations
-
-import os
 
 import torch
 import torch.nn as nn
 
 from ._torch import call, ptr, stream_ptr
 
-# FP32 backward GEMMs: "native" = cuBLAS SGEMM through the library's own
-# handle (vx_gemm_f32; 20% faster training steps than torch.matmul's choice
-# of kernels for these shapes), "emulated" = the same call in cuBLAS's BF16x9
-# FP32 emulation on the tensor cores (another 5%; meets the FP32 parity
-# bars), "torch" = torch.matmul.
-FP32_GEMM = os.environ.get("VX_FP32_GEMM", "native")
+
+def _round_up(x: int, m: int) -> int:
+    return (x + m - 1) // m * m
 
 
-def _gemm_f32(dz: torch.Tensor, other: torch.Tensor, wgrad: bool) -> torch.Tensor:
-    """Row-major FP32 products of the MLP backward through vx_gemm_f32:
-    wgrad: dz^T @ h ([N_out, K_in]); else dz @ W ([S, K_in])."""
-    emulate = int(FP32_GEMM == "emulated")
-    S, n_out = dz.shape
-    dev = dz.device
-    if wgrad:
-        h = other
-        k_in = h.shape[1]
-        out = torch.empty((n_out, k_in), dtype=torch.float32, device=dev)
-        # column-major: out^T (k_in x n_out) = h^T (k_in x S) . dz (S x n_out)
-        call("vx_gemm_f32", 0, 1, k_in, n_out, S, 1.0, ptr(h), k_in, ptr(dz), n_out, 0.0, ptr(out), k_in, emulate,
-             None, 0, stream_ptr(dev))
-    else:
-        W = other
-        k_in = W.shape[1]
-        out = torch.empty((S, k_in), dtype=torch.float32, device=dev)
-        # column-major: out^T (k_in x S) = W^T (k_in x n_out) . dz^T (n_out x S)
-        call("vx_gemm_f32", 0, 0, k_in, S, n_out, 1.0, ptr(W), k_in, ptr(dz), n_out, 0.0, ptr(out), k_in, emulate,
-             None, 0, stream_ptr(dev))
-    return out
+def _pad_width(n: int) -> int:
+    """Column counts of the FP32 kernels' tiles."""
+    for p in (32, 64, 80, 128, 192):
+        if n <= p:
+            return p
+    raise ValueError(f"MLP layer width {n} above 192")
 
 
-def _colsum(dh: torch.Tensor, h: torch.Tensor | None, dz: torch.Tensor | None,
-            out: torch.Tensor | None = None) -> torch.Tensor:
-    M, N = dh.shape
-    if out is None:
-        out = torch.zeros(N, dtype=torch.float32, device=dh.device)
-    dtype = 1 if dh.dtype == torch.bfloat16 else 0
-    call("vx_relu_bwd_colsum", ptr(dh), ptr(h), M, N, dtype, ptr(dz), ptr(out), stream_ptr())
-    return out
+def row_stride(d_in: int, dtype: torch.dtype) -> int:
+    """Row stride of MLP input rows of d_in features for the engine of dtype
+    (zero columns beyond d_in): a multiple of 16 elements for the tensor-core
+    engine (its MMA K step), of 4 for the FP32 engine (16-byte rows)."""
+    return _round_up(d_in, 16 if dtype == torch.bfloat16 else 4)
 
 
-def _head_layer(Ws, hs_last) -> bool:
-    """The last layer is a colour head (3 outputs from a ReLU layer of at
-    most 256 columns in 16-byte row chunks) that the fused head kernels take."""
-    W = Ws[-1]
-    N = W.shape[1]
-    per = 8 if hs_last.dtype == torch.bfloat16 else 4
-    return (len(Ws) >= 2 and W.shape[0] == 3 and N <= 256 and N % per == 0 and hs_last.is_contiguous()
-            and hs_last.data_ptr() % 16 == 0)
-
-
-def mlp_forward(x: torch.Tensor, Ws, bs) -> list[torch.Tensor]:
-    """Linear/ReLU stack on rows x (weights already in x's dtype): returns
-    the activations [x, h1, ..., logits].  A 3-output last layer runs in
-    vx_mlp_head (FP32 accumulation and FP32 logits) instead of a GEMM with a
-    3-wide dimension."""
-    n = len(Ws)
-    hs = [x]
-    h = x
-    for i in range(n):
-        if i < n - 1:
-            h = torch._addmm_activation(bs[i], h, Ws[i].t())
-        elif _head_layer(Ws, h):
-            M, N = h.shape
-            out = torch.empty((M, 3), dtype=torch.float32, device=h.device)
-            W, b = Ws[i].float().contiguous(), bs[i].float().contiguous()
-            call("vx_mlp_head", ptr(h), M, N, N, int(h.dtype == torch.bfloat16), ptr(W), ptr(b), None, ptr(out),
-                 None, 0, 0, stream_ptr(h.device))
-            h = out
-        else:
-            h = torch.addmm(bs[i], h, Ws[i].t())
-        hs.append(h)
-    return hs
-
-
-def mlp_backward(dy: torch.Tensor, hs, Ws, need_dx: bool):
-    """Gradients of mlp_forward: (dx or None, [dW1, db1, ..., dWn, dbn]) with
-    FP32 weight gradients; ReLU backward and the bias gradient are one pass
-    (vx_relu_bwd_colsum); a 3-output head's weight and bias gradients, its
-    input gradient and the ReLU backward below it are one pass
-    (vx_mlp_head_backward)."""
-    n = len(Ws)
-    grads = [None] * (2 * n)
-    dx = None
-    top = n
-    head = _head_layer(Ws, hs[n - 1])
-    # every accumulator of the pass (head dW, dbh, db; the bias gradients of
-    # the layers below) comes from one zero-filled buffer, 16-byte aligned
-    sizes = [3 * hs[n - 1].shape[1], 3, hs[n - 1].shape[1]] if head else [dy.shape[1]]
-    sizes += [Ws[i].shape[1] for i in reversed(range(1, n - 1 if head else n))]
-    offs, total = [], 0
-    for sz in sizes:
-        offs.append(total)
-        total += (sz + 3) // 4 * 4
-    acc = torch.zeros(total, dtype=torch.float32, device=dy.device)
-    views = iter([acc[o:o + sz] for o, sz in zip(offs, sizes)])
-    if head:
-        h = hs[n - 1]
-        M, N = h.shape
-        dev = h.device
-        dW = next(views).view(3, N)
-        dbh = next(views)
-        db = next(views)
-        dz = torch.empty_like(h)
-        W = Ws[n - 1].float().contiguous()
-        dout = dy.float().contiguous()  # kept alive until the kernel is enqueued
-        call("vx_mlp_head_backward", ptr(dout), ptr(h), ptr(W), M, N, int(h.dtype == torch.bfloat16), ptr(dz),
-             ptr(dW), ptr(dbh), ptr(db), stream_ptr(dev))
-        grads[2 * (n - 1)] = dW
-        grads[2 * (n - 1) + 1] = dbh
-        top = n - 1
-    else:
-        dz = dy.to(hs[0].dtype).contiguous()
-        db = _colsum(dz, None, None, next(views))
-    lib_gemm = dz.dtype == torch.float32 and FP32_GEMM != "torch"
-    for i in reversed(range(top)):
-        if lib_gemm:
-            h, W = hs[i].contiguous(), Ws[i].contiguous()
-            grads[2 * i] = _gemm_f32(dz, h, True)
-        else:
-            grads[2 * i] = (dz.t() @ hs[i]).float()
-        grads[2 * i + 1] = db
-        if i > 0:
-            dh = _gemm_f32(dz, W, False) if lib_gemm else dz @ Ws[i]
-            dz_prev = torch.empty_like(dh)
-            db = _colsum(dh, hs[i], dz_prev, next(views))
-            dz = dz_prev
-        elif need_dx:
-            dx = _gemm_f32(dz, W, False) if lib_gemm else dz @ Ws[0]
-    return dx, grads
-
-
-class _MLP(torch.autograd.Function):
+class _TrainMLP(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, x, *params):
-        n = len(params) // 2
-        dt = x.dtype
-        Ws = [params[2 * i].detach().to(dt) for i in range(n)]
-        bs = [params[2 * i + 1].detach().to(dt) for i in range(n)]
-        hs = mlp_forward(x, Ws, bs)
-        ctx.save_for_backward(*hs, *Ws)
-        ctx.n = n
-        return hs[-1]
+    def forward(ctx, x, eng, cols, *params):
+        train = any(ctx.needs_input_grad)
+        eng.pack()
+        logits, st = eng.forward(x, train=train, cols=cols)
+        ctx.eng, ctx.st = eng, st
+        ctx.x_dtype = x.dtype
+        return logits
 
     @staticmethod
     def backward(ctx, dy):
-        n = ctx.n
-        saved = ctx.saved_tensors
-        hs, Ws = saved[: n + 1], saved[n + 1:]
-        dx, grads = mlp_backward(dy, hs, Ws, ctx.needs_input_grad[0])
-        return (dx, *grads)
+        dX, grads = ctx.eng.backward(ctx.st, dy.float().contiguous(), dx_dtype=ctx.x_dtype)
+        ctx.st = None
+        return (dX if ctx.needs_input_grad[0] else None, None, None, *grads)
+
+
+def engine_for(net: nn.Sequential, dtype: torch.dtype, ld: int):
+    """The engine of `net` for input rows of `dtype` with row stride `ld`
+    (cached on the module; its operand buffers follow the parameters)."""
+    cache = net.__dict__.setdefault("_vx_engines", {})
+    key = (dtype, ld)
+    eng = cache.get(key)
+    lin = _linears(net)
+    if eng is None or eng.lin[0].weight.data_ptr() != lin[0].weight.data_ptr():
+        eng = TcTrainMLP(net, ld) if dtype == torch.bfloat16 else F32TrainMLP(net)
+        cache[key] = eng
+    return eng
+
+
+def apply_mlp(net: nn.Sequential, x: torch.Tensor, cols: torch.Tensor | None = None) -> torch.Tensor:
+    """net(x) -> FP32 logits [S, 3] with the hand-written backward.  x: rows
+    [S, ld] FP32 or BF16 (the compute dtype), ld = row_stride(in_features,
+    dtype) or more, zero beyond in_features (pad columns are never written
+    back).  cols: optional [S, >=3] view (row stride given by the tensor) that
+    also receives the logits in x's dtype (the k-branch input columns)."""
+    lin = _linears(net)
+    d_in = lin[0].in_features
+    ld = x.shape[1]
+    if x.stride(1) != 1 or ld < d_in:
+        raise ValueError("MLP rows must be row-contiguous with at least in_features columns")
+    if x.dtype == torch.bfloat16 and ld % 16:
+        ld = _round_up(ld, 16)
+        x = torch.nn.functional.pad(x, (0, ld - x.shape[1]))
+    eng = engine_for(net, x.dtype, ld)
+    return _TrainMLP.apply(x, eng, cols, *net.parameters())
 
 
 def mlp_params(net: nn.Sequential) -> list[torch.Tensor]:
@@ -176,9 +93,154 @@ def mlp_params(net: nn.Sequential) -> list[torch.Tensor]:
     return list(net.parameters())
 
 
-def apply_mlp(net: nn.Sequential, x: torch.Tensor) -> torch.Tensor:
-    """net(x) with the fused backward; x float32 or bfloat16 (compute dtype)."""
-    return _MLP.apply(x.contiguous(), *mlp_params(net))
+def last_relu_masks(net: nn.Sequential) -> list[torch.Tensor] | None:
+    """ReLU decisions (post-ReLU activation > 0) of each hidden layer in the
+    last training forward of `net` through the FP32 engine, [S, W] bool each
+    (rows in the order of the MLP input), or None."""
+    for eng in net.__dict__.get("_vx_engines", {}).values():
+        if isinstance(eng, F32TrainMLP) and eng.last_hs is not None:
+            return [h > 0 for h in eng.last_hs]
+    return None
+
+
+class F32TrainMLP:
+    """Plain-FP32 engine: the hidden layers as FP32 CUDA-core GEMMs with
+    fused epilogues (vx_mlp_f32_rowgemm: +bias and ReLU forward; ReLU mask and
+    bias-gradient column sums backward), their weight gradients summed over
+    rows per CTA (vx_mlp_f32_wgrad) and in a fixed order (vx_mlp_f32_reduce),
+    the 3-wide output layer in vx_mlp_head / vx_mlp_head_backward."""
+
+    def __init__(self, net: nn.Sequential):
+        from . import _abi
+
+        lin = _linears(net)
+        W = lin[0].out_features
+        if not (len(lin) >= 2 and lin[-1].out_features == 3 and W % 4 == 0 and W <= 192
+                and all(m.in_features == W and m.out_features == W for m in lin[1:-1])
+                and lin[-1].in_features == W and lin[0].in_features <= 192):
+            raise ValueError("FP32 MLP engine: Linear(K<=192, W), (L-1) x Linear(W, W), Linear(W, 3), W <= 192")
+        for m in lin:
+            if not (m.weight.is_contiguous() and m.bias.is_contiguous() and m.weight.dtype == torch.float32):
+                raise ValueError("MLP parameters must be contiguous FP32")
+        self.lin, self.W, self.L, self.d_in = lin, W, len(lin) - 1, lin[0].in_features
+        self.Wp = _pad_width(W)
+        if self.Wp != W:
+            raise ValueError("FP32 MLP engine: hidden width must be 32, 64, 80, 128 or 192")
+        dev = lin[0].weight.device
+        self.device = dev
+        J = _abi.MlpPackJob
+        self.Bf, self.Bb, jobs = [], [], []
+        for l in range(self.L):
+            k_in = lin[l].in_features
+            bf = torch.empty((_round_up(k_in, 16), W), dtype=torch.float32, device=dev)       # Bt[k][n] = W_l[n][k]
+            bb = torch.empty((W, _pad_width(k_in)), dtype=torch.float32, device=dev)          # Bt[k][n] = W_l[k][n]
+            jobs.append(J(lin[l].weight.data_ptr(), k_in, W, k_in, W, bf.shape[0], 1, 3, bf.data_ptr()))
+            jobs.append(J(lin[l].weight.data_ptr(), k_in, k_in, W, bb.shape[1], W, 0, 3, bb.data_ptr()))
+            self.Bf.append(bf)
+            self.Bb.append(bb)
+        self.jobs = (J * len(jobs))(*jobs)
+        self.last_hs = None
+
+    def pack(self, stream: int | None = None) -> None:
+        from . import _abi
+
+        _abi.call("vx_mlp_train_pack", self.jobs, len(self.jobs), stream_ptr(self.device) if stream is None else stream)
+
+    def grad_buffers(self) -> list[torch.Tensor]:
+        out = []
+        for m in self.lin:
+            out += [torch.empty_like(m.weight), torch.empty_like(m.bias)]
+        return out
+
+    def _rowgemm(self, mode, A, K, Bt, Np, C, n_store, bias=None, H=None, colsum=None, n_rows_dev=None):
+        from . import _abi
+
+        g = _abi.MlpF32RowGemmArgs()
+        g.M, g.m_dev, g.K, g.A, g.lda = A.shape[0], ptr(n_rows_dev), K, ptr(A), A.stride(0)
+        g.Bt, g.Np, g.mode = ptr(Bt), Np, mode
+        g.bias, g.H, g.ldh = ptr(bias), ptr(H), 0 if H is None else H.stride(0)
+        g.C, g.ldc, g.n_store = ptr(C), C.stride(0), n_store
+        g.colsum, g.colsum_cap = ptr(colsum), 0 if colsum is None else colsum.numel()
+        _abi.call_struct("vx_mlp_f32_rowgemm", g, stream_ptr(A.device))
+
+    def forward(self, X: torch.Tensor, out: torch.Tensor | None = None, train: bool = True,
+                cols: torch.Tensor | None = None, n_rows_dev: torch.Tensor | None = None,
+                saved: dict | None = None):
+        if X.dtype != torch.float32 or X.stride(1) != 1 or X.shape[1] < self.d_in:
+            raise ValueError("rows must be FP32 with >= in_features columns")
+        n, dev, W = X.shape[0], X.device, self.W
+        if out is None:
+            out = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        st = saved if saved is not None else {}
+        if "hs" not in st:
+            st["hs"] = [torch.empty((n, W), dtype=torch.float32, device=dev) for _ in range(self.L)]
+        h, k = X, self.d_in
+        for l in range(self.L):
+            self._rowgemm(0, h, k, self.Bf[l], W, st["hs"][l], W, bias=self.lin[l].bias, n_rows_dev=n_rows_dev)
+            h, k = st["hs"][l], W
+        lh = self.lin[-1]
+        cols_ptr, ld_cols, cols_bf16 = None, 0, 0
+        if cols is not None:
+            cols_ptr, ld_cols, cols_bf16 = ptr(cols), cols.stride(0), int(cols.dtype == torch.bfloat16)
+        call("vx_mlp_head", ptr(h), n, W, W, 0, lh.weight.data_ptr(), lh.bias.data_ptr(), None, ptr(out), cols_ptr,
+             ld_cols, cols_bf16, stream_ptr(dev))
+        st.update(n=n, X=X, n_rows_dev=n_rows_dev)
+        self.last_hs = st["hs"] if train else None
+        return out, (st if train else None)
+
+    def backward(self, st: dict, dY: torch.Tensor, dx_dtype=torch.float32, grads: list | None = None,
+                 dX: torch.Tensor | None = None, work: dict | None = None):
+        from . import _abi, _native
+
+        lib = _native.load()
+        _abi._declare()
+        n, X, hs = st["n"], st["X"], st["hs"]
+        W, L, dev = self.W, self.L, dY.device
+        stp = stream_ptr(dev)
+        nrd = st["n_rows_dev"]
+        if grads is None:
+            grads = self.grad_buffers()
+        w = work if work is not None else {}
+        g_rows = int(lib.vx_mlp_f32_rowgemm_grid(n))
+        g_wg = int(lib.vx_mlp_f32_wgrad_grid(n))
+        Np0 = _pad_width(self.d_in)
+        if "dz" not in w:
+            w["dz"] = [torch.empty((n, W), dtype=torch.float32, device=dev) for _ in range(2)]
+            w["part"] = [torch.empty(g_wg * W * W, dtype=torch.float32, device=dev) for _ in range(L - 1)]
+            w["part0"] = torch.empty(g_wg * W * Np0, dtype=torch.float32, device=dev)
+            w["colsum"] = [torch.empty(g_rows * W, dtype=torch.float32, device=dev) for _ in range(L - 1)]
+        if dX is None:
+            dX = torch.empty((n, X.shape[1]), dtype=torch.float32, device=dev)
+        # the output-layer kernel accumulates dWh, dbh and db_{L-1}
+        dWh, dbh, dbL = grads[2 * L], grads[2 * L + 1], grads[2 * (L - 1) + 1]
+        for t in (dWh, dbh, dbL):
+            t.zero_()
+        lh = self.lin[-1]
+        dz = w["dz"][0]
+        call("vx_mlp_head_backward", ptr(dY), ptr(hs[-1]), lh.weight.data_ptr(), n, W, 0, ptr(dz), ptr(dWh),
+             ptr(dbh), ptr(dbL), stp)
+        sums = []
+        S = _abi.MlpSumJob
+
+        def wgrad(A, B, N, part):
+            g = _abi.MlpF32WgradArgs()
+            g.rows, g.rows_dev, g.A, g.lda, g.B, g.ldb = n, ptr(nrd), ptr(A), A.stride(0), ptr(B), B.stride(0)
+            g.M, g.N, g.part, g.part_cap = W, N, ptr(part), part.numel()
+            _abi.call_struct("vx_mlp_f32_wgrad", g, stp)
+
+        for l in range(L - 1, 0, -1):        # dW_l = dz_{l+1}^T h_l; dz_l = (dz_{l+1} W_l) * [h_l > 0]
+            wgrad(dz, hs[l - 1], W, w["part"][l - 1])
+            sums.append(S(w["part"][l - 1].data_ptr(), g_wg, W * W, W, W, W, grads[2 * l].data_ptr(), W))
+            nxt = w["dz"][(L - l) % 2]
+            self._rowgemm(1, dz, W, self.Bb[l], W, nxt, W, H=hs[l - 1], colsum=w["colsum"][l - 1], n_rows_dev=nrd)
+            sums.append(S(w["colsum"][l - 1].data_ptr(), g_rows, W, W, 1, W, grads[2 * (l - 1) + 1].data_ptr(), W))
+            dz = nxt
+        wgrad(dz, X, self.d_in, w["part0"])  # dW_0 = dz_1^T X
+        sums.append(S(w["part0"].data_ptr(), g_wg, W * Np0, Np0, W, self.d_in, grads[0].data_ptr(), self.d_in))
+        self._rowgemm(2, dz, W, self.Bb[0], Np0, dX, self.d_in, n_rows_dev=nrd)   # dX = dz_1 W_0
+        arr = (S * len(sums))(*sums)
+        _abi.call("vx_mlp_f32_reduce", arr, len(sums), stp)
+        return dX, grads
 
 
 class TensorCoreMLP:
@@ -237,3 +299,191 @@ class TensorCoreMLP:
         a.Whp, a.bh, a.add, a.out = ptr(self.Whp), ptr(self.bh), ptr(add), ptr(out)
         a.cols, a.ld_cols = ptr(cols), ld_cols
         _abi.call_struct("vx_mlp_tc_forward", a, stream_ptr(X.device))
+
+
+def _linears(net: nn.Sequential) -> list:
+    return [m for m in net.modules() if isinstance(m, nn.Linear)]
+
+
+class TcTrainMLP:
+    """A Linear/ReLU colour MLP (hidden width 32/64/128/192, 2 or 3 hidden
+    layers, 3 outputs) trained on the tensor cores: BF16 operands, FP32
+    accumulation, FP32 master weights and FP32 gradients (vx_mlp_train_*).
+
+    K0 is the padded first-layer width (a multiple of 16 >= the Linear's
+    in_features); input rows must have at least K0 columns, zero beyond
+    in_features.  pack() refreshes the BF16 operands from the FP32 masters
+    (one launch); forward() keeps the hidden activations (T-tiles) and ReLU
+    bits for backward(); backward() returns the input gradient and writes the
+    FP32 gradients of every weight and bias.
+    """
+
+    @staticmethod
+    def supports(net: nn.Sequential, K0: int) -> bool:
+        lin = _linears(net)
+        if len(lin) not in (3, 4):
+            return False
+        W = lin[0].out_features
+        return (W in (32, 64, 128, 192) and all(m.out_features == W and m.in_features == W for m in lin[1:-1])
+                and lin[-1].out_features == 3 and lin[-1].in_features == W and lin[0].in_features <= K0 <= 80
+                and K0 % 16 == 0)
+
+    def __init__(self, net: nn.Sequential, K0: int):
+        if not self.supports(net, K0):
+            raise ValueError("tensor-core training MLP: Linear(K<=80, W), (1 or 2) x Linear(W, W), Linear(W, 3) "
+                             "with W in 32/64/128/192")
+        from . import _abi
+
+        lin = _linears(net)
+        self.lin = lin
+        self.W = W = lin[0].out_features
+        self.L = L = len(lin) - 1
+        self.d_in = lin[0].in_features
+        self.K0 = K0
+        dev = lin[0].weight.device
+        self.device = dev
+        bf, f32 = torch.bfloat16, torch.float32
+        self.W0p = torch.empty(K0 * W, dtype=bf, device=dev)
+        self.Wp = torch.empty(max(L - 1, 1) * W * W, dtype=bf, device=dev)
+        self.bias = torch.empty(L * W, dtype=f32, device=dev)
+        self.Whp = torch.empty(16 * W, dtype=bf, device=dev)
+        self.W0Tp = torch.empty(W * K0, dtype=bf, device=dev)
+        self.WTp = torch.empty(max(L - 1, 1) * W * W, dtype=bf, device=dev)
+        J = _abi.MlpPackJob
+
+        def job(src, ld, N, K, Np, Kp, transpose, mode, dst):
+            return J(src.data_ptr(), ld, N, K, Np, Kp, transpose, mode, dst)
+
+        w0 = lin[0].weight
+        jobs = [job(w0, self.d_in, W, self.d_in, W, K0, 0, 0, self.W0p.data_ptr()),
+                job(w0, self.d_in, self.d_in, W, K0, W, 1, 0, self.W0Tp.data_ptr()),
+                job(lin[L].weight, W, 3, W, 16, W, 0, 1, self.Whp.data_ptr())]
+        for l in range(1, L):
+            off = (l - 1) * W * W * 2
+            jobs.append(job(lin[l].weight, W, W, W, W, W, 0, 0, self.Wp.data_ptr() + off))
+            jobs.append(job(lin[l].weight, W, W, W, W, W, 1, 0, self.WTp.data_ptr() + off))
+        for l in range(L):
+            jobs.append(job(lin[l].bias, W, 1, W, 1, W, 0, 2, self.bias.data_ptr() + l * W * 4))
+        for m in lin:
+            if not (m.weight.is_contiguous() and m.bias.is_contiguous() and m.weight.dtype == f32):
+                raise ValueError("MLP parameters must be contiguous FP32")
+        self.jobs = (J * len(jobs))(*jobs)
+
+    def pack(self, stream: int | None = None) -> None:
+        from . import _abi
+
+        _abi.call("vx_mlp_train_pack", self.jobs, len(self.jobs), stream_ptr(self.device) if stream is None else stream)
+
+    @staticmethod
+    def pack_many(mlps, stream: int | None = None) -> None:
+        """One launch for the operands of several MLPs (up to 32 jobs)."""
+        from . import _abi
+
+        jobs = [j for m in mlps for j in m.jobs]
+        arr = (_abi.MlpPackJob * len(jobs))(*jobs)
+        _abi.call("vx_mlp_train_pack", arr, len(jobs), stream_ptr(mlps[0].device) if stream is None else stream)
+
+    def grad_buffers(self) -> list[torch.Tensor]:
+        """FP32 gradient buffers in parameter order [W0, b0, ..., Wh, bh]."""
+        out = []
+        for m in self.lin:
+            out += [torch.empty_like(m.weight), torch.empty_like(m.bias)]
+        return out
+
+    def forward(self, X: torch.Tensor, out: torch.Tensor | None = None, train: bool = True,
+                cols: torch.Tensor | None = None, n_rows_dev: torch.Tensor | None = None,
+                saved: dict | None = None) -> tuple[torch.Tensor, dict | None]:
+        """logits [n, 3] FP32 of X [n, >= K0] BF16 rows.  train: also returns
+        the state backward() needs (hidden T-tiles, ReLU bits); `saved` may
+        pass preallocated ones (graph capture).  cols: optional BF16 view
+        [n, >= 3] that also receives the logits."""
+        from . import _abi
+
+        n = X.shape[0]
+        if X.dtype != torch.bfloat16 or X.shape[1] < self.K0 or X.stride(1) != 1:
+            raise ValueError("rows must be BF16 with >= K0 columns")
+        cap = (n + 127) // 128 * 128
+        dev = X.device
+        if out is None:
+            out = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        st = None
+        if train:
+            st = saved if saved is not None else {}
+            if "H" not in st:
+                st["H"] = torch.empty(self.L * cap * self.W, dtype=torch.bfloat16, device=dev)
+                st["relu"] = torch.empty(self.L * cap * (self.W // 16), dtype=torch.int16, device=dev)
+            st["cap"], st["n"], st["X"], st["n_rows_dev"] = cap, n, X, n_rows_dev
+        a = _abi.MlpTrainFwdArgs()
+        a.n_rows, a.n_rows_dev, a.rows_cap = n, ptr(n_rows_dev), cap
+        a.width, a.n_hidden, a.K0 = self.W, self.L, self.K0
+        a.X, a.ldx = ptr(X), X.stride(0)
+        a.W0p, a.Wp, a.bias, a.Whp = ptr(self.W0p), ptr(self.Wp), ptr(self.bias), ptr(self.Whp)
+        a.bh, a.out = self.lin[-1].bias.data_ptr(), ptr(out)
+        if cols is not None and cols.dtype != torch.bfloat16:
+            raise ValueError("cols must be BF16 for BF16 rows")
+        a.cols, a.ld_cols = ptr(cols), (cols.stride(0) if cols is not None else 0)
+        if train:
+            a.H, a.relu = ptr(st["H"]), ptr(st["relu"])
+        _abi.call_struct("vx_mlp_train_forward", a, stream_ptr(dev))
+        return out, st
+
+    def backward(self, st: dict, dY: torch.Tensor, dx_dtype=torch.bfloat16, grads: list | None = None,
+                 dX: torch.Tensor | None = None, work: dict | None = None) -> tuple[torch.Tensor, list]:
+        """dX [n, K0] (dx_dtype) and the FP32 gradients [dW0, db0, ..., dWh, dbh]
+        (written into `grads` when given).  `work` may pass preallocated
+        scratch (graph capture)."""
+        from . import _abi, _native
+
+        lib = _native.load()
+        _abi._declare()
+        n, cap, X = st["n"], st["cap"], st["X"]
+        W, L, K0 = self.W, self.L, self.K0
+        dev = dY.device
+        stp = stream_ptr(dev)
+        if dY.dtype != torch.float32 or not dY.is_contiguous() or dY.shape[0] != n:
+            raise ValueError("dY must be contiguous FP32 [n, 3]")
+        grid = int(lib.vx_mlp_wgrad_grid(n))
+        w = work if work is not None else {}
+        if "dZ" not in w:
+            w["dZ"] = torch.empty(L * cap * W, dtype=torch.bfloat16, device=dev)
+            w["dYT"] = torch.empty(cap * 16, dtype=torch.bfloat16, device=dev)
+            w["dbh"] = torch.empty(grid * 4, dtype=torch.float32, device=dev)
+            w["part"] = [torch.empty(grid * W * (W + 16), dtype=torch.float32, device=dev) for _ in range(L - 1)]
+            w["part0"] = torch.empty(grid * W * (K0 + 16), dtype=torch.float32, device=dev)
+            w["parth"] = torch.empty(grid * W * 16, dtype=torch.float32, device=dev)
+        if dX is None:
+            dX = torch.empty((n, K0), dtype=dx_dtype, device=dev)
+        if grads is None:
+            grads = self.grad_buffers()
+        b = _abi.MlpTrainBwdArgs()
+        b.n_rows, b.n_rows_dev, b.rows_cap = n, ptr(st["n_rows_dev"]), cap
+        b.width, b.n_hidden, b.K0 = W, L, K0
+        b.dY, b.Wh, b.relu = ptr(dY), self.lin[-1].weight.data_ptr(), ptr(st["relu"])
+        b.WTp, b.W0Tp, b.dZ, b.dYT = ptr(self.WTp), ptr(self.W0Tp), ptr(w["dZ"]), ptr(w["dYT"])
+        b.dX, b.ld_dx, b.dx_bf16 = ptr(dX), dX.stride(0), int(dX.dtype == torch.bfloat16)
+        b.dbh_part, b.dbh_part_cap = ptr(w["dbh"]), grid
+        _abi.call_struct("vx_mlp_train_backward", b, stp)
+        H, dZ = st["H"].data_ptr(), w["dZ"].data_ptr()
+        lay = cap * W * 2   # bytes per layer of T-tiles
+        jobs = []
+
+        def wgrad(A, WA, B, WB, ldb, b_rows, ones, part):
+            g = _abi.MlpWgradArgs()
+            g.n_rows, g.n_rows_dev, g.A, g.WA, g.B, g.WB, g.ldb = n, ptr(st["n_rows_dev"]), A, WA, B, WB, ldb
+            g.b_rows, g.ones, g.part, g.part_cap = b_rows, ones, ptr(part), part.numel()
+            _abi.call_struct("vx_mlp_train_wgrad", g, stp)
+
+        R = _abi.MlpReduceJob
+        for l in range(1, L):   # dW_l = dz_{l+1}^T h_l
+            wgrad(dZ + l * lay, W, H + (l - 1) * lay, W, 0, 0, 1, w["part"][l - 1])
+            jobs.append(R(w["part"][l - 1].data_ptr(), grid, W, W + 16, 0, 0, W, W, grads[2 * l].data_ptr(),
+                          grads[2 * l + 1].data_ptr(), None, 0))
+        wgrad(dZ, W, X.data_ptr(), K0, X.stride(0), 1, 1, w["part0"])      # dW_0 = dz_1^T X
+        jobs.append(R(w["part0"].data_ptr(), grid, W, K0 + 16, 0, 0, K0, self.d_in, grads[0].data_ptr(),
+                      grads[1].data_ptr(), None, 0))
+        wgrad(H + (L - 1) * lay, W, w["dYT"].data_ptr(), 16, 0, 0, 0, w["parth"])   # dWh = dy^T h_L
+        jobs.append(R(w["parth"].data_ptr(), grid, W, 16, 1, 0, 16, 3, grads[2 * L].data_ptr(),
+                      grads[2 * L + 1].data_ptr(), w["dbh"].data_ptr(), grid))
+        arr = (R * len(jobs))(*jobs)
+        _abi.call("vx_mlp_train_reduce", arr, len(jobs), stp)
+        return dX, grads

@@ -9,8 +9,8 @@ global_step=None) over them with one launch per stage for all scenes
 (vx_serve_rays / _march / _rows / _features / _composite); only the colour
 MLPs are issued per scene, on the scene's contiguous rows: for BF16 scenes
 the fused tcgen05 kernel (vx_mlp_tc_forward, hidden activations never leave
-the SM), otherwise GEMMs with the 192 -> 3 output layers in vx_mlp_head
-(FP32 accumulation).  With a bool mask, a thread-per-ray pass over the
+the SM), otherwise the MLP engines of mlp.py (tcgen05 training kernels for
+BF16 rows, FP32 CUDA-core kernels for FP32 rows) in inference mode.  With a bool mask, a thread-per-ray pass over the
 mask's block occupancy starts each ray's march at its first sample that can
 lie in the mask.  The composite writes straight into each request's range
 of an output arena.
@@ -46,7 +46,7 @@ import torch
 from . import _abi
 from . import grid as grid_mod
 from ._torch import ptr, scratch, stream_ptr
-from .mlp import TensorCoreMLP
+from .mlp import TensorCoreMLP, engine_for
 from .voxurf_fine import _feature_cfg, max_steps_bound, smooth_grid
 
 _BYTES_PER_PIXEL = 16  # rgb f32 + depth f32 (device and pinned host)
@@ -100,8 +100,13 @@ class ResidentScene:
         # MLP input rows padded to 16 columns (the tensor-core K step)
         self.ld1 = _round_up(self.d1, 16)
         self.ld2 = _round_up(self.d2a + 3, 16)
-        self.rgbnet = self._mlp(model.rgbnet, self.ld1)
-        self.k_rgbnet = self._mlp(model.k_rgbnet, self.ld2) if self.use_rgb_k else None
+        # MLP engines (operands packed once: the weights of a served scene
+        # do not change); used when the fused inference kernel does not apply
+        self.engines = (engine_for(model.rgbnet, self.dtype, self.ld1),
+                        engine_for(model.k_rgbnet, self.dtype, self.ld2) if self.use_rgb_k else None)
+        for e in self.engines:
+            if e is not None:
+                e.pack()
         # fused tcgen05 forward of both MLPs (BF16 scenes of the 192-wide layout)
         self.tc = None
         if precision == "bf16" and self.use_rgb_k and TensorCoreMLP.supports(model.rgbnet, self.ld1) \
@@ -146,26 +151,12 @@ class ResidentScene:
         self.desc = d
         self.device = dev
 
-    def _mlp(self, net, ld: int):
-        """(hidden [(W, b)], head (W, b)) for the GEMM path; the first layer's
-        W is padded with zero columns to the row stride ld of its input."""
-        lin = [m for m in net.modules() if isinstance(m, torch.nn.Linear)]
-        hidden = []
-        for i, m in enumerate(lin[:-1]):
-            W = m.weight.detach()
-            if i == 0:
-                Wp = torch.zeros((W.shape[0], ld), dtype=self.dtype, device=W.device)
-                Wp[:, :W.shape[1]] = W
-                W = Wp
-            hidden.append((W.to(self.dtype).contiguous(), m.bias.detach().to(self.dtype).contiguous()))
-        head = (lin[-1].weight.detach().float().contiguous(), lin[-1].bias.detach().float().contiguous())
-        return hidden, head
-
     def nbytes(self) -> int:
         ts = [self.sdf, self.k0] + ([self.mask] if self.mask is not None else [])
-        for net in (self.rgbnet, self.k_rgbnet):
-            if net is not None:
-                ts += [t for wb in net[0] for t in wb] + list(net[1])
+        for e in self.engines:
+            if e is not None:
+                ts += [t for t in vars(e).values() if isinstance(t, torch.Tensor)]
+                ts += [t for v in vars(e).values() if isinstance(v, list) for t in v if isinstance(t, torch.Tensor)]
         return sum(t.numel() * t.element_size() for t in ts)
 
 
@@ -271,8 +262,8 @@ class RenderServer:
     def __init__(self, scenes: list[ResidentScene], tick_rays: int = 1 << 19, arena_pixels: int | None = None,
                  hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None, mlp: str = "tc"):
         """mlp: "tc" runs each scene's two colour MLPs as fused tcgen05
-        launches where the scene supports it (BF16, 192-wide), "gemm" as
-        per-layer cuBLAS GEMMs plus vx_mlp_head."""
+        launches where the scene supports it (BF16, 192-wide), "layers" on the
+        MLP engines of mlp.py (one kernel per layer)."""
         if not 1 <= len(scenes) <= 8:
             raise ValueError("1 to 8 resident scenes")
         if not all(s.use_rgb_k and s.k_res for s in scenes):
@@ -294,7 +285,7 @@ class RenderServer:
         self.d2a = scenes[0].d2a
         self.ld1 = scenes[0].ld1
         self.ld2 = scenes[0].ld2
-        if mlp not in ("tc", "gemm"):
+        if mlp not in ("tc", "layers"):
             raise ValueError(mlp)
         self.mlp = mlp
         dev = self.device
@@ -556,31 +547,18 @@ class RenderServer:
                 r.event.record(bs)
                 self.finishing.append(r)
 
-    def _hidden(self, layers, x):
-        h = x
-        for W, b in layers:
-            h = torch._addmm_activation(b, h, W.t())
-        return h
-
     def _shade(self, s: ResidentScene, a: int, b: int, st: int) -> None:
-        n = b - a
-        bf = int(self.bf16)
         if s.tc is not None and self.mlp == "tc":
             # rgbnet -> logits (also into the k_rgbnet input's last columns), then
             # k_rgbnet with the logits as residual, each one fused tcgen05 launch
             s.tc[0].forward(self.X1[a:b], self.logit[a:b], cols=self.X2[a:b, self.d2a:], ld_cols=self.ld2)
             s.tc[1].forward(self.X2[a:b], self.klogit[a:b], add=self.logit[a:b])
             return
-        h = self._hidden(s.rgbnet[0], self.X1[a:b])
-        W, bias = s.rgbnet[1]
-        cols = self.X2[a:b, self.d2a:] if s.k_res else None
-        _abi.call("vx_mlp_head", ptr(h), n, h.shape[1], h.stride(0), bf, ptr(W), ptr(bias), None,
-                  ptr(self.logit[a:b]), ptr(cols), self.ld2, bf, st)
+        cols = self.X2[a:b, self.d2a:self.d2a + 3] if s.k_res else None
+        s.engines[0].forward(self.X1[a:b], out=self.logit[a:b], train=False, cols=cols)
         if s.use_rgb_k:
-            h2 = self._hidden(s.k_rgbnet[0], self.X2[a:b])
-            W2, b2 = s.k_rgbnet[1]
-            _abi.call("vx_mlp_head", ptr(h2), n, h2.shape[1], h2.stride(0), bf, ptr(W2), ptr(b2),
-                      ptr(self.logit[a:b]), ptr(self.klogit[a:b]), None, 0, 0, st)
+            kout, _ = s.engines[1].forward(self.X2[a:b], train=False)
+            torch.add(self.logit[a:b], kout, out=self.klogit[a:b])
 
 
 def plain_render(model, c2w, H: int, W: int, focal: float | None = None, chunk: int = 8192,

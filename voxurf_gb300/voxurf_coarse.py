@@ -23,7 +23,7 @@ import torch.nn as nn
 from . import _abi, _native
 from . import grid as grid_mod
 from ._torch import ptr, stream_ptr
-from .mlp import apply_mlp
+from .mlp import apply_mlp, row_stride
 from .voxurf_fine import FineFrame, gaussian_taps, marching_cubes, max_steps_bound, smooth_grid, smooth_grid_adjoint
 from .voxurf_fine import extract_fields as _extract_fields
 from .voxurf_fine import query_mask
@@ -95,7 +95,7 @@ class _CoarseGeometry(torch.autograd.Function):
         _abi.call_struct("vx_fine_compact", c, st)
 
         xdt = torch.bfloat16 if fr.bf16 else torch.float32
-        Xf = torch.empty((S2, fr.d1), dtype=xdt, device=dev)
+        Xf = torch.empty((S2, fr.ld), dtype=xdt, device=dev)
         normal2 = torch.empty((S2, 3), dtype=torch.float32, device=dev)
         f = _abi.CoarseFeaturesArgs()
         f.n_rows, f.ray2, f.pts2, f.viewdirs = S2, ptr(ray2), ptr(pts2), ptr(fr.viewdirs)
@@ -104,7 +104,7 @@ class _CoarseGeometry(torch.autograd.Function):
             f.k0_bf16 = ptr(fr.k0_bf16)
         else:
             f.k0_f32 = ptr(k0_grid)
-        f.cfg, f.ld, f.X, f.out_bf16, f.normal_out = fr.cfg, fr.d1, ptr(Xf), int(fr.bf16), ptr(normal2)
+        f.cfg, f.ld, f.X, f.out_bf16, f.normal_out = fr.cfg, fr.ld, ptr(Xf), int(fr.bf16), ptr(normal2)
         _abi.call_struct("vx_coarse_features", f, st)
         fr.rec, fr.dw_slot, fr.n2b, fr.alphainv_last = rec, dw_slot, n2b, alphainv_last
         fr.s2_off, fr.ray2, fr.step2, fr.slot2, fr.w2, fr.alpha2, fr.pts2 = s2_off, ray2, step2, slot2, w2, alpha2, pts2
@@ -122,7 +122,7 @@ class _CoarseGeometry(torch.autograd.Function):
         X, Y, Z = fr.geom.X, fr.geom.Y, fr.geom.Z
         S2, N = fr.S2, fr.n_rays
         xdt = torch.bfloat16 if fr.bf16 else torch.float32
-        dX = torch.zeros((S2, fr.d1), dtype=xdt, device=dev) if dX is None else dX.contiguous()
+        dX = torch.zeros((S2, fr.ld), dtype=xdt, device=dev) if dX is None else dX.contiguous()
         dw2 = torch.zeros(S2, dtype=torch.float32, device=dev) if dw2 is None else dw2.contiguous().float()
         dlast = torch.zeros(N, dtype=torch.float32, device=dev) if dlast is None else dlast.contiguous().float()
         d_sdf_s = torch.zeros((X, Y, Z), dtype=torch.float32, device=dev)
@@ -137,7 +137,7 @@ class _CoarseGeometry(torch.autograd.Function):
         b.rec, b.dw_slot, b.n2b = ptr(fr.rec), ptr(fr.dw_slot), ptr(fr.n2b)
         b.alphainv_last, b.d_last = ptr(fr.alphainv_last), ptr(dlast)
         b.pts2, b.slot2, b.dw2 = ptr(fr.pts2), ptr(fr.slot2), ptr(dw2)
-        b.cfg, b.ld, b.dX, b.in_bf16 = fr.cfg, fr.d1, ptr(dX), int(fr.bf16)
+        b.cfg, b.ld, b.dX, b.in_bf16 = fr.cfg, fr.ld, ptr(dX), int(fr.bf16)
         b.d_sdf_smooth, b.d_grad4, b.d_k0 = ptr(d_sdf_s), ptr(dG4), ptr(d_k0)
         if d_grad2 is not None:
             d_grad2 = d_grad2.float().contiguous()
@@ -364,10 +364,12 @@ class Voxurf(nn.Module):
                 self.refresh_k0_shadow()
             fr.k0_bf16 = self._k0_shadow
         fr.d1 = self.dim0
+        # MLP input rows zero-padded to the stride of the MLP engine
+        fr.ld = row_stride(fr.d1, torch.bfloat16 if fr.bf16 else torch.float32)
         fr.render_extras = bool(render_kwargs.get("render_depth", False) or render_kwargs.get("render_grad", False))
         Xf, w2, alphainv_last, normal2, alpha2 = _CoarseGeometry.apply(self.sdf.grid, self.k0.grid, fr)
         fr.normal2 = normal2
-        rgb_logit = apply_mlp(self.rgbnet, Xf).float()
+        rgb_logit = apply_mlp(self.rgbnet, Xf)
         rgb = torch.sigmoid(rgb_logit)
         rgb_marched = _CoarseComposite.apply(w2, rgb_logit, fr, float(render_kwargs["bg"]))
         normal_marched = None

@@ -36,7 +36,7 @@ import torch.nn.functional as F
 from . import _abi, _native
 from . import grid as grid_mod
 from ._torch import ptr, stream_ptr
-from .mlp import apply_mlp
+from .mlp import apply_mlp, row_stride
 
 
 def gaussian_taps(ksize: int, sigma: float) -> np.ndarray:
@@ -221,8 +221,8 @@ class _FineGeometry(torch.autograd.Function):
         _abi.call_struct("vx_fine_compact", c, st)
 
         xdt = torch.bfloat16 if fr.bf16 else torch.float32
-        X1 = torch.empty((S2, fr.d1), dtype=xdt, device=dev)
-        X2 = torch.empty((S2, fr.d2a), dtype=xdt, device=dev)
+        X1 = torch.empty((S2, fr.ld1), dtype=xdt, device=dev)
+        X2 = torch.empty((S2, fr.ld2), dtype=xdt, device=dev)
         normal2 = torch.empty((S2, 3), dtype=torch.float32, device=dev)
         f = _abi.FineFeaturesArgs()
         f.n_rows, f.ray2, f.pts2, f.viewdirs = S2, ptr(ray2), ptr(pts2), ptr(fr.viewdirs)
@@ -232,7 +232,7 @@ class _FineGeometry(torch.autograd.Function):
         else:
             f.k0_f32 = ptr(k0_grid)
         f.cfg = fr.cfg
-        f.ld1, f.ld2 = fr.d1, fr.d2a
+        f.ld1, f.ld2 = fr.ld1, fr.ld2
         f.X1, f.X2, f.out_bf16, f.normal_out = ptr(X1), ptr(X2), int(fr.bf16), ptr(normal2)
         _abi.call_struct("vx_fine_features", f, st)
 
@@ -252,8 +252,8 @@ class _FineGeometry(torch.autograd.Function):
         X, Y, Z = fr.geom.X, fr.geom.Y, fr.geom.Z
         xdt = torch.bfloat16 if fr.bf16 else torch.float32
         S2, N = fr.S2, fr.n_rays
-        dX1 = torch.zeros((S2, fr.d1), dtype=xdt, device=dev) if dX1 is None else dX1.contiguous()
-        dX2 = torch.zeros((S2, fr.d2a), dtype=xdt, device=dev) if dX2 is None else dX2.contiguous()
+        dX1 = torch.zeros((S2, fr.ld1), dtype=xdt, device=dev) if dX1 is None else dX1.contiguous()
+        dX2 = torch.zeros((S2, fr.ld2), dtype=xdt, device=dev) if dX2 is None else dX2.contiguous()
         dw2 = torch.zeros(S2, dtype=torch.float32, device=dev) if dw2 is None else dw2.contiguous().float()
         dlast = torch.zeros(N, dtype=torch.float32, device=dev) if dlast is None else dlast.contiguous().float()
         d_sdf_s = torch.zeros((X, Y, Z), dtype=torch.float32, device=dev)
@@ -266,7 +266,7 @@ class _FineGeometry(torch.autograd.Function):
         b.max_steps, b.rec, b.dw_slot, b.n1 = fr.max_steps, ptr(fr.rec), ptr(fr.dw_slot), ptr(fr.n1)
         b.alphainv_last, b.d_last = ptr(fr.alphainv_last), ptr(dlast)
         b.pts2, b.slot2, b.dw2 = ptr(fr.pts2), ptr(fr.slot2), ptr(dw2)
-        b.cfg, b.ld1, b.ld2 = fr.cfg, fr.d1, fr.d2a
+        b.cfg, b.ld1, b.ld2 = fr.cfg, fr.ld1, fr.ld2
         b.dX1, b.dX2, b.in_bf16 = ptr(dX1), ptr(dX2), int(fr.bf16)
         b.d_sdf_smooth, b.d_k0 = ptr(d_sdf_s), ptr(d_k0)
         _abi.call_struct("vx_fine_backward", b, st)
@@ -639,18 +639,26 @@ class Voxurf(nn.Module):
             fr.k0_bf16 = self._k0_shadow
         fr.d1 = self.dim0
         fr.d2a = self.k_dim0 - (3 if self.k_res else 0)
+        # MLP input rows, zero-padded to the stride of the MLP engine; the
+        # k-branch rows keep 3 columns after the features for the rgbnet
+        # logits (k_res), which the rgbnet forward writes there directly
+        xdt = torch.bfloat16 if fr.bf16 else torch.float32
+        fr.ld1 = row_stride(fr.d1, xdt)
+        fr.ld2 = row_stride(self.k_dim0 if self.use_rgb_k else fr.d2a, xdt)
         fr.render_extras = bool(render_kwargs.get("render_depth", False) or render_kwargs.get("render_grad", False))
         X1, X2a, w2, alphainv_last, normal2, alpha2 = _FineGeometry.apply(self.sdf.grid, self.k0.grid, fr)
         fr.normal2 = normal2
 
-        rgb_logit = self._run_mlp(self.rgbnet, X1)
+        direct_k = self.use_rgb_k and (not self.k_res or self.k_detach_1)
+        logit_cols = X2a[:, fr.d2a:fr.d2a + 3] if (direct_k and self.k_res) else None
+        rgb_logit = self._run_mlp(self.rgbnet, X1, cols=logit_cols)
         rgb = torch.sigmoid(rgb_logit)
         k_rgb_logit = None
         if self.use_rgb_k:
-            feats = [X2a]
-            if self.k_res:
-                feats.append(rgb_logit.detach().to(X2a.dtype) if self.k_detach_1 else rgb_logit.to(X2a.dtype))
-            k_in = torch.cat(feats, -1) if len(feats) > 1 else X2a
+            if direct_k:
+                k_in = X2a          # features, then (k_res) the detached logits written by the rgbnet forward
+            else:
+                k_in = torch.cat([X2a[:, :fr.d2a], rgb_logit.to(X2a.dtype)], -1)
             k_out = self._run_mlp(self.k_rgbnet, k_in)
             k_rgb_logit = (rgb_logit.detach() if self.k_detach_2 else rgb_logit) + k_out
         bg = render_kwargs["bg"]
@@ -686,6 +694,6 @@ class Voxurf(nn.Module):
         self._last_frame = fr
         return ret
 
-    def _run_mlp(self, net: nn.Sequential, x: torch.Tensor) -> torch.Tensor:
+    def _run_mlp(self, net: nn.Sequential, x: torch.Tensor, cols: torch.Tensor | None = None) -> torch.Tensor:
         # x is FP32 or BF16 (the compute dtype); logits come back in FP32
-        return apply_mlp(net, x).float()
+        return apply_mlp(net, x, cols)
