@@ -141,6 +141,30 @@ def neus_alpha(viewdirs, ray_id, dist, sdf, gradients, inv_s):
     return raw.clip(0.0, 1.0).squeeze(-1)
 
 
+def mlp_relu_ties(net, x, device_masks=None, tie=1e-6):
+    """net(x) for a Linear/ReLU stack (voxurf_fine.py:132-151), returning
+    (output, ties).  With device_masks (one [S, W] bool per hidden layer: the
+    device's ReLU decisions, rows in the same order), a pre-activation within
+    tie * (the layer's RMS) of zero takes the device's decision instead of its
+    own sign: there FP32 and FP64 legitimately disagree on the ReLU, like a
+    fast_color_thres tie; `ties` counts them."""
+    lin = [m for m in net.modules() if isinstance(m, nn.Linear)]
+    h, ties = x, 0
+    for i, m in enumerate(lin):
+        h = F.linear(h, m.weight, m.bias)
+        if i == len(lin) - 1:
+            break
+        if device_masks is None:
+            h = torch.relu(h)
+            continue
+        hd = h.detach()
+        near = hd.abs() <= tie * hd.pow(2).mean().sqrt()
+        keep = torch.where(near, device_masks[i].to(hd.device), hd > 0)
+        ties += int(near.sum())
+        h = h * keep.to(h.dtype)
+    return h, ties
+
+
 def pe(x, freq):
     emb = (x.unsqueeze(-1) * freq).flatten(-2)
     return torch.cat([x, emb.sin(), emb.cos()], -1)
@@ -201,9 +225,14 @@ class OracleFine(nn.Module):
             err = err[nonempty_mask.cpu().repeat(3, 1, 1, 1, 1)]
         return (err ** 2).mean() * weight
 
-    def forward(self, rays_o, rays_d, viewdirs, global_step=None, **rk):
+    def forward(self, rays_o, rays_d, viewdirs, global_step=None, relu_device=None, relu_tie=1e-6, **rk):
+        """relu_device: optional {"rgbnet": masks, "k_rgbnet": masks}, the
+        device's ReLU decisions of the same shaded rows (see mlp_relu_ties);
+        the tie count lands in self.relu_ties."""
         dt = self.dtype
         N = len(rays_o)
+        rd = relu_device or {}
+        self.relu_ties = 0
         stepdist = f32(rk["stepsize"] * np.float32(self.voxel_size))
         ru = RenderUtilsOracle
         ray_pts, mask_outbbox, ray_id, step_id, _, _, _ = ru.sample_pts_on_rays(
@@ -254,7 +283,8 @@ class OracleFine(nn.Module):
             parts.append(sdf[:, None])
         parts += [all_feat, all_grad]
         rgb_feat = torch.cat(parts, -1)
-        rgb_logit = self.rgbnet(rgb_feat)
+        rgb_logit, t1 = mlp_relu_ties(self.rgbnet, rgb_feat, rd.get("rgbnet"), relu_tie)
+        self.relu_ties += t1
         rgb = torch.sigmoid(rgb_logit)
         out = {"alphainv_cum": alphainv_last, "weights": weights, "raw_rgb": rgb, "raw_alpha": alpha,
                "gradient": gradient, "ray_id": ray_id, "step_id": step_id, "s_val": s_val, "rgb_feat": rgb_feat}
@@ -273,7 +303,9 @@ class OracleFine(nn.Module):
             if self.k_res:
                 k_feat = torch.cat([k_feat, detached if self.k_detach_1 else rgb_logit], -1)
             base = detached if self.k_detach_2 else rgb_logit
-            k_rgb = torch.sigmoid(base + self.k_rgbnet(k_feat))
+            k_out, t2 = mlp_relu_ties(self.k_rgbnet, k_feat, rd.get("k_rgbnet"), relu_tie)
+            self.relu_ties += t2
+            k_rgb = torch.sigmoid(base + k_out)
             k_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * k_rgb) \
                 + alphainv_last[..., None] * bg
             trace("k_rgb in [0,1]", (k_marched >= 0) & (k_marched <= 1))
@@ -353,12 +385,14 @@ class OracleCoarse(nn.Module):
         self.s_val = model.s_val.clone().float().cpu()
         self.mask = _mask_state(model)
 
-    def forward(self, rays_o, rays_d, viewdirs, global_step=None, device_keep=None, tie_rel=1e-5, **rk):
+    def forward(self, rays_o, rays_d, viewdirs, global_step=None, device_keep=None, tie_rel=1e-5, relu_device=None,
+                relu_tie=1e-6, **rk):
         """device_keep: optional set of (ray_id, step_id) pairs that a device
         run kept after the fast_color_thres test.  A sample whose weight is
         within tie_rel (relative) of the threshold (a tie at FP32 precision)
         then takes the device's decision, so that both sides shade the same
-        set."""
+        set.  relu_device: the device's ReLU decisions of the rgbnet hidden
+        layers for the same shaded rows (see mlp_relu_ties)."""
         dt = self.dtype
         N = len(rays_o)
         stepdist = f32(rk["stepsize"] * np.float32(self.voxel_size))
@@ -406,7 +440,8 @@ class OracleCoarse(nn.Module):
         if self.geo_rgb_dim == 3:
             normal = gradient / (gradient.norm(dim=-1, keepdim=True) + 1e-5)
             rgb_feat = torch.cat([rgb_feat, normal], -1)
-        rgb = torch.sigmoid(self.rgbnet(rgb_feat))
+        logit, self.relu_ties = mlp_relu_ties(self.rgbnet, rgb_feat, relu_device, relu_tie)
+        rgb = torch.sigmoid(logit)
         rgb_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * rgb)
         cum_w = torch.zeros([N, 1], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1))
         rgb_marched = rgb_marched + (1 - cum_w) * rk["bg"]

@@ -82,66 +82,90 @@ def _params(obj_sdf, obj_k0, rgbnet, k_rgbnet):
     return p
 
 
+class _Lazy:
+    """A module fixture's oracle result, computed on first use: the first
+    caller (the FP32 test) passes the device's ReLU decisions for the
+    oracle's near-tie pre-activations; later callers reuse the result."""
+
+    def __init__(self, fn):
+        self.fn, self.val = fn, None
+
+    def get(self, relu_device=None):
+        if self.val is None:
+            self.val = self.fn(relu_device)
+        return self.val
+
+
+def _device_relu(model):
+    from voxurf_gb300.mlp import last_relu_masks
+
+    return {"rgbnet": [m.cpu() for m in last_relu_masks(model.rgbnet)],
+            "k_rgbnet": [m.cpu() for m in last_relu_masks(model.k_rgbnet)]}
+
+
+MAX_RELU_TIES = 64   # pre-activations within 1e-6 of the layer RMS from zero (a handful per batch)
+
+
 @pytest.fixture(scope="module")
 def fine256(cuda):
     """The FP64 oracle's step on the 384-ray sub-batch of the 256^3 bench
     workload: outputs, gradients and the parameter update of one full
     training step (TV add-grad weight / N_rays, utils.Adam lr 1e-3)."""
-    model = configs.build_fine_model(256, "fp32", device=cuda, seed=0, mask_voxels=6.4)
     full = _bench_batch(BENCH_RAYS, BENCH_BATCHES, 0)
     rays = tuple(a[:SUB] for a in full)
-    orc = OracleFine(model, dtype=torch.float64)
-    world_max = float(model.world_size.max())
-    model32 = model
-    del model
-    before = _params(orc.sdf_grid, orc.k0_grid, orc.rgbnet, orc.k_rgbnet)
-    ro, rd, vd, tgt = (torch.from_numpy(a) for a in rays)
-    ret = orc(ro, rd, vd, global_step=1, **RK)
-    loss = train_loss(ret, tgt.double())
-    loss.backward()
-    grads = _oracle_grads(orc)
-    # the reference algorithm's own FP32 error on this batch (same step in
-    # FP32): the FP32 bars are max(1e-5, 3x this)
-    orc32 = OracleFine(model32, dtype=torch.float32)
-    del model32
-    torch.cuda.empty_cache()
-    train_loss(orc32(ro, rd, vd, global_step=1, **RK), tgt).backward()
-    ref32 = {k: _rel_l2(v, grads[k]) for k, v in _oracle_grads(orc32).items()}
-    tv_add_grad(orc32.sdf_grid, 1e-4 / SUB, world_max, True)
-    tv_add_grad(orc32.k0_grid, 1e-4 / SUB, world_max, True)
-    UtilsAdam([([orc32.sdf_grid], 1e-3), ([orc32.k0_grid], 1e-3), (list(orc32.rgbnet.parameters()), 1e-3),
-               (list(orc32.k_rgbnet.parameters()), 1e-3)], betas=(0.9, 0.99)).step()
-    after32 = _params(orc32.sdf_grid, orc32.k0_grid, orc32.rgbnet, orc32.k_rgbnet)
-    del orc32
-    tv_add_grad(orc.sdf_grid, 1e-4 / SUB, world_max, True)
-    tv_add_grad(orc.k0_grid, 1e-4 / SUB, world_max, True)
-    opt = UtilsAdam([([orc.sdf_grid], 1e-3), ([orc.k0_grid], 1e-3), (list(orc.rgbnet.parameters()), 1e-3),
-                     (list(orc.k_rgbnet.parameters()), 1e-3)], betas=(0.9, 0.99))
-    opt.step()
-    after = _params(orc.sdf_grid, orc.k0_grid, orc.rgbnet, orc.k_rgbnet)
-    delta = {k: after[k] - before[k] for k in before}
-    # the reference algorithm's own FP32 update error, measured like the GPU's
-    # (against the FP64 update rounded to FP32 storage)
-    ref32_update = {k: _rel_l2(after32[k] - before[k], (before[k] + delta[k]).float().double() - before[k])
-                    for k in before}
-    del after32
-    out = {"rays": rays, "full": full, "ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in ret.items()},
-           "loss": float(loss.item()), "grads": grads, "ref32": ref32, "ref32_update": ref32_update,
-           "before": before, "delta": delta}
-    del orc, opt, after
-    return out
+
+    def run(relu_device):
+        model = configs.build_fine_model(256, "fp32", device=cuda, seed=0, mask_voxels=6.4)
+        orc = OracleFine(model, dtype=torch.float64)
+        world_max = float(model.world_size.max())
+        model32 = model
+        del model
+        before = _params(orc.sdf_grid, orc.k0_grid, orc.rgbnet, orc.k_rgbnet)
+        ro, rd, vd, tgt = (torch.from_numpy(a) for a in rays)
+        ret = orc(ro, rd, vd, global_step=1, relu_device=relu_device, **RK)
+        ties = orc.relu_ties
+        loss = train_loss(ret, tgt.double())
+        loss.backward()
+        grads = _oracle_grads(orc)
+        # the reference algorithm's own FP32 error on this batch (same step in
+        # FP32): the FP32 bars are max(1e-5, 3x this)
+        orc32 = OracleFine(model32, dtype=torch.float32)
+        del model32
+        torch.cuda.empty_cache()
+        train_loss(orc32(ro, rd, vd, global_step=1, **RK), tgt).backward()
+        ref32 = {k: _rel_l2(v, grads[k]) for k, v in _oracle_grads(orc32).items()}
+        tv_add_grad(orc32.sdf_grid, 1e-4 / SUB, world_max, True)
+        tv_add_grad(orc32.k0_grid, 1e-4 / SUB, world_max, True)
+        UtilsAdam([([orc32.sdf_grid], 1e-3), ([orc32.k0_grid], 1e-3), (list(orc32.rgbnet.parameters()), 1e-3),
+                   (list(orc32.k_rgbnet.parameters()), 1e-3)], betas=(0.9, 0.99)).step()
+        after32 = _params(orc32.sdf_grid, orc32.k0_grid, orc32.rgbnet, orc32.k_rgbnet)
+        del orc32
+        tv_add_grad(orc.sdf_grid, 1e-4 / SUB, world_max, True)
+        tv_add_grad(orc.k0_grid, 1e-4 / SUB, world_max, True)
+        opt = UtilsAdam([([orc.sdf_grid], 1e-3), ([orc.k0_grid], 1e-3), (list(orc.rgbnet.parameters()), 1e-3),
+                         (list(orc.k_rgbnet.parameters()), 1e-3)], betas=(0.9, 0.99))
+        opt.step()
+        after = _params(orc.sdf_grid, orc.k0_grid, orc.rgbnet, orc.k_rgbnet)
+        delta = {k: after[k] - before[k] for k in before}
+        # the reference algorithm's own FP32 update error, measured like the
+        # GPU's (against the FP64 update rounded to FP32 storage)
+        ref32_update = {k: _rel_l2(after32[k] - before[k], (before[k] + delta[k]).float().double() - before[k])
+                        for k in before}
+        return {"ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in ret.items()},
+                "loss": float(loss.item()), "grads": grads, "ref32": ref32, "ref32_update": ref32_update,
+                "before": before, "delta": delta, "relu_ties": ties}
+
+    return {"rays": rays, "full": full, "oracle": _Lazy(run)}
 
 
 def test_fine256_fp32_step_matches_fp64_oracle(cuda, fine256):
     model = configs.build_fine_model(256, "fp32", device=cuda, seed=0, mask_voxels=6.4)
-    o = fine256["ret"]
     # the bench's full 8192-ray forward: its first 384 rays equal the oracle's
     # (rays are independent until the loss)
     full = [torch.from_numpy(a).to(cuda) for a in fine256["full"][:3]]
     with torch.no_grad():
         g = model(*full, global_step=1, **RK)
-    err = (g["rgb_marched"][:SUB].double().cpu() - o["rgb_marched"]).abs().max().item()
-    assert err <= 1e-5, err
+    rgb_full = g["rgb_marched"][:SUB].double().cpu()
     del g
     tr = FineTrainer(model, n_rays=SUB)
     grads = {}
@@ -149,28 +173,34 @@ def test_fine256_fp32_step_matches_fp64_oracle(cuda, fine256):
     ro, rd, vd, tgt = (torch.from_numpy(a).to(cuda) for a in fine256["rays"])
     loss, ret = tr.step(ro, rd, vd, tgt, RK, global_step=1)
     torch.cuda.synchronize()
+    o = fine256["oracle"].get(_device_relu(model))
+    fo = o
+    o = fo["ret"]
+    assert fo["relu_ties"] <= MAX_RELU_TIES
+    err = (rgb_full - o["rgb_marched"]).abs().max().item()
+    assert err <= 1e-5, err
     assert ret["weights"].numel() == o["weights"].numel() > 2000
     assert torch.equal(ret["ray_id"].long().cpu(), o["ray_id"])
     assert torch.equal(model._last_frame.step2.long().cpu(), o["step_id"])
     for key in ("rgb_marched", "rgb_marched0"):
         err = (ret[key].double().detach().cpu() - o[key]).abs().max().item()
         assert err <= 1e-5, (key, err)
-    assert abs(float(loss) - fine256["loss"]) <= 1e-6 * abs(fine256["loss"])
-    errs = {name: _rel_l2(grads[name], ref) for name, ref in fine256["grads"].items()}
-    print("fp32 step vs FP64 (256^3 bench workload):", errs, "reference fp32:", fine256["ref32"])
+    assert abs(float(loss) - fo["loss"]) <= 1e-6 * abs(fo["loss"])
+    errs = {name: _rel_l2(grads[name], ref) for name, ref in fo["grads"].items()}
+    print("fp32 step vs FP64 (256^3 bench workload):", errs, "reference fp32:", fo["ref32"])
     for name, err in errs.items():
-        assert err <= max(1e-5, 3 * fine256["ref32"][name]), (name, err, fine256["ref32"][name])
+        assert err <= max(1e-5, 3 * fo["ref32"][name]), (name, err, fo["ref32"][name])
     # the update of the whole step, against the oracle's updated parameters
     # rounded to the FP32 storage both sides keep them in (otherwise one ulp
     # of a parameter near 1, 6e-8, would count against a 1e-3 Adam step)
     after = _params(model.sdf.grid, model.k0.grid, model.rgbnet, model.k_rgbnet)
     uerr = {}
-    for name, ref in fine256["delta"].items():
-        p0 = fine256["before"][name]
+    for name, ref in fo["delta"].items():
+        p0 = fo["before"][name]
         uerr[name] = _rel_l2(after[name] - p0, (p0 + ref).float().double() - p0)
-    print("fp32 update vs FP64:", uerr, "reference fp32:", fine256["ref32_update"])
+    print("fp32 update vs FP64:", uerr, "reference fp32:", fo["ref32_update"])
     for name, err in uerr.items():
-        assert err <= max(1e-5, 3 * fine256["ref32_update"][name]), ("update", name, err)
+        assert err <= max(1e-5, 3 * fo["ref32_update"][name]), ("update", name, err)
 
 
 # Bounds of the BF16 graph-replayed step against FP64 on this batch, about
@@ -186,22 +216,23 @@ def test_fine256_bf16_graphed_step_vs_fp64_oracle(cuda, fine256):
     ro, rd, vd, tgt = (torch.from_numpy(a).to(cuda) for a in fine256["rays"])
     with torch.no_grad():
         g = model(ro, rd, vd, global_step=1, **RK)
-    o = fine256["ret"]
+    fo = fine256["oracle"].get()
+    o = fo["ret"]
     errs = {"rgb": (g["rgb_marched"].double().cpu() - o["rgb_marched"]).abs().max().item()}
     tr = FineTrainer(model, n_rays=SUB, graphed=True)
     grads = {}
     _grab_grads(tr, grads)
     loss, _ = tr.step(ro, rd, vd, tgt, RK, global_step=1)
     torch.cuda.synchronize()
-    errs["loss"] = abs(float(loss) - fine256["loss"]) / abs(fine256["loss"])
-    for name, ref in fine256["grads"].items():
+    errs["loss"] = abs(float(loss) - fo["loss"]) / abs(fo["loss"])
+    for name, ref in fo["grads"].items():
         errs[name] = _rel_l2(grads[name], ref)
     print("bf16 graphed step vs FP64 (256^3 bench workload):", errs)
     assert errs["rgb"] <= BF16_BOUNDS["rgb"]
     assert errs["loss"] <= BF16_BOUNDS["loss"]
     assert errs["sdf"] <= BF16_BOUNDS["sdf"]
     assert errs["k0"] <= BF16_BOUNDS["k0"]
-    for name in fine256["grads"]:
+    for name in fo["grads"]:
         if "rgbnet" in name:
             assert errs[name] <= BF16_BOUNDS["mlp"], (name, errs[name])
 
@@ -235,57 +266,66 @@ def _long_model(cuda, precision):
 def long384(cuda):
     """The FP64 oracle's forward + backward on the long-ray subset of the
     384^3 bench workload (global_step 0: s-density 0.05)."""
-    model = _long_model(cuda, "fp32")
     rays = _long_ray_subset()
-    orc = OracleFine(model, dtype=torch.float64)
-    del model
-    torch.cuda.empty_cache()
     rk = dict(RK, stepsize=0.25)
-    o = orc(*(torch.from_numpy(a) for a in rays[:3]), global_step=0, **rk)
-    ol = train_loss(o, torch.from_numpy(rays[3]).double())
-    ol.backward()
-    grads = {"sdf": orc.sdf_grid.grad, "k0": orc.k0_grid.grad,
-             "rgbnet": [q.grad for q in orc.rgbnet.parameters()],
-             "k_rgbnet": [q.grad for q in orc.k_rgbnet.parameters()]}
-    # the reference algorithm's own FP32 error on this batch
-    model = _long_model(cuda, "fp32")
-    orc32 = OracleFine(model, dtype=torch.float32)
-    del model
-    torch.cuda.empty_cache()
-    train_loss(orc32(*(torch.from_numpy(a) for a in rays[:3]), global_step=0, **rk),
-               torch.from_numpy(rays[3])).backward()
-    ref32 = {"sdf": _rel_l2(orc32.sdf_grid.grad, grads["sdf"]), "k0": _rel_l2(orc32.k0_grid.grad, grads["k0"])}
-    for net in ("rgbnet", "k_rgbnet"):
-        for (n, q), r in zip(getattr(orc32, net).named_parameters(), grads[net]):
-            ref32[net + "." + n] = _rel_l2(q.grad, r)
-    return {"rays": rays, "rk": rk, "ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in o.items()},
-            "grads": grads, "ref32": ref32}
+
+    def run(relu_device):
+        model = _long_model(cuda, "fp32")
+        orc = OracleFine(model, dtype=torch.float64)
+        del model
+        torch.cuda.empty_cache()
+        o = orc(*(torch.from_numpy(a) for a in rays[:3]), global_step=0, relu_device=relu_device, **rk)
+        ties = orc.relu_ties
+        ol = train_loss(o, torch.from_numpy(rays[3]).double())
+        ol.backward()
+        grads = {"sdf": orc.sdf_grid.grad, "k0": orc.k0_grid.grad,
+                 "rgbnet": [q.grad for q in orc.rgbnet.parameters()],
+                 "k_rgbnet": [q.grad for q in orc.k_rgbnet.parameters()]}
+        del orc
+        # the reference algorithm's own FP32 error on this batch
+        model = _long_model(cuda, "fp32")
+        orc32 = OracleFine(model, dtype=torch.float32)
+        del model
+        torch.cuda.empty_cache()
+        train_loss(orc32(*(torch.from_numpy(a) for a in rays[:3]), global_step=0, **rk),
+                   torch.from_numpy(rays[3])).backward()
+        ref32 = {"sdf": _rel_l2(orc32.sdf_grid.grad, grads["sdf"]),
+                 "k0": _rel_l2(orc32.k0_grid.grad, grads["k0"])}
+        for net in ("rgbnet", "k_rgbnet"):
+            for (n, q), r in zip(getattr(orc32, net).named_parameters(), grads[net]):
+                ref32[net + "." + n] = _rel_l2(q.grad, r)
+        return {"ret": {k: (v.detach() if torch.is_tensor(v) else v) for k, v in o.items()},
+                "grads": grads, "ref32": ref32, "relu_ties": ties}
+
+    return {"rays": rays, "rk": rk, "oracle": _Lazy(run)}
 
 
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
 def test_long_rays_384_vs_fp64_oracle(cuda, precision, long384):
     model = _long_model(cuda, precision)
-    rays, rk, o = long384["rays"], long384["rk"], long384["ret"]
+    rays, rk = long384["rays"], long384["rk"]
     T = lambda a: torch.from_numpy(a).to(cuda)  # noqa: E731
     g = model(T(rays[0]), T(rays[1]), T(rays[2]), global_step=0, **rk)
     gl = train_loss(g, T(rays[3]))
     gl.backward()
     torch.cuda.synchronize()
-    og = long384["grads"]
+    lo = long384["oracle"].get(_device_relu(model) if precision == "fp32" else None)
+    o, og = lo["ret"], lo["grads"]
+    assert lo["relu_ties"] <= MAX_RELU_TIES
     err = (g["rgb_marched"].detach().double().cpu() - o["rgb_marched"]).abs().max().item()
     errs = {"rgb": err, "sdf": _rel_l2(model.sdf.grid.grad, og["sdf"]), "k0": _rel_l2(model.k0.grid.grad, og["k0"])}
     for net in ("rgbnet", "k_rgbnet"):
         for (n, p), q in zip(getattr(model, net).named_parameters(), og[net]):
             errs[net + "." + n] = _rel_l2(p.grad, q)
     print(precision, "384^3 long rays vs FP64:", errs, "shaded", o["weights"].numel(), "reference fp32:",
-          long384["ref32"])
+          lo["ref32"], "relu ties", lo["relu_ties"])
     assert o["weights"].numel() > 1000
     if precision == "fp32":
         assert torch.equal(g["ray_id"].long().cpu(), o["ray_id"])
         assert err <= 1e-5
         for k, v in errs.items():
             if k != "rgb":
-                assert v <= max(1e-5, 3 * long384["ref32"][k]), (k, v, long384["ref32"][k])
+                assert v <= max(1e-5, 3 * lo["ref32"][k]), (k, v, lo["ref32"][k])
     else:
         assert err <= 1e-3
         assert errs["sdf"] <= BF16_BOUNDS["sdf"] and errs["k0"] <= BF16_BOUNDS["k0"]
@@ -315,10 +355,16 @@ def test_coarse_eikonal_bench_batch_vs_fp64_oracle(cuda, precision, rgb_tol, los
     gl.backward()
     fr = model._last_frame
     keep = set(zip(fr.ray2.long().cpu().tolist(), fr.step2.long().cpu().tolist()))
+    from voxurf_gb300.mlp import last_relu_masks
+
+    dev_relu = last_relu_masks(model.rgbnet) if precision == "fp32" else None
+    dev_relu = [m.cpu() for m in dev_relu] if dev_relu is not None else None
 
     def run_oracle(dtype):
         orc = OracleCoarse(model, dtype=dtype)
-        o = orc(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, device_keep=keep, tie_rel=1e-3, **rk)
+        o = orc(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, device_keep=keep, tie_rel=1e-3,
+                relu_device=dev_relu if dtype == torch.float64 else None, **rk)
+        assert orc.relu_ties <= MAX_RELU_TIES
         o_eik = ((o["gradient"].norm(dim=-1) - 1.0) ** 2).mean()
         ol = train_loss(o, torch.from_numpy(tgt).to(dtype), weight_rgb0=0) + 0.1 * o_eik
         ol.backward()

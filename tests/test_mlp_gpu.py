@@ -40,11 +40,18 @@ def test_mlp_fp32_matches_autograd(cuda, M, d_in, width, depth):
 
 
 def test_mlp_bf16_matches_torch_autocast(cuda):
-    """BF16 path against torch's own BF16 autocast of the same nn.Sequential
-    (both round operands to BF16 and accumulate in FP32)."""
+    """BF16 path (tcgen05 engine) against the FP64 result: each gradient within
+    3e-2, or within 1.5x of torch's own BF16 autocast of the same
+    nn.Sequential, whichever is larger (both round operands to BF16 and
+    accumulate in FP32)."""
     net = _net(70, 192, 4, 0).to(cuda)
     x = torch.randn(4096, 70, device=cuda)
     gy = torch.randn(4096, 3, device=cuda)
+    net64 = _net(70, 192, 4, 0).to(cuda).double()
+    net64.load_state_dict({k: v.double() for k, v in net.state_dict().items()})
+    y64 = net64(x.bfloat16().double())
+    (y64 * gy.double()).sum().backward()
+    g64 = [p.grad.clone() for p in net64.parameters()]
     with torch.autocast("cuda", dtype=torch.bfloat16):
         y_ref = net(x.bfloat16())
     (y_ref.float() * gy).sum().backward()
@@ -54,6 +61,8 @@ def test_mlp_bf16_matches_torch_autocast(cuda):
     y16 = apply_mlp(net, x.bfloat16()).float()
     (y16 * gy).sum().backward()
     assert float((y16 - y_ref.float()).abs().max().detach()) < 2e-2
-    for p, r in zip(net.parameters(), g_ref):
+    for p, r, t in zip(net.parameters(), g64, g_ref):
         assert p.grad.dtype == torch.float32
-        assert float((p.grad - r).norm() / r.norm()) < 3e-2
+        e = float((p.grad.double() - r).norm() / r.norm())
+        et = float((t.double() - r).norm() / r.norm())
+        assert e <= max(3e-2, 1.5 * et), (e, et)

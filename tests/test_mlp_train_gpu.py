@@ -8,8 +8,12 @@ Two references on the same seeded inputs:
   layer's weights and dy as BF16 hi + lo pairs): logits, dX and every
   weight/bias gradient within rel-L2 3e-3 (the FP32 tensor-core sums differ
   from FP64 in order, which moves a few BF16 roundings by one unit);
-* torch autograd of the unrounded FP32 MLP (what the reference runs):
-  rel-L2 within 3e-2 (the cost of BF16 operands).
+* torch autograd of the unrounded FP32 MLP (what the reference runs): each
+  output's rel-L2 error within 3e-2 or within 1.5x the error of torch's own
+  BF16 autocast of the same MLP against the same FP32 result, whichever is
+  larger (the input gradient is a sum of products of either sign, which
+  magnifies the BF16 rounding of its operands to several percent in any
+  BF16 implementation).
 Shapes: the fine rgbnet / k_rgbnet (192 wide, 3 hidden layers, K0 80 / 64),
 the coarse rgbnet (128 wide, 2 hidden layers), the test widths 64 and 32;
 row counts of one partial tile, one tile per CTA, and several tiles per CTA
@@ -72,11 +76,19 @@ def _emulate(net, X, dY):
     return logits, dX, grads
 
 
-def _autograd32(net, X, dY):
+def _autograd32(net, X, dY, autocast=False):
+    """torch autograd of net on X (FP32, or torch's BF16 autocast on the GPU)."""
     net32 = [m for m in net.modules() if isinstance(m, nn.Linear)]
+    for m in net32:
+        m.weight.grad = m.bias.grad = None
     x = X.float().clone().requires_grad_(True)
-    y = net.float()(x)
-    y.backward(dY.float())
+    if autocast:
+        with torch.autocast("cuda", dtype=torch.bfloat16):
+            y = net(x)
+        y = y.float()
+    else:
+        y = net.float()(x)
+    y.backward(dY.float().to(y.device))
     L = len(net32) - 1
     grads = {"Wh": net32[L].weight.grad.clone(), "bh": net32[L].bias.grad.clone()}
     for l in range(L):
@@ -122,10 +134,17 @@ def test_mlp_train_matches_torch(cuda, W, L, d_in, K0, n):
     for k in names:
         assert _rel(got[k], e_grads[k]) <= 3e-3, (k, _rel(got[k], e_grads[k]))
     a_logits, a_dX, a_grads = _autograd32(net.cpu(), X[:, :d_in].float(), dY)
-    assert _rel(logits, a_logits) <= 3e-2
-    assert _rel(dX[:, :d_in], a_dX) <= 3e-2
+    net.to(cuda)
+    t_logits, t_dX, t_grads = _autograd32(net, X[:, :d_in].float().to(cuda), dY, autocast=True)
+
+    def bound(ours, torch_bf16, truth, what):
+        e, et = _rel(ours, truth), _rel(torch_bf16, truth)
+        assert e <= max(3e-2, 1.5 * et), (what, e, et)
+
+    bound(logits, t_logits, a_logits, "logits")
+    bound(dX[:, :d_in], t_dX, a_dX, "dX")
     for k in names:
-        assert _rel(got[k], a_grads[k]) <= 3e-2, (k, _rel(got[k], a_grads[k]))
+        bound(got[k], t_grads[k], a_grads[k], k)
 
 
 def test_mlp_train_device_row_count_and_bf16_dx(cuda):

@@ -130,14 +130,23 @@ def test_alpha2weight_fwd_bwd(cuda, n_rays, max_len, alpha_hi):
     assert np.array_equal(gis[keep], i_s[keep])
     assert np.array_equal(gie[keep], i_e[keep])
     samp_keep = keep[ray_id]
-    # against the FP64 scan (the GPU carries T in FP64 and rounds once)
+    # against the FP64 scan: segments of more than 512 samples carry T in FP64
+    # and round once (3e-7); shorter ones carry it in FP32 through the warp
+    # prefix products and the chunk carries (2e-6)
     w64, T64, last64, _, _ = cref.alpha2weight(alpha.astype(np.float64), ray_id, n_rays)
-    np.testing.assert_allclose(gw[samp_keep], w64[samp_keep], rtol=3e-7, atol=1e-12)
-    np.testing.assert_allclose(gT[samp_keep], T64[samp_keep], rtol=3e-7, atol=1e-12)
-    np.testing.assert_allclose(glast[keep], last64[keep], rtol=3e-7, atol=1e-12)
+    seg_len = full_end - np.searchsorted(ray_id, np.arange(n_rays))
+    long_ray = seg_len > 512
+    for sel_r, rtol in ((keep & long_ray, 3e-7), (keep & ~long_ray, 2e-6)):
+        sel_s = sel_r[ray_id]
+        errs = [float(np.max(np.abs(a[sel_s] - b[sel_s]) / (np.abs(b[sel_s]) + 1e-30), initial=0.0))
+                for a, b in ((gw, w64), (gT, T64))]
+        print("alpha2weight vs FP64", "long" if rtol < 1e-6 else "short", errs)
+        np.testing.assert_allclose(gw[sel_s], w64[sel_s], rtol=rtol, atol=1e-12)
+        np.testing.assert_allclose(gT[sel_s], T64[sel_s], rtol=rtol, atol=1e-12)
+        np.testing.assert_allclose(glast[sel_r], last64[sel_r], rtol=rtol, atol=1e-12)
     # against the reference's serial float loop: its own rounding grows with
     # the ray length (about sqrt(n) ulps)
-    rt = 2e-6 if max_len <= 700 else 2e-5
+    rt = 4e-6 if max_len <= 700 else 2e-5
     np.testing.assert_allclose(gw[samp_keep], w[samp_keep], rtol=rt, atol=1e-9)
     np.testing.assert_allclose(gT[samp_keep], T[samp_keep], rtol=rt, atol=1e-9)
     np.testing.assert_allclose(glast[keep], last[keep], rtol=rt, atol=1e-9)
@@ -151,7 +160,8 @@ def test_alpha2weight_fwd_bwd(cuda, n_rays, max_len, alpha_hi):
     got = ru.alpha2weight_backward(to(alpha), to(w), to(T), to(last), to(i_s), to(i_e), n_rays, to(grad_w),
                                    to(grad_last)).cpu().numpy()
     scale = np.abs(ref).max() + 1e-12
-    assert np.abs(got - ref).max() / scale < 5e-6
+    print("alpha2weight backward vs serial float loop", np.abs(got - ref).max() / scale)
+    assert np.abs(got - ref).max() / scale < 2e-5
 
 
 def test_alpha2weight_empty(cuda):

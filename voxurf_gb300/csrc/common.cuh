@@ -79,6 +79,13 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
+// Transmittance precision: a ray of more samples than this carries its
+// transmittance products (forward) and its suffix sums (backward) in FP64;
+// shorter rays in FP32.  GB300 runs FP64 at a small fraction of its FP32
+// rate, and at 512 factors an FP32 product is still within a few 1e-6 of
+// the exact one.  The decision is per ray (warp-uniform).
+constexpr int64_t VX_FP32_SCAN_MAX_STEPS = 512;
+
 // Warp-wide helpers -----------------------------------------------------------
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
@@ -122,6 +129,34 @@ __device__ __forceinline__ T warp_inclusive_sum(T v) {
     if (lane >= o) v += u;
   }
   return v;
+}
+
+// One 32-sample step of a ray's transmittance scan with the T < 1e-3 stop
+// (render_utils_kernel.cu:577-605): the lanes with `keep` multiply in
+// (1 - alpha) in Acc.  T = this lane's exclusive product (FP32); returns the
+// lanes up to and including the first whose inclusive product drops below
+// 1e-3 (all kept lanes when none does).  carry advances to the next step
+// unless the ray stops here, in which case last = the stopping product.
+template <typename Acc>
+__device__ __forceinline__ unsigned transmittance_step(bool keep, float alpha, Acc& carry, Acc& last, bool& stopped,
+                                                       float& T) {
+  const int lane = lane_id();
+  const unsigned keep_mask = __ballot_sync(0xffffffffu, keep);
+  const Acc fct = keep ? Acc(1) - (Acc)alpha : Acc(1);
+  const Acc incl = warp_inclusive_prod(fct) * carry;
+  Acc excl = __shfl_up_sync(0xffffffffu, incl, 1);
+  if (lane == 0) excl = carry;
+  const unsigned stop_mask = __ballot_sync(0xffffffffu, keep && incl < Acc(1e-3));
+  unsigned live = keep_mask;
+  if (stop_mask) {
+    const int ks = __ffs(stop_mask) - 1;
+    live &= (ks == 31) ? 0xffffffffu : ((2u << ks) - 1u);
+    last = __shfl_sync(0xffffffffu, incl, ks);
+    stopped = true;
+  }
+  T = (float)excl;
+  if (!stopped) carry = __shfl_sync(0xffffffffu, incl, 31);
+  return live;
 }
 
 // First index i in [lo, hi) with a[i] >= key (a sorted ascending).

@@ -5,8 +5,9 @@
 // reference walks each ray with one thread (8192 rays -> 32 CTAs on 152 SMs)
 // and a serial loop.  Here one warp owns one ray and walks it 32 samples at a
 // time with a warp prefix product; the running transmittance is carried in
-// FP64 (the only FP64 on the GPU), so the prefix stays accurate on rays of
-// thousands of samples.  Semantics kept exactly:
+// FP64 on segments of more than 512 samples (so the prefix stays accurate on
+// rays of thousands of samples) and in FP32 on shorter ones, as the
+// reference's float loop.  Semantics kept exactly:
 //   T[i] = prod_{j<i} (1 - alpha[j]),  w[i] = T[i] * alpha[i],
 //   stop after the first sample whose inclusive product drops below 1e-3,
 //   samples after the stop keep w = 0, T = 1, grad = 0,
@@ -31,11 +32,12 @@ __device__ __forceinline__ void ray_segment(const int64_t* __restrict__ ray_id, 
 // Warp-level forward scan of one segment.  Writes weight/T for every sample
 // of [beg, end); returns (via lane 0 convention, broadcast) i_end and
 // alphainv_last.
+template <typename Acc>
 __device__ __forceinline__ void scan_segment_fwd(const float* __restrict__ alpha, int64_t beg, int64_t end,
                                                  float* __restrict__ weight, float* __restrict__ T,
                                                  int64_t* i_end_out, float* last_out) {
   const int lane = lane_id();
-  double carry = 1.0;
+  Acc carry = 1;
   bool stopped = false;
   int64_t i_end = end;
   float last = 1.f;
@@ -50,14 +52,14 @@ __device__ __forceinline__ void scan_segment_fwd(const float* __restrict__ alpha
       continue;
     }
     const float a = valid ? alpha[i] : 0.f;
-    const double f = 1.0 - (double)a;
-    const double incl = warp_inclusive_prod(f) * carry;
-    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    const Acc f = Acc(1) - (Acc)a;
+    const Acc incl = warp_inclusive_prod(f) * carry;
+    Acc excl = __shfl_up_sync(0xffffffffu, incl, 1);
     if (lane == 0) excl = carry;
-    const unsigned stop_mask = __ballot_sync(0xffffffffu, valid && incl < 1e-3);
+    const unsigned stop_mask = __ballot_sync(0xffffffffu, valid && incl < Acc(1e-3));
     if (stop_mask) {
       const int k = __ffs(stop_mask) - 1;  // first sample that drops below 1e-3
-      const double incl_k = __shfl_sync(0xffffffffu, incl, k);
+      const Acc incl_k = __shfl_sync(0xffffffffu, incl, k);
       if (valid) {
         if (lane <= k) {
           const float t = (float)excl;
@@ -103,7 +105,10 @@ __global__ void alpha2weight_kernel(const float* __restrict__ alpha, const int64
   }
   int64_t ie;
   float last;
-  scan_segment_fwd(alpha, beg, end, weight, T, &ie, &last);
+  if (end - beg > VX_FP32_SCAN_MAX_STEPS)
+    scan_segment_fwd<double>(alpha, beg, end, weight, T, &ie, &last);
+  else
+    scan_segment_fwd<float>(alpha, beg, end, weight, T, &ie, &last);
   if (lane_id() == 0) {
     i_start[r] = beg;
     i_end[r] = ie;
@@ -114,13 +119,15 @@ __global__ void alpha2weight_kernel(const float* __restrict__ alpha, const int64
 // Reverse scan, render_utils_kernel.cu:671-675:
 //   back = grad_last*alphainv_last;  for i = i_end-1 .. i_start:
 //     grad[i] = gw[i]*T[i] - back/(1-alpha[i]+1e-10);  back += gw[i]*w[i]
-// The running sum `back` is carried in FP64.
+// The running sum `back` is carried in Acc (FP64 on segments of more than
+// 512 samples).
+template <typename Acc>
 __device__ __forceinline__ void scan_segment_bwd(const float* __restrict__ alpha, const float* __restrict__ weight,
                                                  const float* __restrict__ T, const float* __restrict__ grad_w,
                                                  int64_t beg, int64_t end, float back0,
                                                  float* __restrict__ grad) {
   const int lane = lane_id();
-  double carry = (double)back0;
+  Acc carry = (Acc)back0;
   for (int64_t top = end; top > beg; top -= 32) {
     const int64_t i = top - 32 + lane;
     const bool valid = i >= beg;
@@ -131,14 +138,14 @@ __device__ __forceinline__ void scan_segment_bwd(const float* __restrict__ alpha
       t = T[i];
       a = alpha[i];
     }
-    const double term = valid ? (double)(gw * w) : 0.0;
-    const double suffix = warp_inclusive_suffix_sum(term);  // sum of lanes >= this lane
-    double after = __shfl_down_sync(0xffffffffu, suffix, 1);
-    if (lane == 31) after = 0.0;
-    const double back = carry + after;
+    const Acc term = valid ? (Acc)(gw * w) : Acc(0);
+    const Acc suffix = warp_inclusive_suffix_sum(term);  // sum of lanes >= this lane
+    Acc after = __shfl_down_sync(0xffffffffu, suffix, 1);
+    if (lane == 31) after = 0;
+    const Acc back = carry + after;
     if (valid) {
-      const double denom = (double)(1.f - a) + 1e-10;
-      grad[i] = (float)((double)(gw * t) - back / denom);
+      const Acc denom = (Acc)(1.f - a) + Acc(1e-10);
+      grad[i] = (float)((Acc)(gw * t) - back / denom);
     }
     carry += __shfl_sync(0xffffffffu, suffix, 0);
   }
@@ -160,7 +167,10 @@ __global__ void alpha2weight_backward_kernel(const float* __restrict__ alpha, co
     if (lane_id() == 0) set_device_error(err, VX_ERR_BOUNDS);
     return;
   }
-  scan_segment_bwd(alpha, weight, T, grad_weights, beg, end, grad_last[r] * alphainv_last[r], grad);
+  if (end - beg > VX_FP32_SCAN_MAX_STEPS)
+    scan_segment_bwd<double>(alpha, weight, T, grad_weights, beg, end, grad_last[r] * alphainv_last[r], grad);
+  else
+    scan_segment_bwd<float>(alpha, weight, T, grad_weights, beg, end, grad_last[r] * alphainv_last[r], grad);
 }
 
 }  // namespace vx

@@ -274,11 +274,14 @@ extern "C" {
 size_t vx_mlp_f32_rowgemm_grid(int64_t M) { return (size_t)std::max<int64_t>(1, (M + BM - 1) / BM); }
 
 int vx_mlp_f32_rowgemm(const vx_mlp_f32_rowgemm_args* a, void* stream) {
-  if (!a || a->M < 0 || a->K < 1 || !a->A || !a->Bt || !a->C) return VX_ERR_ARG;
+  if (!a || a->M < 0 || a->K < 1 || !a->Bt) return VX_ERR_ARG;
+  // rows of an empty batch may have no storage (null pointers)
+  if (a->M > 0 && (!a->A || !a->C || (a->mode == 1 && !a->H))) return VX_ERR_ARG;
   if (a->mode < 0 || a->mode > 2 || a->lda < a->K || a->n_store < 1 || a->n_store > a->Np || a->ldc < a->n_store)
     return VX_ERR_ARG;
   if ((reinterpret_cast<uintptr_t>(a->Bt) & 15) || (a->mode == 0 && !a->bias) ||
-      (a->mode == 1 && (!a->H || !a->colsum || a->ldh < a->Np || a->colsum_cap < (int64_t)vx_mlp_f32_rowgemm_grid(a->M) * a->Np)))
+      (a->mode == 1 && (!a->colsum || a->ldh < a->Np ||
+                        a->colsum_cap < (int64_t)vx_mlp_f32_rowgemm_grid(a->M) * a->Np)))
     return VX_ERR_ARG;
   if (a->M == 0 && a->mode != 1) return VX_OK;   // mode 1 still writes its (zero) column sums
   RowGemmParams P{};
@@ -316,8 +319,8 @@ size_t vx_mlp_f32_wgrad_grid(int64_t rows) {
 }
 
 int vx_mlp_f32_wgrad(const vx_mlp_f32_wgrad_args* a, void* stream) {
-  if (!a || a->rows < 0 || !a->A || !a->B || !a->part || a->M < 1 || a->N < 1 || a->lda < a->M || a->ldb < a->N)
-    return VX_ERR_ARG;
+  if (!a || a->rows < 0 || !a->part || a->M < 1 || a->N < 1 || a->lda < a->M || a->ldb < a->N) return VX_ERR_ARG;
+  if (a->rows > 0 && (!a->A || !a->B)) return VX_ERR_ARG;   // an empty batch writes zero partials
   auto pad = [](int64_t x) -> int64_t { return x <= 32 ? 32 : x <= 64 ? 64 : x <= 80 ? 80 : x <= 128 ? 128 : x <= 192 ? 192 : -1; };
   const int64_t MP = pad(a->M), NP = pad(a->N);
   if (MP < 0 || NP < 0) return VX_ERR_UNSUPPORTED;

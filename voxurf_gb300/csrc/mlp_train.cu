@@ -1017,6 +1017,10 @@ int vx_mlp_train_backward(const vx_mlp_train_bwd_args* a, void* stream) {
   const int64_t tiles = (a->n_rows + TM - 1) / TM;
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, sm_count()));
   if (!a->dbh_part || a->dbh_part_cap < (int64_t)grid) return VX_ERR_ARG;
+  if (a->n_rows == 0) {   // an empty batch: zero output-layer bias partials, nothing else
+    cudaError_t e = cudaMemsetAsync(a->dbh_part, 0, sizeof(float) * 4 * grid, as_stream(stream));
+    return cuda_status(e);
+  }
   if (!a->dY || !a->Wh || !a->relu || !a->WTp || !a->W0Tp || !a->dZ || !a->dYT || !a->dX) return VX_ERR_ARG;
   if (a->rows_cap < tiles * TM || a->ld_dx < a->K0 || !aligned16(a->WTp) || !aligned16(a->W0Tp) ||
       !aligned16(a->Wh) || !aligned16(a->dZ) || !aligned16(a->dYT) || !aligned16(a->dX) ||
@@ -1040,10 +1044,6 @@ int vx_mlp_train_backward(const vx_mlp_train_bwd_args* a, void* stream) {
   P.dx_bf16 = a->dx_bf16;
   P.dbh_part = a->dbh_part;
   P.err = device_error_ptr();
-  if (a->n_rows == 0) {
-    cudaError_t e = cudaMemsetAsync(a->dbh_part, 0, sizeof(float) * 4 * grid, as_stream(stream));
-    return cuda_status(e);
-  }
   return dispatch(a->width, a->n_hidden, [&](auto Wc, auto Lc) {
     return launch_bwd<decltype(Wc)::value, decltype(Lc)::value>(P, grid, as_stream(stream));
   });
@@ -1055,7 +1055,8 @@ size_t vx_mlp_wgrad_grid(int64_t n_rows) {
 }
 
 int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* a, void* stream) {
-  if (!a || a->n_rows < 0 || !a->A || !a->B || !a->part) return VX_ERR_ARG;
+  if (!a || a->n_rows < 0 || !a->part) return VX_ERR_ARG;
+  if (a->n_rows > 0 && (!a->A || !a->B)) return VX_ERR_ARG;   // an empty batch writes zero partials
   if (a->WA < 16 || a->WA > 256 || a->WA % 16 || a->WB < 16 || a->WB > 240 || a->WB % 16) return VX_ERR_UNSUPPORTED;
   const int MT = (int)((a->WA + TM - 1) / TM);
   const int NC = (int)a->WB + (a->ones ? 16 : 0);
@@ -1064,7 +1065,7 @@ int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* a, void* stream) {
   if ((int64_t)(MT * TM - a->WA) * 16 > (int64_t)WG_TAIL) return VX_ERR_UNSUPPORTED;
   const unsigned grid = (unsigned)vx_mlp_wgrad_grid(a->n_rows);
   if (a->part_cap < (int64_t)grid * a->WA * NC) return VX_ERR_ARG;
-  if (!aligned16(a->A) || !aligned16(a->B) || !aligned16(a->part)) return VX_ERR_ARG;
+  if (!aligned16(a->A) || !aligned16(a->B) || !aligned16(a->part)) return VX_ERR_ARG;   // (null is aligned)
   if (a->b_rows && (a->ldb < a->WB || a->ldb % 8)) return VX_ERR_ARG;
   WgradParams P{};
   P.A = reinterpret_cast<const bf16*>(a->A);

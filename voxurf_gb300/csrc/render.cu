@@ -57,30 +57,18 @@ __device__ __forceinline__ bool mask_hit(const MarchParams& P, const float p[3])
   return mask_lookup(P.mask, P.mX, P.mY, P.mZ, P.mscale, P.mshift, p);
 }
 
-template <bool DENS>
-__global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
-  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (r >= P.n_rays) return;
+// The march of one ray after its setup; Acc (float or double) carries the
+// transmittance product.
+template <bool DENS, typename Acc>
+__device__ __forceinline__ void march_fine_ray(const MarchParams& P, int r, const RayFrame& f, int64_t n_steps,
+                                               const float (&v)[3]) {
   const int lane = lane_id();
   const unsigned lt_mask = (1u << lane) - 1u;
-  float o[3], d[3], v[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    o[a] = __ldg(P.rays_o + 3 * r + a);
-    d[a] = __ldg(P.rays_d + 3 * r + a);
-    v[a] = __ldg(P.viewdirs + 3 * r + a);
-  }
-  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
-  int64_t n_steps = f.n_steps;
-  if (n_steps > P.max_steps) {
-    if (lane == 0) set_device_error(P.err, VX_ERR_CAPACITY);
-    n_steps = P.max_steps;
-  }
   const int64_t slot0 = (int64_t)r * P.max_steps;
-  double carry = 1.0;
+  Acc carry = 1;
   int cnt1 = 0, cnt2 = 0;
   bool stopped = false;
-  double last = 1.0;
+  Acc last = 1;
   for (int base = 0; base < n_steps && !stopped; base += 32) {
     const int k = base + lane;
     bool keep = false;
@@ -101,11 +89,11 @@ __global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
     }
     const unsigned keep_mask = __ballot_sync(0xffffffffu, keep);
     if (keep_mask == 0u) continue;
-    const double fct = keep ? 1.0 - (double)alpha : 1.0;
-    const double incl = warp_inclusive_prod(fct) * carry;
-    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    const Acc fct = keep ? Acc(1) - (Acc)alpha : Acc(1);
+    const Acc incl = warp_inclusive_prod(fct) * carry;
+    Acc excl = __shfl_up_sync(0xffffffffu, incl, 1);
     if (lane == 0) excl = carry;
-    const unsigned stop_mask = __ballot_sync(0xffffffffu, keep && incl < 1e-3);
+    const unsigned stop_mask = __ballot_sync(0xffffffffu, keep && incl < Acc(1e-3));
     unsigned live = keep_mask;
     if (stop_mask) {
       const int ks = __ffs(stop_mask) - 1;
@@ -132,6 +120,30 @@ __global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
     P.n2[r] = cnt2;
     P.alphainv_last[r] = (float)(stopped ? last : carry);
   }
+}
+
+template <bool DENS>
+__global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  int64_t n_steps = f.n_steps;
+  if (n_steps > P.max_steps) {
+    if (lane == 0) set_device_error(P.err, VX_ERR_CAPACITY);
+    n_steps = P.max_steps;
+  }
+  if (f.n_steps > VX_FP32_SCAN_MAX_STEPS)
+    march_fine_ray<DENS, double>(P, r, f, n_steps, v);
+  else
+    march_fine_ray<DENS, float>(P, r, f, n_steps, v);
 }
 
 // ---- compaction of the shaded samples -------------------------------------
@@ -532,7 +544,11 @@ __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P)
   }
   const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
   const int64_t slot0 = (int64_t)r * P.max_steps;
-  double carry = (double)(P.d_last[r] * P.alphainv_last[r]);
+  // suffix sums of the transmittance backward: FP64 for rays of more than
+  // 512 samples (as the forward's products), FP32 otherwise
+  const bool wide = f.n_steps > VX_FP32_SCAN_MAX_STEPS;
+  double carry_d = (double)(P.d_last[r] * P.alphainv_last[r]);
+  float carry_f = P.d_last[r] * P.alphainv_last[r];
   for (int top = n; top > 0; top -= 32) {
     const int j = top - 32 + lane;
     const bool valid = j >= 0;
@@ -543,14 +559,25 @@ __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P)
       gw = P.dw_slot[slot0 + j];
     }
     const float alpha = rc.y, T = rc.z, w = rc.w;
-    const double term = valid ? (double)(gw * w) : 0.0;
-    const double suffix = warp_inclusive_suffix_sum(term);
-    double after = __shfl_down_sync(0xffffffffu, suffix, 1);
-    if (lane == 31) after = 0.0;
-    const double back = carry + after;
-    carry += __shfl_sync(0xffffffffu, suffix, 0);
+    float d_alpha;
+    if (wide) {
+      const double term = valid ? (double)(gw * w) : 0.0;
+      const double suffix = warp_inclusive_suffix_sum(term);
+      double after = __shfl_down_sync(0xffffffffu, suffix, 1);
+      if (lane == 31) after = 0.0;
+      const double back = carry_d + after;
+      carry_d += __shfl_sync(0xffffffffu, suffix, 0);
+      d_alpha = (float)((double)(gw * T) - back / ((double)(1.f - alpha) + 1e-10));
+    } else {
+      const float term = valid ? gw * w : 0.f;
+      const float suffix = warp_inclusive_suffix_sum(term);
+      float after = __shfl_down_sync(0xffffffffu, suffix, 1);
+      if (lane == 31) after = 0.f;
+      const float back = carry_f + after;
+      carry_f += __shfl_sync(0xffffffffu, suffix, 0);
+      d_alpha = gw * T - back / ((1.f - alpha) + 1e-10f);
+    }
     if (!valid) continue;
-    const float d_alpha = (float)((double)(gw * T) - back / ((double)(1.f - alpha) + 1e-10));
     if (d_alpha == 0.f) continue;
     const int k = (int)(__float_as_uint(rc.x) & 0x7fffffffu);
     float p[3], ind[3], s, gr[3];
@@ -621,28 +648,16 @@ struct CoarseMarchParams {
   int* n2b;            // records up to the second scan's stop (backward range)
 };
 
-template <bool DENS>
-__global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) {
+// The coarse march of one ray after its setup; Acc (float or double)
+// carries the two transmittance products.
+template <bool DENS, typename Acc>
+__device__ __forceinline__ void march_coarse_ray(const CoarseMarchParams& C, int r, const RayFrame& f,
+                                                 int64_t n_steps, const float (&v)[3]) {
   const MarchParams& P = C.m;
-  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (r >= P.n_rays) return;
   const int lane = lane_id();
   const unsigned lt_mask = (1u << lane) - 1u;
-  float o[3], d[3], v[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    o[a] = __ldg(P.rays_o + 3 * r + a);
-    d[a] = __ldg(P.rays_d + 3 * r + a);
-    v[a] = __ldg(P.viewdirs + 3 * r + a);
-  }
-  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
-  int64_t n_steps = f.n_steps;
-  if (n_steps > P.max_steps) {
-    if (lane == 0) set_device_error(P.err, VX_ERR_CAPACITY);
-    n_steps = P.max_steps;
-  }
   const int64_t slot0 = (int64_t)r * P.max_steps;
-  double carry1 = 1.0, carry2 = 1.0, last2 = 1.0;
+  Acc carry1 = 1, carry2 = 1, last2 = 1;
   bool stop1 = false, stop2 = false;
   int cnt = 0, cnt_b = 0;
   for (int base = 0; base < n_steps && !stop1; base += 32) {
@@ -667,11 +682,11 @@ __global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) 
     const unsigned in_mask = __ballot_sync(0xffffffffu, inb);
     if (in_mask == 0u) continue;
     // first scan: every in-bbox sample
-    const double f1 = inb ? 1.0 - (double)alpha : 1.0;
-    const double incl1 = warp_inclusive_prod(f1) * carry1;
-    double excl1 = __shfl_up_sync(0xffffffffu, incl1, 1);
+    const Acc f1 = inb ? Acc(1) - (Acc)alpha : Acc(1);
+    const Acc incl1 = warp_inclusive_prod(f1) * carry1;
+    Acc excl1 = __shfl_up_sync(0xffffffffu, incl1, 1);
     if (lane == 0) excl1 = carry1;
-    const unsigned s1 = __ballot_sync(0xffffffffu, inb && incl1 < 1e-3);
+    const unsigned s1 = __ballot_sync(0xffffffffu, inb && incl1 < Acc(1e-3));
     unsigned live1 = in_mask;
     if (s1) {
       const int ks = __ffs(s1) - 1;
@@ -688,11 +703,11 @@ __global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) 
     float T2 = 1.f, w2 = 0.f;
     unsigned live2 = 0u;
     if (!stop2) {
-      const double f2 = sel ? 1.0 - (double)alpha : 1.0;
-      const double incl2 = warp_inclusive_prod(f2) * carry2;
-      double excl2 = __shfl_up_sync(0xffffffffu, incl2, 1);
+      const Acc f2 = sel ? Acc(1) - (Acc)alpha : Acc(1);
+      const Acc incl2 = warp_inclusive_prod(f2) * carry2;
+      Acc excl2 = __shfl_up_sync(0xffffffffu, incl2, 1);
       if (lane == 0) excl2 = carry2;
-      const unsigned s2 = __ballot_sync(0xffffffffu, sel && incl2 < 1e-3);
+      const unsigned s2 = __ballot_sync(0xffffffffu, sel && incl2 < Acc(1e-3));
       live2 = sel_mask;
       if (s2) {
         const int ks = __ffs(s2) - 1;
@@ -722,6 +737,31 @@ __global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) 
     C.n2b[r] = cnt_b;
     P.alphainv_last[r] = (float)(stop2 ? last2 : carry2);
   }
+}
+
+template <bool DENS>
+__global__ void __launch_bounds__(256) march_coarse_kernel(CoarseMarchParams C) {
+  const MarchParams& P = C.m;
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= P.n_rays) return;
+  const int lane = lane_id();
+  float o[3], d[3], v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = __ldg(P.rays_o + 3 * r + a);
+    d[a] = __ldg(P.rays_d + 3 * r + a);
+    v[a] = __ldg(P.viewdirs + 3 * r + a);
+  }
+  const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
+  int64_t n_steps = f.n_steps;
+  if (n_steps > P.max_steps) {
+    if (lane == 0) set_device_error(P.err, VX_ERR_CAPACITY);
+    n_steps = P.max_steps;
+  }
+  if (f.n_steps > VX_FP32_SCAN_MAX_STEPS)
+    march_coarse_ray<DENS, double>(C, r, f, n_steps, v);
+  else
+    march_coarse_ray<DENS, float>(C, r, f, n_steps, v);
 }
 
 struct CoarseFeatParams {
@@ -943,7 +983,11 @@ __global__ void __launch_bounds__(256) geometry_coarse_bwd_kernel(CoarseBwdParam
   }
   const RayFrame f = ray_frame(o, d, P.bmin, P.bmax, P.near, P.stepdist);
   const int64_t slot0 = (int64_t)r * P.max_steps;
-  double carry = (double)(P.d_last[r] * P.alphainv_last[r]);
+  // suffix sums of the transmittance backward: FP64 for rays of more than
+  // 512 samples (as the forward's products), FP32 otherwise
+  const bool wide = f.n_steps > VX_FP32_SCAN_MAX_STEPS;
+  double carry_d = (double)(P.d_last[r] * P.alphainv_last[r]);
+  float carry_f = P.d_last[r] * P.alphainv_last[r];
   for (int top = n; top > 0; top -= 32) {
     const int j = top - 32 + lane;
     const bool valid = j >= 0;
@@ -954,14 +998,25 @@ __global__ void __launch_bounds__(256) geometry_coarse_bwd_kernel(CoarseBwdParam
       gw = P.dw_slot[slot0 + j];
     }
     const float alpha = rc.y, T = rc.z, w = rc.w;
-    const double term = valid ? (double)(gw * w) : 0.0;
-    const double suffix = warp_inclusive_suffix_sum(term);
-    double after = __shfl_down_sync(0xffffffffu, suffix, 1);
-    if (lane == 31) after = 0.0;
-    const double back = carry + after;
-    carry += __shfl_sync(0xffffffffu, suffix, 0);
+    float d_alpha;
+    if (wide) {
+      const double term = valid ? (double)(gw * w) : 0.0;
+      const double suffix = warp_inclusive_suffix_sum(term);
+      double after = __shfl_down_sync(0xffffffffu, suffix, 1);
+      if (lane == 31) after = 0.0;
+      const double back = carry_d + after;
+      carry_d += __shfl_sync(0xffffffffu, suffix, 0);
+      d_alpha = (float)((double)(gw * T) - back / ((double)(1.f - alpha) + 1e-10));
+    } else {
+      const float term = valid ? gw * w : 0.f;
+      const float suffix = warp_inclusive_suffix_sum(term);
+      float after = __shfl_down_sync(0xffffffffu, suffix, 1);
+      if (lane == 31) after = 0.f;
+      const float back = carry_f + after;
+      carry_f += __shfl_sync(0xffffffffu, suffix, 0);
+      d_alpha = gw * T - back / ((1.f - alpha) + 1e-10f);
+    }
     if (!valid) continue;
-    const float d_alpha = (float)((double)(gw * T) - back / ((double)(1.f - alpha) + 1e-10));
     if (d_alpha == 0.f) continue;
     const int k = (int)(__float_as_uint(rc.x) & 0x7fffffffu);
     float p[3], ind[3], gr[3];

@@ -260,7 +260,10 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
     n_steps = P.max_steps;
   }
   uint2* rec = P.rec + (int64_t)r * P.max_steps;
-  double carry = 1.0, last = 1.0;
+  // transmittance product: FP64 for rays of more than 512 samples, FP32 otherwise
+  const bool wide = f.n_steps > VX_FP32_SCAN_MAX_STEPS;
+  double carry_d = 1.0, last_d = 1.0;
+  float carry_f = 1.f, last_f = 1.f;
   int cnt2 = 0;
   bool stopped = false;
   // with an occupancy grid, serve_first_kernel left the first and the last
@@ -289,29 +292,19 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
     }
     const unsigned keep_mask = __ballot_sync(0xffffffffu, keep);
     if (keep_mask == 0u) continue;
-    const double fct = keep ? 1.0 - (double)alpha : 1.0;
-    const double incl = warp_inclusive_prod(fct) * carry;
-    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
-    if (lane == 0) excl = carry;
-    const unsigned stop_mask = __ballot_sync(0xffffffffu, keep && incl < 1e-3);
-    unsigned live = keep_mask;
-    if (stop_mask) {
-      const int ks = __ffs(stop_mask) - 1;
-      live &= (ks == 31) ? 0xffffffffu : ((2u << ks) - 1u);
-      last = __shfl_sync(0xffffffffu, incl, ks);
-      stopped = true;
-    }
+    float T;
+    const unsigned live = wide ? transmittance_step<double>(keep, alpha, carry_d, last_d, stopped, T)
+                               : transmittance_step<float>(keep, alpha, carry_f, last_f, stopped, T);
     const bool mine = (live >> lane) & 1u;
-    const float w = (float)excl * alpha;
+    const float w = T * alpha;
     const bool s2 = mine && (w > S.thres);
     const unsigned s2_mask = __ballot_sync(0xffffffffu, s2);
     if (s2) rec[cnt2 + __popc(s2_mask & lt_mask)] = make_uint2((unsigned)k, __float_as_uint(w));
     cnt2 += __popc(s2_mask);
-    if (!stopped) carry = __shfl_sync(0xffffffffu, incl, 31);
   }
   if (lane == 0) {
     P.n2[r] = cnt2;
-    P.alphainv_last[r] = (float)(stopped ? last : carry);
+    P.alphainv_last[r] = wide ? (float)(stopped ? last_d : carry_d) : (stopped ? last_f : carry_f);
   }
 }
 

@@ -15,6 +15,8 @@ them with one pack launch, and the backward returns FP32 gradients.
 """
 from __future__ import annotations
 
+import weakref
+
 import torch
 import torch.nn as nn
 
@@ -57,10 +59,15 @@ class _TrainMLP(torch.autograd.Function):
         return (dX if ctx.needs_input_grad[0] else None, None, None, *grads)
 
 
+# engines per module, kept beside the module (a deep copy of the module,
+# e.g. an FP64 copy for checking, must not carry the engine's buffers along)
+_ENGINES: "weakref.WeakKeyDictionary[nn.Module, dict]" = weakref.WeakKeyDictionary()
+
+
 def engine_for(net: nn.Sequential, dtype: torch.dtype, ld: int):
     """The engine of `net` for input rows of `dtype` with row stride `ld`
-    (cached on the module; its operand buffers follow the parameters)."""
-    cache = net.__dict__.setdefault("_vx_engines", {})
+    (cached per module; its operand buffers follow the parameters)."""
+    cache = _ENGINES.setdefault(net, {})
     key = (dtype, ld)
     eng = cache.get(key)
     lin = _linears(net)
@@ -97,7 +104,7 @@ def last_relu_masks(net: nn.Sequential) -> list[torch.Tensor] | None:
     """ReLU decisions (post-ReLU activation > 0) of each hidden layer in the
     last training forward of `net` through the FP32 engine, [S, W] bool each
     (rows in the order of the MLP input), or None."""
-    for eng in net.__dict__.get("_vx_engines", {}).values():
+    for eng in _ENGINES.get(net, {}).values():
         if isinstance(eng, F32TrainMLP) and eng.last_hs is not None:
             return [h > 0 for h in eng.last_hs]
     return None
