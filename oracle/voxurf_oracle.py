@@ -148,15 +148,14 @@ def mlp_relu_ties(net, x, device_masks=None, tie=1e-6):
     tie * (the layer's RMS) of zero takes the device's decision instead of its
     own sign: there FP32 and FP64 legitimately disagree on the ReLU, like a
     fast_color_thres tie; `ties` counts them."""
+    if device_masks is None:
+        return net(x), 0          # the module itself (its ReLU modules' hooks fire)
     lin = [m for m in net.modules() if isinstance(m, nn.Linear)]
     h, ties = x, 0
     for i, m in enumerate(lin):
         h = F.linear(h, m.weight, m.bias)
         if i == len(lin) - 1:
             break
-        if device_masks is None:
-            h = torch.relu(h)
-            continue
         hd = h.detach()
         near = hd.abs() <= tie * hd.pow(2).mean().sqrt()
         keep = torch.where(near, device_masks[i].to(hd.device), hd > 0)
