@@ -147,11 +147,13 @@ def mlp_relu_ties(net, x, device_masks=None, tie=1e-6):
     device's ReLU decisions, rows in the same order), a pre-activation within
     tie * (the layer's RMS) of zero takes the device's decision instead of its
     own sign: there FP32 and FP64 legitimately disagree on the ReLU, like a
-    fast_color_thres tie; `ties` counts them."""
+    fast_color_thres tie; `ties` counts them (mlp_relu_ties.examined counts
+    the pre-activations looked at, for bounds proportional to the batch)."""
     if device_masks is None:
         return net(x), 0          # the module itself (its ReLU modules' hooks fire)
     lin = [m for m in net.modules() if isinstance(m, nn.Linear)]
     h, ties = x, 0
+    mlp_relu_ties.examined = 0
     for i, m in enumerate(lin):
         h = F.linear(h, m.weight, m.bias)
         if i == len(lin) - 1:
@@ -160,6 +162,7 @@ def mlp_relu_ties(net, x, device_masks=None, tie=1e-6):
         near = hd.abs() <= tie * hd.pow(2).mean().sqrt()
         keep = torch.where(near, device_masks[i].to(hd.device), hd > 0)
         ties += int(near.sum())
+        mlp_relu_ties.examined += hd.numel()
         h = h * keep.to(h.dtype)
     return h, ties
 
@@ -284,6 +287,7 @@ class OracleFine(nn.Module):
         rgb_feat = torch.cat(parts, -1)
         rgb_logit, t1 = mlp_relu_ties(self.rgbnet, rgb_feat, rd.get("rgbnet"), relu_tie)
         self.relu_ties += t1
+        self.relu_examined = getattr(mlp_relu_ties, "examined", 0) if rd else 0
         rgb = torch.sigmoid(rgb_logit)
         out = {"alphainv_cum": alphainv_last, "weights": weights, "raw_rgb": rgb, "raw_alpha": alpha,
                "gradient": gradient, "ray_id": ray_id, "step_id": step_id, "s_val": s_val, "rgb_feat": rgb_feat}
@@ -304,6 +308,7 @@ class OracleFine(nn.Module):
             base = detached if self.k_detach_2 else rgb_logit
             k_out, t2 = mlp_relu_ties(self.k_rgbnet, k_feat, rd.get("k_rgbnet"), relu_tie)
             self.relu_ties += t2
+            self.relu_examined += getattr(mlp_relu_ties, "examined", 0) if rd else 0
             k_rgb = torch.sigmoid(base + k_out)
             k_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * k_rgb) \
                 + alphainv_last[..., None] * bg
@@ -440,6 +445,7 @@ class OracleCoarse(nn.Module):
             normal = gradient / (gradient.norm(dim=-1, keepdim=True) + 1e-5)
             rgb_feat = torch.cat([rgb_feat, normal], -1)
         logit, self.relu_ties = mlp_relu_ties(self.rgbnet, rgb_feat, relu_device, relu_tie)
+        self.relu_examined = getattr(mlp_relu_ties, "examined", 0) if relu_device is not None else 0
         rgb = torch.sigmoid(logit)
         rgb_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * rgb)
         cum_w = torch.zeros([N, 1], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1))

@@ -103,7 +103,11 @@ def _device_relu(model):
             "k_rgbnet": [m.cpu() for m in last_relu_masks(model.k_rgbnet)]}
 
 
-MAX_RELU_TIES = 64   # pre-activations within 1e-6 of the layer RMS from zero (a handful per batch)
+def _relu_ties_ok(orc):
+    """ReLU ties (pre-activations within 1e-6 of their layer's RMS from zero)
+    are as rare as a smooth density at zero makes them: about 1e-6 of the
+    pre-activations examined, bounded here at 4e-6 of them plus 64."""
+    return orc.relu_ties <= 64 + 4e-6 * getattr(orc, "relu_examined", 0)
 
 
 @pytest.fixture(scope="module")
@@ -124,6 +128,7 @@ def fine256(cuda):
         ro, rd, vd, tgt = (torch.from_numpy(a) for a in rays)
         ret = orc(ro, rd, vd, global_step=1, relu_device=relu_device, **RK)
         ties = orc.relu_ties
+        assert _relu_ties_ok(orc), (orc.relu_ties, orc.relu_examined)
         loss = train_loss(ret, tgt.double())
         loss.backward()
         grads = _oracle_grads(orc)
@@ -176,7 +181,6 @@ def test_fine256_fp32_step_matches_fp64_oracle(cuda, fine256):
     o = fine256["oracle"].get(_device_relu(model))
     fo = o
     o = fo["ret"]
-    assert fo["relu_ties"] <= MAX_RELU_TIES
     err = (rgb_full - o["rgb_marched"]).abs().max().item()
     assert err <= 1e-5, err
     assert ret["weights"].numel() == o["weights"].numel() > 2000
@@ -276,6 +280,7 @@ def long384(cuda):
         torch.cuda.empty_cache()
         o = orc(*(torch.from_numpy(a) for a in rays[:3]), global_step=0, relu_device=relu_device, **rk)
         ties = orc.relu_ties
+        assert _relu_ties_ok(orc), (orc.relu_ties, orc.relu_examined)
         ol = train_loss(o, torch.from_numpy(rays[3]).double())
         ol.backward()
         grads = {"sdf": orc.sdf_grid.grad, "k0": orc.k0_grid.grad,
@@ -311,7 +316,6 @@ def test_long_rays_384_vs_fp64_oracle(cuda, precision, long384):
     torch.cuda.synchronize()
     lo = long384["oracle"].get(_device_relu(model) if precision == "fp32" else None)
     o, og = lo["ret"], lo["grads"]
-    assert lo["relu_ties"] <= MAX_RELU_TIES
     err = (g["rgb_marched"].detach().double().cpu() - o["rgb_marched"]).abs().max().item()
     errs = {"rgb": err, "sdf": _rel_l2(model.sdf.grid.grad, og["sdf"]), "k0": _rel_l2(model.k0.grid.grad, og["k0"])}
     for net in ("rgbnet", "k_rgbnet"):
@@ -364,7 +368,7 @@ def test_coarse_eikonal_bench_batch_vs_fp64_oracle(cuda, precision, rgb_tol, los
         orc = OracleCoarse(model, dtype=dtype)
         o = orc(*(torch.from_numpy(a) for a in (ro, rd, vd)), global_step=1, device_keep=keep, tie_rel=1e-3,
                 relu_device=dev_relu if dtype == torch.float64 else None, **rk)
-        assert orc.relu_ties <= MAX_RELU_TIES
+        assert _relu_ties_ok(orc), (orc.relu_ties, orc.relu_examined)
         o_eik = ((o["gradient"].norm(dim=-1) - 1.0) ** 2).mean()
         ol = train_loss(o, torch.from_numpy(tgt).to(dtype), weight_rgb0=0) + 0.1 * o_eik
         ol.backward()

@@ -132,11 +132,11 @@ def test_alpha2weight_fwd_bwd(cuda, n_rays, max_len, alpha_hi):
     samp_keep = keep[ray_id]
     # against the FP64 scan: segments of more than 512 samples carry T in FP64
     # and round once (3e-7); shorter ones carry it in FP32 through the warp
-    # prefix products and the chunk carries (2e-6)
+    # prefix products and the chunk carries (3e-6; measured 1.6e-6)
     w64, T64, last64, _, _ = cref.alpha2weight(alpha.astype(np.float64), ray_id, n_rays)
     seg_len = full_end - np.searchsorted(ray_id, np.arange(n_rays))
     long_ray = seg_len > 512
-    for sel_r, rtol in ((keep & long_ray, 3e-7), (keep & ~long_ray, 2e-6)):
+    for sel_r, rtol in ((keep & long_ray, 3e-7), (keep & ~long_ray, 3e-6)):
         sel_s = sel_r[ray_id]
         errs = [float(np.max(np.abs(a[sel_s] - b[sel_s]) / (np.abs(b[sel_s]) + 1e-30), initial=0.0))
                 for a, b in ((gw, w64), (gT, T64))]

@@ -45,6 +45,17 @@ struct RowGemmParams {
   float* colsum;             // mode 1: [gridDim.x][Np] per-CTA column sums
 };
 
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// 16-byte asynchronous global -> shared copy, zero fill beyond src_bytes.
+__device__ __forceinline__ void cp16(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ int64_t rows_of(int64_t n, const int64_t* n_dev) {
   if (n_dev) {
     const int64_t d = *n_dev;
@@ -54,7 +65,7 @@ __device__ __forceinline__ int64_t rows_of(int64_t n, const int64_t* n_dev) {
 }
 
 template <int TN>
-__global__ void __launch_bounds__(THREADS) rowgemm_kernel(RowGemmParams P) {
+__global__ void __launch_bounds__(THREADS, 2) rowgemm_kernel(RowGemmParams P) {
   constexpr int NP = 16 * TN;
   __shared__ __align__(16) float As[2][KC][BM];
   __shared__ __align__(16) float Bs[2][KC][NP];
@@ -85,11 +96,12 @@ __global__ void __launch_bounds__(THREADS) rowgemm_kernel(RowGemmParams P) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) As[s][4 * aq + i][am] = r[i];
   };
-  // B stage: KC x NP floats, contiguous in Bt
+  // B stage: KC x NP floats, contiguous in Bt, copied asynchronously
   auto load_b = [&](int kt, int s) {
-    const float4* src = reinterpret_cast<const float4*>(P.Bt + (int64_t)kt * KC * NP);
-    float4* dst = reinterpret_cast<float4*>(&Bs[s][0][0]);
-    for (int i = tid; i < KC * NP / 4; i += THREADS) dst[i] = src[i];
+    const float* src = P.Bt + (int64_t)kt * KC * NP;
+    float* dst = &Bs[s][0][0];
+    for (int i = tid; i < KC * NP / 4; i += THREADS) cp16(dst + 4 * i, src + 4 * i, 16u);
+    cp_commit();
   };
 
   float acc[4][TN];
@@ -102,6 +114,7 @@ __global__ void __launch_bounds__(THREADS) rowgemm_kernel(RowGemmParams P) {
   load_a(0, ra);
   store_a(0, ra);
   load_b(0, 0);
+  cp_wait_all();
   __syncthreads();
   for (int kt = 0; kt < nk; ++kt) {
     const int s = kt & 1;
@@ -130,6 +143,7 @@ __global__ void __launch_bounds__(THREADS) rowgemm_kernel(RowGemmParams P) {
         for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
     if (kt + 1 < nk) store_a(s ^ 1, ra);
+    cp_wait_all();
     __syncthreads();
   }
   // epilogue
@@ -193,8 +207,29 @@ __global__ void __launch_bounds__(THREADS, 1) wgrad_kernel(WgradParams P) {
   const int64_t r1 = std::min<int64_t>(rows, r0 + per);
   const int nst = (int)((r1 - r0 + WG_KC - 1) / WG_KC);
 
+  // rows of A and B -> the stage, 16-byte asynchronous pieces (zero past the
+  // CTA's rows and past M / N) when the rows are 16-byte aligned, otherwise
+  // plain element copies
+  const bool vec = (P.lda & 3) == 0 && (P.ldb & 3) == 0 && ((reinterpret_cast<uintptr_t>(P.A) |
+                                                              reinterpret_cast<uintptr_t>(P.B)) & 15) == 0;
   auto load = [&](int st, int s) {
     const int64_t rb = r0 + (int64_t)st * WG_KC;
+    if (vec) {
+      for (int i = tid; i < WG_KC * MP / 4; i += THREADS) {
+        const int rr = i / (MP / 4), c = 4 * (i % (MP / 4));
+        const int64_t r = rb + rr;
+        const int valid = (r < r1) ? max(0, min(4, P.M - c)) : 0;
+        cp16(&As[s][rr][c], valid ? P.A + r * P.lda + c : P.A, (uint32_t)(4 * valid));
+      }
+      for (int i = tid; i < WG_KC * NP / 4; i += THREADS) {
+        const int rr = i / (NP / 4), c = 4 * (i % (NP / 4));
+        const int64_t r = rb + rr;
+        const int valid = (r < r1) ? max(0, min(4, P.N - c)) : 0;
+        cp16(&Bs[s][rr][c], valid ? P.B + r * P.ldb + c : P.B, (uint32_t)(4 * valid));
+      }
+      cp_commit();
+      return;
+    }
     for (int i = tid; i < WG_KC * MP; i += THREADS) {
       const int rr = i / MP, c = i % MP;
       const int64_t r = rb + rr;
@@ -213,10 +248,11 @@ __global__ void __launch_bounds__(THREADS, 1) wgrad_kernel(WgradParams P) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
   if (nst > 0) load(0, 0);
+  cp_wait_all();
   __syncthreads();
   for (int st = 0; st < nst; ++st) {
     const int s = st & 1;
-    if (st + 1 < nst) load(st + 1, s ^ 1);
+    if (st + 1 < nst) load(st + 1, s ^ 1);   // lands while this stage is computed
 #pragma unroll 4
     for (int k = 0; k < WG_KC; ++k) {
       float a[TM], b[TN];
@@ -229,6 +265,7 @@ __global__ void __launch_bounds__(THREADS, 1) wgrad_kernel(WgradParams P) {
 #pragma unroll
         for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
+    cp_wait_all();
     __syncthreads();
   }
   float* part = P.part + (size_t)blockIdx.x * MP * NP;
@@ -251,15 +288,42 @@ struct SumJobs {
   int n;
 };
 
-__global__ void sum_partials_kernel(SumJobs J) {
+// A block of 256 threads sums 32 consecutive outputs (lane = output): warp w
+// adds the partials of its contiguous eighth of k, then the eight warp sums
+// are added in warp order.  The order is fixed, so the result does not
+// depend on timing.
+__global__ void __launch_bounds__(256) sum_partials_kernel(SumJobs J) {
   const SumJob& S = J.j[blockIdx.y];
+  __shared__ float red[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t total = S.rows * S.cols;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t m = i / S.cols, n = i % S.cols;
-    const float* p = S.part + m * S.part_ld + n;
+  const int64_t per = (S.n_part + 7) / 8, k0 = per * warp, k1 = min(S.n_part, k0 + per);
+  for (int64_t base = (int64_t)blockIdx.x * 32; base < total; base += (int64_t)gridDim.x * 32) {
+    const int64_t i = base + lane;
     float s = 0.f;
-    for (int64_t k = 0; k < S.n_part; ++k) s += p[k * S.part_stride];
-    S.out[m * S.out_ld + n] = s;
+    if (i < total) {
+      const int64_t m = i / S.cols, n = i % S.cols;
+      const float* p = S.part + m * S.part_ld + n;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+      int64_t k = k0;
+      for (; k + 4 <= k1; k += 4) {
+        a0 += p[k * S.part_stride];
+        a1 += p[(k + 1) * S.part_stride];
+        a2 += p[(k + 2) * S.part_stride];
+        a3 += p[(k + 3) * S.part_stride];
+      }
+      for (; k < k1; ++k) a0 += p[k * S.part_stride];
+      s = (a0 + a1) + (a2 + a3);
+    }
+    red[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && i < total) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[w][lane];
+      const int64_t m = i / S.cols, n = i % S.cols;
+      S.out[m * S.out_ld + n] = t;
+    }
+    __syncthreads();
   }
 }
 
@@ -314,8 +378,8 @@ int vx_mlp_f32_rowgemm(const vx_mlp_f32_rowgemm_args* a, void* stream) {
 }
 
 size_t vx_mlp_f32_wgrad_grid(int64_t rows) {
-  // about 1024 rows per CTA, at most one CTA per SM
-  return (size_t)std::max<int64_t>(1, std::min<int64_t>(sm_count(), (rows + 1023) / 1024));
+  // at least 256 rows per CTA, at most one CTA per SM
+  return (size_t)std::max<int64_t>(1, std::min<int64_t>(sm_count(), (rows + 255) / 256));
 }
 
 int vx_mlp_f32_wgrad(const vx_mlp_f32_wgrad_args* a, void* stream) {
@@ -358,7 +422,9 @@ int vx_mlp_f32_reduce(const vx_mlp_sum_job* jobs, int n_jobs, void* stream) {
     J.j[i] = SumJob{s.part, s.n_part, s.part_stride, s.part_ld, s.rows, s.cols, s.out, s.out_ld};
   }
   J.n = n_jobs;
-  dim3 grid(32, (unsigned)n_jobs);
+  int64_t most = 1;
+  for (int i = 0; i < n_jobs; ++i) most = std::max<int64_t>(most, jobs[i].rows * jobs[i].cols);
+  dim3 grid((unsigned)std::min<int64_t>((most + 31) / 32, 2048), (unsigned)n_jobs);
   sum_partials_kernel<<<grid, 256, 0, as_stream(stream)>>>(J);
   return launch_status();
 }

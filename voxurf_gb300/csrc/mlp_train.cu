@@ -784,36 +784,65 @@ struct ReduceJobs {
   int n;
 };
 
-__global__ void mlp_reduce_kernel(ReduceJobs J) {
+// Sum over the n_part partials of D[m][col] (col < NC): a block of 256
+// threads sums 32 consecutive outputs, warp w taking its contiguous eighth
+// of the partials; the eight warp sums are added in warp order (a fixed
+// order: the result does not depend on timing).
+__device__ __forceinline__ float sum_parts(const float* p, int64_t stride, int n_part, int warp) {
+  const int per = (n_part + 7) / 8, k0 = per * warp, k1 = min(n_part, k0 + per);
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  int k = k0;
+  for (; k + 4 <= k1; k += 4) {
+    a0 += p[k * stride];
+    a1 += p[(k + 1) * stride];
+    a2 += p[(k + 2) * stride];
+    a3 += p[(k + 3) * stride];
+  }
+  for (; k < k1; ++k) a0 += p[k * stride];
+  return (a0 + a1) + (a2 + a3);
+}
+
+__global__ void __launch_bounds__(256) mlp_reduce_kernel(ReduceJobs J) {
   const ReduceJob& R = J.j[blockIdx.y];
+  __shared__ float red[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t stride = (int64_t)R.WA * R.NC;
-  if (R.kind == 0) {
-    const int64_t total = (int64_t)R.WA * (R.n_out + 1);
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-      const int m = (int)(i / (R.n_out + 1)), c = (int)(i % (R.n_out + 1));
-      const int col = c < R.n_out ? c : R.WB;
-      const float* p = R.part + (int64_t)m * R.NC + col;
-      float s = 0.f;
-      for (int k = 0; k < R.n_part; ++k) s += p[k * stride];
-      if (c < R.n_out) R.w[(int64_t)m * R.n_out + c] = s;
-      else R.b[m] = s;
-    }
-  } else {
-    const int64_t total = (int64_t)3 * R.WA + 3;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-      if (i < 3 * R.WA) {
+  // outputs: kind 0: WA x (n_out + 1) (weights, then the bias column);
+  //          kind 1: 3 x WA weights, then 3 biases (from the dy partials)
+  const int64_t total = R.kind == 0 ? (int64_t)R.WA * (R.n_out + 1) : (int64_t)3 * R.WA + 3;
+  for (int64_t base = (int64_t)blockIdx.x * 32; base < total; base += (int64_t)gridDim.x * 32) {
+    const int64_t i = base + lane;
+    float s = 0.f;
+    if (i < total) {
+      if (R.kind == 0) {
+        const int m = (int)(i / (R.n_out + 1)), c = (int)(i % (R.n_out + 1));
+        const int col = c < R.n_out ? c : R.WB;
+        s = sum_parts(R.part + (int64_t)m * R.NC + col, stride, R.n_part, warp);
+      } else if (i < 3 * R.WA) {
         const int c = (int)(i / R.WA), m = (int)(i % R.WA);
         const float* p = R.part + (int64_t)m * R.NC;
-        float s = 0.f;
-        for (int k = 0; k < R.n_part; ++k) s += p[k * stride + c] + p[k * stride + c + 3];
-        R.w[(int64_t)c * R.WA + m] = s;
+        s = sum_parts(p + c, stride, R.n_part, warp) + sum_parts(p + c + 3, stride, R.n_part, warp);
       } else {
-        const int c = (int)(i - 3 * R.WA);
-        float s = 0.f;
-        for (int k = 0; k < R.n_bh; ++k) s += R.bh_part[4 * k + c];
-        R.b[c] = s;
+        s = sum_parts(R.bh_part + (i - 3 * R.WA), 4, R.n_bh, warp);
       }
     }
+    red[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && i < total) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[w][lane];
+      if (R.kind == 0) {
+        const int m = (int)(i / (R.n_out + 1)), c = (int)(i % (R.n_out + 1));
+        if (c < R.n_out) R.w[(int64_t)m * R.n_out + c] = t;
+        else R.b[m] = t;
+      } else if (i < 3 * R.WA) {
+        const int c = (int)(i / R.WA), m = (int)(i % R.WA);
+        R.w[(int64_t)c * R.WA + m] = t;
+      } else {
+        R.b[i - 3 * R.WA] = t;
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -1108,7 +1137,10 @@ int vx_mlp_train_reduce(const vx_mlp_reduce_job* jobs, int n_jobs, void* stream)
     d.n_bh = (int)s.n_bh;
   }
   J.n = n_jobs;
-  dim3 grid(64, (unsigned)n_jobs);
+  int64_t most = 1;
+  for (int i = 0; i < n_jobs; ++i)
+    most = std::max<int64_t>(most, jobs[i].kind == 0 ? jobs[i].WA * (jobs[i].n_out + 1) : 3 * jobs[i].WA + 3);
+  dim3 grid((unsigned)std::min<int64_t>((most + 31) / 32, 2048), (unsigned)n_jobs);
   mlp_reduce_kernel<<<grid, 256, 0, as_stream(stream)>>>(J);
   return launch_status();
 }
