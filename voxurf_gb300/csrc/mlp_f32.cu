@@ -64,44 +64,58 @@ __device__ __forceinline__ int64_t rows_of(int64_t n, const int64_t* n_dev) {
   return n;
 }
 
+// 4-byte asynchronous copy (rows whose stride is not a multiple of 4 floats).
+__device__ __forceinline__ void cp4(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int RG_STAGES = 3;   // shared-memory ring of the row GEMM
+constexpr int AS_LD = KC + 4;  // A stage row stride (floats): 16-byte rows, no bank conflicts
+
+// A 64-row tile of C = A Bt: each thread owns 4 rows x TN columns.  Stages of
+// KC columns of A ([64][KC] row-major) and KC rows of Bt ([KC][NP]) arrive by
+// cp.async in a three-deep ring, so the copies of the next two stages are in
+// flight while one is computed; A is read as float4 along k (one load per 4
+// k steps and row), Bt as float4 along n.
 template <int TN>
 __global__ void __launch_bounds__(THREADS, 2) rowgemm_kernel(RowGemmParams P) {
   constexpr int NP = 16 * TN;
-  __shared__ __align__(16) float As[2][KC][BM];
-  __shared__ __align__(16) float Bs[2][KC][NP];
-  __shared__ float red[16][NP];
+  // dynamic shared memory: the A ring, the Bt ring; the column-sum scratch of
+  // the epilogue reuses the A ring
+  extern __shared__ __align__(16) float rg_smem[];
+  auto As = reinterpret_cast<float (*)[BM][AS_LD]>(rg_smem);
+  auto Bs = reinterpret_cast<float (*)[KC][NP]>(rg_smem + RG_STAGES * BM * AS_LD);
+  auto red = reinterpret_cast<float (*)[NP]>(rg_smem);
+  static_assert(16 * NP <= RG_STAGES * BM * AS_LD, "column-sum scratch fits the A ring");
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int64_t M = rows_of(P.M, P.m_dev);
   const int64_t m0 = (int64_t)blockIdx.x * BM;
   if (m0 >= M && P.mode != 1) return;
   const int nk = (P.K + KC - 1) / KC;
-  // A tile loader: row am, k columns [4 aq, 4 aq + 4) of the stage
-  const int am = tid & 63, aq = tid >> 6;
-  const int64_t arow = m0 + am;
-  const bool arow_ok = arow < M;
-  const float* Arow = P.A + (arow_ok ? arow : 0) * P.lda;
   const bool avec = (P.lda & 3) == 0 && (reinterpret_cast<uintptr_t>(P.A) & 15) == 0;
 
-  auto load_a = [&](int kt, float (&r)[4]) {
-    const int k = kt * KC + 4 * aq;
-    if (arow_ok && avec && k + 4 <= P.K) {
-      const float4 v = *reinterpret_cast<const float4*>(Arow + k);
-      r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+  auto load_stage = [&](int kt, int slot) {
+    const int k0 = kt * KC;
+    if (avec) {
+      // 64 rows x 4 pieces of 16 bytes: one piece per thread
+      const int r = tid >> 2, c = 4 * (tid & 3);
+      const int64_t row = m0 + r;
+      const int valid = (row < M) ? max(0, min(4, P.K - (k0 + c))) : 0;
+      cp16(&As[slot][r][c], valid ? P.A + row * P.lda + k0 + c : P.A, (uint32_t)(4 * valid));
     } else {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) r[i] = (arow_ok && k + i < P.K) ? Arow[k + i] : 0.f;
+      for (int i = tid; i < BM * KC; i += THREADS) {
+        const int r = i / KC, c = i % KC;
+        const int64_t row = m0 + r;
+        const bool ok = row < M && k0 + c < P.K;
+        cp4(&As[slot][r][c], ok ? P.A + row * P.lda + k0 + c : P.A, ok ? 4u : 0u);
+      }
     }
-  };
-  auto store_a = [&](int s, const float (&r)[4]) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) As[s][4 * aq + i][am] = r[i];
-  };
-  // B stage: KC x NP floats, contiguous in Bt, copied asynchronously
-  auto load_b = [&](int kt, int s) {
     const float* src = P.Bt + (int64_t)kt * KC * NP;
-    float* dst = &Bs[s][0][0];
+    float* dst = &Bs[slot][0][0];
     for (int i = tid; i < KC * NP / 4; i += THREADS) cp16(dst + 4 * i, src + 4 * i, 16u);
-    cp_commit();
   };
 
   float acc[4][TN];
@@ -110,67 +124,106 @@ __global__ void __launch_bounds__(THREADS, 2) rowgemm_kernel(RowGemmParams P) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
 
-  float ra[4];
-  load_a(0, ra);
-  store_a(0, ra);
-  load_b(0, 0);
-  cp_wait_all();
-  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < RG_STAGES - 1; ++s) {
+    if (s < nk) load_stage(s, s);
+    cp_commit();
+  }
   for (int kt = 0; kt < nk; ++kt) {
-    const int s = kt & 1;
-    if (kt + 1 < nk) {
-      load_a(kt + 1, ra);
-      load_b(kt + 1, s ^ 1);
-    }
+    cp_wait_group<RG_STAGES - 2>();   // stage kt has landed (this thread's copies)
+    __syncthreads();                  // ... everyone's; slot (kt - 1) % S is free
+    if (kt + RG_STAGES - 1 < nk) load_stage(kt + RG_STAGES - 1, (kt + RG_STAGES - 1) % RG_STAGES);
+    cp_commit();
+    const int slot = kt % RG_STAGES;
 #pragma unroll
-    for (int k = 0; k < KC; ++k) {
-      const float4 a4 = *reinterpret_cast<const float4*>(&As[s][k][4 * ty]);
-      const float a[4] = {a4.x, a4.y, a4.z, a4.w};
-      float b[TN];
-      if constexpr (TN % 4 == 0) {
+    for (int k = 0; k < KC; k += 4) {
+      float a[4][4];
 #pragma unroll
-        for (int j = 0; j < TN / 4; ++j) {
-          const float4 b4 = *reinterpret_cast<const float4*>(&Bs[s][k][TN * tx + 4 * j]);
-          b[4 * j] = b4.x; b[4 * j + 1] = b4.y; b[4 * j + 2] = b4.z; b[4 * j + 3] = b4.w;
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < TN; ++j) b[j] = Bs[s][k][TN * tx + j];
+      for (int i = 0; i < 4; ++i) {
+        const float4 v = *reinterpret_cast<const float4*>(&As[slot][4 * ty + i][k]);
+        a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
       }
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int kk = 0; kk < 4; ++kk) {
+        float b[TN];
+        if constexpr (TN % 4 == 0) {
 #pragma unroll
-        for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < TN / 4; ++j) {
+            const float4 b4 = *reinterpret_cast<const float4*>(&Bs[slot][k + kk][TN * tx + 4 * j]);
+            b[4 * j] = b4.x; b[4 * j + 1] = b4.y; b[4 * j + 2] = b4.z; b[4 * j + 3] = b4.w;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < TN; ++j) b[j] = Bs[slot][k + kk][TN * tx + j];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i][kk], b[j], acc[i][j]);
+      }
     }
-    if (kt + 1 < nk) store_a(s ^ 1, ra);
-    cp_wait_all();
-    __syncthreads();
   }
+  cp_wait_group<0>();
   // epilogue
   float cs[TN];
 #pragma unroll
   for (int j = 0; j < TN; ++j) cs[j] = 0.f;
+  const int n0 = TN * tx;
+  const bool cvec = (P.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(P.C) & 15) == 0;
+  const bool hvec = P.mode == 1 && (P.ldh & 3) == 0 && (reinterpret_cast<uintptr_t>(P.H) & 15) == 0;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int64_t m = m0 + 4 * ty + i;
     if (m >= M) continue;
-    float* crow = P.C + m * P.ldc;
+    float v[TN];
 #pragma unroll
-    for (int j = 0; j < TN; ++j) {
-      const int n = TN * tx + j;
-      float v = acc[i][j];
-      if (P.mode == 0) {
-        v = fmaxf(v + P.bias[n], 0.f);
-      } else if (P.mode == 1) {
-        v = P.H[m * P.ldh + n] > 0.f ? v : 0.f;
-        cs[j] += v;
+    for (int j = 0; j < TN; ++j) v[j] = acc[i][j];
+    if (P.mode == 0) {
+#pragma unroll
+      for (int j = 0; j < TN; ++j) v[j] = fmaxf(v[j] + __ldg(P.bias + n0 + j), 0.f);
+    } else if (P.mode == 1) {
+      const float* hrow = P.H + m * P.ldh + n0;
+      bool done = false;
+      if constexpr (TN % 4 == 0) {
+        if (hvec) {
+#pragma unroll
+          for (int j = 0; j < TN; j += 4) {
+            const float4 h = __ldg(reinterpret_cast<const float4*>(hrow + j));
+            v[j] = h.x > 0.f ? v[j] : 0.f;
+            v[j + 1] = h.y > 0.f ? v[j + 1] : 0.f;
+            v[j + 2] = h.z > 0.f ? v[j + 2] : 0.f;
+            v[j + 3] = h.w > 0.f ? v[j + 3] : 0.f;
+          }
+          done = true;
+        }
       }
-      if (n < P.n_store) crow[n] = v;
+      if (!done) {
+#pragma unroll
+        for (int j = 0; j < TN; ++j) v[j] = hrow[j] > 0.f ? v[j] : 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < TN; ++j) cs[j] += v[j];
+    }
+    float* crow = P.C + m * P.ldc;
+    bool stored = false;
+    if constexpr (TN % 4 == 0) {
+      if (n0 + TN <= P.n_store && cvec) {
+#pragma unroll
+        for (int j = 0; j < TN; j += 4)
+          *reinterpret_cast<float4*>(crow + n0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        stored = true;
+      }
+    }
+    if (!stored) {
+#pragma unroll
+      for (int j = 0; j < TN; ++j)
+        if (n0 + j < P.n_store) crow[n0 + j] = v[j];
     }
   }
   if (P.mode == 1) {
+    __syncthreads();   // every thread is done with the A ring
 #pragma unroll
-    for (int j = 0; j < TN; ++j) red[ty][TN * tx + j] = cs[j];
+    for (int j = 0; j < TN; ++j) red[ty][n0 + j] = cs[j];
     __syncthreads();
     for (int n = tid; n < NP; n += THREADS) {
       float s = 0.f;
@@ -366,15 +419,21 @@ int vx_mlp_f32_rowgemm(const vx_mlp_f32_rowgemm_args* a, void* stream) {
   P.colsum = a->colsum;
   const unsigned grid = (unsigned)vx_mlp_f32_rowgemm_grid(a->M);
   cudaStream_t st = as_stream(stream);
+  auto launch = [&](auto kernel, int np) -> int {
+    const size_t smem = sizeof(float) * ((size_t)RG_STAGES * BM * AS_LD + (size_t)RG_STAGES * KC * np);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e);
+    kernel<<<grid, THREADS, smem, st>>>(P);
+    return launch_status();
+  };
   switch (a->Np) {
-    case 32: rowgemm_kernel<2><<<grid, THREADS, 0, st>>>(P); break;
-    case 64: rowgemm_kernel<4><<<grid, THREADS, 0, st>>>(P); break;
-    case 80: rowgemm_kernel<5><<<grid, THREADS, 0, st>>>(P); break;
-    case 128: rowgemm_kernel<8><<<grid, THREADS, 0, st>>>(P); break;
-    case 192: rowgemm_kernel<12><<<grid, THREADS, 0, st>>>(P); break;
+    case 32: return launch(rowgemm_kernel<2>, 32);
+    case 64: return launch(rowgemm_kernel<4>, 64);
+    case 80: return launch(rowgemm_kernel<5>, 80);
+    case 128: return launch(rowgemm_kernel<8>, 128);
+    case 192: return launch(rowgemm_kernel<12>, 192);
     default: return VX_ERR_UNSUPPORTED;
   }
-  return launch_status();
 }
 
 size_t vx_mlp_f32_wgrad_grid(int64_t rows) {
