@@ -48,9 +48,9 @@ MASK_VOXELS = 6.4  # |SDF| < 0.05 at voxel size 2/256
 K0_ELEMS = R ** 3 * 12
 SWEEP_BYTES_PER_ELEM = 28
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k0 sweep
-# launch: ncu capture at 128^3 (402.69 MB read + 253.78 MB written for
-# 25.17M elements) scaled by the element count to 256^3 (x8).
-SWEEP_NCU_TRAFFIC = (402.692608e6 + 253.783552e6) * 8 if R == 256 else None
+# launch, captured at 256^3 (the FP32 step's <12,1,1,0> launch: 3,222.35 MB
+# read + 2,363.16 MB written for 201.3M elements; a single-pass capture).
+SWEEP_NCU_TRAFFIC = 3222352128 + 2363156480 if R == 256 else None
 
 
 def bench_config() -> dict:
@@ -77,7 +77,8 @@ def parse():
     p.add_argument("--no-mesh", action="store_true", help="skip the 512^3 mesh-extraction field measurement")
     p.add_argument("--no-background", action="store_true",
                    help="skip the background-sample generator measurement (scenes without an object mask)")
-    p.add_argument("--micro", choices=["smooth", "mlp_tc", "background"], default=None,
+    p.add_argument("--micro", choices=["smooth", "mlp_tc", "background", "train_fp32", "train_bf16",
+                                       "train_bf16_nograph"], default=None,
                    help="single-kernel timing instead of the step (profiling): the Gaussian smoothing sweep "
                         "on a --grid^3 grid, the fused tensor-core MLP against the GEMM path, or the "
                         "background-sample generator and cumdist_thres")
@@ -330,7 +331,8 @@ def run_ours(args, world, rank, local):
                 "peak": peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                 else "fallback 6800 GB/s", "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                 "bytes_per_launch": alg_bytes, "launch_ms": sweep_avg,
-                "traffic": SWEEP_NCU_TRAFFIC}
+                "traffic": SWEEP_NCU_TRAFFIC, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                "one 256^3 launch" if SWEEP_NCU_TRAFFIC else None}
 
     render = None
     if not args.no_render:
@@ -455,6 +457,42 @@ def _event_ms(fn, warmup, steps):
     return e0.elapsed_time(e1) / steps
 
 
+def run_micro_train(args, dev):
+    """Training steps of one arm alone (profiling driver): `train_fp32` = the
+    plain FP32 step, `train_bf16` = the graph-replayed BF16 step,
+    `train_bf16_nograph` = the same BF16 step launched eagerly (every kernel
+    a separate launch, which profilers can attribute); --grid^3 grids,
+    8192 rays, --warmup untimed steps then --steps timed ones (no minimum)."""
+    import torch
+
+    from voxurf_gb300 import configs
+    from voxurf_gb300.fused_step import GraphedFineStep
+    from voxurf_gb300.train import FineTrainer
+
+    rk = dict(configs.FINE_RENDER_KWARGS)
+    n_b = args.warmup + args.steps
+    batches = [torch.from_numpy(a).to(dev) for a in make_batches(n_b, seed=0)]
+    prec = "fp32" if args.micro == "train_fp32" else "bf16"
+    model = configs.build_fine_model(args.grid, prec, device=dev, seed=0, mask_voxels=MASK_VOXELS)
+    tr = FineTrainer(model, n_rays=N_RAYS, graphed=prec == "bf16")
+    if args.micro == "train_bf16_nograph":
+        tr._engine = GraphedFineStep(tr, rk, use_graphs=False)
+
+    def step(i):
+        return tr.step(batches[0][i], batches[1][i], batches[2][i], batches[3][i], rk)
+
+    for i in range(args.warmup):
+        step(i)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.warmup, n_b):
+        loss, _ = step(i)
+    e1.record()
+    torch.cuda.synchronize()
+    return {"kind": args.micro, "grid": args.grid, "rays": N_RAYS, "steps": args.steps,
+            "ms_per_step": e0.elapsed_time(e1) / max(args.steps, 1), "loss": float(loss)}
+
+
 def run_micro(args, dev):
     """One kernel in isolation (CUDA events on the launching stream, warm-up
     launches first): `smooth` = vx_smooth3d / vx_smooth3d_adjoint (5^3,
@@ -471,6 +509,8 @@ def run_micro(args, dev):
 
     W, S = max(args.warmup, 3), max(args.steps, 10)
     out = {"kind": args.micro}
+    if args.micro.startswith("train_"):
+        return run_micro_train(args, dev)
     if args.micro == "background":
         from voxurf_gb300 import ub360_utils_cuda
 

@@ -204,8 +204,9 @@ int vx_grid_tv_adam_step(const float* param_in, float* param_out, float* grad, f
 /* The same sweep for a gradient that is zero outside the voxels marked in
  * touched [X*Y*Z] (uint8, 4-byte aligned; channel-last 12-channel grids
  * and 1-channel grids with Z % 4 == 0): unmarked voxels take gradient 0
- * without reading it, and zero_grad resets only the marked ones.  The
- * result equals vx_grid_tv_adam_step on the same (dense) gradient. */
+ * without reading it, and zero_grad resets only the marked ones (the marks
+ * stay set: clearing them is a memset).  The result equals
+ * vx_grid_tv_adam_step on the same (dense) gradient. */
 int vx_grid_tv_adam_step_touched(const float* param_in, float* param_out, float* grad, float* exp_avg,
                                  float* exp_avg_sq, const float* per_lr, void* shadow_bf16, int64_t C, int64_t X,
                                  int64_t Y, int64_t Z, int channel_last, int tv_enabled, float tv_weight,
@@ -392,6 +393,41 @@ typedef struct {
   int32_t has_k;            /* 1: the k-branch is used                         */
 } vx_fine_composite_bwd_args;
 int vx_fine_composite_backward(const vx_fine_composite_bwd_args* args, void* stream);
+
+/* Training-step compositing, photometric loss and compositing backward in
+ * one pass (replaces vx_fine_composite + the torch loss of run.py:604-610,
+ * 627 + vx_fine_composite_backward for the fine model with its k-branch).
+ * loss = w_main * mse(rgb_marched, target) + w_rgb0 * mse(rgb_marched0,
+ * target) + w_entropy_last * entropy(clamp(alphainv_last[N-1], 1e-6,
+ * 1-1e-6)); the k-branch logit is logit + kout.  Outputs: rgb0 / rgbk (the
+ * clamped rgb_marched), the gradients of logit (plus that of the k-branch
+ * logit when k_into_logit), of kout, of the shaded weights and of
+ * alphainv_last, and the loss (one float, sums in a fixed order).
+ * scratch >= vx_fine_composite_loss_scratch_bytes(n_rays) device bytes.
+ * The per-row pointers may be NULL when s2_off[n_rays] is 0. */
+typedef struct {
+  int64_t n_rays;           /* > 0                                              */
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;       /* [S2,3] rgbnet logits                            */
+  const float* kout;        /* [S2,3] k_rgbnet output                          */
+  const float* alphainv_last;
+  const float* target;      /* [N,3]                                           */
+  float bg;
+  float w_main, w_rgb0, w_entropy_last;
+  float* rgb0;              /* out [N,3]                                       */
+  float* rgbk;              /* out [N,3]                                       */
+  float* d_logit;           /* out [S2,3]                                      */
+  float* d_kout;            /* out [S2,3]                                      */
+  float* d_w2;              /* out [S2]                                        */
+  float* d_last;            /* out [N]                                         */
+  float* loss;              /* out [1]                                         */
+  void* scratch;
+  size_t scratch_bytes;
+  int32_t k_into_logit;     /* 1: d_logit also receives the k-branch gradient  */
+} vx_fine_composite_loss_args;
+size_t vx_fine_composite_loss_scratch_bytes(int64_t n_rays);
+int vx_fine_composite_loss(const vx_fine_composite_loss_args* args, void* stream);
 
 /* Backward of the march + features: gradients of the smoothed SDF grid
  * (accumulated into d_sdf_smooth) and of k0 (accumulated, channel-last). */
@@ -680,6 +716,17 @@ typedef struct {
 
 /* part[cta][m][n] = sum over the CTA's rows of A[row][m] * B[row][n]. */
 int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* args, void* stream);
+
+/* Up to 8 weight-gradient passes in one launch (e.g. every pass of two MLPs
+ * after their input-gradient chains): pass p runs on ctas[p] >= 1 CTAs,
+ * CTA c of the pass taking tiles c, c + ctas[p], ..., and writes ctas[p]
+ * partials (part_cap >= ctas[p] * WA * (WB + 16 ones)). */
+int vx_mlp_train_wgrad_multi(const vx_mlp_wgrad_args* passes, const int32_t* ctas, int n_passes, void* stream);
+
+/* A split of the GPU's SMs over n_passes passes in proportion to the bytes
+ * each streams per tile (WA + WB), at least 1 and at most
+ * vx_mlp_wgrad_grid(n_rows) CTAs per pass, into ctas[n_passes]. */
+int vx_mlp_wgrad_split(const vx_mlp_wgrad_args* passes, int n_passes, int32_t* ctas);
 
 /* One ordered sum of vx_mlp_train_wgrad partials.  kind 0: w[m][n] = sum
  * part[.][m][n] for n < n_out (ld n_out), b[m] = sum part[.][m][WB]; kind 1

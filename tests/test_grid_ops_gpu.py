@@ -164,12 +164,13 @@ def test_row_sweep_bit_identical_to_generic_sweep(cuda, dense):
 
 @pytest.mark.parametrize("C,dense,shadow", [(12, True, True), (12, False, False), (1, True, False),
                                             (1, False, False)])
-def test_touched_sweep_bit_identical_to_dense_sweep(cuda, C, dense, shadow):
+@pytest.mark.parametrize("Z", [36, 48])
+def test_touched_sweep_bit_identical_to_dense_sweep(cuda, C, dense, shadow, Z):
     """A gradient that is zero outside marked voxels: the sweep that reads it
     only at the marks gives bit-identical parameters, moments and shadow to
     the dense sweep; zero_grad resets exactly the marked voxels; the clear
     kernel then zeroes marked rows and the marks (incl. a ragged tail)."""
-    X, Y, Z = 7, 11, 36
+    X, Y = 7, 11
     rng = np.random.default_rng(C + 2 * int(dense))
     p = rng.normal(size=(X, Y, Z, C)).astype(np.float32)
     marks = rng.uniform(size=(X, Y, Z)) < 0.15

@@ -68,7 +68,12 @@ def test_struct_sizes_match_c_layout():
                "vx_coarse_composite_bwd_args": _abi.CoarseCompositeBwdArgs,
                "vx_coarse_backward_args": _abi.CoarseBackwardArgs, "vx_scene_desc": _abi.SceneDesc,
                "vx_view_chunk": _abi.ViewChunk, "vx_mlp_tc_args": _abi.MlpTcArgs,
-               "vx_bg_sample_args": _abi.BgSampleArgs, "vx_cast_job": _abi.CastJob}
+               "vx_bg_sample_args": _abi.BgSampleArgs, "vx_cast_job": _abi.CastJob,
+               "vx_fine_composite_loss_args": _abi.FineCompositeLossArgs, "vx_mlp_pack_job": _abi.MlpPackJob,
+               "vx_mlp_train_fwd_args": _abi.MlpTrainFwdArgs, "vx_mlp_train_bwd_args": _abi.MlpTrainBwdArgs,
+               "vx_mlp_wgrad_args": _abi.MlpWgradArgs, "vx_mlp_reduce_job": _abi.MlpReduceJob,
+               "vx_mlp_f32_rowgemm_args": _abi.MlpF32RowGemmArgs, "vx_mlp_f32_wgrad_args": _abi.MlpF32WgradArgs,
+               "vx_mlp_sum_job": _abi.MlpSumJob}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "voxurf_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

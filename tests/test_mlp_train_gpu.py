@@ -172,3 +172,44 @@ def test_mlp_train_device_row_count_and_bf16_dx(cuda):
     assert _rel(dX[:n, :d_in].float(), e_dX) <= 5e-3
     for k, v in zip(_names(L), grads):
         assert _rel(v, e_grads[k]) <= 3e-3, k
+
+
+def test_weight_gradients_of_two_mlps_in_one_launch(cuda):
+    """The weight-gradient passes of two MLPs in one launch (the SMs split
+    over eight passes) give the gradients of two separate launches up to
+    the grouping of the FP32 partial sums (rel-L2 1e-5), and the same
+    launch twice gives bit-identical gradients (fixed summation order)."""
+    from voxurf_gb300._torch import stream_ptr
+
+    n = 152 * 128 * 2 + 33
+    nets = [_net(70, 192, 3, seed=21).to(cuda), _net(60, 192, 3, seed=22).to(cuda)]
+    K0s = [80, 64]
+    g = torch.Generator().manual_seed(4)
+    engs, states, dYs = [], [], []
+    for net, K0 in zip(nets, K0s):
+        d_in = net[0].in_features
+        X = torch.zeros((n, K0), dtype=torch.bfloat16)
+        X[:, :d_in] = torch.randn((n, d_in), generator=g).to(torch.bfloat16)
+        tc = TcTrainMLP(net, K0)
+        tc.pack()
+        _, st = tc.forward(X.to(cuda))
+        engs.append(tc)
+        states.append(st)
+        dYs.append((torch.randn((n, 3), generator=g) / n).to(cuda))
+    sep = [tc.backward(st, dY, dx_dtype=torch.float32)[1] for tc, st, dY in zip(engs, states, dYs)]
+    runs = []
+    for _ in range(2):
+        pend, grads = [], []
+        for tc, st, dY in zip(engs, states, dYs):
+            _, gr, p = tc.backward_chain(st, dY, dx_dtype=torch.float32)
+            pend.append(p)
+            grads.append(gr)
+        TcTrainMLP.weight_gradients(pend, stream_ptr(cuda))
+        torch.cuda.synchronize()
+        runs.append([[t.clone() for t in gr] for gr in grads])
+    for a_list, b_list in zip(runs[0], sep):
+        for a, b in zip(a_list, b_list):
+            assert _rel(a, b) <= 1e-5
+    for a_list, b_list in zip(runs[0], runs[1]):
+        for a, b in zip(a_list, b_list):
+            assert torch.equal(a, b)

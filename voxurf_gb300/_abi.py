@@ -69,6 +69,15 @@ class FineCompositeBwdArgs(C.Structure):
     ]
 
 
+class FineCompositeLossArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("s2_off", P), ("w2", P), ("logit", P), ("kout", P), ("alphainv_last", P), ("target", P),
+        ("bg", F), ("w_main", F), ("w_rgb0", F), ("w_entropy_last", F), ("rgb0", P), ("rgbk", P), ("d_logit", P),
+        ("d_kout", P), ("d_w2", P), ("d_last", P), ("loss", P), ("scratch", P), ("scratch_bytes", C.c_size_t),
+        ("k_into_logit", I32),
+    ]
+
+
 class FineBackwardArgs(C.Structure):
     _fields_ = [
         ("n_rays", I64), ("n_rows", I64), ("rays_o", P), ("rays_d", P), ("viewdirs", P), ("near", F),
@@ -224,6 +233,7 @@ _STRUCT_FNS = {
     "vx_fine_features": FineFeaturesArgs,
     "vx_fine_composite": FineCompositeArgs,
     "vx_fine_composite_backward": FineCompositeBwdArgs,
+    "vx_fine_composite_loss": FineCompositeLossArgs,
     "vx_fine_backward": FineBackwardArgs,
     "vx_mlp_tc_forward": MlpTcArgs,
     "vx_mlp_train_forward": MlpTrainFwdArgs,
@@ -275,6 +285,10 @@ def _declare():
     lib.vx_mlp_train_pack.restype = C.c_int
     lib.vx_mlp_train_reduce.argtypes = [C.POINTER(MlpReduceJob), C.c_int, P]
     lib.vx_mlp_train_reduce.restype = C.c_int
+    lib.vx_mlp_train_wgrad_multi.argtypes = [C.POINTER(MlpWgradArgs), P, C.c_int, P]
+    lib.vx_mlp_train_wgrad_multi.restype = C.c_int
+    lib.vx_mlp_wgrad_split.argtypes = [C.POINTER(MlpWgradArgs), C.c_int, P]
+    lib.vx_mlp_wgrad_split.restype = C.c_int
     lib.vx_mlp_wgrad_grid.argtypes = [I64]
     lib.vx_mlp_wgrad_grid.restype = C.c_size_t
     lib.vx_mlp_f32_rowgemm_grid.argtypes = [I64]
@@ -291,6 +305,8 @@ def _declare():
     lib.vx_sdf_gradient_grid.restype = C.c_int
     lib.vx_sdf_gradient_grid_adjoint.argtypes = [P, P, I64, I64, I64, F, C.c_int, C.c_int, P]
     lib.vx_sdf_gradient_grid_adjoint.restype = C.c_int
+    lib.vx_fine_composite_loss_scratch_bytes.argtypes = [I64]
+    lib.vx_fine_composite_loss_scratch_bytes.restype = C.c_size_t
     lib.vx_smooth_grad_tv_scratch_bytes.argtypes = [I64, I64, I64]
     lib.vx_smooth_grad_tv_scratch_bytes.restype = C.c_size_t
     lib.vx_smooth_grad_tv.argtypes = [P, P, I64, I64, I64, F, P, P, P]
@@ -327,5 +343,6 @@ def struct_names() -> list[str]:
                                 "vx_smooth_grad_tv_scratch_bytes", "vx_smooth_grad_tv",
                                 "vx_sdf_field", "vx_density_mask", "vx_hit_coarse_geo", "vx_bg_samples_count",
                                 "vx_bg_samples_fill", "vx_cast_rows_bf16", "vx_mlp_train_pack",
-                                "vx_mlp_train_reduce", "vx_mlp_wgrad_grid", "vx_mlp_f32_rowgemm_grid",
-                                "vx_mlp_f32_wgrad_grid", "vx_mlp_f32_reduce"] + list(_SERVE_SIGNATURES)
+                                "vx_mlp_train_reduce", "vx_mlp_wgrad_grid", "vx_mlp_train_wgrad_multi", "vx_mlp_wgrad_split", "vx_mlp_f32_rowgemm_grid",
+                                "vx_mlp_f32_wgrad_grid", "vx_mlp_f32_reduce",
+                                "vx_fine_composite_loss_scratch_bytes"] + list(_SERVE_SIGNATURES)

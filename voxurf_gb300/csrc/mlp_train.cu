@@ -67,7 +67,7 @@ __host__ __device__ inline int64_t tt_off(int r, int c, int C) {
   return ((int64_t)((r >> 3) * (C >> 3) + (c >> 3)) << 6) + ((r & 7) << 3) + (c & 7);
 }
 
-__host__ inline uint32_t tmem_cols_for(int need) {
+__host__ __device__ inline uint32_t tmem_cols_for(int need) {
   uint32_t c = 32;
   while ((int)c < need) c <<= 1;
   return c;
@@ -604,6 +604,15 @@ struct WgradParams {
   int* err;
 };
 
+// Several passes in one launch: CTAs [cta0[p], cta0[p+1]) run pass p (the
+// passes of one or more MLPs stream their tiles side by side).
+constexpr int MAX_WG_PASSES = 8;
+struct WgradPasses {
+  WgradParams p[MAX_WG_PASSES];
+  int cta0[MAX_WG_PASSES + 1];
+  int n;
+};
+
 constexpr int WG_LOADERS = 4;                    // warps 0-3: loads, write-out
 constexpr int WG_THREADS = 32 * (WG_LOADERS + 1);
 constexpr uint32_t WG_TAIL = 2048;               // readable bytes after each A stage (M-tile rows past WA)
@@ -611,11 +620,16 @@ constexpr uint32_t WG_TAIL = 2048;               // readable bytes after each A 
 __host__ __device__ inline size_t wg_a_bytes(int WA) { return (size_t)TM * WA * 2 + WG_TAIL; }
 __host__ __device__ inline size_t wg_b_bytes(int WB) { return (size_t)TM * WB * 2; }
 
-__global__ void __launch_bounds__(WG_THREADS, 1) mlp_wgrad_kernel(WgradParams P, uint32_t tmem_cols) {
+__global__ void __launch_bounds__(WG_THREADS, 1) mlp_wgrad_kernel(const __grid_constant__ WgradPasses PS) {
   extern __shared__ __align__(1024) uint8_t smem[];
+  int pi = 0;
+  while (pi + 1 < PS.n && PS.cta0[pi + 1] <= (int)blockIdx.x) ++pi;
+  const WgradParams& P = PS.p[pi];
+  const int cta = (int)blockIdx.x - PS.cta0[pi], n_cta = PS.cta0[pi + 1] - PS.cta0[pi];
   const int WA = P.WA, WB = P.WB;
   const int MT = (WA + TM - 1) / TM;
   const int NC = WB + (P.ones ? 16 : 0);
+  const uint32_t tmem_cols = tmem_cols_for(MT * NC);
   const size_t ab = wg_a_bytes(WA), bbytes = wg_b_bytes(WB);
   uint8_t* As[2] = {smem, smem + ab};
   uint8_t* Bs[2] = {smem + 2 * ab, smem + 2 * ab + bbytes};
@@ -659,7 +673,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1) mlp_wgrad_kernel(WgradParams P,
   if (!mma_warp) {
     // ---- producers: tile t of this CTA into stage t % 2 ----
     int64_t t = 0;
-    for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++t) {
+    for (int64_t tile = cta; tile < n_tiles && ok; tile += n_cta, ++t) {
       const int s = (int)(t & 1);
       if (t >= 2) {
         ok = mbar_wait(bar_empty + s, (uint32_t)(((t >> 1) - 1) & 1));
@@ -696,7 +710,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1) mlp_wgrad_kernel(WgradParams P,
     const uint32_t id_w = idesc(TM, WB, 1, 1), id_1 = idesc(TM, 16, 1, 0);
     const uint32_t ones_a = smem_u32(ones_s);
     int64_t t = 0;
-    for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++t) {
+    for (int64_t tile = cta; tile < n_tiles && ok; tile += n_cta, ++t) {
       const int s = (int)(t & 1);
       ok = mbar_wait(bar_full + s, (uint32_t)((t >> 1) & 1));
       fence_after();
@@ -726,13 +740,13 @@ __global__ void __launch_bounds__(WG_THREADS, 1) mlp_wgrad_kernel(WgradParams P,
   }
   // ---- write-out: D rows (lane = m) of each M-tile ----
   if (!mma_warp) {
-    const bool any = blockIdx.x < n_tiles;
+    const bool any = cta < n_tiles;
     bool okd = true;
     if (any) {
       okd = mbar_wait(bar_done, 0);
       fence_after();
     }
-    float* part = P.part + (size_t)blockIdx.x * WA * NC;
+    float* part = P.part + (size_t)cta * WA * NC;
     for (int mt = 0; mt < MT && okd; ++mt) {
       const int m = mt * TM + 32 * warp + lane;
       const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(mt * NC);
@@ -1083,8 +1097,14 @@ size_t vx_mlp_wgrad_grid(int64_t n_rows) {
   return (size_t)std::max<int64_t>(1, std::min<int64_t>(tiles, sm_count()));
 }
 
-int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* a, void* stream) {
-  if (!a || a->n_rows < 0 || !a->part) return VX_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+// Checks one pass and fills its kernel parameters; ctas = its CTA count.
+int wgrad_pass(const vx_mlp_wgrad_args* a, int64_t ctas, vx::mt::WgradParams& P, size_t& smem) {
+  using namespace vx::mt;
+  if (!a || a->n_rows < 0 || !a->part || ctas < 1) return VX_ERR_ARG;
   if (a->n_rows > 0 && (!a->A || !a->B)) return VX_ERR_ARG;   // an empty batch writes zero partials
   if (a->WA < 16 || a->WA > 256 || a->WA % 16 || a->WB < 16 || a->WB > 240 || a->WB % 16) return VX_ERR_UNSUPPORTED;
   const int MT = (int)((a->WA + TM - 1) / TM);
@@ -1092,11 +1112,10 @@ int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* a, void* stream) {
   if (MT * NC > 512) return VX_ERR_UNSUPPORTED;
   // the last M-tile's rows past WA read (MT*128 - WA)/8 core matrices past the A stage
   if ((int64_t)(MT * TM - a->WA) * 16 > (int64_t)WG_TAIL) return VX_ERR_UNSUPPORTED;
-  const unsigned grid = (unsigned)vx_mlp_wgrad_grid(a->n_rows);
-  if (a->part_cap < (int64_t)grid * a->WA * NC) return VX_ERR_ARG;
+  if (a->part_cap < ctas * a->WA * NC) return VX_ERR_ARG;
   if (!aligned16(a->A) || !aligned16(a->B) || !aligned16(a->part)) return VX_ERR_ARG;   // (null is aligned)
   if (a->b_rows && (a->ldb < a->WB || a->ldb % 8)) return VX_ERR_ARG;
-  WgradParams P{};
+  P = WgradParams{};
   P.A = reinterpret_cast<const bf16*>(a->A);
   P.WA = (int)a->WA;
   P.B = reinterpret_cast<const bf16*>(a->B);
@@ -1108,11 +1127,84 @@ int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* a, void* stream) {
   P.n_rows_dev = a->n_rows_dev;
   P.part = a->part;
   P.err = device_error_ptr();
-  const size_t smem = wgrad_smem(P.WA, P.WB);
+  smem = std::max(smem, wgrad_smem(P.WA, P.WB));
+  return VX_OK;
+}
+
+int wgrad_launch(const vx::mt::WgradPasses& PS, size_t smem, void* stream) {
+  using namespace vx::mt;
   cudaError_t e = cudaFuncSetAttribute(mlp_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e);
-  mlp_wgrad_kernel<<<grid, WG_THREADS, smem, as_stream(stream)>>>(P, tmem_cols_for(MT * NC));
+  mlp_wgrad_kernel<<<(unsigned)PS.cta0[PS.n], WG_THREADS, smem, as_stream(stream)>>>(PS);
   return launch_status();
+}
+
+}  // namespace
+
+extern "C" {
+
+int vx_mlp_train_wgrad(const vx_mlp_wgrad_args* a, void* stream) {
+  if (!a) return VX_ERR_ARG;
+  WgradPasses PS{};
+  size_t smem = 0;
+  const int64_t grid = (int64_t)vx_mlp_wgrad_grid(a->n_rows);
+  const int s = wgrad_pass(a, grid, PS.p[0], smem);
+  if (s) return s;
+  PS.n = 1;
+  PS.cta0[0] = 0;
+  PS.cta0[1] = (int)grid;
+  return wgrad_launch(PS, smem, stream);
+}
+
+int vx_mlp_wgrad_split(const vx_mlp_wgrad_args* passes, int n_passes, int32_t* ctas) {
+  if (!passes || !ctas || n_passes < 1 || n_passes > MAX_WG_PASSES) return VX_ERR_ARG;
+  const int64_t budget = std::max<int64_t>(sm_count(), n_passes);
+  double w[MAX_WG_PASSES], tot = 0.0;
+  for (int p = 0; p < n_passes; ++p) {
+    const vx_mlp_wgrad_args& a = passes[p];
+    if (a.WA < 16 || a.WB < 16) return VX_ERR_ARG;
+    w[p] = (double)a.WA + (double)a.WB;    // bytes per tile row (both operands)
+    tot += w[p];
+  }
+  // largest remainder over the budget, then at least 1 and at most one CTA per tile
+  int64_t given = 0;
+  double rem[MAX_WG_PASSES];
+  for (int p = 0; p < n_passes; ++p) {
+    const double share = (double)budget * w[p] / tot;
+    ctas[p] = (int32_t)share;
+    rem[p] = share - (double)ctas[p];
+    given += ctas[p];
+  }
+  while (given < budget) {
+    int best = 0;
+    for (int p = 1; p < n_passes; ++p)
+      if (rem[p] > rem[best]) best = p;
+    ++ctas[best];
+    rem[best] = -1.0;
+    ++given;
+  }
+  for (int p = 0; p < n_passes; ++p) {
+    const int64_t cap = (int64_t)vx_mlp_wgrad_grid(passes[p].n_rows);
+    ctas[p] = (int32_t)std::max<int64_t>(1, std::min<int64_t>(ctas[p], cap));
+  }
+  return VX_OK;
+}
+
+int vx_mlp_train_wgrad_multi(const vx_mlp_wgrad_args* passes, const int32_t* ctas, int n_passes, void* stream) {
+  if (!passes || !ctas || n_passes < 1 || n_passes > MAX_WG_PASSES) return VX_ERR_ARG;
+  WgradPasses PS{};
+  size_t smem = 0;
+  int64_t total = 0;
+  PS.cta0[0] = 0;
+  for (int p = 0; p < n_passes; ++p) {
+    const int s = wgrad_pass(&passes[p], ctas[p], PS.p[p], smem);
+    if (s) return s;
+    total += ctas[p];
+    if (total > 65535) return VX_ERR_ARG;
+    PS.cta0[p + 1] = (int)total;
+  }
+  PS.n = n_passes;
+  return wgrad_launch(PS, smem, stream);
 }
 
 int vx_mlp_train_reduce(const vx_mlp_reduce_job* jobs, int n_jobs, void* stream) {

@@ -393,6 +393,143 @@ __global__ void __launch_bounds__(256) composite_fine_bwd_kernel(CompositeBwdPar
   }
 }
 
+// ---- compositing + photometric loss + compositing backward (training) -------
+// One warp per ray.  The forward sums of composite_fine_kernel, the loss
+// gradient of the ray's colours (known as soon as they are), then the
+// backward of composite_fine_bwd_kernel from registers: run.py:604-610 and
+// 627 (weight_main * mse(rgb_marched) + weight_rgb0 * mse(rgb_marched0) +
+// weight_entropy_last * entropy(alphainv_cum[-1])) differentiated by hand.
+// The k-branch logit is logit + kout (voxurf_fine.py:746, FP32 add).  Each
+// block leaves its two squared-error sums (rays in warp order) for
+// composite_loss_sum_kernel.
+struct CompositeLossParams {
+  int n_rays;
+  const int64_t* s2_off;
+  const float* w2;
+  const float* logit;
+  const float* kout;
+  const float* alphainv_last;
+  const float* target;
+  float bg;
+  float g_scale_k, g_scale_0;   // 2 w / (3N) for rgb_marched and rgb_marched0
+  float w_entropy;
+  float* rgb0;
+  float* rgbk;
+  float* d_logit;
+  float* d_kout;
+  float* d_w2;
+  float* d_last;
+  float2* part;                 // [gridDim.x] (sum dk^2, sum d0^2)
+  float* entropy;               // [1] entropy term of the last ray (before its weight)
+  int k_into_logit;
+};
+
+__global__ void __launch_bounds__(256) composite_loss_fine_kernel(CompositeLossParams P) {
+  __shared__ float2 wpart[8];
+  const int wib = threadIdx.x >> 5;
+  const int r = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int lane = lane_id();
+  float sk = 0.f, s0 = 0.f;
+  if (r < P.n_rays) {
+    const int64_t b = P.s2_off[r], e = P.s2_off[r + 1];
+    float a0[3] = {0.f, 0.f, 0.f}, ak[3] = {0.f, 0.f, 0.f};
+    for (int64_t i = b + lane; i < e; i += 32) {
+      const float w = P.w2[i];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float l = P.logit[3 * i + c];
+        a0[c] += w * sigmoidf_(l);
+        ak[c] += w * sigmoidf_(l + P.kout[3 * i + c]);
+      }
+    }
+    float g0[3], gk[3];
+    const float last = P.alphainv_last[r];
+    const float bgt = last * P.bg;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float t = P.target[3 * r + c];
+      const float rgb0 = warp_sum(a0[c]) + bgt;
+      const float raw = warp_sum(ak[c]) + bgt;
+      const float rgbk = fminf(fmaxf(raw, 0.f), 1.f);
+      const float d0 = rgb0 - t, dk = rgbk - t;
+      s0 += d0 * d0;
+      sk += dk * dk;
+      g0[c] = d0 * P.g_scale_0;
+      gk[c] = (raw >= 0.f && raw <= 1.f) ? dk * P.g_scale_k : 0.f;   // clamp backward
+      if (lane == 0) {
+        P.rgb0[3 * r + c] = rgb0;
+        P.rgbk[3 * r + c] = rgbk;
+      }
+    }
+    for (int64_t i = b + lane; i < e; i += 32) {
+      const float w = P.w2[i];
+      float dw = 0.f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float l = P.logit[3 * i + c];
+        const float y0 = sigmoidf_(l);
+        const float yk = sigmoidf_(l + P.kout[3 * i + c]);
+        const float dl0 = (w * g0[c]) * (1.f - y0) * y0;
+        const float dlk = (w * gk[c]) * (1.f - yk) * yk;
+        P.d_logit[3 * i + c] = P.k_into_logit ? dl0 + dlk : dl0;
+        P.d_kout[3 * i + c] = dlk;
+        dw += g0[c] * y0;
+        dw += gk[c] * yk;
+      }
+      P.d_w2[i] = dw;
+    }
+    if (lane == 0) {
+      float dl = P.bg * (g0[0] + g0[1] + g0[2] + gk[0] + gk[1] + gk[2]);
+      if (r == P.n_rays - 1 && P.w_entropy > 0.f) {
+        // pout = clamp(alphainv_last, 1e-6, 1 - 1e-6); d/dp of -(p log p + (1-p) log(1-p)) = log(1-p) - log p
+        const float lo = 1e-6f, hi = (float)(1.0 - 1e-6);
+        const float pc = fminf(fmaxf(last, lo), hi);
+        const float lp = logf(pc), lq = logf(1.f - pc);
+        P.entropy[0] = -(pc * lp + (1.f - pc) * lq);
+        if (last >= lo && last <= hi) dl += P.w_entropy * (lq - lp);
+      }
+      P.d_last[r] = dl;
+    }
+  }
+  if (lane == 0) wpart[wib] = make_float2(sk, s0);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float2 t = make_float2(0.f, 0.f);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t.x += wpart[w].x;
+      t.y += wpart[w].y;
+    }
+    P.part[blockIdx.x] = t;
+  }
+}
+
+// loss = w_main * sum_k / (3N) + w_rgb0 * sum_0 / (3N) + w_entropy * entropy,
+// the block partials added in a fixed order (each thread a contiguous run,
+// then the 256 run sums in thread order).
+__global__ void __launch_bounds__(256) composite_loss_sum_kernel(const float2* part, int n_part, const float* entropy,
+                                                                 float w_main, float w_rgb0, float w_entropy,
+                                                                 float inv_numel, float* loss) {
+  __shared__ float2 s[256];
+  const int per = (n_part + 255) / 256, k0 = threadIdx.x * per, k1 = min(n_part, k0 + per);
+  float2 t = make_float2(0.f, 0.f);
+  for (int k = k0; k < k1; ++k) {
+    t.x += part[k].x;
+    t.y += part[k].y;
+  }
+  s[threadIdx.x] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float2 a = make_float2(0.f, 0.f);
+    for (int i = 0; i < 256; ++i) {
+      a.x += s[i].x;
+      a.y += s[i].y;
+    }
+    float l = w_main * (a.x * inv_numel) + w_rgb0 * (a.y * inv_numel);
+    if (w_entropy > 0.f) l += w_entropy * entropy[0];
+    loss[0] = l;
+  }
+}
+
 // ---- backward: features of shaded rows -> dense gradient grids ---------------
 struct FeatBwdParams {
   int64_t n_rows;
@@ -1315,6 +1452,49 @@ int vx_fine_composite_backward(const vx_fine_composite_bwd_args* A, void* stream
   P.d_last = A->d_last;
   P.has_k = A->has_k;
   composite_fine_bwd_kernel<<<warp_blocks(A->n_rays), 256, 0, as_stream(stream)>>>(P);
+  return launch_status();
+}
+
+size_t vx_fine_composite_loss_scratch_bytes(int64_t n_rays) {
+  return (size_t)(warp_blocks(n_rays > 0 ? n_rays : 1) + 2) * sizeof(float2);
+}
+
+int vx_fine_composite_loss(const vx_fine_composite_loss_args* A, void* stream) {
+  if (!A || A->n_rays <= 0) return VX_ERR_ARG;
+  // the per-row buffers (w2, logit, kout, d_logit, d_kout, d_w2) are read
+  // only for rows that s2_off gives; they may be NULL when there are none
+  if (!A->s2_off || !A->alphainv_last || !A->target || !A->rgb0 || !A->rgbk || !A->d_last || !A->loss ||
+      !A->scratch)
+    return VX_ERR_ARG;
+  if (A->n_rays > INT32_MAX / 32) return VX_ERR_TOO_LARGE;
+  if (A->scratch_bytes < vx_fine_composite_loss_scratch_bytes(A->n_rays)) return VX_ERR_ARG;
+  CompositeLossParams P{};
+  P.n_rays = (int)A->n_rays;
+  P.s2_off = A->s2_off;
+  P.w2 = A->w2;
+  P.logit = A->logit;
+  P.kout = A->kout;
+  P.alphainv_last = A->alphainv_last;
+  P.target = A->target;
+  P.bg = A->bg;
+  const double numel = 3.0 * (double)A->n_rays;
+  P.g_scale_k = (float)(2.0 * (double)A->w_main / numel);
+  P.g_scale_0 = (float)(2.0 * (double)A->w_rgb0 / numel);
+  P.w_entropy = A->w_entropy_last;
+  P.rgb0 = A->rgb0;
+  P.rgbk = A->rgbk;
+  P.d_logit = A->d_logit;
+  P.d_kout = A->d_kout;
+  P.d_w2 = A->d_w2;
+  P.d_last = A->d_last;
+  const unsigned blocks = warp_blocks(A->n_rays);
+  P.part = reinterpret_cast<float2*>(A->scratch);
+  P.entropy = reinterpret_cast<float*>(P.part + blocks + 1);
+  P.k_into_logit = A->k_into_logit;
+  cudaStream_t st = as_stream(stream);
+  composite_loss_fine_kernel<<<blocks, 256, 0, st>>>(P);
+  composite_loss_sum_kernel<<<1, 256, 0, st>>>(P.part, (int)blocks, P.entropy, A->w_main, A->w_rgb0,
+                                                 A->w_entropy_last, (float)(1.0 / numel), A->loss);
   return launch_status();
 }
 

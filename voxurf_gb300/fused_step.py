@@ -95,6 +95,8 @@ class GraphedFineStep:
         self.s2_off = torch.empty(N + 1, dtype=i64, device=dev)
         self.scan_bytes = int(_native.load().vx_scan_scratch_bytes(N))
         self.scan_tmp = torch.empty(max(self.scan_bytes, 16), dtype=torch.uint8, device=dev)
+        _abi._declare()
+        self.loss_scratch_bytes = int(_native.load().vx_fine_composite_loss_scratch_bytes(N))
         # gradients (the optimizer's p.grad) and per-step device scalars
         self.d_sdf_s = torch.empty((X, Y, Z), dtype=f32, device=dev)
         self.d_sdf = torch.zeros_like(model.sdf.grid)
@@ -164,10 +166,18 @@ class GraphedFineStep:
         for p, g in zip(self.rgb_params + self.k_params, entry["grads"]):
             p.grad = g
         self.k0_group["touched"] = self.k0_touched
+        # the k0 sweep (TV + Adam) resets the touched gradient rows (part B
+        # clears the marks); without a TV weight k0 takes the plain Adam
+        # update, so reset the rows here
+        sweep_resets = bool(self.k0_group.get("tv_weight", 0.0))
         try:
             tr.optimizer.step(zero_grad=True)
         finally:
             self.k0_group.pop("touched", None)
+        if not sweep_resets:
+            X, Y, Z = self.XYZ
+            _native.call("vx_grid_clear_touched", ptr(self.d_k0), ptr(self.k0_touched), X * Y * Z, 12,
+                         stream_ptr(self.dev))
         return entry["loss"], S2
 
     def _pick_capacity(self, S2: int, kptr: int) -> int:
@@ -186,7 +196,13 @@ class GraphedFineStep:
         side = torch.cuda.Stream(self.dev)
         side.wait_stream(torch.cuda.current_stream(self.dev))
         with torch.cuda.stream(side):
-            self._part_b(cap)            # warm-up (idempotent: accumulators are cleared first)
+            self._part_b(cap)            # warm-up
+            # the k0 gradient accumulates over the touched voxels and is reset
+            # by the optimizer sweep: undo the warm-up's contribution before
+            # the replay (the sdf gradient buffer is cleared by part B itself)
+            X, Y, Z = self.XYZ
+            _native.call("vx_grid_clear_touched", ptr(self.d_k0), ptr(self.k0_touched), X * Y * Z, 12,
+                         stream_ptr(self.dev))
         torch.cuda.current_stream(self.dev).wait_stream(side)
         g = torch.cuda.CUDAGraph()
         c0 = _native.launch_count()
@@ -237,8 +253,10 @@ class GraphedFineStep:
         n_rows_dev = self.s2_off[N:]          # device S2
         self.dyn.copy_(self.dyn_host, non_blocking=True)
         self.d_sdf_s.zero_()
+        # the marks of the previous step's scatter (its gradient rows were
+        # reset by the optimizer sweep, which reads the marks)
+        self.k0_touched.zero_()
         X, Y, Z = self.XYZ
-        _native.call("vx_grid_clear_touched", ptr(self.d_k0), ptr(self.k0_touched), X * Y * Z, 12, st)
         o, d, v, target = self.inp[0], self.inp[1], self.inp[2], self.inp[3]
         # compaction
         ray2 = torch.empty(cap, dtype=i32, device=dev)
@@ -278,48 +296,45 @@ class GraphedFineStep:
         cols = X2[:, self.d2a:self.d2a + 3] if self.k_res else None
         logit, st1 = self.eng1.forward(X1, train=True, cols=cols, n_rows_dev=n_rows_dev, saved=sv[0])
         kout, st2 = self.eng2.forward(X2, train=True, n_rows_dev=n_rows_dev, saved=sv[1])
-        klogit = logit + kout
-        # compositing
+        # compositing, loss (run.py:604-610, 627, fine dtu_e2e weights) and the
+        # compositing backward in one pass; rows at or beyond S2 stay unwritten
+        # (the tensor-core MLP backward reads S2 rows; the FP32 engine runs
+        # over the capacity and needs zeros there)
+        wm, we, w0 = self.tr.loss_weights
         rgb0 = torch.empty((N, 3), dtype=f32, device=dev)
         rgbk = torch.empty((N, 3), dtype=f32, device=dev)
-        rgbk_raw = torch.empty((N, 3), dtype=f32, device=dev)
-        a = _abi.FineCompositeArgs()
-        a.n_rays, a.s2_off, a.w2 = N, ptr(self.s2_off), ptr(w2)
-        a.logit, a.klogit, a.alphainv_last, a.bg = ptr(logit), ptr(klogit), ptr(self.alast), self.bg
-        a.rgb0, a.rgbk, a.rgbk_raw, a.has_k = ptr(rgb0), ptr(rgbk), ptr(rgbk_raw), 1
-        _abi.call_struct("vx_fine_composite", a, st)
-        # loss (run.py:604-636, fine dtu_e2e weights) and its gradient
-        wm, we, w0 = self.tr.loss_weights
-        dk = rgbk - target
-        d0 = rgb0 - target
-        loss = wm * (dk * dk).mean() + w0 * (d0 * d0).mean()
-        g_rgbk = dk * (2.0 * wm / dk.numel())
-        g_rgb0 = d0 * (2.0 * w0 / d0.numel())
-        g_last = torch.zeros(N, dtype=f32, device=dev)
-        if we > 0:
-            p_raw = self.alast[N - 1:]
-            pc = p_raw.clamp(1e-6, 1 - 1e-6)
-            loss = loss + we * (-(pc * torch.log(pc) + (1 - pc) * torch.log(1 - pc))).mean()
-            inside = ((p_raw >= 1e-6) & (p_raw <= 1 - 1e-6)).float()
-            g_last[N - 1:] = we * (torch.log(1 - pc) - torch.log(pc)) * inside
-        # compositing backward
-        d_logit = torch.zeros((cap, 3), dtype=f32, device=dev)
-        d_klogit = torch.zeros((cap, 3), dtype=f32, device=dev)
+        loss = torch.empty(1, dtype=f32, device=dev)
+        rows_alloc = torch.empty if self.bf16 else torch.zeros
+        d_logit = rows_alloc((cap, 3), dtype=f32, device=dev)
+        d_klogit = rows_alloc((cap, 3), dtype=f32, device=dev)
         d_w2 = torch.empty(cap, dtype=f32, device=dev)
         d_last = torch.empty(N, dtype=f32, device=dev)
-        b = _abi.FineCompositeBwdArgs()
-        b.n_rays, b.s2_off, b.w2, b.logit = N, ptr(self.s2_off), ptr(w2), ptr(logit)
-        b.klogit, b.rgbk_raw = ptr(klogit), ptr(rgbk_raw)
-        b.g_rgb0, b.g_rgbk, b.bg, b.g_last_in = ptr(g_rgb0), ptr(g_rgbk), self.bg, ptr(g_last)
-        b.d_logit, b.d_klogit, b.d_w2, b.d_last, b.has_k = ptr(d_logit), ptr(d_klogit), ptr(d_w2), ptr(d_last), 1
-        _abi.call_struct("vx_fine_composite_backward", b, st)
+        nb = self.loss_scratch_bytes
+        scratch = torch.empty(nb, dtype=torch.uint8, device=dev)
+        a = _abi.FineCompositeLossArgs()
+        a.n_rays, a.s2_off, a.w2 = N, ptr(self.s2_off), ptr(w2)
+        a.logit, a.kout, a.alphainv_last, a.target, a.bg = ptr(logit), ptr(kout), ptr(self.alast), ptr(target), \
+            self.bg
+        a.w_main, a.w_rgb0, a.w_entropy_last = wm, w0, we
+        a.rgb0, a.rgbk, a.d_logit, a.d_kout, a.d_w2, a.d_last = ptr(rgb0), ptr(rgbk), ptr(d_logit), \
+            ptr(d_klogit), ptr(d_w2), ptr(d_last)
+        a.loss, a.scratch, a.scratch_bytes = ptr(loss), ptr(scratch), nb
+        a.k_into_logit = int(not model.k_detach_2)
+        _abi.call_struct("vx_fine_composite_loss", a, st)
         # MLP backward (k-branch first: its logit input may feed d_logit)
-        dX2, g2 = self.eng2.backward(st2, d_klogit, dx_dtype=xdt, grads=self.g2, work=sv[3])
-        if not model.k_detach_2:
-            d_logit = d_logit + d_klogit
-        if self.k_res and not model.k_detach_1:
-            d_logit = d_logit + dX2[:, self.d2a:self.d2a + 3].float()
-        dX1, g1 = self.eng1.backward(st1, d_logit, dx_dtype=xdt, grads=self.g1, work=sv[2])
+        if self.bf16:
+            # both input-gradient chains, then the weight-gradient passes of
+            # both MLPs in one launch and their sums in another
+            dX2, g2, pend2 = self.eng2.backward_chain(st2, d_klogit, dx_dtype=xdt, grads=self.g2, work=sv[3])
+            if self.k_res and not model.k_detach_1:
+                d_logit = d_logit + dX2[:, self.d2a:self.d2a + 3].float()
+            dX1, g1, pend1 = self.eng1.backward_chain(st1, d_logit, dx_dtype=xdt, grads=self.g1, work=sv[2])
+            TcTrainMLP.weight_gradients([pend2, pend1], st)
+        else:
+            dX2, g2 = self.eng2.backward(st2, d_klogit, dx_dtype=xdt, grads=self.g2, work=sv[3])
+            if self.k_res and not model.k_detach_1:
+                d_logit = d_logit + dX2[:, self.d2a:self.d2a + 3].float()
+            dX1, g1 = self.eng1.backward(st1, d_logit, dx_dtype=xdt, grads=self.g1, work=sv[2])
         # march / feature backward into the grid gradients
         bw = _abi.FineBackwardArgs()
         bw.n_rays, bw.n_rows = N, cap
@@ -340,4 +355,4 @@ class GraphedFineStep:
                       X, Y, Z, self.taps.ctypes.data, len(self.taps), 0, st)
         else:
             self.d_sdf.view(X, Y, Z).copy_(self.d_sdf_s)
-        return {"loss": loss.detach(), "grads": g1 + g2, "S2_cap": cap}
+        return {"loss": loss[0], "grads": g1 + g2, "S2_cap": cap}

@@ -439,6 +439,16 @@ class TcTrainMLP:
         """dX [n, K0] (dx_dtype) and the FP32 gradients [dW0, db0, ..., dWh, dbh]
         (written into `grads` when given).  `work` may pass preallocated
         scratch (graph capture)."""
+        dX, grads, pending = self.backward_chain(st, dY, dx_dtype, grads, dX, work)
+        TcTrainMLP.weight_gradients([pending], stream_ptr(dY.device))
+        return dX, grads
+
+    def backward_chain(self, st: dict, dY: torch.Tensor, dx_dtype=torch.bfloat16, grads: list | None = None,
+                       dX: torch.Tensor | None = None, work: dict | None = None):
+        """The input-gradient chain alone: dX and the dz T-tiles of every
+        layer.  Returns (dX, grads, pending); the weight gradients are
+        written into grads by weight_gradients([pending, ...]), which runs
+        the weight-gradient passes of several MLPs in one launch."""
         from . import _abi, _native
 
         lib = _native.load()
@@ -472,25 +482,47 @@ class TcTrainMLP:
         _abi.call_struct("vx_mlp_train_backward", b, stp)
         H, dZ = st["H"].data_ptr(), w["dZ"].data_ptr()
         lay = cap * W * 2   # bytes per layer of T-tiles
-        jobs = []
+        R = _abi.MlpReduceJob
+        pending = []   # (pass arguments, reduce job of its n_part partials)
 
-        def wgrad(A, WA, B, WB, ldb, b_rows, ones, part):
+        def wgrad(A, WA, B, WB, ldb, b_rows, ones, part, job):
             g = _abi.MlpWgradArgs()
             g.n_rows, g.n_rows_dev, g.A, g.WA, g.B, g.WB, g.ldb = n, ptr(st["n_rows_dev"]), A, WA, B, WB, ldb
             g.b_rows, g.ones, g.part, g.part_cap = b_rows, ones, ptr(part), part.numel()
-            _abi.call_struct("vx_mlp_train_wgrad", g, stp)
+            pending.append((g, job))
 
-        R = _abi.MlpReduceJob
         for l in range(1, L):   # dW_l = dz_{l+1}^T h_l
-            wgrad(dZ + l * lay, W, H + (l - 1) * lay, W, 0, 0, 1, w["part"][l - 1])
-            jobs.append(R(w["part"][l - 1].data_ptr(), grid, W, W + 16, 0, 0, W, W, grads[2 * l].data_ptr(),
-                          grads[2 * l + 1].data_ptr(), None, 0))
-        wgrad(dZ, W, X.data_ptr(), K0, X.stride(0), 1, 1, w["part0"])      # dW_0 = dz_1^T X
-        jobs.append(R(w["part0"].data_ptr(), grid, W, K0 + 16, 0, 0, K0, self.d_in, grads[0].data_ptr(),
-                      grads[1].data_ptr(), None, 0))
-        wgrad(H + (L - 1) * lay, W, w["dYT"].data_ptr(), 16, 0, 0, 0, w["parth"])   # dWh = dy^T h_L
-        jobs.append(R(w["parth"].data_ptr(), grid, W, 16, 1, 0, 16, 3, grads[2 * L].data_ptr(),
-                      grads[2 * L + 1].data_ptr(), w["dbh"].data_ptr(), grid))
-        arr = (R * len(jobs))(*jobs)
-        _abi.call("vx_mlp_train_reduce", arr, len(jobs), stp)
-        return dX, grads
+            pl = w["part"][l - 1]
+            wgrad(dZ + l * lay, W, H + (l - 1) * lay, W, 0, 0, 1, pl,
+                  lambda k, pl=pl, l=l: R(pl.data_ptr(), k, W, W + 16, 0, 0, W, W, grads[2 * l].data_ptr(),
+                                          grads[2 * l + 1].data_ptr(), None, 0))
+        wgrad(dZ, W, X.data_ptr(), K0, X.stride(0), 1, 1, w["part0"],      # dW_0 = dz_1^T X
+              lambda k: R(w["part0"].data_ptr(), k, W, K0 + 16, 0, 0, K0, self.d_in, grads[0].data_ptr(),
+                          grads[1].data_ptr(), None, 0))
+        wgrad(H + (L - 1) * lay, W, w["dYT"].data_ptr(), 16, 0, 0, 0, w["parth"],   # dWh = dy^T h_L
+              lambda k: R(w["parth"].data_ptr(), k, W, 16, 1, 0, 16, 3, grads[2 * L].data_ptr(),
+                          grads[2 * L + 1].data_ptr(), w["dbh"].data_ptr(), grid))
+        return dX, grads, pending
+
+    @staticmethod
+    def weight_gradients(pendings: list, stream: int) -> None:
+        """Every weight-gradient pass of the given backward_chain results in
+        one launch per 8 passes (the SMs split over the passes in proportion
+        to their bytes), then their ordered sums in one launch per 8."""
+        import ctypes
+
+        from . import _abi, _native
+
+        lib = _native.load()
+        _abi._declare()
+        items = [it for p in pendings for it in p]
+        for i in range(0, len(items), 8):
+            grp = items[i:i + 8]
+            k = len(grp)
+            arr = (_abi.MlpWgradArgs * k)(*[g for g, _ in grp])
+            ctas = (ctypes.c_int32 * k)()
+            _native.check(lib.vx_mlp_wgrad_split(arr, k, ctas), "vx_mlp_wgrad_split")
+            _native.check(lib.vx_mlp_train_wgrad_multi(arr, ctas, k, stream), "vx_mlp_train_wgrad_multi")
+            jobs = [mk(int(ctas[j])) for j, (_, mk) in enumerate(grp)]
+            _abi.call("vx_mlp_train_reduce", (_abi.MlpReduceJob * k)(*jobs), k, stream)
+

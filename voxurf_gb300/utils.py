@@ -119,10 +119,14 @@ class Adam(torch.optim.Optimizer):
         C, X, Y, Z = p.size(1), p.size(2), p.size(3), p.size(4)
         cl = C > 1 and not p.is_contiguous()
         shadow = group.get("shadow")
+        touched = group.get("touched")
+        # with a touched map, zero_grad also resets the marked gradient rows in
+        # the same sweep (the gradient buffer is then reused by the next
+        # step's scatter); without one, the gradient is dropped
+        reset = int(bool(zero_grad) and touched is not None)
         args = (ptr(p), ptr(spare), ptr(g), ptr(state["exp_avg"]), ptr(state["exp_avg_sq"]), ptr(per_lr),
                 ptr(shadow), C, X, Y, Z, int(cl), 1, float(tv_w), int(bool(group.get("tv_dense", True))),
-                float(group["lr"]), float(beta1), float(beta2), float(group["eps"]), int(state["step"]), 0)
-        touched = group.get("touched")
+                float(group["lr"]), float(beta1), float(beta2), float(group["eps"]), int(state["step"]), reset)
         if touched is not None:
             # the gradient is zero outside the marked voxels (the fused step's scatter)
             call("vx_grid_tv_adam_step_touched", *args, ptr(touched), st)
