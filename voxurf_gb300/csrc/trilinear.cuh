@@ -144,4 +144,124 @@ __device__ __forceinline__ void mark_corners(uint8_t* __restrict__ touched, cons
   }
 }
 
+// ---- aggregated scatters ----------------------------------------------------
+// Probes of one point along one axis a (the finite differences of the SDF
+// gradient and the hierarchical features) move only coordinate a: every
+// probe's eight corners share the point's two b and two c corners, so their
+// contributions are summed per a-plane in registers and each plane leaves
+// with one reduction per (b, c) corner.  PlaneAcc covers the planes
+// floor(ind_a) - 3 .. floor(ind_a) + 4 (probes up to 3 voxels away); a
+// contribution outside that window goes straight to the grid.
+constexpr int VX_PLANES = 8;
+
+struct PlaneAcc {
+  float v[VX_PLANES];
+  int base;  // plane of slot 0
+};
+
+__device__ __forceinline__ void plane_acc_init(PlaneAcc& A, float ind_a) {
+#pragma unroll
+  for (int s = 0; s < VX_PLANES; ++s) A.v[s] = 0.f;
+  A.base = (int)floorf(ind_a) - 3;
+}
+
+// Adds the contribution d of a trilinear lookup at ind with coordinate a
+// replaced by x (the planes floor(x) and floor(x) + 1).
+__device__ __forceinline__ void plane_acc_add(PlaneAcc& A, float* __restrict__ grid, const GridGeom& g,
+                                              const float ind[3], int a, float x, float d) {
+  if (d == 0.f) return;
+  const float x0f = floorf(x);
+  const int s0 = (int)x0f - A.base;
+  if (s0 >= 0 && s0 + 1 < VX_PLANES) {
+    const float t = x - x0f;
+    // the slot is a run-time index: every slot takes a selected addend (zero
+    // for all but two) so the accumulator stays in registers
+#pragma unroll
+    for (int s = 0; s < VX_PLANES; ++s) {
+      const float add = (s == s0) ? d * (1.f - t) : ((s == s0 + 1) ? d * t : 0.f);
+      A.v[s] += add;
+    }
+  } else {
+    float p[3] = {ind[0], ind[1], ind[2]};
+    p[a] = x;
+    scatter1(grid, corners_of(g, p[0], p[1], p[2]), d);
+  }
+}
+
+// One reduction per in-grid (plane, b, c) corner with a nonzero sum.
+__device__ __forceinline__ void plane_acc_flush(const PlaneAcc& A, float* __restrict__ grid, const GridGeom& g,
+                                                const float ind[3], int a) {
+  const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+  const float fb0 = floorf(ind[b]), fc0 = floorf(ind[c]);
+  const int b0 = (int)fb0, c0 = (int)fc0;
+  const float tb = ind[b] - fb0, tc = ind[c] - fc0;
+  const float wb[2] = {1.f - tb, tb}, wc[2] = {1.f - tc, tc};
+  const int na = gsize(g, a), nb = gsize(g, b), nc = gsize(g, c);
+  const int64_t sa = a == 0 ? (int64_t)g.Y * g.Z : (a == 1 ? g.Z : 1);
+  const int64_t sb = b == 0 ? (int64_t)g.Y * g.Z : (b == 1 ? g.Z : 1);
+  const int64_t sc = c == 0 ? (int64_t)g.Y * g.Z : (c == 1 ? g.Z : 1);
+#pragma unroll
+  for (int s = 0; s < VX_PLANES; ++s) {
+    const int pa = A.base + s;
+    if (A.v[s] == 0.f || pa < 0 || pa >= na) continue;
+#pragma unroll
+    for (int db = 0; db < 2; ++db)
+#pragma unroll
+      for (int dc = 0; dc < 2; ++dc) {
+        const int jb = b0 + db, jc = c0 + dc;
+        const float w = wb[db] * wc[dc];
+        if (jb < 0 || jb >= nb || jc < 0 || jc >= nc || w == 0.f) continue;
+        atomicAdd(grid + pa * sa + jb * sb + jc * sc, A.v[s] * w);
+      }
+  }
+}
+
+// Channel-last 12-channel scatter of one trilinear lookup per lane (at
+// continuous index fi, fj, fk), reduced over the lanes of a warp first: the
+// rows of a warp are consecutive shaded samples (ray-major, 0.5 voxel
+// apart), so runs of lanes share a corner voxel.  For each corner q the runs
+// of equal voxel offsets are summed by a segmented reduction (five shuffle
+// steps) and the run's first lane issues the three red.global.add.v4 of the
+// sum.  All 32 lanes must call it; a lane without a lookup passes live =
+// false.  Corner weights and offsets are those of corners_of.
+__device__ __forceinline__ void scatter12_warp(float* __restrict__ grid, const GridGeom& g, float fi, float fj,
+                                               float fk, const float d[12], bool live) {
+  const unsigned full = 0xffffffffu;
+  const int lane = lane_id();
+  const float fi0 = floorf(fi), fj0 = floorf(fj), fk0 = floorf(fk);
+  const int i0 = (int)fi0, j0 = (int)fj0, k0 = (int)fk0;
+  const float ti = fi - fi0, tj = fj - fj0, tk = fk - fk0;
+#pragma unroll 1
+  for (int q = 0; q < 8; ++q) {
+    const int di = q >> 2, dj = (q >> 1) & 1, dk = q & 1;
+    const int ii = i0 + di, jj = j0 + dj, kk = k0 + dk;
+    const bool in = (ii >= 0) & (ii < g.X) & (jj >= 0) & (jj < g.Y) & (kk >= 0) & (kk < g.Z);
+    const float w = (di ? ti : 1.f - ti) * (dj ? tj : 1.f - tj) * (dk ? tk : 1.f - tk);
+    const int key = (live && in && w != 0.f) ? (ii * g.Y + jj) * g.Z + kk : -1;
+    if (__all_sync(full, key < 0)) continue;
+    const int nxt = __shfl_down_sync(full, key, 1);
+    const int prv = __shfl_up_sync(full, key, 1);
+    const unsigned tails = __ballot_sync(full, lane == 31 || nxt != key);
+    const int seg_end = lane + __ffs(tails >> lane) - 1;
+    const float wq = key >= 0 ? w : 0.f;
+    float v[12];
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) v[ch] = wq * d[ch];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const bool take = lane + o <= seg_end;
+#pragma unroll
+      for (int ch = 0; ch < 12; ++ch) {
+        const float t = __shfl_down_sync(full, v[ch], o);
+        if (take) v[ch] += t;
+      }
+    }
+    if ((lane == 0 || prv != key) && key >= 0) {
+      float* p = grid + (int64_t)key * 12;
+#pragma unroll
+      for (int u = 0; u < 3; ++u) red_add_v4(p + 4 * u, v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+    }
+  }
+}
+
 }  // namespace vx
