@@ -960,6 +960,10 @@ typedef struct {
   int32_t n_samples;        /* int(|grid shape + 1| / stepsize) + 1 */
   int32_t outbbox_only;     /* 1: the coarse model's additional mask_outbbox test */
   int64_t n_rays;
+  int32_t inner;            /* 1: the foreground samples instead (:846-849): the
+                               points with |p| < 1, not inverted, no distance
+                               test; outer_pts receives p, pts_org may be NULL */
+  int32_t reserved;
 } vx_bg_sample_args;
 
 /* Phase 1: counts [n_rays] kept samples per ray and offsets [n_rays+1]
@@ -973,6 +977,105 @@ int vx_bg_samples_count(const vx_bg_sample_args* args, int64_t* counts, int64_t*
  * vx_device_error(). */
 int vx_bg_samples_fill(const vx_bg_sample_args* args, const int64_t* offsets, int64_t capacity, float* outer_pts,
                        float* pts_org, int64_t* ray_id, int64_t* step_id, void* stream);
+
+/* ---- the maskless fine model (lib/voxurf_womask_fine.py:833-1071) ----
+ * Foreground samples: vx_bg_samples_* with inner = 1; their feature rows:
+ * vx_fine_features / vx_fine_backward (n_rays = 0); weights:
+ * vx_alpha2weight. */
+
+/* Foreground alpha (forward, d_alpha == NULL): the SDF and its +-1-voxel
+ * finite-difference gradient on the smoothed grid at each sample
+ * (grid_sampler(..., sample_grad=True, displace=1.0), :876) and the NeuS
+ * alpha of neus_alpha_from_sdf_scatter(use_mid) (:879-880, :606-634).
+ * Backward (d_alpha != NULL): the alpha adjoint accumulated into
+ * d_sdf_smooth. */
+typedef struct {
+  int64_t n;                /* samples                                          */
+  const float* pts;         /* [n,3]                                            */
+  const int64_t* ray_id;    /* [n]                                              */
+  const float* viewdirs;    /* [N,3]                                            */
+  vx_grid_geom grid;
+  const float* sdf_smooth;  /* [X,Y,Z]                                          */
+  float voxel_size, inv_s, dist;
+  float* alpha;             /* forward out [n]                                  */
+  const float* d_alpha;     /* backward in [n], or NULL for the forward         */
+  float* d_sdf_smooth;      /* backward: accumulated [X,Y,Z]                    */
+} vx_womask_fg_alpha_args;
+int vx_womask_fg_alpha(const vx_womask_fg_alpha_args* args, void* stream);
+
+/* Background alpha: bg_density (trilinear, zero padding) at the inverted
+ * points and activate_density, alpha = 1 - exp(-softplus(d + act_shift) *
+ * interval) (:898-900, :542-544); backward (d_alpha != NULL) accumulates
+ * into d_density. */
+typedef struct {
+  int64_t n;
+  const float* pts;         /* [n,3] inverted points                            */
+  vx_grid_geom grid;        /* the background grid                              */
+  const float* density;     /* [X,Y,Z]                                          */
+  float act_shift, interval;
+  float* alpha;             /* forward out [n]                                  */
+  const float* d_alpha;     /* backward in [n] or NULL                          */
+  float* d_density;         /* backward: accumulated [X,Y,Z]                    */
+} vx_womask_bg_alpha_args;
+int vx_womask_bg_alpha(const vx_womask_bg_alpha_args* args, void* stream);
+
+/* Background MLP rows (:955-970): [bg_k0 at the inverted point (12, when
+ * bg_k0 != NULL), PE((p_org - xyz_min) / (xyz_max - xyz_min), posbase_pe),
+ * PE(viewdir, viewbase_pe)], zero to ld; a negative PE count leaves that
+ * block out.  Backward (dX != NULL): columns 0-11 of dX accumulated into
+ * d_bg_k0 [X,Y,Z,12]. */
+typedef struct {
+  int64_t n;
+  const float* outer_pts;   /* [n,3] inverted                                   */
+  const float* pts_org;     /* [n,3]                                            */
+  const int64_t* ray_id;    /* [n]                                              */
+  const float* viewdirs;    /* [N,3]                                            */
+  vx_grid_geom grid;        /* the background grid (xyz_min/max also normalise) */
+  const float* bg_k0;       /* [X,Y,Z,12] or NULL                               */
+  int64_t posbase_pe, viewbase_pe;
+  int64_t ld;
+  void* X;                  /* forward out [n, ld] (BF16 when bf16)              */
+  int32_t bf16, reserved;
+  const void* dX;           /* backward in [n, ld] or NULL                      */
+  float* d_bg_k0;           /* backward: accumulated                            */
+} vx_womask_bg_features_args;
+int vx_womask_bg_features(const vx_womask_bg_features_args* args, void* stream);
+
+/* Foreground/background compositing (:972-1012).  Per ray r: s0 = sum w
+ * sigmoid(logit), sk = sum w sigmoid(logit + kout), cum = sum w over rows
+ * [fg_off[r], fg_off[r+1]); sb = sum w_bg sigmoid(bg_logit) over
+ * [bg_off[r], bg_off[r+1]); bg = clamp(sb, 0, 1); rgb0 = clamp(clamp(s0) +
+ * (1 - cum) bg), rgbk = clamp(clamp(sk) + (1 - cum) bg), ainv = 1 - cum,
+ * in_marched = clamp(sk) (clamp(s0) without k-branch), bg_marched = bg; the
+ * per-ray sums go to stats [N,10] for the backward.  Backward (d_w !=
+ * NULL): gradients of logit (plus the k-branch's when k_into_logit), kout,
+ * w, bg_logit and w_bg from g_rgb0, g_rgbk, g_ainv (each may be NULL). */
+typedef struct {
+  int64_t n_rays;
+  const int64_t* fg_off;    /* [N+1]                                            */
+  const float* w;           /* [S]                                              */
+  const float* logit;       /* [S,3]                                            */
+  const float* kout;        /* [S,3] or NULL (no k-branch)                      */
+  const int64_t* bg_off;    /* [N+1]                                            */
+  const float* bw;          /* [B]                                              */
+  const float* blogit;      /* [B,3]                                            */
+  float* stats;             /* [N,10]: forward out, backward in                 */
+  float* rgb0;
+  float* rgbk;
+  float* ainv;
+  float* in_marched;
+  float* bg_marched;
+  const float* g_rgb0;
+  const float* g_rgbk;
+  const float* g_ainv;
+  float* d_logit;
+  float* d_kout;
+  float* d_w;
+  float* d_blogit;
+  float* d_bw;
+  int32_t k_into_logit, reserved;
+} vx_womask_composite_args;
+int vx_womask_composite(const vx_womask_composite_args* args, void* stream);
 
 #ifdef __cplusplus
 }

@@ -17,7 +17,7 @@ script stubs them:
     reference's checkpoint loading relies on).
 PYTHONDONTWRITEBYTECODE keeps the read-only reference tree clean.
 
-    VOXURF_REFERENCE=<reference checkout> python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt]
+    VOXURF_REFERENCE=<reference checkout> python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt] [bg] [womask]
     (default: all)
 """
 from __future__ import annotations
@@ -403,10 +403,72 @@ def bg_fixture(path, seed=8):
     print("wrote", path)
 
 
+def womask_step_fixture(path, R=16, R_bg=12, n_rays=96, width=32, seed=9):
+    """One training step of the reference's maskless fine model
+    (lib/voxurf_womask_fine.py:833-1071) in float64, loss of run.py:604-610
+    and 627 (rgb_marched, entropy of alphainv_cum[-1], rgb_marched0 x 0.5).
+    The two per-ray jitters of sample_ray_ori (torch.rand_like at :808, once
+    for the foreground samples, once for the background samples) are fixed
+    by the fixture; global_step 1 also runs _set_sphere_nonempty_mask."""
+    import lib.voxurf_womask_fine as rw
+    from voxurf_gb300 import configs, synthetic
+
+    ours = configs.build_womask_model(R, "fp32", device="cpu", seed=seed, width=width, R_bg=R_bg)
+    kw = configs.womask_model_kwargs(R, "fp32", width, R_bg)
+    kw.pop("precision")
+    ref = rw.Voxurf(**kw)
+    sd = _state_from_ours(ours)
+    missing, unexpected = ref.load_state_dict(sd, strict=False)
+    assert not unexpected, unexpected
+    sd = {k: v for k, v in ref.state_dict().items()}
+    ref = ref.double()
+    ro, rd, vd = synthetic.random_rays(n_rays, seed=seed + 11)
+    tgt = configs.train_targets(n_rays, seed)
+    g = torch.Generator().manual_seed(seed + 5)
+    jit = torch.rand((2, n_rays), generator=g)
+    rk = dict(configs.FINE_RENDER_KWARGS, bg=1)
+    T = lambda a: torch.from_numpy(a).double()
+    calls = []
+    rand_like = torch.rand_like
+
+    def fixed_rand_like(x):
+        calls.append(x.shape)
+        return jit[len(calls) - 1][:, None].to(x.dtype).clone()
+
+    torch.rand_like = fixed_rand_like
+    try:
+        ret = ref(T(ro), T(rd), T(vd), global_step=1, **rk)
+    finally:
+        torch.rand_like = rand_like
+    assert len(calls) == 2, calls
+    target = T(tgt)
+    loss = torch.nn.functional.mse_loss(ret["rgb_marched"], target)
+    pout = ret["alphainv_cum"][..., -1].clamp(1e-6, 1 - 1e-6)
+    loss = loss + 0.001 * (-(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean())
+    loss = loss + torch.nn.functional.mse_loss(ret["rgb_marched0"], target) * 0.5
+    loss.backward()
+    out = {"R": R, "R_bg": R_bg, "n_rays": n_rays, "width": width, "seed": seed, "rays_o": ro, "rays_d": rd,
+           "viewdirs": vd, "target": tgt, "jitter": jit.numpy(),
+           "rgb_marched": ret["rgb_marched"].detach().numpy(), "rgb_marched0": ret["rgb_marched0"].detach().numpy(),
+           "alphainv_cum": ret["alphainv_cum"].detach().numpy(), "in_marched": ret["in_marched"].detach().numpy(),
+           "out_marched": ret["out_marched"].detach().numpy(), "n_weights": np.array(ret["weights"].numel()),
+           "n_bg_weights": np.array(ret["bg_weights"].numel()), "loss": np.array(loss.item())}
+    for name in ("sdf", "k0", "bg_density", "bg_k0"):
+        out["grad_" + name] = getattr(ref, name).grid.grad.numpy()
+    for net in ("rgbnet", "k_rgbnet", "bg_rgbnet"):
+        for n, p in getattr(ref, net).named_parameters():
+            out[f"grad_{net}.{n}"] = p.grad.numpy()
+    for k, v in sd.items():
+        if v.dtype.is_floating_point:
+            out["state." + k] = v.float().numpy()
+    np.savez_compressed(path, **out)
+    print("wrote", path, "fg samples", ret["weights"].numel(), "bg samples", ret["bg_weights"].numel())
+
+
 def main():
     install_stubs()
     torch.set_default_dtype(torch.float32)
-    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg"]
+    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg", "womask"]
     if "ops" in which:
         ops_fixture(os.path.join(HERE, "ops_golden.npz"))
     if "fine" in which:
@@ -419,6 +481,8 @@ def main():
         ckpt_fixture(HERE)
     if "bg" in which:
         bg_fixture(os.path.join(HERE, "bg_golden.npz"))
+    if "womask" in which:
+        womask_step_fixture(os.path.join(HERE, "womask_step_golden.npz"))
 
 
 if __name__ == "__main__":

@@ -73,7 +73,10 @@ def test_struct_sizes_match_c_layout():
                "vx_mlp_train_fwd_args": _abi.MlpTrainFwdArgs, "vx_mlp_train_bwd_args": _abi.MlpTrainBwdArgs,
                "vx_mlp_wgrad_args": _abi.MlpWgradArgs, "vx_mlp_reduce_job": _abi.MlpReduceJob,
                "vx_mlp_f32_rowgemm_args": _abi.MlpF32RowGemmArgs, "vx_mlp_f32_wgrad_args": _abi.MlpF32WgradArgs,
-               "vx_mlp_sum_job": _abi.MlpSumJob}
+               "vx_mlp_sum_job": _abi.MlpSumJob, "vx_womask_fg_alpha_args": _abi.WomaskFgAlphaArgs,
+               "vx_womask_bg_alpha_args": _abi.WomaskBgAlphaArgs,
+               "vx_womask_bg_features_args": _abi.WomaskBgFeaturesArgs,
+               "vx_womask_composite_args": _abi.WomaskCompositeArgs}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "voxurf_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -97,7 +97,38 @@ class BgSampleArgs(C.Structure):
     _fields_ = [
         ("rays_o", P), ("rays_d", P), ("jitter", P), ("xyz_min", F * 3), ("xyz_max", F * 3), ("near", F),
         ("far", F), ("stepdist", F), ("dist_thres", F), ("n_samples", I32), ("outbbox_only", I32),
-        ("n_rays", I64),
+        ("n_rays", I64), ("inner", I32), ("reserved", I32),
+    ]
+
+
+class WomaskFgAlphaArgs(C.Structure):
+    _fields_ = [
+        ("n", I64), ("pts", P), ("ray_id", P), ("viewdirs", P), ("grid", GridGeom), ("sdf_smooth", P),
+        ("voxel_size", F), ("inv_s", F), ("dist", F), ("alpha", P), ("d_alpha", P), ("d_sdf_smooth", P),
+    ]
+
+
+class WomaskBgAlphaArgs(C.Structure):
+    _fields_ = [
+        ("n", I64), ("pts", P), ("grid", GridGeom), ("density", P), ("act_shift", F), ("interval", F),
+        ("alpha", P), ("d_alpha", P), ("d_density", P),
+    ]
+
+
+class WomaskBgFeaturesArgs(C.Structure):
+    _fields_ = [
+        ("n", I64), ("outer_pts", P), ("pts_org", P), ("ray_id", P), ("viewdirs", P), ("grid", GridGeom),
+        ("bg_k0", P), ("posbase_pe", I64), ("viewbase_pe", I64), ("ld", I64), ("X", P), ("bf16", I32),
+        ("reserved", I32), ("dX", P), ("d_bg_k0", P),
+    ]
+
+
+class WomaskCompositeArgs(C.Structure):
+    _fields_ = [
+        ("n_rays", I64), ("fg_off", P), ("w", P), ("logit", P), ("kout", P), ("bg_off", P), ("bw", P),
+        ("blogit", P), ("stats", P), ("rgb0", P), ("rgbk", P), ("ainv", P), ("in_marched", P),
+        ("bg_marched", P), ("g_rgb0", P), ("g_rgbk", P), ("g_ainv", P), ("d_logit", P), ("d_kout", P),
+        ("d_w", P), ("d_blogit", P), ("d_bw", P), ("k_into_logit", I32), ("reserved", I32),
     ]
 
 
@@ -241,6 +272,10 @@ _STRUCT_FNS = {
     "vx_mlp_train_wgrad": MlpWgradArgs,
     "vx_mlp_f32_rowgemm": MlpF32RowGemmArgs,
     "vx_mlp_f32_wgrad": MlpF32WgradArgs,
+    "vx_womask_fg_alpha": WomaskFgAlphaArgs,
+    "vx_womask_bg_alpha": WomaskBgAlphaArgs,
+    "vx_womask_bg_features": WomaskBgFeaturesArgs,
+    "vx_womask_composite": WomaskCompositeArgs,
 }
 
 _SERVE_SIGNATURES = {

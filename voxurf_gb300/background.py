@@ -33,8 +33,13 @@ def n_samples_for(grid_shape, stepsize: float) -> int:
 
 def background_samples(rays_o, rays_d, xyz_min, xyz_max, near: float, far: float, stepsize: float, voxel_size,
                        n_samples: int, jitter=None, *, step_voxel_size=None, dist_thres_factor: float = 0.5,
-                       outbbox_only: bool = False):
+                       outbbox_only: bool = False, inner: bool = False):
     """-> (outer_pts [M,3], outer_pts_org [M,3], outer_ray_id [M], outer_step_id [M]).
+
+    ``inner=True`` gives the maskless fine model's foreground samples instead
+    (voxurf_womask_fine.py:843-849): the same sample placement, the points
+    with |p| < 1, not inverted and without the distance test; the return is
+    then (pts [M,3], None, ray_id [M], step_id [M]).
 
     ``voxel_size`` is the model's float32 voxel size; the step distance
     (``stepsize * step_voxel_size``, :810-812, with step_voxel_size =
@@ -64,6 +69,7 @@ def background_samples(rays_o, rays_d, xyz_min, xyz_max, near: float, far: float
     args.dist_thres = float(np.float32(np.float32(vs * np.float32(stepsize)) * np.float32(dist_thres_factor)))
     args.n_samples = int(n_samples)
     args.outbbox_only = int(bool(outbbox_only))
+    args.inner = int(bool(inner))
     args.n_rays = n
     counts = torch.empty(n, dtype=torch.int64, device=dev)
     offsets = torch.empty(n + 1, dtype=torch.int64, device=dev)
@@ -76,7 +82,7 @@ def background_samples(rays_o, rays_d, xyz_min, xyz_max, near: float, far: float
                   "vx_bg_samples_count")
     total = int(offsets[-1].item())
     outer = torch.empty((total, 3), dtype=torch.float32, device=dev)
-    org = torch.empty((total, 3), dtype=torch.float32, device=dev)
+    org = None if inner else torch.empty((total, 3), dtype=torch.float32, device=dev)
     ray_id = torch.empty(total, dtype=torch.int64, device=dev)
     step_id = torch.empty(total, dtype=torch.int64, device=dev)
     _native.check(lib.vx_bg_samples_fill(C.byref(args), ptr(offsets), total, ptr(outer), ptr(org), ptr(ray_id),

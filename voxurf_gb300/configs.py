@@ -66,6 +66,41 @@ def build_fine_model(R: int = 256, precision: str = "fp32", device="cuda", seed:
     return model
 
 
+def womask_model_kwargs(R: int = 64, precision: str = "fp32", width: int = 128, R_bg: int | None = None) -> dict:
+    """Maskless fine stage (lib/voxurf_womask_fine.py) with the fine model's
+    feature settings above, a background grid of R_bg^3 (default R^3) and
+    the background MLP of the reference's defaults (bg_k0 12 + PE(xyz, 5)
+    33 + PE(view, 4) 27 = 72 -> width x2 -> 3)."""
+    kw = fine_model_kwargs(R, precision, width)
+    kw.update(num_voxels_bg=(R_bg or R) ** 3, bg_fast_color_thres=1e-4, bg_rgbnet_dim=12, bg_posbase_pe=5,
+              bg_viewbase_pe=4, bg_rgbnet_width=width, bg_rgbnet_depth=3)
+    return kw
+
+
+def build_womask_model(R: int = 64, precision: str = "fp32", device="cuda", seed: int = 0, width: int = 128,
+                       R_bg: int | None = None):
+    """Maskless fine model with a synthetic scene: the sphere r=0.5 SDF (+
+    noise) inside the unit sphere, k0 and bg_k0 ~ N(0, 0.1), bg_density ~
+    N(1, 2) (alphas of a few percent per background sample)."""
+    from .voxurf_womask import VoxurfWomask
+
+    torch.manual_seed(seed)
+    model = VoxurfWomask(**womask_model_kwargs(R, precision, width, R_bg))
+    Rb = int(model.world_size_bg[0])
+    with torch.no_grad():
+        model.sdf.grid.data = torch.from_numpy(synthetic.make_sdf("sphere", R, seed=seed))[None, None].clone()
+        k0 = synthetic.make_k0(R, 12, seed=seed + 1)
+        model.k0.grid.data = k0.permute(3, 0, 1, 2)[None].contiguous(memory_format=torch.channels_last_3d)
+        bk = synthetic.make_k0(Rb, 12, seed=seed + 2)
+        model.bg_k0.grid.data = bk.permute(3, 0, 1, 2)[None].contiguous(memory_format=torch.channels_last_3d)
+        g = torch.Generator().manual_seed(seed + 3)
+        model.bg_density.grid.data = (torch.randn((1, 1, Rb, Rb, Rb), generator=g) * 2.0 + 1.0)
+    model = model.to(device)
+    if precision == "bf16":
+        model.refresh_k0_shadow()
+    return model
+
+
 # Render-server scenes: sphere_torus with different sizes per scene
 # (sphere r, torus R, torus r), each with its own seed.
 SERVE_SHAPES = [(0.45, 0.6, 0.15), (0.40, 0.55, 0.12), (0.50, 0.65, 0.18), (0.35, 0.50, 0.10)]

@@ -164,8 +164,9 @@ __global__ void __launch_bounds__(BG_THREADS) bg_samples_kernel(
     float p[3] = {0.f, 0.f, 0.f}, q[3] = {0.f, 0.f, 0.f};
     bool keep = false;
     if (valid) {
-      keep = !bg_point(a, R, k, p, q);
-      if (a.outbbox_only) {
+      const bool inside = bg_point(a, R, k, p, q);
+      keep = a.inner ? inside : !inside;
+      if (a.outbbox_only && !a.inner) {
         // voxurf_womask_coarse.py:641 keeps only samples outside the bbox
         // (sample_ray_ori's mask_outbbox, voxurf_womask_fine.py:814)
         bool out = R.miss;
@@ -173,6 +174,29 @@ __global__ void __launch_bounds__(BG_THREADS) bg_samples_kernel(
         for (int i = 0; i < 3; ++i) out = out || (a.xyz_min[i] > p[i]) || (p[i] > a.xyz_max[i]);
         keep = keep && out;
       }
+    }
+    if (a.inner) {
+      // foreground samples (voxurf_womask_fine.py:846-849): the points
+      // inside the unit sphere, no inversion and no distance test
+      const unsigned ball = __ballot_sync(FULL, keep);
+      if (FILL) {
+        if (keep) {
+          const int64_t o = idx + __popc(ball & ((1u << lane) - 1u));
+          if (o < capacity && o < end) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              outer_pts[3 * o + i] = p[i];
+              if (pts_org) pts_org[3 * o + i] = p[i];
+            }
+            ray_id[o] = r;
+            step_id[o] = k;
+          }
+        }
+        idx += __popc(ball);
+      } else {
+        n += __popc(ball);
+      }
+      continue;
     }
     // dist of :866 between this sample's and the previous inverted point
     float prevq[3];
@@ -265,7 +289,7 @@ int vx_bg_samples_fill(const vx_bg_sample_args* args, const int64_t* offsets, in
                        float* pts_org, int64_t* ray_id, int64_t* step_id, void* stream) {
   if (!bg_args_ok(args) || capacity < 0) return VX_ERR_ARG;
   if (args->n_rays == 0 || capacity == 0) return VX_OK;
-  if (!offsets || !outer_pts || !pts_org || !ray_id || !step_id) return VX_ERR_ARG;
+  if (!offsets || !outer_pts || (!pts_org && !args->inner) || !ray_id || !step_id) return VX_ERR_ARG;
   bg_samples_kernel<true><<<bg_blocks(args->n_rays), BG_THREADS, 0, as_stream(stream)>>>(
       *args, nullptr, offsets, capacity, outer_pts, pts_org, ray_id, step_id, device_error_ptr());
   return launch_status();

@@ -146,6 +146,47 @@ __device__ __forceinline__ AlphaState neus_alpha(float s, const float gr[3], con
   return a;
 }
 
+// Adjoint of neus_alpha at one sample (continuous grid index ind, view
+// direction v) for an incoming d_alpha, scattered into the gradient of the
+// (smoothed) SDF grid: the SDF and its +-1-voxel finite-difference gradient
+// are recomputed, the clip passes the gradient only where the raw alpha lies
+// in [0, 1], and the centre and the six probes are summed per plane of each
+// axis before their reductions (the centre joins axis 0).
+__device__ __forceinline__ void neus_alpha_adjoint_scatter(float d_alpha, const float ind[3], const float v[3],
+                                                           float inv_s, float dist, const float* __restrict__ sdf,
+                                                           const GridGeom& g, float voxel_size,
+                                                           float* __restrict__ d_sdf) {
+  float s, gr[3];
+  sdf_and_grad(sdf, g, voxel_size, ind, &s, gr);
+  const AlphaState a = neus_alpha(s, gr, v, inv_s, dist);
+  if (!(a.raw >= 0.f && a.raw <= 1.f)) return;  // clip backward
+  const float den = a.P + 1e-5f;
+  const float dP = d_alpha * a.Q / (den * den);
+  const float dQ = -d_alpha / den;
+  const float d_prev = dP * a.P * a.nP * inv_s;
+  const float d_next = dQ * a.Q * a.nQ * inv_s;
+  const float d_s = d_prev + d_next;
+  const float d_ic = (d_next - d_prev) * dist * 0.5f;
+  const float d_cos = a.cosv < 0.f ? d_ic : 0.f;
+#pragma unroll
+  for (int axis = 0; axis < 3; ++axis) {
+    const float dg = d_cos * v[axis];
+    if (axis > 0 && dg == 0.f) continue;
+    PlaneAcc acc;
+    plane_acc_init(acc, ind[axis]);
+    if (axis == 0) plane_acc_add(acc, d_sdf, g, ind, 0, ind[0], d_s);
+    if (dg != 0.f) {
+      const float hi = (float)(gsize(g, axis) - 1);
+      const float xm = fminf(fmaxf(ind[axis] - 1.f, 0.f), hi);
+      const float xp = fminf(fmaxf(ind[axis] + 1.f, 0.f), hi);
+      const float dfd = dg / (xp - xm) / voxel_size;
+      plane_acc_add(acc, d_sdf, g, ind, axis, xp, dfd);
+      plane_acc_add(acc, d_sdf, g, ind, axis, xm, -dfd);
+    }
+    plane_acc_flush(acc, d_sdf, g, ind, axis);
+  }
+}
+
 __device__ __forceinline__ bool outside_bbox(const float p[3], const float* mn, const float* mx) {
   return (mn[0] > p[0]) | (mn[1] > p[1]) | (mn[2] > p[2]) | (mx[0] < p[0]) | (mx[1] < p[1]) | (mx[2] < p[2]);
 }

@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(128) features_fine_bwd_kernel(FeatBwdParams P)
   float d_center = 0.f, dgx = 0.f, dgy = 0.f, dgz = 0.f;
   int feat_col = 0, grad_col = 0;
   if (live) {
-    P.dw_slot[P.slot2[row]] = P.dw2[row];
+    if (P.dw_slot) P.dw_slot[P.slot2[row]] = P.dw2[row];
     const float p[3] = {P.pts2[3 * row], P.pts2[3 * row + 1], P.pts2[3 * row + 2]};
     to_index(P.g, p, ind);
     dx1 = reinterpret_cast<const T*>(P.dX1) + row * P.ld1;
@@ -730,39 +730,10 @@ __global__ void __launch_bounds__(256) geometry_fine_bwd_kernel(GeomBwdParams P)
     if (!valid) continue;
     if (d_alpha == 0.f) continue;
     const int k = (int)(__float_as_uint(rc.x) & 0x7fffffffu);
-    float p[3], ind[3], s, gr[3];
+    float p[3], ind[3];
     sample_point(f, P.stepdist, k, p);
     to_index(P.g, p, ind);
-    sdf_and_grad(P.sdf, P.g, P.voxel_size, ind, &s, gr);
-    const AlphaState a = neus_alpha(s, gr, v, inv_s, P.dist);
-    if (!(a.raw >= 0.f && a.raw <= 1.f)) continue;  // clip backward
-    const float den = a.P + 1e-5f;
-    const float dP = d_alpha * a.Q / (den * den);
-    const float dQ = -d_alpha / den;
-    const float d_prev = dP * a.P * a.nP * inv_s;
-    const float d_next = dQ * a.Q * a.nQ * inv_s;
-    const float d_s = d_prev + d_next;
-    const float d_ic = (d_next - d_prev) * P.dist * 0.5f;
-    const float d_cos = a.cosv < 0.f ? d_ic : 0.f;
-    // the centre and the six +-1 probes, summed per plane of each axis (the
-    // centre joins axis 0): 48 corner reductions instead of 56
-#pragma unroll
-    for (int axis = 0; axis < 3; ++axis) {
-      const float dg = d_cos * v[axis];
-      if (axis > 0 && dg == 0.f) continue;
-      PlaneAcc acc;
-      plane_acc_init(acc, ind[axis]);
-      if (axis == 0) plane_acc_add(acc, P.d_sdf, P.g, ind, 0, ind[0], d_s);
-      if (dg != 0.f) {
-        const float hi = (float)(gsize(P.g, axis) - 1);
-        const float xm = fminf(fmaxf(ind[axis] - 1.f, 0.f), hi);
-        const float xp = fminf(fmaxf(ind[axis] + 1.f, 0.f), hi);
-        const float dfd = dg / (xp - xm) / P.voxel_size;
-        plane_acc_add(acc, P.d_sdf, P.g, ind, axis, xp, dfd);
-        plane_acc_add(acc, P.d_sdf, P.g, ind, axis, xm, -dfd);
-      }
-      plane_acc_flush(acc, P.d_sdf, P.g, ind, axis);
-    }
+    neus_alpha_adjoint_scatter(d_alpha, ind, v, inv_s, P.dist, P.sdf, P.g, P.voxel_size, P.d_sdf);
   }
 }
 
