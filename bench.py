@@ -75,6 +75,7 @@ def parse():
     p.add_argument("--no-eikonal", action="store_true",
                    help="skip the eikonal-training (coarse 96^3, 8192/32768 rays) measurement")
     p.add_argument("--no-mesh", action="store_true", help="skip the 512^3 mesh-extraction field measurement")
+    p.add_argument("--no-womask", action="store_true", help="skip the maskless (womask) model's training step")
     p.add_argument("--no-background", action="store_true",
                    help="skip the background-sample generator measurement (scenes without an object mask)")
     p.add_argument("--micro", choices=["smooth", "mlp_tc", "background", "train_fp32", "train_bf16",
@@ -343,6 +344,9 @@ def run_ours(args, world, rank, local):
     eikonal = None
     if not args.no_eikonal and R == 256:
         eikonal = run_eikonal(args, dev)
+    womask = None
+    if not args.no_womask and R == 256:
+        womask = run_womask(args, dev)
     mesh = None
     if not args.no_mesh and R == 256:
         mesh = run_mesh_query(args, dev)
@@ -366,6 +370,7 @@ def run_ours(args, world, rank, local):
             "render": render,
             "long_rays": long_rays,
             "eikonal_train": eikonal,
+            "womask_train": womask,
             "mesh_query": mesh,
             "background_samples": bg_samples,
             "roofline": roofline,
@@ -679,6 +684,52 @@ def run_eikonal(args, dev):
         res["bf16_vs_fp32_rgb_max_abs"] = float((first["bf16"][1] - first["fp32"][1]).abs().max())
         res["bf16_vs_fp32_loss_rel"] = abs(first["bf16"][0] - first["fp32"][0]) / max(abs(first["fp32"][0]), 1e-30)
         out[f"rays_{n}"] = res
+    return out
+
+
+WM_R = 256
+
+
+def run_womask(args, dev):
+    """Maskless fine model (foreground NeuS SDF inside the unit sphere,
+    inverted-sphere background density grid): SDF + k0 256^3, bg_density +
+    bg_k0 256^3, rgbnet / k_rgbnet 192 wide x4, bg_rgbnet 72 -> 192 x2 -> 3,
+    8192 rays per step, full steps (forward, loss, backward, Adam) through
+    the autograd path (foreground and background sample generation,
+    boolean selections and MLP row counts read back by the host each step):
+    FP32 and BF16."""
+    import numpy as np
+    import torch
+
+    from voxurf_gb300 import configs, synthetic
+    from voxurf_gb300.train import FineTrainer
+
+    rk = dict(configs.FINE_RENDER_KWARGS)
+    W, S = 3, 10
+    o, d, v = synthetic.random_rays(N_RAYS * (W + S), seed=21)
+    t = configs.train_targets(N_RAYS * (W + S), 21)
+    b = [torch.from_numpy(np.ascontiguousarray(a.reshape(W + S, N_RAYS, 3))).to(dev) for a in (o, d, v, t)]
+    out = {"workload": f"womask fine: SDF/k0 {WM_R}^3, bg_density/bg_k0 {WM_R}^3, rgbnet/k_rgbnet 192x4, "
+                       f"bg_rgbnet 72->192x3->3, {N_RAYS} rays/step, sphere r=0.5 foreground"}
+    for precision in ("fp32", "bf16"):
+        model = configs.build_womask_model(WM_R, precision, device=dev, seed=0, width=192)
+        tr = FineTrainer(model, n_rays=N_RAYS)
+        for i in range(W):
+            loss, ret = tr.step(b[0][i], b[1][i], b[2][i], b[3][i], rk, global_step=i + 2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(W, W + S):
+            loss, ret = tr.step(b[0][i], b[1][i], b[2][i], b[3][i], rk, global_step=i + 2)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / S
+        out[precision] = {"ms_per_step": ms, "rays_per_s": N_RAYS / (ms / 1000.0),
+                          "fg_rows_last_step": int(ret["weights"].numel()),
+                          "bg_rows_last_step": int(ret["bg_weights"].numel()), "loss": float(loss)}
+        del tr, model, ret
+        torch.cuda.empty_cache()
+    out["speedup_bf16_vs_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
     return out
 
 

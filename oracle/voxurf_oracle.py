@@ -74,10 +74,30 @@ def _mask_state(model):
     return ("grid", mc.mask.cpu(), mc.xyz2ijk_scale.cpu().float(), mc.xyz2ijk_shift.cpu().float())
 
 
-def _apply_mask(mask, pts32):
+def _apply_mask(mask, pts32, ops=RenderUtilsOracle):
     if mask[0] == "grid":
-        return RenderUtilsOracle.maskcache_lookup(mask[1], pts32, mask[2], mask[3])
-    return maskcache_query(*mask[1:], pts32)
+        dev = pts32.device
+        return ops.maskcache_lookup(mask[1].to(dev), pts32, mask[2].to(dev), mask[3].to(dev))
+    return maskcache_query(*[m.to(pts32.device) if torch.is_tensor(m) else m for m in mask[1:]], pts32)
+
+
+class _Alphas2WeightsOps(torch.autograd.Function):
+    """lib/voxurf_fine.py:981-997 over a given render_utils op set (the
+    oracle's restatement or a drop-in module)."""
+
+    @staticmethod
+    def forward(ctx, alpha, ray_id, N, ops):
+        w, T, last, i_s, i_e = ops.alpha2weight(alpha, ray_id, N)
+        ctx.save_for_backward(alpha, w, T, last, i_s, i_e)
+        ctx.n_rays, ctx.ops = N, ops
+        return w, last
+
+    @staticmethod
+    def backward(ctx, grad_w, grad_last):
+        alpha, w, T, last, i_s, i_e = ctx.saved_tensors
+        g = ctx.ops.alpha2weight_backward(alpha, w, T, last, i_s, i_e, ctx.n_rays, grad_w.contiguous(),
+                                          grad_last.contiguous())
+        return g, None, None, None
 
 
 def extract_fields(grid, xyz_min, xyz_max, bound_min, bound_max, resolution, sign=-1.0):
@@ -98,10 +118,11 @@ def sample_sdfs(xyz, grid, displace_list, xyz_min, xyz_max, voxel_size, use_grad
     xyz = xyz.reshape(1, 1, 1, -1, 3)
     ind_norm = ((xyz - xyz_min) / (xyz_max - xyz_min)).flip((-1,)) * 2 - 1
     gs = grid.size()[-3:]
-    size_zyx = torch.tensor([gs[2], gs[1], gs[0]])
+    dev = xyz.device
+    size_zyx = torch.tensor([gs[2], gs[1], gs[0]], device=dev)
     ind = ((ind_norm + 1) / 2) * (size_zyx - 1)
-    offset = torch.tensor([[-1, 0, 0], [1, 0, 0], [0, -1, 0], [0, 1, 0], [0, 0, -1], [0, 0, 1]])
-    displace = torch.tensor(displace_list)
+    offset = torch.tensor([[-1, 0, 0], [1, 0, 0], [0, -1, 0], [0, 1, 0], [0, 0, -1], [0, 0, 1]], device=dev)
+    displace = torch.tensor(displace_list, device=dev)
     offset = offset[:, None, :] * displace[None, :, None]
     all_ind = ind.unsqueeze(-2) + offset.view(-1, 3)
     all_ind = all_ind.view(1, 1, 1, -1, 3)
@@ -178,11 +199,20 @@ def f32(v) -> float:
 
 class OracleFine(nn.Module):
     """Reference fine-stage step (voxurf_fine.py:620-802) with parameters
-    copied from a voxurf_gb300 fine model."""
+    copied from a voxurf_gb300 fine model.
 
-    def __init__(self, model, dtype=torch.float64):
+    ops / device: the render_utils op set the step calls (sample_pts_on_rays,
+    maskcache_lookup, alpha2weight and its backward, with the reference
+    extension's signatures) and the device of every tensor.  The default is
+    the oracle's own restatement on the CPU; a drop-in module with float32
+    on a GPU runs the reference's step on that module's kernels, as the
+    reference itself would after its extension is swapped."""
+
+    def __init__(self, model, dtype=torch.float64, ops=None, device="cpu"):
         super().__init__()
         self.dtype = dtype
+        self.ops = RenderUtilsOracle if ops is None else ops
+        self.device = torch.device(device)
         sd = {k: v.detach().cpu() for k, v in model.state_dict().items()}
         self.sdf_grid = nn.Parameter(sd["sdf.grid"].contiguous().to(dtype))
         self.k0_grid = nn.Parameter(sd["k0.grid"].contiguous().to(dtype))
@@ -210,6 +240,13 @@ class OracleFine(nn.Module):
         # None, or a dict holding the detached rgbnet logits of a base
         # forward (recorded on first use, then reused): see forward()
         self.frozen = None
+        if self.device.type != "cpu":
+            self.to(self.device)
+            for k in ("xyz_min", "xyz_max", "xyz_min32", "xyz_max32", "posfreq", "viewfreq", "k_posfreq",
+                      "k_viewfreq"):
+                setattr(self, k, getattr(self, k).to(self.device))
+            if self.smooth_sdf:
+                self.kernel = self.kernel.to(self.device)
 
     def smoothed(self):
         return smooth3d(self.sdf_grid, self.kernel) if self.smooth_sdf else self.sdf_grid
@@ -236,16 +273,18 @@ class OracleFine(nn.Module):
         rd = relu_device or {}
         self.relu_ties = 0
         stepdist = f32(rk["stepsize"] * np.float32(self.voxel_size))
-        ru = RenderUtilsOracle
+        ru = self.ops
+        dev = self.device
         ray_pts, mask_outbbox, ray_id, step_id, _, _, _ = ru.sample_pts_on_rays(
-            rays_o.float().cpu(), rays_d.float().cpu(), self.xyz_min32, self.xyz_max32, rk["near"], 1e9, stepdist)
+            rays_o.float().to(dev).contiguous(), rays_d.float().to(dev).contiguous(), self.xyz_min32,
+            self.xyz_max32, rk["near"], 1e9, stepdist)
         inb = ~mask_outbbox
         ray_pts32, ray_id, step_id = ray_pts[inb], ray_id[inb], step_id[inb]
         if self.mask is not None:
-            m = _apply_mask(self.mask, ray_pts32)
+            m = _apply_mask(self.mask, ray_pts32.contiguous(), ru)
             ray_pts32, ray_id, step_id = ray_pts32[m], ray_id[m], step_id[m]
         ray_pts = ray_pts32.to(dt)
-        viewdirs = viewdirs.cpu().to(dt)
+        viewdirs = viewdirs.to(dev).to(dt)
         sdf_grid = self.smoothed()
         sdf = grid_sample_pts(sdf_grid, ray_pts, self.xyz_min, self.xyz_max)[:, 0]
         _, g = sample_sdfs(ray_pts, sdf_grid, [1.0], self.xyz_min, self.xyz_max, self.voxel_size, False)
@@ -267,7 +306,7 @@ class OracleFine(nn.Module):
             trace("alpha > thres", m)
             alpha, ray_id, ray_pts, step_id, gradient, sdf = alpha[m], ray_id[m], ray_pts[m], step_id[m], \
                 gradient[m], sdf[m]
-        weights, alphainv_last = Alphas2WeightsOracle.apply(alpha, ray_id, N)
+        weights, alphainv_last = _Alphas2WeightsOps.apply(alpha.contiguous(), ray_id.contiguous(), N, ru)
         if thr > 0:
             m = weights > thr
             trace("weights > thres", m)
@@ -310,12 +349,12 @@ class OracleFine(nn.Module):
             self.relu_ties += t2
             self.relu_examined += getattr(mlp_relu_ties, "examined", 0) if rd else 0
             k_rgb = torch.sigmoid(base + k_out)
-            k_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * k_rgb) \
+            k_marched = torch.zeros([N, 3], dtype=dt, device=dev).index_add(0, ray_id, weights.unsqueeze(-1) * k_rgb) \
                 + alphainv_last[..., None] * bg
             trace("k_rgb in [0,1]", (k_marched >= 0) & (k_marched <= 1))
             out["rgb_marched"] = k_marched.clamp(0, 1)
             out["k_rgb_feat"] = k_feat
-        rgb_marched = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * rgb) \
+        rgb_marched = torch.zeros([N, 3], dtype=dt, device=dev).index_add(0, ray_id, weights.unsqueeze(-1) * rgb) \
             + alphainv_last[..., None] * bg
         if self.use_rgb_k:
             out["rgb_marched0"] = rgb_marched
@@ -323,10 +362,10 @@ class OracleFine(nn.Module):
             out["rgb_marched"] = rgb_marched
         if rk.get("render_depth", False):
             with torch.no_grad():
-                out["depth"] = torch.zeros([N], dtype=dt).index_add(0, ray_id, weights * step_id * dist)
+                out["depth"] = torch.zeros([N], dtype=dt, device=dev).index_add(0, ray_id, weights * step_id * dist)
         if rk.get("render_grad", False):
             normal = gradient / (gradient.norm(2, -1, keepdim=True) + 1e-6)
-            out["normal_marched"] = torch.zeros([N, 3], dtype=dt).index_add(0, ray_id, weights.unsqueeze(-1) * normal)
+            out["normal_marched"] = torch.zeros([N, 3], dtype=dt, device=dev).index_add(0, ray_id, weights.unsqueeze(-1) * normal)
         return out
 
 

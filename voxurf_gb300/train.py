@@ -40,14 +40,15 @@ class FineTrainer:
     rgb_marched0 term).
 
     lr_* are the per-group learning rates (utils.create_optimizer_or_freeze_model
-    groups sdf / k0 / rgbnet / k_rgbnet); tv_sdf / tv_k0 are the weights
+    groups sdf / k0 / rgbnet / k_rgbnet, and lr_bg for the maskless model's
+    bg_density / bg_k0 / bg_rgbnet); tv_sdf / tv_k0 are the weights
     given to *_total_variation_add_grad before the division by the batch
     size (run.py:647-655); tv_dense mirrors `global_step < tv_dense_before`.
     """
 
     def __init__(self, model, lr_sdf=1e-3, lr_k0=1e-3, lr_rgbnet=1e-3, lr_k_rgbnet=1e-3, tv_sdf=1e-4, tv_k0=1e-4,
                  tv_dense=True, n_rays=8192, loss_weights=(1.0, 0.001, 0.5), weight_tv_density=0.0,
-                 smooth_grad_tv=0.0, weight_eikonal=0.0, graphed=False):
+                 smooth_grad_tv=0.0, weight_eikonal=0.0, graphed=False, lr_bg=1e-3):
         self.model = model
         self.n_rays = n_rays
         # graphed=True: steps replay CUDA graphs on static buffers
@@ -72,6 +73,14 @@ class FineTrainer:
         ]
         if getattr(model, "k_rgbnet", None) is not None:   # the coarse model has no k-branch
             groups.append({"params": list(model.k_rgbnet.parameters()), "lr": lr_k_rgbnet, "name": "k_rgbnet"})
+        # the maskless model's background (its own groups in
+        # create_optimizer_or_freeze_model: bg_density, bg_k0, bg_rgbnet)
+        for name in ("bg_density", "bg_k0"):
+            g = getattr(model, name, None)
+            if g is not None:
+                groups.append({"params": [g.grid], "lr": lr_bg, "name": name})
+        if getattr(model, "bg_rgbnet", None) is not None:
+            groups.append({"params": list(model.bg_rgbnet.parameters()), "lr": lr_bg, "name": "bg_rgbnet"})
         self.optimizer = Adam(groups, betas=(0.9, 0.99))
         self.loss_weights = loss_weights
         self.global_step = 0
