@@ -503,8 +503,8 @@ def run_micro(args, dev):
     launches first): `smooth` = vx_smooth3d / vx_smooth3d_adjoint (5^3,
     sigma 0.8) on a --grid^3 FP32 grid, 8 algorithmic bytes per voxel (12
     with accumulation); `mlp_tc` = the fused tcgen05 colour MLP
-    (70(80) -> 192 x3 -> 3, BF16 rows) against the cuBLAS GEMM path with
-    the head kernel, at 131,072 and 2,097,152 rows."""
+    (70(80) -> 192 x3 -> 3, BF16 rows) against torch's BF16 GEMMs (its
+    cuBLAS) with the head kernel, at 131,072 and 2,097,152 rows."""
     import numpy as np
     import torch
     import torch.nn as nn

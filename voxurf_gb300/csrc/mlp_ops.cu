@@ -3,7 +3,9 @@
 //   dz = dh * (h > 0)      (ReLU backward, h = the layer's post-ReLU output)
 //   db += sum_rows dz      (bias gradient, FP32 accumulation)
 // One pass over dh/h instead of torch's threshold_backward + a strided
-// column reduction.  The GEMMs (dW = dz^T x, dx = dz W) stay in cuBLAS.
+// column reduction, for callers that run the layer GEMMs themselves (the
+// library's own training engines fuse this step into their kernels:
+// mlp_train.cu, mlp_f32.cu).
 #include "common.cuh"
 
 namespace vx {

@@ -14,13 +14,15 @@ the fused sm_103a kernels of libvoxurf_gb300.so:
       backward: recomputes interpolated values, reverse transmittance scan,
       NeuS alpha adjoint, trilinear scatter into the smoothed-grid gradient
       and k0, then the smoothing adjoint.
-  rgbnet / k_rgbnet: nn.Linear stacks (cuBLAS GEMMs; BF16 in the
-      mixed-precision mode).
+  rgbnet / k_rgbnet: nn.Linear stacks run by the library's own MLP
+      engines (mlp.apply_mlp): tcgen05 BF16 kernels in the mixed-precision
+      mode, CUDA-core FP32 kernels in the plain mode.
   _FineComposite (autograd.Function): per-ray compositing and its backward.
 
 precision='fp32' is the plain FP32 path; precision='bf16' samples k0 from a
 BF16 shadow copy and runs both MLPs in BF16 with FP32 accumulation, while
-the SDF grid, alpha, normals and the transmittance stay FP32 (FP64 carry).
+the SDF grid, alpha, normals and the transmittance stay FP32 (an FP64
+carry for rays of more than 512 samples).
 """
 from __future__ import annotations
 
