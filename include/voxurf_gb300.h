@@ -287,6 +287,10 @@ typedef struct {
   const float* mask_density; /* [X,Y,Z] max-pooled density (NULL: none)       */
   vx_grid_geom mask_dgrid;
   float mask_act_shift, mask_voxel_size_ratio, mask_thres;
+  /* 1: keep only the samples with |p| < 1 (torch.linalg.norm in float32), the
+     foreground of the maskless coarse model (voxurf_womask_coarse.py:625-628) */
+  int32_t unit_sphere;
+  int32_t reserved0;
 } vx_fine_march_args;
 int vx_fine_march(const vx_fine_march_args* args, void* stream);
 
@@ -488,10 +492,13 @@ int vx_smooth_grad_tv(const float* G, const uint8_t* mask, int64_t X, int64_t Y,
 /* March with the coarse semantics: gradient from the [X,Y,Z,4] grid of the
  * raw SDF, weights from a second Alphas2Weights over the weight > thres set
  * (:540-550).  Records of that set go to the per-ray slots (all flagged);
- * n1 = n2 = their count, n2b = the count up to the second scan's stop. */
+ * n1 = n2 = their count, n2b = the count up to the second scan's stop.  The
+ * maskless coarse model (voxurf_womask_coarse.py:620-674) marches the same
+ * way with march.unit_sphere = 1, no mask, and grad4 built from the smoothed
+ * SDF (:657); the backward's d_grad4 then belongs to the smoothed grid. */
 typedef struct {
   vx_fine_march_args march;
-  const float* grad4;       /* [X,Y,Z,4] vx_sdf_gradient_grid(layout 1) of the raw SDF */
+  const float* grad4;       /* [X,Y,Z,4] vx_sdf_gradient_grid(layout 1) of the SDF */
   int32_t* n2b;             /* out [N]                                          */
 } vx_coarse_march_args;
 int vx_coarse_march(const vx_coarse_march_args* args, void* stream);
@@ -1047,9 +1054,12 @@ int vx_womask_bg_features(const vx_womask_bg_features_args* args, void* stream);
  * [bg_off[r], bg_off[r+1]); bg = clamp(sb, 0, 1); rgb0 = clamp(clamp(s0) +
  * (1 - cum) bg), rgbk = clamp(clamp(sk) + (1 - cum) bg), ainv = 1 - cum,
  * in_marched = clamp(sk) (clamp(s0) without k-branch), bg_marched = bg; the
- * per-ray sums go to stats [N,10] for the backward.  Backward (d_w !=
- * NULL): gradients of logit (plus the k-branch's when k_into_logit), kout,
- * w, bg_logit and w_bg from g_rgb0, g_rgbk, g_ainv (each may be NULL). */
+ * per-ray sums go to stats [N,10] for the backward.  With unclamped_parts =
+ * 1 the sums s0, sk and sb enter unclamped (the coarse model,
+ * voxurf_womask_coarse.py:731-742: rgb = clamp(s0 + (1 - cum) sb)).
+ * Backward (d_w != NULL): gradients of logit (plus the k-branch's when
+ * k_into_logit), kout, w, bg_logit and w_bg from g_rgb0, g_rgbk, g_ainv
+ * (each may be NULL). */
 typedef struct {
   int64_t n_rays;
   const int64_t* fg_off;    /* [N+1]                                            */
@@ -1073,7 +1083,7 @@ typedef struct {
   float* d_w;
   float* d_blogit;
   float* d_bw;
-  int32_t k_into_logit, reserved;
+  int32_t k_into_logit, unclamped_parts;
 } vx_womask_composite_args;
 int vx_womask_composite(const vx_womask_composite_args* args, void* stream);
 

@@ -17,7 +17,7 @@ script stubs them:
     reference's checkpoint loading relies on).
 PYTHONDONTWRITEBYTECODE keeps the read-only reference tree clean.
 
-    VOXURF_REFERENCE=<reference checkout> python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt] [bg] [womask]
+    VOXURF_REFERENCE=<reference checkout> python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt] [bg] [womask] [womask_coarse]
     (default: all)
 """
 from __future__ import annotations
@@ -465,10 +465,75 @@ def womask_step_fixture(path, R=16, R_bg=12, n_rays=96, width=32, seed=9):
     print("wrote", path, "fg samples", ret["weights"].numel(), "bg samples", ret["bg_weights"].numel())
 
 
+def womask_coarse_step_fixture(path, R=16, R_bg=12, n_rays=96, width=32, seed=13):
+    """One training step of the reference's maskless coarse model
+    (lib/voxurf_womask_coarse.py:611-780) in float64 with the
+    dtu_e2e_womask coarse settings (no bg_k0), loss of run.py:604-610
+    (rgb_marched and the entropy of alphainv_cum[-1]).  The per-ray jitter
+    of the background samples (torch.rand_like at :587, the one draw of the
+    step: the foreground samples come from sample_ray_cuda) is fixed by the
+    fixture; global_step 1 also runs _set_sphere_nonempty_mask."""
+    import lib.voxurf_womask_coarse as rw
+    from voxurf_gb300 import configs, synthetic
+
+    ours = configs.build_womask_coarse_model(R, "fp32", device="cpu", seed=seed, width=width, R_bg=R_bg)
+    kw = configs.womask_coarse_model_kwargs(R, "fp32", width, R_bg)
+    kw.pop("precision")
+    ref = rw.Voxurf(**kw)
+    sd = _state_from_ours(ours)
+    missing, unexpected = ref.load_state_dict(sd, strict=False)
+    assert not unexpected, unexpected
+    sd = {k: v for k, v in ref.state_dict().items()}
+    ref = ref.double()
+    ro, rd, vd = synthetic.random_rays(n_rays, seed=seed + 11)
+    tgt = configs.train_targets(n_rays, seed)
+    g = torch.Generator().manual_seed(seed + 5)
+    jit = torch.rand((n_rays,), generator=g)
+    rk = dict(configs.COARSE_RENDER_KWARGS, bg=1)
+    T = lambda a: torch.from_numpy(a).double()
+    calls = []
+    rand_like = torch.rand_like
+
+    def fixed_rand_like(x):
+        calls.append(x.shape)
+        return jit[:, None].to(x.dtype).clone()
+
+    torch.rand_like = fixed_rand_like
+    # the gradient grid and inv_s take the default dtype (voxurf_womask_coarse.py:457, 490)
+    torch.set_default_dtype(torch.float64)
+    try:
+        ret = ref(T(ro), T(rd), T(vd), global_step=1, **rk)
+    finally:
+        torch.rand_like = rand_like
+        torch.set_default_dtype(torch.float32)
+    assert len(calls) == 1, calls
+    target = T(tgt)
+    loss = torch.nn.functional.mse_loss(ret["rgb_marched"], target)
+    pout = ret["alphainv_cum"][..., -1].clamp(1e-6, 1 - 1e-6)
+    loss = loss + 0.001 * (-(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean())
+    loss.backward()
+    out = {"R": R, "R_bg": R_bg, "n_rays": n_rays, "width": width, "seed": seed, "rays_o": ro, "rays_d": rd,
+           "viewdirs": vd, "target": tgt, "jitter": jit.numpy(),
+           "rgb_marched": ret["rgb_marched"].detach().numpy(), "alphainv_cum": ret["alphainv_cum"].detach().numpy(),
+           "in_marched": ret["in_marched"].detach().numpy(), "out_marched": ret["out_marched"].detach().numpy(),
+           "weights": ret["weights"].detach().numpy(), "bg_weights": ret["bg_weights"].detach().numpy(),
+           "loss": np.array(loss.item())}
+    for name in ("sdf", "k0", "bg_density"):
+        out["grad_" + name] = getattr(ref, name).grid.grad.numpy()
+    for net in ("rgbnet", "bg_rgbnet"):
+        for n, p in getattr(ref, net).named_parameters():
+            out[f"grad_{net}.{n}"] = p.grad.numpy()
+    for k, v in sd.items():
+        if v.dtype.is_floating_point:
+            out["state." + k] = v.float().numpy()
+    np.savez_compressed(path, **out)
+    print("wrote", path, "fg samples", ret["weights"].numel(), "bg samples", ret["bg_weights"].numel())
+
+
 def main():
     install_stubs()
     torch.set_default_dtype(torch.float32)
-    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg", "womask"]
+    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg", "womask", "womask_coarse"]
     if "ops" in which:
         ops_fixture(os.path.join(HERE, "ops_golden.npz"))
     if "fine" in which:
@@ -483,6 +548,8 @@ def main():
         bg_fixture(os.path.join(HERE, "bg_golden.npz"))
     if "womask" in which:
         womask_step_fixture(os.path.join(HERE, "womask_step_golden.npz"))
+    if "womask_coarse" in which:
+        womask_coarse_step_fixture(os.path.join(HERE, "womask_coarse_step_golden.npz"))
 
 
 if __name__ == "__main__":

@@ -28,3 +28,30 @@ def test_inputs_must_be_cuda_float32():
         background.background_samples(o, o, [-1] * 3, [1] * 3, 0.2, 6.0, 0.5, 2.0 / 24, 87)
     with pytest.raises(RuntimeError, match="CUDA"):
         ub360_utils_cuda.cumdist_thres(torch.zeros((2, 5)), 0.1)
+
+
+def test_womask_coarse_model_parameters_match_reference_state():
+    """The maskless coarse model's parameters and buffers carry the
+    reference's names and shapes (the state of its float64 golden run)."""
+    from voxurf_gb300 import configs
+
+    z = np.load(os.path.join(os.path.dirname(GOLDEN), "womask_coarse_step_golden.npz"))
+    R, Rb, width = int(z["R"]), int(z["R_bg"]), int(z["width"])
+    model = configs.build_womask_coarse_model(R, "fp32", device="cpu", seed=int(z["seed"]), width=width, R_bg=Rb)
+    ours = {k: tuple(v.shape) for k, v in model.state_dict().items()}
+    ref = {k[len("state."):]: z[k].shape for k in z.files if k.startswith("state.")}
+    ref = {k: v for k, v in ref.items() if k.split(".")[0] not in ("smooth_conv", "grad_conv", "tv_smooth_conv")}
+    assert ours == ref
+    # same initial state as the fixture (both are built by the same builder)
+    for k, v in model.state_dict().items():
+        assert np.array_equal(v.float().numpy(), z["state." + k]), k
+
+
+def test_womask_coarse_model_rejects_swapped_frequencies():
+    from voxurf_gb300 import configs
+    from voxurf_gb300.voxurf_womask_coarse import VoxurfWomaskCoarse
+
+    kw = configs.womask_coarse_model_kwargs(8, "fp32", 16)
+    kw["bg_posbase_pe"] = 4
+    with pytest.raises(ValueError, match="bg_posbase_pe"):
+        VoxurfWomaskCoarse(**kw)

@@ -1,0 +1,120 @@
+"""The maskless coarse model (lib/voxurf_womask_coarse.py:611-780): one
+training step (forward, loss, backward) against the reference model's own
+float64 run (tests/golden/womask_coarse_step_golden.npz, made by
+tests/golden/make_golden.py with the reference's background jitter fixed).
+
+FP32 bars as the other golden step tests: rgb_marched, alphainv_cum,
+in_marched, out_marched and the per-sample weights within 1e-5 absolute;
+every parameter gradient (sdf, k0, bg_density, rgbnet, bg_rgbnet) within
+rel-L2 1e-5.  The kept foreground and background sample counts equal the
+reference's.  BF16 (k0 from its BF16 copy, both MLPs on the tensor cores):
+colours within 2e-3, gradients rel-L2 within 5e-2.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from voxurf_gb300 import configs
+from voxurf_gb300.train import fine_loss
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+WC = np.load(os.path.join(HERE, "womask_coarse_step_golden.npz"))
+
+
+def _model(device, precision):
+    from voxurf_gb300.voxurf_womask_coarse import VoxurfWomaskCoarse
+
+    R, Rb, width = int(WC["R"]), int(WC["R_bg"]), int(WC["width"])
+    model = VoxurfWomaskCoarse(**configs.womask_coarse_model_kwargs(R, precision, width, Rb))
+    sd = {k[len("state."):]: torch.from_numpy(WC[k]) for k in WC.files if k.startswith("state.")}
+    # the reference's smoothing / gradient convolutions are fixed-kernel
+    # modules there; here the smoothing is a kernel parameterised by its taps
+    sd = {k: v for k, v in sd.items() if not k.split(".")[0] in ("smooth_conv", "grad_conv", "tv_smooth_conv")}
+    missing, unexpected = model.load_state_dict(sd, strict=False)
+    assert not unexpected, unexpected
+    assert not [k for k in missing if k.endswith(("grid", "weight", "bias"))], missing
+    model = model.to(device)
+    if precision == "bf16":
+        model.refresh_k0_shadow()
+    return model
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64).reshape(-1), np.asarray(b, np.float64).reshape(-1)
+    return float(np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30))
+
+
+def _inputs(cuda):
+    T = lambda a: torch.from_numpy(np.asarray(a)).to(cuda)
+    return T(WC["rays_o"]), T(WC["rays_d"]), T(WC["viewdirs"]), T(WC["target"]), T(WC["jitter"])
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_womask_coarse_step_vs_reference_golden(cuda, precision):
+    model = _model(cuda, precision)
+    ro, rd, vd, target, jit = _inputs(cuda)
+    rk = dict(configs.COARSE_RENDER_KWARGS, bg=1)
+    ret = model(ro, rd, vd, global_step=1, bg_jitter=jit, **rk)
+    loss = fine_loss(ret, target, weight_rgb0=0.0)
+    loss.backward()
+    torch.cuda.synchronize()
+    assert ret["weights"].numel() == WC["weights"].size
+    assert ret["bg_weights"].numel() == WC["bg_weights"].size
+    col_tol = 1e-5 if precision == "fp32" else 2e-3
+    for k in ("rgb_marched", "alphainv_cum", "in_marched", "out_marched", "weights", "bg_weights"):
+        err = np.abs(ret[k].detach().float().cpu().numpy() - WC[k]).max()
+        assert err <= col_tol, (k, err)
+    g_tol = 1e-5 if precision == "fp32" else 5e-2
+    errs = {}
+    for name in ("sdf", "k0", "bg_density"):
+        g = getattr(model, name).grid.grad.contiguous().cpu().numpy()
+        errs[name] = _rel(g, WC["grad_" + name])
+    for net in ("rgbnet", "bg_rgbnet"):
+        for n, p in getattr(model, net).named_parameters():
+            errs[f"{net}.{n}"] = _rel(p.grad.cpu().numpy(), WC[f"grad_{net}.{n}"])
+    print(precision, {k: f"{v:.2e}" for k, v in errs.items()})
+    bad = {k: v for k, v in errs.items() if not v <= g_tol}
+    assert not bad, bad
+    assert abs(float(loss.detach()) - float(WC["loss"])) <= col_tol * max(1.0, float(WC["loss"]))
+
+
+def test_womask_coarse_foreground_inside_unit_sphere(cuda):
+    """Every shaded foreground sample lies inside the unit sphere and the
+    bbox; every background sample comes from a ray's own offsets."""
+    model = _model(cuda, "fp32")
+    ro, rd, vd, _, jit = _inputs(cuda)
+    rk = dict(configs.COARSE_RENDER_KWARGS, bg=1)
+    with torch.no_grad():
+        model(ro, rd, vd, global_step=1, bg_jitter=jit, **rk)
+    fr = model._last_frame
+    pts = fr.pts2.double()
+    assert pts.numel() > 0
+    assert bool((torch.linalg.norm(pts, dim=-1) < 1.0).all())
+    ray2 = fr.ray2.long()
+    assert bool((ray2[1:] >= ray2[:-1]).all())
+
+
+def test_womask_coarse_render_without_training(cuda):
+    """global_step None: no jitter, no sphere reset; render_depth and
+    render_grad give per-ray depth and normals."""
+    model = _model(cuda, "fp32")
+    ro, rd, vd, _, _ = _inputs(cuda)
+    rk = dict(configs.COARSE_RENDER_KWARGS, bg=1, render_depth=True, render_grad=True)
+    before = model.sdf.grid.detach().clone()
+    with torch.no_grad():
+        ret = model(ro, rd, vd, **rk)
+    n = ro.shape[0]
+    assert ret["rgb_marched"].shape == (n, 3) and ret["alphainv_cum"].shape == (n,)
+    assert ret["normal_marched"].shape == (n, 3) and ret["depth"].shape == (n,)
+    assert torch.equal(before, model.sdf.grid.detach())
+    assert torch.isfinite(ret["rgb_marched"]).all()
+    # depth = sum w * step * dist over each ray's shaded samples
+    fr = model._last_frame
+    w = ret["weights"].double()
+    dep = torch.zeros(n, dtype=torch.float64, device=cuda).index_add_(
+        0, fr.ray2.long(), w * fr.step2.double() * fr.dist)
+    assert torch.allclose(ret["depth"].double(), dep, atol=1e-5)

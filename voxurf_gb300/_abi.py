@@ -25,7 +25,7 @@ class FineMarchArgs(C.Structure):
         ("inv_s", F), ("dist", F), ("fast_color_thres", F), ("max_steps", I64),
         ("rec", P), ("dw_slot", P), ("n1", P), ("n2", P), ("alphainv_last", P),
         ("mask_density", P), ("mask_dgrid", GridGeom), ("mask_act_shift", F), ("mask_voxel_size_ratio", F),
-        ("mask_thres", F),
+        ("mask_thres", F), ("unit_sphere", I32), ("reserved0", I32),
     ]
 
 
@@ -128,7 +128,7 @@ class WomaskCompositeArgs(C.Structure):
         ("n_rays", I64), ("fg_off", P), ("w", P), ("logit", P), ("kout", P), ("bg_off", P), ("bw", P),
         ("blogit", P), ("stats", P), ("rgb0", P), ("rgbk", P), ("ainv", P), ("in_marched", P),
         ("bg_marched", P), ("g_rgb0", P), ("g_rgbk", P), ("g_ainv", P), ("d_logit", P), ("d_kout", P),
-        ("d_w", P), ("d_blogit", P), ("d_bw", P), ("k_into_logit", I32), ("reserved", I32),
+        ("d_w", P), ("d_blogit", P), ("d_bw", P), ("k_into_logit", I32), ("unclamped_parts", I32),
     ]
 
 

@@ -101,6 +101,48 @@ def build_womask_model(R: int = 64, precision: str = "fp32", device="cuda", seed
     return model
 
 
+def womask_coarse_model_kwargs(R: int = 96, precision: str = "fp32", width: int = 128, R_bg: int | None = None,
+                               bg_k0: bool = False) -> dict:
+    """Maskless coarse stage (lib/voxurf_womask_coarse.py) with the
+    configs/dtu_e2e_womask/coarse.py settings on top of
+    configs/default_fine_s.py: rgbnet k0 12 + PE(xyz, 5) 33 + PE(view, 4) 27
+    + normal 3 = 75 -> width -> 3; bg_rgbnet PE(xyz, 5) + PE(view, 4) = 60
+    (+ bg_k0 12 with bg_k0) -> width x3 -> 3; smoothing 5^3 sigma 0.8;
+    s_ratio 200, s_start 0.5; both selection thresholds 1e-4."""
+    return dict(
+        xyz_min=BBOX[0], xyz_max=BBOX[1], num_voxels=R ** 3, num_voxels_base=R ** 3, num_voxels_bg=(R_bg or R) ** 3,
+        alpha_init=1e-2, fast_color_thres=1e-4, bg_fast_color_thres=1e-4, rgbnet_dim=12, rgbnet_direct=True,
+        rgbnet_full_implicit=False, rgbnet_depth=3, rgbnet_width=width, posbase_pe=5, viewbase_pe=4, geo_rgb_dim=3,
+        bg_rgbnet_dim=12 if bg_k0 else 0, bg_posbase_pe=5, bg_viewbase_pe=4, bg_rgbnet_width=width,
+        bg_rgbnet_depth=4, smooth_ksize=5, smooth_sigma=0.8, sdf_thr=0.5, tv_in_sphere=False, smooth_scale=True,
+        s_ratio=200, s_start=0.5, precision=precision,
+    )
+
+
+def build_womask_coarse_model(R: int = 96, precision: str = "fp32", device="cuda", seed: int = 0, width: int = 128,
+                              R_bg: int | None = None, bg_k0: bool = False):
+    """Maskless coarse model with the sphere r=0.5 SDF (+ noise), k0 (and
+    bg_k0) ~ N(0, 0.1) and bg_density ~ N(1, 2)."""
+    from .voxurf_womask_coarse import VoxurfWomaskCoarse
+
+    torch.manual_seed(seed)
+    model = VoxurfWomaskCoarse(**womask_coarse_model_kwargs(R, precision, width, R_bg, bg_k0))
+    Rb = int(model.world_size_bg[0])
+    with torch.no_grad():
+        model.sdf.grid.data = torch.from_numpy(synthetic.make_sdf("sphere", R, seed=seed))[None, None].clone()
+        k0 = synthetic.make_k0(R, 12, seed=seed + 1)
+        model.k0.grid.data = k0.permute(3, 0, 1, 2)[None].contiguous(memory_format=torch.channels_last_3d)
+        if bg_k0:
+            bk = synthetic.make_k0(Rb, 12, seed=seed + 2)
+            model.bg_k0.grid.data = bk.permute(3, 0, 1, 2)[None].contiguous(memory_format=torch.channels_last_3d)
+        g = torch.Generator().manual_seed(seed + 3)
+        model.bg_density.grid.data = (torch.randn((1, 1, Rb, Rb, Rb), generator=g) * 2.0 + 1.0)
+    model = model.to(device)
+    if precision == "bf16":
+        model.refresh_k0_shadow()
+    return model
+
+
 # Render-server scenes: sphere_torus with different sizes per scene
 # (sphere r, torus R, torus r), each with its own seed.
 SERVE_SHAPES = [(0.45, 0.6, 0.15), (0.40, 0.55, 0.12), (0.50, 0.65, 0.18), (0.35, 0.50, 0.10)]

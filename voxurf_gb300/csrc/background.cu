@@ -80,12 +80,6 @@ __global__ void __launch_bounds__(CD_RAYS) cumdist_thres_kernel(const float* __r
 // ---------------------------------------------------------------------------
 // Background samples of one ray.
 
-// |v| as torch's norm reduction forms it: squares accumulated with fused
-// multiply-adds in x, y, z order, then a correctly rounded square root.
-__device__ __forceinline__ float norm3(float x, float y, float z) {
-  return __fsqrt_rn(__fmaf_rn(z, z, __fmaf_rn(y, y, fmul(x, x))));
-}
-
 struct BgRay {
   float o[3], d[3];
   float t_min, d_norm, jit;

@@ -79,6 +79,12 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
+// |v| as torch's norm reduction forms it: squares accumulated with fused
+// multiply-adds in x, y, z order, then a correctly rounded square root.
+__device__ __forceinline__ float norm3(float x, float y, float z) {
+  return __fsqrt_rn(__fmaf_rn(z, z, __fmaf_rn(y, y, fmul(x, x))));
+}
+
 // Transmittance precision: a ray of more samples than this carries its
 // transmittance products (forward) and its suffix sums (backward) in FP64;
 // shorter rays in FP32.  GB300 runs FP64 at a small fraction of its FP32

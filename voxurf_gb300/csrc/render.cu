@@ -41,6 +41,7 @@ struct MarchParams {
   const uint8_t* mask;     // optional bool grid for maskcache_lookup semantics
   int mX, mY, mZ;
   float mscale[3], mshift[3];
+  int unit_sphere;         // keep only |p| < 1 (the maskless coarse model)
   float inv_s, dist, thres;
   int max_steps;
   // outputs
@@ -77,6 +78,7 @@ __device__ __forceinline__ void march_fine_ray(const MarchParams& P, int r, cons
       float p[3];
       sample_point(f, P.stepdist, k, p);
       bool inb = !outside_bbox(p, P.bmin, P.bmax);
+      if (inb && P.unit_sphere) inb = norm3(p[0], p[1], p[2]) < 1.f;
       if (inb && P.mask) inb = mask_hit(P, p);
       if (DENS && inb) inb = density_mask_hit(P.dm, p);
       if (inb) {
@@ -795,6 +797,7 @@ __device__ __forceinline__ void march_coarse_ray(const CoarseMarchParams& C, int
       float p[3];
       sample_point(f, P.stepdist, k, p);
       inb = !outside_bbox(p, P.bmin, P.bmax);
+      if (inb && P.unit_sphere) inb = norm3(p[0], p[1], p[2]) < 1.f;
       if (inb && P.mask) inb = mask_hit(P, p);
       if (DENS && inb) inb = density_mask_hit(P.dm, p);
       if (inb) {
@@ -1285,6 +1288,7 @@ int vx_fine_march(const vx_fine_march_args* A, void* stream) {
     P.mscale[a] = A->mask_scale[a];
     P.mshift[a] = A->mask_shift[a];
   }
+  P.unit_sphere = A->unit_sphere != 0;
   P.inv_s = A->inv_s;
   P.dist = A->dist;
   P.thres = A->fast_color_thres;
@@ -1589,6 +1593,7 @@ int vx_coarse_march(const vx_coarse_march_args* A, void* stream) {
   P.mX = (int)M->mask_X;
   P.mY = (int)M->mask_Y;
   P.mZ = (int)M->mask_Z;
+  P.unit_sphere = M->unit_sphere != 0;
   P.inv_s = M->inv_s;
   P.dist = M->dist;
   P.thres = M->fast_color_thres;

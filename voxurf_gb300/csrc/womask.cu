@@ -226,10 +226,14 @@ struct WmCompParams {
   float* d_blogit;
   float* d_bw;
   int k_into_logit;
+  int unclamped_parts;    // 1: the in/bg sums enter unclamped (the coarse model)
 };
 
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
 __device__ __forceinline__ bool in01(float x) { return x >= 0.f && x <= 1.f; }
+// a per-branch sum as it enters the final mix: clamped (fine model) or not
+__device__ __forceinline__ float part(const WmCompParams& P, float x) { return P.unclamped_parts ? x : clamp01(x); }
+__device__ __forceinline__ bool part_live(const WmCompParams& P, float x) { return P.unclamped_parts || in01(x); }
 
 __global__ void __launch_bounds__(256) wm_composite_kernel(WmCompParams P) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -262,13 +266,13 @@ __global__ void __launch_bounds__(256) wm_composite_kernel(WmCompParams P) {
     const float one_m = 1.f - cum;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float bgm = clamp01(sb[c]);
-      const float in0 = clamp01(s0[c]);
+      const float bgm = part(P, sb[c]);
+      const float in0 = part(P, s0[c]);
       P.rgb0[3 * r + c] = clamp01(in0 + one_m * bgm);
       P.bg_marched[3 * r + c] = bgm;
       float inm = in0;
       if (P.kout) {
-        const float ink = clamp01(sk[c]);
+        const float ink = part(P, sk[c]);
         P.rgbk[3 * r + c] = clamp01(ink + one_m * bgm);
         inm = ink;
       }
@@ -291,23 +295,23 @@ __global__ void __launch_bounds__(256) wm_composite_bwd_kernel(WmCompParams P) {
   float g_s0[3], g_sk[3], g_sb[3], g_onem = P.g_ainv ? P.g_ainv[r] : 0.f;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float bgm = clamp01(st[6 + c]);
+    const float bgm = part(P, st[6 + c]);
     float g_bgm = 0.f;
-    // rgbnet: rgb0 = clamp(clamp(s0) + (1 - cum) * bg)
-    const float in0 = clamp01(st[c]);
+    // rgbnet: rgb0 = clamp(part(s0) + (1 - cum) * part(sb))
+    const float in0 = part(P, st[c]);
     const float g_u0 = (P.g_rgb0 && in01(in0 + one_m * bgm)) ? P.g_rgb0[3 * r + c] : 0.f;
-    g_s0[c] = in01(st[c]) ? g_u0 : 0.f;
+    g_s0[c] = part_live(P, st[c]) ? g_u0 : 0.f;
     g_onem += g_u0 * bgm;
     g_bgm += g_u0 * one_m;
     g_sk[c] = 0.f;
     if (P.kout) {
-      const float ink = clamp01(st[3 + c]);
+      const float ink = part(P, st[3 + c]);
       const float g_uk = (P.g_rgbk && in01(ink + one_m * bgm)) ? P.g_rgbk[3 * r + c] : 0.f;
-      g_sk[c] = in01(st[3 + c]) ? g_uk : 0.f;
+      g_sk[c] = part_live(P, st[3 + c]) ? g_uk : 0.f;
       g_onem += g_uk * bgm;
       g_bgm += g_uk * one_m;
     }
-    g_sb[c] = in01(st[6 + c]) ? g_bgm : 0.f;
+    g_sb[c] = part_live(P, st[6 + c]) ? g_bgm : 0.f;
   }
   const float g_cum = -g_onem;
   for (int64_t i = P.fg_off[r] + lane; i < P.fg_off[r + 1]; i += 32) {
@@ -481,6 +485,7 @@ int vx_womask_composite(const vx_womask_composite_args* a, void* stream) {
   P.d_blogit = a->d_blogit;
   P.d_bw = a->d_bw;
   P.k_into_logit = a->k_into_logit;
+  P.unclamped_parts = a->unclamped_parts != 0;
   if (bwd)
     wm_composite_bwd_kernel<<<warp_grid(a->n_rays), 256, 0, as_stream(stream)>>>(P);
   else

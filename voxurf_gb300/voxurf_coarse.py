@@ -53,7 +53,10 @@ class _CoarseGeometry(torch.autograd.Function):
         X, Y, Z = fr.geom.X, fr.geom.Y, fr.geom.Z
         raw = sdf_grid.reshape(X, Y, Z)
         fr.sdf_s = smooth_grid(sdf_grid, fr.taps) if fr.taps is not None else raw
-        fr.G4 = sdf_gradient_grid(raw, fr.voxel_size)
+        # the gradient grid of the raw SDF (voxurf_coarse.py:531), or of the
+        # smoothed one in the maskless model (voxurf_womask_coarse.py:657)
+        grad_src = fr.sdf_s if fr.grad_of_smoothed else raw
+        fr.G4 = sdf_gradient_grid(grad_src.contiguous(), fr.voxel_size)
         N, ms = fr.n_rays, fr.max_steps
         rec = torch.empty((N * ms, 4), dtype=torch.float32, device=dev)
         dw_slot = torch.empty(N * ms, dtype=torch.float32, device=dev)
@@ -68,6 +71,7 @@ class _CoarseGeometry(torch.autograd.Function):
         m.sdf_smooth, m.voxel_size = ptr(fr.sdf_s), fr.voxel_size
         if fr.mask_cache is not None:
             fr.mask_cache.fill_march(m)
+        m.unit_sphere = int(fr.unit_sphere)
         m.inv_s, m.dist, m.fast_color_thres, m.max_steps = fr.inv_s, fr.dist, fr.thres, ms
         m.rec, m.dw_slot, m.n1, m.n2, m.alphainv_last = ptr(rec), ptr(dw_slot), ptr(n1), ptr(n2), ptr(alphainv_last)
         a.grad4, a.n2b = ptr(fr.G4), ptr(n2b)
@@ -143,8 +147,11 @@ class _CoarseGeometry(torch.autograd.Function):
             d_grad2 = d_grad2.float().contiguous()
             b.d_grad2 = ptr(d_grad2)
         _abi.call_struct("vx_coarse_backward", b, st)
+        if fr.grad_of_smoothed:
+            _abi.call("vx_sdf_gradient_grid_adjoint", ptr(dG4), ptr(d_sdf_s), X, Y, Z, float(fr.voxel_size), 1, 1, st)
         d_sdf = smooth_grid_adjoint(d_sdf_s, fr.taps) if fr.taps is not None else d_sdf_s
-        _abi.call("vx_sdf_gradient_grid_adjoint", ptr(dG4), ptr(d_sdf), X, Y, Z, float(fr.voxel_size), 1, 1, st)
+        if not fr.grad_of_smoothed:
+            _abi.call("vx_sdf_gradient_grid_adjoint", ptr(dG4), ptr(d_sdf), X, Y, Z, float(fr.voxel_size), 1, 1, st)
         return d_sdf.reshape(ctx.sdf_shape), (d_k0 if fr.use_k0 else None), None
 
 
@@ -336,9 +343,10 @@ class Voxurf(nn.Module):
         w = weight * self.world_size.max() / 128
         self.k0.total_variation_add_grad(w, w, w, dense_mode)
 
-    def forward(self, rays_o, rays_d, viewdirs, global_step=None, **render_kwargs):
+    def march_frame(self, rays_o, rays_d, viewdirs, inv_s: float, render_kwargs) -> FineFrame:
+        """The per-forward state of _CoarseGeometry: rays, sampling, grid
+        geometry, NeuS constants, feature layout."""
         N = len(rays_o)
-        s_val, inv_s = self.neus_s_val(global_step)
         fr = FineFrame()
         fr.n_rays = N
         fr.rays_o = rays_o.contiguous().float()
@@ -355,6 +363,7 @@ class Voxurf(nn.Module):
         fr.max_steps = max_steps_bound(grid_mod.host_values(self.xyz_min), grid_mod.host_values(self.xyz_max), fr.stepdist)
         fr.taps = self.smooth_taps if self.smooth_sdf else None
         fr.mask_cache = self.mask_cache  # MaskGrid (bool) or MaskCache (density), or None
+        fr.unit_sphere, fr.grad_of_smoothed = False, False
         fr.cfg = _coarse_cfg(self)
         fr.use_k0 = not self.rgbnet_full_implicit
         fr.bf16 = self.precision == "bf16"
@@ -367,6 +376,11 @@ class Voxurf(nn.Module):
         # MLP input rows zero-padded to the stride of the MLP engine
         fr.ld = row_stride(fr.d1, torch.bfloat16 if fr.bf16 else torch.float32)
         fr.render_extras = bool(render_kwargs.get("render_depth", False) or render_kwargs.get("render_grad", False))
+        return fr
+
+    def forward(self, rays_o, rays_d, viewdirs, global_step=None, **render_kwargs):
+        s_val, inv_s = self.neus_s_val(global_step)
+        fr = self.march_frame(rays_o, rays_d, viewdirs, inv_s, render_kwargs)
         Xf, w2, alphainv_last, normal2, alpha2 = _CoarseGeometry.apply(self.sdf.grid, self.k0.grid, fr)
         fr.normal2 = normal2
         rgb_logit = apply_mlp(self.rgbnet, Xf)

@@ -213,7 +213,7 @@ class _BgFeatures(torch.autograd.Function):
 
 class _WomaskComposite(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, w, logit, kout, bw, blogit, fg_off, bg_off, k_into_logit: bool):
+    def forward(ctx, w, logit, kout, bw, blogit, fg_off, bg_off, k_into_logit: bool, unclamped_parts: bool = False):
         N = fg_off.numel() - 1
         dev = w.device
         f32 = torch.float32
@@ -229,9 +229,10 @@ class _WomaskComposite(torch.autograd.Function):
         a.n_rays, a.fg_off, a.w, a.logit, a.kout = N, ptr(fg_off), ptr(w), ptr(logit), ptr(kout)
         a.bg_off, a.bw, a.blogit, a.stats = ptr(bg_off), ptr(bw), ptr(blogit), ptr(stats)
         a.rgb0, a.rgbk, a.ainv, a.in_marched, a.bg_marched = ptr(rgb0), ptr(rgbk), ptr(ainv), ptr(in_m), ptr(bg_m)
+        a.unclamped_parts = int(bool(unclamped_parts))
         _abi.call_struct("vx_womask_composite", a, stream_ptr())
         ctx.save_for_backward(w, logit, kout, bw, blogit, fg_off, bg_off, stats)
-        ctx.k_into_logit = bool(k_into_logit)
+        ctx.k_into_logit, ctx.unclamped_parts = bool(k_into_logit), bool(unclamped_parts)
         ctx.mark_non_differentiable(in_m, bg_m)
         return (rgbk if rgbk is not None else rgb0), rgb0, ainv, in_m, bg_m
 
@@ -256,9 +257,9 @@ class _WomaskComposite(torch.autograd.Function):
         a.g_rgb0, a.g_rgbk, a.g_ainv = ptr(g_rgb0), ptr(g_rgbk), ptr(g_ainv)
         a.d_logit, a.d_kout, a.d_w, a.d_blogit, a.d_bw = ptr(d_logit), ptr(d_kout), ptr(d_w), ptr(d_blogit), \
             ptr(d_bw)
-        a.k_into_logit = int(ctx.k_into_logit)
+        a.k_into_logit, a.unclamped_parts = int(ctx.k_into_logit), int(ctx.unclamped_parts)
         _abi.call_struct("vx_womask_composite", a, stream_ptr())
-        return d_w, d_logit, d_kout, d_bw, d_blogit, None, None, None
+        return d_w, d_logit, d_kout, d_bw, d_blogit, None, None, None, None
 
 
 def _ray_offsets(ray_id: torch.Tensor, n_rays: int) -> torch.Tensor:
