@@ -487,6 +487,37 @@ size_t vx_smooth_grad_tv_scratch_bytes(int64_t X, int64_t Y, int64_t Z);
 int vx_smooth_grad_tv(const float* G, const uint8_t* mask, int64_t X, int64_t Y, int64_t Z, float grad_scale,
                       float* dG, double* partial, void* stream);
 
+/* ---- loss-form total variation over a voxel mask ----------------------------
+ * total_variation(v, mask) of the model files and its gradient, for
+ * density_total_variation(sdf_tv, bg_density_tv) / k0_total_variation /
+ * bg_k0_total_variation (voxurf_coarse.py:300-320, voxurf_fine.py:412-432,
+ * voxurf_womask_fine.py:500-548, voxurf_womask_coarse.py:398-440).
+ * Selected pairs along axis a: (p, p + e_a) with both voxels inside the grid
+ * and in the mask; every channel uses the voxel mask.  S_a = sum of |v[p +
+ * e_a] - v[p]| over them, P_a = C x their number, M = C x the mask's voxels.
+ *   mode 0 (voxurf_coarse.py:702-715): (S_0 + S_1 + S_2) / 3 / M
+ *   mode 1 (voxurf_fine.py:956-969 and the maskless models):
+ *          (S_0/P_0 + S_1/P_1 + S_2/P_2) / 3
+ * loss = weight x that; axis_scale[a] = d loss / d |diff| of one selected
+ * pair of axis a.  Sums in FP64 in a fixed order (deterministic). */
+typedef struct {
+  const float* v;           /* [C,X,Y,Z] (channel_last 0) or [X,Y,Z,C]           */
+  int64_t C, X, Y, Z;
+  int32_t channel_last;
+  int32_t mode;             /* 0 or 1, above                                    */
+  const uint8_t* mask;      /* [X,Y,Z] voxel mask, or NULL (every voxel)        */
+  float weight;
+  float* loss;              /* out [1] (device)                                 */
+  float* axis_scale;        /* out [3] (device), read by the backward           */
+  void* scratch;            /* vx_tv_loss_scratch_bytes(X, Y, Z) bytes          */
+  size_t scratch_bytes;
+} vx_tv_loss_args;
+size_t vx_tv_loss_scratch_bytes(int64_t X, int64_t Y, int64_t Z);
+int vx_tv_loss(const vx_tv_loss_args* args, void* stream);
+/* grad (v's layout) += g_loss[0] (device scalar) x d loss / d v, from the
+ * axis_scale the forward wrote; sign(0) = 0 as torch's abs. */
+int vx_tv_loss_backward(const vx_tv_loss_args* args, const float* g_loss, float* grad, void* stream);
+
 /* ---- fused coarse-model rendering (lib/voxurf_coarse.py:513-619) ---------- */
 
 /* March with the coarse semantics: gradient from the [X,Y,Z,4] grid of the

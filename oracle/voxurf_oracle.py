@@ -558,3 +558,26 @@ def tv_add_grad(grid_param, weight, world_size_max, dense_mode, mask=None):
                                                               dense_mode)
     else:
         tv_add_grad_torch(grid_param.data, grid_param.grad, w, w, w, dense_mode, mask)
+
+
+def total_variation_loss(v: torch.Tensor, mask=None, mode: int = 1) -> torch.Tensor:
+    """total_variation(v, mask) of the model files: the absolute forward
+    differences along X, Y and Z, restricted to the pairs whose two voxels
+    are in the mask (the mask holds v's channels, or one channel that is
+    repeated).  mode 0, lib/voxurf_coarse.py:702-715: the three sums over 3
+    x the mask's entries; mode 1, lib/voxurf_fine.py:956-969 (the maskless
+    models hold copies): the mean of each axis's selection, averaged."""
+    C = v.shape[1]
+    if mask is not None and mask.shape[1] != C:
+        mask = mask.expand(-1, C, -1, -1, -1)
+    sums, means = [], []
+    for dim in (2, 3, 4):
+        n = v.shape[dim]
+        d = (v.narrow(dim, 1, n - 1) - v.narrow(dim, 0, n - 1)).abs()
+        if mask is not None:
+            d = d[mask.narrow(dim, 0, n - 1) & mask.narrow(dim, 1, n - 1)]
+        sums.append(d.sum())
+        means.append(d.mean())
+    if mode == 0:
+        return (sums[0] + sums[1] + sums[2]) / 3 / mask.sum()
+    return (means[0] + means[1] + means[2]) / 3

@@ -17,7 +17,7 @@ script stubs them:
     reference's checkpoint loading relies on).
 PYTHONDONTWRITEBYTECODE keeps the read-only reference tree clean.
 
-    VOXURF_REFERENCE=<reference checkout> python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt] [bg] [womask] [womask_coarse]
+    VOXURF_REFERENCE=<reference checkout> python tests/golden/make_golden.py [ops] [fine] [coarse] [mesh] [ckpt] [bg] [womask] [womask_coarse] [tv]
     (default: all)
 """
 from __future__ import annotations
@@ -342,6 +342,39 @@ def ckpt_fixture(dirpath, R=16, seed=7):
     print("wrote", ckpt_c, ckpt_f, "shaded samples", ret["weights"].numel(), "hits", int(hit.sum()))
 
 
+def tv_fixture(path, seed=21):
+    """The loss-form total variation of the model files, called directly:
+    lib/voxurf_coarse.py:702-715 (sum over 3 x the mask's entries) and
+    lib/voxurf_fine.py:956-969 (per-axis means; the maskless models'
+    copies, voxurf_womask_fine.py:1242-1255 and voxurf_womask_coarse.py:
+    858-871, are the same statements), in float64 with their gradients by
+    autograd.  Grids of 1 and 12 channels with quantised values (so that
+    some neighbour differences are exactly zero), with a random voxel mask
+    and, for the mean form, without one."""
+    import lib.voxurf_coarse as rc
+    import lib.voxurf_fine as rf
+
+    g = torch.Generator().manual_seed(seed)
+    out = {}
+    for C, shape in ((1, (9, 10, 11)), (12, (7, 8, 9))):
+        v = torch.randint(0, 5, (1, C, *shape), generator=g).double() / 4.0
+        v = v + (torch.rand((1, C, *shape), generator=g, dtype=torch.float64) < 0.5) * torch.randn(
+            (1, C, *shape), generator=g, dtype=torch.float64) * 0.1
+        mask = torch.rand((1, 1, *shape), generator=g) < 0.7
+        out[f"c{C}_v"] = v.numpy()
+        out[f"c{C}_mask"] = mask.numpy()
+        for name, fn, m in (("sum", rc.total_variation, mask), ("mean", rf.total_variation, mask),
+                            ("mean_nomask", rf.total_variation, None)):
+            x = v.clone().requires_grad_(True)
+            mm = None if m is None else m.repeat(1, C, 1, 1, 1)
+            loss = fn(x, mm)
+            loss.backward()
+            out[f"c{C}_{name}_loss"] = np.array(loss.item())
+            out[f"c{C}_{name}_grad"] = x.grad.numpy()
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
 def bg_fixture(path, seed=8):
     """Background samples of the models without an object mask: the
     reference's sample_ray_ori and outside_sphere_trans (womask fine
@@ -523,17 +556,40 @@ def womask_coarse_step_fixture(path, R=16, R_bg=12, n_rays=96, width=32, seed=13
     for net in ("rgbnet", "bg_rgbnet"):
         for n, p in getattr(ref, net).named_parameters():
             out[f"grad_{net}.{n}"] = p.grad.numpy()
+    # the ori_tv regularisers of the coarse stage (run.py:617-626) on the
+    # state of the same step: density_total_variation(sdf_tv=0.1,
+    # smooth_grad_tv=0.05) + 0.01 k0_total_variation(), with tv_in_sphere
+    # True (the unit-sphere voxel mask; the dtu_e2e_womask setting False
+    # makes the mask all ones).  self.gradient comes from a second, identical
+    # forward (the first one's graph is spent).
+    for p in ref.parameters():
+        p.grad = None
+    ref.tv_in_sphere = True
+    calls.clear()
+    torch.rand_like = fixed_rand_like
+    torch.set_default_dtype(torch.float64)
+    try:
+        ref(T(ro), T(rd), T(vd), global_step=1, **rk)
+        tv = ref.density_total_variation(sdf_tv=0.1, smooth_grad_tv=0.05) + 0.01 * ref.k0_total_variation()
+    finally:
+        torch.rand_like = rand_like
+        torch.set_default_dtype(torch.float32)
+    tv.backward()
+    out["tv_loss"] = np.array(tv.item())
+    out["tv_grad_sdf"] = ref.sdf.grid.grad.numpy()
+    out["tv_grad_k0"] = ref.k0.grid.grad.numpy()
     for k, v in sd.items():
         if v.dtype.is_floating_point:
             out["state." + k] = v.float().numpy()
     np.savez_compressed(path, **out)
-    print("wrote", path, "fg samples", ret["weights"].numel(), "bg samples", ret["bg_weights"].numel())
+    print("wrote", path, "fg samples", ret["weights"].numel(), "bg samples", ret["bg_weights"].numel(),
+          "tv", tv.item())
 
 
 def main():
     install_stubs()
     torch.set_default_dtype(torch.float32)
-    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg", "womask", "womask_coarse"]
+    which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg", "womask", "womask_coarse", "tv"]
     if "ops" in which:
         ops_fixture(os.path.join(HERE, "ops_golden.npz"))
     if "fine" in which:
@@ -550,6 +606,8 @@ def main():
         womask_step_fixture(os.path.join(HERE, "womask_step_golden.npz"))
     if "womask_coarse" in which:
         womask_coarse_step_fixture(os.path.join(HERE, "womask_coarse_step_golden.npz"))
+    if "tv" in which:
+        tv_fixture(os.path.join(HERE, "tv_golden.npz"))
 
 
 if __name__ == "__main__":

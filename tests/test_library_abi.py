@@ -76,7 +76,7 @@ def test_struct_sizes_match_c_layout():
                "vx_mlp_sum_job": _abi.MlpSumJob, "vx_womask_fg_alpha_args": _abi.WomaskFgAlphaArgs,
                "vx_womask_bg_alpha_args": _abi.WomaskBgAlphaArgs,
                "vx_womask_bg_features_args": _abi.WomaskBgFeaturesArgs,
-               "vx_womask_composite_args": _abi.WomaskCompositeArgs}
+               "vx_womask_composite_args": _abi.WomaskCompositeArgs, "vx_tv_loss_args": _abi.TvLossArgs}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "voxurf_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

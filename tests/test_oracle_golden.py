@@ -205,3 +205,19 @@ def test_cumdist_thres_restatement():
             if want[r, i]:
                 cum = np.float32(0)
     assert np.array_equal(m, want)
+
+
+@pytest.mark.parametrize("C", [1, 12])
+@pytest.mark.parametrize("form", ["sum", "mean", "mean_nomask"])
+def test_total_variation_loss_restatement(C, form):
+    """The loss-form total_variation (sum and per-axis mean forms) and its
+    gradient against the reference functions' own float64 outputs."""
+    from oracle.voxurf_oracle import total_variation_loss
+
+    z = np.load(os.path.join(HERE, "tv_golden.npz"))
+    v = torch.from_numpy(z[f"c{C}_v"]).requires_grad_(True)
+    mask = None if form == "mean_nomask" else torch.from_numpy(z[f"c{C}_mask"])
+    loss = total_variation_loss(v, mask, mode=0 if form == "sum" else 1)
+    loss.backward()
+    assert abs(loss.item() - float(z[f"c{C}_{form}_loss"])) <= 1e-12
+    assert np.abs(v.grad.numpy() - z[f"c{C}_{form}_grad"]).max() <= 1e-12

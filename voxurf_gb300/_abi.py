@@ -101,6 +101,13 @@ class BgSampleArgs(C.Structure):
     ]
 
 
+class TvLossArgs(C.Structure):
+    _fields_ = [
+        ("v", P), ("C", I64), ("X", I64), ("Y", I64), ("Z", I64), ("channel_last", I32), ("mode", I32),
+        ("mask", P), ("weight", F), ("loss", P), ("axis_scale", P), ("scratch", P), ("scratch_bytes", C.c_size_t),
+    ]
+
+
 class WomaskFgAlphaArgs(C.Structure):
     _fields_ = [
         ("n", I64), ("pts", P), ("ray_id", P), ("viewdirs", P), ("grid", GridGeom), ("sdf_smooth", P),
@@ -346,6 +353,12 @@ def _declare():
     lib.vx_smooth_grad_tv_scratch_bytes.restype = C.c_size_t
     lib.vx_smooth_grad_tv.argtypes = [P, P, I64, I64, I64, F, P, P, P]
     lib.vx_smooth_grad_tv.restype = C.c_int
+    lib.vx_tv_loss_scratch_bytes.argtypes = [I64, I64, I64]
+    lib.vx_tv_loss_scratch_bytes.restype = C.c_size_t
+    lib.vx_tv_loss.argtypes = [C.POINTER(TvLossArgs), P]
+    lib.vx_tv_loss.restype = C.c_int
+    lib.vx_tv_loss_backward.argtypes = [C.POINTER(TvLossArgs), P, P, P]
+    lib.vx_tv_loss_backward.restype = C.c_int
     SP = C.POINTER(SceneDesc)
     for name, args in _SERVE_SIGNATURES.items():
         fn = getattr(lib, name)
@@ -380,4 +393,5 @@ def struct_names() -> list[str]:
                                 "vx_bg_samples_fill", "vx_cast_rows_bf16", "vx_mlp_train_pack",
                                 "vx_mlp_train_reduce", "vx_mlp_wgrad_grid", "vx_mlp_train_wgrad_multi", "vx_mlp_wgrad_split", "vx_mlp_f32_rowgemm_grid",
                                 "vx_mlp_f32_wgrad_grid", "vx_mlp_f32_reduce",
-                                "vx_fine_composite_loss_scratch_bytes"] + list(_SERVE_SIGNATURES)
+                                "vx_fine_composite_loss_scratch_bytes", "vx_tv_loss_scratch_bytes", "vx_tv_loss",
+                                "vx_tv_loss_backward"] + list(_SERVE_SIGNATURES)

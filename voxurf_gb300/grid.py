@@ -14,6 +14,7 @@ Differences by design:
 """
 from __future__ import annotations
 
+import ctypes
 import weakref
 
 import numpy as np
@@ -21,7 +22,7 @@ import torch
 import torch.nn as nn
 import torch.nn.functional as F
 
-from . import _abi, render_utils_cuda
+from . import _abi, _native, render_utils_cuda
 from ._torch import call, ptr, stream_ptr
 
 
@@ -82,6 +83,68 @@ class _GridSample(torch.autograd.Function):
 
 def _is_channel_last(t: torch.Tensor) -> bool:
     return t.size(1) > 1 and t.is_contiguous(memory_format=torch.channels_last_3d) and not t.is_contiguous()
+
+
+class _TVLoss(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, v, mask_u8, mode: int, weight: float):
+        X, Y, Z = v.shape[-3:]
+        dev = v.device
+        cl = _is_channel_last(v)
+        if not (cl or v.is_contiguous()):
+            v = v.contiguous()
+        a = _abi.TvLossArgs()
+        a.v, a.C, a.X, a.Y, a.Z, a.channel_last, a.mode = ptr(v), v.size(1), X, Y, Z, int(cl), int(mode)
+        a.mask, a.weight = ptr(mask_u8), float(weight)
+        loss = torch.empty(1, dtype=torch.float32, device=dev)
+        scale = torch.empty(3, dtype=torch.float32, device=dev)
+        _abi._declare()
+        nb = int(_native.load().vx_tv_loss_scratch_bytes(X, Y, Z))
+        sc = torch.empty(nb, dtype=torch.uint8, device=dev)
+        a.loss, a.axis_scale, a.scratch, a.scratch_bytes = ptr(loss), ptr(scale), ptr(sc), nb
+        _abi.call_struct("vx_tv_loss", a, stream_ptr())
+        ctx.save_for_backward(v, mask_u8, scale)
+        ctx.mode, ctx.cl = int(mode), cl
+        return loss[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        v, mask_u8, scale = ctx.saved_tensors
+        X, Y, Z = v.shape[-3:]
+        d = torch.zeros_like(v, memory_format=torch.channels_last_3d if ctx.cl else torch.contiguous_format)
+        a = _abi.TvLossArgs()
+        a.v, a.C, a.X, a.Y, a.Z, a.channel_last, a.mode = ptr(v), v.size(1), X, Y, Z, int(ctx.cl), ctx.mode
+        a.mask, a.axis_scale = ptr(mask_u8), ptr(scale)
+        g = g.reshape(1).float().contiguous()
+        _abi._declare()
+        _native.check(_native.load().vx_tv_loss_backward(ctypes.byref(a), ptr(g), ptr(d), stream_ptr()),
+                      "vx_tv_loss_backward")
+        return d, None, None, None
+
+
+def voxel_mask_u8(mask, shape) -> torch.Tensor | None:
+    """[X, Y, Z] uint8 copy of a [1, 1, X, Y, Z] (or [X, Y, Z]) bool mask; None
+    stays None (every voxel)."""
+    if mask is None:
+        return None
+    m = mask.detach().reshape(mask.shape[-3:])
+    if tuple(m.shape) != tuple(shape):
+        raise ValueError(f"mask of shape {tuple(m.shape)} on a grid of shape {tuple(shape)}")
+    return m.to(torch.uint8).contiguous()
+
+
+def total_variation(v: torch.Tensor, mask=None, mode: int = 1, weight: float = 1.0) -> torch.Tensor:
+    """weight x total_variation(v, mask) of the model files, on the library's
+    kernels (vx_tv_loss): v [1, C, X, Y, Z] (either memory layout), mask the
+    [1, 1, X, Y, Z] voxel mask (the reference's ``mask.repeat(1, C, ...)``
+    is implied) or None.  mode 1: the mean of each axis's selected |diff|,
+    averaged over the axes (lib/voxurf_fine.py:956-969 and the maskless
+    models); mode 0: their sum over 3 x the mask's entries
+    (lib/voxurf_coarse.py:702-715).  Differentiable in v."""
+    if v.dim() != 5 or v.size(0) != 1:
+        raise ValueError("v must be [1, C, X, Y, Z]")
+    m = voxel_mask_u8(mask, v.shape[-3:]).to(v.device) if mask is not None else None
+    return _TVLoss.apply(v, m, int(mode), float(weight))
 
 
 class DenseGrid(nn.Module):

@@ -26,7 +26,7 @@ from ._torch import ptr, stream_ptr
 from .mlp import apply_mlp, row_stride
 from .voxurf_fine import FineFrame, gaussian_taps, marching_cubes, max_steps_bound, smooth_grid, smooth_grid_adjoint
 from .voxurf_fine import extract_fields as _extract_fields
-from .voxurf_fine import query_mask
+from .voxurf_fine import _SmoothGradTV, query_mask, tv_mask
 
 
 def sdf_gradient_grid(sdf: torch.Tensor, voxel_size: float) -> torch.Tensor:
@@ -342,6 +342,38 @@ class Voxurf(nn.Module):
     def k0_total_variation_add_grad(self, weight, dense_mode):
         w = weight * self.world_size.max() / 128
         self.k0.total_variation_add_grad(w, w, w, dense_mode)
+
+    def _tv_nonempty(self):
+        if self.nonempty_mask is None:
+            # voxurf_coarse.py:303-306 index self.nonempty_mask, which only a
+            # mask cache sets
+            raise ValueError("the coarse model's TV losses need the non-empty mask of a mask cache")
+        return self.nonempty_mask
+
+    def density_total_variation(self, sdf_tv=0, smooth_grad_tv=0, sdf_thrd=0.999):
+        """voxurf_coarse.py:300-308, the ori_tv loss terms of the coarse
+        stage (run.py:617-626): sdf_tv x total_variation(sdf.grid,
+        nonempty_mask) / 2 / voxel_size in the coarse file's sum form, and
+        smooth_grad_tv on the raw SDF's gradient grid (:534)."""
+        mask = self._tv_nonempty()
+        tv = 0
+        if sdf_tv > 0:
+            tv = tv + grid_mod.total_variation(self.sdf.grid, mask, mode=0,
+                                               weight=float(sdf_tv / 2 / self.voxel_size.float()))
+        if smooth_grad_tv > 0:
+            u8, count = tv_mask(self, mask, self.sdf.grid)
+            tv = tv + _SmoothGradTV.apply(self.sdf.grid, u8, float(self.voxel_size), count) * smooth_grad_tv
+        return tv
+
+    def k0_total_variation(self, k0_tv=1., k0_grad_tv=0.):
+        """voxurf_coarse.py:310-320: the sum form over the non-empty mask
+        repeated on the 12 channels."""
+        if k0_grad_tv > 0:
+            raise NotImplementedError
+        tv = 0
+        if k0_tv > 0:
+            tv = tv + grid_mod.total_variation(self.k0.grid, self._tv_nonempty(), mode=0)
+        return tv
 
     def march_frame(self, rays_o, rays_d, viewdirs, inv_s: float, render_kwargs) -> FineFrame:
         """The per-forward state of _CoarseGeometry: rays, sampling, grid

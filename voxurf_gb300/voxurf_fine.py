@@ -356,6 +356,23 @@ class _SmoothGradTV(torch.autograd.Function):
         return d_sdf, None, None, None
 
 
+def tv_mask(owner, mask, grid):
+    """(uint8 [X, Y, Z] copy of a bool voxel mask on the grid's device, or
+    None; its voxel count), cached on ``owner`` while the mask tensor is
+    unchanged (one host read of the count per new mask)."""
+    X, Y, Z = (int(v) for v in grid.shape[-3:])
+    if mask is None:
+        return None, X * Y * Z
+    key = (mask.data_ptr(), mask.numel(), mask._version, str(grid.device))
+    cache = owner.__dict__.setdefault("_tv_mask_cache", {})
+    hit = cache.get(key)
+    if hit is None:
+        cache.clear()
+        u8 = grid_mod.voxel_mask_u8(mask, (X, Y, Z)).to(grid.device)
+        hit = cache[key] = (u8, int(u8.sum().item()))
+    return hit
+
+
 def _abi_scratch_bytes(X, Y, Z) -> int:
     _abi._declare()
     return int(_native.load().vx_smooth_grad_tv_scratch_bytes(X, Y, Z))
@@ -567,23 +584,31 @@ class Voxurf(nn.Module):
         return marching_cubes(u, threshold, bound_min, bound_max, resolution)
 
     def density_total_variation(self, sdf_tv=0, smooth_grad_tv=0, grad_tv=0, smooth_sdf_tv=0):
-        """voxurf_fine.py:412-421.  smooth_grad_tv runs on the sm_103a kernels;
-        the masked-mean |diff| sdf_tv form (used only with ori_tv, never by
-        the fine configs) is not built.  Without a mask cache the reference
-        fails (nonempty_mask is None); here every voxel counts."""
-        if sdf_tv > 0:
-            raise NotImplementedError("sdf_tv (the ori_tv loss form) is not built; use sdf_total_variation_add_grad")
+        """voxurf_fine.py:412-421: sdf_tv = total_variation(sdf.grid,
+        nonempty_mask) / 2 / voxel_size (the per-axis mean form) and
+        smooth_grad_tv on the raw SDF's gradient grid, both on the sm_103a
+        kernels.  Without a mask cache the reference's smooth_grad_tv fails
+        (nonempty_mask is None); here every voxel counts."""
+        if grad_tv > 0 or smooth_sdf_tv > 0:
+            raise NotImplementedError("grad_tv / smooth_sdf_tv are accepted but unused by the reference")
         tv = 0
+        if sdf_tv > 0:
+            tv = tv + grid_mod.total_variation(self.sdf.grid, self.nonempty_mask, mode=1,
+                                               weight=float(sdf_tv / 2 / self.voxel_size.float()))
         if smooth_grad_tv > 0:
-            nm = self.nonempty_mask
-            key = None if nm is None else (nm.data_ptr(), nm.numel())
-            if getattr(self, "_nonempty_key", "unset") != key:
-                self._nonempty_u8 = None if nm is None else nm.reshape(nm.shape[-3:]).to(torch.uint8).contiguous()
-                ws = self.sdf.grid.shape[-3:]
-                self._nonempty_count = int(ws[0] * ws[1] * ws[2]) if nm is None else int(nm.sum().item())
-                self._nonempty_key = key
-            tv = tv + _SmoothGradTV.apply(self.sdf.grid, self._nonempty_u8, float(self.voxel_size),
-                                          self._nonempty_count) * smooth_grad_tv
+            u8, count = tv_mask(self, self.nonempty_mask, self.sdf.grid)
+            tv = tv + _SmoothGradTV.apply(self.sdf.grid, u8, float(self.voxel_size), count) * smooth_grad_tv
+        return tv
+
+    def k0_total_variation(self, k0_tv=1., k0_grad_tv=0.):
+        """voxurf_fine.py:423-432 (which passes the DenseGrid module itself to
+        total_variation; the grid is meant): the per-axis mean form over the
+        non-empty mask."""
+        if k0_grad_tv > 0:
+            raise NotImplementedError
+        tv = 0
+        if k0_tv > 0:
+            tv = tv + grid_mod.total_variation(self.k0.grid, self.nonempty_mask, mode=1)
         return tv
 
     def k0_total_variation_add_grad(self, weight, dense_mode):

@@ -42,7 +42,7 @@ from . import grid as grid_mod
 from ._torch import ptr, stream_ptr
 from .background import background_samples, n_samples_for
 from .mlp import apply_mlp, row_stride
-from .voxurf_fine import Voxurf, _feature_cfg, _mlp, smooth_grid, smooth_grid_adjoint
+from .voxurf_fine import Voxurf, _SmoothGradTV, _feature_cfg, _mlp, smooth_grid, smooth_grid_adjoint, tv_mask
 
 # global steps at which the forward resets the SDF outside the unit sphere
 # (voxurf_womask_fine.py:836-838)
@@ -269,7 +269,73 @@ def _ray_offsets(ray_id: torch.Tensor, n_rays: int) -> torch.Tensor:
     return off
 
 
-class VoxurfWomask(Voxurf):
+class MasklessTV:
+    """The regularisers of the maskless models (voxurf_womask_fine.py:484-548,
+    voxurf_womask_coarse.py:398-440), mixed into both.  The TV mask is the
+    non-empty mask, else the unit-sphere mask; with tv_in_sphere False the
+    reference sets that mask to all ones in place (every voxel counts).  The
+    smooth_grad_tv term takes the gradient grid of the smoothed SDF, as the
+    forward does (self.gradient at voxurf_womask_fine.py:878,
+    voxurf_womask_coarse.py:657); the smoothing is recomputed here, inside
+    the same autograd graph as the loss."""
+
+    def _sphere_mask_now(self):
+        if self.sphere_mask is None:
+            g = self.sdf.grid
+            lo, hi = self.xyz_min.float(), self.xyz_max.float()
+            axes = [torch.linspace(lo[a], hi[a], g.shape[2 + a], device=g.device) for a in range(3)]
+            xs, ys, zs = torch.meshgrid(*axes, indexing="ij")
+            return ((xs ** 2 + ys ** 2 + zs ** 2) < 1.0)[None, None]
+        return self.sphere_mask
+
+    def _tv_region(self):
+        if not self.tv_in_sphere:
+            return None
+        return self.nonempty_mask if self.nonempty_mask is not None else self._sphere_mask_now()
+
+    def density_total_variation(self, sdf_tv=0, smooth_grad_tv=0, bg_density_tv=0.):
+        mask = self._tv_region()
+        inv2vs = 1.0 / 2.0 / float(self.voxel_size.float())
+        tv = 0
+        if sdf_tv > 0:
+            tv = tv + grid_mod.total_variation(self.sdf.grid, mask, mode=1, weight=inv2vs * sdf_tv)
+        if smooth_grad_tv > 0:
+            taps = self.smooth_taps if self.smooth_sdf else None
+            u8, count = tv_mask(self, mask, self.sdf.grid)
+            sdf_s = _Smooth.apply(self.sdf.grid, taps)
+            tv = tv + _SmoothGradTV.apply(sdf_s, u8, float(self.voxel_size), count) * smooth_grad_tv
+        if bg_density_tv > 0:
+            # voxurf_womask_coarse.py:414 passes the DenseGrid module itself;
+            # its grid is meant (as voxurf_womask_fine.py:514)
+            tv = tv + grid_mod.total_variation(self.bg_density.grid, None, mode=1, weight=inv2vs * bg_density_tv)
+        return tv
+
+    def k0_total_variation(self, k0_tv=1., k0_grad_tv=0.):
+        if k0_grad_tv > 0:
+            raise NotImplementedError
+        tv = 0
+        if k0_tv > 0:
+            tv = tv + grid_mod.total_variation(self.k0.grid, self._tv_region(), mode=1)
+        return tv
+
+    def bg_k0_total_variation(self, bg_k0_tv=1., bg_k0_grad_tv=0.):
+        if bg_k0_grad_tv > 0:
+            raise NotImplementedError
+        tv = 0
+        if bg_k0_tv > 0 and self.bg_k0 is not None and self.bg_k0_dim > 0:
+            tv = tv + grid_mod.total_variation(self.bg_k0.grid, self._tv_region(), mode=1)
+        return tv
+
+    def bg_density_total_variation_add_grad(self, weight, dense_mode):
+        w = weight * self.world_size.max() / 128
+        self.bg_density.total_variation_add_grad(w, w, w, dense_mode)
+
+    def bg_k0_total_variation_add_grad(self, weight, dense_mode):
+        w = weight * self.world_size.max() / 128
+        self.bg_k0.total_variation_add_grad(w, w, w, dense_mode)
+
+
+class VoxurfWomask(MasklessTV, Voxurf):
     """lib/voxurf_womask_fine.py:31-303 (constructor) and :833-1071 (forward)."""
 
     def __init__(self, xyz_min, xyz_max, num_voxels=0, num_voxels_bg=0, num_voxels_base=0, alpha_init=None,

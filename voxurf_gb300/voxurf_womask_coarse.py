@@ -41,12 +41,13 @@ from . import grid as grid_mod
 from .background import background_samples, n_samples_for
 from .mlp import apply_mlp, row_stride
 from .voxurf_coarse import Voxurf, _CoarseGeometry
-from .voxurf_womask import SPHERE_STEPS, _Alpha2Weight, _BgAlpha, _BgFeatures, _ray_offsets, _WomaskComposite
+from .voxurf_womask import (SPHERE_STEPS, MasklessTV, _Alpha2Weight, _BgAlpha, _BgFeatures, _ray_offsets,
+                            _WomaskComposite)
 from . import _abi
 from ._torch import ptr, stream_ptr
 
 
-class VoxurfWomaskCoarse(Voxurf):
+class VoxurfWomaskCoarse(MasklessTV, Voxurf):
     """lib/voxurf_womask_coarse.py:35-224 (constructor) and :611-780 (forward)."""
 
     def __init__(self, xyz_min, xyz_max, num_voxels=0, num_voxels_bg=0, num_voxels_base=0, alpha_init=None,
