@@ -344,9 +344,10 @@ def run_ours(args, world, rank, local):
     eikonal = None
     if not args.no_eikonal and R == 256:
         eikonal = run_eikonal(args, dev)
-    womask = None
+    womask = womask_coarse = None
     if not args.no_womask and R == 256:
         womask = run_womask(args, dev)
+        womask_coarse = run_womask_coarse(args, dev)
     mesh = None
     if not args.no_mesh and R == 256:
         mesh = run_mesh_query(args, dev)
@@ -371,6 +372,7 @@ def run_ours(args, world, rank, local):
             "long_rays": long_rays,
             "eikonal_train": eikonal,
             "womask_train": womask,
+            "womask_coarse_train": womask_coarse,
             "mesh_query": mesh,
             "background_samples": bg_samples,
             "roofline": roofline,
@@ -714,6 +716,53 @@ def run_womask(args, dev):
     for precision in ("fp32", "bf16"):
         model = configs.build_womask_model(WM_R, precision, device=dev, seed=0, width=192)
         tr = FineTrainer(model, n_rays=N_RAYS)
+        for i in range(W):
+            loss, ret = tr.step(b[0][i], b[1][i], b[2][i], b[3][i], rk, global_step=i + 2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(W, W + S):
+            loss, ret = tr.step(b[0][i], b[1][i], b[2][i], b[3][i], rk, global_step=i + 2)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / S
+        out[precision] = {"ms_per_step": ms, "rays_per_s": N_RAYS / (ms / 1000.0),
+                          "fg_rows_last_step": int(ret["weights"].numel()),
+                          "bg_rows_last_step": int(ret["bg_weights"].numel()), "loss": float(loss)}
+        del tr, model, ret
+        torch.cuda.empty_cache()
+    out["speedup_bf16_vs_fp32"] = out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"]
+    return out
+
+
+WC_R = 96
+
+
+def run_womask_coarse(args, dev):
+    """Maskless coarse model with the dtu_e2e_womask coarse settings: SDF +
+    k0 96^3, bg_density 96^3, rgbnet 75 -> 128 -> 3, bg_rgbnet 60 -> 128 x3
+    -> 3, 8192 rays per step; full steps (forward, loss, the ori_tv loss
+    terms: 0.01 x (sdf_tv 0.1 + smooth_grad_tv 0.05) + 0.01 x k0 TV,
+    backward, Adam with the config's learning rates) through the autograd
+    path: FP32 and BF16."""
+    import numpy as np
+    import torch
+
+    from voxurf_gb300 import configs, synthetic
+    from voxurf_gb300.train import FineTrainer
+
+    rk = dict(configs.COARSE_RENDER_KWARGS)
+    W, S = 3, 10
+    o, d, v = synthetic.random_rays(N_RAYS * (W + S), seed=23)
+    t = configs.train_targets(N_RAYS * (W + S), 23)
+    b = [torch.from_numpy(np.ascontiguousarray(a.reshape(W + S, N_RAYS, 3))).to(dev) for a in (o, d, v, t)]
+    out = {"workload": f"womask coarse: SDF/k0 {WC_R}^3, bg_density {WC_R}^3, rgbnet 75->128->3, "
+                       f"bg_rgbnet 60->128x3->3, {N_RAYS} rays/step, ori_tv loss terms, sphere r=0.5 foreground"}
+    for precision in ("fp32", "bf16"):
+        model = configs.build_womask_coarse_model(WC_R, precision, device=dev, seed=0, width=128)
+        tr = FineTrainer(model, lr_sdf=0.1, lr_k0=0.1, lr_rgbnet=1e-3, lr_bg=0.1, n_rays=N_RAYS,
+                         loss_weights=(1.0, 0.0, 0.0), weight_tv_density=0.01, smooth_grad_tv=0.05, ori_tv=True,
+                         sdf_tv=0.1, weight_tv_k0=0.01)
         for i in range(W):
             loss, ret = tr.step(b[0][i], b[1][i], b[2][i], b[3][i], rk, global_step=i + 2)
         torch.cuda.synchronize()

@@ -118,3 +118,24 @@ def test_womask_coarse_render_without_training(cuda):
     dep = torch.zeros(n, dtype=torch.float64, device=cuda).index_add_(
         0, fr.ray2.long(), w * fr.step2.double() * fr.dist)
     assert torch.allclose(ret["depth"].double(), dep, atol=1e-5)
+
+
+def test_womask_coarse_trains_with_the_ori_tv_terms(cuda):
+    """FineTrainer with the coarse configuration's loss-form TV terms: a few
+    steps on one batch lower the loss; every trained group moves."""
+    from voxurf_gb300 import synthetic
+    from voxurf_gb300.train import FineTrainer
+
+    model = configs.build_womask_coarse_model(24, "fp32", device=cuda, seed=1, width=32)
+    tr = FineTrainer(model, lr_sdf=0.01, lr_k0=0.05, lr_rgbnet=1e-2, lr_bg=0.05, n_rays=1024,
+                     loss_weights=(1.0, 0.0, 0.0), weight_tv_density=0.01, smooth_grad_tv=0.05, ori_tv=True,
+                     sdf_tv=0.1, weight_tv_k0=0.01)
+    o, d, v = (torch.from_numpy(a).to(cuda) for a in synthetic.random_rays(1024, seed=5))
+    t = torch.from_numpy(configs.train_targets(1024, 5)).to(cuda)
+    before = {n: p.detach().clone() for n, p in model.named_parameters()}
+    rk = dict(configs.COARSE_RENDER_KWARGS)
+    losses = [float(tr.step(o, d, v, t, rk, global_step=i + 2)[0]) for i in range(8)]
+    assert all(np.isfinite(losses)) and losses[-1] < losses[0], losses
+    moved = [n for n, p in model.named_parameters() if p.numel() and not torch.equal(before[n], p.detach())]
+    for n in ("sdf.grid", "k0.grid", "bg_density.grid", "rgbnet.0.weight", "bg_rgbnet.0.weight"):
+        assert n in moved, (n, moved)

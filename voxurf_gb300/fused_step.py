@@ -51,8 +51,9 @@ def _round_up(x: int, m: int) -> int:
 class GraphedFineStep:
     def __init__(self, trainer, render_kwargs: dict, bucket_rows: int = 8192, use_graphs: bool = True):
         model = trainer.model
-        if trainer.weight_eikonal > 0 or (trainer.weight_tv_density > 0 and trainer.smooth_grad_tv > 0):
-            raise NotImplementedError("graphed step: eikonal / smooth_grad_tv terms run on the eager path")
+        if trainer.weight_eikonal > 0 or (trainer.weight_tv_density > 0 and (trainer.smooth_grad_tv > 0
+                                                                               or trainer.ori_tv)):
+            raise NotImplementedError("graphed step: eikonal / smooth_grad_tv / ori_tv terms run on the eager path")
         if not model.use_rgb_k:
             raise NotImplementedError("graphed step: the k-branch configuration (use_rgb_k) only")
         self.tr, self.model, self.rk = trainer, model, dict(render_kwargs)

@@ -44,11 +44,15 @@ class FineTrainer:
     bg_density / bg_k0 / bg_rgbnet); tv_sdf / tv_k0 are the weights
     given to *_total_variation_add_grad before the division by the batch
     size (run.py:647-655); tv_dense mirrors `global_step < tv_dense_before`.
+    ori_tv=True takes the TV terms as losses instead (run.py:617-626, the
+    coarse configs): weight_tv_density x density_total_variation(sdf_tv)
+    and weight_tv_k0 x k0_total_variation(), with no add-grad sweeps.
     """
 
     def __init__(self, model, lr_sdf=1e-3, lr_k0=1e-3, lr_rgbnet=1e-3, lr_k_rgbnet=1e-3, tv_sdf=1e-4, tv_k0=1e-4,
                  tv_dense=True, n_rays=8192, loss_weights=(1.0, 0.001, 0.5), weight_tv_density=0.0,
-                 smooth_grad_tv=0.0, weight_eikonal=0.0, graphed=False, lr_bg=1e-3):
+                 smooth_grad_tv=0.0, weight_eikonal=0.0, graphed=False, lr_bg=1e-3, ori_tv=False, sdf_tv=0.0,
+                 weight_tv_k0=0.0):
         self.model = model
         self.n_rays = n_rays
         # graphed=True: steps replay CUDA graphs on static buffers
@@ -57,6 +61,9 @@ class FineTrainer:
         self._engine = None
         # run.py:617-622: loss += weight_tv_density * density_total_variation(smooth_grad_tv=...)
         self.weight_tv_density, self.smooth_grad_tv = weight_tv_density, smooth_grad_tv
+        self.ori_tv, self.sdf_tv, self.weight_tv_k0 = bool(ori_tv), sdf_tv, weight_tv_k0
+        if self.ori_tv:   # run.py:642: the add-grad sweeps run only without ori_tv
+            tv_sdf = tv_k0 = 0.0
         # eikonal term mean((|grad| - 1)^2) on the shaded samples' FD gradient
         # (no counterpart in the reference loss; used by the differentiation workload)
         self.weight_eikonal = weight_eikonal
@@ -77,7 +84,7 @@ class FineTrainer:
         # create_optimizer_or_freeze_model: bg_density, bg_k0, bg_rgbnet)
         for name in ("bg_density", "bg_k0"):
             g = getattr(model, name, None)
-            if g is not None:
+            if g is not None and g.grid.numel() > 0:
                 groups.append({"params": [g.grid], "lr": lr_bg, "name": name})
         if getattr(model, "bg_rgbnet", None) is not None:
             groups.append({"params": list(model.bg_rgbnet.parameters()), "lr": lr_bg, "name": "bg_rgbnet"})
@@ -104,6 +111,11 @@ class FineTrainer:
         if self.weight_tv_density > 0 and self.smooth_grad_tv > 0:
             loss = loss + self.weight_tv_density * self.model.density_total_variation(
                 smooth_grad_tv=self.smooth_grad_tv)
+        if self.weight_tv_density > 0 and self.ori_tv:
+            if self.sdf_tv > 0:
+                loss = loss + self.weight_tv_density * self.model.density_total_variation(sdf_tv=self.sdf_tv)
+            if self.weight_tv_k0 > 0:
+                loss = loss + self.weight_tv_k0 * self.model.k0_total_variation()
         if self.weight_eikonal > 0 and ret["gradient"].numel() > 0:
             loss = loss + self.weight_eikonal * eikonal_loss(ret["gradient"])
         loss.backward()
