@@ -88,6 +88,8 @@ def parse():
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
     p.add_argument("--render-grid", type=int, default=256, help="scene grid size (256 is the benchmark)")
     p.add_argument("--render-tick", type=int, default=1 << 20, help="rays packed per tick")
+    p.add_argument("--render-staging", type=int, default=0, choices=[-1, 0, 1],
+                   help="row assembly of the features kernel (serve.RenderServer staging)")
     p.add_argument("--grid", type=int, default=256, help="grid resolution (256 is the benchmark; smaller sizes "
                                                          "serve profiler captures)")
     args = p.parse_args()
@@ -505,8 +507,9 @@ def run_micro(args, dev):
     launches first): `smooth` = vx_smooth3d / vx_smooth3d_adjoint (5^3,
     sigma 0.8) on a --grid^3 FP32 grid, 8 algorithmic bytes per voxel (12
     with accumulation); `mlp_tc` = the fused tcgen05 colour MLP
-    (70(80) -> 192 x3 -> 3, BF16 rows) against torch's BF16 GEMMs (its
-    cuBLAS) with the head kernel, at 131,072 and 2,097,152 rows."""
+    (70(80) -> 192 x3 -> 3, BF16 rows; one and two tiles in flight per CTA)
+    against torch's BF16 GEMMs (its cuBLAS) with the head kernel, at 131,072
+    and 2,097,152 rows."""
     import numpy as np
     import torch
     import torch.nn as nn
@@ -572,7 +575,8 @@ def run_micro(args, dev):
 
         flops = n * 2 * (80 * 192 + 2 * 192 * 192 + 3 * 192)
         row = {}
-        for name, fn in (("gemm", gemm), ("tc", lambda: tc.forward(X, res))):
+        for name, fn in (("gemm", gemm), ("tc_one_tile", lambda: tc.forward(X, res, pipeline=0)),
+                         ("tc", lambda: tc.forward(X, res, pipeline=1))):
             ms = _event_ms(fn, W, S)
             row[name] = {"ms": ms, "tflops": flops / ms / 1e9}
         out[f"rows_{n}"] = row
@@ -807,7 +811,8 @@ def run_render(args, dev):
         m.s_val = torch.ones(1) * s_val
         m.precision = "fp32"   # the plain render path
         m._k0_shadow = None
-    server = serve.RenderServer(scenes, tick_rays=args.render_tick, arena_pixels=32 << 20)
+    server = serve.RenderServer(scenes, tick_rays=args.render_tick, arena_pixels=32 << 20,
+                                staging=args.render_staging)
     torch.cuda.synchronize()
     serve.run_stream(server, serve.request_stream(6, float("inf"), RENDER_SCENES, seed=99))  # warm-up
     n = args.render_requests

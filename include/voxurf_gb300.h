@@ -653,6 +653,9 @@ typedef struct {
   float* out;               /* [n_rows,3] logits                                    */
   void* cols;               /* optional: the logits also stored as BF16 at cols[row*ld_cols + 0..2] */
   int64_t ld_cols;
+  int32_t pipeline;         /* 0: one 128-row tile in flight per CTA; 1: two (the MMAs of one tile
+                               run while the other's accumulator is converted; same results) */
+  int32_t reserved0;
 } vx_mlp_tc_args;
 
 /* out = Wh relu(W2 relu(W1 relu(W0 x + b0) + b1) + b2) + bh (+ add) for every
@@ -917,17 +920,28 @@ int vx_serve_march(const vx_scene_desc* scenes_host, int32_t n_scenes, const flo
                    const float* viewdirs, const int32_t* ray_scene, int64_t n_rays, int64_t max_steps, void* rec,
                    int32_t* n2, float* alphainv_last, void* stream);
 
-/* ray2[s2_off[r] + j] = r for j < s2_off[r+1] - s2_off[r]. */
-int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, void* stream);
+/* ray2[s2_off[r] + j] = r for j < s2_off[r+1] - s2_off[r]; rows at or
+ * beyond `capacity` are skipped (the caller compares s2_off[n_rays] with its
+ * capacity). */
+int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, int64_t capacity, void* stream);
 
 /* MLP input rows of the shaded samples (the column layout of
  * vx_fine_features; every scene of one call shares cfg).  Row strides:
  * ld1 >= the rgbnet columns, ld2 >= the k_rgbnet columns + 3, the last 3
- * being the rgbnet logits that vx_mlp_head writes. */
+ * being the rgbnet logits that vx_mlp_head writes.  n_rows is the row
+ * count, or with n_rows_dev != NULL the capacity of X1 / X2 / ray2: the
+ * rows then are min(*n_rows_dev, n_rows) (a device count, so the launch
+ * needs no host read; rows beyond the capacity are skipped and the caller
+ * compares).  staging: 1 assembles each CTA's rows in shared memory and
+ * writes them out coalesced (38 KB per CTA at the fine layout), 0 stores
+ * from each row's thread (no dynamic shared memory, so CTAs fit beside a
+ * kernel that holds most of an SM's shared memory), -1 chooses 1 where it
+ * fits the default 48 KB. */
 int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const vx_fine_feature_cfg* cfg,
                       const float* rays_o, const float* rays_d, const float* viewdirs, const int32_t* ray_scene,
                       int64_t max_steps, const void* rec, const int64_t* s2_off, const int32_t* ray2, int64_t n_rows,
-                      int64_t ld1, int64_t ld2, void* X1, void* X2, int32_t out_bf16, void* stream);
+                      const int64_t* n_rows_dev, int64_t ld1, int64_t ld2, void* X1, void* X2, int32_t out_bf16,
+                      int32_t staging, void* stream);
 
 /* Output layer of a colour MLP (voxurf_fine.py:141-151): out[i,:] =
  * H[i,:width] W^T + b (+ add[i,:]) with FP32 accumulation; when cols is

@@ -72,3 +72,29 @@ def test_tc_mlp_rejects_unsupported(cuda):
     assert not TensorCoreMLP.supports(net, 112)
     with pytest.raises(ValueError):
         TensorCoreMLP(net, 112)
+
+
+@pytest.mark.parametrize("K0,ld", [(80, 80), (64, 72)])
+@pytest.mark.parametrize("n", [1, 128, 129, 383, 5000, 152 * 128 * 2 + 77, 152 * 128 * 5 + 1])
+def test_two_tiles_in_flight_is_bit_identical(cuda, K0, ld, n):
+    """pipeline 1 (two tiles in flight per CTA, a shared A operand) issues the
+    same MMAs and epilogue arithmetic as pipeline 0: identical logits,
+    residual sums and BF16 columns, for tile counts that leave a CTA's last
+    pair half empty and for every row past the end untouched."""
+    k_in = K0 - 10
+    net = _net(k_in, n + K0, cuda)
+    X = torch.zeros((n, ld), dtype=torch.bfloat16, device=cuda)
+    X[:, :k_in] = (torch.randn((n, k_in), device=cuda) * 0.7).to(torch.bfloat16)
+    add = torch.randn((n, 3), device=cuda)
+    mlp = TensorCoreMLP(net, K0)
+    res = []
+    for pipeline in (0, 1):
+        out = torch.full((n + 5, 3), float("nan"), device=cuda)
+        cols = torch.full((n, 8), -7.0, dtype=torch.bfloat16, device=cuda)
+        mlp.forward(X, out[:n], add=add, cols=cols, ld_cols=8, pipeline=pipeline)
+        torch.cuda.synchronize()
+        res.append((out, cols))
+    assert torch.equal(res[0][0][:n], res[1][0][:n])
+    assert torch.isnan(res[1][0][n:]).all()
+    assert torch.equal(res[0][1], res[1][1])
+    assert bool((res[1][1][:, 3:] == -7.0).all())

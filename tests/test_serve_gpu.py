@@ -164,3 +164,29 @@ def test_admission_waits_for_arena(cuda):
     for i, r in enumerate(reqs):
         rgb, _ = ref.render(0, _pose(30 + i), 40, 40)
         assert np.abs(r.rgb - rgb).max() <= 1e-6
+
+
+@pytest.mark.parametrize("staging", [0, 1])
+def test_row_capacity_growth_and_feature_staging(cuda, staging):
+    """A tick with more shaded rows than its slot holds grows the slot and
+    redoes the tick's rows and features (the row count is read on the
+    device, so the first pass skipped the rows beyond the capacity); both
+    row assemblies of the features kernel give the same images as a server
+    whose slots never overflow."""
+    models = _models(cuda, "bf16", n=2)   # BF16 rows: both assemblies apply
+    views = [(0, _pose(60), 40, 48), (1, _pose(61), 36, 36), (0, _pose(62), 20, 30)]
+    out = []
+    for rpr, stg in ((0.05, staging), (6.0, -1)):
+        srv = _server(cuda, models, "bf16", tick_rays=1500, staging=stg, rows_per_ray=rpr)
+        cap0 = [sl.rows_cap for sl in srv.slots]
+        reqs = [srv.submit(*v) for v in views]
+        srv.run_until_idle()
+        caps = [sl.rows_cap for sl in srv.slots]
+        out.append((srv.rows_shaded, [r.rgb for r in reqs], [r.depth for r in reqs], cap0, caps))
+    rows, rgbs, depths, cap0, caps = out[0]
+    assert rows == out[1][0] and rows > 0
+    assert any(c > c0 for c, c0 in zip(caps, cap0))   # the small slots grew
+    for a, b in zip(rgbs, out[1][1]):
+        assert np.abs(a - b).max() <= 1e-6
+    for a, b in zip(depths, out[1][2]):
+        assert np.abs(a - b).max() <= 1e-6

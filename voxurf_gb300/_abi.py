@@ -183,7 +183,7 @@ class MlpTcArgs(C.Structure):
     _fields_ = [
         ("X", P), ("ldx", I64), ("K0", I64), ("n_rows", I64), ("width", I64), ("W0p", P), ("W1p", P), ("W2p", P),
         ("b0", P), ("b1", P), ("b2", P), ("Whp", P), ("bh", P), ("add", P), ("out", P), ("cols", P),
-        ("ld_cols", I64),
+        ("ld_cols", I64), ("pipeline", I32), ("reserved0", I32),
     ]
 
 
@@ -288,10 +288,10 @@ _STRUCT_FNS = {
 _SERVE_SIGNATURES = {
     "vx_serve_rays": [P, I32, I64, P, P, P, P, P, P],
     "vx_serve_march": ["scenes", I32, P, P, P, P, I64, I64, P, P, P, P],
-    "vx_serve_rows": [P, I64, P, P],
+    "vx_serve_rows": [P, I64, P, I64, P],
     "vx_mask_occupancy": [P, I64, I64, I64, I32, P, P],
-    "vx_serve_features": ["scenes", I32, C.POINTER(FineFeatureCfg), P, P, P, P, I64, P, P, P, I64, I64, I64, P, P,
-                          I32, P],
+    "vx_serve_features": ["scenes", I32, C.POINTER(FineFeatureCfg), P, P, P, P, I64, P, P, P, I64, P, I64, I64, P,
+                          P, I32, I32, P],
     "vx_serve_composite": ["scenes", I32, P, I64, I64, P, P, P, P, P, P, P, P, P],
 }
 

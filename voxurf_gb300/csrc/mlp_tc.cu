@@ -516,6 +516,292 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(MlpTcParams P) {
   }
 }
 
+// ---- two tiles in flight ----------------------------------------------------
+// mlp_tc2_kernel keeps two 128-row tiles (slots 0 and 1) in flight so that
+// the MMAs of one run while the epilogue converts the other's accumulator.
+// Tensor memory (512 columns): one accumulator per slot (D0 = 0-191, D1 =
+// 192-383), ONE shared A operand (384-479) and an output-layer accumulator
+// per slot (480-495, 496-511).  Shared memory: the weights (as above) and an
+// input tile per slot (2 x 20 KB at K0 = 80).
+//
+// MMA order per pair of tiles: L0(0), L0(1) (A = the input tiles), then
+// L1(0), L1(1), L2(0), L2(1), H(0), H(1), each from the A operand, which the
+// epilogue fills in the same order: E0(0), E0(1), E1(0), E1(1), E2(0),
+// E2(1), where E_l(t) converts D_t after L_l(t) (+bias, ReLU, BF16, into
+// registers) and stores it into the A operand once the MMA that read the A
+// operand last has completed: E0(1) after L1(0), E1(0) after L1(1), E1(1)
+// after L2(0), E2(0) after L2(1), E2(1) after H(0), E0(0) after H(1) of the
+// previous pair (implied: L0(0) is issued after it and its commit covers
+// it).  So while L_l(t) runs, the epilogue converts the other slot's
+// accumulator.  The MMAs and the epilogue arithmetic are those of
+// mlp_tc_kernel in the same order (bit-identical results).  An odd tile
+// count gives the CTA's last pair an empty second tile (zero rows, no
+// output).
+__device__ __forceinline__ uint32_t tm2_d(int t) { return t ? 192u : 0u; }
+__device__ __forceinline__ uint32_t tm2_h(int t) { return t ? 496u : 480u; }
+constexpr uint32_t TM2_A = 384;
+
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// This thread's hidden columns [96 part, +96) of accumulator `dcol` (its
+// TMEM lane): +bias, ReLU, BF16 pairs -> pk (A operand columns [48 part, +48)).
+__device__ __forceinline__ void tc2_convert(uint32_t tmem_row, uint32_t dcol, const float* bl, int part,
+                                            uint32_t (&pk)[48]) {
+  uint32_t v[3][32];
+  tc_ld96(tmem_row + dcol + (uint32_t)(96 * part), v);
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 bq = *reinterpret_cast<const float4*>(bl + 96 * part + 32 * j + 4 * q);
+      const float h0 = fmaxf(__uint_as_float(v[j][4 * q + 0]) + bq.x, 0.f);
+      const float h1 = fmaxf(__uint_as_float(v[j][4 * q + 1]) + bq.y, 0.f);
+      const float h2 = fmaxf(__uint_as_float(v[j][4 * q + 2]) + bq.z, 0.f);
+      const float h3 = fmaxf(__uint_as_float(v[j][4 * q + 3]) + bq.w, 0.f);
+      pk[16 * j + 2 * q] = pack_bf16(h0, h1);
+      pk[16 * j + 2 * q + 1] = pack_bf16(h2, h3);
+    }
+}
+
+// pk -> A operand columns [48 part, +48) of this thread's lane, then the
+// hand-off to the MMA warp (one arrival per warp).
+__device__ __forceinline__ void tc2_store_a(uint32_t tmem_row, int part, const uint32_t (&pk)[48], uint64_t* bar_a,
+                                            int lane) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    uint32_t s16[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) s16[i] = pk[16 * j + i];
+    tc_st16(tmem_row + TM2_A + (uint32_t)(48 * part + 16 * j), s16);
+  }
+  tc_wait_st();
+  tc_fence_before();
+  __syncwarp();
+  if (lane == 0) mbar_arrive(bar_a);
+}
+
+// Output layer of one tile: hi + lo parts of each logit, + bias (+ residual).
+__device__ __forceinline__ void tc2_head(const MlpTcParams& P, uint32_t tmem_row, int t, int64_t row, float bh0,
+                                         float bh1, float bh2) {
+  uint32_t hv[16];
+  tc_ld16(tmem_row + tm2_h(t), hv);
+  if (row < P.n_rows) {
+    float a0 = (__uint_as_float(hv[0]) + __uint_as_float(hv[3])) + bh0;
+    float a1 = (__uint_as_float(hv[1]) + __uint_as_float(hv[4])) + bh1;
+    float a2 = (__uint_as_float(hv[2]) + __uint_as_float(hv[5])) + bh2;
+    if (P.add) {
+      a0 += P.add[3 * row + 0];
+      a1 += P.add[3 * row + 1];
+      a2 += P.add[3 * row + 2];
+    }
+    P.out[3 * row + 0] = a0;
+    P.out[3 * row + 1] = a1;
+    P.out[3 * row + 2] = a2;
+    if (P.cols) {
+      __nv_bfloat16* cp = P.cols + row * P.ld_cols;
+      cp[0] = __float2bfloat16_rn(a0);
+      cp[1] = __float2bfloat16_rn(a1);
+      cp[2] = __float2bfloat16_rn(a2);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc2_kernel(MlpTcParams P) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int K0 = P.K0;
+  __nv_bfloat16* W0s = reinterpret_cast<__nv_bfloat16*>(smem);
+  __nv_bfloat16* W1s = W0s + (size_t)K0 * TC_N;
+  __nv_bfloat16* W2s = W1s + (size_t)TC_N * TC_N;
+  __nv_bfloat16* Xs0 = W2s + (size_t)TC_N * TC_N;                   // [K0/8][128][8] slot 0 input tile
+  __nv_bfloat16* Xs1 = Xs0 + (size_t)K0 * TC_M;                     // slot 1
+  __nv_bfloat16* WHs = Xs1 + (size_t)K0 * TC_M;                     // [24][16][8] output layer
+  float* bias_s = reinterpret_cast<float*>(WHs + (size_t)TC_NH * TC_N);  // [3][192]
+  uint64_t* bar_w = reinterpret_cast<uint64_t*>(bias_s + 3 * TC_N);
+  uint64_t* bar_d = bar_w + 1;    // [2] accumulator of slot t complete
+  uint64_t* bar_h = bar_w + 3;    // [2] output layer of slot t complete
+  uint64_t* bar_x = bar_w + 5;    // [2] input tile of slot t in shared memory
+  uint64_t* bar_a = bar_w + 7;    // A operand filled
+  uint64_t* bar_fin = bar_w + 8;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_w + 9);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool mma_warp = warp == TC_EPI_WARPS;
+  const int quarter = warp & 3, part = (warp >> 2) & 1;  // TMEM lanes 32*quarter.., column half `part`
+  const int epi_threads = 32 * TC_EPI_WARPS;
+  const int64_t n_tiles = (P.n_rows + TC_M - 1) / TC_M;
+  const int64_t n_j = (int64_t)blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int64_t n_pairs = (n_j + 1) / 2;
+  const int64_t g = gridDim.x;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(bar_w, 1);
+    for (int t = 0; t < 2; ++t) {
+      mbar_init(bar_d + t, 1);
+      mbar_init(bar_h + t, 1);
+      mbar_init(bar_x + t, TC_EPI_WARPS);
+    }
+    mbar_init(bar_a, TC_EPI_WARPS);
+    mbar_init(bar_fin, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t w0b = (uint32_t)K0 * TC_N * 2, w1b = (uint32_t)TC_N * TC_N * 2, bb = TC_N * 4,
+                   whb = (uint32_t)TC_NH * TC_N * 2;
+    mbar_expect_tx(bar_w, w0b + 2 * w1b + whb + 3 * bb);
+    bulk_g2s(W0s, P.W0p, w0b, bar_w);
+    bulk_g2s(W1s, P.W1p, w1b, bar_w);
+    bulk_g2s(W2s, P.W2p, w1b, bar_w);
+    bulk_g2s(WHs, P.Whp, whb, bar_w);
+    bulk_g2s(bias_s, P.b0, bb, bar_w);
+    bulk_g2s(bias_s + TC_N, P.b1, bb, bar_w);
+    bulk_g2s(bias_s + 2 * TC_N, P.b2, bb, bar_w);
+  }
+  if (!mma_warp && n_pairs > 0) {
+    // the first pair's input tiles (a tile past the last one is all zero rows)
+    load_x_tile(P, Xs0, ((int64_t)blockIdx.x) * TC_M, tid, epi_threads);
+    load_x_tile(P, Xs1, ((int64_t)blockIdx.x + g) * TC_M, tid, epi_threads);
+    cp_async_wait_all();
+    fence_async_smem();
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(bar_x);
+      mbar_arrive(bar_x + 1);
+    }
+  }
+  bool ok = mbar_wait(bar_w, 0);
+  const float bh0 = __ldg(P.bh + 0), bh1 = __ldg(P.bh + 1), bh2 = __ldg(P.bh + 2);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tmem_row = tmem + ((uint32_t)(32 * quarter) << 16);
+  const uint32_t x_s0 = smem_u32(Xs0), x_s1 = smem_u32(Xs1);
+  const uint32_t w_s0 = smem_u32(W0s), w_s1 = smem_u32(W1s), w_s2 = smem_u32(W2s), wh_s = smem_u32(WHs);
+
+  if (mma_warp) {
+    uint32_t ph_a = 0;
+    for (int64_t p = 0; p < n_pairs && ok; ++p) {
+      for (int t = 0; t < 2 && ok; ++t) {
+        ok = mbar_wait(bar_x + t, (uint32_t)(p & 1));
+        tc_fence_after();
+        if (!ok) break;
+        if (lane == 0) tc_layer(tmem + tm2_d(t), t ? x_s1 : x_s0, w_s0, K0, bar_d + t);
+        __syncwarp();
+      }
+#pragma unroll 1
+      for (int step = 0; step < 6 && ok; ++step) {
+        const int t = step & 1, layer = 1 + (step >> 1);  // layer 3: the output layer
+        ok = mbar_wait(bar_a, ph_a);
+        ph_a ^= 1u;
+        tc_fence_after();
+        if (!ok) break;
+        if (lane == 0) {
+          if (layer < 3)
+            tc_layer_ta(tmem + tm2_d(t), tmem + TM2_A, layer == 1 ? w_s1 : w_s2, TC_N, TC_N, bar_d + t);
+          else
+            tc_layer_ta(tmem + tm2_h(t), tmem + TM2_A, wh_s, TC_NH, TC_N, bar_h + t);
+        }
+        __syncwarp();
+      }
+    }
+    // nothing of this CTA's may still be in flight when the tensor memory is
+    // released
+    if (lane == 0) {
+      tc_commit(bar_fin);
+      if (!mbar_wait(bar_fin, 0)) ok = false;
+    }
+    __syncwarp();
+  } else {
+    uint32_t pk[48];
+    for (int64_t p = 0; p < n_pairs && ok; ++p) {
+      const bool more = p + 1 < n_pairs;
+      const uint32_t d0 = (uint32_t)((3 * p) & 1), d1 = d0 ^ 1u, d2 = d0, hp = (uint32_t)(p & 1);
+      // E0(0): L0(0) done -> slot 0's input tile is free: prefetch the next one
+      ok = mbar_wait(bar_d, d0);
+      tc_fence_after();
+      if (!ok) break;
+      if (more) load_x_tile(P, Xs0, ((int64_t)blockIdx.x + (2 * p + 2) * g) * TC_M, tid, epi_threads);
+      tc2_convert(tmem_row, tm2_d(0), bias_s, part, pk);
+      tc2_store_a(tmem_row, part, pk, bar_a, lane);
+      // E0(1)
+      ok = mbar_wait(bar_d + 1, d0);
+      tc_fence_after();
+      if (!ok) break;
+      if (more) load_x_tile(P, Xs1, ((int64_t)blockIdx.x + (2 * p + 3) * g) * TC_M, tid, epi_threads);
+      tc2_convert(tmem_row, tm2_d(1), bias_s, part, pk);
+      ok = mbar_wait(bar_d, d1);  // L1(0) done: the A operand is free
+      tc_fence_after();
+      if (!ok) break;
+      tc2_store_a(tmem_row, part, pk, bar_a, lane);
+      // E1(0) (L1(0) done)
+      tc2_convert(tmem_row, tm2_d(0), bias_s + TC_N, part, pk);
+      ok = mbar_wait(bar_d + 1, d1);  // L1(1) done
+      tc_fence_after();
+      if (!ok) break;
+      tc2_store_a(tmem_row, part, pk, bar_a, lane);
+      // E1(1) (L1(1) done)
+      tc2_convert(tmem_row, tm2_d(1), bias_s + TC_N, part, pk);
+      ok = mbar_wait(bar_d, d2);  // L2(0) done
+      tc_fence_after();
+      if (!ok) break;
+      tc2_store_a(tmem_row, part, pk, bar_a, lane);
+      // E2(0) (L2(0) done)
+      tc2_convert(tmem_row, tm2_d(0), bias_s + 2 * TC_N, part, pk);
+      ok = mbar_wait(bar_d + 1, d2);  // L2(1) done
+      tc_fence_after();
+      if (!ok) break;
+      tc2_store_a(tmem_row, part, pk, bar_a, lane);
+      if (more) {
+        // slot 0's next input tile is in shared memory
+        cp_async_wait_one();
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_x);
+      }
+      // E2(1) (L2(1) done)
+      tc2_convert(tmem_row, tm2_d(1), bias_s + 2 * TC_N, part, pk);
+      ok = mbar_wait(bar_h, hp);  // H(0) done
+      tc_fence_after();
+      if (!ok) break;
+      tc2_store_a(tmem_row, part, pk, bar_a, lane);
+      if (more) {
+        cp_async_wait_all();
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_x + 1);
+      }
+      if (part == 0) {
+        const int64_t r0 = ((int64_t)blockIdx.x + 2 * p * g) * TC_M + 32 * quarter + lane;
+        tc2_head(P, tmem_row, 0, r0, bh0, bh1, bh2);
+        ok = mbar_wait(bar_h + 1, hp);
+        tc_fence_after();
+        if (!ok) break;
+        tc2_head(P, tmem_row, 1, r0 + g * TC_M, bh0, bh1, bh2);
+        tc_fence_before();
+      }
+    }
+    cp_async_wait_all();
+  }
+  if (!ok) set_device_error(P.err, VX_ERR_TIMEOUT);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
+static size_t mlp_tc2_smem_bytes(int K0) {
+  return (size_t)K0 * TC_N * 2 + 2 * (size_t)TC_N * TC_N * 2 + 2 * (size_t)K0 * TC_M * 2 +
+         (size_t)TC_NH * TC_N * 2 + 3 * TC_N * 4 + 9 * 8 + 8;
+}
+
 // [N, K] row-major FP32 weights -> [K/8][N][8] BF16 (K padded with zeros to Kp).
 __global__ void mlp_tc_pack_kernel(const float* __restrict__ W, int N, int K, int Kp, __nv_bfloat16* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -544,7 +830,7 @@ int vx_mlp_tc_pack(const float* W, int64_t N, int64_t K, int64_t Kp, void* out, 
 }
 
 int vx_mlp_tc_forward(const vx_mlp_tc_args* A, void* stream) {
-  if (!A || A->n_rows < 0) return VX_ERR_ARG;
+  if (!A || A->n_rows < 0 || (A->pipeline != 0 && A->pipeline != 1)) return VX_ERR_ARG;
   if (A->n_rows == 0) return VX_OK;
   if (A->width != TC_N || A->K0 < 16 || A->K0 > TC_KMAX0 || A->K0 % 16) return VX_ERR_UNSUPPORTED;
   if (!A->X || !A->W0p || !A->W1p || !A->W2p || !A->b0 || !A->b1 || !A->b2 || !A->Whp || !A->bh || !A->out)
@@ -573,10 +859,19 @@ int vx_mlp_tc_forward(const vx_mlp_tc_args* A, void* stream) {
   P.cols = reinterpret_cast<__nv_bfloat16*>(A->cols);
   P.ld_cols = A->ld_cols;
   P.err = device_error_ptr();
+  const int64_t tiles = (A->n_rows + TC_M - 1) / TC_M;
+  if (A->pipeline == 1) {
+    const size_t smem = mlp_tc2_smem_bytes(P.K0);
+    cudaError_t e = cudaFuncSetAttribute(mlp_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e);
+    const int64_t pairs = (tiles + 1) / 2;
+    const unsigned grid = (unsigned)(pairs < sm_count() ? pairs : sm_count());
+    mlp_tc2_kernel<<<grid, TC_THREADS, smem, as_stream(stream)>>>(P);
+    return launch_status();
+  }
   const size_t smem = mlp_tc_smem_bytes(P.K0);
   cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e);
-  const int64_t tiles = (A->n_rows + TC_M - 1) / TC_M;
   const unsigned grid = (unsigned)(tiles < sm_count() ? tiles : sm_count());
   mlp_tc_kernel<<<grid, TC_THREADS, smem, as_stream(stream)>>>(P);
   return launch_status();

@@ -310,10 +310,10 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
 
 // ---- row -> ray --------------------------------------------------------------
 __global__ void __launch_bounds__(256) serve_rows_kernel(const int64_t* __restrict__ s2_off, int n_rays,
-                                                         int* __restrict__ ray2) {
+                                                         int* __restrict__ ray2, int64_t capacity) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= n_rays) return;
-  const int64_t b = s2_off[r], e = s2_off[r + 1];
+  const int64_t b = s2_off[r], e = min(s2_off[r + 1], capacity);
   for (int64_t i = b + lane_id(); i < e; i += 32) ray2[i] = r;
 }
 
@@ -329,7 +329,8 @@ struct ServeFeatParams {
   const uint2* rec;
   const int64_t* s2_off;
   const int* ray2;
-  int64_t n_rows;
+  int64_t n_rows;              // rows, or the capacity with n_rows_dev
+  const int64_t* n_rows_dev;   // device row count or null
   int64_t ld1, ld2;
   int cols1, cols2;  // feature columns; X1 [cols1, ld1) and X2 [cols2 + 3, ld2) are zero-filled
   void* X1;
@@ -343,13 +344,15 @@ template <typename T, int KK, bool STAGE>
 __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
   extern __shared__ __align__(16) unsigned char feat_stage[];
-  load_scenes(P.T, sh);
+  const int64_t n_rows = P.n_rows_dev ? min(*P.n_rows_dev, P.n_rows) : P.n_rows;
   const int64_t row0 = (int64_t)blockIdx.x * blockDim.x;
+  if (row0 >= n_rows) return;  // uniform over the block
+  load_scenes(P.T, sh);
   const int64_t row = row0 + threadIdx.x;
   T* s1 = reinterpret_cast<T*>(feat_stage);
   const int64_t sl1 = stage_ld<T>(P.ld1), sl2 = stage_ld<T>(P.ld2);
   T* s2 = s1 + (int64_t)blockDim.x * sl1;
-  if (row < P.n_rows) {
+  if (row < n_rows) {
     const int r = P.ray2[row];
     const SceneK& S = sh[P.ray_scene[r]];  // validated by the march
     const int j = (int)(row - P.s2_off[r]);
@@ -373,7 +376,7 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
   }
   if (STAGE) {
     __syncthreads();
-    const int nv = (int)max((int64_t)0, min((int64_t)blockDim.x, P.n_rows - row0));
+    const int nv = (int)max((int64_t)0, min((int64_t)blockDim.x, n_rows - row0));
     copy_rows_out(s1, reinterpret_cast<T*>(P.X1) + row0 * P.ld1, nv, P.ld1);
     copy_rows_out(s2, reinterpret_cast<T*>(P.X2) + row0 * P.ld2, nv, P.ld2);
   }
@@ -650,19 +653,21 @@ int vx_mask_occupancy(const uint8_t* mask, int64_t mX, int64_t mY, int64_t mZ, i
   return launch_status();
 }
 
-int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, void* stream) {
-  if (n_rays < 0 || n_rays > INT32_MAX) return VX_ERR_ARG;
+int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, int64_t capacity, void* stream) {
+  if (n_rays < 0 || n_rays > INT32_MAX || capacity < 0) return VX_ERR_ARG;
   if (n_rays == 0) return VX_OK;
   if (!s2_off || !ray2) return VX_ERR_ARG;
-  serve_rows_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(s2_off, (int)n_rays, ray2);
+  serve_rows_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(s2_off, (int)n_rays, ray2, capacity);
   return launch_status();
 }
 
 int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const vx_fine_feature_cfg* cfg,
                       const float* rays_o, const float* rays_d, const float* viewdirs, const int32_t* ray_scene,
                       int64_t max_steps, const void* rec, const int64_t* s2_off, const int32_t* ray2, int64_t n_rows,
-                      int64_t ld1, int64_t ld2, void* X1, void* X2, int32_t out_bf16, void* stream) {
-  if (n_rows < 0 || !cfg || max_steps < 1 || max_steps > INT32_MAX) return VX_ERR_ARG;
+                      const int64_t* n_rows_dev, int64_t ld1, int64_t ld2, void* X1, void* X2, int32_t out_bf16,
+                      int32_t staging, void* stream) {
+  if (n_rows < 0 || !cfg || max_steps < 1 || max_steps > INT32_MAX || staging < -1 || staging > 1)
+    return VX_ERR_ARG;
   if (n_rows == 0) return VX_OK;
   ServeFeatParams P{};
   int s = scene_table(scenes_host, n_scenes, P.T);
@@ -680,6 +685,7 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
   P.s2_off = s2_off;
   P.ray2 = ray2;
   P.n_rows = n_rows;
+  P.n_rows_dev = n_rows_dev;
   P.ld1 = ld1;
   P.ld2 = ld2;
   P.cols1 = (int)x1_cols(cfg);
@@ -692,9 +698,11 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
   // shared memory within the default 48 KB
   const size_t esz = out_bf16 ? 2 : 4;
   const size_t shm = 128 * (size_t)(ld1 + ld2 + 2 * (4 / esz)) * esz;
-  const bool stage = ((size_t)ld1 * esz) % 4 == 0 && ((size_t)ld2 * esz) % 4 == 0 &&
-                     shm + sizeof(SceneK) * VX_SERVE_MAX_SCENES <= 48 * 1024 &&
-                     ((reinterpret_cast<uintptr_t>(X1) | reinterpret_cast<uintptr_t>(X2)) & 3) == 0;
+  const bool stage_ok = ((size_t)ld1 * esz) % 4 == 0 && ((size_t)ld2 * esz) % 4 == 0 &&
+                        shm + sizeof(SceneK) * VX_SERVE_MAX_SCENES <= 48 * 1024 &&
+                        ((reinterpret_cast<uintptr_t>(X1) | reinterpret_cast<uintptr_t>(X2)) & 3) == 0;
+  if (staging == 1 && !stage_ok) return VX_ERR_UNSUPPORTED;
+  const bool stage = staging != 0 && stage_ok;
 #define VX_FEAT_LAUNCH(T, KK)                                    \
   if (stage)                                                     \
     serve_features_kernel<T, KK, true><<<b, 128, shm, st>>>(P);  \

@@ -259,6 +259,7 @@ class TensorCoreMLP:
     tensor-core tile.  Inference only (no autograd)."""
 
     WIDTH = 192
+    pipeline = 1   # two 128-row tiles in flight per CTA (vx_mlp_tc_args.pipeline)
 
     @staticmethod
     def supports(net: nn.Sequential, K0: int) -> bool:
@@ -295,11 +296,14 @@ class TensorCoreMLP:
         self.bh = lin[3].bias.detach().float().contiguous()
 
     def forward(self, X: torch.Tensor, out: torch.Tensor, add: torch.Tensor | None = None,
-                cols: torch.Tensor | None = None, ld_cols: int = 0) -> None:
-        """out[i] = MLP(X[i, :K0]) (+ add[i]); X [n, ldx] BF16 rows, out [n,3] FP32."""
+                cols: torch.Tensor | None = None, ld_cols: int = 0, pipeline: int | None = None) -> None:
+        """out[i] = MLP(X[i, :K0]) (+ add[i]); X [n, ldx] BF16 rows, out [n,3] FP32.
+        pipeline: tiles in flight per CTA minus one (0 or 1; default
+        self.pipeline); both give the same results."""
         from . import _abi
 
         a = _abi.MlpTcArgs()
+        a.pipeline = self.pipeline if pipeline is None else int(pipeline)
         a.X, a.ldx, a.K0, a.n_rows, a.width = ptr(X), X.stride(0), self.K0, X.shape[0], self.WIDTH
         a.W0p, a.W1p, a.W2p = (ptr(t) for t in self.packed)
         a.b0, a.b1, a.b2 = (ptr(t) for t in self.biases)

@@ -15,14 +15,17 @@ mask's block occupancy starts each ray's march at its first sample that can
 lie in the mask.  The composite writes straight into each request's range
 of an output arena.
 
-A tick has a front half (rays, march, row scan; on the front stream) and a
-back half (rows, features, MLPs, compositing; on the back stream), and the
-two halves of consecutive ticks overlap: the host launches the front half
-of tick t+1 and the back half of tick t before it waits for tick t+1's row
-counts (the tick's one host synchronisation), so the march of one tick
-runs beside the MLPs of the previous one.  Two workspace slots alternate
-between ticks; a slot is reused once its previous tick's compositing is
-done (an event).
+A tick has a front half (rays, march, row scan, rows, features; on the
+front stream) and a back half (the MLPs and compositing; on the back
+stream), and the two halves of consecutive ticks overlap: the host
+launches the front half of tick t+1 and the back half of tick t, then
+waits for tick t+1's row counts (the tick's one host synchronisation,
+taken right after the scan: the features kernel reads the row count on the
+device).  So the march and feature gathers of one tick (load/store and
+integer work, many warps) run beside the tensor-core MLPs of the previous
+one (one CTA of 9 warps per SM).  Two workspace slots alternate between
+ticks, each with its own MLP input rows; a slot is reused once its
+previous tick's compositing is done (an event).
 
 Admission is by device memory: a request is admitted once the arena (sized
 from free HBM when the server starts) has room for its pixels and fewer
@@ -223,7 +226,7 @@ class OutputArena:
 
 class _TickSlot:
     """Device workspace of one tick in flight (rays, per-ray sample records,
-    row offsets) and its pinned host staging."""
+    row offsets, the MLP input rows) and its pinned host staging."""
 
     def __init__(self, N: int, max_steps: int, scan_bytes: int, max_chunks: int, dev):
         self.rays = torch.empty((3, N, 3), dtype=torch.float32, device=dev)
@@ -242,6 +245,8 @@ class _TickSlot:
         self.idx_host = torch.empty(16, dtype=torch.int64, pin_memory=True)   # scene bounds, staged
         self.idx_dev = torch.empty(16, dtype=torch.int64, device=dev)
         self.ev_back = None   # recorded after the back half of the slot's last tick
+        self.rows_cap = 0     # shaded rows the slot's ray2 / X1 / X2 hold
+        self.ray2 = self.X1 = self.X2 = None
 
 
 class _Tick:
@@ -255,13 +260,21 @@ class _Tick:
         self.bounds: list[int] = []
         self.row_bounds: list[int] = []
         self.finished: list = []
-        self.ev_front = None
+        self.ev_bounds = None   # row counts in pinned memory
+        self.ev_front = None    # front half done (MLP input rows written)
 
 
 class RenderServer:
     def __init__(self, scenes: list[ResidentScene], tick_rays: int = 1 << 19, arena_pixels: int | None = None,
-                 hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None, mlp: str = "tc"):
-        """mlp: "tc" runs each scene's two colour MLPs as fused tcgen05
+                 hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None, mlp: str = "tc",
+                 staging: int = 0, rows_per_ray: float = 6.0):
+        """staging: the features kernel's row assembly (vx_serve_features: 0
+        stores each row from its thread and needs no dynamic shared memory,
+        so its CTAs fit on the SMs beside the tensor-core MLP of the other
+        tick; 1 stages rows in shared memory; -1 chooses 1 where it fits).
+        rows_per_ray: the initial shaded-row capacity of a slot per tick ray
+        (a slot grows when a tick has more).
+        mlp: "tc" runs each scene's two colour MLPs as fused tcgen05
         launches where the scene supports it (BF16, 192-wide), "layers" on the
         MLP engines of mlp.py (one kernel per layer)."""
         if not 1 <= len(scenes) <= 8:
@@ -288,6 +301,9 @@ class RenderServer:
         if mlp not in ("tc", "layers"):
             raise ValueError(mlp)
         self.mlp = mlp
+        if staging not in (-1, 0, 1):
+            raise ValueError(staging)
+        self.staging = int(staging)
         dev = self.device
         N = self.tick_rays
         # per-tick workspace (fixed size), two slots: while the back half of
@@ -301,8 +317,10 @@ class RenderServer:
         self.front_stream = torch.cuda.Stream(dev)
         self.back_stream = torch.cuda.Stream(dev)
         self.pending = None   # the tick whose back half is not launched yet
-        self.rows_cap = 0
-        self._grow_rows(N * 4)
+        self.rows_cap = 0     # logit rows
+        self._grow_rows(N * 6)
+        for sl in self.slots:
+            self._grow_slot_rows(sl, int(N * rows_per_ray))
         # output arena (device) and its pinned host mirror
         if arena_pixels is None:
             free, _ = self.mem_info()
@@ -440,6 +458,8 @@ class RenderServer:
 
     # ---- device work ------------------------------------------------------------
     def _grow_rows(self, n: int) -> None:
+        """The logit buffers (shared by the ticks: only the back stream uses
+        them)."""
         n = _round_up(max(n, 1), 1 << 16)
         if n <= self.rows_cap:
             return
@@ -447,11 +467,33 @@ class RenderServer:
         if self.rows_cap:
             self.back_stream.synchronize()   # the old rows are no longer read
         self.rows_cap = n
-        self.ray2 = torch.empty(n, dtype=torch.int32, device=dev)
-        self.X1 = torch.empty((n, self.ld1), dtype=self.dtype, device=dev)
-        self.X2 = torch.empty((n, self.ld2), dtype=self.dtype, device=dev)
         self.logit = torch.empty((n, 3), dtype=torch.float32, device=dev)
         self.klogit = torch.empty((n, 3), dtype=torch.float32, device=dev)
+
+    def _grow_slot_rows(self, sl: _TickSlot, n: int) -> None:
+        """A slot's MLP input rows; the caller has made sure no queued work
+        reads the old ones."""
+        n = _round_up(max(n, 1), 1024)
+        if n <= sl.rows_cap:
+            return
+        dev = self.device
+        sl.ray2 = sl.X1 = sl.X2 = None
+        sl.rows_cap = n
+        sl.ray2 = torch.empty(n, dtype=torch.int32, device=dev)
+        sl.X1 = torch.empty((n, self.ld1), dtype=self.dtype, device=dev)
+        sl.X2 = torch.empty((n, self.ld2), dtype=self.dtype, device=dev)
+
+    def _rows_and_features(self, t: "_Tick", st: int) -> None:
+        """ray2 and the MLP input rows of a tick, sized on the device (the
+        row count is s2_off[N]); rows beyond the slot's capacity are skipped
+        and redone by _row_bounds after it grows the slot."""
+        sl = self.slots[t.slot]
+        o, d, v = sl.rays[0], sl.rays[1], sl.rays[2]
+        N = t.N
+        _abi.call("vx_serve_rows", ptr(sl.s2_off), N, ptr(sl.ray2), sl.rows_cap, st)
+        _abi.call("vx_serve_features", self.table, len(self.scenes), ctypes.byref(self.cfg), ptr(o), ptr(d), ptr(v),
+                  ptr(sl.ray_scene), self.max_steps, ptr(sl.rec), ptr(sl.s2_off), ptr(sl.ray2), sl.rows_cap,
+                  ptr(sl.s2_off[N:]), self.ld1, self.ld2, ptr(sl.X1), ptr(sl.X2), int(self.bf16), self.staging, st)
 
     def _front(self, batch) -> "_Tick":
         """Rays, march and the row scan of one tick on the front stream."""
@@ -500,15 +542,29 @@ class RenderServer:
             _abi.call("vx_exclusive_scan_i32", ptr(sl.n2), N, ptr(sl.s2_off), ptr(sl.scan_tmp), self.scan_bytes,
                       st)
             sl.bounds_host[:nb].copy_(sl.s2_off.index_select(0, sl.idx_dev[:nb]), non_blocking=True)
+            t.ev_bounds = torch.cuda.Event()
+            t.ev_bounds.record(fs)
+            self._rows_and_features(t, st)
             t.ev_front = torch.cuda.Event()
             t.ev_front.record(fs)
         return t
 
     def _row_bounds(self, t: "_Tick") -> None:
-        t.ev_front.synchronize()
+        t.ev_bounds.synchronize()
         t.row_bounds = self.slots[t.slot].bounds_host[:len(t.bounds)].tolist()
         t.S2 = t.row_bounds[-1]
         self.rows_shaded += t.S2
+        sl = self.slots[t.slot]
+        if t.S2 > sl.rows_cap:
+            # more shaded rows than the slot holds: grow it and redo the
+            # tick's rows and features (the skipped rows were not written)
+            fs = self.front_stream
+            fs.synchronize()
+            self._grow_slot_rows(sl, t.S2 + t.S2 // 4)
+            with torch.cuda.stream(fs):
+                self._rows_and_features(t, fs.cuda_stream)
+                t.ev_front = torch.cuda.Event()
+                t.ev_front.record(fs)
 
     def _back(self, t: "_Tick") -> None:
         """Rows, features, MLPs and compositing of a tick on the back stream,
@@ -519,20 +575,15 @@ class RenderServer:
         with torch.cuda.stream(bs):
             bs.wait_event(t.ev_front)
             S2, N = t.S2, t.N
-            o, d, v = sl.rays[0], sl.rays[1], sl.rays[2]
             tab, ns = self.table, len(self.scenes)
             if S2 > self.rows_cap:
                 self._grow_rows(S2)
             if S2 > 0:
-                _abi.call("vx_serve_rows", ptr(sl.s2_off), N, ptr(self.ray2), st)
-                _abi.call("vx_serve_features", tab, ns, ctypes.byref(self.cfg), ptr(o), ptr(d), ptr(v),
-                          ptr(sl.ray_scene), self.max_steps, ptr(sl.rec), ptr(sl.s2_off), ptr(self.ray2), S2,
-                          self.ld1, self.ld2, ptr(self.X1), ptr(self.X2), int(self.bf16), st)
                 with torch.no_grad():
                     for g, sc in enumerate(t.scene_ids):
                         a, b = t.row_bounds[g], t.row_bounds[g + 1]
                         if b > a:
-                            self._shade(self.scenes[sc], a, b, st)
+                            self._shade(self.scenes[sc], sl, a, b, st)
             use_k = self.scenes[0].use_rgb_k
             _abi.call("vx_serve_composite", tab, ns, ptr(sl.ray_scene), N, self.max_steps, ptr(sl.rec),
                       ptr(sl.s2_off), ptr(self.logit), ptr(self.klogit) if use_k else None, ptr(sl.alast),
@@ -547,17 +598,18 @@ class RenderServer:
                 r.event.record(bs)
                 self.finishing.append(r)
 
-    def _shade(self, s: ResidentScene, a: int, b: int, st: int) -> None:
+    def _shade(self, s: ResidentScene, sl: _TickSlot, a: int, b: int, st: int) -> None:
+        X1, X2 = sl.X1, sl.X2
         if s.tc is not None and self.mlp == "tc":
             # rgbnet -> logits (also into the k_rgbnet input's last columns), then
             # k_rgbnet with the logits as residual, each one fused tcgen05 launch
-            s.tc[0].forward(self.X1[a:b], self.logit[a:b], cols=self.X2[a:b, self.d2a:], ld_cols=self.ld2)
-            s.tc[1].forward(self.X2[a:b], self.klogit[a:b], add=self.logit[a:b])
+            s.tc[0].forward(X1[a:b], self.logit[a:b], cols=X2[a:b, self.d2a:], ld_cols=self.ld2)
+            s.tc[1].forward(X2[a:b], self.klogit[a:b], add=self.logit[a:b])
             return
-        cols = self.X2[a:b, self.d2a:self.d2a + 3] if s.k_res else None
-        s.engines[0].forward(self.X1[a:b], out=self.logit[a:b], train=False, cols=cols)
+        cols = X2[a:b, self.d2a:self.d2a + 3] if s.k_res else None
+        s.engines[0].forward(X1[a:b], out=self.logit[a:b], train=False, cols=cols)
         if s.use_rgb_k:
-            kout, _ = s.engines[1].forward(self.X2[a:b], train=False)
+            kout, _ = s.engines[1].forward(X2[a:b], train=False)
             torch.add(self.logit[a:b], kout, out=self.klogit[a:b])
 
 
