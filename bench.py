@@ -87,8 +87,8 @@ def parse():
     p.add_argument("--render-only", action="store_true", help="only the render-server measurement (profiling)")
     p.add_argument("--render-plain", type=int, default=8, help="requests rendered by the plain per-request path")
     p.add_argument("--render-grid", type=int, default=256, help="scene grid size (256 is the benchmark)")
-    p.add_argument("--render-tick", type=int, default=1 << 20, help="rays packed per tick")
-    p.add_argument("--render-staging", type=int, default=0, choices=[-1, 0, 1],
+    p.add_argument("--render-tick", type=int, default=1 << 21, help="rays packed per tick")
+    p.add_argument("--render-staging", type=int, default=-1, choices=[-1, 0, 1],
                    help="row assembly of the features kernel (serve.RenderServer staging)")
     p.add_argument("--grid", type=int, default=256, help="grid resolution (256 is the benchmark; smaller sizes "
                                                          "serve profiler captures)")

@@ -267,7 +267,7 @@ class _Tick:
 class RenderServer:
     def __init__(self, scenes: list[ResidentScene], tick_rays: int = 1 << 19, arena_pixels: int | None = None,
                  hbm_reserve: int = 8 << 30, max_active: int = 64, device=None, mem_info=None, mlp: str = "tc",
-                 staging: int = 0, rows_per_ray: float = 6.0):
+                 staging: int = -1, rows_per_ray: float = 8.0):
         """staging: the features kernel's row assembly (vx_serve_features: 0
         stores each row from its thread and needs no dynamic shared memory,
         so its CTAs fit on the SMs beside the tensor-core MLP of the other
