@@ -309,12 +309,14 @@ __global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
 }
 
 // ---- row -> ray --------------------------------------------------------------
+// Thread per ray: a ray has a few shaded rows (about five at the fine
+// shapes), so a warp per ray would leave most lanes idle.
 __global__ void __launch_bounds__(256) serve_rows_kernel(const int64_t* __restrict__ s2_off, int n_rays,
                                                          int* __restrict__ ray2, int64_t capacity) {
-  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rays) return;
   const int64_t b = s2_off[r], e = min(s2_off[r + 1], capacity);
-  for (int64_t i = b + lane_id(); i < e; i += 32) ray2[i] = r;
+  for (int64_t i = b; i < e; ++i) ray2[i] = r;
 }
 
 // ---- features ----------------------------------------------------------------
@@ -486,12 +488,12 @@ struct ServeCompositeParams {
   float* out_depth;
 };
 
+// Thread per ray (a few shaded rows each), the ray's rows summed in order.
 __global__ void __launch_bounds__(256) serve_composite_kernel(ServeCompositeParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
   load_scenes(P.T, sh);
-  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= P.n_rays) return;
-  const int lane = lane_id();
   const int sc = P.ray_scene[r];
   if (sc < 0 || sc >= P.T.n) return;  // reported by the march
   const SceneK& S = sh[sc];
@@ -499,17 +501,14 @@ __global__ void __launch_bounds__(256) serve_composite_kernel(ServeCompositePara
   const uint2* rec = P.rec + (int64_t)r * P.max_steps;
   const float* lg = P.klogit ? P.klogit : P.logit;
   float acc[3] = {0.f, 0.f, 0.f}, dep = 0.f;
-  for (int64_t i = b + lane; i < e; i += 32) {
+  for (int64_t i = b; i < e; ++i) {
     const uint2 rc = rec[i - b];
     const float w = __uint_as_float(rc.y);
 #pragma unroll
     for (int c = 0; c < 3; ++c) acc[c] += w * sigmoidf_(lg[3 * i + c]);
     dep += w * ((float)rc.x * S.stepdist);
   }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) acc[c] = warp_sum(acc[c]);
-  dep = warp_sum(dep);
-  if (lane == 0) {
+  {
     const float bgt = P.alphainv_last[r] * S.bg;
     const int64_t o = P.ray_out[r];
 #pragma unroll
@@ -657,7 +656,8 @@ int vx_serve_rows(const int64_t* s2_off, int64_t n_rays, int32_t* ray2, int64_t 
   if (n_rays < 0 || n_rays > INT32_MAX || capacity < 0) return VX_ERR_ARG;
   if (n_rays == 0) return VX_OK;
   if (!s2_off || !ray2) return VX_ERR_ARG;
-  serve_rows_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(s2_off, (int)n_rays, ray2, capacity);
+  serve_rows_kernel<<<(unsigned)((n_rays + 255) / 256), 256, 0, as_stream(stream)>>>(s2_off, (int)n_rays, ray2,
+                                                                                  capacity);
   return launch_status();
 }
 
@@ -779,7 +779,7 @@ int vx_serve_composite(const vx_scene_desc* scenes_host, int32_t n_scenes, const
   P.ray_out = ray_out;
   P.out_rgb = out_rgb;
   P.out_depth = out_depth;
-  serve_composite_kernel<<<warp_blocks(n_rays), 256, 0, as_stream(stream)>>>(P);
+  serve_composite_kernel<<<(unsigned)((n_rays + 255) / 256), 256, 0, as_stream(stream)>>>(P);
   return launch_status();
 }
 
