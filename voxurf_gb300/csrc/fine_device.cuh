@@ -524,8 +524,43 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
                                                   const float* __restrict__ k0f,
                                                   const __nv_bfloat16* __restrict__ k0h, const FeatLayout& L,
                                                   const float p[3], const float v[3], T* x1, T* x2, float g1[3]) {
+  // Columns are written as soon as their values exist (k0, the encodings,
+  // then the SDF features), so few of them are live at once.
   float ind[3];
   to_index(g, p, ind);
+  {
+    float k0v[12];
+    const Corners c = corners_of(g, ind[0], ind[1], ind[2]);
+    if (k0h)
+      gatherC<12>(k0h, c, k0v);
+    else
+      gatherC<12>(k0f, c, k0v);
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) put(x2, ch, k0v[ch]);
+    if (L.use_rgbnet_k0) {
+#pragma unroll
+      for (int ch = 0; ch < 12; ++ch) put(x1, ch, k0v[ch]);
+    }
+  }
+  int col = L.use_rgbnet_k0 ? 12 : 0;
+  const int pe1 = col;  // the two encodings of x1 start here
+  int col2 = 12;
+  {
+    float xyzn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) xyzn[a] = (p[a] - g.mn[a]) / (g.mx[a] - g.mn[a]);
+    col = put_pe(x1, col, xyzn, L.pos_pe);
+    col = put_pe(x1, col, v, L.view_pe);
+    if (REUSE && L.kpos_pe == L.pos_pe && L.kview_pe == L.view_pe) {
+      // same encodings as x1 (rows staged in shared memory): copy, do not recompute
+      const int n = (3 + 6 * L.pos_pe) + (3 + 6 * L.view_pe);
+      copy_cols(x1, pe1, x2, col2, n);
+      col2 += n;
+    } else {
+      col2 = put_pe(x2, col2, xyzn, L.kpos_pe);
+      col2 = put_pe(x2, col2, v, L.kview_pe);
+    }
+  }
   float s;
   float feat[6 * KK], graw[3 * KK];
   float disp[KK];
@@ -549,25 +584,6 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
   g1[0] = gu[0];
   g1[1] = gu[1];
   g1[2] = gu[2];
-  float k0v[12];
-  const Corners c = corners_of(g, ind[0], ind[1], ind[2]);
-  if (k0h)
-    gatherC<12>(k0h, c, k0v);
-  else
-    gatherC<12>(k0f, c, k0v);
-  float xyzn[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) xyzn[a] = (p[a] - g.mn[a]) / (g.mx[a] - g.mn[a]);
-
-  int col = 0;
-  if (L.use_rgbnet_k0) {
-#pragma unroll
-    for (int ch = 0; ch < 12; ++ch) put(x1, ch, k0v[ch]);
-    col = 12;
-  }
-  const int pe1 = col;  // the two encodings of x1 start here
-  col = put_pe(x1, col, xyzn, L.pos_pe);
-  col = put_pe(x1, col, v, L.view_pe);
   if (L.center_sdf) put(x1, col++, s);
 #pragma unroll
   for (int q = 0; q < 6 * KK; ++q) put(x1, col + q, feat[q]);
@@ -580,22 +596,10 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
     put(x1, col + 1 * KK + kk, b / nrm);
     put(x1, col + 2 * KK + kk, cc / nrm);
   }
-  col = 12;
-#pragma unroll
-  for (int ch = 0; ch < 12; ++ch) put(x2, ch, k0v[ch]);
-  if (REUSE && L.kpos_pe == L.pos_pe && L.kview_pe == L.view_pe) {
-    // same encodings as x1 (rows staged in shared memory): copy, do not recompute
-    const int n = (3 + 6 * L.pos_pe) + (3 + 6 * L.view_pe);
-    copy_cols(x1, pe1, x2, col, n);
-    col += n;
-  } else {
-    col = put_pe(x2, col, xyzn, L.kpos_pe);
-    col = put_pe(x2, col, v, L.kview_pe);
-  }
-  put(x2, col++, g1[0]);
-  put(x2, col++, g1[1]);
-  put(x2, col++, g1[2]);
-  if (L.k_center_sdf) put(x2, col++, s);
+  put(x2, col2++, g1[0]);
+  put(x2, col2++, g1[1]);
+  put(x2, col2++, g1[2]);
+  if (L.k_center_sdf) put(x2, col2++, s);
 }
 
 }  // namespace vx
