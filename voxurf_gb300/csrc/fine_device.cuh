@@ -100,9 +100,67 @@ __device__ __forceinline__ void to_index(const GridGeom& g, const float p[3], fl
   for (int a = 0; a < 3; ++a) ind[a] = world_to_index(g, a, p[a]);
 }
 
-// SDF and gradient (xyz order) at one point: centre + 6 probes at +-1 voxel.
+// SDF and gradient (xyz order) at one point: centre + 6 probes at +-1 voxel
+// (each probe's coordinate clamped to the grid), as seven trilinear lookups.
+// Away from the grid's faces a probe is the centre's lookup moved by one
+// cell: when ind[a] +- 1 is exact in float (its fraction equals the
+// centre's, which fails only where the sum crosses a power of two) and no
+// probe is clamped or leaves the grid, every lookup uses the centre's eight
+// weights, and the probes read the centre's corner values plus one new
+// plane each.  The weights are the same floats corners_of forms and the sums
+// run in the same corner order, so this fast path gives the seven lookups'
+// values bit for bit; every other point takes the seven lookups.
 __device__ __forceinline__ void sdf_and_grad(const float* __restrict__ sdf, const GridGeom& g, float voxel_size,
                                              const float ind[3], float* s, float gr[3]) {
+  const int dims[3] = {g.X, g.Y, g.Z};
+  float t[3];
+  int i0[3];
+  bool fast = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float f0 = floorf(ind[a]);
+    i0[a] = (int)f0;
+    t[a] = ind[a] - f0;
+    const float qm = ind[a] - 1.f, qp = ind[a] + 1.f;
+    const float fm = floorf(qm), fp = floorf(qp);
+    fast = fast && (i0[a] >= 1) && (i0[a] + 2 <= dims[a] - 1) && (qm - fm == t[a]) && (qp - fp == t[a]) &&
+           ((int)fm == i0[a] - 1) && ((int)fp == i0[a] + 1);
+  }
+  if (fast) {
+    const int sx = g.Y * g.Z, sy = g.Z;
+    const float* b = sdf + ((int64_t)i0[0] * g.Y + i0[1]) * g.Z + i0[2];
+    const float wi[2] = {1.f - t[0], t[0]}, wj[2] = {1.f - t[1], t[1]}, wk[2] = {1.f - t[2], t[2]};
+    float w[8], vc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int di = q >> 2, dj = (q >> 1) & 1, dk = q & 1;
+      w[q] = wi[di] * wj[dj] * wk[dk];
+      vc[q] = __ldg(b + di * sx + dj * sy + dk);
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc += w[q] * vc[q];
+    *s = acc;
+    const int st[3] = {sx, sy, 1};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const int bit = 4 >> a;  // corner-index bit of axis a
+      float fmv = 0.f, fpv = 0.f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int di = q >> 2, dj = (q >> 1) & 1, dk = q & 1;
+        const int off = di * sx + dj * sy + dk;
+        // probe -1: its lower plane is new (i0 - 1), its upper plane is the centre's lower
+        const float vm = (q & bit) ? vc[q & ~bit] : __ldg(b + off - st[a]);
+        // probe +1: its lower plane is the centre's upper, its upper plane is new (i0 + 2)
+        const float vp = (q & bit) ? __ldg(b + off + st[a]) : vc[q | bit];
+        fmv += w[q] * vm;
+        fpv += w[q] * vp;
+      }
+      gr[a] = ((fpv - fmv) * (1.f / ((ind[a] + 1.f) - (ind[a] - 1.f)))) / voxel_size;
+    }
+    return;
+  }
   *s = sample1(sdf, g, ind[0], ind[1], ind[2]);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {

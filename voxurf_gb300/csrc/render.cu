@@ -125,7 +125,7 @@ __device__ __forceinline__ void march_fine_ray(const MarchParams& P, int r, cons
 }
 
 template <bool DENS>
-__global__ void __launch_bounds__(256) march_fine_kernel(MarchParams P) {
+__global__ void __launch_bounds__(256, 4) march_fine_kernel(MarchParams P) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= P.n_rays) return;
   const int lane = lane_id();

@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256) serve_first_kernel(ServeMarchParams P) {
 }
 
 template <bool DENS>  // some scene carries a MaskCache density mask
-__global__ void __launch_bounds__(256) serve_march_kernel(ServeMarchParams P) {
+__global__ void __launch_bounds__(256, 4) serve_march_kernel(ServeMarchParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
   load_scenes(P.T, sh);
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
