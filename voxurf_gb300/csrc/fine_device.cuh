@@ -577,7 +577,7 @@ __device__ __forceinline__ void hier_features_k(const float* __restrict__ sdf, c
 // KK = L.K (instantiated per displacement count).  REUSE: x1 and x2 are
 // rows staged in shared memory, so x2's positional encodings are copied
 // from x1 when both use the same frequencies.
-template <typename T, int KK, bool REUSE = false>
+template <typename T, int KK, bool REUSE = false, bool COMPACT = false>
 __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf, const GridGeom& g, float vs,
                                                   const float* __restrict__ k0f,
                                                   const __nv_bfloat16* __restrict__ k0h, const FeatLayout& L,
@@ -603,17 +603,23 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
   int col = L.use_rgbnet_k0 ? 12 : 0;
   const int pe1 = col;  // the two encodings of x1 start here
   int col2 = 12;
+  // COMPACT: x2 holds only its own columns (k0, then the gradient and the
+  // tail): its encodings equal x1's and are taken from x1 when the rows are
+  // copied out, so x2 column c >= 12 + n_pe lives at c - n_pe
+  const int n_pe = (3 + 6 * L.pos_pe) + (3 + 6 * L.view_pe);
+  const int shift2 = COMPACT ? n_pe : 0;
   {
     float xyzn[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) xyzn[a] = (p[a] - g.mn[a]) / (g.mx[a] - g.mn[a]);
     col = put_pe(x1, col, xyzn, L.pos_pe);
     col = put_pe(x1, col, v, L.view_pe);
-    if (REUSE && L.kpos_pe == L.pos_pe && L.kview_pe == L.view_pe) {
+    if (COMPACT) {
+      col2 += n_pe;
+    } else if (REUSE && L.kpos_pe == L.pos_pe && L.kview_pe == L.view_pe) {
       // same encodings as x1 (rows staged in shared memory): copy, do not recompute
-      const int n = (3 + 6 * L.pos_pe) + (3 + 6 * L.view_pe);
-      copy_cols(x1, pe1, x2, col2, n);
-      col2 += n;
+      copy_cols(x1, pe1, x2, col2, n_pe);
+      col2 += n_pe;
     } else {
       col2 = put_pe(x2, col2, xyzn, L.kpos_pe);
       col2 = put_pe(x2, col2, v, L.kview_pe);
@@ -654,10 +660,44 @@ __device__ __forceinline__ void fine_feature_rows(const float* __restrict__ sdf,
     put(x1, col + 1 * KK + kk, b / nrm);
     put(x1, col + 2 * KK + kk, cc / nrm);
   }
-  put(x2, col2++, g1[0]);
-  put(x2, col2++, g1[1]);
-  put(x2, col2++, g1[2]);
-  if (L.k_center_sdf) put(x2, col2++, s);
+  put(x2, col2++ - shift2, g1[0]);
+  put(x2, col2++ - shift2, g1[1]);
+  put(x2, col2++ - shift2, g1[2]);
+  if (L.k_center_sdf) put(x2, col2++ - shift2, s);
+}
+
+// Staged row stride of n elements: an odd number of 4-byte words (bank-
+// conflict-free column writes by the 32 threads of a warp).
+template <typename T>
+__host__ __device__ constexpr int64_t odd_words_ld(int64_t n) {
+  return ((n * (int64_t)sizeof(T) / 4) % 2 == 1) ? n : n + 4 / (int64_t)sizeof(T);
+}
+
+// Copy-out of compact x2 rows: x2 word w of a row comes from the x2 stage
+// (its k0 words and, after the encodings, its tail) or from the x1 stage
+// (the encodings, starting at x1 column pe1).  Columns 12, pe1 and n_pe are
+// word-aligned (even for BF16).
+template <typename T>
+__device__ __forceinline__ void copy_rows_out_compact(const T* stage1, int64_t sl1, const T* stage2, int64_t sl2,
+                                                      T* dst, int n_rows, int64_t ld2, int pe1, int n_pe) {
+  constexpr int EPW = 4 / (int)sizeof(T);  // elements per word
+  const int words = (int)(ld2 / EPW), k0w = 12 / EPW, pew = n_pe / EPW, pe1w = pe1 / EPW;
+  const int sw1 = (int)(sl1 / EPW), sw2 = (int)(sl2 / EPW);
+  const uint32_t* s1 = reinterpret_cast<const uint32_t*>(stage1);
+  const uint32_t* s2 = reinterpret_cast<const uint32_t*>(stage2);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int r = warp; r < n_rows; r += nw)
+    for (int w = lane; w < words; w += 32) {
+      uint32_t v;
+      if (w < k0w)
+        v = s2[r * sw2 + w];
+      else if (w < k0w + pew)
+        v = s1[r * sw1 + pe1w + (w - k0w)];
+      else
+        v = s2[r * sw2 + (w - pew)];
+      d[(int64_t)r * words + w] = v;
+    }
 }
 
 }  // namespace vx

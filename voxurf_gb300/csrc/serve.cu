@@ -342,7 +342,10 @@ struct ServeFeatParams {
 // STAGE: rows assembled in shared memory (bank-conflict-free padded stride),
 // written out one row per warp in coalesced words (the logit columns
 // [cols2, cols2+3) are zero until the rgbnet output layer fills them).
-template <typename T, int KK, bool STAGE>
+// COMPACT (with STAGE, when x2's encodings equal x1's): the x2 stage holds
+// only x2's own columns and the copy-out takes the encodings from the x1
+// stage (27 instead of 38 KB per CTA at the fine layout: one CTA more per SM).
+template <typename T, int KK, bool STAGE, bool COMPACT = false>
 __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) {
   __shared__ SceneK sh[VX_SERVE_MAX_SCENES];
   extern __shared__ __align__(16) unsigned char feat_stage[];
@@ -352,7 +355,9 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
   load_scenes(P.T, sh);
   const int64_t row = row0 + threadIdx.x;
   T* s1 = reinterpret_cast<T*>(feat_stage);
-  const int64_t sl1 = stage_ld<T>(P.ld1), sl2 = stage_ld<T>(P.ld2);
+  const int n_pe = (3 + 6 * P.L.pos_pe) + (3 + 6 * P.L.view_pe);
+  const int shift2 = COMPACT ? n_pe : 0;
+  const int64_t sl1 = stage_ld<T>(P.ld1), sl2 = COMPACT ? odd_words_ld<T>(P.ld2 - n_pe) : stage_ld<T>(P.ld2);
   T* s2 = s1 + (int64_t)blockDim.x * sl1;
   if (row < n_rows) {
     const int r = P.ray2[row];
@@ -372,15 +377,19 @@ __global__ void __launch_bounds__(128) serve_features_kernel(ServeFeatParams P) 
     T* x1 = STAGE ? s1 + (int64_t)threadIdx.x * sl1 : reinterpret_cast<T*>(P.X1) + row * P.ld1;
     T* x2 = STAGE ? s2 + (int64_t)threadIdx.x * sl2 : reinterpret_cast<T*>(P.X2) + row * P.ld2;
     float g1[3];
-    fine_feature_rows<T, KK, STAGE>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
+    fine_feature_rows<T, KK, STAGE, COMPACT>(S.sdf, S.g, S.vs, S.k0f, S.k0h, P.L, p, v, x1, x2, g1);
     for (int c = P.cols1; c < P.ld1; ++c) put(x1, c, 0.f);
-    for (int c = STAGE ? P.cols2 : P.cols2 + 3; c < P.ld2; ++c) put(x2, c, 0.f);
+    for (int c = STAGE ? P.cols2 : P.cols2 + 3; c < P.ld2; ++c) put(x2, c - shift2, 0.f);
   }
   if (STAGE) {
     __syncthreads();
     const int nv = (int)max((int64_t)0, min((int64_t)blockDim.x, n_rows - row0));
     copy_rows_out(s1, reinterpret_cast<T*>(P.X1) + row0 * P.ld1, nv, P.ld1);
-    copy_rows_out(s2, reinterpret_cast<T*>(P.X2) + row0 * P.ld2, nv, P.ld2);
+    if (COMPACT)
+      copy_rows_out_compact(s1, sl1, s2, sl2, reinterpret_cast<T*>(P.X2) + row0 * P.ld2, nv, P.ld2,
+                            P.L.use_rgbnet_k0 ? 12 : 0, n_pe);
+    else
+      copy_rows_out(s2, reinterpret_cast<T*>(P.X2) + row0 * P.ld2, nv, P.ld2);
   }
 }
 
@@ -703,10 +712,21 @@ int vx_serve_features(const vx_scene_desc* scenes_host, int32_t n_scenes, const 
                         ((reinterpret_cast<uintptr_t>(X1) | reinterpret_cast<uintptr_t>(X2)) & 3) == 0;
   if (staging == 1 && !stage_ok) return VX_ERR_UNSUPPORTED;
   const bool stage = staging != 0 && stage_ok;
-#define VX_FEAT_LAUNCH(T, KK)                                    \
-  if (stage)                                                     \
-    serve_features_kernel<T, KK, true><<<b, 128, shm, st>>>(P);  \
-  else                                                           \
+  // compact x2 staging: x2's encodings are x1's (same frequencies) and the
+  // column groups are 4-byte aligned
+  const int64_t n_pe = (3 + 6 * P.L.pos_pe) + (3 + 6 * P.L.view_pe);
+  const int64_t epw = 4 / (int64_t)esz;
+  const bool compact = stage && P.L.kpos_pe == P.L.pos_pe && P.L.kview_pe == P.L.view_pe && n_pe % epw == 0 &&
+                       (P.L.use_rgbnet_k0 ? 12 : 0) % epw == 0 && 12 % epw == 0;
+  // the strides of stage_ld and odd_words_ld, in elements
+  const int64_t nc = ld2 - n_pe, sl2c = ((nc * (int64_t)esz / 4) % 2 == 1) ? nc : nc + epw;
+  const size_t shm_c = 128 * (size_t)(ld1 + epw + sl2c) * esz;
+#define VX_FEAT_LAUNCH(T, KK)                                          \
+  if (compact)                                                         \
+    serve_features_kernel<T, KK, true, true><<<b, 128, shm_c, st>>>(P); \
+  else if (stage)                                                      \
+    serve_features_kernel<T, KK, true><<<b, 128, shm, st>>>(P);        \
+  else                                                                 \
     serve_features_kernel<T, KK, false><<<b, 128, 0, st>>>(P)
 #define VX_FEAT_SWITCH(T)        \
   switch (P.L.K) {               \
