@@ -4,11 +4,19 @@
  * It is the checker for the sm_103a kernels of voxurf_gb300; nothing in the
  * product links or calls it.
  *
- * Floating-point semantics follow the reference source as written in C:
- * one rounding per operation (this file must be compiled with
- * -ffp-contract=off so that no a*b+c is fused), float arithmetic where the
- * source uses float, and the implicit double promotions of the source where
- * it mixes in double literals (e.g. `T_cum *= (1. - alpha[i])`).
+ * Floating-point semantics follow the reference's compiled kernels: one
+ * rounding per operation (this file must be compiled with -ffp-contract=off
+ * so that the compiler fuses nothing on its own), except for the a*b+c that
+ * the reference's nvcc build (default --fmad=true) computes as one fused
+ * multiply-add, written here as C99 fmaf: the ray norm
+ * sqrt(fma(z,z, fma(x,x, y*y))), the ray start fma(d, t_min, o), the sample
+ * point fma(dir, dist, start), the mask index fma(xyz, scale, shift), the
+ * suffix sum of alpha2weight's backward and the two Adam moments.  Which
+ * expressions are fused was measured by running the reference's own kernels
+ * on the GPU against every candidate form (tests/test_zy_reference_kernels_gpu.py).
+ * Float arithmetic where the source uses float, and the implicit double
+ * promotions of the source where it mixes in double literals
+ * (e.g. `T_cum *= (1. - alpha[i])`).
  */
 #include <math.h>
 #include <stdint.h>
@@ -30,12 +38,10 @@ static void clip_one(const float* o, const float* d, const float* mn, const floa
   *tmax = fmaxf(fminf(fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)), far), near);
 }
 
-/* render_utils_kernel.cu:48-51 */
+/* render_utils_kernel.cu:48-51: the compiled kernel fuses x*x and z*z into
+ * the sum, fma(z, z, fma(x, x, y*y)) */
 static float rnorm_of(const float* d) {
-  float s = d[0] * d[0];
-  s = s + d[1] * d[1];
-  s = s + d[2] * d[2];
-  return sqrtf(s);
+  return sqrtf(fmaf(d[2], d[2], fmaf(d[0], d[0], d[1] * d[1])));
 }
 
 /* render_utils_kernel.cu:53 */
@@ -63,7 +69,7 @@ void vxo_infer_ray_start_dir(const float* rays_o, const float* rays_d, const flo
     const float* d = rays_d + 3 * r;
     float rn = rnorm_of(d);
     for (int a = 0; a < 3; ++a) {
-      start[3 * r + a] = o[a] + d[a] * t_min[r];
+      start[3 * r + a] = fmaf(d[a], t_min[r], o[a]);
       dir[3 * r + a] = d[a] / rn;
     }
   }
@@ -95,14 +101,14 @@ void vxo_sample_fill(const float* rays_o, const float* rays_d, const float* xyz_
     float rn = rnorm_of(d);
     float st[3], dr[3];
     for (int a = 0; a < 3; ++a) {
-      st[a] = o[a] + d[a] * t_min[r];
+      st[a] = fmaf(d[a], t_min[r], o[a]);
       dr[a] = d[a] / rn;
     }
     for (int64_t k = 0; k < n_steps[r]; ++k, ++idx) {
       float dist = stepdist * (float)k;
-      float px = st[0] + dr[0] * dist;
-      float py = st[1] + dr[1] * dist;
-      float pz = st[2] + dr[2] * dist;
+      float px = fmaf(dr[0], dist, st[0]);
+      float py = fmaf(dr[1], dist, st[1]);
+      float pz = fmaf(dr[2], dist, st[2]);
       ray_pts[3 * idx + 0] = px;
       ray_pts[3 * idx + 1] = py;
       ray_pts[3 * idx + 2] = pz;
@@ -128,9 +134,9 @@ static int round_to_int(float v) {
 void vxo_maskcache_lookup(const uint8_t* world, int64_t si, int64_t sj, int64_t sk, const float* xyz, int64_t n,
                           const float* scale, const float* shift, uint8_t* out) {
   for (int64_t p = 0; p < n; ++p) {
-    int i = round_to_int(xyz[3 * p + 0] * scale[0] + shift[0]);
-    int j = round_to_int(xyz[3 * p + 1] * scale[1] + shift[1]);
-    int k = round_to_int(xyz[3 * p + 2] * scale[2] + shift[2]);
+    int i = round_to_int(fmaf(xyz[3 * p + 0], scale[0], shift[0]));
+    int j = round_to_int(fmaf(xyz[3 * p + 1], scale[1], shift[1]));
+    int k = round_to_int(fmaf(xyz[3 * p + 2], scale[2], shift[2]));
     uint8_t v = 0;
     if (0 <= i && i < si && 0 <= j && j < sj && 0 <= k && k < sk) v = world[((int64_t)i * sj + j) * sk + k] ? 1 : 0;
     out[p] = v;
@@ -190,7 +196,7 @@ void vxo_alpha2weight_backward(const float* alpha, const float* weight, const fl
     float back_cum = grad_last[r] * alphainv_last[r];
     for (int i = i_e - 1; i >= i_s; --i) {
       grad[i] = grad_weights[i] * T[i] - back_cum / (1 - alpha[i] + 1e-10);
-      back_cum += grad_weights[i] * weight[i];
+      back_cum = fmaf(grad_weights[i], weight[i], back_cum);
     }
   }
 }
@@ -288,8 +294,8 @@ void vxo_adam_upd(int mode, float* param, const float* grad, float* exp_avg, flo
   const float step_size = lr * sqrtf(1 - powf(beta2, (float)step)) / (1 - powf(beta1, (float)step));
   for (int64_t i = 0; i < n; ++i) {
     if (mode == 1 && grad[i] == 0) continue;
-    exp_avg[i] = beta1 * exp_avg[i] + (1 - beta1) * grad[i];
-    exp_avg_sq[i] = beta2 * exp_avg_sq[i] + (1 - beta2) * grad[i] * grad[i];
+    exp_avg[i] = fmaf(beta1, exp_avg[i], (1 - beta1) * grad[i]);
+    exp_avg_sq[i] = fmaf(beta2, exp_avg_sq[i], (1 - beta2) * grad[i] * grad[i]);
     if (mode == 2)
       param[i] -= step_size * perlr[i] * exp_avg[i] / (sqrtf(exp_avg_sq[i]) + eps);
     else
@@ -364,4 +370,12 @@ void vxo_bg_samples(const float* rays_o, const float* rays_d, const float* jitte
       keep[s] = (uint8_t)kp;
     }
   }
+}
+
+/* ---- correctly rounded a*b+c, elementwise ------------------------------------
+ * C99 fmaf rounds once.  The contracted forms of the reference's float
+ * expressions (nvcc's default --fmad=true turns a*b+c into one fused
+ * multiply-add where it applies) are built from this in oracle/fma_forms.py. */
+void vxo_fmaf(const float* a, const float* b, const float* c, float* out, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) out[i] = fmaf(a[i], b[i], c[i]);
 }

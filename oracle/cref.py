@@ -199,3 +199,12 @@ def bg_samples(rays_o, rays_d, xyz_min, xyz_max, near, far, stepdist, dist_thres
                                       jitter, outbbox_only)
     ray_id, step_id = np.nonzero(keep)
     return inv[keep], pts[keep], ray_id.astype(np.int64), step_id.astype(np.int64)
+
+
+def fmaf(a, b, c):
+    """Elementwise correctly rounded float32 a*b+c (C99 fmaf), broadcasting."""
+    a, b, c = np.broadcast_arrays(np.asarray(a, np.float32), np.asarray(b, np.float32), np.asarray(c, np.float32))
+    a, b, c = _f32(a), _f32(b), _f32(c)
+    out = np.empty(a.shape, np.float32)
+    lib().vxo_fmaf(_p(a), _p(b), _p(c), _p(out), C.c_int64(a.size))
+    return out

@@ -85,6 +85,13 @@ __device__ __forceinline__ float norm3(float x, float y, float z) {
   return __fsqrt_rn(__fmaf_rn(z, z, __fmaf_rn(y, y, fmul(x, x))));
 }
 
+// |d| of a ray as the reference's compiled sampling kernels compute
+// sqrt(dx*dx + dy*dy + dz*dz) (render_utils_kernel.cu:48-51, 67-70; nvcc's
+// --fmad=true fuses dx*dx and then dz*dz into the sum).
+__device__ __forceinline__ float ray_norm3(float x, float y, float z) {
+  return __fsqrt_rn(__fmaf_rn(z, z, __fmaf_rn(x, x, fmul(y, y))));
+}
+
 // Transmittance precision: a ray of more samples than this carries its
 // transmittance products (forward) and its suffix sums (backward) in FP64;
 // shorter rays in FP32.  GB300 runs FP64 at a small fraction of its FP32

@@ -26,13 +26,13 @@ __device__ __forceinline__ RayFrame ray_frame(const float* o, const float* d, co
   const float bx = fdiv(fsub(mn[0], o[0]), vx), by = fdiv(fsub(mn[1], o[1]), vy), bz = fdiv(fsub(mn[2], o[2]), vz);
   const float t_min = fmaxf(fminf(fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz)), far), near);
   const float t_max = fmaxf(fminf(fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)), far), near);
-  const float rn = __fsqrt_rn(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
+  const float rn = ray_norm3(d[0], d[1], d[2]);
   RayFrame f;
   const float c = ceilf(fdiv(fmul(fsub(t_max, t_min), rn), stepdist));
   f.n_steps = (int64_t)fmax((double)c, 1.0);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    f.st[a] = fadd(o[a], fmul(d[a], t_min));
+    f.st[a] = __fmaf_rn(d[a], t_min, o[a]);  // fused as in the reference's compiled kernel
     f.dr[a] = fdiv(d[a], rn);
   }
   return f;
@@ -41,7 +41,7 @@ __device__ __forceinline__ RayFrame ray_frame(const float* o, const float* d, co
 __device__ __forceinline__ void sample_point(const RayFrame& f, float stepdist, int k, float p[3]) {
   const float dist = fmul(stepdist, (float)k);
 #pragma unroll
-  for (int a = 0; a < 3; ++a) p[a] = fadd(f.st[a], fmul(f.dr[a], dist));
+  for (int a = 0; a < 3; ++a) p[a] = __fmaf_rn(f.dr[a], dist, f.st[a]);
 }
 
 // Pinhole ray through pixel centre (i, j) (+0.5 already added) of a camera
@@ -249,13 +249,14 @@ __device__ __forceinline__ bool outside_bbox(const float p[3], const float* mn, 
   return (mn[0] > p[0]) | (mn[1] > p[1]) | (mn[2] > p[2]) | (mx[0] < p[0]) | (mx[1] < p[1]) | (mx[2] < p[2]);
 }
 
-// maskcache_lookup semantics (render_utils_kernel.cu:374-392): nearest voxel,
-// round half away from zero, false outside the grid.
+// maskcache_lookup semantics (render_utils_kernel.cu:374-392): nearest voxel
+// of xyz*scale + shift (one fused multiply-add, as the reference's compiled
+// kernel computes it), round half away from zero, false outside the grid.
 __device__ __forceinline__ bool mask_lookup(const uint8_t* __restrict__ mask, int mX, int mY, int mZ,
                                             const float* scale, const float* shift, const float p[3]) {
   int ijk[3];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) ijk[a] = (int)roundf(fadd(fmul(p[a], scale[a]), shift[a]));
+  for (int a = 0; a < 3; ++a) ijk[a] = (int)roundf(__fmaf_rn(p[a], scale[a], shift[a]));
   if (ijk[0] < 0 || ijk[0] >= mX || ijk[1] < 0 || ijk[1] >= mY || ijk[2] < 0 || ijk[2] >= mZ) return false;
   return mask[((int64_t)ijk[0] * mY + ijk[1]) * mZ + ijk[2]] != 0;
 }

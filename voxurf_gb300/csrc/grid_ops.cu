@@ -111,8 +111,9 @@ __global__ void adam_upd_kernel(float* __restrict__ param, const float* __restri
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const float g = grad[i];
     if (MODE == 1 && g == 0.f) continue;
-    const float m = fadd(fmul(beta1, exp_avg[i]), fmul(fsub(1.f, beta1), g));
-    const float v = fadd(fmul(beta2, exp_avg_sq[i]), fmul(fmul(fsub(1.f, beta2), g), g));
+    // the reference's compiled kernel fuses beta1*m and beta2*v into the sums
+    const float m = __fmaf_rn(beta1, exp_avg[i], fmul(fsub(1.f, beta1), g));
+    const float v = __fmaf_rn(beta2, exp_avg_sq[i], fmul(fmul(fsub(1.f, beta2), g), g));
     exp_avg[i] = m;
     exp_avg_sq[i] = v;
     const float num = (MODE == 2) ? fmul(fmul(step_size, perlr[i]), m) : fmul(step_size, m);

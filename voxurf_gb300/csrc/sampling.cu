@@ -69,9 +69,11 @@ __device__ __forceinline__ RayClip clip_ray(const float* __restrict__ o, const f
   return c;
 }
 
-// sqrt(dx*dx + dy*dy + dz*dz), render_utils_kernel.cu:48-51
+// sqrt(dx*dx + dy*dy + dz*dz), render_utils_kernel.cu:48-51, in the form the
+// reference's compiled kernel computes it: dx*dx and dz*dz fused into the
+// sum, sqrt(fma(dz, dz, fma(dx, dx, dy*dy)))
 __device__ __forceinline__ float ray_norm(const float* __restrict__ d) {
-  return __fsqrt_rn(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
+  return ray_norm3(d[0], d[1], d[2]);
 }
 
 // max(ceil((t_max-t_min)*|d|/stepdist), 1), render_utils_kernel.cu:53
@@ -111,7 +113,7 @@ __global__ void infer_ray_start_dir_kernel(const float* __restrict__ rays_o, con
   const float t = t_min[r];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    rays_start[3 * r + a] = fadd(o[a], fmul(d[a], t));
+    rays_start[3 * r + a] = __fmaf_rn(d[a], t, o[a]);
     rays_dir[3 * r + a] = fdiv(d[a], rn);
   }
 }
@@ -150,7 +152,7 @@ __global__ void sample_fill_kernel(const float* __restrict__ rays_o, const float
   float st[3], dr[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    st[a] = fadd(o[a], fmul(d[a], t));
+    st[a] = __fmaf_rn(d[a], t, o[a]);
     dr[a] = fdiv(d[a], rn);
   }
   const float mn0 = xyz_min[0], mn1 = xyz_min[1], mn2 = xyz_min[2];
@@ -163,9 +165,9 @@ __global__ void sample_fill_kernel(const float* __restrict__ rays_o, const float
     if (idx >= capacity) break;
     const int64_t k = idx - beg;
     const float dist = fmul(stepdist, (float)k);
-    const float px = fadd(st[0], fmul(dr[0], dist));
-    const float py = fadd(st[1], fmul(dr[1], dist));
-    const float pz = fadd(st[2], fmul(dr[2], dist));
+    const float px = __fmaf_rn(dr[0], dist, st[0]);
+    const float py = __fmaf_rn(dr[1], dist, st[1]);
+    const float pz = __fmaf_rn(dr[2], dist, st[2]);
     ray_pts[3 * idx + 0] = px;
     ray_pts[3 * idx + 1] = py;
     ray_pts[3 * idx + 2] = pz;
@@ -175,10 +177,11 @@ __global__ void sample_fill_kernel(const float* __restrict__ rays_o, const float
   }
 }
 
-// C `round` (half away from zero) of x*scale + shift, one rounding per op
-// (render_utils_kernel.cu:385-387).
+// C `round` (half away from zero) of x*scale + shift
+// (render_utils_kernel.cu:385-387), fused into one multiply-add as the
+// reference's compiled kernel computes it.
 __device__ __forceinline__ int mask_index(float x, float scale, float shift) {
-  return (int)roundf(fadd(fmul(x, scale), shift));
+  return (int)roundf(__fmaf_rn(x, scale, shift));
 }
 
 __global__ void maskcache_lookup_kernel(const uint8_t* __restrict__ world, const float* __restrict__ xyz,
