@@ -590,24 +590,28 @@ def main():
     install_stubs()
     torch.set_default_dtype(torch.float32)
     which = sys.argv[1:] or ["ops", "fine", "coarse", "mesh", "ckpt", "bg", "womask", "womask_coarse", "tv"]
+    # VOXURF_GOLDEN_OUT: write elsewhere (tests/test_golden_reproducible.py
+    # regenerates into a temporary directory and compares)
+    out = os.environ.get("VOXURF_GOLDEN_OUT", HERE)
+    os.makedirs(out, exist_ok=True)
     if "ops" in which:
-        ops_fixture(os.path.join(HERE, "ops_golden.npz"))
+        ops_fixture(os.path.join(out, "ops_golden.npz"))
     if "fine" in which:
-        fine_step_fixture(os.path.join(HERE, "fine_step_golden.npz"))
+        fine_step_fixture(os.path.join(out, "fine_step_golden.npz"))
     if "coarse" in which:
-        coarse_step_fixture(os.path.join(HERE, "coarse_step_golden.npz"))
+        coarse_step_fixture(os.path.join(out, "coarse_step_golden.npz"))
     if "mesh" in which:
-        mesh_fixture(os.path.join(HERE, "mesh_golden.npz"))
+        mesh_fixture(os.path.join(out, "mesh_golden.npz"))
     if "ckpt" in which:
-        ckpt_fixture(HERE)
+        ckpt_fixture(out)
     if "bg" in which:
-        bg_fixture(os.path.join(HERE, "bg_golden.npz"))
+        bg_fixture(os.path.join(out, "bg_golden.npz"))
     if "womask" in which:
-        womask_step_fixture(os.path.join(HERE, "womask_step_golden.npz"))
+        womask_step_fixture(os.path.join(out, "womask_step_golden.npz"))
     if "womask_coarse" in which:
-        womask_coarse_step_fixture(os.path.join(HERE, "womask_coarse_step_golden.npz"))
+        womask_coarse_step_fixture(os.path.join(out, "womask_coarse_step_golden.npz"))
     if "tv" in which:
-        tv_fixture(os.path.join(HERE, "tv_golden.npz"))
+        tv_fixture(os.path.join(out, "tv_golden.npz"))
 
 
 if __name__ == "__main__":
