@@ -4,7 +4,8 @@ numpy/ctypes front-end of ``oracle/cref.c``, the serial CPU restatement of
 the reference's CUDA ops (Voxurf lib/cuda/render_utils_kernel.cu,
 total_variation_kernel.cu, adam_upd_kernel.cu).  ``build()`` compiles it with
 gcc into ``oracle/_build/libvxoracle.so`` (-ffp-contract=off: one rounding
-per operation, as the source reads).
+per operation, except the multiply-adds that the reference's compiled
+kernels fuse, written as fmaf in the source).
 """
 from __future__ import annotations
 

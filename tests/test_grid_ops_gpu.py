@@ -1,6 +1,7 @@
 """Parity of the TV and Adam drop-ins (and the fused grid sweep) with the
-oracle.  The float pipelines are rounded once per operation on both sides,
-so the reference-kernel restatements must match bit for bit."""
+oracle.  The float pipelines round the same operations on both sides (once
+per operation, and the Adam moments with the fused multiply-adds of the
+reference's compiled kernel), so the restatements must match bit for bit."""
 import numpy as np
 import pytest
 import torch

@@ -2,8 +2,8 @@
 
 Integer and index outputs (N_steps, ray_id, step_id, mask_outbbox, the mask
 lookup, i_start, i_end) must match bit for bit; so must t_min/t_max and the
-sample points, whose float pipeline is rounded once per operation on both
-sides.  Transmittance/weights use a warp-parallel FP64 scan on the GPU and
+sample points, whose float pipeline rounds the same operations on both
+sides (the reference kernels' fused multiply-adds included).  Transmittance/weights use a warp-parallel FP64 scan on the GPU and
 the serial float loop in the oracle: tolerance 2e-6 relative.
 """
 import numpy as np

@@ -70,9 +70,10 @@ int exclusive_scan(const Tin* in, int64_t n, Tout* out, void* scratch, size_t sc
 
 // ---------------------------------------------------------------------------
 // Uncontracted IEEE float arithmetic.  The index-producing stages (ray/bbox
-// clip, sample counts, sample positions, mask rounding) are computed with
-// one rounding per operation so that the results are reproducible bit for
-// bit by a CPU restatement with the same operation order.
+// clip, sample counts, sample positions, mask rounding) round every
+// operation once, except the multiply-adds that the reference's compiled
+// kernels fuse (written as __fmaf_rn where they occur), so that the results
+// equal the reference's kernels and a CPU restatement bit for bit.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }

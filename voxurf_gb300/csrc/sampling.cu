@@ -9,8 +9,10 @@
 //     samples, coalesced), replacing six launches, two cumsums and the host
 //     `.item()` of render_utils_kernel.cu:212;
 //   * every float operation that feeds an index or a bbox/mask decision is
-//     rounded once (no FMA contraction), so the CPU oracle reproduces the
-//     outputs bit for bit.
+//     rounded once, except the multiply-adds that the reference's compiled
+//     kernels fuse (ray norm, ray start, sample point, mask index), which
+//     are one __fmaf_rn here too: the outputs equal the reference kernels'
+//     and the CPU oracle's bit for bit.
 #include <math.h>
 #include <mutex>
 #include "common.cuh"
